@@ -1,0 +1,416 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 measurement operator (degrid + grid Mvis/s).
+
+A step is one forward Phi x followed by one adjoint Phi^H y (y = the forward
+result) on the 1024^2-image workload: 2048^2 grid (oversampling 2),
+10^7 visibilities (70% Gaussian core with sigma = 0.15 N, 30% uniform),
+Kaiser-Bessel J = 6, complex<float> arithmetic.  ``value`` is visibilities
+per second through degrid + grid with inputs resident in HBM; ``e2e`` is the
+same metric through the host complex<double> entry points, host<->device
+copies included.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+``--impl reference`` times the CPU FP64 restatement of the reference
+operator (CSR G and G^H, row-parallel SpMV, unitary FFT) on the host cores.
+Under torchrun (N > 1) every rank runs an independent replica (weak scaling).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "purify-1_gb300"))
+
+METRIC = "degrid+grid Mvis/s at 1024^2 (Phi then Phi^H per step), FP32 vs FP64 plain"
+WORKLOAD = ("1024^2 image, 2048^2 grid, M=1e7 visibilities (70% Gaussian core sigma=0.15N, "
+            "30% uniform), Kaiser-Bessel Ju=Jv=6, weights 1")
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=50)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--M", type=int, default=10_000_000)
+    p.add_argument("--imsize", type=int, default=1024)
+    p.add_argument("--J", type=int, default=6)
+    p.add_argument("--cpu-sample", type=int, default=1_000_000,
+                   help="visibilities in the CPU-baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--threads", type=int, default=0, help="CTA threads (tuning)")
+    p.add_argument("--max-per-item", type=int, default=0)
+    return p.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def workload(args, seed):
+    from purify_gb300 import synthetic
+    n = args.imsize
+    u, v = synthetic.mixed_uv(args.M, 2 * n, 2 * n, 0.7, 0.15, seed=seed)
+    x = synthetic.sky_image(n, n, seed=seed)
+    return u, v, x
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of each kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.rows = []
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(device)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append((time.time(), parts))
+
+    def window(self, t0, t1):
+        return [p for (t, p) in self.rows if t0 <= t <= t1]
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self, rows):
+        if not rows:
+            return None
+
+        def num(s):
+            try:
+                return float(s)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        smax = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if "Active" in r[5 + k]})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+# --------------------------------------------------------------- CPU oracle --
+def cpu_reference(u, v, x, imsize, J, sample, steps=2, warmup=1):
+    """Times the FP64 oracle on a bounded sample of the same coverage and
+    extrapolates the per-visibility cost to the full M."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    threads = oracle.get_threads()
+    M = u.size
+    Ms = min(sample, M)
+    idx = np.random.default_rng(123).choice(M, Ms, replace=False) if Ms < M else np.arange(M)
+    op0 = oracle.Operator(u[:0], v[:0], None, None, imsize, imsize, 2.0, kernel="kb", Ju=J, Jv=J)
+    ops = oracle.Operator(u[idx], v[idx], None, None, imsize, imsize, 2.0, kernel="kb", Ju=J,
+                          Jv=J)
+
+    def pair_time(op):
+        ts = []
+        for k in range(warmup + steps):
+            t0 = time.perf_counter()
+            y = op.forward(x)
+            op.adjoint(y)
+            if k >= warmup:
+                ts.append(time.perf_counter() - t0)
+        return statistics.median(ts)
+
+    t_fixed = pair_time(op0)
+    t_sample = pair_time(ops)
+    per_vis = max(t_sample - t_fixed, 0.0) / Ms
+    t_full = t_fixed + per_vis * M
+    return {
+        "value": M / t_full / 1e6, "unit": "Mvis/s", "cores": threads, "kind": "port",
+        "sample": ("Phi then Phi^H of the FP64 oracle (CSR G/G^H, OpenMP SpMV, radix-2 FFT) on "
+                   "%d of the %d visibilities with the full %d^2 grid; median of %d pairs; "
+                   "per-visibility cost extrapolated linearly to M=%d (fixed pad+FFT+crop part "
+                   "%.3f s timed with M=0)" % (Ms, M, 2 * imsize, steps, M, t_fixed)),
+        "t_pair_sample_s": t_sample, "t_fixed_s": t_fixed,
+    }
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    u, v, x = workload(args, seed=0)
+    # each step: one pair on the bounded sample (see cpu_reference)
+    cb = cpu_reference(u, v, x, args.imsize, args.J, args.cpu_sample, steps=max(1, args.steps),
+                       warmup=max(1, args.warmup))
+    line = {
+        "metric": METRIC, "value": cb["value"], "unit": "Mvis/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": args.M / cb["value"] / 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded (PCG64) coverage and point-source + Gaussian-blob sky",
+        "config": {"workload": WORKLOAD, "parallelism": "host threads"},
+        "impl": "reference", "cpu_baseline": cb,
+        "e2e": {"value": cb["value"], "unit": "Mvis/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------- GPU ----
+def run_gb300(args):
+    import torch
+    import purify_gb300 as pgb
+
+    world, rank, local = dist_env()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pgb.build()
+
+    u, v, x = workload(args, seed=rank)
+    n, M, N = args.imsize, args.M, args.imsize * args.imsize
+    kw = dict(imsizey=n, imsizex=n, oversample_ratio=2.0, kernel="kb", Ju=args.J, Jv=args.J,
+              device=local)
+    t0 = time.perf_counter()
+    op = pgb.MeasurementOperator(u, v, None, None, power_iters=0, precision="fp32", **kw)
+    t_create = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    norm = op.power_method(20, 1e-4)
+    t_power = time.perf_counter() - t0
+    info = op.info()
+
+    stream = torch.cuda.current_stream(dev)
+    xd = torch.from_numpy(x).to(torch.complex64).to(dev)
+    yd = torch.empty(M, dtype=torch.complex64, device=dev)
+    xo = torch.empty(N, dtype=torch.complex64, device=dev)
+
+    def step():
+        op.forward_into(xd, yd, stream)
+        op.adjoint_into(yd, xo, stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    sampler = ClockSampler(local) if rank == 0 else None
+    if sampler:
+        time.sleep(0.5)
+    op.stage_timing(True)
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    w0 = time.time()
+    evs[0].record(stream)
+    for k in range(args.steps):
+        step()
+        evs[k + 1].record(stream)
+    torch.cuda.synchronize(dev)
+    w1 = time.time()
+    if dist:
+        dist.barrier()
+    total_ms = evs[0].elapsed_time(evs[-1])
+    per_step = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
+    stages = op.stage_times()
+    op.stage_timing(False)
+    clocks = None
+    if sampler:
+        time.sleep(0.3)
+        sampler.stop()
+        clocks = sampler.summary(sampler.window(w0 - 0.25, w1 + 0.25)) or sampler.summary(
+            sampler.rows)
+    ms_per_step = total_ms / args.steps
+    if dist:
+        t = torch.tensor([ms_per_step], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_per_step = float(t.item())
+    value = world * M / (ms_per_step * 1e-3) / 1e6
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "Mvis/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded (PCG64) coverage and point-source + Gaussian-blob sky",
+        "config": {"workload": WORKLOAD, "global_visibilities": world * M,
+                   "l2": "inputs larger than L2 (about 300 MB of coverage state and "
+                         "visibilities read per step vs 129 MB L2)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "latency_ms": {"p50": float(np.percentile(per_step, 50)),
+                       "p99": float(np.percentile(per_step, 99))},
+        "create_s": t_create, "power_method_s": t_power, "norm": norm,
+        "stages_ms_per_launch": {k: (ms / nl if nl else None) for k, (ms, nl) in stages.items()},
+        "gpu_launches": 5 * args.steps,
+        "clocks": clocks,
+    }
+
+    # roofline of the dominant kernel (degrid or grid), algorithmic bytes:
+    # per visibility u,v (2 x 8 B) + weight + visibility (2 x 8 B); the grid once (8 B/cell)
+    s = 8
+    alg = {"degrid": M * (16 + 2 * s) + s * info["ftsizeu"] * info["ftsizev"],
+           "grid": M * (16 + 2 * s) + s * info["ftsizeu"] * info["ftsizev"]}
+    kern = max(("degrid", "grid"), key=lambda k: stages[k][0] / max(stages[k][1], 1))
+    dur = stages[kern][0] / max(stages[kern][1], 1) * 1e-3
+    peak, peak_kind = measured_peak()
+    achieved = alg[kern] / dur / 1e9
+    traffic = profiled_traffic().get(kern)
+    out["roofline"] = {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak,
+                       "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                       "algorithmic_bytes": alg[kern],
+                       "traffic": (traffic * M / 1e7) if traffic else None}
+    # whole-step HBM view: B_fwd + B_adj (algorithmic, c64)
+    NuNv = info["ftsizeu"] * info["ftsizev"]
+    b_step = 2 * M * (16 + 2 * s) + s * (7 * NuNv + 3 * N)
+    out["step_roofline"] = {"algorithmic_bytes": b_step,
+                            "achieved_gbs": b_step / (ms_per_step * 1e-3) / 1e9,
+                            "frac": b_step / (ms_per_step * 1e-3) / 1e9 / peak}
+
+    # FP32 vs FP64 GPU, same coverage and norm
+    if not args.no_fp64:
+        op64 = pgb.MeasurementOperator(u, v, None, None, power_iters=0, precision="fp64", **kw)
+        op64.set_norm(norm)
+        x64 = xd.to(torch.complex128)
+        y64 = torch.empty(M, dtype=torch.complex128, device=dev)
+        xo64 = torch.empty(N, dtype=torch.complex128, device=dev)
+        for _ in range(max(1, args.warmup)):
+            op64.forward_into(x64, y64, stream)
+            op64.adjoint_into(y64, xo64, stream)
+        k64 = max(3, args.steps // 5)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        for _ in range(k64):
+            op64.forward_into(x64, y64, stream)
+            op64.adjoint_into(y64, xo64, stream)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms64 = e0.elapsed_time(e1) / k64
+        # errors of the FP32 path against the FP64 path (same input)
+        op.forward_into(xd, yd, stream)
+        op.adjoint_into(y64.to(torch.complex64), xo, stream)
+        op64.forward_into(x64, y64, stream)
+        op64.adjoint_into(y64, xo64, stream)
+        torch.cuda.synchronize(dev)
+        f32y, f64y = yd.cpu().numpy(), y64.cpu().numpy()
+        f32x, f64x = xo.cpu().numpy(), xo64.cpu().numpy()
+        out["fp64"] = {"value": world * M / (ms64 * 1e-3) / 1e6, "ms_per_step": ms64,
+                       "speedup_fp32_over_fp64": ms64 / ms_per_step}
+        out["rel_l2_fp32_vs_fp64"] = {"forward": rel_l2(f32y, f64y), "adjoint": rel_l2(f32x, f64x)}
+        # FP64 GPU vs the CPU FP64 oracle on a row sample (forward rows are independent)
+        try:
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import oracle
+            oracle.build()
+            idx = np.random.default_rng(7).choice(M, 20000, replace=False)
+            ref = oracle.Operator(u[idx], v[idx], None, None, n, n, 2.0, kernel="kb", Ju=args.J,
+                                  Jv=args.J)
+            ref.set_norm(norm)
+            yr = ref.forward(x)
+            out["rel_l2_vs_oracle_forward_rows"] = {"fp32": rel_l2(f32y[idx], yr),
+                                                    "fp64": rel_l2(f64y[idx], yr),
+                                                    "rows": 20000}
+        except Exception as e:  # the oracle is a checker only
+            out["rel_l2_vs_oracle_forward_rows"] = {"error": str(e)}
+        del op64
+
+    # end to end through the host complex<double> entry points, pinned buffers
+    xh = torch.from_numpy(x).pin_memory()
+    yh = torch.empty(M, dtype=torch.complex128).pin_memory()
+    xoh = torch.empty(N, dtype=torch.complex128).pin_memory()
+    xhn, yhn, xohn = xh.numpy(), yh.numpy(), xoh.numpy()
+    import ctypes
+    L = pgb.load()
+
+    def e2e_step():
+        pgb._check(L.purify_gb300_forward_host(op.handle, xhn.ctypes.data_as(ctypes.c_void_p),
+                                               yhn.ctypes.data_as(ctypes.c_void_p)))
+        pgb._check(L.purify_gb300_adjoint_host(op.handle, yhn.ctypes.data_as(ctypes.c_void_p),
+                                               xohn.ctypes.data_as(ctypes.c_void_p)))
+    e2e_step()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    t_e2e = (time.perf_counter() - t0) / args.e2e_steps
+    if dist:
+        t = torch.tensor([t_e2e], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    out["e2e"] = {"value": world * M / t_e2e / 1e6, "unit": "Mvis/s", "ms_per_step": t_e2e * 1e3,
+                  "h2d_bytes_per_step": 16 * (N + M), "d2h_bytes_per_step": 16 * (M + N),
+                  "api": "purify_gb300_forward_host + purify_gb300_adjoint_host "
+                         "(complex<double> host vectors)"}
+
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_reference(u, v, x, n, args.J, args.cpu_sample)
+    out["info"] = {k: info[k] for k in ("occupied_cells", "work_items", "tasks", "device_bytes",
+                                        "kernel_fit_error")}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

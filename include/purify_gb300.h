@@ -1,0 +1,202 @@
+/*
+ * purify_gb300.h — C ABI of the GB300 measurement operator.
+ *
+ * The operator is PURIFY's Phi = G F Z S / ||Phi'||: gridding correction S,
+ * zero padding Z, an oversampled unitary FFT F and Kaiser-Bessel (or other
+ * kernel) degridding G, plus its adjoint.  It replaces the serial and GPU
+ * slots of the reference's operator factory:
+ *
+ *   measurementoperator::init_degrid_operator_2d   cpp/purify/operators.h:372-414
+ *   gpu::measurementoperator::init_degrid_operator_2d  cpp/purify/operators_gpu.h:292-332
+ *   factory::measurement_operator_factory (gpu_serial)  cpp/purify/measurement_operator_factory.h:38-96
+ *
+ * Conventions (those of the reference):
+ *   image vectors  imsizey x imsizex, index j * imsizex + i (row j is v/y)
+ *   grid           ftsizev x ftsizeu with ftsize = floor(oversample * imsize)
+ *   u, v           visibility coordinates in grid pixels (the "raw" overload);
+ *                  purify_gb300_lambda_to_pixels converts from wavelengths
+ *   complex data   interleaved (re, im); c128 = double pairs, c64 = float pairs
+ *   precision      PURIFY_GB300_FP32 computes with complex<float> buffers (c64
+ *                  device I/O), PURIFY_GB300_FP64 with complex<double> (c128)
+ *
+ * Every function returns a purify_gb300_status; on failure
+ * purify_gb300_last_error() holds a message for the calling thread.  Nothing
+ * throws across this boundary.  Applies of one operator are ordered on an
+ * internal CUDA stream (joined to the caller's stream by events), so one
+ * operator may be shared by threads.
+ */
+#ifndef PURIFY_GB300_H
+#define PURIFY_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  PURIFY_GB300_OK = 0,
+  PURIFY_GB300_INVALID_ARGUMENT = 1, /* reference: std::runtime_error on sizes (operators.cc:18-20) */
+  PURIFY_GB300_UNSUPPORTED = 2,
+  PURIFY_GB300_CUDA_ERROR = 3,
+  PURIFY_GB300_OUT_OF_MEMORY = 4,
+  PURIFY_GB300_NORM_NOT_POSITIVE = 5, /* reference: init_normalise, operators.h:185-189 */
+  PURIFY_GB300_REJECTED = 6,          /* serving: request refused by admission control */
+  PURIFY_GB300_TIMEOUT = 7,
+  PURIFY_GB300_INTERNAL = 8
+} purify_gb300_status;
+
+/* Kernel ids in the order of kernels::kernel (cpp/purify/kernels.h:15). */
+typedef enum {
+  PURIFY_GB300_KERNEL_KB = 0,
+  PURIFY_GB300_KERNEL_GAUSS = 1,
+  PURIFY_GB300_KERNEL_BOX = 2,
+  PURIFY_GB300_KERNEL_PSWF = 3,
+  PURIFY_GB300_KERNEL_KBMIN = 4,
+  PURIFY_GB300_KERNEL_GAUSS_ALT = 5
+} purify_gb300_kernel;
+
+typedef enum { PURIFY_GB300_FP32 = 0, PURIFY_GB300_FP64 = 1 } purify_gb300_precision;
+
+typedef struct purify_gb300_operator purify_gb300_operator;
+
+/* Everything init_degrid_operator_2d takes (operators.h:373-380), plus the
+ * precision.  power_iters = 0 leaves the norm at 1 (call power_method later). */
+typedef struct {
+  const double *u;       /* M coordinates, grid pixels */
+  const double *v;       /* M */
+  const double *w;       /* M, or NULL (only read when w_term != 0) */
+  const double *weights; /* M complex (c128), or NULL for all ones */
+  int64_t M;
+  uint32_t imsizey, imsizex;
+  double oversample_ratio; /* default 2 */
+  uint32_t power_iters;    /* default 100 */
+  double power_tol;        /* default 1e-4 */
+  int32_t kernel;          /* purify_gb300_kernel, default KB */
+  uint32_t Ju, Jv;         /* default 4, 4 */
+  int32_t w_term;          /* default 0 */
+  uint32_t Jw;             /* default 6 */
+  double cellx, celly;     /* arcsec, default 1, 1 */
+  int32_t precision;       /* purify_gb300_precision */
+  int32_t device;          /* CUDA device ordinal */
+} purify_gb300_create_args;
+
+/* Fills `args` with the reference's defaults (operators.h:373-380). */
+void purify_gb300_default_args(purify_gb300_create_args *args);
+
+/* Builds S, Z, F and G (the coverage plan) on the device, then runs the power
+ * method when power_iters > 0 and normalises both directions by the norm.
+ * Replaces measurementoperator::init_degrid_operator_2d (operators.h:373-396). */
+int purify_gb300_operator_create(const purify_gb300_create_args *args,
+                                 purify_gb300_operator **out);
+int purify_gb300_operator_destroy(purify_gb300_operator *op);
+
+/* Phi x and Phi^H y on device buffers of the operator's precision (c64 for
+ * FP32, c128 for FP64).  x has imsizey*imsizex values, y has M values.  The
+ * work is ordered after prior work on `stream` (a cudaStream_t, 0 = legacy
+ * default stream) and later work on `stream` sees the result.
+ * Replaces the direct/indirect closures of operators.h:325-326,393-395. */
+int purify_gb300_forward(purify_gb300_operator *op, const void *x, void *y, void *stream);
+int purify_gb300_adjoint(purify_gb300_operator *op, const void *y, void *x, void *stream);
+
+/* Same on host complex<double> vectors (the reference's Vector<t_complex>);
+ * copies in and out of the device inside the call, which returns when the
+ * result is in `y` / `x`.  Replaces the host_wrapper path of
+ * operators_gpu.h:42-68. */
+int purify_gb300_forward_host(purify_gb300_operator *op, const double *x, double *y);
+int purify_gb300_adjoint_host(purify_gb300_operator *op, const double *y, double *x);
+
+/* G and G^H alone on device buffers of the operator's precision: grid is
+ * ftsizev*ftsizeu values (index p * ftsizeu + q), vis is M values.  Replaces
+ * the closures of operators::init_gridding_matrix_2d (operators.h:123-145). */
+int purify_gb300_degrid(purify_gb300_operator *op, const void *grid, void *vis, void *stream);
+int purify_gb300_grid(purify_gb300_operator *op, const void *vis, void *grid, void *stream);
+
+/* Gridding correction S(j, i) as imsizey*imsizex complex<double> values
+ * (row j, column i), as details::init_correction2d builds it
+ * (operators.cc:101-121).  Host only. */
+int purify_gb300_correction(int32_t kernel, uint32_t Ju, uint32_t Jv, uint32_t imsizey,
+                            uint32_t imsizex, double oversample_ratio, double *S_out);
+
+/* Power method on Phi'^H Phi' (the unnormalised operator) from the all-ones
+ * vector; sets and returns ||Phi'|| (operators.h:390-392, sopt::power_method). */
+int purify_gb300_power_method(purify_gb300_operator *op, uint32_t iters, double tol,
+                              double *norm_out);
+/* Sets / reads the norm both directions divide by (operators.h:185-189). */
+int purify_gb300_set_norm(purify_gb300_operator *op, double norm);
+int purify_gb300_get_norm(const purify_gb300_operator *op, double *norm);
+
+/* Per-stage device timing with CUDA events recorded on the operator's own
+ * stream around each stage (pad, FFT forward, degrid, grid, fold, FFT
+ * inverse, crop).  enable != 0 starts recording and clears the totals;
+ * purify_gb300_stage_times waits for the recorded work and returns the total
+ * milliseconds and launch count of each stage (7 entries each).  No
+ * counterpart in the reference (its benchmarks time whole applies with
+ * std::chrono, cpp/benchmarks/measurement_operator.cc:124-125). */
+#define PURIFY_GB300_STAGES 7
+int purify_gb300_stage_timing(purify_gb300_operator *op, int enable);
+int purify_gb300_stage_times(purify_gb300_operator *op, double *total_ms, int64_t *launches);
+
+typedef struct {
+  int64_t M;
+  uint32_t imsizey, imsizex, ftsizev, ftsizeu;
+  uint32_t Ju, Jv;
+  int32_t precision;
+  int32_t kernel;
+  int32_t w_term;
+  int64_t nnz;             /* non-zeros of G (taps) */
+  int64_t occupied_cells;  /* distinct base cells of the coverage */
+  int64_t work_items;      /* lane work items incl. padding */
+  int64_t tasks;           /* CTA tasks per apply */
+  int64_t device_bytes;    /* device memory held by the operator */
+  double kernel_fit_error; /* max |poly - kernel| of the tap weights (abs) */
+  double norm;
+} purify_gb300_info;
+int purify_gb300_operator_info(const purify_gb300_operator *op, purify_gb300_info *info);
+
+/* utilities::set_cell_size + uv_scale (utilities.cc:208-278): wavelengths ->
+ * grid pixels for a ftsizeu x ftsizev grid; cell sizes in arcsec, 0 derives
+ * them from max |u|, |v| as the reference does. */
+int purify_gb300_lambda_to_pixels(const double *u, const double *v, int64_t M, double cellx,
+                                  double celly, uint32_t ftsizeu, uint32_t ftsizev,
+                                  double *u_out, double *v_out);
+
+/* ---- Host-side introspection (no GPU work) --------------------------------
+ * The coverage plan the operator uploads: visibilities in plan order (tile,
+ * then base cell), their FP64 fractional offsets, sign-folded weights, the
+ * permutation to caller order, the 32-lane work items and the CTA tasks.
+ * No counterpart in the reference (its G is an explicit CSR matrix,
+ * operators.cc:8-46); exposed so host logic can be tested without a GPU. */
+typedef struct purify_gb300_plan purify_gb300_plan;
+int purify_gb300_plan_create(const double *u, const double *v, const double *weights, int64_t M,
+                             uint32_t ftsizeu, uint32_t ftsizev, uint32_t J,
+                             purify_gb300_plan **out);
+/* sizes[0..6] = M, work items, tasks, tiles along u, tiles along v,
+ * window rows, window columns. */
+int purify_gb300_plan_sizes(const purify_gb300_plan *plan, int64_t *sizes);
+/* frac: 2M doubles (t_u, t_v); weight: 2M doubles; perm: M; item_first and
+ * item_code: work items; tasks: 8 int32 per task (P, Q, H, W, batch_begin,
+ * batch_end, tile, 0); tile_tasks: tiles + 1; tu_start: tiles_u + 1;
+ * tv_start: tiles_v + 1.  Any pointer may be NULL. */
+int purify_gb300_plan_export(const purify_gb300_plan *plan, double *frac, double *weight,
+                             int32_t *perm, int32_t *item_first, int32_t *item_code,
+                             int32_t *tasks, int32_t *tile_tasks, int32_t *tu_start,
+                             int32_t *tv_start);
+int purify_gb300_plan_destroy(purify_gb300_plan *plan);
+/* Tap weights as the device evaluates them: for each t in [0, 1) the J values
+ * (-1)^j kernel(t + J/2 - 1 - j), j = 0..J-1, from the fitted polynomials
+ * evaluated in the precision's arithmetic (out: n * J doubles).  Returns the
+ * fit's max deviation in *fit_error when non-null.  kernels.cc:7-230. */
+int purify_gb300_kernel_taps(int32_t kernel, uint32_t J, double oversample_ratio,
+                             int32_t precision, const double *t, int64_t n, double *out,
+                             double *fit_error);
+
+/* Message of the last failing call on this thread ("" when none). */
+const char *purify_gb300_last_error(void);
+/* Library version string. */
+const char *purify_gb300_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PURIFY_GB300_H */

@@ -1,0 +1,806 @@
+// ============================================================================
+//  purify_oracle.cpp — CPU FP64 restatement of PURIFY's measurement operator.
+//
+//  TEST INFRASTRUCTURE ONLY.  This file is the parity checker for the GB300
+//  measurement operator: tests/, __graft_entry__.smoke() and the CPU-baseline
+//  leg of bench.py load it.  Nothing in the product library links, calls or
+//  falls back to it.
+//
+//  It restates, in std::complex<double>, the reference algorithm exactly as
+//  the reference structures it:
+//    * explicit row-major CSR interpolation matrix G and an explicit copy of
+//      its adjoint (cpp/purify/operators.h:123-145),
+//    * a row-parallel OpenMP SpMV (cpp/purify/utilities.h:143-159),
+//    * a unitary 2-D FFT (cpp/purify/operators.h:206-261; FFTW is absent, so a
+//      radix-2 / Bluestein FFT written here stands in for it),
+//    * the gridding correction S (cpp/purify/operators.cc:101-121) and the
+//      zero-padding operator Z (cpp/purify/operators.h:147-183),
+//    * a power method for the operator norm (call site
+//      cpp/purify/operators.h:390-395; the sopt implementation is absent, see
+//      or_power_method below).
+//  Third-party arithmetic that the reference takes from libraries is restated:
+//    * Boost cyl_bessel_i(0, x)  -> std::cyl_bessel_i (libstdc++ C++17 special
+//      math), pinned against the reference's kernel golden vectors at 1e-13;
+//    * Boost sinc_pi             -> sin(x)/x with the x == 0 limit;
+//    * FFTW3 dft_2d              -> the FFT below (sign convention of FFTW:
+//      forward = exp(-2 pi i jk/n), backward = exp(+2 pi i jk/n), unscaled).
+//
+//  Every exported entry point is extern "C" so that Python (ctypes) can load
+//  the compiled library without a binding generator.
+// ============================================================================
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <cstring>
+#include <functional>
+#include <memory>
+#include <numeric>
+#include <stdexcept>
+#include <string>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace oracle {
+
+using t_real = double;
+using t_complex = std::complex<double>;
+using t_int = std::int64_t;
+// constant::pi, cpp/purify/types.h:55
+constexpr t_real pi = 3.14159265358979323846;
+
+// Kernel identifiers follow the order of kernels::kernel (cpp/purify/kernels.h:15).
+enum KernelId { KB = 0, GAUSS = 1, BOX = 2, PSWF = 3, KBMIN = 4, GAUSS_ALT = 5 };
+
+// ---------------------------------------------------------------- kernels --
+// cpp/purify/kernels.cc:15-22
+t_real kaiser_bessel_general(t_real x, t_int J, t_real alpha) {
+  const t_real a = 2 * x / J;
+  return std::cyl_bessel_i(0.0, alpha * std::sqrt(1 - a * a)) / std::cyl_bessel_i(0.0, alpha);
+}
+// cpp/purify/kernels.cc:7-13  (alpha = 2.34 J, Fessler et al. 2003)
+t_real kaiser_bessel(t_real x, t_int J) { return kaiser_bessel_general(x, J, 2.34 * J); }
+
+// cpp/purify/kernels.cc:24-38.  The constant 38828.11016883 is the
+// reference's normalisation; it is pinned by expected_S_data.
+t_real ft_kaiser_bessel_general(t_real x, t_int J, t_real alpha) {
+  const t_complex eta =
+      std::sqrt(t_complex((pi * x * J) * (pi * x * J) - alpha * alpha, 0.0));
+  const t_real normalisation = 38828.11016883;
+  return std::real(std::sin(eta) / eta) / normalisation;
+}
+// cpp/purify/kernels.cc:40-47
+t_real ft_kaiser_bessel(t_real x, t_int J) { return ft_kaiser_bessel_general(x, J, 2.34 * J); }
+
+// cpp/purify/kernels.cc:206-217
+t_real gaussian_general(t_real x, t_int, t_real sigma) {
+  const t_real a = x / sigma;
+  return std::exp(-a * a * 0.5);
+}
+// cpp/purify/kernels.cc:219-230
+t_real ft_gaussian_general(t_real x, t_int, t_real sigma) {
+  const t_real a = x * sigma * pi;
+  return std::sqrt(pi / 2) / sigma * std::exp(-a * a * 2);
+}
+// cpp/purify/kernels.cc:49-69  (sigma = 0.31 J^0.52)
+t_real gaussian(t_real x, t_int J) { return gaussian_general(x, J, 0.31 * std::pow(J, 0.52)); }
+t_real ft_gaussian(t_real x, t_int J) {
+  return ft_gaussian_general(x, J, 0.31 * std::pow(J, 0.52));
+}
+
+// cpp/purify/kernels.cc:71-105.  Schwab (1983) rational approximation of the
+// J = 6, alpha = 1 prolate spheroidal wave function; two branches in |eta|.
+t_real calc_for_pswf(t_real eta0, t_int J, t_real alpha) {
+  static const t_real p1[6] = {8.203343e-2, -3.644705e-1, 6.278660e-1,
+                               -5.335581e-1, 2.312756e-1, 2 * 0.0};
+  static const t_real p2[6] = {4.028559e-3, -3.697768e-2, 1.021332e-1,
+                               -1.201436e-1, 6.412774e-2, 2 * 0.0};
+  static const t_real q1[3] = {1., 8.212018e-1, 2.078043e-1};
+  static const t_real q2[3] = {1., 9.599102e-1, 2.918724e-1};
+  if (J != 6 || alpha != 1) return 0;
+  auto fraction = [](t_real eta, const t_real *p, const t_real *q) {
+    t_real num = p[5];
+    for (int i = 1; i <= 5; ++i) num = eta * num + p[5 - i];
+    t_real den = q[2];
+    for (int i = 1; i <= 2; ++i) den = eta * den + q[2 - i];
+    return num / den;
+  };
+  const t_real ae = std::abs(eta0);
+  if (0 <= ae && ae <= 0.75) return fraction(eta0 * eta0 - 0.75 * 0.75, p1, q1);
+  if (0.75 < ae && ae <= 1) return fraction(eta0 * eta0 - 1 * 1, p2, q2);
+  return 0;
+}
+// cpp/purify/kernels.cc:107-122
+t_real pswf(t_real x, t_int J) {
+  const t_real eta0 = 2 * x / J;
+  const t_real alpha = 1;
+  return calc_for_pswf(eta0, J, alpha) * std::pow(1 - eta0 * eta0, alpha);
+}
+// cpp/purify/kernels.cc:124-142
+t_real ft_pswf(t_real x, t_int J) { return calc_for_pswf(2 * x, J, 1); }
+
+// cpp/purify/kernels.cc:188-205 (sinc_pi restated as sin(z)/z, 1 at z = 0)
+t_real pill_box(t_real, t_int J) { return 1. / static_cast<t_real>(J); }
+t_real ft_pill_box(t_real x, t_int J) {
+  const t_real z = J * x * pi;
+  return z == 0 ? 1.0 : std::sin(z) / z;
+}
+
+// kbmin's alpha, cpp/purify/kernels.cc:259-266
+t_real kbmin_alpha(t_int J, t_real os) {
+  return pi * std::sqrt(J * J / (os * os) * (os - 0.5) * (os - 0.5) - 0.8);
+}
+
+// Spatial kernel value for a kernel id; the per-id formulas are those that
+// create_kernels binds (cpp/purify/kernels.cc:245-319).
+t_real kernel_value(int id, t_real x, t_int J, t_real os) {
+  switch (id) {
+    case KB: return kaiser_bessel(x, J);
+    case KBMIN: return kaiser_bessel_general(x, J, kbmin_alpha(J, os));
+    case PSWF: return pswf(x, J);
+    case GAUSS: return gaussian(x, J);
+    case BOX: return pill_box(x, J);
+    case GAUSS_ALT: return gaussian_general(x, J, 1.0);
+  }
+  throw std::runtime_error("Did not choose valid kernel.");
+}
+// Fourier-domain kernel value evaluated at the already-shifted argument
+// (create_kernels passes x / ftsize - 0.5).
+t_real ft_kernel_value(int id, t_real x, t_int J, t_real os) {
+  switch (id) {
+    case KB: return ft_kaiser_bessel(x, J);
+    case KBMIN: return ft_kaiser_bessel_general(x, J, kbmin_alpha(J, os));
+    case PSWF: return ft_pswf(x, J);
+    case GAUSS: return ft_gaussian(x, J);
+    case BOX: return ft_pill_box(x, J);
+    case GAUSS_ALT: return ft_gaussian_general(x, J, 1.0);
+  }
+  throw std::runtime_error("Did not choose valid kernel.");
+}
+
+// ------------------------------------------------------------- utilities --
+// utilities::mod, cpp/purify/utilities.cc:350-357
+t_real mod(t_real x, t_real y) {
+  t_real r = std::fmod(x, y);
+  if (r < 0) r = y + r;
+  return r;
+}
+
+// ------------------------------------------------------------------ FFT ---
+// Unitary 2-D DFT over a row-major Nv x Nu array (fastest index u), the
+// layout fftw_plan_dft_2d(ftsizev, ftsizeu, ...) uses (operators.h:233-241).
+// Power-of-two lengths use an iterative radix-2 Cooley-Tukey transform; other
+// lengths use Bluestein's chirp-z algorithm on a power-of-two convolution.
+class FFT1D {
+ public:
+  explicit FFT1D(t_int n) : n_(n) {
+    pow2_ = n > 0 && (n & (n - 1)) == 0;
+    if (pow2_) {
+      build_radix2(n_, tw_, rev_);
+    } else {
+      m_ = 1;
+      while (m_ < 2 * n_ - 1) m_ <<= 1;
+      build_radix2(m_, tw_, rev_);
+      chirp_.resize(n_);
+      for (t_int k = 0; k < n_; ++k) {
+        // exp(-i pi k^2 / n) with k^2 reduced mod 2n to keep the argument small
+        const t_int k2 = (k * k) % (2 * n_);
+        chirp_[k] = std::polar(1.0, -pi * static_cast<t_real>(k2) / n_);
+      }
+      std::vector<t_complex> b(m_, 0.0);
+      b[0] = std::conj(chirp_[0]);
+      for (t_int k = 1; k < n_; ++k) b[k] = b[m_ - k] = std::conj(chirp_[k]);
+      radix2(b.data(), m_, false);
+      bhat_ = b;
+    }
+  }
+  // sign: forward = exp(-2 pi i jk / n); inverse = exp(+2 pi i jk / n); unscaled.
+  void run(t_complex *x, bool inverse) const {
+    if (pow2_) {
+      radix2(x, n_, inverse);
+      return;
+    }
+    if (inverse) {
+      for (t_int k = 0; k < n_; ++k) x[k] = std::conj(x[k]);
+    }
+    std::vector<t_complex> a(m_, 0.0);
+    for (t_int k = 0; k < n_; ++k) a[k] = x[k] * chirp_[k];
+    radix2(a.data(), m_, false);
+    for (t_int k = 0; k < m_; ++k) a[k] *= bhat_[k];
+    radix2(a.data(), m_, true);
+    const t_real s = 1.0 / m_;
+    for (t_int k = 0; k < n_; ++k) x[k] = a[k] * s * chirp_[k];
+    if (inverse) {
+      for (t_int k = 0; k < n_; ++k) x[k] = std::conj(x[k]);
+    }
+  }
+
+ private:
+  static void build_radix2(t_int n, std::vector<t_complex> &tw, std::vector<t_int> &rev) {
+    tw.resize(n / 2 > 0 ? n / 2 : 1);
+    for (t_int k = 0; k < n / 2; ++k) tw[k] = std::polar(1.0, -2 * pi * k / n);
+    rev.resize(n);
+    int lg = 0;
+    while ((t_int(1) << lg) < n) ++lg;
+    for (t_int i = 0; i < n; ++i) {
+      t_int r = 0;
+      for (int b = 0; b < lg; ++b)
+        if (i & (t_int(1) << b)) r |= t_int(1) << (lg - 1 - b);
+      rev[i] = r;
+    }
+  }
+  void radix2(t_complex *x, t_int n, bool inverse) const {
+    const std::vector<t_int> &rev = rev_;
+    for (t_int i = 0; i < n; ++i)
+      if (i < rev[i]) std::swap(x[i], x[rev[i]]);
+    const t_int full = pow2_ ? n_ : m_;
+    for (t_int len = 2; len <= n; len <<= 1) {
+      const t_int half = len / 2, step = full / len;
+      for (t_int i = 0; i < n; i += len)
+        for (t_int j = 0; j < half; ++j) {
+          t_complex w = tw_[j * step];
+          if (inverse) w = std::conj(w);
+          const t_complex a = x[i + j], b = x[i + j + half] * w;
+          x[i + j] = a + b;
+          x[i + j + half] = a - b;
+        }
+    }
+  }
+  t_int n_, m_ = 0;
+  bool pow2_;
+  std::vector<t_complex> tw_, chirp_, bhat_;
+  std::vector<t_int> rev_;
+};
+
+struct FFT2D {
+  t_int nv, nu;
+  FFT1D fu, fv;
+  FFT2D(t_int nv_, t_int nu_) : nv(nv_), nu(nu_), fu(nu_), fv(nv_) {}
+  // out = F in (forward) or F^H in (inverse), each divided by sqrt(nu*nv)
+  // as in operators.h:242-259.
+  void run(const t_complex *in, t_complex *out, bool inverse) const {
+    if (out != in) std::copy(in, in + nv * nu, out);
+#pragma omp parallel for schedule(static)
+    for (t_int r = 0; r < nv; ++r) fu.run(out + r * nu, inverse);
+#pragma omp parallel
+    {
+      std::vector<t_complex> col(nv);
+#pragma omp for schedule(static)
+      for (t_int c = 0; c < nu; ++c) {
+        for (t_int r = 0; r < nv; ++r) col[r] = out[r * nu + c];
+        fv.run(col.data(), inverse);
+        for (t_int r = 0; r < nv; ++r) out[r * nu + c] = col[r];
+      }
+    }
+    const t_real s = 1.0 / std::sqrt(static_cast<t_real>(nv * nu));
+#pragma omp parallel for schedule(static)
+    for (t_int k = 0; k < nv * nu; ++k) out[k] *= s;
+  }
+};
+
+// -------------------------------------------------------- sparse matrix ---
+// Row-major CSR with 64-bit offsets (the reference's Sparse<t_complex> is an
+// Eigen RowMajor matrix, types.h:27-28; 64-bit offsets let the oracle hold
+// the larger benchmark operators).
+struct CSR {
+  t_int rows = 0, cols = 0;
+  std::vector<t_int> offsets;
+  std::vector<std::int32_t> index;
+  std::vector<t_complex> value;
+  // Row-parallel product, the structure of sparse_multiply_matrix
+  // (utilities.h:143-159): every row is summed by one thread, in column order.
+  void multiply(const t_complex *x, t_complex *y) const {
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (t_int k = 0; k < rows; ++k) {
+      t_complex acc = 0;
+      for (t_int e = offsets[k]; e < offsets[k + 1]; ++e) acc += value[e] * x[index[e]];
+      y[k] = acc;
+    }
+  }
+  // Conjugate transpose, the explicit copy that operators.h:135-136 keeps.
+  CSR adjoint() const {
+    CSR a;
+    a.rows = cols;
+    a.cols = rows;
+    a.offsets.assign(cols + 1, 0);
+    for (t_int e = 0; e < offsets[rows]; ++e) a.offsets[index[e] + 1]++;
+    for (t_int c = 0; c < cols; ++c) a.offsets[c + 1] += a.offsets[c];
+    a.index.resize(offsets[rows]);
+    a.value.resize(offsets[rows]);
+    std::vector<t_int> fill(a.offsets.begin(), a.offsets.end() - 1);
+    for (t_int r = 0; r < rows; ++r)  // ascending r keeps every adjoint row sorted
+      for (t_int e = offsets[r]; e < offsets[r + 1]; ++e) {
+        const t_int d = fill[index[e]]++;
+        a.index[d] = static_cast<std::int32_t>(r);
+        a.value[d] = std::conj(value[e]);
+      }
+    return a;
+  }
+};
+
+// ---------------------------------------------------- w-projection rows ---
+// projection_kernels::pixel_to_lambda, cpp/purify/projection_kernels.cc:28-30
+t_real pixel_to_lambda(t_real cell, t_int imsize, t_real os) {
+  return 60. * 60. * 180. / cell / std::floor(os * imsize) / pi;
+}
+// w_projection_kernel_approx (projection_kernels.cc:16-22, 31-47).  Outside
+// the region where the small-angle chirp is valid the reference returns 1.
+struct WKernelApprox {
+  t_real du, dv;
+  t_complex operator()(t_real u, t_real v, t_real w) const {
+    if ((std::abs(u * du / w) < 1) && (std::abs(v * dv / w) < 1)) {
+      const t_complex I(0., 1.);
+      const t_real uu = u * du, vv = v * dv;
+      return std::exp(-pi * I * (uu * uu + vv * vv) / w) / w / I;
+    }
+    return 1.;
+  }
+};
+
+// convol::linear_convol_1d (convolution.h:42-52): out(j) = sum_k f(k) g(n-1-j+k)
+// over a zero-padded g of length n + Jf - 1 + (Jf - 1).
+static void linear_convol_1d(const t_complex *f, t_int Jf, const t_complex *gpad, t_int gpad_n,
+                             t_complex *out) {
+  const t_int n_out = gpad_n - Jf + 1;
+  for (t_int j = 0; j < n_out; ++j) {
+    t_complex acc = 0;
+    for (t_int k = 0; k < Jf; ++k) acc += f[k] * gpad[n_out - j - 1 + k];
+    out[j] = acc;
+  }
+}
+// convol::linear_convol_2d (convolution.h:54-82) followed by the row layout of
+// projection_kernels::projection (projection_kernels.cc:59-85).  Returns a
+// (Jv+Jw-1) x (Ju+Jw-1) column-major matrix K(jv, ju) = K[ju * rows + jv].
+// Note the reference evaluates the v-axis factor with the u-slot kernel
+// (projection_kernels.cc:72-75); that is kept.
+static std::vector<t_complex> projection(const std::function<t_real(t_real)> &kernelu,
+                                         const WKernelApprox *kw, bool box_w, t_real u, t_real v,
+                                         t_real w, t_int Ju, t_int Jv, t_int Jw) {
+  const t_real du = u - std::floor(u - Ju * 0.5);
+  const t_real dv = v - std::floor(v - Jv * 0.5);
+  const t_real dwu = u - std::floor(u - Jw * 0.5);
+  const t_real dwv = v - std::floor(v - Jw * 0.5);
+  std::vector<t_complex> fu(Ju), fv(Jv), g(Jw * Jw);  // g column-major (Jw rows x Jw cols)
+  for (t_int i = 0; i < Ju; ++i) fu[i] = kernelu(du - i - 1);
+  for (t_int i = 0; i < Jv; ++i) fv[i] = kernelu(dv - i - 1);
+  for (t_int ju = 0; ju < Jw; ++ju)
+    for (t_int jv = 0; jv < Jw; ++jv)
+      g[ju * Jw + jv] = box_w ? t_complex(1.) : (*kw)(dwu - ju - 1, dwv - jv - 1, w);
+  // buffer: (Jv + Jw - 1) x Jw, column i = convolution of fv with padded g.col(i)
+  const t_int brow = Jv + Jw - 1;
+  std::vector<t_complex> buffer(brow * Jw);
+  {
+    const t_int pad = Jv - 1;
+    std::vector<t_complex> gp(Jw + 2 * pad);
+    for (t_int i = 0; i < Jw; ++i) {
+      std::fill(gp.begin(), gp.end(), t_complex(0.));
+      for (t_int r = 0; r < Jw; ++r) gp[pad + r] = g[i * Jw + r];
+      linear_convol_1d(fv.data(), Jv, gp.data(), static_cast<t_int>(gp.size()),
+                       buffer.data() + i * brow);
+    }
+  }
+  const t_int ocol = Ju + Jw - 1;
+  std::vector<t_complex> out(brow * ocol);
+  {
+    const t_int pad = Ju - 1;
+    std::vector<t_complex> bp(Jw + 2 * pad), row(ocol);
+    for (t_int r = 0; r < brow; ++r) {
+      std::fill(bp.begin(), bp.end(), t_complex(0.));
+      for (t_int c = 0; c < Jw; ++c) bp[pad + c] = buffer[c * brow + r];
+      linear_convol_1d(fu.data(), Ju, bp.data(), static_cast<t_int>(bp.size()), row.data());
+      for (t_int c = 0; c < ocol; ++c) out[c * brow + r] = row[c];
+    }
+  }
+  return out;
+}
+
+// ------------------------------------------------------ gridding matrix ---
+struct GriddingArgs {
+  const t_real *u, *v, *w;
+  const t_complex *weights;
+  t_int M;
+  t_int imsizey, imsizex;
+  t_real os;
+  int kernel;
+  t_int Ju, Jv;
+  bool w_term;
+  t_int Jw;
+  const std::int32_t *jw_rows;  // optional per-row w-support (uniform Jw when null)
+  bool box_w;                   // box_proj() w-kernel (projection_kernels.cc:8-10)
+  t_real cellx, celly;
+};
+
+// details::init_gridding_matrix_2d, plain (operators.cc:8-46) and with
+// w-projection (operators.cc:49-99).  kernelu/kernelv are the functions that
+// base_degrid_operator_2d passes in the (kernelu, kernelv) slots; it passes
+// (kernelv, kernelu) (operators.h:322-324), which the caller reproduces.
+CSR init_gridding_matrix_2d(const GriddingArgs &a, const std::function<t_real(t_real)> &kernelu,
+                            const std::function<t_real(t_real)> &kernelv) {
+  const t_int ftsizev = static_cast<t_int>(std::floor(a.imsizey * a.os));
+  const t_int ftsizeu = static_cast<t_int>(std::floor(a.imsizex * a.os));
+  CSR G;
+  G.rows = a.M;
+  G.cols = ftsizeu * ftsizev;
+  G.offsets.assign(a.M + 1, 0);
+  const t_complex I(0, 1);
+  if (!a.w_term) {
+    const t_int ju_max = std::min(a.Ju, ftsizeu);
+    const t_int jv_max = std::min(a.Jv, ftsizev);
+    const t_int per = ju_max * jv_max;
+    for (t_int m = 0; m <= a.M; ++m) G.offsets[m] = m * per;
+    G.index.resize(a.M * per);
+    G.value.resize(a.M * per);
+#pragma omp parallel for schedule(static)
+    for (t_int m = 0; m < a.M; ++m) {
+      std::vector<std::pair<std::int32_t, t_complex>> row;
+      row.reserve(per);
+      for (t_int ju = 1; ju < ju_max + 1; ++ju)
+        for (t_int jv = 1; jv < jv_max + 1; ++jv) {
+          const t_real k_u = std::floor(a.u[m] - ju_max * 0.5);
+          const t_real k_v = std::floor(a.v[m] - jv_max * 0.5);
+          const t_int q = static_cast<t_int>(mod(k_u + ju, ftsizeu));
+          const t_int p = static_cast<t_int>(mod(k_v + jv, ftsizev));
+          const t_int index = p * ftsizeu + q;  // utilities::sub2ind (utilities.cc:321-333)
+          const t_complex val = std::exp(-2 * pi * I * ((k_u + ju) * 0.5 + (k_v + jv) * 0.5)) *
+                                kernelu(a.u[m] - (k_u + ju)) * kernelv(a.v[m] - (k_v + jv)) *
+                                a.weights[m];
+          row.emplace_back(static_cast<std::int32_t>(index), val);
+        }
+      std::sort(row.begin(), row.end(),
+                [](const auto &x, const auto &y) { return x.first < y.first; });
+      for (t_int e = 0; e < per; ++e) {
+        G.index[m * per + e] = row[e].first;
+        G.value[m * per + e] = row[e].second;
+      }
+    }
+    return G;
+  }
+  // w-projection rows (operators.cc:49-99), optionally with a per-row Jw.
+  for (t_int m = 0; m < a.M; ++m) {
+    const t_int Jw = a.jw_rows ? a.jw_rows[m] : a.Jw;
+    G.offsets[m + 1] = G.offsets[m] + (Jw + a.Ju - 1) * (Jw + a.Jv - 1);
+  }
+  G.index.resize(G.offsets[a.M]);
+  G.value.resize(G.offsets[a.M]);
+  WKernelApprox kw{pixel_to_lambda(a.cellx, a.imsizex, a.os),
+                   pixel_to_lambda(a.celly, a.imsizey, a.os)};
+#pragma omp parallel for schedule(dynamic, 64)
+  for (t_int m = 0; m < a.M; ++m) {
+    const t_int Jw = a.jw_rows ? a.jw_rows[m] : a.Jw;
+    const t_int Jwu = Jw + a.Ju - 1, Jwv = Jw + a.Jv - 1;
+    const std::vector<t_complex> K =
+        projection(kernelu, &kw, a.box_w, a.u[m], a.v[m], a.w[m], a.Ju, a.Jv, Jw);
+    const t_int kwu = static_cast<t_int>(std::floor(a.u[m] - Jwu * 0.5));
+    const t_int kwv = static_cast<t_int>(std::floor(a.v[m] - Jwv * 0.5));
+    std::vector<std::pair<std::int32_t, t_complex>> row;
+    row.reserve(Jwu * Jwv);
+    for (t_int ju = 1; ju < Jwu + 1; ++ju)
+      for (t_int jv = 1; jv < Jwv + 1; ++jv) {
+        const t_int q = static_cast<t_int>(mod(static_cast<t_real>(kwu + ju), ftsizeu));
+        const t_int p = static_cast<t_int>(mod(static_cast<t_real>(kwv + jv), ftsizev));
+        const t_int index = p * ftsizeu + q;
+        const t_complex val =
+            std::exp(-2 * pi * I * ((kwu + ju) * 0.5 + (kwv + jv) * 0.5)) *
+            K[(ju - 1) * Jwv + (jv - 1)] * a.weights[m];
+        row.emplace_back(static_cast<std::int32_t>(index), val);
+      }
+    std::sort(row.begin(), row.end(),
+              [](const auto &x, const auto &y) { return x.first < y.first; });
+    const t_int o = G.offsets[m];
+    for (size_t e = 0; e < row.size(); ++e) {
+      G.index[o + e] = row[e].first;
+      G.value[o + e] = row[e].second;
+    }
+  }
+  return G;
+}
+
+// ------------------------------------------------------- correction S -----
+// details::init_correction2d (operators.cc:101-121) with the w = 0 chirp of
+// wproj_utilities::generate_chirp (wproj_utilities.cc:76-109), which is
+// 1/(Nx Ny) in every pixel.  Returns S(j, i) row-major, j over imsizey.
+std::vector<t_complex> init_correction2d(int kernel, t_int Ju, t_int Jv, t_int imsizey,
+                                         t_int imsizex, t_real os) {
+  const t_int ftsizeu = static_cast<t_int>(std::floor(imsizex * os));
+  const t_int ftsizev = static_cast<t_int>(std::floor(imsizey * os));
+  const t_int x_start = static_cast<t_int>(std::floor(ftsizeu * 0.5 - imsizex * 0.5));
+  const t_int y_start = static_cast<t_int>(std::floor(ftsizev * 0.5 - imsizey * 0.5));
+  // ftkernelu/v of create_kernels: ft(x / ftsize - 0.5) (kernels.cc:249-254)
+  auto ftu = [&](t_real x) {
+    return ft_kernel_value(kernel, x / ftsizeu - 0.5, Ju, os);
+  };
+  auto ftv = [&](t_real x) {
+    return ft_kernel_value(kernel, x / ftsizev - 0.5, Jv, os);
+  };
+  const t_real nz = static_cast<t_real>(imsizey * imsizex);
+  const t_complex chirp = t_complex(1., 0.) / nz;  // generate_chirp at w_rate = 0
+  std::vector<t_complex> S(imsizey * imsizex);
+  for (t_int j = 0; j < imsizey; ++j) {
+    const t_real a = 1e0 / ftv(y_start + j + 0.5);  // range = 0.5, 1.5, ... (operators.cc:111-112)
+    for (t_int i = 0; i < imsizex; ++i) {
+      const t_real b = 1e0 / ftu(x_start + i + 0.5);
+      S[j * imsizex + i] = (a * b) * t_complex(1., 0.) * chirp * static_cast<t_real>(imsizex) *
+                           static_cast<t_real>(imsizey);
+    }
+  }
+  return S;
+}
+
+// ---------------------------------------------------------- the operator --
+struct Operator {
+  t_int M, imsizey, imsizex, ftsizev, ftsizeu, x_start, y_start;
+  CSR G, GH;
+  std::vector<t_complex> S;
+  std::unique_ptr<FFT2D> fft;
+  t_real norm = 1.0;
+  mutable std::vector<t_complex> grid_a, grid_b;
+
+  // Phi' x = G F Z S x (operators.h:298-329), then / norm (operators.h:185-189).
+  void forward(const t_complex *x, t_complex *y) const {
+    std::fill(grid_a.begin(), grid_a.end(), t_complex(0.));
+    // init_zero_padding_2d direct (operators.h:157-169)
+#pragma omp parallel for schedule(static)
+    for (t_int j = 0; j < imsizey; ++j)
+      for (t_int i = 0; i < imsizex; ++i)
+        grid_a[(y_start + j) * ftsizeu + x_start + i] = S[j * imsizex + i] * (x[j * imsizex + i] / norm);
+    fft->run(grid_a.data(), grid_b.data(), false);
+    G.multiply(grid_b.data(), y);
+  }
+  // Phi'^H y = Z^H F^H G^H y, then / norm.
+  void adjoint(const t_complex *y, t_complex *x) const {
+    GH.multiply(y, grid_a.data());
+    fft->run(grid_a.data(), grid_b.data(), true);
+    // init_zero_padding_2d indirect (operators.h:170-181)
+#pragma omp parallel for schedule(static)
+    for (t_int j = 0; j < imsizey; ++j)
+      for (t_int i = 0; i < imsizex; ++i)
+        x[j * imsizex + i] =
+            std::conj(S[j * imsizex + i]) * grid_b[(y_start + j) * ftsizeu + x_start + i] / norm;
+  }
+};
+
+static t_real stable_norm(const std::vector<t_complex> &x) {
+  t_real scale = 0, ssq = 1;
+  for (const auto &c : x)
+    for (t_real a : {std::abs(c.real()), std::abs(c.imag())}) {
+      if (a == 0) continue;
+      if (scale < a) {
+        ssq = 1 + ssq * (scale / a) * (scale / a);
+        scale = a;
+      } else {
+        ssq += (a / scale) * (a / scale);
+      }
+    }
+  return scale * std::sqrt(ssq);
+}
+
+}  // namespace oracle
+
+using namespace oracle;
+
+namespace {
+thread_local std::string g_error;
+template <class F>
+int guarded(F &&f) {
+  try {
+    f();
+    return 0;
+  } catch (const std::exception &e) {
+    g_error = e.what();
+    return 1;
+  }
+}
+}  // namespace
+
+extern "C" {
+
+const char *or_last_error() { return g_error.c_str(); }
+
+void or_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+int or_get_threads() {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+// Spatial kernel values (kernels.cc) at n points.
+int or_kernel_values(int kernel, int J, double os, const double *x, int64_t n, double *out) {
+  return guarded([&] {
+    for (int64_t k = 0; k < n; ++k) out[k] = kernel_value(kernel, x[k], J, os);
+  });
+}
+// Fourier-domain kernel values at n (already shifted) points.
+int or_ft_kernel_values(int kernel, int J, double os, const double *x, int64_t n, double *out) {
+  return guarded([&] {
+    for (int64_t k = 0; k < n; ++k) out[k] = ft_kernel_value(kernel, x[k], J, os);
+  });
+}
+// Modified Bessel I0 (the Boost cyl_bessel_i(0, .) restated).
+int or_bessel_i0(const double *x, int64_t n, double *out) {
+  return guarded([&] {
+    for (int64_t k = 0; k < n; ++k) out[k] = std::cyl_bessel_i(0.0, x[k]);
+  });
+}
+// Gridding correction S as an imsizey x imsizex row-major complex array.
+int or_correction(int kernel, int Ju, int Jv, int imsizey, int imsizex, double os, double *S_out) {
+  return guarded([&] {
+    const auto S = init_correction2d(kernel, Ju, Jv, imsizey, imsizex, os);
+    for (size_t k = 0; k < S.size(); ++k) {
+      S_out[2 * k] = S[k].real();
+      S_out[2 * k + 1] = S[k].imag();
+    }
+  });
+}
+// Unitary 2-D FFT of a row-major nv x nu complex array.
+int or_fft2(int nv, int nu, const double *in, double *out, int inverse) {
+  return guarded([&] {
+    FFT2D f(nv, nu);
+    f.run(reinterpret_cast<const t_complex *>(in), reinterpret_cast<t_complex *>(out),
+          inverse != 0);
+  });
+}
+
+// measurementoperator::init_degrid_operator_2d without the power method
+// (operators.h:372-396): builds S, Z, F, G and G^H.  u, v, w are in pixels.
+// weights: M complex values (interleaved re, im).  jw_rows (nullable) gives a
+// per-row w-support; box_w selects box_proj() as the w-kernel.
+void *or_create(const double *u, const double *v, const double *w, const double *weights,
+                int64_t M, int imsizey, int imsizex, double os, int kernel, int Ju, int Jv,
+                int w_term, int Jw, double cellx, double celly, const int32_t *jw_rows,
+                int box_w) {
+  Operator *op = nullptr;
+  int rc = guarded([&] {
+    if (kernel == PSWF && (Ju != 6 || Jv != 6))
+      throw std::runtime_error("Incorrect input: PSWF requires a support of 6");
+    std::unique_ptr<Operator> o(new Operator());
+    o->M = M;
+    o->imsizey = imsizey;
+    o->imsizex = imsizex;
+    o->ftsizeu = static_cast<t_int>(std::floor(imsizex * os));
+    o->ftsizev = static_cast<t_int>(std::floor(imsizey * os));
+    o->x_start = static_cast<t_int>(std::floor(o->ftsizeu * 0.5 - imsizex * 0.5));
+    o->y_start = static_cast<t_int>(std::floor(o->ftsizev * 0.5 - imsizey * 0.5));
+    o->S = init_correction2d(kernel, Ju, Jv, imsizey, imsizex, os);
+    o->fft.reset(new FFT2D(o->ftsizev, o->ftsizeu));
+    o->grid_a.assign(o->ftsizeu * o->ftsizev, 0.);
+    o->grid_b.assign(o->ftsizeu * o->ftsizev, 0.);
+    // w - mean(w) (operators.h:323); the mean itself only reaches S, where
+    // init_correction2d ignores it.
+    std::vector<t_real> wc(M, 0.0);
+    if (M > 0 && w) {
+      t_real mean = 0;
+      for (int64_t m = 0; m < M; ++m) mean += w[m];
+      mean /= static_cast<t_real>(M);
+      for (int64_t m = 0; m < M; ++m) wc[m] = w[m] - mean;
+    }
+    GriddingArgs a{u,      v,  wc.data(), reinterpret_cast<const t_complex *>(weights),
+                   M,      imsizey, imsizex, os, kernel, Ju, Jv, w_term != 0, Jw, jw_rows,
+                   box_w != 0, cellx, celly};
+    // create_kernels (kernels.cc:233-323): kbu uses Ju, kbv uses Jv; the
+    // gridding matrix receives (kernelv, kernelu) in its (u, v) slots.
+    auto kfu = [kernel, Ju, os](t_real x) { return kernel_value(kernel, x, Ju, os); };
+    auto kfv = [kernel, Jv, os](t_real x) { return kernel_value(kernel, x, Jv, os); };
+    o->G = init_gridding_matrix_2d(a, kfv, kfu);
+    o->GH = o->G.adjoint();
+    op = o.release();
+  });
+  return rc == 0 ? op : nullptr;
+}
+
+void or_destroy(void *h) { delete static_cast<Operator *>(h); }
+
+int64_t or_nnz(void *h) { return static_cast<Operator *>(h)->G.offsets.back(); }
+void or_shape(void *h, int64_t *out6) {
+  auto *o = static_cast<Operator *>(h);
+  out6[0] = o->M;
+  out6[1] = o->imsizey;
+  out6[2] = o->imsizex;
+  out6[3] = o->ftsizev;
+  out6[4] = o->ftsizeu;
+  out6[5] = o->G.offsets.back();
+}
+// Copy of G in CSR form (offsets M+1, index nnz, values nnz complex).
+void or_get_G(void *h, int64_t *offsets, int32_t *index, double *values) {
+  auto *o = static_cast<Operator *>(h);
+  std::copy(o->G.offsets.begin(), o->G.offsets.end(), offsets);
+  std::copy(o->G.index.begin(), o->G.index.end(), index);
+  for (size_t k = 0; k < o->G.value.size(); ++k) {
+    values[2 * k] = o->G.value[k].real();
+    values[2 * k + 1] = o->G.value[k].imag();
+  }
+}
+void or_G_forward(void *h, const double *grid, double *vis) {
+  static_cast<Operator *>(h)->G.multiply(reinterpret_cast<const t_complex *>(grid),
+                                         reinterpret_cast<t_complex *>(vis));
+}
+void or_G_adjoint(void *h, const double *vis, double *grid) {
+  static_cast<Operator *>(h)->GH.multiply(reinterpret_cast<const t_complex *>(vis),
+                                          reinterpret_cast<t_complex *>(grid));
+}
+void or_forward(void *h, const double *x, double *y) {
+  static_cast<Operator *>(h)->forward(reinterpret_cast<const t_complex *>(x),
+                                      reinterpret_cast<t_complex *>(y));
+}
+void or_adjoint(void *h, const double *y, double *x) {
+  static_cast<Operator *>(h)->adjoint(reinterpret_cast<const t_complex *>(y),
+                                      reinterpret_cast<t_complex *>(x));
+}
+void or_set_norm(void *h, double norm) { static_cast<Operator *>(h)->norm = norm; }
+double or_get_norm(void *h) { return static_cast<Operator *>(h)->norm; }
+
+// Power method for ||Phi'|| (the norm applied by operators.h:390-395).  The
+// sopt implementation is absent from the reference tree; this is the standard
+// power iteration on Phi'^H Phi' from x0 (ones when null), normalising the
+// iterate each round, stopping when the relative change of the eigenvalue
+// estimate falls below tol^2, and returning sqrt(eigenvalue).  iters == 0
+// returns 1.  The operator's current norm is ignored (the power method runs
+// on the unnormalised operator) and is then set to the result.
+int or_power_method(void *h, int iters, double tol, const double *x0, double *norm_out) {
+  return guarded([&] {
+    auto *o = static_cast<Operator *>(h);
+    const t_int N = o->imsizey * o->imsizex;
+    o->norm = 1.0;
+    if (iters <= 0) {
+      *norm_out = 1.0;
+      return;
+    }
+    std::vector<t_complex> x(N, t_complex(1., 0.)), y(o->M);
+    if (x0)
+      for (t_int k = 0; k < N; ++k) x[k] = t_complex(x0[2 * k], x0[2 * k + 1]);
+    t_real nx = stable_norm(x);
+    for (auto &c : x) c /= nx;
+    t_real old_value = 0, value = 1;
+    for (int i = 0; i < iters; ++i) {
+      o->forward(x.data(), y.data());
+      o->adjoint(y.data(), x.data());
+      value = stable_norm(x);
+      if (!(value > 0)) throw std::runtime_error("Operator norm is not greater than zero.");
+      for (auto &c : x) c /= value;
+      if (tol * tol > std::abs(old_value - value) / old_value) {
+        old_value = value;
+        break;
+      }
+      old_value = value;
+    }
+    o->norm = std::sqrt(old_value);
+    *norm_out = o->norm;
+  });
+}
+
+// utilities::set_cell_size (utilities.cc:208-256) for lambda units, and
+// utilities::uv_scale (utilities.cc:258-278): lambda -> radians -> pixels.
+// cell sizes of 0 are derived from max |u|, |v| as the reference does.
+void or_lambda_to_pixels(const double *u, const double *v, int64_t M, double cellx, double celly,
+                         int ftsizeu, int ftsizev, double *u_out, double *v_out) {
+  double max_u = 0, max_v = 0;
+  for (int64_t m = 0; m < M; ++m) {
+    max_u = std::max(max_u, u[m] * u[m]);
+    max_v = std::max(max_v, v[m] * v[m]);
+  }
+  max_u = std::sqrt(max_u);
+  max_v = std::sqrt(max_v);
+  double cu = cellx, cv = celly;
+  if (cu == 0 && cv == 0) {
+    cu = (180 * 3600) / max_u / pi / 3;
+    cv = (180 * 3600) / max_v / pi / 3;
+  }
+  if (cv == 0) cv = cu;
+  const double su = 180 * 3600 / cu / pi, sv = 180 * 3600 / cv / pi;
+  for (int64_t m = 0; m < M; ++m) {
+    const double ur = u[m] / su * 2 * pi, vr = v[m] / sv * 2 * pi;
+    u_out[m] = ur / (2 * pi) * ftsizeu;
+    v_out[m] = vr / (2 * pi) * ftsizev;
+  }
+}
+
+}  // extern "C"

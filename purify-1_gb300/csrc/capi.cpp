@@ -1,0 +1,364 @@
+// extern "C" boundary: translates pg::Error into status codes and a
+// thread-local message; nothing throws across it.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/purify_gb300.h"
+#include "gridding_kernels.h"
+#include "operator.h"
+#include "plan.h"
+
+struct purify_gb300_operator {
+  std::unique_ptr<pg::Operator> impl;
+};
+struct purify_gb300_plan {
+  pg::Plan plan;
+};
+
+namespace {
+thread_local std::string g_last_error;
+
+template <class F>
+int guard(F &&f) {
+  try {
+    g_last_error.clear();
+    f();
+    return PURIFY_GB300_OK;
+  } catch (const pg::Error &e) {
+    g_last_error = e.what();
+    return int(e.status);
+  } catch (const std::bad_alloc &) {
+    g_last_error = "host allocation failed";
+    return PURIFY_GB300_OUT_OF_MEMORY;
+  } catch (const std::exception &e) {
+    g_last_error = e.what();
+    return PURIFY_GB300_INTERNAL;
+  }
+}
+
+int null_arg(const char *what) {
+  g_last_error = std::string(what) + " is null";
+  return PURIFY_GB300_INVALID_ARGUMENT;
+}
+}  // namespace
+
+extern "C" {
+
+const char *purify_gb300_last_error(void) { return g_last_error.c_str(); }
+const char *purify_gb300_version(void) { return "purify_gb300 0.1.0 (sm_103a)"; }
+
+void purify_gb300_default_args(purify_gb300_create_args *a) {
+  if (!a) return;
+  std::memset(a, 0, sizeof(*a));
+  a->oversample_ratio = 2.0;
+  a->power_iters = 100;
+  a->power_tol = 1e-4;
+  a->kernel = PURIFY_GB300_KERNEL_KB;
+  a->Ju = 4;
+  a->Jv = 4;
+  a->w_term = 0;
+  a->Jw = 6;
+  a->cellx = 1.0;
+  a->celly = 1.0;
+  a->precision = PURIFY_GB300_FP32;
+  a->device = 0;
+}
+
+int purify_gb300_operator_create(const purify_gb300_create_args *a, purify_gb300_operator **out) {
+  if (!a) return null_arg("args");
+  if (!out) return null_arg("out");
+  *out = nullptr;
+  return guard([&] {
+    pg::OperatorConfig c;
+    c.u = a->u;
+    c.v = a->v;
+    c.w = a->w;
+    c.weights = a->weights;
+    c.M = a->M;
+    c.imsizey = int(a->imsizey);
+    c.imsizex = int(a->imsizex);
+    c.oversample_ratio = a->oversample_ratio;
+    c.power_iters = int(a->power_iters);
+    c.power_tol = a->power_tol;
+    c.kernel = a->kernel;
+    c.Ju = int(a->Ju);
+    c.Jv = int(a->Jv);
+    c.w_term = a->w_term != 0;
+    c.Jw = int(a->Jw);
+    c.cellx = a->cellx;
+    c.celly = a->celly;
+    c.fp64 = a->precision == PURIFY_GB300_FP64;
+    c.device = a->device;
+    if (a->precision != PURIFY_GB300_FP32 && a->precision != PURIFY_GB300_FP64)
+      throw pg::Error(pg::kInvalidArgument, "unknown precision");
+    auto *h = new purify_gb300_operator();
+    try {
+      h->impl = pg::Operator::create(c);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+int purify_gb300_operator_destroy(purify_gb300_operator *op) {
+  return guard([&] { delete op; });
+}
+
+int purify_gb300_forward(purify_gb300_operator *op, const void *x, void *y, void *stream) {
+  if (!op) return null_arg("operator");
+  return guard([&] {
+    const pg::OperatorInfo i = op->impl->info();
+    if ((!x && i.imsizex * int64_t(i.imsizey) > 0) || (!y && i.M > 0))
+      throw pg::Error(pg::kInvalidArgument, "null buffer");
+    op->impl->forward(x, y, static_cast<cudaStream_t>(stream));
+  });
+}
+int purify_gb300_adjoint(purify_gb300_operator *op, const void *y, void *x, void *stream) {
+  if (!op) return null_arg("operator");
+  return guard([&] {
+    const pg::OperatorInfo i = op->impl->info();
+    if ((!x && i.imsizex * int64_t(i.imsizey) > 0) || (!y && i.M > 0))
+      throw pg::Error(pg::kInvalidArgument, "null buffer");
+    op->impl->adjoint(y, x, static_cast<cudaStream_t>(stream));
+  });
+}
+int purify_gb300_degrid(purify_gb300_operator *op, const void *grid, void *vis, void *stream) {
+  if (!op) return null_arg("operator");
+  return guard([&] {
+    const pg::OperatorInfo i = op->impl->info();
+    if (!grid || (!vis && i.M > 0)) throw pg::Error(pg::kInvalidArgument, "null buffer");
+    op->impl->degrid(grid, vis, static_cast<cudaStream_t>(stream));
+  });
+}
+int purify_gb300_grid(purify_gb300_operator *op, const void *vis, void *grid, void *stream) {
+  if (!op) return null_arg("operator");
+  return guard([&] {
+    const pg::OperatorInfo i = op->impl->info();
+    if (!grid || (!vis && i.M > 0)) throw pg::Error(pg::kInvalidArgument, "null buffer");
+    op->impl->grid(vis, grid, static_cast<cudaStream_t>(stream));
+  });
+}
+int purify_gb300_correction(int32_t kernel, uint32_t Ju, uint32_t Jv, uint32_t imsizey,
+                            uint32_t imsizex, double os, double *S_out) {
+  if (!S_out) return null_arg("S_out");
+  return guard([&] {
+    const std::string why = pg::check_kernel_request(kernel, int(Ju), int(Jv));
+    if (!why.empty()) throw pg::Error(pg::kInvalidArgument, why);
+    if (imsizey == 0 || imsizex == 0 || !(os > 0))
+      throw pg::Error(pg::kInvalidArgument, "empty image or bad oversampling");
+    std::vector<double> S(size_t(imsizey) * imsizex);
+    pg::correction_factors(kernel, int(Ju), int(Jv), int(imsizey), int(imsizex), os, S.data());
+    for (size_t k = 0; k < S.size(); ++k) {
+      S_out[2 * k] = S[k];
+      S_out[2 * k + 1] = 0.0;
+    }
+  });
+}
+int purify_gb300_stage_timing(purify_gb300_operator *op, int enable) {
+  if (!op) return null_arg("operator");
+  return guard([&] { op->impl->set_stage_timing(enable != 0); });
+}
+int purify_gb300_stage_times(purify_gb300_operator *op, double *total_ms, int64_t *launches) {
+  if (!op) return null_arg("operator");
+  return guard([&] { op->impl->stage_times(total_ms, launches); });
+}
+int purify_gb300_forward_host(purify_gb300_operator *op, const double *x, double *y) {
+  if (!op) return null_arg("operator");
+  return guard([&] { op->impl->forward_host(x, y); });
+}
+int purify_gb300_adjoint_host(purify_gb300_operator *op, const double *y, double *x) {
+  if (!op) return null_arg("operator");
+  return guard([&] { op->impl->adjoint_host(y, x); });
+}
+int purify_gb300_power_method(purify_gb300_operator *op, uint32_t iters, double tol,
+                              double *norm_out) {
+  if (!op) return null_arg("operator");
+  return guard([&] {
+    const double n = op->impl->power_method(int(iters), tol);
+    if (norm_out) *norm_out = n;
+  });
+}
+int purify_gb300_set_norm(purify_gb300_operator *op, double norm) {
+  if (!op) return null_arg("operator");
+  return guard([&] { op->impl->set_norm(norm); });
+}
+int purify_gb300_get_norm(const purify_gb300_operator *op, double *norm) {
+  if (!op) return null_arg("operator");
+  if (!norm) return null_arg("norm");
+  return guard([&] { *norm = op->impl->norm(); });
+}
+int purify_gb300_operator_info(const purify_gb300_operator *op, purify_gb300_info *info) {
+  if (!op) return null_arg("operator");
+  if (!info) return null_arg("info");
+  return guard([&] {
+    const pg::OperatorInfo i = op->impl->info();
+    info->M = i.M;
+    info->imsizey = uint32_t(i.imsizey);
+    info->imsizex = uint32_t(i.imsizex);
+    info->ftsizev = uint32_t(i.ftsizev);
+    info->ftsizeu = uint32_t(i.ftsizeu);
+    info->Ju = uint32_t(i.Ju);
+    info->Jv = uint32_t(i.Jv);
+    info->precision = i.fp64 ? PURIFY_GB300_FP64 : PURIFY_GB300_FP32;
+    info->kernel = i.kernel;
+    info->w_term = i.w_term ? 1 : 0;
+    info->nnz = i.nnz;
+    info->occupied_cells = i.occupied_cells;
+    info->work_items = i.work_items;
+    info->tasks = i.tasks;
+    info->device_bytes = i.device_bytes;
+    info->kernel_fit_error = i.kernel_fit_error;
+    info->norm = i.norm;
+  });
+}
+
+// utilities::set_cell_size (utilities.cc:208-256) then uv_scale
+// (utilities.cc:258-278) for coordinates given in wavelengths.
+int purify_gb300_lambda_to_pixels(const double *u, const double *v, int64_t M, double cellx,
+                                  double celly, uint32_t ftsizeu, uint32_t ftsizev,
+                                  double *u_out, double *v_out) {
+  if (M > 0 && (!u || !v || !u_out || !v_out)) return null_arg("coordinate buffer");
+  return guard([&] {
+    constexpr double pi = 3.14159265358979323846;
+    double mu = 0, mv = 0;
+    for (int64_t m = 0; m < M; ++m) {
+      mu = std::max(mu, u[m] * u[m]);
+      mv = std::max(mv, v[m] * v[m]);
+    }
+    double cu = cellx, cv = celly;
+    if (cu == 0 && cv == 0) {
+      cu = (180 * 3600) / std::sqrt(mu) / pi / 3;
+      cv = (180 * 3600) / std::sqrt(mv) / pi / 3;
+    }
+    if (cv == 0) cv = cu;
+    const double su = 180 * 3600 / cu / pi, sv = 180 * 3600 / cv / pi;
+    for (int64_t m = 0; m < M; ++m) {
+      const double ur = u[m] / su * 2 * pi, vr = v[m] / sv * 2 * pi;
+      u_out[m] = ur / (2 * pi) * ftsizeu;
+      v_out[m] = vr / (2 * pi) * ftsizev;
+    }
+  });
+}
+
+int purify_gb300_plan_create(const double *u, const double *v, const double *weights, int64_t M,
+                             uint32_t ftsizeu, uint32_t ftsizev, uint32_t J,
+                             purify_gb300_plan **out) {
+  if (!out) return null_arg("out");
+  *out = nullptr;
+  return guard([&] {
+    pg::PlanRequest rq;
+    rq.u = u;
+    rq.v = v;
+    rq.weights = reinterpret_cast<const std::complex<double> *>(weights);
+    rq.M = M;
+    rq.Nu = int(ftsizeu);
+    rq.Nv = int(ftsizev);
+    rq.Ju = rq.Jv = int(J);
+    auto *p = new purify_gb300_plan();
+    try {
+      p->plan = pg::build_plan(rq);
+    } catch (const std::invalid_argument &e) {
+      delete p;
+      throw pg::Error(pg::kInvalidArgument, e.what());
+    }
+    *out = p;
+  });
+}
+
+int purify_gb300_plan_sizes(const purify_gb300_plan *p, int64_t *sizes) {
+  if (!p || !sizes) return null_arg("plan or sizes");
+  const pg::Plan &P = p->plan;
+  sizes[0] = P.M;
+  sizes[1] = int64_t(P.item_first.size());
+  sizes[2] = int64_t(P.tasks.size());
+  sizes[3] = P.tu.n;
+  sizes[4] = P.tv.n;
+  sizes[5] = P.win_rows;
+  sizes[6] = P.win_cols;
+  return PURIFY_GB300_OK;
+}
+
+int purify_gb300_plan_export(const purify_gb300_plan *p, double *frac, double *weight,
+                             int32_t *perm, int32_t *item_first, int32_t *item_code,
+                             int32_t *tasks, int32_t *tile_tasks, int32_t *tu_start,
+                             int32_t *tv_start) {
+  if (!p) return null_arg("plan");
+  const pg::Plan &P = p->plan;
+  for (int64_t i = 0; i < P.M; ++i) {
+    if (frac) {
+      frac[2 * i] = P.frac_u[i];
+      frac[2 * i + 1] = P.frac_v[i];
+    }
+    if (weight) {
+      weight[2 * i] = P.weight[i].real();
+      weight[2 * i + 1] = P.weight[i].imag();
+    }
+    if (perm) perm[i] = P.perm[i];
+  }
+  for (size_t k = 0; k < P.item_first.size(); ++k) {
+    if (item_first) item_first[k] = P.item_first[k];
+    if (item_code) item_code[k] = P.item_code[k];
+  }
+  if (tasks)
+    for (size_t k = 0; k < P.tasks.size(); ++k) {
+      const pg::Task &t = P.tasks[k];
+      const int32_t row[8] = {t.P, t.Q, t.H, t.W, t.batch_begin, t.batch_end, t.tile, 0};
+      std::memcpy(tasks + 8 * k, row, sizeof(row));
+    }
+  if (tile_tasks) std::copy(P.tile_tasks.begin(), P.tile_tasks.end(), tile_tasks);
+  if (tu_start) std::copy(P.tu.start.begin(), P.tu.start.end(), tu_start);
+  if (tv_start) std::copy(P.tv.start.begin(), P.tv.start.end(), tv_start);
+  return PURIFY_GB300_OK;
+}
+
+int purify_gb300_plan_destroy(purify_gb300_plan *p) {
+  delete p;
+  return PURIFY_GB300_OK;
+}
+
+int purify_gb300_kernel_taps(int32_t kernel, uint32_t J, double os, int32_t precision,
+                             const double *t, int64_t n, double *out, double *fit_error) {
+  return guard([&] {
+    const std::string why = pg::check_kernel_request(kernel, int(J), int(J));
+    if (!why.empty()) throw pg::Error(pg::kInvalidArgument, why);
+    if (J < 1 || J > pg::kMaxJ) throw pg::Error(pg::kUnsupported, "support out of range");
+    const bool f64 = precision == PURIFY_GB300_FP64;
+    const int nc = f64 ? pg::kCoefF64 : pg::kCoefF32;
+    const pg::GriddingKernel k(kernel, int(J), os);
+    const pg::AxisFit fit = pg::fit_axis(k, int(J), nc);
+    if (fit_error) *fit_error = fit.max_error;
+    for (int64_t q = 0; q < n; ++q) {
+      for (uint32_t j = 0; j < J; ++j) {
+        int s = 0;
+        double x;
+        if (fit.nsub > 1) {
+          const double ts = f64 ? t[q] * fit.nsub : double(float(t[q]) * float(fit.nsub));
+          s = std::min(int(ts), fit.nsub - 1);
+          x = f64 ? 2 * (ts - s) - 1 : double(2.0f * (float(ts) - float(s)) - 1.0f);
+        } else {
+          x = f64 ? 2 * t[q] - 1 : double(2.0f * float(t[q]) - 1.0f);
+        }
+        const double *c = &fit.coef[(size_t(j) * fit.nsub + s) * nc];
+        if (f64) {
+          double acc = c[nc - 1];
+          for (int k2 = nc - 2; k2 >= 0; --k2) acc = std::fma(acc, x, c[k2]);
+          out[q * J + j] = acc;
+        } else {
+          float acc = float(c[nc - 1]);
+          const float xf = float(x);
+          for (int k2 = nc - 2; k2 >= 0; --k2) acc = std::fma(acc, xf, float(c[k2]));
+          out[q * J + j] = acc;
+        }
+      }
+    }
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,480 @@
+// sm_103a kernels of the measurement operator Phi = G F Z S and its adjoint.
+//
+// The FFT F is cuFFT; every other stage is here:
+//   pad_kernel     Z S     image -> zero-padded grid, correction and scale fused
+//   degrid_kernel  G       grid window staged in shared memory, one lane per
+//                          work item (a base cell and up to K visibilities)
+//   grid_kernel    G^H     lanes accumulate a J x J block per work item in
+//                          registers and flush it into a warp-private window
+//                          in a fixed order; warp windows are summed in order
+//   fold_kernel            fixed-order sum of the task windows covering a cell
+//   crop_kernel    S^H Z^H grid -> image, correction and scale fused
+// No float atomics are used anywhere, so every result is bit-reproducible for
+// a given plan and launch shape.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "device_kernels.h"
+
+namespace pg {
+namespace {
+
+template <typename real>
+struct Cplx;
+template <>
+struct Cplx<float> {
+  using type = float2;
+};
+template <>
+struct Cplx<double> {
+  using type = double2;
+};
+template <typename real>
+using cplx = typename Cplx<real>::type;
+
+// Tap weights of one axis by Horner's rule.  With SUB = false every lane
+// reads the same coefficient at the same time, so the coefficients come
+// straight from the constant bank of the kernel parameters.
+template <typename real, int J, bool SUB, int NC>
+__device__ __forceinline__ void tap_weights(const PolyAxis<real, NC> &P, int nsub, real t,
+                                            real (&k)[J]) {
+  int s = 0;
+  real x;
+  if (SUB) {
+    const real ts = t * real(nsub);
+    s = min(int(ts), nsub - 1);
+    x = real(2) * (ts - real(s)) - real(1);
+  } else {
+    x = real(2) * t - real(1);
+  }
+#pragma unroll
+  for (int j = 0; j < J; ++j) {
+    real acc = P.c[j][s][NC - 1];
+#pragma unroll
+    for (int c = NC - 2; c >= 0; --c) acc = fma(acc, x, P.c[j][s][c]);
+    k[j] = acc;
+  }
+}
+
+template <typename real, int J, bool SUB>
+__global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a,
+                                                     const __grid_constant__ PolyTable<real> poly) {
+  using C = cplx<real>;
+  constexpr int NC = PolyCount<real>::value;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *win = reinterpret_cast<C *>(smem_raw);
+  const Task tk = a.tasks[blockIdx.x];
+  const int WW = tk.W + J - 1, WH = tk.H + J - 1;
+  const C *grid = static_cast<const C *>(a.grid);
+  // Stage the (wrapped) window of the grid this tile's footprints touch.
+  for (int idx = threadIdx.x; idx < WW * WH; idx += blockDim.x) {
+    const int lp = idx / WW, lq = idx - lp * WW;
+    int p = tk.P + lp;
+    if (p >= a.Nv) p -= a.Nv;
+    int q = tk.Q + lq;
+    if (q >= a.Nu) q -= a.Nu;
+    win[idx] = grid[size_t(p) * a.Nu + q];
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const C *frac = static_cast<const C *>(a.frac);
+  const C *weight = static_cast<const C *>(a.weight);
+  C *out = static_cast<C *>(a.vis_out);
+  for (int b = tk.batch_begin + warp; b < tk.batch_end; b += nw) {
+    const int2 it = a.items[size_t(b) * kBatch + lane];
+    const int cnt = item_count(it.y);
+    if (cnt == 0) continue;
+    const int lp = item_lp(it.y), lq = item_lq(it.y);
+    C F[J][J];
+#pragma unroll
+    for (int jv = 0; jv < J; ++jv)
+#pragma unroll
+      for (int ju = 0; ju < J; ++ju) F[jv][ju] = win[(lp + jv) * WW + lq + ju];
+    for (int k = 0; k < cnt; ++k) {
+      const int i = it.x + k;
+      const C t = frac[i];
+      const C w = weight[i];
+      const int m = a.perm ? a.perm[i] : i;
+      real ku[J], kv[J];
+      tap_weights<real, J, SUB>(poly.u, poly.nsub_u, t.x, ku);
+      tap_weights<real, J, SUB>(poly.v, poly.nsub_v, t.y, kv);
+      real sr = 0, si = 0;
+#pragma unroll
+      for (int jv = 0; jv < J; ++jv) {
+        real rr = 0, ri = 0;
+#pragma unroll
+        for (int ju = 0; ju < J; ++ju) {
+          rr = fma(ku[ju], F[jv][ju].x, rr);
+          ri = fma(ku[ju], F[jv][ju].y, ri);
+        }
+        sr = fma(kv[jv], rr, sr);
+        si = fma(kv[jv], ri, si);
+      }
+      C y;
+      y.x = sr * w.x - si * w.y;
+      y.y = sr * w.y + si * w.x;
+      out[m] = y;
+    }
+  }
+}
+
+template <typename real, int J, bool SUB>
+__global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a,
+                                                   const __grid_constant__ PolyTable<real> poly) {
+  using C = cplx<real>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *wins = reinterpret_cast<C *>(smem_raw);
+  const Task tk = a.tasks[blockIdx.x];
+  const int WW = tk.W + J - 1, WH = tk.H + J - 1, WN = WW * WH;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int idx = threadIdx.x; idx < nw * WN; idx += blockDim.x) wins[idx] = C{0, 0};
+  __syncthreads();
+  C *mine = wins + warp * WN;
+  const C *frac = static_cast<const C *>(a.frac);
+  const C *weight = static_cast<const C *>(a.weight);
+  const C *vin = static_cast<const C *>(a.vis_in);
+  for (int b = tk.batch_begin + warp; b < tk.batch_end; b += nw) {
+    const int2 it = a.items[size_t(b) * kBatch + lane];
+    const int cnt = item_count(it.y);
+    const int lp = item_lp(it.y), lq = item_lq(it.y);
+    C acc[J][J];
+#pragma unroll
+    for (int jv = 0; jv < J; ++jv)
+#pragma unroll
+      for (int ju = 0; ju < J; ++ju) acc[jv][ju] = C{0, 0};
+    for (int k = 0; k < cnt; ++k) {
+      const int i = it.x + k;
+      const C t = frac[i];
+      const C w = weight[i];
+      const int m = a.perm ? a.perm[i] : i;
+      const C yv = vin[m];
+      // conj(weight) * y: G^H holds the conjugated entries of G.
+      const real zr = w.x * yv.x + w.y * yv.y;
+      const real zi = w.x * yv.y - w.y * yv.x;
+      real ku[J], kv[J];
+      tap_weights<real, J, SUB>(poly.u, poly.nsub_u, t.x, ku);
+      tap_weights<real, J, SUB>(poly.v, poly.nsub_v, t.y, kv);
+#pragma unroll
+      for (int jv = 0; jv < J; ++jv) {
+        const real ar = zr * kv[jv], ai = zi * kv[jv];
+#pragma unroll
+        for (int ju = 0; ju < J; ++ju) {
+          acc[jv][ju].x = fma(ar, ku[ju], acc[jv][ju].x);
+          acc[jv][ju].y = fma(ai, ku[ju], acc[jv][ju].y);
+        }
+      }
+    }
+    // Flush.  The items of one batch have distinct base cells, so at each
+    // (jv, ju) step the 32 lanes update 32 distinct cells; steps are ordered
+    // by __syncwarp, which makes the summation order a function of the plan.
+#pragma unroll
+    for (int jv = 0; jv < J; ++jv)
+#pragma unroll
+      for (int ju = 0; ju < J; ++ju) {
+        if (cnt > 0) {
+          C *cell = mine + (lp + jv) * WW + lq + ju;
+          C c = *cell;
+          c.x += acc[jv][ju].x;
+          c.y += acc[jv][ju].y;
+          *cell = c;
+        }
+        __syncwarp();
+      }
+  }
+  __syncthreads();
+  C *out = static_cast<C *>(a.tilebuf) + size_t(blockIdx.x) * a.slot_stride;
+  for (int idx = threadIdx.x; idx < WN; idx += blockDim.x) {
+    C s = wins[idx];
+    for (int w = 1; w < nw; ++w) {
+      const C o = wins[w * WN + idx];
+      s.x += o.x;
+      s.y += o.y;
+    }
+    out[idx] = s;
+  }
+}
+
+template <typename real>
+__device__ __forceinline__ void add_tile(const FoldArgs &f, int ta, int tb, int r, int c,
+                                         cplx<real> &s) {
+  const cplx<real> *buf = static_cast<const cplx<real> *>(f.tilebuf);
+  const int t = ta * f.ntu + tb;
+  const int WW = (f.tu_start[tb + 1] - f.tu_start[tb]) + f.Ju - 1;
+  for (int k = f.tile_tasks[t]; k < f.tile_tasks[t + 1]; ++k) {
+    const cplx<real> v = buf[size_t(k) * f.slot_stride + size_t(r) * WW + c];
+    s.x += v.x;
+    s.y += v.y;
+  }
+}
+
+template <typename real>
+__global__ void fold_kernel(const FoldArgs f) {
+  const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= int64_t(f.Nu) * f.Nv) return;
+  const int p = int(idx / f.Nu), q = int(idx - int64_t(p) * f.Nu);
+  const int a = f.tv_of[p], b = f.tu_of[q];
+  const int lp = p - f.tv_start[a], lq = q - f.tu_start[b];
+  cplx<real> s{0, 0};
+  add_tile<real>(f, a, b, lp, lq, s);
+  const bool up = lp < f.Jv - 1, left = lq < f.Ju - 1;
+  const int a2 = a == 0 ? f.ntv - 1 : a - 1;
+  const int b2 = b == 0 ? f.ntu - 1 : b - 1;
+  const int hp = f.tv_start[a2 + 1] - f.tv_start[a2];
+  const int wp = f.tu_start[b2 + 1] - f.tu_start[b2];
+  if (up) add_tile<real>(f, a2, b, lp + hp, lq, s);
+  if (left) add_tile<real>(f, a, b2, lp, lq + wp, s);
+  if (up && left) add_tile<real>(f, a2, b2, lp + hp, lq + wp, s);
+  static_cast<cplx<real> *>(f.grid)[idx] = s;
+}
+
+template <typename real>
+__global__ void pad_kernel(const cplx<real> *__restrict__ x, const real *__restrict__ su,
+                           const real *__restrict__ sv, cplx<real> *__restrict__ grid, int Nx,
+                           int Ny, int Nu, int x0, int y0) {
+  const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= int64_t(Nx) * Ny) return;
+  const int j = int(idx / Nx), i = int(idx - int64_t(j) * Nx);
+  const real s = su[i] * sv[j];
+  const cplx<real> v = x[idx];
+  grid[int64_t(y0 + j) * Nu + x0 + i] = cplx<real>{s * v.x, s * v.y};
+}
+
+template <typename real>
+__global__ void crop_kernel(const cplx<real> *__restrict__ grid, const real *__restrict__ su,
+                            const real *__restrict__ sv, cplx<real> *__restrict__ x, int Nx,
+                            int Ny, int Nu, int x0, int y0) {
+  const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= int64_t(Nx) * Ny) return;
+  const int j = int(idx / Nx), i = int(idx - int64_t(j) * Nx);
+  const real s = su[i] * sv[j];
+  const cplx<real> v = grid[int64_t(y0 + j) * Nu + x0 + i];
+  x[idx] = cplx<real>{s * v.x, s * v.y};
+}
+
+template <typename real>
+__global__ void from_c128_kernel(const double2 *__restrict__ src, cplx<real> *__restrict__ dst,
+                                 int64_t n) {
+  for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n;
+       k += int64_t(gridDim.x) * blockDim.x) {
+    const double2 v = src[k];
+    dst[k] = cplx<real>{real(v.x), real(v.y)};
+  }
+}
+template <typename real>
+__global__ void to_c128_kernel(const cplx<real> *__restrict__ src, double2 *__restrict__ dst,
+                               int64_t n) {
+  for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n;
+       k += int64_t(gridDim.x) * blockDim.x) {
+    const cplx<real> v = src[k];
+    dst[k] = double2{double(v.x), double(v.y)};
+  }
+}
+
+// Fixed-shape two-stage reduction: block b sums elements b*256+tid + k*stride
+// in ascending k, then a fixed tree; the second stage sums the block partials
+// in a fixed tree.  The result depends only on n.
+template <typename real>
+__global__ void sq_norm_partial(const cplx<real> *__restrict__ x, int64_t n,
+                                double *__restrict__ partial) {
+  __shared__ double red[256];
+  double s = 0;
+  for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n;
+       k += int64_t(gridDim.x) * blockDim.x) {
+    const cplx<real> v = x[k];
+    s += double(v.x) * double(v.x) + double(v.y) * double(v.y);
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+__global__ void sq_norm_final(const double *__restrict__ partial, int n, double *__restrict__ out) {
+  __shared__ double red[512];
+  red[threadIdx.x] = threadIdx.x < n ? partial[threadIdx.x] : 0.0;
+  __syncthreads();
+  for (int w = 256; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
+}
+
+template <typename real>
+__global__ void scale_kernel(cplx<real> *x, int64_t n, real s) {
+  for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n;
+       k += int64_t(gridDim.x) * blockDim.x) {
+    cplx<real> v = x[k];
+    v.x *= s;
+    v.y *= s;
+    x[k] = v;
+  }
+}
+template <typename real>
+__global__ void fill_kernel(cplx<real> *x, int64_t n, real value) {
+  for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n;
+       k += int64_t(gridDim.x) * blockDim.x)
+    x[k] = cplx<real>{value, real(0)};
+}
+
+int stream_blocks(int64_t n, int threads) {
+  const int64_t b = (n + threads - 1) / threads;
+  return int(b < 1 ? 1 : (b > 152 * 32 ? 152 * 32 : b));
+}
+
+// Dispatch on the support J (templated so the J x J block stays in registers)
+// and on whether the kernel polynomial has sub-segments (narrow kernels, PSWF).
+
+template <typename real, int J, bool SUB>
+cudaError_t launch_one(bool degrid, const ApplyArgs<real> &a, const PolyTable<real> &poly,
+                       int ntasks, size_t smem, int threads, cudaStream_t s) {
+  auto fn = degrid ? degrid_kernel<real, J, SUB> : grid_kernel<real, J, SUB>;
+  if (smem > 48 * 1024) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+  }
+  fn<<<ntasks, threads, smem, s>>>(a, poly);
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_apply(bool degrid, const ApplyArgs<real> &a, const PolyTable<real> &poly,
+                         int J, int ntasks, size_t smem, int threads, cudaStream_t s) {
+  if (ntasks == 0) return cudaSuccess;
+  const bool sub = poly.nsub_u > 1 || poly.nsub_v > 1;
+#define PG_CASE(JJ)                                                                    \
+  case JJ:                                                                             \
+    return sub ? launch_one<real, JJ, true>(degrid, a, poly, ntasks, smem, threads, s) \
+               : launch_one<real, JJ, false>(degrid, a, poly, ntasks, smem, threads, s);
+  switch (J) {
+    PG_CASE(1)
+    PG_CASE(2)
+    PG_CASE(3)
+    PG_CASE(4)
+    PG_CASE(5)
+    PG_CASE(6)
+    PG_CASE(7)
+    PG_CASE(8)
+  }
+#undef PG_CASE
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+size_t degrid_smem_bytes(int precision_bytes, int, int win_rows, int win_cols,
+                         const LaunchShape &) {
+  return size_t(win_rows) * win_cols * 2 * precision_bytes;
+}
+size_t grid_smem_bytes(int precision_bytes, int, int win_rows, int win_cols,
+                       const LaunchShape &shape) {
+  return size_t(shape.threads / 32) * win_rows * win_cols * 2 * precision_bytes;
+}
+
+template <typename real>
+cudaError_t launch_degrid(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
+                          int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
+                          cudaStream_t s) {
+  const size_t smem = degrid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape);
+  return launch_apply<real>(true, a, poly, J, ntasks, smem, shape.threads, s);
+}
+template <typename real>
+cudaError_t launch_grid(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
+                        int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
+                        cudaStream_t s) {
+  const size_t smem = grid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape);
+  return launch_apply<real>(false, a, poly, J, ntasks, smem, shape.threads, s);
+}
+
+template <typename real>
+cudaError_t launch_fold(const FoldArgs &f, cudaStream_t s) {
+  const int64_t n = int64_t(f.Nu) * f.Nv;
+  const int threads = 256;
+  fold_kernel<real><<<int((n + threads - 1) / threads), threads, 0, s>>>(f);
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_pad(const void *x, const real *su, const real *sv, void *grid, int Nx, int Ny,
+                       int Nu, int x0, int y0, cudaStream_t s) {
+  const int64_t n = int64_t(Nx) * Ny;
+  if (n == 0) return cudaSuccess;
+  pad_kernel<real><<<int((n + 255) / 256), 256, 0, s>>>(
+      static_cast<const cplx<real> *>(x), su, sv, static_cast<cplx<real> *>(grid), Nx, Ny, Nu, x0,
+      y0);
+  return cudaGetLastError();
+}
+template <typename real>
+cudaError_t launch_crop(const void *grid, const real *su, const real *sv, void *x, int Nx, int Ny,
+                        int Nu, int x0, int y0, cudaStream_t s) {
+  const int64_t n = int64_t(Nx) * Ny;
+  if (n == 0) return cudaSuccess;
+  crop_kernel<real><<<int((n + 255) / 256), 256, 0, s>>>(
+      static_cast<const cplx<real> *>(grid), su, sv, static_cast<cplx<real> *>(x), Nx, Ny, Nu,
+      x0, y0);
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_from_c128(const void *src, void *dst, int64_t n, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  from_c128_kernel<real><<<stream_blocks(n, 256), 256, 0, s>>>(
+      static_cast<const double2 *>(src), static_cast<cplx<real> *>(dst), n);
+  return cudaGetLastError();
+}
+template <typename real>
+cudaError_t launch_to_c128(const void *src, void *dst, int64_t n, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  to_c128_kernel<real><<<stream_blocks(n, 256), 256, 0, s>>>(
+      static_cast<const cplx<real> *>(src), static_cast<double2 *>(dst), n);
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_sq_norm(const void *x, int64_t n, double *partial, double *out,
+                           cudaStream_t s) {
+  sq_norm_partial<real><<<kNormBlocks, 256, 0, s>>>(static_cast<const cplx<real> *>(x), n,
+                                                     partial);
+  sq_norm_final<<<1, kNormBlocks, 0, s>>>(partial, kNormBlocks, out);
+  return cudaGetLastError();
+}
+template <typename real>
+cudaError_t launch_scale(void *x, int64_t n, double scale, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  scale_kernel<real><<<stream_blocks(n, 256), 256, 0, s>>>(static_cast<cplx<real> *>(x), n,
+                                                           real(scale));
+  return cudaGetLastError();
+}
+template <typename real>
+cudaError_t launch_fill(void *x, int64_t n, double value, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  fill_kernel<real><<<stream_blocks(n, 256), 256, 0, s>>>(static_cast<cplx<real> *>(x), n,
+                                                          real(value));
+  return cudaGetLastError();
+}
+
+#define PG_INSTANTIATE(real)                                                                    \
+  template cudaError_t launch_degrid<real>(const ApplyArgs<real> &, const PolyTable<real> &, int, \
+                                           int, int, int, const LaunchShape &, cudaStream_t);   \
+  template cudaError_t launch_grid<real>(const ApplyArgs<real> &, const PolyTable<real> &, int,   \
+                                         int, int, int, const LaunchShape &, cudaStream_t);     \
+  template cudaError_t launch_fold<real>(const FoldArgs &, cudaStream_t);                       \
+  template cudaError_t launch_pad<real>(const void *, const real *, const real *, void *, int,  \
+                                        int, int, int, int, cudaStream_t);                      \
+  template cudaError_t launch_crop<real>(const void *, const real *, const real *, void *, int, \
+                                         int, int, int, int, cudaStream_t);                     \
+  template cudaError_t launch_from_c128<real>(const void *, void *, int64_t, cudaStream_t);     \
+  template cudaError_t launch_to_c128<real>(const void *, void *, int64_t, cudaStream_t);       \
+  template cudaError_t launch_sq_norm<real>(const void *, int64_t, double *, double *,          \
+                                            cudaStream_t);                                      \
+  template cudaError_t launch_scale<real>(void *, int64_t, double, cudaStream_t);               \
+  template cudaError_t launch_fill<real>(void *, int64_t, double, cudaStream_t);
+
+PG_INSTANTIATE(float)
+PG_INSTANTIATE(double)
+
+}  // namespace pg

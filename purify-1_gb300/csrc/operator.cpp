@@ -1,0 +1,669 @@
+#include "operator.h"
+
+#include <cufft.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "device_kernels.h"
+#include "gridding_kernels.h"
+#include "plan.h"
+
+namespace pg {
+
+void cuda_check(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return;
+  if (e == cudaErrorMemoryAllocation)
+    throw Error(kOutOfMemory, std::string(what) + ": " + cudaGetErrorString(e));
+  throw Error(kCudaError, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+namespace {
+
+void cufft_check(cufftResult r, const char *what) {
+  if (r == CUFFT_SUCCESS) return;
+  if (r == CUFFT_ALLOC_FAILED) throw Error(kOutOfMemory, std::string(what) + ": cuFFT alloc failed");
+  throw Error(kCudaError, std::string(what) + ": cuFFT error " + std::to_string(int(r)));
+}
+
+// Device allocation owned by the operator.
+class DeviceBuffer {
+ public:
+  DeviceBuffer() = default;
+  DeviceBuffer(const DeviceBuffer &) = delete;
+  DeviceBuffer &operator=(const DeviceBuffer &) = delete;
+  ~DeviceBuffer() {
+    if (p_) cudaFree(p_);
+  }
+  void alloc(size_t bytes, int64_t *counter) {
+    if (bytes == 0) bytes = 16;
+    cuda_check(cudaMalloc(&p_, bytes), "cudaMalloc");
+    bytes_ = bytes;
+    if (counter) *counter += int64_t(bytes);
+  }
+  void upload(const void *src, size_t bytes, cudaStream_t s) {
+    if (bytes) cuda_check(cudaMemcpyAsync(p_, src, bytes, cudaMemcpyHostToDevice, s), "upload");
+  }
+  template <typename T>
+  T *as() const {
+    return static_cast<T *>(p_);
+  }
+  void *get() const { return p_; }
+  size_t bytes() const { return bytes_; }
+
+ private:
+  void *p_ = nullptr;
+  size_t bytes_ = 0;
+};
+
+class DeviceGuard {
+ public:
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev_);
+    if (prev_ != dev) cuda_check(cudaSetDevice(dev), "cudaSetDevice");
+    dev_ = dev;
+  }
+  ~DeviceGuard() {
+    if (prev_ != dev_) cudaSetDevice(prev_);
+  }
+
+ private:
+  int prev_ = 0, dev_ = 0;
+};
+
+template <typename real>
+struct Traits;
+template <>
+struct Traits<float> {
+  static constexpr cufftType kType = CUFFT_C2C;
+  static cufftResult exec(cufftHandle h, void *in, void *out, int dir) {
+    return cufftExecC2C(h, static_cast<cufftComplex *>(in), static_cast<cufftComplex *>(out), dir);
+  }
+};
+template <>
+struct Traits<double> {
+  static constexpr cufftType kType = CUFFT_Z2Z;
+  static cufftResult exec(cufftHandle h, void *in, void *out, int dir) {
+    return cufftExecZ2Z(h, static_cast<cufftDoubleComplex *>(in),
+                        static_cast<cufftDoubleComplex *>(out), dir);
+  }
+};
+
+template <typename real>
+class OperatorT final : public Operator {
+ public:
+  explicit OperatorT(const OperatorConfig &cfg);
+  ~OperatorT() override;
+  void forward(const void *x, void *y, cudaStream_t stream) override;
+  void adjoint(const void *y, void *x, cudaStream_t stream) override;
+  void degrid(const void *grid, void *vis, cudaStream_t stream) override;
+  void grid(const void *vis, void *grid, cudaStream_t stream) override;
+  void forward_host(const double *x, double *y) override;
+  void adjoint_host(const double *y, double *x) override;
+  double power_method(int iters, double tol) override;
+  void set_norm(double norm) override;
+  double norm() const override { return norm_; }
+  OperatorInfo info() const override { return info_; }
+  void set_stage_timing(bool on) override;
+  void stage_times(double *total_ms, int64_t *launches) override;
+
+ private:
+  enum Stage { kPad = 0, kFftF, kDegrid, kGrid, kFold, kFftI, kCrop };
+  // Events bracketing one stage launch; recorded only while timing is on.
+  void mark_begin(int stage);
+  void mark_end(int stage);
+  void drain_timing();
+  struct Mark {
+    int stage;
+    cudaEvent_t a, b;
+  };
+  bool timing_ = false;
+  std::vector<Mark> marks_;
+  std::vector<cudaEvent_t> event_pool_;
+  size_t marks_used_ = 0;
+  double stage_ms_[kStages] = {};
+  int64_t stage_n_[kStages] = {};
+  using C = std::complex<real>;
+  void forward_on_stream(const void *x, void *y);
+  void adjoint_on_stream(const void *y, void *x);
+  void degrid_on_stream(const void *grid, void *y);
+  void grid_on_stream(const void *y, void *grid);
+  void join(cudaStream_t user);
+  void release(cudaStream_t user);
+  void upload_correction();
+  void ensure_host_staging();
+
+  OperatorInfo info_;
+  int device_ = 0;
+  int Nx_ = 0, Ny_ = 0, Nu_ = 0, Nv_ = 0, x0_ = 0, y0_ = 0, J_ = 0;
+  int64_t M_ = 0, N_ = 0;
+  double norm_ = 1.0;
+  std::vector<double> su_, sv_;  // 1 / ft kernel at the image pixels (unscaled)
+  std::vector<real> su_scaled_, sv_real_;
+  PolyTable<real> poly_{};
+  LaunchShape shape_;
+  int ntasks_ = 0, win_rows_ = 0, win_cols_ = 0, ntu_ = 0, ntv_ = 0;
+  int64_t slot_stride_ = 0;
+
+  cudaStream_t stream_ = nullptr;
+  cudaEvent_t ev_in_ = nullptr, ev_out_ = nullptr;
+  cufftHandle fft_ = 0;
+  bool fft_ok_ = false;
+  std::mutex mu_;
+
+  DeviceBuffer frac_, weight_, perm_, items_, tasks_, tile_tasks_, tu_start_, tv_start_, tu_of_,
+      tv_of_, su_d_, sv_d_, pad_, work_, tilebuf_, norm_partial_, norm_out_;
+  DeviceBuffer x128_, y128_, xc_, yc_, pm_x_, pm_y_;
+  bool staging_ = false, pm_ready_ = false;
+};
+
+template <typename real>
+OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
+  device_ = cfg.device;
+  DeviceGuard guard(device_);
+  Nx_ = cfg.imsizex;
+  Ny_ = cfg.imsizey;
+  Nu_ = int(std::floor(cfg.imsizex * cfg.oversample_ratio));
+  Nv_ = int(std::floor(cfg.imsizey * cfg.oversample_ratio));
+  x0_ = int(std::floor(Nu_ * 0.5 - Nx_ * 0.5));
+  y0_ = int(std::floor(Nv_ * 0.5 - Ny_ * 0.5));
+  J_ = cfg.Ju;
+  M_ = cfg.M;
+  N_ = int64_t(Nx_) * Ny_;
+
+  // Kernel state, FP64 fit.  The reference builds G with (kernelv, kernelu)
+  // in its (u, v) slots (operators.h:322-324); with Ju == Jv both are the same
+  // function, which is the only case accepted here.
+  GriddingKernel kern(cfg.kernel, J_, cfg.oversample_ratio);
+  const int nc = PolyCount<real>::value;
+  const AxisFit fit = fit_axis(kern, J_, nc);
+  std::memset(&poly_, 0, sizeof(poly_));
+  for (int j = 0; j < J_; ++j)
+    for (int s = 0; s < fit.nsub; ++s)
+      for (int k = 0; k < nc; ++k) {
+        const real c = real(fit.coef[(size_t(j) * fit.nsub + s) * nc + k]);
+        poly_.u.c[j][s][k] = c;
+        poly_.v.c[j][s][k] = c;
+      }
+  poly_.nsub_u = poly_.nsub_v = fit.nsub;
+
+  // Gridding correction S(j, i) = 1 / (ftv(y0 + j + 0.5) ftu(x0 + i + 0.5))
+  // (operators.cc:101-121; the w = 0 chirp times Nx Ny is 1).
+  su_.resize(Nx_);
+  sv_.resize(Ny_);
+  for (int i = 0; i < Nx_; ++i)
+    su_[i] = 1.0 / kern.correction((x0_ + i + 0.5) / Nu_ - 0.5);
+  for (int j = 0; j < Ny_; ++j)
+    sv_[j] = 1.0 / kern.correction((y0_ + j + 0.5) / Nv_ - 0.5);
+
+  // Coverage plan (FP64 coordinates, tile sort, work items).
+  PlanRequest rq;
+  rq.u = cfg.u;
+  rq.v = cfg.v;
+  rq.weights = reinterpret_cast<const std::complex<double> *>(cfg.weights);
+  rq.M = cfg.M;
+  rq.Nu = Nu_;
+  rq.Nv = Nv_;
+  rq.Ju = cfg.Ju;
+  rq.Jv = cfg.Jv;
+  rq.tile = cfg.tile > 0 ? cfg.tile : kTile;
+  rq.max_per_item = cfg.max_per_item > 0 ? cfg.max_per_item : 16;
+  Plan plan;
+  try {
+    plan = build_plan(rq);
+  } catch (const std::invalid_argument &e) {
+    throw Error(kInvalidArgument, e.what());
+  }
+  shape_.threads = cfg.threads > 0 ? cfg.threads : 128;
+  ntasks_ = int(plan.tasks.size());
+  win_rows_ = plan.win_rows;
+  win_cols_ = plan.win_cols;
+  ntu_ = plan.tu.n;
+  ntv_ = plan.tv.n;
+  slot_stride_ = int64_t(win_rows_) * win_cols_;
+
+  cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+  cuda_check(cudaEventCreateWithFlags(&ev_in_, cudaEventDisableTiming), "cudaEventCreate");
+  cuda_check(cudaEventCreateWithFlags(&ev_out_, cudaEventDisableTiming), "cudaEventCreate");
+
+  int64_t bytes = 0;
+  {
+    std::vector<C> fr(M_), wt(M_);
+    for (int64_t i = 0; i < M_; ++i) {
+      fr[i] = C(real(plan.frac_u[i]), real(plan.frac_v[i]));
+      wt[i] = C(real(plan.weight[i].real()), real(plan.weight[i].imag()));
+    }
+    frac_.alloc(sizeof(C) * M_, &bytes);
+    frac_.upload(fr.data(), sizeof(C) * M_, stream_);
+    weight_.alloc(sizeof(C) * M_, &bytes);
+    weight_.upload(wt.data(), sizeof(C) * M_, stream_);
+    perm_.alloc(sizeof(int32_t) * M_, &bytes);
+    perm_.upload(plan.perm.data(), sizeof(int32_t) * M_, stream_);
+    const size_t ni = plan.item_first.size();
+    std::vector<int2> it(ni);
+    for (size_t k = 0; k < ni; ++k) it[k] = int2{plan.item_first[k], plan.item_code[k]};
+    items_.alloc(sizeof(int2) * ni, &bytes);
+    items_.upload(it.data(), sizeof(int2) * ni, stream_);
+    tasks_.alloc(sizeof(Task) * plan.tasks.size(), &bytes);
+    tasks_.upload(plan.tasks.data(), sizeof(Task) * plan.tasks.size(), stream_);
+    tile_tasks_.alloc(sizeof(int32_t) * plan.tile_tasks.size(), &bytes);
+    tile_tasks_.upload(plan.tile_tasks.data(), sizeof(int32_t) * plan.tile_tasks.size(), stream_);
+    tu_start_.alloc(sizeof(int32_t) * plan.tu.start.size(), &bytes);
+    tu_start_.upload(plan.tu.start.data(), sizeof(int32_t) * plan.tu.start.size(), stream_);
+    tv_start_.alloc(sizeof(int32_t) * plan.tv.start.size(), &bytes);
+    tv_start_.upload(plan.tv.start.data(), sizeof(int32_t) * plan.tv.start.size(), stream_);
+    tu_of_.alloc(sizeof(int32_t) * plan.tu.of.size(), &bytes);
+    tu_of_.upload(plan.tu.of.data(), sizeof(int32_t) * plan.tu.of.size(), stream_);
+    tv_of_.alloc(sizeof(int32_t) * plan.tv.of.size(), &bytes);
+    tv_of_.upload(plan.tv.of.data(), sizeof(int32_t) * plan.tv.of.size(), stream_);
+    su_d_.alloc(sizeof(real) * Nx_, &bytes);
+    sv_d_.alloc(sizeof(real) * Ny_, &bytes);
+    const size_t gbytes = sizeof(C) * size_t(Nu_) * Nv_;
+    pad_.alloc(gbytes, &bytes);
+    cuda_check(cudaMemsetAsync(pad_.get(), 0, gbytes, stream_), "cudaMemset");
+    work_.alloc(gbytes, &bytes);
+    tilebuf_.alloc(sizeof(C) * size_t(slot_stride_) * std::max(ntasks_, 1), &bytes);
+    norm_partial_.alloc(sizeof(double) * kNormBlocks, &bytes);
+    norm_out_.alloc(sizeof(double), &bytes);
+    // The staging vectors above are pageable; wait before they go out of scope.
+    cuda_check(cudaStreamSynchronize(stream_), "upload");
+  }
+  cufft_check(cufftPlan2d(&fft_, Nv_, Nu_, Traits<real>::kType), "cufftPlan2d");
+  fft_ok_ = true;
+  cufft_check(cufftSetStream(fft_, stream_), "cufftSetStream");
+  size_t ws = 0;
+  if (cufftGetSize(fft_, &ws) == CUFFT_SUCCESS) bytes += int64_t(ws);
+
+  info_.M = M_;
+  info_.imsizey = Ny_;
+  info_.imsizex = Nx_;
+  info_.ftsizev = Nv_;
+  info_.ftsizeu = Nu_;
+  info_.Ju = cfg.Ju;
+  info_.Jv = cfg.Jv;
+  info_.fp64 = cfg.fp64;
+  info_.kernel = cfg.kernel;
+  info_.w_term = cfg.w_term;
+  info_.nnz = M_ * int64_t(cfg.Ju) * cfg.Jv;
+  info_.occupied_cells = plan.occupied_cells;
+  info_.work_items = int64_t(plan.item_first.size());
+  info_.tasks = ntasks_;
+  info_.device_bytes = bytes;
+  info_.kernel_fit_error = fit.max_error;
+
+  set_norm(1.0);
+  if (cfg.power_iters > 0) power_method(cfg.power_iters, cfg.power_tol);
+}
+
+template <typename real>
+OperatorT<real>::~OperatorT() {
+  if (stream_) cudaStreamSynchronize(stream_);
+  for (cudaEvent_t e : event_pool_) cudaEventDestroy(e);
+  if (fft_ok_) cufftDestroy(fft_);
+  if (ev_in_) cudaEventDestroy(ev_in_);
+  if (ev_out_) cudaEventDestroy(ev_out_);
+  if (stream_) cudaStreamDestroy(stream_);
+}
+
+template <typename real>
+void OperatorT<real>::upload_correction() {
+  // Phi = G F Z S / norm with a unitary F: fold 1 / (sqrt(Nu Nv) norm) into S.
+  const double c = 1.0 / (std::sqrt(double(Nu_) * double(Nv_)) * norm_);
+  su_scaled_.resize(Nx_);
+  sv_real_.resize(Ny_);
+  for (int i = 0; i < Nx_; ++i) su_scaled_[i] = real(su_[i] * c);
+  for (int j = 0; j < Ny_; ++j) sv_real_[j] = real(sv_[j]);
+  su_d_.upload(su_scaled_.data(), sizeof(real) * Nx_, stream_);
+  sv_d_.upload(sv_real_.data(), sizeof(real) * Ny_, stream_);
+  cuda_check(cudaStreamSynchronize(stream_), "correction upload");
+}
+
+template <typename real>
+void OperatorT<real>::set_norm(double norm) {
+  if (!(norm > 0)) throw Error(kNormNotPositive, "Operator norm is not greater than zero.");
+  DeviceGuard guard(device_);
+  std::lock_guard<std::mutex> lock(mu_);
+  norm_ = norm;
+  info_.norm = norm;
+  upload_correction();
+}
+
+template <typename real>
+void OperatorT<real>::join(cudaStream_t user) {
+  cuda_check(cudaEventRecord(ev_in_, user), "cudaEventRecord");
+  cuda_check(cudaStreamWaitEvent(stream_, ev_in_, 0), "cudaStreamWaitEvent");
+}
+template <typename real>
+void OperatorT<real>::release(cudaStream_t user) {
+  cuda_check(cudaEventRecord(ev_out_, stream_), "cudaEventRecord");
+  cuda_check(cudaStreamWaitEvent(user, ev_out_, 0), "cudaStreamWaitEvent");
+}
+
+template <typename real>
+void OperatorT<real>::degrid_on_stream(const void *grid, void *y) {
+  ApplyArgs<real> a;
+  a.grid = grid;
+  a.tasks = tasks_.as<Task>();
+  a.items = items_.as<int2>();
+  a.frac = frac_.get();
+  a.weight = weight_.get();
+  a.perm = perm_.as<int32_t>();
+  a.vis_out = y;
+  a.Nu = Nu_;
+  a.Nv = Nv_;
+  mark_begin(kDegrid);
+  cuda_check(launch_degrid<real>(a, poly_, J_, ntasks_, win_rows_, win_cols_, shape_, stream_),
+             "degrid");
+  mark_end(kDegrid);
+}
+
+template <typename real>
+void OperatorT<real>::grid_on_stream(const void *y, void *grid) {
+  ApplyArgs<real> a;
+  a.tilebuf = tilebuf_.get();
+  a.tasks = tasks_.as<Task>();
+  a.items = items_.as<int2>();
+  a.frac = frac_.get();
+  a.weight = weight_.get();
+  a.perm = perm_.as<int32_t>();
+  a.vis_in = y;
+  a.Nu = Nu_;
+  a.Nv = Nv_;
+  a.slot_stride = slot_stride_;
+  mark_begin(kGrid);
+  cuda_check(launch_grid<real>(a, poly_, J_, ntasks_, win_rows_, win_cols_, shape_, stream_),
+             "grid");
+  mark_end(kGrid);
+  FoldArgs f;
+  f.tilebuf = tilebuf_.get();
+  f.slot_stride = slot_stride_;
+  f.tile_tasks = tile_tasks_.as<int32_t>();
+  f.tu_start = tu_start_.as<int32_t>();
+  f.tv_start = tv_start_.as<int32_t>();
+  f.tu_of = tu_of_.as<int32_t>();
+  f.tv_of = tv_of_.as<int32_t>();
+  f.ntu = ntu_;
+  f.ntv = ntv_;
+  f.Ju = J_;
+  f.Jv = J_;
+  f.Nu = Nu_;
+  f.Nv = Nv_;
+  f.grid = grid;
+  mark_begin(kFold);
+  cuda_check(launch_fold<real>(f, stream_), "fold");
+  mark_end(kFold);
+}
+
+template <typename real>
+void OperatorT<real>::forward_on_stream(const void *x, void *y) {
+  mark_begin(kPad);
+  cuda_check(launch_pad<real>(x, su_d_.as<real>(), sv_d_.as<real>(), pad_.get(), Nx_, Ny_, Nu_,
+                              x0_, y0_, stream_),
+             "pad");
+  mark_end(kPad);
+  mark_begin(kFftF);
+  cufft_check(Traits<real>::exec(fft_, pad_.get(), work_.get(), CUFFT_FORWARD), "cufftExec");
+  mark_end(kFftF);
+  degrid_on_stream(work_.get(), y);
+}
+
+template <typename real>
+void OperatorT<real>::adjoint_on_stream(const void *y, void *x) {
+  grid_on_stream(y, work_.get());
+  mark_begin(kFftI);
+  cufft_check(Traits<real>::exec(fft_, work_.get(), work_.get(), CUFFT_INVERSE), "cufftExec");
+  mark_end(kFftI);
+  mark_begin(kCrop);
+  cuda_check(launch_crop<real>(work_.get(), su_d_.as<real>(), sv_d_.as<real>(), x, Nx_, Ny_, Nu_,
+                               x0_, y0_, stream_),
+             "crop");
+  mark_end(kCrop);
+}
+
+template <typename real>
+void OperatorT<real>::degrid(const void *grid, void *vis, cudaStream_t user) {
+  DeviceGuard guard(device_);
+  std::lock_guard<std::mutex> lock(mu_);
+  join(user);
+  degrid_on_stream(grid, vis);
+  release(user);
+}
+template <typename real>
+void OperatorT<real>::grid(const void *vis, void *grid, cudaStream_t user) {
+  DeviceGuard guard(device_);
+  std::lock_guard<std::mutex> lock(mu_);
+  join(user);
+  grid_on_stream(vis, grid);
+  release(user);
+}
+
+template <typename real>
+void OperatorT<real>::forward(const void *x, void *y, cudaStream_t user) {
+  DeviceGuard guard(device_);
+  std::lock_guard<std::mutex> lock(mu_);
+  join(user);
+  forward_on_stream(x, y);
+  release(user);
+}
+template <typename real>
+void OperatorT<real>::adjoint(const void *y, void *x, cudaStream_t user) {
+  DeviceGuard guard(device_);
+  std::lock_guard<std::mutex> lock(mu_);
+  join(user);
+  adjoint_on_stream(y, x);
+  release(user);
+}
+
+template <typename real>
+void OperatorT<real>::ensure_host_staging() {
+  if (staging_) return;
+  int64_t *cnt = &info_.device_bytes;
+  x128_.alloc(16 * size_t(N_), cnt);
+  y128_.alloc(16 * size_t(M_), cnt);
+  if (sizeof(real) != sizeof(double)) {
+    xc_.alloc(sizeof(C) * size_t(N_), cnt);
+    yc_.alloc(sizeof(C) * size_t(M_), cnt);
+  }
+  staging_ = true;
+}
+
+template <typename real>
+void OperatorT<real>::forward_host(const double *x, double *y) {
+  DeviceGuard guard(device_);
+  std::lock_guard<std::mutex> lock(mu_);
+  ensure_host_staging();
+  const bool f64 = sizeof(real) == sizeof(double);
+  cuda_check(cudaMemcpyAsync(x128_.get(), x, 16 * size_t(N_), cudaMemcpyHostToDevice, stream_),
+             "H2D");
+  void *xin = x128_.get();
+  void *yout = y128_.get();
+  if (!f64) {
+    cuda_check(launch_from_c128<real>(x128_.get(), xc_.get(), N_, stream_), "convert");
+    xin = xc_.get();
+    yout = yc_.get();
+  }
+  forward_on_stream(xin, yout);
+  if (!f64) cuda_check(launch_to_c128<real>(yc_.get(), y128_.get(), M_, stream_), "convert");
+  cuda_check(cudaMemcpyAsync(y, y128_.get(), 16 * size_t(M_), cudaMemcpyDeviceToHost, stream_),
+             "D2H");
+  cuda_check(cudaStreamSynchronize(stream_), "forward_host");
+}
+
+template <typename real>
+void OperatorT<real>::adjoint_host(const double *y, double *x) {
+  DeviceGuard guard(device_);
+  std::lock_guard<std::mutex> lock(mu_);
+  ensure_host_staging();
+  const bool f64 = sizeof(real) == sizeof(double);
+  cuda_check(cudaMemcpyAsync(y128_.get(), y, 16 * size_t(M_), cudaMemcpyHostToDevice, stream_),
+             "H2D");
+  void *yin = y128_.get();
+  void *xout = x128_.get();
+  if (!f64) {
+    cuda_check(launch_from_c128<real>(y128_.get(), yc_.get(), M_, stream_), "convert");
+    yin = yc_.get();
+    xout = xc_.get();
+  }
+  adjoint_on_stream(yin, xout);
+  if (!f64) cuda_check(launch_to_c128<real>(xc_.get(), x128_.get(), N_, stream_), "convert");
+  cuda_check(cudaMemcpyAsync(x, x128_.get(), 16 * size_t(N_), cudaMemcpyDeviceToHost, stream_),
+             "D2H");
+  cuda_check(cudaStreamSynchronize(stream_), "adjoint_host");
+}
+
+// Power iteration on Phi'^H Phi' from the normalised all-ones vector
+// (operators.h:390-391).  The eigenvalue estimate is the FP64 2-norm of the
+// iterate after each round; the iteration stops when its relative change
+// drops below tol^2, and ||Phi'|| = sqrt(estimate).  The reductions are FP64
+// and deterministic.
+template <typename real>
+double OperatorT<real>::power_method(int iters, double tol) {
+  DeviceGuard guard(device_);
+  if (iters <= 0) {
+    set_norm(1.0);
+    return 1.0;
+  }
+  double result = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu_);
+    if (!pm_ready_) {
+      int64_t *cnt = &info_.device_bytes;
+      pm_x_.alloc(sizeof(C) * size_t(N_), cnt);
+      pm_y_.alloc(sizeof(C) * size_t(M_), cnt);
+      pm_ready_ = true;
+    }
+    const double saved = norm_;
+    norm_ = 1.0;
+    upload_correction();
+    try {
+      cuda_check(launch_fill<real>(pm_x_.get(), N_, 1.0 / std::sqrt(double(N_)), stream_), "fill");
+      double old_value = 0;
+      for (int i = 0; i < iters; ++i) {
+        forward_on_stream(pm_x_.get(), pm_y_.get());
+        adjoint_on_stream(pm_y_.get(), pm_x_.get());
+        cuda_check(launch_sq_norm<real>(pm_x_.get(), N_, norm_partial_.as<double>(),
+                                        norm_out_.as<double>(), stream_),
+                   "norm");
+        double sq = 0;
+        cuda_check(cudaMemcpyAsync(&sq, norm_out_.get(), sizeof(double), cudaMemcpyDeviceToHost,
+                                   stream_),
+                   "D2H");
+        cuda_check(cudaStreamSynchronize(stream_), "power_method");
+        const double value = std::sqrt(sq);
+        if (!(value > 0)) throw Error(kNormNotPositive, "Operator norm is not greater than zero.");
+        cuda_check(launch_scale<real>(pm_x_.get(), N_, 1.0 / value, stream_), "scale");
+        if (tol * tol > std::abs(old_value - value) / old_value) {
+          old_value = value;
+          break;
+        }
+        old_value = value;
+      }
+      result = std::sqrt(old_value);
+    } catch (...) {
+      norm_ = saved;
+      upload_correction();
+      throw;
+    }
+  }
+  set_norm(result);
+  return result;
+}
+
+template <typename real>
+void OperatorT<real>::mark_begin(int stage) {
+  if (!timing_) return;
+  if (marks_used_ == marks_.size()) {
+    if (marks_.size() >= 4096) {
+      drain_timing();
+    } else {
+      Mark m{stage, nullptr, nullptr};
+      cuda_check(cudaEventCreate(&m.a), "cudaEventCreate");
+      cuda_check(cudaEventCreate(&m.b), "cudaEventCreate");
+      event_pool_.push_back(m.a);
+      event_pool_.push_back(m.b);
+      marks_.push_back(m);
+    }
+  }
+  marks_[marks_used_].stage = stage;
+  cuda_check(cudaEventRecord(marks_[marks_used_].a, stream_), "cudaEventRecord");
+}
+template <typename real>
+void OperatorT<real>::mark_end(int) {
+  if (!timing_) return;
+  cuda_check(cudaEventRecord(marks_[marks_used_].b, stream_), "cudaEventRecord");
+  ++marks_used_;
+}
+template <typename real>
+void OperatorT<real>::drain_timing() {
+  cuda_check(cudaStreamSynchronize(stream_), "timing");
+  for (size_t k = 0; k < marks_used_; ++k) {
+    float ms = 0;
+    cuda_check(cudaEventElapsedTime(&ms, marks_[k].a, marks_[k].b), "cudaEventElapsedTime");
+    stage_ms_[marks_[k].stage] += ms;
+    stage_n_[marks_[k].stage] += 1;
+  }
+  marks_used_ = 0;
+}
+template <typename real>
+void OperatorT<real>::set_stage_timing(bool on) {
+  DeviceGuard guard(device_);
+  std::lock_guard<std::mutex> lock(mu_);
+  if (on) {
+    drain_timing();
+    for (int k = 0; k < kStages; ++k) {
+      stage_ms_[k] = 0;
+      stage_n_[k] = 0;
+    }
+  }
+  timing_ = on;
+}
+template <typename real>
+void OperatorT<real>::stage_times(double *total_ms, int64_t *launches) {
+  DeviceGuard guard(device_);
+  std::lock_guard<std::mutex> lock(mu_);
+  drain_timing();
+  for (int k = 0; k < kStages; ++k) {
+    if (total_ms) total_ms[k] = stage_ms_[k];
+    if (launches) launches[k] = stage_n_[k];
+  }
+}
+
+}  // namespace
+
+void correction_factors(int kernel, int Ju, int Jv, int imsizey, int imsizex, double os,
+                        double *S) {
+  const int Nu = int(std::floor(imsizex * os)), Nv = int(std::floor(imsizey * os));
+  const int x0 = int(std::floor(Nu * 0.5 - imsizex * 0.5));
+  const int y0 = int(std::floor(Nv * 0.5 - imsizey * 0.5));
+  const GriddingKernel ku(kernel, Ju, os), kv(kernel, Jv, os);
+  std::vector<double> su(imsizex);
+  for (int i = 0; i < imsizex; ++i) su[i] = 1.0 / ku.correction((x0 + i + 0.5) / Nu - 0.5);
+  for (int j = 0; j < imsizey; ++j) {
+    const double a = 1.0 / kv.correction((y0 + j + 0.5) / Nv - 0.5);
+    for (int i = 0; i < imsizex; ++i) S[size_t(j) * imsizex + i] = a * su[i];
+  }
+}
+
+std::unique_ptr<Operator> Operator::create(const OperatorConfig &cfg) {
+  if (cfg.imsizex <= 0 || cfg.imsizey <= 0) throw Error(kInvalidArgument, "empty image");
+  if (!(cfg.oversample_ratio > 0)) throw Error(kInvalidArgument, "oversample_ratio must be > 0");
+  if (cfg.M < 0) throw Error(kInvalidArgument, "negative number of visibilities");
+  if (cfg.M > 0 && (!cfg.u || !cfg.v)) throw Error(kInvalidArgument, "u and v must be given");
+  const std::string why = check_kernel_request(cfg.kernel, cfg.Ju, cfg.Jv);
+  if (!why.empty()) throw Error(kInvalidArgument, why);
+  if (cfg.Ju != cfg.Jv)
+    throw Error(kUnsupported, "the GB300 operator requires Ju == Jv");
+  if (cfg.Ju < 1 || cfg.Ju > kMaxJ)
+    throw Error(kUnsupported, "kernel support must be between 1 and 8 taps");
+  if (cfg.w_term) throw Error(kUnsupported, "w-projection is served by the w-stack operator");
+  if (cfg.threads != 0 && (cfg.threads % 32 != 0 || cfg.threads < 32 || cfg.threads > 256))
+    throw Error(kInvalidArgument, "threads must be a multiple of 32 in [32, 256]");
+  if (cfg.fp64) return std::unique_ptr<Operator>(new OperatorT<double>(cfg));
+  return std::unique_ptr<Operator>(new OperatorT<float>(cfg));
+}
+
+}  // namespace pg

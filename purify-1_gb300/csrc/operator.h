@@ -1,0 +1,85 @@
+// Host side of the GB300 measurement operator: device state of one coverage,
+// cuFFT plan, and the apply / power-method drivers.
+#pragma once
+#include <cuda_runtime_api.h>
+
+#include <cstdint>
+#include <memory>
+#include <stdexcept>
+#include <string>
+
+#include "pg_types.h"
+
+namespace pg {
+
+class Error : public std::runtime_error {
+ public:
+  Error(Status s, const std::string &msg) : std::runtime_error(msg), status(s) {}
+  Status status;
+};
+
+// Throws pg::Error on a CUDA failure, naming the call.
+void cuda_check(cudaError_t e, const char *what);
+
+struct OperatorConfig {
+  const double *u = nullptr, *v = nullptr, *w = nullptr;
+  const double *weights = nullptr;  // interleaved complex, or null
+  int64_t M = 0;
+  int imsizey = 0, imsizex = 0;
+  double oversample_ratio = 2.0;
+  int power_iters = 100;
+  double power_tol = 1e-4;
+  int kernel = kKB;
+  int Ju = 4, Jv = 4;
+  bool w_term = false;
+  int Jw = 6;
+  double cellx = 1.0, celly = 1.0;
+  bool fp64 = false;
+  int device = 0;
+  // tuning (defaults chosen by the autotuner's table when left at 0)
+  int threads = 0;
+  int max_per_item = 0;
+  int tile = 0;
+};
+
+// S(j, i) = 1 / (ftv(y0 + j + 0.5) ftu(x0 + i + 0.5)) for the kernel, as
+// row-major imsizey x imsizex reals.
+void correction_factors(int kernel, int Ju, int Jv, int imsizey, int imsizex, double os,
+                        double *S);
+
+struct OperatorInfo {
+  int64_t M = 0;
+  int imsizey = 0, imsizex = 0, ftsizev = 0, ftsizeu = 0, Ju = 0, Jv = 0;
+  bool fp64 = false;
+  int kernel = 0;
+  bool w_term = false;
+  int64_t nnz = 0, occupied_cells = 0, work_items = 0, tasks = 0, device_bytes = 0;
+  double kernel_fit_error = 0, norm = 1;
+};
+
+class Operator {
+ public:
+  static std::unique_ptr<Operator> create(const OperatorConfig &cfg);
+  virtual ~Operator() = default;
+
+  // Device buffers of the operator's precision; ordered after `stream`.
+  virtual void forward(const void *x, void *y, cudaStream_t stream) = 0;
+  virtual void adjoint(const void *y, void *x, cudaStream_t stream) = 0;
+  // G and G^H alone (no correction, padding or FFT).
+  virtual void degrid(const void *grid, void *vis, cudaStream_t stream) = 0;
+  virtual void grid(const void *vis, void *grid, cudaStream_t stream) = 0;
+  // Host complex<double> buffers; synchronous.
+  virtual void forward_host(const double *x, double *y) = 0;
+  virtual void adjoint_host(const double *y, double *x) = 0;
+  // Sets the norm to ||Phi'|| from the power method and returns it.
+  virtual double power_method(int iters, double tol) = 0;
+  virtual void set_norm(double norm) = 0;
+  virtual double norm() const = 0;
+  virtual OperatorInfo info() const = 0;
+  // Stage timing (see purify_gb300_stage_timing).
+  static constexpr int kStages = 7;
+  virtual void set_stage_timing(bool on) = 0;
+  virtual void stage_times(double *total_ms, int64_t *launches) = 0;
+};
+
+}  // namespace pg

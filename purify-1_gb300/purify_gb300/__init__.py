@@ -1,0 +1,368 @@
+"""Python mirror of the GB300 measurement operator's C ABI.
+
+``MeasurementOperator`` takes the arguments of the reference's
+``measurementoperator::init_degrid_operator_2d`` (cpp/purify/operators.h:373-380)
+with u, v in grid pixels, and applies Phi / Phi^H through
+``libpurify_gb300.so``:
+
+* ``forward(x)`` / ``adjoint(y)`` on torch CUDA tensors of the operator's
+  complex dtype (complex64 for FP32, complex128 for FP64) run on the device
+  and return device tensors;
+* ``forward(x)`` / ``adjoint(y)`` on numpy arrays go through the host entry
+  points (complex128 in and out, copies inside the call), like the
+  reference's ``Vector<t_complex>`` closures.
+
+There is no CPU fallback: if the native library cannot be loaded every call
+raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from ._build import LIB_PATH, build  # noqa: F401
+
+KERNELS = {"kb": 0, "gauss": 1, "box": 2, "pswf": 3, "kbmin": 4, "gauss_alt": 5}
+PRECISIONS = {"fp32": 0, "fp64": 1}
+STATUS = {
+    0: "OK", 1: "INVALID_ARGUMENT", 2: "UNSUPPORTED", 3: "CUDA_ERROR", 4: "OUT_OF_MEMORY",
+    5: "NORM_NOT_POSITIVE", 6: "REJECTED", 7: "TIMEOUT", 8: "INTERNAL",
+}
+
+
+class PurifyError(RuntimeError):
+    """A non-zero status from the native library."""
+
+    def __init__(self, status, message):
+        super().__init__("%s: %s" % (STATUS.get(status, status), message))
+        self.status = status
+
+
+class CreateArgs(ctypes.Structure):
+    _fields_ = [
+        ("u", ctypes.c_void_p), ("v", ctypes.c_void_p), ("w", ctypes.c_void_p),
+        ("weights", ctypes.c_void_p), ("M", ctypes.c_int64),
+        ("imsizey", ctypes.c_uint32), ("imsizex", ctypes.c_uint32),
+        ("oversample_ratio", ctypes.c_double), ("power_iters", ctypes.c_uint32),
+        ("power_tol", ctypes.c_double), ("kernel", ctypes.c_int32),
+        ("Ju", ctypes.c_uint32), ("Jv", ctypes.c_uint32), ("w_term", ctypes.c_int32),
+        ("Jw", ctypes.c_uint32), ("cellx", ctypes.c_double), ("celly", ctypes.c_double),
+        ("precision", ctypes.c_int32), ("device", ctypes.c_int32),
+    ]
+
+
+class Info(ctypes.Structure):
+    _fields_ = [
+        ("M", ctypes.c_int64), ("imsizey", ctypes.c_uint32), ("imsizex", ctypes.c_uint32),
+        ("ftsizev", ctypes.c_uint32), ("ftsizeu", ctypes.c_uint32), ("Ju", ctypes.c_uint32),
+        ("Jv", ctypes.c_uint32), ("precision", ctypes.c_int32), ("kernel", ctypes.c_int32),
+        ("w_term", ctypes.c_int32), ("nnz", ctypes.c_int64), ("occupied_cells", ctypes.c_int64),
+        ("work_items", ctypes.c_int64), ("tasks", ctypes.c_int64),
+        ("device_bytes", ctypes.c_int64), ("kernel_fit_error", ctypes.c_double),
+        ("norm", ctypes.c_double),
+    ]
+
+
+# Every symbol include/purify_gb300.h declares (checked by the CPU tests).
+EXPORTS = [
+    "purify_gb300_default_args", "purify_gb300_operator_create", "purify_gb300_operator_destroy",
+    "purify_gb300_forward", "purify_gb300_adjoint", "purify_gb300_forward_host",
+    "purify_gb300_adjoint_host", "purify_gb300_power_method", "purify_gb300_set_norm",
+    "purify_gb300_get_norm", "purify_gb300_operator_info", "purify_gb300_lambda_to_pixels",
+    "purify_gb300_last_error", "purify_gb300_version", "purify_gb300_plan_create",
+    "purify_gb300_plan_sizes", "purify_gb300_plan_export", "purify_gb300_plan_destroy",
+    "purify_gb300_kernel_taps", "purify_gb300_degrid", "purify_gb300_grid",
+    "purify_gb300_correction", "purify_gb300_stage_timing", "purify_gb300_stage_times",
+]
+STAGES = ["pad", "fft_forward", "degrid", "grid", "fold", "fft_inverse", "crop"]
+
+_lib = None
+
+
+def load(path=None):
+    """Loads (building first if absent) and returns the ctypes library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        build()
+    L = ctypes.CDLL(path)
+    vp, P = ctypes.c_void_p, ctypes.POINTER
+    L.purify_gb300_last_error.restype = ctypes.c_char_p
+    L.purify_gb300_version.restype = ctypes.c_char_p
+    L.purify_gb300_default_args.argtypes = [P(CreateArgs)]
+    L.purify_gb300_default_args.restype = None
+    L.purify_gb300_operator_create.argtypes = [P(CreateArgs), P(vp)]
+    L.purify_gb300_operator_destroy.argtypes = [vp]
+    for f in (L.purify_gb300_forward, L.purify_gb300_adjoint):
+        f.argtypes = [vp, vp, vp, vp]
+    for f in (L.purify_gb300_forward_host, L.purify_gb300_adjoint_host):
+        f.argtypes = [vp, vp, vp]
+    L.purify_gb300_power_method.argtypes = [vp, ctypes.c_uint32, ctypes.c_double,
+                                            P(ctypes.c_double)]
+    L.purify_gb300_set_norm.argtypes = [vp, ctypes.c_double]
+    L.purify_gb300_get_norm.argtypes = [vp, P(ctypes.c_double)]
+    L.purify_gb300_operator_info.argtypes = [vp, P(Info)]
+    L.purify_gb300_lambda_to_pixels.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_double,
+                                                ctypes.c_double, ctypes.c_uint32,
+                                                ctypes.c_uint32, vp, vp]
+    L.purify_gb300_plan_create.argtypes = [vp, vp, vp, ctypes.c_int64, ctypes.c_uint32,
+                                           ctypes.c_uint32, ctypes.c_uint32, P(vp)]
+    L.purify_gb300_plan_sizes.argtypes = [vp, vp]
+    L.purify_gb300_plan_export.argtypes = [vp] + [vp] * 9
+    L.purify_gb300_plan_destroy.argtypes = [vp]
+    L.purify_gb300_kernel_taps.argtypes = [ctypes.c_int32, ctypes.c_uint32, ctypes.c_double,
+                                           ctypes.c_int32, vp, ctypes.c_int64, vp,
+                                           P(ctypes.c_double)]
+    for f in (L.purify_gb300_degrid, L.purify_gb300_grid):
+        f.argtypes = [vp, vp, vp, vp]
+    L.purify_gb300_correction.argtypes = [ctypes.c_int32, ctypes.c_uint32, ctypes.c_uint32,
+                                          ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double, vp]
+    L.purify_gb300_stage_timing.argtypes = [vp, ctypes.c_int]
+    L.purify_gb300_stage_times.argtypes = [vp, vp, vp]
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise PurifyError(rc, load().purify_gb300_last_error().decode())
+
+
+def _np_ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def lambda_to_pixels(u, v, cellx, celly, ftsizeu, ftsizev):
+    """Wavelengths -> grid pixels (utilities.cc:208-278)."""
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    uo, vo = np.empty_like(u), np.empty_like(v)
+    _check(load().purify_gb300_lambda_to_pixels(_np_ptr(u), _np_ptr(v), u.size, cellx, celly,
+                                                ftsizeu, ftsizev, _np_ptr(uo), _np_ptr(vo)))
+    return uo, vo
+
+
+def correction(kernel, Ju, Jv, imsizey, imsizex, oversample_ratio=2.0):
+    """S(j, i) of details::init_correction2d as an (imsizey, imsizex) array."""
+    out = np.empty(int(imsizey) * int(imsizex), dtype=np.complex128)
+    _check(load().purify_gb300_correction(KERNELS[kernel], int(Ju), int(Jv), int(imsizey),
+                                          int(imsizex), float(oversample_ratio), _np_ptr(out)))
+    return out.reshape(int(imsizey), int(imsizex))
+
+
+def kernel_taps(kernel, J, t, oversample_ratio=2.0, precision="fp32"):
+    """Tap weights as the device computes them: array (len(t), J) and the
+    fit's max deviation (see purify_gb300_kernel_taps)."""
+    t = np.ascontiguousarray(t, dtype=np.float64).ravel()
+    out = np.empty((t.size, int(J)), dtype=np.float64)
+    err = ctypes.c_double()
+    _check(load().purify_gb300_kernel_taps(KERNELS[kernel], int(J), float(oversample_ratio),
+                                           PRECISIONS[precision], _np_ptr(t), t.size,
+                                           _np_ptr(out), ctypes.byref(err)))
+    return out, err.value
+
+
+class CoveragePlan:
+    """Host-side copy of the coverage plan (purify_gb300_plan_*)."""
+
+    def __init__(self, u, v, ftsizeu, ftsizev, J, weights=None):
+        L = load()
+        u = np.ascontiguousarray(u, dtype=np.float64).ravel()
+        v = np.ascontiguousarray(v, dtype=np.float64).ravel()
+        wt = None if weights is None else np.ascontiguousarray(weights, dtype=np.complex128)
+        h = ctypes.c_void_p()
+        _check(L.purify_gb300_plan_create(_np_ptr(u), _np_ptr(v), _np_ptr(wt), u.size,
+                                          int(ftsizeu), int(ftsizev), int(J), ctypes.byref(h)))
+        try:
+            sz = np.zeros(7, dtype=np.int64)
+            _check(L.purify_gb300_plan_sizes(h, _np_ptr(sz)))
+            M, ni, nt, ntu, ntv, wr, wc = (int(s) for s in sz)
+            self.frac = np.empty((M, 2))
+            self.weight = np.empty(M, dtype=np.complex128)
+            self.perm = np.empty(M, dtype=np.int32)
+            self.item_first = np.empty(ni, dtype=np.int32)
+            self.item_code = np.empty(ni, dtype=np.int32)
+            self.tasks = np.empty((nt, 8), dtype=np.int32)
+            self.tile_tasks = np.empty(ntu * ntv + 1, dtype=np.int32)
+            self.tu_start = np.empty(ntu + 1, dtype=np.int32)
+            self.tv_start = np.empty(ntv + 1, dtype=np.int32)
+            _check(L.purify_gb300_plan_export(
+                h, _np_ptr(self.frac), _np_ptr(self.weight), _np_ptr(self.perm),
+                _np_ptr(self.item_first), _np_ptr(self.item_code), _np_ptr(self.tasks),
+                _np_ptr(self.tile_tasks), _np_ptr(self.tu_start), _np_ptr(self.tv_start)))
+        finally:
+            L.purify_gb300_plan_destroy(h)
+        self.M, self.ntu, self.ntv, self.win_rows, self.win_cols = M, ntu, ntv, wr, wc
+        self.Nu, self.Nv, self.J = int(ftsizeu), int(ftsizev), int(J)
+
+
+def _is_torch(x):
+    return type(x).__module__.startswith("torch")
+
+
+class MeasurementOperator:
+    """Phi = G F Z S / ||Phi'|| on one GPU (see the module docstring)."""
+
+    def __init__(self, u, v, w=None, weights=None, imsizey=256, imsizex=256,
+                 oversample_ratio=2.0, power_iters=100, power_tol=1e-4, kernel="kb", Ju=4, Jv=4,
+                 w_term=False, Jw=6, cellx=1.0, celly=1.0, precision="fp32", device=0):
+        L = load()
+        u = np.ascontiguousarray(u, dtype=np.float64).ravel()
+        v = np.ascontiguousarray(v, dtype=np.float64).ravel()
+        M = u.size
+        if v.size != M:
+            raise PurifyError(1, "Size of u and v vectors are not the same for creating gridding matrix.")
+        w = None if w is None else np.ascontiguousarray(w, dtype=np.float64).ravel()
+        wt = None if weights is None else np.ascontiguousarray(weights, dtype=np.complex128).ravel()
+        a = CreateArgs()
+        L.purify_gb300_default_args(ctypes.byref(a))
+        a.u, a.v = _np_ptr(u), _np_ptr(v)
+        a.w = _np_ptr(w)
+        a.weights = _np_ptr(wt)
+        a.M = M
+        a.imsizey, a.imsizex = int(imsizey), int(imsizex)
+        a.oversample_ratio = float(oversample_ratio)
+        a.power_iters = int(power_iters)
+        a.power_tol = float(power_tol)
+        a.kernel = KERNELS[kernel] if isinstance(kernel, str) else int(kernel)
+        a.Ju, a.Jv = int(Ju), int(Jv)
+        a.w_term = 1 if w_term else 0
+        a.Jw = int(Jw)
+        a.cellx, a.celly = float(cellx), float(celly)
+        a.precision = PRECISIONS[precision]
+        a.device = int(device)
+        h = ctypes.c_void_p()
+        _check(L.purify_gb300_operator_create(ctypes.byref(a), ctypes.byref(h)))
+        self._h = h
+        self.precision = precision
+        self.M = M
+        self.imsizey, self.imsizex = int(imsizey), int(imsizex)
+        self.device = int(device)
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            load().purify_gb300_operator_destroy(h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def complex_dtype(self):
+        import torch
+        return torch.complex64 if self.precision == "fp32" else torch.complex128
+
+    def info(self):
+        i = Info()
+        _check(load().purify_gb300_operator_info(self._h, ctypes.byref(i)))
+        return {k: getattr(i, k) for k, _ in Info._fields_}
+
+    @property
+    def norm(self):
+        n = ctypes.c_double()
+        _check(load().purify_gb300_get_norm(self._h, ctypes.byref(n)))
+        return n.value
+
+    def set_norm(self, norm):
+        _check(load().purify_gb300_set_norm(self._h, float(norm)))
+
+    def power_method(self, iters=100, tol=1e-4):
+        n = ctypes.c_double()
+        _check(load().purify_gb300_power_method(self._h, int(iters), float(tol), ctypes.byref(n)))
+        return n.value
+
+    def stage_timing(self, enable=True):
+        """Start (clearing totals) or stop per-stage CUDA-event timing."""
+        _check(load().purify_gb300_stage_timing(self._h, 1 if enable else 0))
+
+    def stage_times(self):
+        """{stage: (total_ms, launches)} recorded since timing was enabled."""
+        ms = np.zeros(len(STAGES))
+        n = np.zeros(len(STAGES), dtype=np.int64)
+        _check(load().purify_gb300_stage_times(self._h, _np_ptr(ms), _np_ptr(n)))
+        return {s: (float(ms[k]), int(n[k])) for k, s in enumerate(STAGES)}
+
+    # -- device path -------------------------------------------------------
+    def _stream(self, stream):
+        import torch
+        if stream is None:
+            stream = torch.cuda.current_stream(self.device)
+        return ctypes.c_void_p(stream.cuda_stream)
+
+    def forward_into(self, x, y, stream=None):
+        _check(load().purify_gb300_forward(self._h, ctypes.c_void_p(x.data_ptr()),
+                                           ctypes.c_void_p(y.data_ptr()), self._stream(stream)))
+        return y
+
+    def adjoint_into(self, y, x, stream=None):
+        _check(load().purify_gb300_adjoint(self._h, ctypes.c_void_p(y.data_ptr()),
+                                           ctypes.c_void_p(x.data_ptr()), self._stream(stream)))
+        return x
+
+    def degrid_into(self, grid, vis, stream=None):
+        """G alone: grid (ftsizev*ftsizeu) -> vis (M), device tensors."""
+        _check(load().purify_gb300_degrid(self._h, ctypes.c_void_p(grid.data_ptr()),
+                                          ctypes.c_void_p(vis.data_ptr()), self._stream(stream)))
+        return vis
+
+    def grid_into(self, vis, grid, stream=None):
+        """G^H alone: vis (M) -> grid (ftsizev*ftsizeu), device tensors."""
+        _check(load().purify_gb300_grid(self._h, ctypes.c_void_p(vis.data_ptr()),
+                                        ctypes.c_void_p(grid.data_ptr()), self._stream(stream)))
+        return grid
+
+    def _check_device_tensor(self, t, n):
+        if not t.is_cuda or t.dtype != self.complex_dtype or not t.is_contiguous() or t.numel() != n:
+            raise PurifyError(1, "expected a contiguous CUDA %s tensor of %d values"
+                              % (self.complex_dtype, n))
+
+    # -- reference-facing apply -------------------------------------------
+    def forward(self, x, stream=None):
+        """Phi x.  x: imsizey*imsizex values."""
+        n = self.imsizey * self.imsizex
+        if _is_torch(x):
+            import torch
+            self._check_device_tensor(x, n)
+            y = torch.empty(self.M, dtype=self.complex_dtype, device=x.device)
+            return self.forward_into(x, y, stream)
+        x = np.ascontiguousarray(x, dtype=np.complex128).ravel()
+        if x.size != n:
+            raise PurifyError(1, "image vector has %d values, expected %d" % (x.size, n))
+        y = np.empty(self.M, dtype=np.complex128)
+        _check(load().purify_gb300_forward_host(self._h, _np_ptr(x), _np_ptr(y)))
+        return y
+
+    def adjoint(self, y, stream=None):
+        """Phi^H y.  y: M values."""
+        n = self.imsizey * self.imsizex
+        if _is_torch(y):
+            import torch
+            self._check_device_tensor(y, self.M)
+            x = torch.empty(n, dtype=self.complex_dtype, device=y.device)
+            return self.adjoint_into(y, x, stream)
+        y = np.ascontiguousarray(y, dtype=np.complex128).ravel()
+        if y.size != self.M:
+            raise PurifyError(1, "visibility vector has %d values, expected %d" % (y.size, self.M))
+        x = np.empty(n, dtype=np.complex128)
+        _check(load().purify_gb300_adjoint_host(self._h, _np_ptr(y), _np_ptr(x)))
+        return x
+
+
+def init_degrid_operator_2d(u, v, w, weights, imsizey, imsizex, oversample_ratio=2.0,
+                            power_iters=100, power_tol=1e-4, kernel="kb", Ju=4, Jv=4,
+                            w_term=False, Jw=6, cellx=1.0, celly=1.0, precision="fp32",
+                            device=0):
+    """The reference's factory signature (operators.h:373-380), u/v in pixels."""
+    return MeasurementOperator(u, v, w, weights, imsizey, imsizex, oversample_ratio, power_iters,
+                               power_tol, kernel, Ju, Jv, w_term, Jw, cellx, celly, precision,
+                               device)

@@ -1,0 +1,231 @@
+"""GPU measurement operator against the CPU FP64 oracle and the reference's
+golden vectors.  Every call goes through the C ABI (libpurify_gb300.so).
+
+Tolerances (relative L2 unless stated):
+  FP64 GPU path vs oracle        1e-10
+  FP32 GPU path vs oracle        1e-5   (the BASELINE target for FP32)
+  golden G / G^H (operators.cc)  1e-5   isApprox, as the reference test
+  golden M31 Phi x               1e-6   isApprox after max-normalisation
+  adjoint dot-product test       1e-6 (FP32), 1e-12 (FP64), relative to ||Phi x|| ||y||
+"""
+import numpy as np
+import pytest
+
+from conftest import golden, is_approx, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp32": 1e-5, "fp64": 1e-10}
+DOT_TOL = {"fp32": 1e-6, "fp64": 1e-12}
+
+
+def to_dev(torch, a, precision):
+    dt = torch.complex64 if precision == "fp32" else torch.complex128
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.complex128)).to(dtype=dt).cuda()
+
+
+def to_np(t):
+    return t.cpu().numpy().astype(np.complex128)
+
+
+def make_pair(pg, oracle_mod, u, v, n_y, n_x, kernel="kb", J=4, weights=None,
+              precision="fp32", oversample=2.0):
+    gop = pg.MeasurementOperator(u, v, None, weights, n_y, n_x, oversample, power_iters=0,
+                                 kernel=kernel, Ju=J, Jv=J, precision=precision)
+    oop = oracle_mod.Operator(u, v, None, weights, n_y, n_x, oversample, kernel=kernel, Ju=J, Jv=J)
+    return gop, oop
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_golden_gridding_matrix(pg, cuda, precision):
+    g = golden("operators")
+    op = pg.MeasurementOperator(g["u"], g["v"], None, None, 16, 16, 2.0, power_iters=0,
+                                kernel="kb", Ju=4, Jv=4, precision=precision)
+    torch = cuda
+    vis = torch.empty(10, dtype=op.complex_dtype, device="cuda")
+    op.degrid_into(to_dev(torch, g["direct_input"], precision), vis)
+    torch.cuda.synchronize()
+    assert is_approx(to_np(vis), g["expected_direct"], 1e-5)
+    grid = torch.empty(1024, dtype=op.complex_dtype, device="cuda")
+    op.grid_into(to_dev(torch, g["indirect_input"], precision), grid)
+    torch.cuda.synchronize()
+    assert is_approx(to_np(grid), g["expected_indirect"], 1e-5)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("name,J", [("kb", 4), ("pswf", 6), ("gauss", 6)])
+def test_golden_m31(pg, cuda, precision, name, J):
+    m = golden("measurement_operator")
+    x = m["m31"].astype(np.complex128)
+    op = pg.MeasurementOperator(m["v"], m["u"], None, None, 256, 256, 2.0, power_iters=1,
+                                power_tol=1e-9, kernel=name, Ju=J, Jv=J, precision=precision)
+    y = op.forward(x)  # host complex<double> entry point
+    e = m[name + "_exact"]
+    assert is_approx(y / np.abs(y).max(), e / np.abs(e).max(), 1e-6)
+
+
+@pytest.fixture(scope="module")
+def small_config():
+    from purify_gb300 import synthetic
+    return synthetic.config_small(seed=0)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_small_config_parity(pg, oracle_mod, cuda, small_config, precision):
+    """256^2 image, 512^2 grid, 1e5 visibilities, KB J=4 (the CPU-runnable case)."""
+    c = small_config
+    torch = cuda
+    rng = np.random.default_rng(1)
+    wt = np.exp(1j * rng.uniform(0, 2 * np.pi, c["u"].size)) * rng.uniform(0.5, 2, c["u"].size)
+    gop, oop = make_pair(pg, oracle_mod, c["u"], c["v"], 256, 256, "kb", 4, wt, precision)
+    y_ref = oop.forward(c["x"])
+    y = to_np(gop.forward(to_dev(torch, c["x"], precision)))
+    assert rel_l2(y, y_ref) < TOL[precision], rel_l2(y, y_ref)
+    yy = (rng.standard_normal(c["u"].size) + 1j * rng.standard_normal(c["u"].size))
+    x_ref = oop.adjoint(yy)
+    x = to_np(gop.adjoint(to_dev(torch, yy, precision)))
+    assert rel_l2(x, x_ref) < TOL[precision], rel_l2(x, x_ref)
+    # adjoint dot-product test <Phi x, y> = <x, Phi^H y>
+    lhs = np.vdot(yy, y)
+    rhs = np.vdot(x, c["x"])
+    assert abs(lhs - rhs) <= DOT_TOL[precision] * np.linalg.norm(y) * np.linalg.norm(yy)
+
+
+@pytest.mark.parametrize("kernel,J", [("kb", 1), ("kb", 2), ("kb", 3), ("kb", 5), ("kb", 6),
+                                      ("kb", 7), ("kb", 8), ("pswf", 6), ("gauss", 4),
+                                      ("gauss", 2), ("box", 3), ("kbmin", 4),
+                                      ("gauss_alt", 5)])
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_kernels_and_supports(pg, oracle_mod, cuda, kernel, J, precision):
+    torch = cuda
+    rng = np.random.default_rng(J)
+    M, n = 4000, 48
+    u = rng.normal(0, 20, M)
+    v = rng.normal(0, 20, M)
+    gop, oop = make_pair(pg, oracle_mod, u, v, n, n, kernel, J, None, precision)
+    x = rng.standard_normal(n * n) + 1j * rng.standard_normal(n * n)
+    y = to_np(gop.forward(to_dev(torch, x, precision)))
+    assert rel_l2(y, oop.forward(x)) < TOL[precision]
+    yy = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    xx = to_np(gop.adjoint(to_dev(torch, yy, precision)))
+    assert rel_l2(xx, oop.adjoint(yy)) < TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("ny,nx,os,spread", [
+    (20, 36, 2.0, 30.0),     # non-square, non power of two grid (40 x 72)
+    (33, 17, 2.0, 200.0),    # odd sizes, coordinates far outside the grid (periodic wrap)
+    (64, 64, 1.5, 20.0),     # oversampling 1.5 (grid 96^2)
+])
+def test_shapes_and_wrap(pg, oracle_mod, cuda, precision, ny, nx, os, spread):
+    torch = cuda
+    rng = np.random.default_rng(ny * nx)
+    M = 3000
+    u = rng.normal(0, spread, M)
+    v = rng.normal(0, spread, M)
+    gop, oop = make_pair(pg, oracle_mod, u, v, ny, nx, "kb", 4, None, precision, os)
+    x = rng.standard_normal(ny * nx) + 1j * rng.standard_normal(ny * nx)
+    y = to_np(gop.forward(to_dev(torch, x, precision)))
+    assert rel_l2(y, oop.forward(x)) < TOL[precision]
+    yy = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    xx = to_np(gop.adjoint(to_dev(torch, yy, precision)))
+    assert rel_l2(xx, oop.adjoint(yy)) < TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_dense_single_cell_and_single_visibility(pg, oracle_mod, cuda, precision):
+    torch = cuda
+    rng = np.random.default_rng(5)
+    for M, spread in ((5000, 0.0), (1, 3.0)):
+        u = 0.3 + spread * rng.standard_normal(M)
+        v = -0.7 + spread * rng.standard_normal(M)
+        gop, oop = make_pair(pg, oracle_mod, u, v, 32, 32, "kb", 6, None, precision)
+        x = rng.standard_normal(1024) + 1j * rng.standard_normal(1024)
+        y = to_np(gop.forward(to_dev(torch, x, precision)))
+        assert rel_l2(y, oop.forward(x)) < TOL[precision]
+        yy = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+        xx = to_np(gop.adjoint(to_dev(torch, yy, precision)))
+        assert rel_l2(xx, oop.adjoint(yy)) < TOL[precision]
+
+
+def test_empty_coverage(pg, cuda):
+    torch = cuda
+    op = pg.MeasurementOperator(np.zeros(0), np.zeros(0), None, None, 16, 16, power_iters=0)
+    x = torch.ones(256, dtype=torch.complex64, device="cuda")
+    assert op.forward(x).numel() == 0
+    xa = op.adjoint(torch.zeros(0, dtype=torch.complex64, device="cuda"))
+    torch.cuda.synchronize()
+    assert float(xa.abs().max()) == 0.0
+    with pytest.raises(pg.PurifyError) as e:
+        op.power_method(10, 1e-4)
+    assert e.value.status == 5  # operators.h:187, "Operator norm is not greater than zero."
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_power_method_matches_oracle(pg, oracle_mod, cuda, small_config, precision):
+    c = small_config
+    gop, oop = make_pair(pg, oracle_mod, c["u"][:20000], c["v"][:20000], 256, 256, "kb", 4, None,
+                         precision)
+    n_gpu = gop.power_method(100, 1e-4)
+    n_ref = oop.power_method(100, 1e-4)
+    assert abs(n_gpu - n_ref) / n_ref < (1e-5 if precision == "fp32" else 1e-10)
+    # the normalised operator has ||Phi^H Phi|| = 1 (operators.cc:147-154)
+    n2 = gop.norm
+    gop.set_norm(n2)
+    torch = cuda
+    x = to_dev(torch, np.random.default_rng(0).standard_normal(65536), precision)
+    for _ in range(60):
+        x = gop.adjoint(gop.forward(x))
+        lam = float(torch.linalg.vector_norm(x))
+        x = x / lam
+    assert abs(lam - 1.0) < 1e-3
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_determinism(pg, cuda, small_config, precision):
+    """Two applies, and two independently built operators, agree bit for bit
+    (the reference checks 1e-12 after 100 Phi^H Phi rounds, operators.cc:155-168)."""
+    torch = cuda
+    c = small_config
+    ops = [pg.MeasurementOperator(c["u"], c["v"], None, None, 256, 256, power_iters=5,
+                                  precision=precision) for _ in range(2)]
+    assert ops[0].norm == ops[1].norm
+    x0 = to_dev(torch, c["x"], precision)
+    a, b = x0.clone(), x0.clone()
+    for _ in range(20):
+        a = ops[0].adjoint(ops[0].forward(a))
+        b = ops[1].adjoint(ops[1].forward(b))
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)
+    y1 = ops[0].forward(x0)
+    y2 = ops[0].forward(x0)
+    torch.cuda.synchronize()
+    assert torch.equal(y1, y2)
+
+
+def test_host_entry_points_match_device(pg, cuda, small_config):
+    torch = cuda
+    c = small_config
+    op = pg.MeasurementOperator(c["u"], c["v"], None, None, 256, 256, power_iters=3)
+    y_host = op.forward(c["x"])
+    y_dev = to_np(op.forward(to_dev(torch, c["x"], "fp32")))
+    assert np.array_equal(y_host, y_dev)
+    x_host = op.adjoint(y_host)
+    x_dev = to_np(op.adjoint(to_dev(torch, y_host, "fp32")))
+    assert np.array_equal(x_host, x_dev)
+
+
+def test_caller_stream_ordering(pg, cuda, small_config):
+    """Applies on a side stream are ordered after prior work on that stream."""
+    torch = cuda
+    c = small_config
+    op = pg.MeasurementOperator(c["u"], c["v"], None, None, 256, 256, power_iters=0)
+    s = torch.cuda.Stream()
+    x = to_dev(torch, c["x"], "fp32")
+    ref = to_np(op.forward(x))
+    with torch.cuda.stream(s):
+        x2 = x * 2  # enqueued on s
+        y2 = torch.empty(op.M, dtype=torch.complex64, device="cuda")
+        op.forward_into(x2, y2, stream=s)
+    s.synchronize()
+    assert rel_l2(to_np(y2), 2 * ref) < 1e-6

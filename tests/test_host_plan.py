@@ -1,0 +1,134 @@
+"""Host logic of the GB300 operator on the CPU: tap-weight polynomials and the
+coverage plan.  The plan is replayed in numpy exactly as the device kernels
+consume it (windows, work items, tasks, fold order) and compared with the
+oracle's explicit CSR G and G^H (operators.cc:8-46, operators.h:123-145)."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+KERNEL_CASES = [("kb", J) for J in range(1, 9)] + [
+    ("pswf", 6), ("gauss", 4), ("gauss", 6), ("box", 3), ("kbmin", 4), ("gauss_alt", 5)]
+
+
+@pytest.mark.parametrize("kernel,J", KERNEL_CASES)
+def test_tap_polynomials_match_kernel(pg, oracle_mod, kernel, J):
+    t = np.random.default_rng(J).random(4001)
+    t[:3] = [0.0, 0.5, np.nextafter(1.0, 0.0)]
+    j = np.arange(J)
+    args = t[:, None] + J / 2.0 - 1.0 - j[None, :]
+    exact = oracle_mod.kernel_values(kernel, J, args.ravel()).reshape(args.shape)
+    exact *= np.where(j % 2 == 1, -1.0, 1.0)[None, :]
+    peak = np.abs(exact).max()
+    f64, e64 = pg.kernel_taps(kernel, J, t, precision="fp64")
+    f32, e32 = pg.kernel_taps(kernel, J, t, precision="fp32")
+    assert np.abs(f64 - exact).max() <= 1e-12 * peak, (e64, np.abs(f64 - exact).max())
+    # FP32: the fit is within 3e-8 of the kernel; Horner in FP32 adds rounding.
+    assert np.abs(f32 - exact).max() <= 3e-7 * peak, (e32, np.abs(f32 - exact).max())
+
+
+def replay_degrid(plan, taps_u, taps_v, grid):
+    """y[perm[i]] = w_i sum_jv sum_ju kv ku window[lp+jv, lq+ju], as degrid_kernel."""
+    J, Nu, Nv = plan.J, plan.Nu, plan.Nv
+    y = np.zeros(plan.M, dtype=np.complex128)
+    g = grid.reshape(Nv, Nu)
+    for (P, Q, H, W, b0, b1, tile, _) in plan.tasks:
+        for b in range(b0, b1):
+            for lane in range(32):
+                k = b * 32 + lane
+                code = int(plan.item_code[k])
+                lp, lq, cnt = code & 0xFF, (code >> 8) & 0xFF, (code >> 16) & 0xFFFF
+                assert lp < H and lq < W
+                rows = (P + lp + np.arange(J)) % Nv
+                cols = (Q + lq + np.arange(J)) % Nu
+                F = g[np.ix_(rows, cols)]
+                for i in range(plan.item_first[k], plan.item_first[k] + cnt):
+                    y[plan.perm[i]] = plan.weight[i] * (taps_v[i] @ F @ taps_u[i])
+    return y
+
+
+def replay_grid(plan, taps_u, taps_v, vis):
+    """Task windows as grid_kernel writes them, then fold_kernel's fixed-order sum."""
+    J, Nu, Nv = plan.J, plan.Nu, plan.Nv
+    windows = []
+    seen_cells = []
+    for (P, Q, H, W, b0, b1, tile, _) in plan.tasks:
+        win = np.zeros((H + J - 1, W + J - 1), dtype=np.complex128)
+        for b in range(b0, b1):
+            cells = set()
+            for lane in range(32):
+                k = b * 32 + lane
+                code = int(plan.item_code[k])
+                lp, lq, cnt = code & 0xFF, (code >> 8) & 0xFF, (code >> 16) & 0xFFFF
+                if cnt == 0:
+                    continue
+                assert (lp, lq) not in cells, "two items of one base cell in a batch"
+                cells.add((lp, lq))
+                for i in range(plan.item_first[k], plan.item_first[k] + cnt):
+                    z = np.conj(plan.weight[i]) * vis[plan.perm[i]]
+                    win[lp:lp + J, lq:lq + J] += z * np.outer(taps_v[i], taps_u[i])
+            seen_cells.append(len(cells))
+        windows.append(win)
+    ntu, ntv = plan.ntu, plan.ntv
+    grid = np.zeros((Nv, Nu), dtype=np.complex128)
+    tu, tv = plan.tu_start, plan.tv_start
+    for p in range(Nv):
+        a = np.searchsorted(tv, p, side="right") - 1
+        for q in range(Nu):
+            b = np.searchsorted(tu, q, side="right") - 1
+            lp, lq = p - tv[a], q - tu[b]
+            a2, b2 = (a - 1) % ntv, (b - 1) % ntu
+            hp, wp = tv[a2 + 1] - tv[a2], tu[b2 + 1] - tu[b2]
+            s = 0j
+            for (ta, tb, r, c, on) in ((a, b, lp, lq, True), (a2, b, lp + hp, lq, lp < J - 1),
+                                       (a, b2, lp, lq + wp, lq < J - 1),
+                                       (a2, b2, lp + hp, lq + wp, lp < J - 1 and lq < J - 1)):
+                if not on:
+                    continue
+                t = ta * ntu + tb
+                for k in range(plan.tile_tasks[t], plan.tile_tasks[t + 1]):
+                    s += windows[k][r, c]
+            grid[p, q] = s
+    return grid.ravel()
+
+
+@pytest.mark.parametrize("n,J,M,spread,seed", [
+    (16, 4, 10, 1.0, 0),     # the reference's golden operator shape
+    (24, 6, 300, 12.0, 1),   # grid 48: two uneven tiles per axis
+    (40, 3, 500, 40.0, 2),   # u, v well outside the grid: periodic wrap
+    (20, 8, 200, 3.0, 3),    # dense: many visibilities per cell, several layers
+    (18, 5, 64, 9.0, 4),     # odd support, 36-cell grid
+])
+def test_plan_replay_matches_oracle_G(pg, oracle_mod, n, J, M, spread, seed):
+    rng = np.random.default_rng(seed)
+    u = rng.normal(0, spread, M)
+    v = rng.normal(0, spread, M)
+    wt = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    Nu = Nv = 2 * n
+    plan = pg.CoveragePlan(u, v, Nu, Nv, J, weights=wt)
+    assert sorted(plan.perm.tolist()) == list(range(M))
+    taps_u, _ = pg.kernel_taps("kb", J, plan.frac[:, 0], precision="fp64")
+    taps_v, _ = pg.kernel_taps("kb", J, plan.frac[:, 1], precision="fp64")
+    op = oracle_mod.Operator(u, v, None, wt, n, n, 2.0, kernel="kb", Ju=J, Jv=J)
+    grid = rng.standard_normal(Nu * Nv) + 1j * rng.standard_normal(Nu * Nv)
+    y = replay_degrid(plan, taps_u, taps_v, grid)
+    assert rel_l2(y, op.G_forward(grid)) < 1e-12
+    vis = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    g = replay_grid(plan, taps_u, taps_v, vis)
+    assert rel_l2(g, op.G_adjoint(vis)) < 1e-12
+
+
+def test_plan_empty_and_bad_sizes(pg):
+    p = pg.CoveragePlan(np.zeros(0), np.zeros(0), 32, 32, 4)
+    assert p.M == 0 and p.item_first.size == 0
+    with pytest.raises(pg.PurifyError):
+        pg.CoveragePlan(np.zeros(3), np.zeros(3), 4, 4, 6)  # grid smaller than the support
+
+
+def test_plan_balances_dense_cells(pg):
+    # 5000 visibilities in one cell: split into items of <= 16, one per layer
+    u = np.full(5000, 0.25)
+    v = np.full(5000, -0.5)
+    p = pg.CoveragePlan(u, v, 64, 64, 4)
+    counts = (p.item_code >> 16) & 0xFFFF
+    assert counts.sum() == 5000 and counts.max() <= 16
