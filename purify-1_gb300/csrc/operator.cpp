@@ -650,7 +650,10 @@ void correction_factors(int kernel, int Ju, int Jv, int imsizey, int imsizex, do
 
 std::unique_ptr<Operator> Operator::create(const OperatorConfig &cfg) {
   if (cfg.imsizex <= 0 || cfg.imsizey <= 0) throw Error(kInvalidArgument, "empty image");
-  if (!(cfg.oversample_ratio > 0)) throw Error(kInvalidArgument, "oversample_ratio must be > 0");
+  // The zero-padding operator places the image inside the grid
+  // (operators.h:147-183), which needs a grid at least as large as the image.
+  if (!(cfg.oversample_ratio >= 1.0))
+    throw Error(kInvalidArgument, "oversample_ratio must be >= 1");
   if (cfg.M < 0) throw Error(kInvalidArgument, "negative number of visibilities");
   if (cfg.M > 0 && (!cfg.u || !cfg.v)) throw Error(kInvalidArgument, "u and v must be given");
   const std::string why = check_kernel_request(cfg.kernel, cfg.Ju, cfg.Jv);
