@@ -137,7 +137,7 @@ class ClockSampler:
         sm = [num(r[1]) for r in rows if num(r[1]) is not None]
         smax = [num(r[2]) for r in rows if num(r[2]) is not None]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for r in rows for k in range(4) if "Active" in r[5 + k]})
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k] == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
                 "samples": len(rows)}
@@ -321,7 +321,7 @@ def run_gb300(args):
     if not args.no_fp64:
         op64 = pgb.MeasurementOperator(u, v, None, None, power_iters=0, precision="fp64", **kw)
         op64.set_norm(norm)
-        x64 = xd.to(torch.complex128)
+        x64 = torch.from_numpy(x).to(dev)
         y64 = torch.empty(M, dtype=torch.complex128, device=dev)
         xo64 = torch.empty(N, dtype=torch.complex128, device=dev)
         for _ in range(max(1, args.warmup)):
@@ -339,8 +339,8 @@ def run_gb300(args):
         ms64 = e0.elapsed_time(e1) / k64
         # errors of the FP32 path against the FP64 path (same input)
         op.forward_into(xd, yd, stream)
-        op.adjoint_into(y64.to(torch.complex64), xo, stream)
         op64.forward_into(x64, y64, stream)
+        op.adjoint_into(y64.to(torch.complex64), xo, stream)
         op64.adjoint_into(y64, xo64, stream)
         torch.cuda.synchronize(dev)
         f32y, f64y = yd.cpu().numpy(), y64.cpu().numpy()
