@@ -174,6 +174,7 @@ def test_power_method_matches_oracle(pg, oracle_mod, cuda, small_config, precisi
     # changes by less than tol^2, returns 1 within tol
     torch = cuda
     tol = 1e-4
+    gop.power_method(3000, 1e-6)
     x = to_dev(torch, np.random.default_rng(0).standard_normal(65536), precision)
     x = x / torch.linalg.vector_norm(x)
     old = 0.0
