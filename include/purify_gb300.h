@@ -128,12 +128,13 @@ int purify_gb300_get_norm(const purify_gb300_operator *op, double *norm);
 
 /* Per-stage device timing with CUDA events recorded on the operator's own
  * stream around each stage (pad, FFT forward, degrid, grid, fold, FFT
- * inverse, crop).  enable != 0 starts recording and clears the totals;
- * purify_gb300_stage_times waits for the recorded work and returns the total
- * milliseconds and launch count of each stage (7 entries each).  No
+ * inverse, crop, compact, expand).  enable != 0 starts recording and clears
+ * the totals; purify_gb300_stage_times waits for the recorded work and
+ * returns the total milliseconds and launch count of each stage
+ * (PURIFY_GB300_STAGES entries each).  No
  * counterpart in the reference (its benchmarks time whole applies with
  * std::chrono, cpp/benchmarks/measurement_operator.cc:124-125). */
-#define PURIFY_GB300_STAGES 7
+#define PURIFY_GB300_STAGES 9
 int purify_gb300_stage_timing(purify_gb300_operator *op, int enable);
 int purify_gb300_stage_times(purify_gb300_operator *op, double *total_ms, int64_t *launches);
 
@@ -162,26 +163,31 @@ int purify_gb300_lambda_to_pixels(const double *u, const double *v, int64_t M, d
                                   double *u_out, double *v_out);
 
 /* ---- Host-side introspection (no GPU work) --------------------------------
- * The coverage plan the operator uploads: visibilities in plan order (tile,
- * then base cell), their FP64 fractional offsets, sign-folded weights, the
- * permutation to caller order, the 32-lane work items and the CTA tasks.
- * No counterpart in the reference (its G is an explicit CSR matrix,
- * operators.cc:8-46); exposed so host logic can be tested without a GPU. */
+ * The coverage plan the operator uploads.  Visibilities are sorted by uv tile
+ * and base cell and grouped into work items (one base cell, up to 16
+ * visibilities); 32 items with distinct base cells form a batch, and a batch
+ * owns 32 * kmax "slots" (kmax = its longest item) with lane l's k-th
+ * visibility in slot base + 32 k + l.  No counterpart in the reference (its G
+ * is an explicit CSR matrix, operators.cc:8-46); exposed so host logic can be
+ * tested without a GPU. */
 typedef struct purify_gb300_plan purify_gb300_plan;
 int purify_gb300_plan_create(const double *u, const double *v, const double *weights, int64_t M,
                              uint32_t ftsizeu, uint32_t ftsizev, uint32_t J,
                              purify_gb300_plan **out);
-/* sizes[0..6] = M, work items, tasks, tiles along u, tiles along v,
- * window rows, window columns. */
+/* sizes[0..8] = M, slots, batches, tasks, tiles along u, tiles along v,
+ * window rows, window columns, unit-weight flag. */
 int purify_gb300_plan_sizes(const purify_gb300_plan *plan, int64_t *sizes);
-/* frac: 2M doubles (t_u, t_v); weight: 2M doubles; perm: M; item_first and
- * item_code: work items; tasks: 8 int32 per task (P, Q, H, W, batch_begin,
- * batch_end, tile, 0); tile_tasks: tiles + 1; tu_start: tiles_u + 1;
- * tv_start: tiles_v + 1.  Any pointer may be NULL. */
+/* Per slot: frac (2 doubles t_u, t_v), weight (2 doubles, the weight times the
+ * phase sign (-1)^(k_u + k_v); 0 for null slots), slot_user (caller index or
+ * -1).  Per visibility: user_slot.  Per batch: batches (2 int32: first slot,
+ * kmax) and lane_code (32 int32: lp | lq << 8 | count << 16).  Per task:
+ * tasks (8 int32: P, Q, H, W, batch_begin, batch_end, tile, 0).  tile_tasks:
+ * tiles + 1; tu_start: tiles_u + 1; tv_start: tiles_v + 1.  Any pointer may
+ * be NULL. */
 int purify_gb300_plan_export(const purify_gb300_plan *plan, double *frac, double *weight,
-                             int32_t *perm, int32_t *item_first, int32_t *item_code,
-                             int32_t *tasks, int32_t *tile_tasks, int32_t *tu_start,
-                             int32_t *tv_start);
+                             int32_t *slot_user, int32_t *user_slot, int32_t *batches,
+                             int32_t *lane_code, int32_t *tasks, int32_t *tile_tasks,
+                             int32_t *tu_start, int32_t *tv_start);
 int purify_gb300_plan_destroy(purify_gb300_plan *plan);
 /* Tap weights as the device evaluates them: for each t in [0, 1) the J values
  * (-1)^j kernel(t + J/2 - 1 - j), j = 0..J-1, from the fitted polynomials

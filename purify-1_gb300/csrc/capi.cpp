@@ -276,36 +276,46 @@ int purify_gb300_plan_sizes(const purify_gb300_plan *p, int64_t *sizes) {
   if (!p || !sizes) return null_arg("plan or sizes");
   const pg::Plan &P = p->plan;
   sizes[0] = P.M;
-  sizes[1] = int64_t(P.item_first.size());
-  sizes[2] = int64_t(P.tasks.size());
-  sizes[3] = P.tu.n;
-  sizes[4] = P.tv.n;
-  sizes[5] = P.win_rows;
-  sizes[6] = P.win_cols;
+  sizes[1] = P.S;
+  sizes[2] = int64_t(P.batch_base.size());
+  sizes[3] = int64_t(P.tasks.size());
+  sizes[4] = P.tu.n;
+  sizes[5] = P.tv.n;
+  sizes[6] = P.win_rows;
+  sizes[7] = P.win_cols;
+  sizes[8] = P.unit_weights ? 1 : 0;
   return PURIFY_GB300_OK;
 }
 
 int purify_gb300_plan_export(const purify_gb300_plan *p, double *frac, double *weight,
-                             int32_t *perm, int32_t *item_first, int32_t *item_code,
-                             int32_t *tasks, int32_t *tile_tasks, int32_t *tu_start,
-                             int32_t *tv_start) {
+                             int32_t *slot_user, int32_t *user_slot, int32_t *batches,
+                             int32_t *lane_code, int32_t *tasks, int32_t *tile_tasks,
+                             int32_t *tu_start, int32_t *tv_start) {
   if (!p) return null_arg("plan");
   const pg::Plan &P = p->plan;
-  for (int64_t i = 0; i < P.M; ++i) {
+  for (int64_t s = 0; s < P.S; ++s) {
     if (frac) {
-      frac[2 * i] = P.frac_u[i];
-      frac[2 * i + 1] = P.frac_v[i];
+      frac[2 * s] = P.frac_u[s];
+      frac[2 * s + 1] = P.frac_v[s];
     }
     if (weight) {
-      weight[2 * i] = P.weight[i].real();
-      weight[2 * i + 1] = P.weight[i].imag();
+      std::complex<double> w;
+      if (P.unit_weights)
+        w = P.slot_user[s] < 0 ? 0.0 : (P.flip[s] ? -1.0 : 1.0);
+      else
+        w = P.weight[s];
+      weight[2 * s] = w.real();
+      weight[2 * s + 1] = w.imag();
     }
-    if (perm) perm[i] = P.perm[i];
+    if (slot_user) slot_user[s] = P.slot_user[s];
   }
-  for (size_t k = 0; k < P.item_first.size(); ++k) {
-    if (item_first) item_first[k] = P.item_first[k];
-    if (item_code) item_code[k] = P.item_code[k];
-  }
+  if (user_slot) std::copy(P.user_slot.begin(), P.user_slot.end(), user_slot);
+  for (size_t b = 0; b < P.batch_base.size(); ++b)
+    if (batches) {
+      batches[2 * b] = P.batch_base[b];
+      batches[2 * b + 1] = P.batch_kmax[b];
+    }
+  if (lane_code) std::copy(P.lane_code.begin(), P.lane_code.end(), lane_code);
   if (tasks)
     for (size_t k = 0; k < P.tasks.size(); ++k) {
       const pg::Task &t = P.tasks[k];

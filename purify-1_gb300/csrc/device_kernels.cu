@@ -3,12 +3,14 @@
 // The FFT F is cuFFT; every other stage is here:
 //   pad_kernel     Z S     image -> zero-padded grid, correction and scale fused
 //   degrid_kernel  G       grid window staged in shared memory, one lane per
-//                          work item (a base cell and up to K visibilities)
+//                          work item (a base cell and up to K visibilities),
+//                          visibilities in slot order (coalesced per warp)
 //   grid_kernel    G^H     lanes accumulate a J x J block per work item in
 //                          registers and flush it into a warp-private window
 //                          in a fixed order; warp windows are summed in order
 //   fold_kernel            fixed-order sum of the task windows covering a cell
 //   crop_kernel    S^H Z^H grid -> image, correction and scale fused
+//   compact/expand         caller order <-> slot order of the visibilities
 // No float atomics are used anywhere, so every result is bit-reproducible for
 // a given plan and launch shape.
 #include <cuda_runtime.h>
@@ -57,11 +59,17 @@ __device__ __forceinline__ void tap_weights(const PolyAxis<real, NC> &P, int nsu
   }
 }
 
+// Streaming loads of the coverage state: read once per apply, so they are
+// marked evict-first and leave L2 to the visibility and grid data.
+template <typename T>
+__device__ __forceinline__ T stream_load(const T *p) {
+  return __ldcs(p);
+}
+
 template <typename real, int J, bool SUB>
 __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a,
                                                      const __grid_constant__ PolyTable<real> poly) {
   using C = cplx<real>;
-  constexpr int NC = PolyCount<real>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *win = reinterpret_cast<C *>(smem_raw);
   const Task tk = a.tasks[blockIdx.x];
@@ -80,24 +88,24 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a,
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const C *frac = static_cast<const C *>(a.frac);
   const C *weight = static_cast<const C *>(a.weight);
-  C *out = static_cast<C *>(a.vis_out);
+  C *out = static_cast<C *>(a.slot_out);
+  const bool unit = weight == nullptr;
   for (int b = tk.batch_begin + warp; b < tk.batch_end; b += nw) {
-    const int2 it = a.items[size_t(b) * kBatch + lane];
-    const int cnt = item_count(it.y);
-    if (cnt == 0) continue;
-    const int lp = item_lp(it.y), lq = item_lq(it.y);
+    const int2 bt = a.batches[b];
+    const int code = a.lane_code[size_t(b) * kBatch + lane];
+    const int lp = item_lp(code), lq = item_lq(code);
     C F[J][J];
 #pragma unroll
     for (int jv = 0; jv < J; ++jv)
 #pragma unroll
       for (int ju = 0; ju < J; ++ju) F[jv][ju] = win[(lp + jv) * WW + lq + ju];
-    for (int k = 0; k < cnt; ++k) {
-      const int i = it.x + k;
-      const C t = frac[i];
-      const C w = weight[i];
-      const int m = a.perm ? a.perm[i] : i;
+    // Lanes past their item's end compute on null slots; those results are
+    // never read, so the loop has no per-lane branch.
+    for (int k = 0; k < bt.y; ++k) {
+      const size_t i = size_t(bt.x) + size_t(k) * kBatch + lane;
+      const C t = stream_load(frac + i);
       real ku[J], kv[J];
-      tap_weights<real, J, SUB>(poly.u, poly.nsub_u, t.x, ku);
+      tap_weights<real, J, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
       tap_weights<real, J, SUB>(poly.v, poly.nsub_v, t.y, kv);
       real sr = 0, si = 0;
 #pragma unroll
@@ -112,9 +120,16 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a,
         si = fma(kv[jv], ri, si);
       }
       C y;
-      y.x = sr * w.x - si * w.y;
-      y.y = sr * w.y + si * w.x;
-      out[m] = y;
+      if (unit) {
+        const real sg = copysign(real(1), t.x);
+        y.x = sg * sr;
+        y.y = sg * si;
+      } else {
+        const C w = stream_load(weight + i);
+        y.x = sr * w.x - si * w.y;
+        y.y = sr * w.y + si * w.x;
+      }
+      out[i] = y;
     }
   }
 }
@@ -133,27 +148,36 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a,
   C *mine = wins + warp * WN;
   const C *frac = static_cast<const C *>(a.frac);
   const C *weight = static_cast<const C *>(a.weight);
-  const C *vin = static_cast<const C *>(a.vis_in);
+  const C *vin = static_cast<const C *>(a.slot_in);
+  const bool unit = weight == nullptr;
   for (int b = tk.batch_begin + warp; b < tk.batch_end; b += nw) {
-    const int2 it = a.items[size_t(b) * kBatch + lane];
-    const int cnt = item_count(it.y);
-    const int lp = item_lp(it.y), lq = item_lq(it.y);
+    const int2 bt = a.batches[b];
+    const int code = a.lane_code[size_t(b) * kBatch + lane];
+    const int cnt = item_count(code);
+    const int lp = item_lp(code), lq = item_lq(code);
     C acc[J][J];
 #pragma unroll
     for (int jv = 0; jv < J; ++jv)
 #pragma unroll
       for (int ju = 0; ju < J; ++ju) acc[jv][ju] = C{0, 0};
-    for (int k = 0; k < cnt; ++k) {
-      const int i = it.x + k;
-      const C t = frac[i];
-      const C w = weight[i];
-      const int m = a.perm ? a.perm[i] : i;
-      const C yv = vin[m];
-      // conj(weight) * y: G^H holds the conjugated entries of G.
-      const real zr = w.x * yv.x + w.y * yv.y;
-      const real zi = w.x * yv.y - w.y * yv.x;
+    // Null slots hold a zero visibility, so they add nothing.
+    for (int k = 0; k < bt.y; ++k) {
+      const size_t i = size_t(bt.x) + size_t(k) * kBatch + lane;
+      const C t = stream_load(frac + i);
+      const C yv = vin[i];
+      real zr, zi;
+      if (unit) {
+        const real sg = copysign(real(1), t.x);
+        zr = sg * yv.x;
+        zi = sg * yv.y;
+      } else {
+        // conj(weight) * y: G^H holds the conjugated entries of G.
+        const C w = stream_load(weight + i);
+        zr = w.x * yv.x + w.y * yv.y;
+        zi = w.x * yv.y - w.y * yv.x;
+      }
       real ku[J], kv[J];
-      tap_weights<real, J, SUB>(poly.u, poly.nsub_u, t.x, ku);
+      tap_weights<real, J, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
       tap_weights<real, J, SUB>(poly.v, poly.nsub_v, t.y, kv);
 #pragma unroll
       for (int jv = 0; jv < J; ++jv) {
@@ -192,6 +216,25 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a,
       s.y += o.y;
     }
     out[idx] = s;
+  }
+}
+
+template <typename real>
+__global__ void compact_kernel(const cplx<real> *__restrict__ slots,
+                               const int32_t *__restrict__ user_slot,
+                               cplx<real> *__restrict__ out, int64_t M) {
+  for (int64_t m = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; m < M;
+       m += int64_t(gridDim.x) * blockDim.x)
+    __stcs(out + m, slots[__ldcs(user_slot + m)]);
+}
+template <typename real>
+__global__ void expand_kernel(const cplx<real> *__restrict__ in,
+                              const int32_t *__restrict__ slot_user,
+                              cplx<real> *__restrict__ slots, int64_t S) {
+  for (int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; s < S;
+       s += int64_t(gridDim.x) * blockDim.x) {
+    const int32_t m = __ldcs(slot_user + s);
+    slots[s] = m >= 0 ? in[m] : cplx<real>{0, 0};
   }
 }
 
@@ -420,6 +463,23 @@ cudaError_t launch_crop(const void *grid, const real *su, const real *sv, void *
 }
 
 template <typename real>
+cudaError_t launch_compact(const void *slots, const int32_t *user_slot, void *out, int64_t M,
+                           cudaStream_t s) {
+  if (M == 0) return cudaSuccess;
+  compact_kernel<real><<<stream_blocks(M, 256), 256, 0, s>>>(
+      static_cast<const cplx<real> *>(slots), user_slot, static_cast<cplx<real> *>(out), M);
+  return cudaGetLastError();
+}
+template <typename real>
+cudaError_t launch_expand(const void *in, const int32_t *slot_user, void *slots, int64_t S,
+                          cudaStream_t s) {
+  if (S == 0) return cudaSuccess;
+  expand_kernel<real><<<stream_blocks(S, 256), 256, 0, s>>>(
+      static_cast<const cplx<real> *>(in), slot_user, static_cast<cplx<real> *>(slots), S);
+  return cudaGetLastError();
+}
+
+template <typename real>
 cudaError_t launch_from_c128(const void *src, void *dst, int64_t n, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   from_c128_kernel<real><<<stream_blocks(n, 256), 256, 0, s>>>(
@@ -467,6 +527,10 @@ cudaError_t launch_fill(void *x, int64_t n, double value, cudaStream_t s) {
                                         int, int, int, int, cudaStream_t);                      \
   template cudaError_t launch_crop<real>(const void *, const real *, const real *, void *, int, \
                                          int, int, int, int, cudaStream_t);                     \
+  template cudaError_t launch_compact<real>(const void *, const int32_t *, void *, int64_t,      \
+                                           cudaStream_t);                                      \
+  template cudaError_t launch_expand<real>(const void *, const int32_t *, void *, int64_t,       \
+                                          cudaStream_t);                                       \
   template cudaError_t launch_from_c128<real>(const void *, void *, int64_t, cudaStream_t);     \
   template cudaError_t launch_to_c128<real>(const void *, void *, int64_t, cudaStream_t);       \
   template cudaError_t launch_sq_norm<real>(const void *, int64_t, double *, double *,          \

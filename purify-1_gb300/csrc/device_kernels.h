@@ -11,20 +11,21 @@
 namespace pg {
 
 // Pointers and sizes of one coverage plus the I/O buffers of one apply.
-// Complex arrays hold interleaved (re, im) pairs of `real`.
+// Complex arrays hold interleaved (re, im) pairs of `real`.  Visibility
+// vectors here are in slot order (see plan.h).
 template <typename real>
 struct ApplyArgs {
-  const void *grid = nullptr;    // degrid input: Nv x Nu complex
-  void *tilebuf = nullptr;       // grid output: one window per task
+  const void *grid = nullptr;       // degrid input: Nv x Nu complex
+  void *tilebuf = nullptr;          // grid output: one window per task
   const Task *tasks = nullptr;
-  const int2 *items = nullptr;
-  const void *frac = nullptr;    // M x (t_u, t_v)
-  const void *weight = nullptr;  // M complex
-  const int32_t *perm = nullptr; // plan order -> caller order, or null
-  void *vis_out = nullptr;       // degrid output, M complex (caller order)
-  const void *vis_in = nullptr;  // grid input, M complex (caller order)
+  const int2 *batches = nullptr;    // {first slot, kmax}
+  const int32_t *lane_code = nullptr;  // item_pack per batch lane
+  const void *frac = nullptr;       // S x (t_u, t_v); sign of t_u = phase flip if unit weights
+  const void *weight = nullptr;     // S complex weights with the flip folded in, or null
+  void *slot_out = nullptr;         // degrid output, S complex
+  const void *slot_in = nullptr;    // grid input, S complex
   int Nu = 0, Nv = 0;
-  int64_t slot_stride = 0;       // complex elements per tilebuf slot
+  int64_t slot_stride = 0;          // complex elements per tilebuf slot
 };
 
 struct LaunchShape {
@@ -71,6 +72,15 @@ cudaError_t launch_pad(const void *x, const real *su, const real *sv, void *grid
 template <typename real>
 cudaError_t launch_crop(const void *grid, const real *su, const real *sv, void *x, int Nx, int Ny,
                         int Nu, int x0, int y0, cudaStream_t s);
+
+// Caller order <-> slot order.  compact: out[m] = slots[user_slot[m]], m < M.
+// expand: slots[s] = in[slot_user[s]] (0 where slot_user[s] < 0), s < S.
+template <typename real>
+cudaError_t launch_compact(const void *slots, const int32_t *user_slot, void *out, int64_t M,
+                           cudaStream_t s);
+template <typename real>
+cudaError_t launch_expand(const void *in, const int32_t *slot_user, void *slots, int64_t S,
+                          cudaStream_t s);
 
 // complex<double> <-> complex<real> conversion of n values.
 template <typename real>

@@ -112,7 +112,7 @@ class OperatorT final : public Operator {
   void stage_times(double *total_ms, int64_t *launches) override;
 
  private:
-  enum Stage { kPad = 0, kFftF, kDegrid, kGrid, kFold, kFftI, kCrop };
+  enum Stage { kPad = 0, kFftF, kDegrid, kGrid, kFold, kFftI, kCrop, kCompact, kExpand };
   // Events bracketing one stage launch; recorded only while timing is on.
   void mark_begin(int stage);
   void mark_end(int stage);
@@ -130,8 +130,14 @@ class OperatorT final : public Operator {
   using C = std::complex<real>;
   void forward_on_stream(const void *x, void *y);
   void adjoint_on_stream(const void *y, void *x);
+  // G and G^H between the grid and the slot-ordered visibility buffer.
+  void degrid_slots(const void *grid);
+  void grid_slots(void *grid);
   void degrid_on_stream(const void *grid, void *y);
   void grid_on_stream(const void *y, void *grid);
+  // Phi' / Phi'^H with visibilities kept in slot order (power method).
+  void forward_slots(const void *x);
+  void adjoint_slots(void *x);
   void join(cudaStream_t user);
   void release(cudaStream_t user);
   void upload_correction();
@@ -140,7 +146,8 @@ class OperatorT final : public Operator {
   OperatorInfo info_;
   int device_ = 0;
   int Nx_ = 0, Ny_ = 0, Nu_ = 0, Nv_ = 0, x0_ = 0, y0_ = 0, J_ = 0;
-  int64_t M_ = 0, N_ = 0;
+  int64_t M_ = 0, N_ = 0, S_ = 0;
+  bool unit_weights_ = true;
   double norm_ = 1.0;
   std::vector<double> su_, sv_;  // 1 / ft kernel at the image pixels (unscaled)
   std::vector<real> su_scaled_, sv_real_;
@@ -155,9 +162,10 @@ class OperatorT final : public Operator {
   bool fft_ok_ = false;
   std::mutex mu_;
 
-  DeviceBuffer frac_, weight_, perm_, items_, tasks_, tile_tasks_, tu_start_, tv_start_, tu_of_,
-      tv_of_, su_d_, sv_d_, pad_, work_, tilebuf_, norm_partial_, norm_out_;
-  DeviceBuffer x128_, y128_, xc_, yc_, pm_x_, pm_y_;
+  DeviceBuffer frac_, weight_, slot_user_, user_slot_, batches_, lane_code_, tasks_, tile_tasks_,
+      tu_start_, tv_start_, tu_of_, tv_of_, su_d_, sv_d_, pad_, work_, tilebuf_, slots_,
+      norm_partial_, norm_out_;
+  DeviceBuffer x128_, y128_, xc_, yc_, pm_x_;
   bool staging_ = false, pm_ready_ = false;
 };
 
@@ -232,22 +240,35 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
 
   int64_t bytes = 0;
   {
-    std::vector<C> fr(M_), wt(M_);
-    for (int64_t i = 0; i < M_; ++i) {
-      fr[i] = C(real(plan.frac_u[i]), real(plan.frac_v[i]));
-      wt[i] = C(real(plan.weight[i].real()), real(plan.weight[i].imag()));
+    S_ = plan.S;
+    unit_weights_ = plan.unit_weights;
+    std::vector<C> fr(S_);
+    for (int64_t i = 0; i < S_; ++i) {
+      // unit weights: the phase sign (-1)^(k_u + k_v) rides in the sign of t_u
+      const double tu = (unit_weights_ && plan.flip[i]) ? -plan.frac_u[i] : plan.frac_u[i];
+      fr[i] = C(real(tu), real(plan.frac_v[i]));
     }
-    frac_.alloc(sizeof(C) * M_, &bytes);
-    frac_.upload(fr.data(), sizeof(C) * M_, stream_);
-    weight_.alloc(sizeof(C) * M_, &bytes);
-    weight_.upload(wt.data(), sizeof(C) * M_, stream_);
-    perm_.alloc(sizeof(int32_t) * M_, &bytes);
-    perm_.upload(plan.perm.data(), sizeof(int32_t) * M_, stream_);
-    const size_t ni = plan.item_first.size();
-    std::vector<int2> it(ni);
-    for (size_t k = 0; k < ni; ++k) it[k] = int2{plan.item_first[k], plan.item_code[k]};
-    items_.alloc(sizeof(int2) * ni, &bytes);
-    items_.upload(it.data(), sizeof(int2) * ni, stream_);
+    frac_.alloc(sizeof(C) * S_, &bytes);
+    frac_.upload(fr.data(), sizeof(C) * S_, stream_);
+    if (!unit_weights_) {
+      std::vector<C> wt(S_);
+      for (int64_t i = 0; i < S_; ++i)
+        wt[i] = C(real(plan.weight[i].real()), real(plan.weight[i].imag()));
+      weight_.alloc(sizeof(C) * S_, &bytes);
+      weight_.upload(wt.data(), sizeof(C) * S_, stream_);
+      cuda_check(cudaStreamSynchronize(stream_), "upload");
+    }
+    slot_user_.alloc(sizeof(int32_t) * S_, &bytes);
+    slot_user_.upload(plan.slot_user.data(), sizeof(int32_t) * S_, stream_);
+    user_slot_.alloc(sizeof(int32_t) * M_, &bytes);
+    user_slot_.upload(plan.user_slot.data(), sizeof(int32_t) * M_, stream_);
+    const size_t nb = plan.batch_base.size();
+    std::vector<int2> bt(nb);
+    for (size_t k = 0; k < nb; ++k) bt[k] = int2{plan.batch_base[k], plan.batch_kmax[k]};
+    batches_.alloc(sizeof(int2) * nb, &bytes);
+    batches_.upload(bt.data(), sizeof(int2) * nb, stream_);
+    lane_code_.alloc(sizeof(int32_t) * plan.lane_code.size(), &bytes);
+    lane_code_.upload(plan.lane_code.data(), sizeof(int32_t) * plan.lane_code.size(), stream_);
     tasks_.alloc(sizeof(Task) * plan.tasks.size(), &bytes);
     tasks_.upload(plan.tasks.data(), sizeof(Task) * plan.tasks.size(), stream_);
     tile_tasks_.alloc(sizeof(int32_t) * plan.tile_tasks.size(), &bytes);
@@ -267,6 +288,7 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
     cuda_check(cudaMemsetAsync(pad_.get(), 0, gbytes, stream_), "cudaMemset");
     work_.alloc(gbytes, &bytes);
     tilebuf_.alloc(sizeof(C) * size_t(slot_stride_) * std::max(ntasks_, 1), &bytes);
+    slots_.alloc(sizeof(C) * S_, &bytes);
     norm_partial_.alloc(sizeof(double) * kNormBlocks, &bytes);
     norm_out_.alloc(sizeof(double), &bytes);
     // The staging vectors above are pageable; wait before they go out of scope.
@@ -290,7 +312,7 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
   info_.w_term = cfg.w_term;
   info_.nnz = M_ * int64_t(cfg.Ju) * cfg.Jv;
   info_.occupied_cells = plan.occupied_cells;
-  info_.work_items = int64_t(plan.item_first.size());
+  info_.work_items = int64_t(plan.lane_code.size());
   info_.tasks = ntasks_;
   info_.device_bytes = bytes;
   info_.kernel_fit_error = fit.max_error;
@@ -344,15 +366,15 @@ void OperatorT<real>::release(cudaStream_t user) {
 }
 
 template <typename real>
-void OperatorT<real>::degrid_on_stream(const void *grid, void *y) {
+void OperatorT<real>::degrid_slots(const void *grid) {
   ApplyArgs<real> a;
   a.grid = grid;
   a.tasks = tasks_.as<Task>();
-  a.items = items_.as<int2>();
+  a.batches = batches_.as<int2>();
+  a.lane_code = lane_code_.as<int32_t>();
   a.frac = frac_.get();
-  a.weight = weight_.get();
-  a.perm = perm_.as<int32_t>();
-  a.vis_out = y;
+  a.weight = unit_weights_ ? nullptr : weight_.get();
+  a.slot_out = slots_.get();
   a.Nu = Nu_;
   a.Nv = Nv_;
   mark_begin(kDegrid);
@@ -362,15 +384,15 @@ void OperatorT<real>::degrid_on_stream(const void *grid, void *y) {
 }
 
 template <typename real>
-void OperatorT<real>::grid_on_stream(const void *y, void *grid) {
+void OperatorT<real>::grid_slots(void *grid) {
   ApplyArgs<real> a;
   a.tilebuf = tilebuf_.get();
   a.tasks = tasks_.as<Task>();
-  a.items = items_.as<int2>();
+  a.batches = batches_.as<int2>();
+  a.lane_code = lane_code_.as<int32_t>();
   a.frac = frac_.get();
-  a.weight = weight_.get();
-  a.perm = perm_.as<int32_t>();
-  a.vis_in = y;
+  a.weight = unit_weights_ ? nullptr : weight_.get();
+  a.slot_in = slots_.get();
   a.Nu = Nu_;
   a.Nv = Nv_;
   a.slot_stride = slot_stride_;
@@ -399,7 +421,25 @@ void OperatorT<real>::grid_on_stream(const void *y, void *grid) {
 }
 
 template <typename real>
-void OperatorT<real>::forward_on_stream(const void *x, void *y) {
+void OperatorT<real>::degrid_on_stream(const void *grid, void *y) {
+  degrid_slots(grid);
+  mark_begin(kCompact);
+  cuda_check(launch_compact<real>(slots_.get(), user_slot_.as<int32_t>(), y, M_, stream_),
+             "compact");
+  mark_end(kCompact);
+}
+
+template <typename real>
+void OperatorT<real>::grid_on_stream(const void *y, void *grid) {
+  mark_begin(kExpand);
+  cuda_check(launch_expand<real>(y, slot_user_.as<int32_t>(), slots_.get(), S_, stream_),
+             "expand");
+  mark_end(kExpand);
+  grid_slots(grid);
+}
+
+template <typename real>
+void OperatorT<real>::forward_slots(const void *x) {
   mark_begin(kPad);
   cuda_check(launch_pad<real>(x, su_d_.as<real>(), sv_d_.as<real>(), pad_.get(), Nx_, Ny_, Nu_,
                               x0_, y0_, stream_),
@@ -408,12 +448,12 @@ void OperatorT<real>::forward_on_stream(const void *x, void *y) {
   mark_begin(kFftF);
   cufft_check(Traits<real>::exec(fft_, pad_.get(), work_.get(), CUFFT_FORWARD), "cufftExec");
   mark_end(kFftF);
-  degrid_on_stream(work_.get(), y);
+  degrid_slots(work_.get());
 }
 
 template <typename real>
-void OperatorT<real>::adjoint_on_stream(const void *y, void *x) {
-  grid_on_stream(y, work_.get());
+void OperatorT<real>::adjoint_slots(void *x) {
+  grid_slots(work_.get());
   mark_begin(kFftI);
   cufft_check(Traits<real>::exec(fft_, work_.get(), work_.get(), CUFFT_INVERSE), "cufftExec");
   mark_end(kFftI);
@@ -422,6 +462,24 @@ void OperatorT<real>::adjoint_on_stream(const void *y, void *x) {
                                x0_, y0_, stream_),
              "crop");
   mark_end(kCrop);
+}
+
+template <typename real>
+void OperatorT<real>::forward_on_stream(const void *x, void *y) {
+  forward_slots(x);
+  mark_begin(kCompact);
+  cuda_check(launch_compact<real>(slots_.get(), user_slot_.as<int32_t>(), y, M_, stream_),
+             "compact");
+  mark_end(kCompact);
+}
+
+template <typename real>
+void OperatorT<real>::adjoint_on_stream(const void *y, void *x) {
+  mark_begin(kExpand);
+  cuda_check(launch_expand<real>(y, slot_user_.as<int32_t>(), slots_.get(), S_, stream_),
+             "expand");
+  mark_end(kExpand);
+  adjoint_slots(x);
 }
 
 template <typename real>
@@ -533,7 +591,6 @@ double OperatorT<real>::power_method(int iters, double tol) {
     if (!pm_ready_) {
       int64_t *cnt = &info_.device_bytes;
       pm_x_.alloc(sizeof(C) * size_t(N_), cnt);
-      pm_y_.alloc(sizeof(C) * size_t(M_), cnt);
       pm_ready_ = true;
     }
     const double saved = norm_;
@@ -543,8 +600,9 @@ double OperatorT<real>::power_method(int iters, double tol) {
       cuda_check(launch_fill<real>(pm_x_.get(), N_, 1.0 / std::sqrt(double(N_)), stream_), "fill");
       double old_value = 0;
       for (int i = 0; i < iters; ++i) {
-        forward_on_stream(pm_x_.get(), pm_y_.get());
-        adjoint_on_stream(pm_y_.get(), pm_x_.get());
+        // visibilities stay in slot order between the two halves
+        forward_slots(pm_x_.get());
+        adjoint_slots(pm_x_.get());
         cuda_check(launch_sq_norm<real>(pm_x_.get(), N_, norm_partial_.as<double>(),
                                         norm_out_.as<double>(), stream_),
                    "norm");

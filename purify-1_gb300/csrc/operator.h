@@ -77,7 +77,7 @@ class Operator {
   virtual double norm() const = 0;
   virtual OperatorInfo info() const = 0;
   // Stage timing (see purify_gb300_stage_timing).
-  static constexpr int kStages = 7;
+  static constexpr int kStages = 9;
   virtual void set_stage_timing(bool on) = 0;
   virtual void stage_times(double *total_ms, int64_t *launches) = 0;
 };

@@ -26,6 +26,13 @@ double wrap(double x, double y) {
   if (r < 0) r += y;
   return r;
 }
+
+struct Item {
+  int32_t first;  // first visibility in cell-sorted order
+  int32_t count;
+  int32_t cell;   // cell index inside the tile
+  int32_t lp, lq;
+};
 }  // namespace
 
 Plan build_plan(const PlanRequest &rq) {
@@ -33,10 +40,11 @@ Plan build_plan(const PlanRequest &rq) {
   if (rq.M > 0 && (!rq.u || !rq.v)) throw std::invalid_argument("u and v must be given");
   if (rq.Ju < 1 || rq.Jv < 1) throw std::invalid_argument("kernel support must be >= 1");
   if (rq.Nu < 1 || rq.Nv < 1) throw std::invalid_argument("empty grid");
-  if (rq.M > int64_t(INT32_MAX) - 1024)
-    throw std::invalid_argument("more visibilities than int32 indices can address");
+  if (rq.M > int64_t(INT32_MAX) / 2)
+    throw std::invalid_argument("more visibilities than int32 slot indices can address");
   if (rq.max_per_item < 1 || rq.max_per_item > 0xffff)
     throw std::invalid_argument("max_per_item out of range");
+  if (rq.tile < 1 || rq.tile > 255) throw std::invalid_argument("tile edge out of range");
 
   Plan P;
   P.M = rq.M;
@@ -47,17 +55,16 @@ Plan build_plan(const PlanRequest &rq) {
   P.tu = make_tiling(rq.Nu, rq.tile);
   P.tv = make_tiling(rq.Nv, rq.tile);
   // A window reaches J - 1 cells into the next tile; it must not reach two
-  // tiles ahead, so every tile must be at least J - 1 cells wide.
-  const int min_w = P.tu.start[1] - P.tu.start[0];
-  const int min_h = P.tv.start[1] - P.tv.start[0];
+  // tiles ahead, so every tile must be at least J - 1 cells wide, and the
+  // grid must hold the support.
+  if (rq.Nu < rq.Ju || rq.Nv < rq.Jv)
+    throw std::invalid_argument("grid is smaller than the kernel support");
   for (int b = 0; b < P.tu.n; ++b)
-    if (P.tu.start[b + 1] - P.tu.start[b] < rq.Ju - 1 || rq.Nu < rq.Ju)
-      throw std::invalid_argument("grid width is smaller than the kernel support");
+    if (P.tu.start[b + 1] - P.tu.start[b] < rq.Ju - 1)
+      throw std::invalid_argument("grid width is too small for the kernel support");
   for (int b = 0; b < P.tv.n; ++b)
-    if (P.tv.start[b + 1] - P.tv.start[b] < rq.Jv - 1 || rq.Nv < rq.Jv)
-      throw std::invalid_argument("grid height is smaller than the kernel support");
-  (void)min_w;
-  (void)min_h;
+    if (P.tv.start[b + 1] - P.tv.start[b] < rq.Jv - 1)
+      throw std::invalid_argument("grid height is too small for the kernel support");
 
   const int ntu = P.tu.n, ntv = P.tv.n, ntiles = ntu * ntv;
   // Cell rank: tiles in row-major order, cells row-major inside a tile.
@@ -87,47 +94,35 @@ Plan build_plan(const PlanRequest &rq) {
     const int q0 = int(wrap(ku + 1, rq.Nu));
     const int p0 = int(wrap(kv + 1, rq.Nv));
     // exp(-2 pi i ((k_u + j_u) + (k_v + j_v)) / 2) = (-1)^(k_u + k_v) (-1)^(j_u + j_v);
-    // the first factor goes into the weight, the second into the polynomials.
+    // the first factor goes with the weight, the second into the polynomials.
     flip[m] = uint8_t((int64_t(ku) + int64_t(kv)) & 1);
     const int a = P.tv.of[p0], b = P.tu.of[q0];
     const int t = a * ntu + b;
     const int w = P.tu.start[b + 1] - P.tu.start[b];
     rank[m] = tile_cell0[t] + int64_t(p0 - P.tv.start[a]) * w + (q0 - P.tu.start[b]);
   }
+  if (rq.weights)
+    for (int64_t m = 0; m < M && P.unit_weights; ++m)
+      if (rq.weights[m] != std::complex<double>(1.0, 0.0)) P.unit_weights = false;
 
-  // Stable counting sort by cell rank.
+  // Stable counting sort by cell rank: sorted[k] is a caller index.
   std::vector<int64_t> cell_first(ncells + 1, 0);
   for (int64_t m = 0; m < M; ++m) cell_first[rank[m] + 1]++;
   for (int64_t c = 0; c < ncells; ++c) cell_first[c + 1] += cell_first[c];
-  P.perm.resize(M);
+  std::vector<int32_t> sorted(M);
   {
     std::vector<int64_t> fill(cell_first.begin(), cell_first.end() - 1);
-    for (int64_t m = 0; m < M; ++m) P.perm[fill[rank[m]]++] = int32_t(m);
-  }
-  P.frac_u.resize(M);
-  P.frac_v.resize(M);
-  P.weight.resize(M);
-#pragma omp parallel for schedule(static)
-  for (int64_t i = 0; i < M; ++i) {
-    const int32_t m = P.perm[i];
-    P.frac_u[i] = tu[m];
-    P.frac_v[i] = tv[m];
-    std::complex<double> wgt = rq.weights ? rq.weights[m] : std::complex<double>(1.0, 0.0);
-    P.weight[i] = flip[m] ? -wgt : wgt;
+    for (int64_t m = 0; m < M; ++m) sorted[fill[rank[m]]++] = int32_t(m);
   }
 
-  // Work items, tile by tile.  A cell with c visibilities becomes
-  // ceil(c / K) items of nearly equal size.  Items are grouped in layers by
-  // chunk index, so a layer never holds two items of one cell; each layer is
-  // ordered by descending size (lanes of a batch then run equal loops) and
-  // padded to a whole number of 32-item batches.  Any batch therefore holds
-  // at most one item per base cell.
+  // Work items and batches, tile by tile.
   const int K = rq.max_per_item;
   P.tile_tasks.assign(ntiles + 1, 0);
-  struct Item {
-    int32_t first, lp, lq, count, chunk;
-  };
   std::vector<Item> items;
+  std::vector<int32_t> stamp;  // per cell of the tile: last batch that took it
+  std::vector<uint8_t> taken;
+  // slot assignment collected per batch: (slot, sorted index) pairs
+  std::vector<int64_t> slot_sorted;  // slot -> sorted index or -1
   for (int a = 0; a < ntv; ++a)
     for (int b = 0; b < ntu; ++b) {
       const int t = a * ntu + b;
@@ -140,55 +135,114 @@ Plan build_plan(const PlanRequest &rq) {
         P.occupied_cells++;
         P.max_cell_count = std::max<int64_t>(P.max_cell_count, n);
         const int local = int(c - tile_cell0[t]);
-        const int lp = local / w, lq = local % w;
         const int64_t chunks = (n + K - 1) / K;
         const int64_t base = n / chunks, rem = n % chunks;
         int64_t first = cell_first[c];
         for (int64_t k = 0; k < chunks; ++k) {
           const int32_t cnt = int32_t(base + (k < rem ? 1 : 0));
-          items.push_back({int32_t(first), lp, lq, cnt, int32_t(k)});
+          items.push_back({int32_t(first), cnt, local, local / w, local % w});
           first += cnt;
         }
       }
       P.real_items += int64_t(items.size());
-      const int64_t item0 = int64_t(P.item_first.size());
-      // Layer order: chunk index ascending, then size descending; stable, so
-      // items of equal size keep their cell order.
-      std::stable_sort(items.begin(), items.end(), [](const Item &x, const Item &y) {
-        return x.chunk != y.chunk ? x.chunk < y.chunk : x.count > y.count;
-      });
-      for (size_t k = 0; k < items.size(); ++k) {
-        if (k > 0 && items[k].chunk != items[k - 1].chunk)
-          while ((P.item_first.size() - item0) % kBatch) {
-            P.item_first.push_back(0);
-            P.item_code.push_back(0);
+      // Longest items first (lanes of a batch then run equal loops); stable,
+      // so equal sizes keep cell order.
+      std::stable_sort(items.begin(), items.end(),
+                       [](const Item &x, const Item &y) { return x.count > y.count; });
+      // Greedy packing: scan the pending items in order, take one unless its
+      // cell is already in the batch.  The scan looks at most `reach` pending
+      // items past the first one it had to skip.
+      stamp.assign(size_t(h) * w, -1);
+      taken.assign(items.size(), 0);
+      size_t front = 0;
+      int32_t batch_id = 0;
+      const int64_t task_batch0 = int64_t(P.batch_base.size());
+      std::vector<size_t> lanes;
+      while (true) {
+        while (front < items.size() && taken[front]) ++front;
+        if (front == items.size()) break;
+        lanes.clear();
+        size_t skipped = 0;
+        for (size_t k = front; k < items.size() && lanes.size() < size_t(kBatch); ++k) {
+          if (taken[k]) continue;
+          if (stamp[items[k].cell] == batch_id) {
+            if (++skipped > 256) break;
+            continue;
           }
-        P.item_first.push_back(items[k].first);
-        P.item_code.push_back(item_pack(items[k].lp, items[k].lq, items[k].count));
+          stamp[items[k].cell] = batch_id;
+          taken[k] = 1;
+          lanes.push_back(k);
+        }
+        int kmax = 0;
+        for (size_t k : lanes) kmax = std::max(kmax, int(items[k].count));
+        const int64_t base = P.S;
+        P.batch_base.push_back(int32_t(base));
+        P.batch_kmax.push_back(kmax);
+        P.S += int64_t(kBatch) * kmax;
+        if (P.S > int64_t(INT32_MAX)) throw std::invalid_argument("too many slots");
+        slot_sorted.resize(P.S, -1);
+        for (int l = 0; l < kBatch; ++l) {
+          if (l < int(lanes.size())) {
+            const Item &it = items[lanes[l]];
+            P.lane_code.push_back(item_pack(it.lp, it.lq, it.count));
+            for (int k = 0; k < it.count; ++k)
+              slot_sorted[base + int64_t(kBatch) * k + l] = it.first + k;
+          } else {
+            P.lane_code.push_back(0);
+          }
+        }
+        ++batch_id;
       }
-      while ((P.item_first.size() - item0) % kBatch) {
-        P.item_first.push_back(0);
-        P.item_code.push_back(0);
-      }
-      const int64_t nb = (int64_t(P.item_first.size()) - item0) / kBatch;
-      const int64_t b0 = item0 / kBatch;
-      for (int64_t s = 0; s < nb; s += rq.max_batches_per_task) {
+      // Tasks: consecutive batches of the tile, bounded in slots and batches.
+      const int64_t nb = int64_t(P.batch_base.size()) - task_batch0;
+      int64_t s = 0;
+      while (s < nb) {
+        int64_t e = s, slots = 0;
+        while (e < nb && (e == s || (e - s < rq.max_batches_per_task &&
+                                     slots + int64_t(kBatch) * P.batch_kmax[task_batch0 + e] <=
+                                         rq.max_slots_per_task))) {
+          slots += int64_t(kBatch) * P.batch_kmax[task_batch0 + e];
+          ++e;
+        }
         Task tk{};
         tk.P = P.tv.start[a];
         tk.Q = P.tu.start[b];
         tk.H = h;
         tk.W = w;
-        tk.batch_begin = int32_t(b0 + s);
-        tk.batch_end = int32_t(b0 + std::min<int64_t>(nb, s + rq.max_batches_per_task));
+        tk.batch_begin = int32_t(task_batch0 + s);
+        tk.batch_end = int32_t(task_batch0 + e);
         tk.tile = t;
         P.tasks.push_back(tk);
+        s = e;
       }
       P.tile_tasks[t + 1] = int32_t(P.tasks.size());
       P.win_rows = std::max(P.win_rows, h + rq.Jv - 1);
       P.win_cols = std::max(P.win_cols, w + rq.Ju - 1);
     }
-  if (P.item_first.size() > size_t(INT32_MAX))
-    throw std::invalid_argument("too many work items for int32 indexing");
+
+  // Per-slot coverage state.
+  const int64_t S = P.S;
+  P.frac_u.assign(S, 0.0);
+  P.frac_v.assign(S, 0.0);
+  P.flip.assign(S, 0);
+  P.slot_user.assign(S, -1);
+  P.user_slot.assign(M, -1);
+  if (!P.unit_weights) P.weight.assign(S, std::complex<double>(0.0, 0.0));
+#pragma omp parallel for schedule(static)
+  for (int64_t s = 0; s < S; ++s) {
+    const int64_t k = slot_sorted[s];
+    if (k < 0) continue;
+    const int32_t m = sorted[k];
+    P.frac_u[s] = tu[m];
+    P.frac_v[s] = tv[m];
+    P.flip[s] = flip[m];
+    P.slot_user[s] = m;
+    P.user_slot[m] = int32_t(s);
+    if (!P.unit_weights) {
+      const std::complex<double> wgt = rq.weights[m];
+      P.weight[s] = flip[m] ? -wgt : wgt;
+    }
+  }
   return P;
 }
 

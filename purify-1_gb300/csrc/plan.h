@@ -1,5 +1,13 @@
 // Coverage planning (host, FP64): everything about a set of visibilities that
 // does not change between applies of the operator.
+//
+// Visibilities are sorted by uv tile and base cell, grouped into work items
+// (one base cell, up to K visibilities) and packed into batches of 32 items,
+// one item per lane, no two items of a batch on the same base cell.  Each
+// batch owns 32 * kmax consecutive "slots" (kmax = its largest item): lane l's
+// k-th visibility sits in slot base + 32 k + l, so a warp that walks k reads
+// 256 contiguous bytes per access and every lane runs the same loop.  Lanes
+// whose item is shorter than kmax own null slots (no visibility).
 #pragma once
 #include <complex>
 #include <cstdint>
@@ -17,8 +25,9 @@ struct PlanRequest {
   int Nu = 0, Nv = 0;  // grid width (u, fastest) and height (v)
   int Ju = 4, Jv = 4;  // taps per axis
   int tile = kTile;
-  int max_per_item = 16;        // visibilities of one cell handled by one lane
+  int max_per_item = 16;         // visibilities of one cell handled by one lane
   int max_batches_per_task = 64;
+  int64_t max_slots_per_task = 16384;
 };
 
 // Tiling of one grid axis: tile b covers [start[b], start[b + 1]).
@@ -29,17 +38,26 @@ struct AxisTiling {
 };
 
 struct Plan {
-  int64_t M = 0;
+  int64_t M = 0;  // visibilities
+  int64_t S = 0;  // slots (>= M)
   int Nu = 0, Nv = 0, Ju = 0, Jv = 0;
-  AxisTiling tu, tv;                 // tilings of the u (columns) and v (rows) axes
-  std::vector<double> frac_u, frac_v;  // plan order, in [0, 1)
-  std::vector<std::complex<double>> weight;  // plan order, phase sign folded in
-  std::vector<int32_t> perm;         // plan order -> caller order
-  std::vector<int32_t> item_first;   // per work item
-  std::vector<int32_t> item_code;    // per work item (item_pack)
+  AxisTiling tu, tv;  // tilings of the u (columns) and v (rows) axes
+  // True when every weight is exactly 1: the weight stream is then replaced
+  // by the phase sign alone.
+  bool unit_weights = true;
+  // per slot
+  std::vector<double> frac_u, frac_v;        // in [0, 1); 0 for null slots
+  std::vector<uint8_t> flip;                 // (-1)^(k_u + k_v) == -1
+  std::vector<std::complex<double>> weight;  // weight with the sign folded in (empty when unit)
+  std::vector<int32_t> slot_user;            // caller index, -1 for null slots
+  // per visibility
+  std::vector<int32_t> user_slot;  // caller index -> slot
+  // per batch
+  std::vector<int32_t> batch_base, batch_kmax;
+  std::vector<int32_t> lane_code;  // batch * 32 + lane -> item_pack(lp, lq, count)
   std::vector<Task> tasks;
-  std::vector<int32_t> tile_tasks;   // ntiles + 1 offsets into tasks
-  int win_rows = 0, win_cols = 0;    // largest window: (H + Jv - 1) x (W + Ju - 1)
+  std::vector<int32_t> tile_tasks;  // ntiles + 1 offsets into tasks
+  int win_rows = 0, win_cols = 0;   // largest window: (H + Jv - 1) x (W + Ju - 1)
   // statistics
   int64_t occupied_cells = 0;
   int64_t real_items = 0;

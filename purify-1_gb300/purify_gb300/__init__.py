@@ -74,7 +74,8 @@ EXPORTS = [
     "purify_gb300_kernel_taps", "purify_gb300_degrid", "purify_gb300_grid",
     "purify_gb300_correction", "purify_gb300_stage_timing", "purify_gb300_stage_times",
 ]
-STAGES = ["pad", "fft_forward", "degrid", "grid", "fold", "fft_inverse", "crop"]
+STAGES = ["pad", "fft_forward", "degrid", "grid", "fold", "fft_inverse", "crop", "compact",
+          "expand"]
 
 _lib = None
 
@@ -110,7 +111,7 @@ def load(path=None):
     L.purify_gb300_plan_create.argtypes = [vp, vp, vp, ctypes.c_int64, ctypes.c_uint32,
                                            ctypes.c_uint32, ctypes.c_uint32, P(vp)]
     L.purify_gb300_plan_sizes.argtypes = [vp, vp]
-    L.purify_gb300_plan_export.argtypes = [vp] + [vp] * 9
+    L.purify_gb300_plan_export.argtypes = [vp] + [vp] * 10
     L.purify_gb300_plan_destroy.argtypes = [vp]
     L.purify_gb300_kernel_taps.argtypes = [ctypes.c_int32, ctypes.c_uint32, ctypes.c_double,
                                            ctypes.c_int32, vp, ctypes.c_int64, vp,
@@ -176,25 +177,28 @@ class CoveragePlan:
         _check(L.purify_gb300_plan_create(_np_ptr(u), _np_ptr(v), _np_ptr(wt), u.size,
                                           int(ftsizeu), int(ftsizev), int(J), ctypes.byref(h)))
         try:
-            sz = np.zeros(7, dtype=np.int64)
+            sz = np.zeros(9, dtype=np.int64)
             _check(L.purify_gb300_plan_sizes(h, _np_ptr(sz)))
-            M, ni, nt, ntu, ntv, wr, wc = (int(s) for s in sz)
-            self.frac = np.empty((M, 2))
-            self.weight = np.empty(M, dtype=np.complex128)
-            self.perm = np.empty(M, dtype=np.int32)
-            self.item_first = np.empty(ni, dtype=np.int32)
-            self.item_code = np.empty(ni, dtype=np.int32)
+            M, S, nb, nt, ntu, ntv, wr, wc, unit = (int(s) for s in sz)
+            self.frac = np.empty((S, 2))
+            self.weight = np.empty(S, dtype=np.complex128)
+            self.slot_user = np.empty(S, dtype=np.int32)
+            self.user_slot = np.empty(M, dtype=np.int32)
+            self.batches = np.empty((nb, 2), dtype=np.int32)
+            self.lane_code = np.empty((nb, 32), dtype=np.int32)
             self.tasks = np.empty((nt, 8), dtype=np.int32)
             self.tile_tasks = np.empty(ntu * ntv + 1, dtype=np.int32)
             self.tu_start = np.empty(ntu + 1, dtype=np.int32)
             self.tv_start = np.empty(ntv + 1, dtype=np.int32)
             _check(L.purify_gb300_plan_export(
-                h, _np_ptr(self.frac), _np_ptr(self.weight), _np_ptr(self.perm),
-                _np_ptr(self.item_first), _np_ptr(self.item_code), _np_ptr(self.tasks),
-                _np_ptr(self.tile_tasks), _np_ptr(self.tu_start), _np_ptr(self.tv_start)))
+                h, _np_ptr(self.frac), _np_ptr(self.weight), _np_ptr(self.slot_user),
+                _np_ptr(self.user_slot), _np_ptr(self.batches), _np_ptr(self.lane_code),
+                _np_ptr(self.tasks), _np_ptr(self.tile_tasks), _np_ptr(self.tu_start),
+                _np_ptr(self.tv_start)))
         finally:
             L.purify_gb300_plan_destroy(h)
-        self.M, self.ntu, self.ntv, self.win_rows, self.win_cols = M, ntu, ntv, wr, wc
+        self.M, self.S, self.ntu, self.ntv = M, S, ntu, ntv
+        self.win_rows, self.win_cols, self.unit_weights = wr, wc, bool(unit)
         self.Nu, self.Nv, self.J = int(ftsizeu), int(ftsizev), int(J)
 
 

@@ -27,47 +27,50 @@ def test_tap_polynomials_match_kernel(pg, oracle_mod, kernel, J):
     assert np.abs(f32 - exact).max() <= 3e-7 * peak, (e32, np.abs(f32 - exact).max())
 
 
+def _lanes(plan, b):
+    base, kmax = plan.batches[b]
+    for lane in range(32):
+        code = int(plan.lane_code[b, lane])
+        lp, lq, cnt = code & 0xFF, (code >> 8) & 0xFF, (code >> 16) & 0xFFFF
+        yield lane, lp, lq, cnt, [base + 32 * k + lane for k in range(kmax)]
+
+
 def replay_degrid(plan, taps_u, taps_v, grid):
-    """y[perm[i]] = w_i sum_jv sum_ju kv ku window[lp+jv, lq+ju], as degrid_kernel."""
+    """Slot values as degrid_kernel writes them, then compact_kernel."""
     J, Nu, Nv = plan.J, plan.Nu, plan.Nv
-    y = np.zeros(plan.M, dtype=np.complex128)
+    slots = np.zeros(plan.S, dtype=np.complex128)
     g = grid.reshape(Nv, Nu)
     for (P, Q, H, W, b0, b1, tile, _) in plan.tasks:
         for b in range(b0, b1):
-            for lane in range(32):
-                k = b * 32 + lane
-                code = int(plan.item_code[k])
-                lp, lq, cnt = code & 0xFF, (code >> 8) & 0xFF, (code >> 16) & 0xFFFF
+            for lane, lp, lq, cnt, sl in _lanes(plan, b):
                 assert lp < H and lq < W
                 rows = (P + lp + np.arange(J)) % Nv
                 cols = (Q + lq + np.arange(J)) % Nu
                 F = g[np.ix_(rows, cols)]
-                for i in range(plan.item_first[k], plan.item_first[k] + cnt):
-                    y[plan.perm[i]] = plan.weight[i] * (taps_v[i] @ F @ taps_u[i])
-    return y
+                for k, i in enumerate(sl):
+                    assert (plan.slot_user[i] >= 0) == (k < cnt)
+                    slots[i] = plan.weight[i] * (taps_v[i] @ F @ taps_u[i])
+    return slots[plan.user_slot]
 
 
 def replay_grid(plan, taps_u, taps_v, vis):
-    """Task windows as grid_kernel writes them, then fold_kernel's fixed-order sum."""
+    """expand_kernel, task windows as grid_kernel writes them, then
+    fold_kernel's fixed-order sum."""
     J, Nu, Nv = plan.J, plan.Nu, plan.Nv
+    slots = np.where(plan.slot_user >= 0, vis[np.maximum(plan.slot_user, 0)], 0)
     windows = []
-    seen_cells = []
     for (P, Q, H, W, b0, b1, tile, _) in plan.tasks:
         win = np.zeros((H + J - 1, W + J - 1), dtype=np.complex128)
         for b in range(b0, b1):
             cells = set()
-            for lane in range(32):
-                k = b * 32 + lane
-                code = int(plan.item_code[k])
-                lp, lq, cnt = code & 0xFF, (code >> 8) & 0xFF, (code >> 16) & 0xFFFF
+            for lane, lp, lq, cnt, sl in _lanes(plan, b):
                 if cnt == 0:
                     continue
                 assert (lp, lq) not in cells, "two items of one base cell in a batch"
                 cells.add((lp, lq))
-                for i in range(plan.item_first[k], plan.item_first[k] + cnt):
-                    z = np.conj(plan.weight[i]) * vis[plan.perm[i]]
+                for i in sl:
+                    z = np.conj(plan.weight[i]) * slots[i]
                     win[lp:lp + J, lq:lq + J] += z * np.outer(taps_v[i], taps_u[i])
-            seen_cells.append(len(cells))
         windows.append(win)
     ntu, ntv = plan.ntu, plan.ntv
     grid = np.zeros((Nv, Nu), dtype=np.complex128)
@@ -106,7 +109,9 @@ def test_plan_replay_matches_oracle_G(pg, oracle_mod, n, J, M, spread, seed):
     wt = rng.standard_normal(M) + 1j * rng.standard_normal(M)
     Nu = Nv = 2 * n
     plan = pg.CoveragePlan(u, v, Nu, Nv, J, weights=wt)
-    assert sorted(plan.perm.tolist()) == list(range(M))
+    assert not plan.unit_weights
+    assert sorted(plan.user_slot.tolist()) == sorted(np.flatnonzero(plan.slot_user >= 0).tolist())
+    assert np.array_equal(plan.slot_user[plan.user_slot], np.arange(M))
     taps_u, _ = pg.kernel_taps("kb", J, plan.frac[:, 0], precision="fp64")
     taps_v, _ = pg.kernel_taps("kb", J, plan.frac[:, 1], precision="fp64")
     op = oracle_mod.Operator(u, v, None, wt, n, n, 2.0, kernel="kb", Ju=J, Jv=J)
@@ -118,9 +123,25 @@ def test_plan_replay_matches_oracle_G(pg, oracle_mod, n, J, M, spread, seed):
     assert rel_l2(g, op.G_adjoint(vis)) < 1e-12
 
 
+def test_unit_weights_plan_matches_oracle(pg, oracle_mod):
+    rng = np.random.default_rng(8)
+    M, n, J = 400, 24, 4
+    u = rng.normal(0, 10, M)
+    v = rng.normal(0, 10, M)
+    plan = pg.CoveragePlan(u, v, 2 * n, 2 * n, J)
+    assert plan.unit_weights
+    taps_u, _ = pg.kernel_taps("kb", J, plan.frac[:, 0], precision="fp64")
+    taps_v, _ = pg.kernel_taps("kb", J, plan.frac[:, 1], precision="fp64")
+    op = oracle_mod.Operator(u, v, None, None, n, n, 2.0, kernel="kb", Ju=J, Jv=J)
+    grid = rng.standard_normal(4 * n * n) + 1j * rng.standard_normal(4 * n * n)
+    assert rel_l2(replay_degrid(plan, taps_u, taps_v, grid), op.G_forward(grid)) < 1e-12
+    vis = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    assert rel_l2(replay_grid(plan, taps_u, taps_v, vis), op.G_adjoint(vis)) < 1e-12
+
+
 def test_plan_empty_and_bad_sizes(pg):
     p = pg.CoveragePlan(np.zeros(0), np.zeros(0), 32, 32, 4)
-    assert p.M == 0 and p.item_first.size == 0
+    assert p.M == 0 and p.S == 0 and p.batches.shape[0] == 0
     with pytest.raises(pg.PurifyError):
         pg.CoveragePlan(np.zeros(3), np.zeros(3), 4, 4, 6)  # grid smaller than the support
 
@@ -130,5 +151,6 @@ def test_plan_balances_dense_cells(pg):
     u = np.full(5000, 0.25)
     v = np.full(5000, -0.5)
     p = pg.CoveragePlan(u, v, 64, 64, 4)
-    counts = (p.item_code >> 16) & 0xFFFF
+    counts = (p.lane_code >> 16) & 0xFFFF
     assert counts.sum() == 5000 and counts.max() <= 16
+    assert (p.slot_user >= 0).sum() == 5000
