@@ -91,6 +91,20 @@ int purify_gb300_operator_create(const purify_gb300_create_args *args,
                                  purify_gb300_operator **out);
 int purify_gb300_operator_destroy(purify_gb300_operator *op);
 
+/* Launch and layout parameters; 0 (or -1 for fused_permute) picks the
+ * default.  No counterpart in the reference (its operator has no launch
+ * shapes); the autotuner searches these. */
+typedef struct {
+  int32_t threads;       /* CTA threads of the degrid/grid kernels, multiple of 32, <= 256 */
+  int32_t max_per_item;  /* visibilities of one base cell given to one lane (<= 65535) */
+  int32_t tile;          /* uv tile edge in grid cells (<= 255) */
+  int32_t fused_permute; /* 1: degrid/grid touch caller-ordered visibilities directly,
+                            0: via a slot-ordered buffer and gather kernels, -1: default */
+} purify_gb300_tuning;
+int purify_gb300_operator_create_tuned(const purify_gb300_create_args *args,
+                                       const purify_gb300_tuning *tuning,
+                                       purify_gb300_operator **out);
+
 /* Phi x and Phi^H y on device buffers of the operator's precision (c64 for
  * FP32, c128 for FP64).  x has imsizey*imsizex values, y has M values.  The
  * work is ordered after prior work on `stream` (a cudaStream_t, 0 = legacy

@@ -70,6 +70,12 @@ void purify_gb300_default_args(purify_gb300_create_args *a) {
 }
 
 int purify_gb300_operator_create(const purify_gb300_create_args *a, purify_gb300_operator **out) {
+  return purify_gb300_operator_create_tuned(a, nullptr, out);
+}
+
+int purify_gb300_operator_create_tuned(const purify_gb300_create_args *a,
+                                       const purify_gb300_tuning *t,
+                                       purify_gb300_operator **out) {
   if (!a) return null_arg("args");
   if (!out) return null_arg("out");
   *out = nullptr;
@@ -94,6 +100,12 @@ int purify_gb300_operator_create(const purify_gb300_create_args *a, purify_gb300
     c.celly = a->celly;
     c.fp64 = a->precision == PURIFY_GB300_FP64;
     c.device = a->device;
+    if (t) {
+      c.threads = t->threads;
+      c.max_per_item = t->max_per_item;
+      c.tile = t->tile;
+      c.fused_permute = t->fused_permute;
+    }
     if (a->precision != PURIFY_GB300_FP32 && a->precision != PURIFY_GB300_FP64)
       throw pg::Error(pg::kInvalidArgument, "unknown precision");
     auto *h = new purify_gb300_operator();

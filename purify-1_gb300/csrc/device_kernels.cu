@@ -100,10 +100,18 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a,
 #pragma unroll
       for (int ju = 0; ju < J; ++ju) F[jv][ju] = win[(lp + jv) * WW + lq + ju];
     // Lanes past their item's end compute on null slots; those results are
-    // never read, so the loop has no per-lane branch.
-    for (int k = 0; k < bt.y; ++k) {
-      const size_t i = size_t(bt.x) + size_t(k) * kBatch + lane;
-      const C t = stream_load(frac + i);
+    // never read, so the loop has no per-lane branch.  The next slot's
+    // coverage state is loaded one iteration ahead.
+    size_t i = size_t(bt.x) + lane;
+    C t_next = bt.y > 0 ? stream_load(frac + i) : C{0, 0};
+    int m_next = (a.slot_user && bt.y > 0) ? __ldcs(a.slot_user + i) : 0;
+    for (int k = 0; k < bt.y; ++k, i += kBatch) {
+      const C t = t_next;
+      const int m = m_next;
+      if (k + 1 < bt.y) {
+        t_next = stream_load(frac + i + kBatch);
+        if (a.slot_user) m_next = __ldcs(a.slot_user + i + kBatch);
+      }
       real ku[J], kv[J];
       tap_weights<real, J, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
       tap_weights<real, J, SUB>(poly.v, poly.nsub_v, t.y, kv);
@@ -129,7 +137,10 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a,
         y.x = sr * w.x - si * w.y;
         y.y = sr * w.y + si * w.x;
       }
-      out[i] = y;
+      if (!a.slot_user)
+        out[i] = y;
+      else if (m >= 0)
+        out[m] = y;
     }
   }
 }
@@ -160,11 +171,31 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a,
     for (int jv = 0; jv < J; ++jv)
 #pragma unroll
       for (int ju = 0; ju < J; ++ju) acc[jv][ju] = C{0, 0};
-    // Null slots hold a zero visibility, so they add nothing.
-    for (int k = 0; k < bt.y; ++k) {
-      const size_t i = size_t(bt.x) + size_t(k) * kBatch + lane;
-      const C t = stream_load(frac + i);
-      const C yv = vin[i];
+    // Null slots hold a zero visibility, so they add nothing.  The next
+    // slot's state is loaded one iteration ahead.
+    size_t i = size_t(bt.x) + lane;
+    C t_next{0, 0}, y_next{0, 0};
+    if (bt.y > 0) {
+      t_next = stream_load(frac + i);
+      if (a.slot_user) {
+        const int m = __ldcs(a.slot_user + i);
+        y_next = m >= 0 ? vin[m] : C{0, 0};
+      } else {
+        y_next = vin[i];
+      }
+    }
+    for (int k = 0; k < bt.y; ++k, i += kBatch) {
+      const C t = t_next;
+      const C yv = y_next;
+      if (k + 1 < bt.y) {
+        t_next = stream_load(frac + i + kBatch);
+        if (a.slot_user) {
+          const int m = __ldcs(a.slot_user + i + kBatch);
+          y_next = m >= 0 ? vin[m] : C{0, 0};
+        } else {
+          y_next = vin[i + kBatch];
+        }
+      }
       real zr, zi;
       if (unit) {
         const real sg = copysign(real(1), t.x);

@@ -24,6 +24,10 @@ struct ApplyArgs {
   const void *weight = nullptr;     // S complex weights with the flip folded in, or null
   void *slot_out = nullptr;         // degrid output, S complex
   const void *slot_in = nullptr;    // grid input, S complex
+  // When set, visibilities are read / written in caller order directly:
+  // slot s holds visibility slot_user[s] (-1 = null slot), slot_out and
+  // slot_in then point at caller-ordered M-vectors.
+  const int32_t *slot_user = nullptr;
   int Nu = 0, Nv = 0;
   int64_t slot_stride = 0;          // complex elements per tilebuf slot
 };

@@ -131,13 +131,13 @@ class OperatorT final : public Operator {
   void forward_on_stream(const void *x, void *y);
   void adjoint_on_stream(const void *y, void *x);
   // G and G^H between the grid and the slot-ordered visibility buffer.
-  void degrid_slots(const void *grid);
-  void grid_slots(void *grid);
+  void degrid_slots(const void *grid, void *caller_vis = nullptr);
+  void grid_slots(void *grid, const void *caller_vis = nullptr);
   void degrid_on_stream(const void *grid, void *y);
   void grid_on_stream(const void *y, void *grid);
   // Phi' / Phi'^H with visibilities kept in slot order (power method).
-  void forward_slots(const void *x);
-  void adjoint_slots(void *x);
+  void forward_slots(const void *x, void *caller_vis = nullptr);
+  void adjoint_slots(void *x, const void *caller_vis = nullptr);
   void join(cudaStream_t user);
   void release(cudaStream_t user);
   void upload_correction();
@@ -148,6 +148,7 @@ class OperatorT final : public Operator {
   int Nx_ = 0, Ny_ = 0, Nu_ = 0, Nv_ = 0, x0_ = 0, y0_ = 0, J_ = 0;
   int64_t M_ = 0, N_ = 0, S_ = 0;
   bool unit_weights_ = true;
+  bool fused_permute_ = true;
   double norm_ = 1.0;
   std::vector<double> su_, sv_;  // 1 / ft kernel at the image pixels (unscaled)
   std::vector<real> su_scaled_, sv_real_;
@@ -227,6 +228,7 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
     throw Error(kInvalidArgument, e.what());
   }
   shape_.threads = cfg.threads > 0 ? cfg.threads : 128;
+  fused_permute_ = cfg.fused_permute != 0;
   ntasks_ = int(plan.tasks.size());
   win_rows_ = plan.win_rows;
   win_cols_ = plan.win_cols;
@@ -366,7 +368,7 @@ void OperatorT<real>::release(cudaStream_t user) {
 }
 
 template <typename real>
-void OperatorT<real>::degrid_slots(const void *grid) {
+void OperatorT<real>::degrid_slots(const void *grid, void *caller_vis) {
   ApplyArgs<real> a;
   a.grid = grid;
   a.tasks = tasks_.as<Task>();
@@ -374,7 +376,8 @@ void OperatorT<real>::degrid_slots(const void *grid) {
   a.lane_code = lane_code_.as<int32_t>();
   a.frac = frac_.get();
   a.weight = unit_weights_ ? nullptr : weight_.get();
-  a.slot_out = slots_.get();
+  a.slot_out = caller_vis ? caller_vis : slots_.get();
+  a.slot_user = caller_vis ? slot_user_.as<int32_t>() : nullptr;
   a.Nu = Nu_;
   a.Nv = Nv_;
   mark_begin(kDegrid);
@@ -384,7 +387,7 @@ void OperatorT<real>::degrid_slots(const void *grid) {
 }
 
 template <typename real>
-void OperatorT<real>::grid_slots(void *grid) {
+void OperatorT<real>::grid_slots(void *grid, const void *caller_vis) {
   ApplyArgs<real> a;
   a.tilebuf = tilebuf_.get();
   a.tasks = tasks_.as<Task>();
@@ -392,7 +395,8 @@ void OperatorT<real>::grid_slots(void *grid) {
   a.lane_code = lane_code_.as<int32_t>();
   a.frac = frac_.get();
   a.weight = unit_weights_ ? nullptr : weight_.get();
-  a.slot_in = slots_.get();
+  a.slot_in = caller_vis ? caller_vis : slots_.get();
+  a.slot_user = caller_vis ? slot_user_.as<int32_t>() : nullptr;
   a.Nu = Nu_;
   a.Nv = Nv_;
   a.slot_stride = slot_stride_;
@@ -422,6 +426,10 @@ void OperatorT<real>::grid_slots(void *grid) {
 
 template <typename real>
 void OperatorT<real>::degrid_on_stream(const void *grid, void *y) {
+  if (fused_permute_) {
+    degrid_slots(grid, y);
+    return;
+  }
   degrid_slots(grid);
   mark_begin(kCompact);
   cuda_check(launch_compact<real>(slots_.get(), user_slot_.as<int32_t>(), y, M_, stream_),
@@ -431,6 +439,10 @@ void OperatorT<real>::degrid_on_stream(const void *grid, void *y) {
 
 template <typename real>
 void OperatorT<real>::grid_on_stream(const void *y, void *grid) {
+  if (fused_permute_) {
+    grid_slots(grid, y);
+    return;
+  }
   mark_begin(kExpand);
   cuda_check(launch_expand<real>(y, slot_user_.as<int32_t>(), slots_.get(), S_, stream_),
              "expand");
@@ -439,7 +451,7 @@ void OperatorT<real>::grid_on_stream(const void *y, void *grid) {
 }
 
 template <typename real>
-void OperatorT<real>::forward_slots(const void *x) {
+void OperatorT<real>::forward_slots(const void *x, void *caller_vis) {
   mark_begin(kPad);
   cuda_check(launch_pad<real>(x, su_d_.as<real>(), sv_d_.as<real>(), pad_.get(), Nx_, Ny_, Nu_,
                               x0_, y0_, stream_),
@@ -448,12 +460,12 @@ void OperatorT<real>::forward_slots(const void *x) {
   mark_begin(kFftF);
   cufft_check(Traits<real>::exec(fft_, pad_.get(), work_.get(), CUFFT_FORWARD), "cufftExec");
   mark_end(kFftF);
-  degrid_slots(work_.get());
+  degrid_slots(work_.get(), caller_vis);
 }
 
 template <typename real>
-void OperatorT<real>::adjoint_slots(void *x) {
-  grid_slots(work_.get());
+void OperatorT<real>::adjoint_slots(void *x, const void *caller_vis) {
+  grid_slots(work_.get(), caller_vis);
   mark_begin(kFftI);
   cufft_check(Traits<real>::exec(fft_, work_.get(), work_.get(), CUFFT_INVERSE), "cufftExec");
   mark_end(kFftI);
@@ -466,6 +478,10 @@ void OperatorT<real>::adjoint_slots(void *x) {
 
 template <typename real>
 void OperatorT<real>::forward_on_stream(const void *x, void *y) {
+  if (fused_permute_) {
+    forward_slots(x, y);
+    return;
+  }
   forward_slots(x);
   mark_begin(kCompact);
   cuda_check(launch_compact<real>(slots_.get(), user_slot_.as<int32_t>(), y, M_, stream_),
@@ -475,6 +491,10 @@ void OperatorT<real>::forward_on_stream(const void *x, void *y) {
 
 template <typename real>
 void OperatorT<real>::adjoint_on_stream(const void *y, void *x) {
+  if (fused_permute_) {
+    adjoint_slots(x, y);
+    return;
+  }
   mark_begin(kExpand);
   cuda_check(launch_expand<real>(y, slot_user_.as<int32_t>(), slots_.get(), S_, stream_),
              "expand");

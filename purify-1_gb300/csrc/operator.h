@@ -40,6 +40,10 @@ struct OperatorConfig {
   int threads = 0;
   int max_per_item = 0;
   int tile = 0;
+  // 1: degrid/grid read and write caller-ordered visibilities directly;
+  // 0: through a slot-ordered buffer and separate gather kernels;
+  // -1: choose (currently: direct).
+  int fused_permute = -1;
 };
 
 // S(j, i) = 1 / (ftv(y0 + j + 0.5) ftu(x0 + i + 0.5)) for the kernel, as

@@ -51,6 +51,11 @@ class CreateArgs(ctypes.Structure):
     ]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("threads", ctypes.c_int32), ("max_per_item", ctypes.c_int32),
+                ("tile", ctypes.c_int32), ("fused_permute", ctypes.c_int32)]
+
+
 class Info(ctypes.Structure):
     _fields_ = [
         ("M", ctypes.c_int64), ("imsizey", ctypes.c_uint32), ("imsizex", ctypes.c_uint32),
@@ -73,6 +78,7 @@ EXPORTS = [
     "purify_gb300_plan_sizes", "purify_gb300_plan_export", "purify_gb300_plan_destroy",
     "purify_gb300_kernel_taps", "purify_gb300_degrid", "purify_gb300_grid",
     "purify_gb300_correction", "purify_gb300_stage_timing", "purify_gb300_stage_times",
+    "purify_gb300_operator_create_tuned",
 ]
 STAGES = ["pad", "fft_forward", "degrid", "grid", "fold", "fft_inverse", "crop", "compact",
           "expand"]
@@ -96,6 +102,7 @@ def load(path=None):
     L.purify_gb300_default_args.restype = None
     L.purify_gb300_operator_create.argtypes = [P(CreateArgs), P(vp)]
     L.purify_gb300_operator_destroy.argtypes = [vp]
+    L.purify_gb300_operator_create_tuned.argtypes = [P(CreateArgs), P(Tuning), P(vp)]
     for f in (L.purify_gb300_forward, L.purify_gb300_adjoint):
         f.argtypes = [vp, vp, vp, vp]
     for f in (L.purify_gb300_forward_host, L.purify_gb300_adjoint_host):
@@ -211,7 +218,8 @@ class MeasurementOperator:
 
     def __init__(self, u, v, w=None, weights=None, imsizey=256, imsizex=256,
                  oversample_ratio=2.0, power_iters=100, power_tol=1e-4, kernel="kb", Ju=4, Jv=4,
-                 w_term=False, Jw=6, cellx=1.0, celly=1.0, precision="fp32", device=0):
+                 w_term=False, Jw=6, cellx=1.0, celly=1.0, precision="fp32", device=0,
+                 tuning=None):
         L = load()
         u = np.ascontiguousarray(u, dtype=np.float64).ravel()
         v = np.ascontiguousarray(v, dtype=np.float64).ravel()
@@ -238,7 +246,13 @@ class MeasurementOperator:
         a.precision = PRECISIONS[precision]
         a.device = int(device)
         h = ctypes.c_void_p()
-        _check(L.purify_gb300_operator_create(ctypes.byref(a), ctypes.byref(h)))
+        if tuning:
+            t = Tuning(int(tuning.get("threads", 0)), int(tuning.get("max_per_item", 0)),
+                       int(tuning.get("tile", 0)), int(tuning.get("fused_permute", -1)))
+            _check(L.purify_gb300_operator_create_tuned(ctypes.byref(a), ctypes.byref(t),
+                                                        ctypes.byref(h)))
+        else:
+            _check(L.purify_gb300_operator_create(ctypes.byref(a), ctypes.byref(h)))
         self._h = h
         self.precision = precision
         self.M = M
