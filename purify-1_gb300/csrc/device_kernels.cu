@@ -66,14 +66,46 @@ __device__ __forceinline__ T stream_load(const T *p) {
   return __ldcs(p);
 }
 
+// Shared-memory layout of a task: the grid window(s), then the batch
+// headers {first slot, kmax} and the 32 lane codes of each batch.
+struct TaskHeaders {
+  int2 *hdr;
+  int *code;
+};
+template <typename A>
+__device__ __forceinline__ TaskHeaders load_headers(const A &a, const Task &tk,
+                                                    unsigned char *base) {
+  TaskHeaders h;
+  h.hdr = reinterpret_cast<int2 *>(base);
+  h.code = reinterpret_cast<int *>(base + sizeof(int2) * kMaxTaskBatches);
+  const int nbt = tk.batch_end - tk.batch_begin;
+  for (int k = threadIdx.x; k < nbt; k += blockDim.x) h.hdr[k] = a.batches[tk.batch_begin + k];
+  for (int k = threadIdx.x; k < nbt * kBatch; k += blockDim.x)
+    h.code[k] = a.lane_code[size_t(tk.batch_begin) * kBatch + k];
+  return h;
+}
+
+// Visibility read for the grid kernel: slot order, or caller order through
+// slot_user (0 for null slots).
+template <typename real>
+__device__ __forceinline__ cplx<real> read_vis(const ApplyArgs<real> &a, const cplx<real> *vin,
+                                              size_t i) {
+  if (a.slot_user) {
+    const int m = __ldcs(a.slot_user + i);
+    return m >= 0 ? vin[m] : cplx<real>{0, 0};
+  }
+  return vin[i];
+}
+
 template <typename real, int J, bool SUB>
 __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a,
                                                      const __grid_constant__ PolyTable<real> poly) {
   using C = cplx<real>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C *win = reinterpret_cast<C *>(smem_raw);
   const Task tk = a.tasks[blockIdx.x];
   const int WW = tk.W + J - 1, WH = tk.H + J - 1;
+  C *win = reinterpret_cast<C *>(smem_raw);
+  const TaskHeaders th = load_headers(a, tk, smem_raw + a.win_bytes);
   const C *grid = static_cast<const C *>(a.grid);
   // Stage the (wrapped) window of the grid this tile's footprints touch.
   for (int idx = threadIdx.x; idx < WW * WH; idx += blockDim.x) {
@@ -86,62 +118,84 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a,
   }
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int nbt = tk.batch_end - tk.batch_begin;
   const C *frac = static_cast<const C *>(a.frac);
   const C *weight = static_cast<const C *>(a.weight);
   C *out = static_cast<C *>(a.slot_out);
   const bool unit = weight == nullptr;
-  for (int b = tk.batch_begin + warp; b < tk.batch_end; b += nw) {
-    const int2 bt = a.batches[b];
-    const int code = a.lane_code[size_t(b) * kBatch + lane];
+  int lb = warp;
+  if (lb >= nbt) return;
+  // One flattened loop over (batch, k) per warp; the next slot's coverage
+  // state is loaded one step ahead, across batch boundaries too.  Lanes past
+  // their item's end compute on null slots, whose results are never read.
+  int2 bt = th.hdr[lb];
+  int k = 0;
+  size_t i = size_t(bt.x) + lane;
+  C F[J][J];
+  auto load_F = [&](int code) {
     const int lp = item_lp(code), lq = item_lq(code);
-    C F[J][J];
 #pragma unroll
     for (int jv = 0; jv < J; ++jv)
 #pragma unroll
       for (int ju = 0; ju < J; ++ju) F[jv][ju] = win[(lp + jv) * WW + lq + ju];
-    // Lanes past their item's end compute on null slots; those results are
-    // never read, so the loop has no per-lane branch.  The next slot's
-    // coverage state is loaded one iteration ahead.
-    size_t i = size_t(bt.x) + lane;
-    C t_next = bt.y > 0 ? stream_load(frac + i) : C{0, 0};
-    int m_next = (a.slot_user && bt.y > 0) ? __ldcs(a.slot_user + i) : 0;
-    for (int k = 0; k < bt.y; ++k, i += kBatch) {
-      const C t = t_next;
-      const int m = m_next;
-      if (k + 1 < bt.y) {
-        t_next = stream_load(frac + i + kBatch);
-        if (a.slot_user) m_next = __ldcs(a.slot_user + i + kBatch);
+  };
+  load_F(th.code[lb * kBatch + lane]);
+  C t_next = stream_load(frac + i);
+  int m_next = a.slot_user ? __ldcs(a.slot_user + i) : 0;
+  while (true) {
+    const C t = t_next;
+    const int m = m_next;
+    const size_t i_cur = i;
+    // advance to the next slot of this warp
+    bool new_batch = false;
+    if (k + 1 < bt.y) {
+      ++k;
+      i += kBatch;
+    } else {
+      lb += nw;
+      new_batch = true;
+      if (lb < nbt) {
+        bt = th.hdr[lb];
+        k = 0;
+        i = size_t(bt.x) + lane;
       }
-      real ku[J], kv[J];
-      tap_weights<real, J, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
-      tap_weights<real, J, SUB>(poly.v, poly.nsub_v, t.y, kv);
-      real sr = 0, si = 0;
-#pragma unroll
-      for (int jv = 0; jv < J; ++jv) {
-        real rr = 0, ri = 0;
-#pragma unroll
-        for (int ju = 0; ju < J; ++ju) {
-          rr = fma(ku[ju], F[jv][ju].x, rr);
-          ri = fma(ku[ju], F[jv][ju].y, ri);
-        }
-        sr = fma(kv[jv], rr, sr);
-        si = fma(kv[jv], ri, si);
-      }
-      C y;
-      if (unit) {
-        const real sg = copysign(real(1), t.x);
-        y.x = sg * sr;
-        y.y = sg * si;
-      } else {
-        const C w = stream_load(weight + i);
-        y.x = sr * w.x - si * w.y;
-        y.y = sr * w.y + si * w.x;
-      }
-      if (!a.slot_user)
-        out[i] = y;
-      else if (m >= 0)
-        out[m] = y;
     }
+    const bool more = !new_batch || lb < nbt;
+    if (more) {
+      t_next = stream_load(frac + i);
+      if (a.slot_user) m_next = __ldcs(a.slot_user + i);
+    }
+    real ku[J], kv[J];
+    tap_weights<real, J, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
+    tap_weights<real, J, SUB>(poly.v, poly.nsub_v, t.y, kv);
+    real sr = 0, si = 0;
+#pragma unroll
+    for (int jv = 0; jv < J; ++jv) {
+      real rr = 0, ri = 0;
+#pragma unroll
+      for (int ju = 0; ju < J; ++ju) {
+        rr = fma(ku[ju], F[jv][ju].x, rr);
+        ri = fma(ku[ju], F[jv][ju].y, ri);
+      }
+      sr = fma(kv[jv], rr, sr);
+      si = fma(kv[jv], ri, si);
+    }
+    C y;
+    if (unit) {
+      const real sg = copysign(real(1), t.x);
+      y.x = sg * sr;
+      y.y = sg * si;
+    } else {
+      const C w = stream_load(weight + i_cur);
+      y.x = sr * w.x - si * w.y;
+      y.y = sr * w.y + si * w.x;
+    }
+    if (!a.slot_user)
+      out[i_cur] = y;
+    else if (m >= 0)
+      out[m] = y;
+    if (!more) break;
+    if (new_batch) load_F(th.code[lb * kBatch + lane]);
   }
 }
 
@@ -150,52 +204,54 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a,
                                                    const __grid_constant__ PolyTable<real> poly) {
   using C = cplx<real>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C *wins = reinterpret_cast<C *>(smem_raw);
   const Task tk = a.tasks[blockIdx.x];
   const int WW = tk.W + J - 1, WH = tk.H + J - 1, WN = WW * WH;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  C *wins = reinterpret_cast<C *>(smem_raw);
+  const TaskHeaders th = load_headers(a, tk, smem_raw + a.win_bytes);
   for (int idx = threadIdx.x; idx < nw * WN; idx += blockDim.x) wins[idx] = C{0, 0};
   __syncthreads();
   C *mine = wins + warp * WN;
+  const int nbt = tk.batch_end - tk.batch_begin;
   const C *frac = static_cast<const C *>(a.frac);
   const C *weight = static_cast<const C *>(a.weight);
   const C *vin = static_cast<const C *>(a.slot_in);
   const bool unit = weight == nullptr;
-  for (int b = tk.batch_begin + warp; b < tk.batch_end; b += nw) {
-    const int2 bt = a.batches[b];
-    const int code = a.lane_code[size_t(b) * kBatch + lane];
-    const int cnt = item_count(code);
-    const int lp = item_lp(code), lq = item_lq(code);
+  int lb = warp;
+  if (lb < nbt) {
+    int2 bt = th.hdr[lb];
+    int code = th.code[lb * kBatch + lane];
+    int k = 0;
+    size_t i = size_t(bt.x) + lane;
     C acc[J][J];
 #pragma unroll
     for (int jv = 0; jv < J; ++jv)
 #pragma unroll
       for (int ju = 0; ju < J; ++ju) acc[jv][ju] = C{0, 0};
-    // Null slots hold a zero visibility, so they add nothing.  The next
-    // slot's state is loaded one iteration ahead.
-    size_t i = size_t(bt.x) + lane;
-    C t_next{0, 0}, y_next{0, 0};
-    if (bt.y > 0) {
-      t_next = stream_load(frac + i);
-      if (a.slot_user) {
-        const int m = __ldcs(a.slot_user + i);
-        y_next = m >= 0 ? vin[m] : C{0, 0};
-      } else {
-        y_next = vin[i];
-      }
-    }
-    for (int k = 0; k < bt.y; ++k, i += kBatch) {
+    C t_next = stream_load(frac + i);
+    C y_next = read_vis(a, vin, i);
+    while (true) {
       const C t = t_next;
       const C yv = y_next;
+      const size_t i_cur = i;
+      bool new_batch = false;
       if (k + 1 < bt.y) {
-        t_next = stream_load(frac + i + kBatch);
-        if (a.slot_user) {
-          const int m = __ldcs(a.slot_user + i + kBatch);
-          y_next = m >= 0 ? vin[m] : C{0, 0};
-        } else {
-          y_next = vin[i + kBatch];
-        }
+        ++k;
+        i += kBatch;
+      } else {
+        new_batch = true;
       }
+      int2 bt_next = bt;
+      if (new_batch && lb + nw < nbt) {
+        bt_next = th.hdr[lb + nw];
+        i = size_t(bt_next.x) + lane;
+      }
+      const bool more = !new_batch || lb + nw < nbt;
+      if (more) {
+        t_next = stream_load(frac + i);
+        y_next = read_vis(a, vin, i);
+      }
+      // Null slots hold a zero visibility, so they add nothing.
       real zr, zi;
       if (unit) {
         const real sg = copysign(real(1), t.x);
@@ -203,7 +259,7 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a,
         zi = sg * yv.y;
       } else {
         // conj(weight) * y: G^H holds the conjugated entries of G.
-        const C w = stream_load(weight + i);
+        const C w = stream_load(weight + i_cur);
         zr = w.x * yv.x + w.y * yv.y;
         zi = w.x * yv.y - w.y * yv.x;
       }
@@ -219,23 +275,34 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a,
           acc[jv][ju].y = fma(ai, ku[ju], acc[jv][ju].y);
         }
       }
-    }
-    // Flush.  The items of one batch have distinct base cells, so at each
-    // (jv, ju) step the 32 lanes update 32 distinct cells; steps are ordered
-    // by __syncwarp, which makes the summation order a function of the plan.
+      if (new_batch) {
+        // Flush.  The items of one batch have distinct base cells, so at each
+        // (jv, ju) step the 32 lanes update 32 distinct cells; steps are
+        // ordered by __syncwarp, which makes the summation order a function
+        // of the plan.
+        const int cnt = item_count(code);
+        const int lp = item_lp(code), lq = item_lq(code);
 #pragma unroll
-    for (int jv = 0; jv < J; ++jv)
+        for (int jv = 0; jv < J; ++jv)
 #pragma unroll
-      for (int ju = 0; ju < J; ++ju) {
-        if (cnt > 0) {
-          C *cell = mine + (lp + jv) * WW + lq + ju;
-          C c = *cell;
-          c.x += acc[jv][ju].x;
-          c.y += acc[jv][ju].y;
-          *cell = c;
-        }
-        __syncwarp();
+          for (int ju = 0; ju < J; ++ju) {
+            if (cnt > 0) {
+              C *cell = mine + (lp + jv) * WW + lq + ju;
+              C c = *cell;
+              c.x += acc[jv][ju].x;
+              c.y += acc[jv][ju].y;
+              *cell = c;
+            }
+            acc[jv][ju] = C{0, 0};
+            __syncwarp();
+          }
+        lb += nw;
+        if (!more) break;
+        bt = bt_next;
+        code = th.code[lb * kBatch + lane];
+        k = 0;
       }
+    }
   }
   __syncthreads();
   C *out = static_cast<C *>(a.tilebuf) + size_t(blockIdx.x) * a.slot_stride;
@@ -269,37 +336,57 @@ __global__ void expand_kernel(const cplx<real> *__restrict__ in,
   }
 }
 
-template <typename real>
-__device__ __forceinline__ void add_tile(const FoldArgs &f, int ta, int tb, int r, int c,
-                                         cplx<real> &s) {
-  const cplx<real> *buf = static_cast<const cplx<real> *>(f.tilebuf);
-  const int t = ta * f.ntu + tb;
-  const int WW = (f.tu_start[tb + 1] - f.tu_start[tb]) + f.Ju - 1;
-  for (int k = f.tile_tasks[t]; k < f.tile_tasks[t + 1]; ++k) {
-    const cplx<real> v = buf[size_t(k) * f.slot_stride + size_t(r) * WW + c];
-    s.x += v.x;
-    s.y += v.y;
-  }
-}
-
+// One CTA per tile.  A cell sums, in this order, the windows of its own
+// tile's tasks, then those of the tile above, the tile to the left and the
+// tile above-left, where their J - 1 halo rows / columns reach into it.
 template <typename real>
 __global__ void fold_kernel(const FoldArgs f) {
-  const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (idx >= int64_t(f.Nu) * f.Nv) return;
-  const int p = int(idx / f.Nu), q = int(idx - int64_t(p) * f.Nu);
-  const int a = f.tv_of[p], b = f.tu_of[q];
-  const int lp = p - f.tv_start[a], lq = q - f.tu_start[b];
-  cplx<real> s{0, 0};
-  add_tile<real>(f, a, b, lp, lq, s);
-  const bool up = lp < f.Jv - 1, left = lq < f.Ju - 1;
+  using C = cplx<real>;
+  const int t = blockIdx.x;
+  const int a = t / f.ntu, b = t - (t / f.ntu) * f.ntu;
   const int a2 = a == 0 ? f.ntv - 1 : a - 1;
   const int b2 = b == 0 ? f.ntu - 1 : b - 1;
-  const int hp = f.tv_start[a2 + 1] - f.tv_start[a2];
-  const int wp = f.tu_start[b2 + 1] - f.tu_start[b2];
-  if (up) add_tile<real>(f, a2, b, lp + hp, lq, s);
-  if (left) add_tile<real>(f, a, b2, lp, lq + wp, s);
-  if (up && left) add_tile<real>(f, a2, b2, lp + hp, lq + wp, s);
-  static_cast<cplx<real> *>(f.grid)[idx] = s;
+  const int P = f.tv_start[a], Q = f.tu_start[b];
+  const int H = f.tv_start[a + 1] - P, W = f.tu_start[b + 1] - Q;
+  const int Hu = f.tv_start[a2 + 1] - f.tv_start[a2];  // height of the tile above
+  const int Wl = f.tu_start[b2 + 1] - f.tu_start[b2];  // width of the tile to the left
+  const int WWo = W + f.Ju - 1, WWl = Wl + f.Ju - 1;
+  const int tu = a2 * f.ntu + b, tl = a * f.ntu + b2, td = a2 * f.ntu + b2;
+  const int own0 = f.tile_tasks[t], own1 = f.tile_tasks[t + 1];
+  const int up0 = f.tile_tasks[tu], up1 = f.tile_tasks[tu + 1];
+  const int lf0 = f.tile_tasks[tl], lf1 = f.tile_tasks[tl + 1];
+  const int dg0 = f.tile_tasks[td], dg1 = f.tile_tasks[td + 1];
+  const C *buf = static_cast<const C *>(f.tilebuf);
+  C *grid = static_cast<C *>(f.grid);
+  for (int idx = threadIdx.x; idx < H * W; idx += blockDim.x) {
+    const int lp = idx / W, lq = idx - lp * W;
+    C s{0, 0};
+    for (int k = own0; k < own1; ++k) {
+      const C v = buf[size_t(k) * f.slot_stride + lp * WWo + lq];
+      s.x += v.x;
+      s.y += v.y;
+    }
+    const bool up = lp < f.Jv - 1, left = lq < f.Ju - 1;
+    if (up)
+      for (int k = up0; k < up1; ++k) {
+        const C v = buf[size_t(k) * f.slot_stride + (lp + Hu) * WWo + lq];
+        s.x += v.x;
+        s.y += v.y;
+      }
+    if (left)
+      for (int k = lf0; k < lf1; ++k) {
+        const C v = buf[size_t(k) * f.slot_stride + lp * WWl + lq + Wl];
+        s.x += v.x;
+        s.y += v.y;
+      }
+    if (up && left)
+      for (int k = dg0; k < dg1; ++k) {
+        const C v = buf[size_t(k) * f.slot_stride + (lp + Hu) * WWl + lq + Wl];
+        s.x += v.x;
+        s.y += v.y;
+      }
+    grid[size_t(P + lp) * f.Nu + Q + lq] = s;
+  }
 }
 
 template <typename real>
@@ -440,13 +527,20 @@ cudaError_t launch_apply(bool degrid, const ApplyArgs<real> &a, const PolyTable<
 
 }  // namespace
 
+size_t window_bytes(int precision_bytes, int win_rows, int win_cols, const LaunchShape &shape,
+                    bool per_warp) {
+  const size_t one = size_t(win_rows) * win_cols * 2 * precision_bytes;
+  const size_t b = per_warp ? one * size_t(shape.threads / 32) : one;
+  return (b + 15) / 16 * 16;
+}
+constexpr size_t kHeaderBytes = kMaxTaskBatches * (sizeof(int2) + kBatch * sizeof(int));
 size_t degrid_smem_bytes(int precision_bytes, int, int win_rows, int win_cols,
-                         const LaunchShape &) {
-  return size_t(win_rows) * win_cols * 2 * precision_bytes;
+                         const LaunchShape &shape) {
+  return window_bytes(precision_bytes, win_rows, win_cols, shape, false) + kHeaderBytes;
 }
 size_t grid_smem_bytes(int precision_bytes, int, int win_rows, int win_cols,
                        const LaunchShape &shape) {
-  return size_t(shape.threads / 32) * win_rows * win_cols * 2 * precision_bytes;
+  return window_bytes(precision_bytes, win_rows, win_cols, shape, true) + kHeaderBytes;
 }
 
 template <typename real>
@@ -454,21 +548,23 @@ cudaError_t launch_degrid(const ApplyArgs<real> &a, const PolyTable<real> &poly,
                           int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
                           cudaStream_t s) {
   const size_t smem = degrid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape);
-  return launch_apply<real>(true, a, poly, J, ntasks, smem, shape.threads, s);
+  ApplyArgs<real> b = a;
+  b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, false));
+  return launch_apply<real>(true, b, poly, J, ntasks, smem, shape.threads, s);
 }
 template <typename real>
 cudaError_t launch_grid(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
                         int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
                         cudaStream_t s) {
   const size_t smem = grid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape);
-  return launch_apply<real>(false, a, poly, J, ntasks, smem, shape.threads, s);
+  ApplyArgs<real> b = a;
+  b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, true));
+  return launch_apply<real>(false, b, poly, J, ntasks, smem, shape.threads, s);
 }
 
 template <typename real>
 cudaError_t launch_fold(const FoldArgs &f, cudaStream_t s) {
-  const int64_t n = int64_t(f.Nu) * f.Nv;
-  const int threads = 256;
-  fold_kernel<real><<<int((n + threads - 1) / threads), threads, 0, s>>>(f);
+  fold_kernel<real><<<f.ntu * f.ntv, 256, 0, s>>>(f);
   return cudaGetLastError();
 }
 

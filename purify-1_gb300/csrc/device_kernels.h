@@ -30,6 +30,7 @@ struct ApplyArgs {
   const int32_t *slot_user = nullptr;
   int Nu = 0, Nv = 0;
   int64_t slot_stride = 0;          // complex elements per tilebuf slot
+  int win_bytes = 0;  // set by the launchers: shared bytes before the batch headers
 };
 
 struct LaunchShape {

@@ -228,7 +228,7 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
     throw Error(kInvalidArgument, e.what());
   }
   shape_.threads = cfg.threads > 0 ? cfg.threads : 128;
-  fused_permute_ = cfg.fused_permute != 0;
+  fused_permute_ = cfg.fused_permute == 1;
   ntasks_ = int(plan.tasks.size());
   win_rows_ = plan.win_rows;
   win_cols_ = plan.win_cols;

@@ -42,7 +42,7 @@ struct OperatorConfig {
   int tile = 0;
   // 1: degrid/grid read and write caller-ordered visibilities directly;
   // 0: through a slot-ordered buffer and separate gather kernels;
-  // -1: choose (currently: direct).
+  // -1: default (the gather kernels; measured faster on the benchmark workload).
   int fused_permute = -1;
 };
 

@@ -47,6 +47,8 @@ constexpr int kCoefF64 = 17;
 constexpr int kTile = 32;
 // Lanes per batch: every batch holds 32 work items, one per lane.
 constexpr int kBatch = 32;
+// Most batches one CTA task may hold (its headers are staged in shared memory).
+constexpr int kMaxTaskBatches = 64;
 
 // One CTA work unit.  A tile is the rectangle [P, P+H) x [Q, Q+W) of base
 // cells; its grid window is (H + J - 1) x (W + J - 1) cells starting at (P, Q),

@@ -45,6 +45,8 @@ Plan build_plan(const PlanRequest &rq) {
   if (rq.max_per_item < 1 || rq.max_per_item > 0xffff)
     throw std::invalid_argument("max_per_item out of range");
   if (rq.tile < 1 || rq.tile > 255) throw std::invalid_argument("tile edge out of range");
+  if (rq.max_batches_per_task < 1 || rq.max_batches_per_task > kMaxTaskBatches)
+    throw std::invalid_argument("max_batches_per_task out of range");
 
   Plan P;
   P.M = rq.M;

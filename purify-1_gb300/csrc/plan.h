@@ -26,7 +26,7 @@ struct PlanRequest {
   int Ju = 4, Jv = 4;  // taps per axis
   int tile = kTile;
   int max_per_item = 16;         // visibilities of one cell handled by one lane
-  int max_batches_per_task = 64;
+  int max_batches_per_task = kMaxTaskBatches;
   int64_t max_slots_per_task = 16384;
 };
 
