@@ -357,27 +357,12 @@ int purify_gb300_kernel_taps(int32_t kernel, uint32_t J, double os, int32_t prec
     const pg::AxisFit fit = pg::fit_axis(k, int(J), nc);
     if (fit_error) *fit_error = fit.max_error;
     for (int64_t q = 0; q < n; ++q) {
-      for (uint32_t j = 0; j < J; ++j) {
-        int s = 0;
-        double x;
-        if (fit.nsub > 1) {
-          const double ts = f64 ? t[q] * fit.nsub : double(float(t[q]) * float(fit.nsub));
-          s = std::min(int(ts), fit.nsub - 1);
-          x = f64 ? 2 * (ts - s) - 1 : double(2.0f * (float(ts) - float(s)) - 1.0f);
-        } else {
-          x = f64 ? 2 * t[q] - 1 : double(2.0f * float(t[q]) - 1.0f);
-        }
-        const double *c = &fit.coef[(size_t(j) * fit.nsub + s) * nc];
-        if (f64) {
-          double acc = c[nc - 1];
-          for (int k2 = nc - 2; k2 >= 0; --k2) acc = std::fma(acc, x, c[k2]);
-          out[q * J + j] = acc;
-        } else {
-          float acc = float(c[nc - 1]);
-          const float xf = float(x);
-          for (int k2 = nc - 2; k2 >= 0; --k2) acc = std::fma(acc, xf, float(c[k2]));
-          out[q * J + j] = acc;
-        }
+      if (f64) {
+        pg::eval_taps<double>(fit, int(J), t[q], out + q * J);
+      } else {
+        float kf[pg::kMaxJ];
+        pg::eval_taps<float>(fit, int(J), t[q], kf);
+        for (uint32_t j = 0; j < J; ++j) out[q * J + j] = kf[j];
       }
     }
   });

@@ -37,25 +37,42 @@ using cplx = typename Cplx<real>::type;
 
 // Tap weights of one axis by Horner's rule.  With SUB = false every lane
 // reads the same coefficient at the same time, so the coefficients come
-// straight from the constant bank of the kernel parameters.
+// straight from the constant bank of the kernel parameters.  Every kernel of
+// the family is even, so tap J-1-j at x is (-1)^(J-1) times tap j at -x: the
+// pair shares one evaluation split into even and odd parts,
+// P_j(x) = E(x^2) + x O(x^2), P_{J-1-j}(x) = (-1)^(J-1) (E(x^2) - x O(x^2)).
 template <typename real, int J, bool SUB, int NC>
 __device__ __forceinline__ void tap_weights(const PolyAxis<real, NC> &P, int nsub, real t,
                                             real (&k)[J]) {
-  int s = 0;
-  real x;
   if (SUB) {
     const real ts = t * real(nsub);
-    s = min(int(ts), nsub - 1);
-    x = real(2) * (ts - real(s)) - real(1);
-  } else {
-    x = real(2) * t - real(1);
+    const int s = min(int(ts), nsub - 1);
+    const real x = real(2) * (ts - real(s)) - real(1);
+#pragma unroll
+    for (int j = 0; j < J; ++j) {
+      real acc = P.c[j][s][NC - 1];
+#pragma unroll
+      for (int c = NC - 2; c >= 0; --c) acc = fma(acc, x, P.c[j][s][c]);
+      k[j] = acc;
+    }
+    return;
   }
+  const real x = real(2) * t - real(1);
+  const real x2 = x * x;
+  constexpr int NE = (NC + 1) / 2, NO = NC / 2;  // even / odd coefficient counts
 #pragma unroll
-  for (int j = 0; j < J; ++j) {
-    real acc = P.c[j][s][NC - 1];
+  for (int j = 0; j < (J + 1) / 2; ++j) {
+    real e = P.c[j][0][2 * (NE - 1)];
 #pragma unroll
-    for (int c = NC - 2; c >= 0; --c) acc = fma(acc, x, P.c[j][s][c]);
-    k[j] = acc;
+    for (int c = NE - 2; c >= 0; --c) e = fma(e, x2, P.c[j][0][2 * c]);
+    real o = P.c[j][0][2 * NO - 1];
+#pragma unroll
+    for (int c = NO - 2; c >= 0; --c) o = fma(o, x2, P.c[j][0][2 * c + 1]);
+    k[j] = fma(x, o, e);
+    if (J - 1 - j != j) {
+      const real mirror = fma(-x, o, e);
+      k[J - 1 - j] = (J % 2 == 1) ? mirror : -mirror;
+    }
   }
 }
 

@@ -170,7 +170,7 @@ def test_power_method_matches_oracle(pg, oracle_mod, cuda, small_config, precisi
     # then differ only by arithmetic precision
     n_gpu = gop.power_method(100, 0.0)
     n_ref = oop.power_method(100, 0.0)
-    assert abs(n_gpu - n_ref) / n_ref < (1e-6 if precision == "fp32" else 1e-12)
+    assert abs(n_gpu - n_ref) / n_ref < (1e-5 if precision == "fp32" else 1e-12)
     if precision == "fp64":  # and the same stopping round with the reference's rule
         assert abs(gop.power_method(100, 1e-4) - oop.power_method(100, 1e-4)) / n_ref < 1e-12
     # the normalised operator has ||Phi^H Phi|| = 1 (operators.cc:147-154): a
