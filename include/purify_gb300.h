@@ -100,8 +100,6 @@ typedef struct {
   int32_t tile;          /* uv tile edge in grid cells (<= 255) */
   int32_t fused_permute; /* 1: degrid/grid touch caller-ordered visibilities directly,
                             0: via a slot-ordered buffer and gather kernels, -1: default */
-  int32_t const_poly;    /* 1: kernel polynomial from the constant-bank table, 0: from the
-                            kernel parameters, -1: default (1) */
 } purify_gb300_tuning;
 int purify_gb300_operator_create_tuned(const purify_gb300_create_args *args,
                                        const purify_gb300_tuning *tuning,

@@ -105,7 +105,6 @@ int purify_gb300_operator_create_tuned(const purify_gb300_create_args *a,
       c.max_per_item = t->max_per_item;
       c.tile = t->tile;
       c.fused_permute = t->fused_permute;
-      c.const_poly = t->const_poly < 0 ? 1 : t->const_poly;
     }
     if (a->precision != PURIFY_GB300_FP32 && a->precision != PURIFY_GB300_FP64)
       throw pg::Error(pg::kInvalidArgument, "unknown precision");

@@ -35,25 +35,6 @@ struct Cplx<double> {
 template <typename real>
 using cplx = typename Cplx<real>::type;
 
-// Kernel-polynomial tables in the constant bank.  Read at compile-time
-// offsets they are plain constant operands of the FMAs.  One table per
-// precision; the host orders updates after the last launch that read it.
-__constant__ PolyTable<float> g_poly_f32;
-__constant__ PolyTable<double> g_poly_f64;
-template <typename real>
-__device__ __forceinline__ const PolyTable<real> &const_poly();
-template <>
-__device__ __forceinline__ const PolyTable<float> &const_poly<float>() {
-  return g_poly_f32;
-}
-template <>
-__device__ __forceinline__ const PolyTable<double> &const_poly<double>() {
-  return g_poly_f64;
-}
-
-// Coefficient sources of the degrid / grid kernels.
-enum CoefSource { kParamSmooth = 0, kParamSub = 1, kConstSmooth = 2 };
-
 // Tap weights of one axis by Horner's rule.  With SUB = false every lane
 // reads the same coefficient at the same time, so the coefficients come
 // straight from the constant bank of the kernel parameters.  Every kernel of
@@ -133,12 +114,10 @@ __device__ __forceinline__ cplx<real> read_vis(const ApplyArgs<real> &a, const c
   return vin[i];
 }
 
-template <typename real, int J, int CS>
+template <typename real, int J, bool SUB>
 __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a,
-                                                     const __grid_constant__ PolyTable<real> param_poly) {
+                                                     const __grid_constant__ PolyTable<real> poly) {
   using C = cplx<real>;
-  constexpr bool SUB = CS == kParamSub;
-  const PolyTable<real> &poly = CS == kConstSmooth ? const_poly<real>() : param_poly;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Task tk = a.tasks[blockIdx.x];
   const int WW = tk.W + J - 1, WH = tk.H + J - 1;
@@ -237,12 +216,10 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a,
   }
 }
 
-template <typename real, int J, int CS>
+template <typename real, int J, bool SUB>
 __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a,
-                                                   const __grid_constant__ PolyTable<real> param_poly) {
+                                                   const __grid_constant__ PolyTable<real> poly) {
   using C = cplx<real>;
-  constexpr bool SUB = CS == kParamSub;
-  const PolyTable<real> &poly = CS == kConstSmooth ? const_poly<real>() : param_poly;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Task tk = a.tasks[blockIdx.x];
   const int WW = tk.W + J - 1, WH = tk.H + J - 1, WN = WW * WH;
@@ -529,10 +506,10 @@ int stream_blocks(int64_t n, int threads) {
 // Dispatch on the support J (templated so the J x J block stays in registers)
 // and on whether the kernel polynomial has sub-segments (narrow kernels, PSWF).
 
-template <typename real, int J, int CS>
+template <typename real, int J, bool SUB>
 cudaError_t launch_one(bool degrid, const ApplyArgs<real> &a, const PolyTable<real> &poly,
                        int ntasks, size_t smem, int threads, cudaStream_t s) {
-  auto fn = degrid ? degrid_kernel<real, J, CS> : grid_kernel<real, J, CS>;
+  auto fn = degrid ? degrid_kernel<real, J, SUB> : grid_kernel<real, J, SUB>;
   if (smem > 48 * 1024) {
     const cudaError_t e =
         cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
@@ -544,19 +521,13 @@ cudaError_t launch_one(bool degrid, const ApplyArgs<real> &a, const PolyTable<re
 
 template <typename real>
 cudaError_t launch_apply(bool degrid, const ApplyArgs<real> &a, const PolyTable<real> &poly,
-                         int J, int ntasks, size_t smem, int threads, bool const_bank,
-                         cudaStream_t s) {
+                         int J, int ntasks, size_t smem, int threads, cudaStream_t s) {
   if (ntasks == 0) return cudaSuccess;
-  const int cs = (poly.nsub_u > 1 || poly.nsub_v > 1) ? kParamSub
-                 : const_bank                         ? kConstSmooth
-                                                      : kParamSmooth;
-#define PG_CASE(JJ)                                                                          \
-  case JJ:                                                                                   \
-    if (cs == kParamSub)                                                                     \
-      return launch_one<real, JJ, kParamSub>(degrid, a, poly, ntasks, smem, threads, s);     \
-    if (cs == kConstSmooth)                                                                  \
-      return launch_one<real, JJ, kConstSmooth>(degrid, a, poly, ntasks, smem, threads, s);  \
-    return launch_one<real, JJ, kParamSmooth>(degrid, a, poly, ntasks, smem, threads, s);
+  const bool sub = poly.nsub_u > 1 || poly.nsub_v > 1;
+#define PG_CASE(JJ)                                                                    \
+  case JJ:                                                                             \
+    return sub ? launch_one<real, JJ, true>(degrid, a, poly, ntasks, smem, threads, s) \
+               : launch_one<real, JJ, false>(degrid, a, poly, ntasks, smem, threads, s);
   switch (J) {
     PG_CASE(1)
     PG_CASE(2)
@@ -596,7 +567,7 @@ cudaError_t launch_degrid(const ApplyArgs<real> &a, const PolyTable<real> &poly,
   const size_t smem = degrid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape);
   ApplyArgs<real> b = a;
   b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, false));
-  return launch_apply<real>(true, b, poly, J, ntasks, smem, shape.threads, shape.const_bank, s);
+  return launch_apply<real>(true, b, poly, J, ntasks, smem, shape.threads, s);
 }
 template <typename real>
 cudaError_t launch_grid(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
@@ -605,18 +576,7 @@ cudaError_t launch_grid(const ApplyArgs<real> &a, const PolyTable<real> &poly, i
   const size_t smem = grid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape);
   ApplyArgs<real> b = a;
   b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, true));
-  return launch_apply<real>(false, b, poly, J, ntasks, smem, shape.threads, shape.const_bank, s);
-}
-
-template <typename real>
-cudaError_t upload_const_poly(const PolyTable<real> *host, cudaStream_t s) {
-  const void *sym = nullptr;
-  if (sizeof(real) == sizeof(float))
-    sym = static_cast<const void *>(&g_poly_f32);
-  else
-    sym = static_cast<const void *>(&g_poly_f64);
-  return cudaMemcpyToSymbolAsync(sym, host, sizeof(PolyTable<real>), 0, cudaMemcpyHostToDevice,
-                                 s);
+  return launch_apply<real>(false, b, poly, J, ntasks, smem, shape.threads, s);
 }
 
 template <typename real>
@@ -707,7 +667,6 @@ cudaError_t launch_fill(void *x, int64_t n, double value, cudaStream_t s) {
   template cudaError_t launch_grid<real>(const ApplyArgs<real> &, const PolyTable<real> &, int,   \
                                          int, int, int, const LaunchShape &, cudaStream_t);     \
   template cudaError_t launch_fold<real>(const FoldArgs &, cudaStream_t);                       \
-  template cudaError_t upload_const_poly<real>(const PolyTable<real> *, cudaStream_t);          \
   template cudaError_t launch_pad<real>(const void *, const real *, const real *, void *, int,  \
                                         int, int, int, int, cudaStream_t);                      \
   template cudaError_t launch_crop<real>(const void *, const real *, const real *, void *, int, \

@@ -34,14 +34,8 @@ struct ApplyArgs {
 };
 
 struct LaunchShape {
-  int threads = 128;       // 32 x warps per CTA
-  bool const_bank = true;  // kernel polynomial from the constant-bank table
+  int threads = 128;  // 32 x warps per CTA
 };
-
-// Copies a kernel-polynomial table into the constant-bank table of its
-// precision, ordered on `s`.  `host` must be pinned and outlive the copy.
-template <typename real>
-cudaError_t upload_const_poly(const PolyTable<real> *host, cudaStream_t s);
 
 // Largest dynamic shared memory a launch of the given shape needs, in bytes.
 size_t degrid_smem_bytes(int precision_bytes, int J, int win_rows, int win_cols,

@@ -6,8 +6,6 @@
 #include <cmath>
 #include <complex>
 #include <cstring>
-#include <atomic>
-#include <map>
 #include <mutex>
 #include <vector>
 
@@ -76,17 +74,6 @@ class DeviceGuard {
  private:
   int prev_ = 0, dev_ = 0;
 };
-
-// The constant-bank polynomial table of each precision is one per device and
-// process.  An operator that launches with it first waits for the last launch
-// that read another operator's table, then replaces it.
-struct ConstTableState {
-  uint64_t owner = 0;
-  cudaEvent_t last = nullptr;
-};
-std::mutex g_const_mu;
-std::map<std::pair<int, int>, ConstTableState> g_const_tables;  // (device, bytes of real)
-std::atomic<uint64_t> g_operator_ids{1};
 
 template <typename real>
 struct Traits;
@@ -162,12 +149,6 @@ class OperatorT final : public Operator {
   int64_t M_ = 0, N_ = 0, S_ = 0;
   bool unit_weights_ = true;
   bool fused_permute_ = true;
-  uint64_t id_ = 0;
-  PolyTable<real> *poly_pinned_ = nullptr;  // host copy for the constant-bank upload
-  // Holds g_const_mu while a launch that reads the constant-bank table is
-  // enqueued; the table is (re)loaded first when another operator owns it.
-  void acquire_const_table(std::unique_lock<std::mutex> &lk);
-  void release_const_table(std::unique_lock<std::mutex> &lk);
   double norm_ = 1.0;
   std::vector<double> su_, sv_;  // 1 / ft kernel at the image pixels (unscaled)
   std::vector<real> su_scaled_, sv_real_;
@@ -247,8 +228,6 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
     throw Error(kInvalidArgument, e.what());
   }
   shape_.threads = cfg.threads > 0 ? cfg.threads : 128;
-  shape_.const_bank = cfg.const_poly != 0;
-  id_ = g_operator_ids.fetch_add(1);
   fused_permute_ = cfg.fused_permute == 1;
   ntasks_ = int(plan.tasks.size());
   win_rows_ = plan.win_rows;
@@ -317,9 +296,6 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
     // The staging vectors above are pageable; wait before they go out of scope.
     cuda_check(cudaStreamSynchronize(stream_), "upload");
   }
-  cuda_check(cudaMallocHost(reinterpret_cast<void **>(&poly_pinned_), sizeof(PolyTable<real>)),
-             "cudaMallocHost");
-  std::memcpy(static_cast<void *>(poly_pinned_), &poly_, sizeof(PolyTable<real>));
   cufft_check(cufftPlan2d(&fft_, Nv_, Nu_, Traits<real>::kType), "cufftPlan2d");
   fft_ok_ = true;
   cufft_check(cufftSetStream(fft_, stream_), "cufftSetStream");
@@ -351,12 +327,6 @@ template <typename real>
 OperatorT<real>::~OperatorT() {
   if (stream_) cudaStreamSynchronize(stream_);
   for (cudaEvent_t e : event_pool_) cudaEventDestroy(e);
-  {
-    std::lock_guard<std::mutex> lk(g_const_mu);
-    auto it = g_const_tables.find({device_, int(sizeof(real))});
-    if (it != g_const_tables.end() && it->second.owner == id_) it->second.owner = 0;
-  }
-  if (poly_pinned_) cudaFreeHost(poly_pinned_);
   if (fft_ok_) cufftDestroy(fft_);
   if (ev_in_) cudaEventDestroy(ev_in_);
   if (ev_out_) cudaEventDestroy(ev_out_);
@@ -410,13 +380,10 @@ void OperatorT<real>::degrid_slots(const void *grid, void *caller_vis) {
   a.slot_user = caller_vis ? slot_user_.as<int32_t>() : nullptr;
   a.Nu = Nu_;
   a.Nv = Nv_;
-  std::unique_lock<std::mutex> lk;
-  acquire_const_table(lk);
   mark_begin(kDegrid);
   cuda_check(launch_degrid<real>(a, poly_, J_, ntasks_, win_rows_, win_cols_, shape_, stream_),
              "degrid");
   mark_end(kDegrid);
-  release_const_table(lk);
 }
 
 template <typename real>
@@ -433,13 +400,10 @@ void OperatorT<real>::grid_slots(void *grid, const void *caller_vis) {
   a.Nu = Nu_;
   a.Nv = Nv_;
   a.slot_stride = slot_stride_;
-  std::unique_lock<std::mutex> lk;
-  acquire_const_table(lk);
   mark_begin(kGrid);
   cuda_check(launch_grid<real>(a, poly_, J_, ntasks_, win_rows_, win_cols_, shape_, stream_),
              "grid");
   mark_end(kGrid);
-  release_const_table(lk);
   FoldArgs f;
   f.tilebuf = tilebuf_.get();
   f.slot_stride = slot_stride_;
@@ -685,26 +649,6 @@ double OperatorT<real>::power_method(int iters, double tol) {
   }
   set_norm(result);
   return result;
-}
-
-template <typename real>
-void OperatorT<real>::acquire_const_table(std::unique_lock<std::mutex> &lk) {
-  if (!shape_.const_bank || poly_.nsub_u > 1 || poly_.nsub_v > 1 || ntasks_ == 0) return;
-  lk = std::unique_lock<std::mutex>(g_const_mu);
-  ConstTableState &st = g_const_tables[{device_, int(sizeof(real))}];
-  if (!st.last) cuda_check(cudaEventCreateWithFlags(&st.last, cudaEventDisableTiming), "event");
-  if (st.owner != id_) {
-    cuda_check(cudaStreamWaitEvent(stream_, st.last, 0), "cudaStreamWaitEvent");
-    cuda_check(upload_const_poly<real>(poly_pinned_, stream_), "constant table upload");
-    st.owner = id_;
-  }
-}
-template <typename real>
-void OperatorT<real>::release_const_table(std::unique_lock<std::mutex> &lk) {
-  if (!lk.owns_lock()) return;
-  ConstTableState &st = g_const_tables[{device_, int(sizeof(real))}];
-  cuda_check(cudaEventRecord(st.last, stream_), "cudaEventRecord");
-  lk.unlock();
 }
 
 template <typename real>

@@ -44,9 +44,6 @@ struct OperatorConfig {
   // 0: through a slot-ordered buffer and separate gather kernels;
   // -1: default (the gather kernels; measured faster on the benchmark workload).
   int fused_permute = -1;
-  // 1: kernel polynomial read from the constant-bank table (default);
-  // 0: from the kernel parameters.
-  int const_poly = 1;
 };
 
 // S(j, i) = 1 / (ftv(y0 + j + 0.5) ftu(x0 + i + 0.5)) for the kernel, as

@@ -53,8 +53,7 @@ class CreateArgs(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("threads", ctypes.c_int32), ("max_per_item", ctypes.c_int32),
-                ("tile", ctypes.c_int32), ("fused_permute", ctypes.c_int32),
-                ("const_poly", ctypes.c_int32)]
+                ("tile", ctypes.c_int32), ("fused_permute", ctypes.c_int32)]
 
 
 class Info(ctypes.Structure):
@@ -249,8 +248,7 @@ class MeasurementOperator:
         h = ctypes.c_void_p()
         if tuning:
             t = Tuning(int(tuning.get("threads", 0)), int(tuning.get("max_per_item", 0)),
-                       int(tuning.get("tile", 0)), int(tuning.get("fused_permute", -1)),
-                       int(tuning.get("const_poly", -1)))
+                       int(tuning.get("tile", 0)), int(tuning.get("fused_permute", -1)))
             _check(L.purify_gb300_operator_create_tuned(ctypes.byref(a), ctypes.byref(t),
                                                         ctypes.byref(h)))
         else:
