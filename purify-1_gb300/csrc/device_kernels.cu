@@ -83,12 +83,30 @@ __device__ __forceinline__ T stream_load(const T *p) {
   return __ldcs(p);
 }
 
+// Asynchronous global -> shared copies (cp.async): a CTA issues its whole
+// prologue at once and waits one time, instead of one load latency per
+// strided loop iteration.
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void *smem, const void *gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  if (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem), "n"(BYTES)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
 // Shared-memory layout of a task: the grid window(s), then the batch
 // headers {first slot, kmax} and the 32 lane codes of each batch.
 struct TaskHeaders {
   int2 *hdr;
   int *code;
 };
+// Issues the asynchronous copies of a task's batch headers and lane codes;
+// the caller waits with cp_async_wait_all() + __syncthreads().
 template <typename A>
 __device__ __forceinline__ TaskHeaders load_headers(const A &a, const Task &tk,
                                                     unsigned char *base) {
@@ -96,9 +114,12 @@ __device__ __forceinline__ TaskHeaders load_headers(const A &a, const Task &tk,
   h.hdr = reinterpret_cast<int2 *>(base);
   h.code = reinterpret_cast<int *>(base + sizeof(int2) * kMaxTaskBatches);
   const int nbt = tk.batch_end - tk.batch_begin;
-  for (int k = threadIdx.x; k < nbt; k += blockDim.x) h.hdr[k] = a.batches[tk.batch_begin + k];
-  for (int k = threadIdx.x; k < nbt * kBatch; k += blockDim.x)
-    h.code[k] = a.lane_code[size_t(tk.batch_begin) * kBatch + k];
+  for (int k = threadIdx.x; k < nbt; k += blockDim.x)
+    cp_async<8>(h.hdr + k, a.batches + tk.batch_begin + k);
+  // lane codes: 32 ints (128 bytes) per batch, copied in 16-byte pieces
+  const int *src = a.lane_code + size_t(tk.batch_begin) * kBatch;
+  for (int k = threadIdx.x; k < nbt * (kBatch / 4); k += blockDim.x)
+    cp_async<16>(h.code + 4 * k, src + 4 * k);
   return h;
 }
 
@@ -131,8 +152,9 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a,
     if (p >= a.Nv) p -= a.Nv;
     int q = tk.Q + lq;
     if (q >= a.Nu) q -= a.Nu;
-    win[idx] = grid[size_t(p) * a.Nu + q];
+    cp_async<sizeof(C)>(win + idx, grid + size_t(p) * a.Nu + q);
   }
+  cp_async_wait_all();
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const int nbt = tk.batch_end - tk.batch_begin;
@@ -148,6 +170,7 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a,
   int2 bt = th.hdr[lb];
   int k = 0;
   size_t i = size_t(bt.x) + lane;
+  int cnt = item_count(th.code[lb * kBatch + lane]);
   C F[J][J];
   auto load_F = [&](int code) {
     const int lp = item_lp(code), lq = item_lq(code);
@@ -163,6 +186,7 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a,
     const C t = t_next;
     const int m = m_next;
     const size_t i_cur = i;
+    const bool real_slot = k < cnt;  // null slots (past the lane's item) get 0
     // advance to the next slot of this warp
     bool new_batch = false;
     if (k + 1 < bt.y) {
@@ -208,11 +232,15 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a,
       y.y = sr * w.y + si * w.x;
     }
     if (!a.slot_user)
-      out[i_cur] = y;
+      out[i_cur] = real_slot ? y : C{0, 0};
     else if (m >= 0)
       out[m] = y;
     if (!more) break;
-    if (new_batch) load_F(th.code[lb * kBatch + lane]);
+    if (new_batch) {
+      const int code = th.code[lb * kBatch + lane];
+      cnt = item_count(code);
+      load_F(code);
+    }
   }
 }
 
@@ -227,6 +255,7 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a,
   C *wins = reinterpret_cast<C *>(smem_raw);
   const TaskHeaders th = load_headers(a, tk, smem_raw + a.win_bytes);
   for (int idx = threadIdx.x; idx < nw * WN; idx += blockDim.x) wins[idx] = C{0, 0};
+  cp_async_wait_all();
   __syncthreads();
   C *mine = wins + warp * WN;
   const int nbt = tk.batch_end - tk.batch_begin;
@@ -373,9 +402,9 @@ __global__ void fold_kernel(const FoldArgs f) {
   const int up0 = f.tile_tasks[tu], up1 = f.tile_tasks[tu + 1];
   const int lf0 = f.tile_tasks[tl], lf1 = f.tile_tasks[tl + 1];
   const int dg0 = f.tile_tasks[td], dg1 = f.tile_tasks[td + 1];
-  const C *buf = static_cast<const C *>(f.tilebuf);
-  C *grid = static_cast<C *>(f.grid);
-  for (int idx = threadIdx.x; idx < H * W; idx += blockDim.x) {
+  const C *__restrict__ buf = static_cast<const C *>(f.tilebuf);
+  C *__restrict__ grid = static_cast<C *>(f.grid);
+  auto cell_sum = [&](int idx) {
     const int lp = idx / W, lq = idx - lp * W;
     C s{0, 0};
     for (int k = own0; k < own1; ++k) {
@@ -402,7 +431,25 @@ __global__ void fold_kernel(const FoldArgs f) {
         s.x += v.x;
         s.y += v.y;
       }
-    grid[size_t(P + lp) * f.Nu + Q + lq] = s;
+    return s;
+  };
+  // Four cells per thread per round, loads first, so their latencies overlap.
+  constexpr int R = 4;
+  for (int base = threadIdx.x; base < H * W; base += R * blockDim.x) {
+    C s[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int idx = base + r * blockDim.x;
+      if (idx < H * W) s[r] = cell_sum(idx);
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int idx = base + r * blockDim.x;
+      if (idx < H * W) {
+        const int lp = idx / W, lq = idx - lp * W;
+        grid[size_t(P + lp) * f.Nu + Q + lq] = s[r];
+      }
+    }
   }
 }
 

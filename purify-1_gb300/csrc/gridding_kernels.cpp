@@ -170,7 +170,8 @@ AxisFit fit_axis(const GriddingKernel &kernel, int taps, int ncoef) {
 
   // Fewest sub-segments that meet the target; a kernel that changes quickly
   // over one tap (narrow supports, the branch point of the PSWF) gets 2 or 4.
-  const double target = ncoef >= kCoefF64 ? 1e-13 : 3e-8;
+  // FP32: the rounding of an FP32 Horner chain is ~1e-7 of the peak already.
+  const double target = ncoef >= kCoefF64 ? 1e-13 : 1.5e-7;
   AxisFit best;
   for (int nsub = 1; nsub <= kMaxSub; nsub *= 2) {
     AxisFit fit;

@@ -240,3 +240,32 @@ def test_caller_stream_ordering(pg, cuda, small_config):
         op.forward_into(x2, y2, stream=s)
     s.synchronize()
     assert rel_l2(to_np(y2), 2 * ref) < 1e-6
+
+
+def test_operators_with_different_kernels_interleaved(pg, oracle_mod, cuda):
+    """Operators with different kernels, applied alternately on two streams,
+    each give their own result."""
+    torch = cuda
+    rng = np.random.default_rng(21)
+    M, n = 6000, 64
+    u = rng.normal(0, 25, M)
+    v = rng.normal(0, 25, M)
+    specs = [("kb", 4), ("gauss", 6), ("kbmin", 5)]
+    ops = [pg.MeasurementOperator(u, v, None, None, n, n, power_iters=0, kernel=k, Ju=J, Jv=J)
+           for k, J in specs]
+    refs = [oracle_mod.Operator(u, v, None, None, n, n, kernel=k, Ju=J, Jv=J) for k, J in specs]
+    x = rng.standard_normal(n * n) + 1j * rng.standard_normal(n * n)
+    xd = to_dev(torch, x, "fp32")
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    outs = []
+    for rep in range(3):
+        for k, op in enumerate(ops):
+            s = streams[(rep + k) % 2]
+            y = torch.empty(M, dtype=torch.complex64, device="cuda")
+            xd.record_stream(s)
+            with torch.cuda.stream(s):
+                op.forward_into(xd, y, stream=s)
+            outs.append((k, y, s))
+    torch.cuda.synchronize()
+    for k, y, _ in outs:
+        assert rel_l2(to_np(y), refs[k].forward(x)) < 1e-5
