@@ -99,7 +99,8 @@ typedef struct {
   int32_t max_per_item;  /* visibilities of one base cell given to one lane (<= 65535) */
   int32_t tile;          /* uv tile edge in grid cells (<= 255) */
   int32_t fused_permute; /* 1: degrid/grid touch caller-ordered visibilities directly,
-                            0: via a slot-ordered buffer and gather kernels, -1: default */
+                            0: via a slot-ordered buffer and gather kernels, -1: default
+                            (direct for Phi, gather for Phi^H) */
 } purify_gb300_tuning;
 int purify_gb300_operator_create_tuned(const purify_gb300_create_args *args,
                                        const purify_gb300_tuning *tuning,

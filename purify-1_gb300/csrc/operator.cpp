@@ -148,7 +148,7 @@ class OperatorT final : public Operator {
   int Nx_ = 0, Ny_ = 0, Nu_ = 0, Nv_ = 0, x0_ = 0, y0_ = 0, J_ = 0;
   int64_t M_ = 0, N_ = 0, S_ = 0;
   bool unit_weights_ = true;
-  bool fused_permute_ = true;
+  bool fused_forward_ = true, fused_adjoint_ = false;
   double norm_ = 1.0;
   std::vector<double> su_, sv_;  // 1 / ft kernel at the image pixels (unscaled)
   std::vector<real> su_scaled_, sv_real_;
@@ -228,7 +228,11 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
     throw Error(kInvalidArgument, e.what());
   }
   shape_.threads = cfg.threads > 0 ? cfg.threads : 128;
-  fused_permute_ = cfg.fused_permute == 1;
+  // Measured on the 10^7-visibility benchmark: the forward is faster writing
+  // caller order directly (scattered stores), the adjoint faster with a
+  // separate gather into slot order.
+  fused_forward_ = cfg.fused_permute != 0;
+  fused_adjoint_ = cfg.fused_permute == 1;
   ntasks_ = int(plan.tasks.size());
   win_rows_ = plan.win_rows;
   win_cols_ = plan.win_cols;
@@ -426,7 +430,7 @@ void OperatorT<real>::grid_slots(void *grid, const void *caller_vis) {
 
 template <typename real>
 void OperatorT<real>::degrid_on_stream(const void *grid, void *y) {
-  if (fused_permute_) {
+  if (fused_forward_) {
     degrid_slots(grid, y);
     return;
   }
@@ -439,7 +443,7 @@ void OperatorT<real>::degrid_on_stream(const void *grid, void *y) {
 
 template <typename real>
 void OperatorT<real>::grid_on_stream(const void *y, void *grid) {
-  if (fused_permute_) {
+  if (fused_adjoint_) {
     grid_slots(grid, y);
     return;
   }
@@ -478,7 +482,7 @@ void OperatorT<real>::adjoint_slots(void *x, const void *caller_vis) {
 
 template <typename real>
 void OperatorT<real>::forward_on_stream(const void *x, void *y) {
-  if (fused_permute_) {
+  if (fused_forward_) {
     forward_slots(x, y);
     return;
   }
@@ -491,7 +495,7 @@ void OperatorT<real>::forward_on_stream(const void *x, void *y) {
 
 template <typename real>
 void OperatorT<real>::adjoint_on_stream(const void *y, void *x) {
-  if (fused_permute_) {
+  if (fused_adjoint_) {
     adjoint_slots(x, y);
     return;
   }

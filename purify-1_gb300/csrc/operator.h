@@ -42,7 +42,7 @@ struct OperatorConfig {
   int tile = 0;
   // 1: degrid/grid read and write caller-ordered visibilities directly;
   // 0: through a slot-ordered buffer and separate gather kernels;
-  // -1: default (the gather kernels; measured faster on the benchmark workload).
+  // -1: default (direct for the forward, gather for the adjoint).
   int fused_permute = -1;
 };
 

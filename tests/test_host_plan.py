@@ -66,7 +66,8 @@ def replay_grid(plan, taps_u, taps_v, vis):
             for lane, lp, lq, cnt, sl in _lanes(plan, b):
                 if cnt == 0:
                     continue
-                assert (lp, lq) not in cells, "two items of one base cell in a batch"
+                # the row-phase flush needs: same base row => >= J columns apart
+                assert all(r != lp or abs(c - lq) >= J for (r, c) in cells), "batch clash"
                 cells.add((lp, lq))
                 for i in sl:
                     z = np.conj(plan.weight[i]) * slots[i]
