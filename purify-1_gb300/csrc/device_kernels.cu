@@ -322,30 +322,26 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a,
         }
       }
       if (new_batch) {
-        // Flush, one footprint row per phase.  Two items of a batch never
-        // share a base row within J columns, so within a phase the 32 lanes
-        // touch disjoint cells; phases are ordered by __syncwarp, which makes
-        // the summation order a function of the plan.
+        // Flush.  The items of one batch have distinct base cells, so at each
+        // (jv, ju) step the 32 lanes update 32 distinct cells; steps are
+        // ordered by __syncwarp, which makes the summation order a function
+        // of the plan.
         const int cnt = item_count(code);
         const int lp = item_lp(code), lq = item_lq(code);
 #pragma unroll
-        for (int jv = 0; jv < J; ++jv) {
-          if (cnt > 0) {
-            C *row = mine + (lp + jv) * WW + lq;
-            C c[J];
+        for (int jv = 0; jv < J; ++jv)
 #pragma unroll
-            for (int ju = 0; ju < J; ++ju) c[ju] = row[ju];
-#pragma unroll
-            for (int ju = 0; ju < J; ++ju) {
-              c[ju].x += acc[jv][ju].x;
-              c[ju].y += acc[jv][ju].y;
-              row[ju] = c[ju];
+          for (int ju = 0; ju < J; ++ju) {
+            if (cnt > 0) {
+              C *cell = mine + (lp + jv) * WW + lq + ju;
+              C c = *cell;
+              c.x += acc[jv][ju].x;
+              c.y += acc[jv][ju].y;
+              *cell = c;
             }
+            acc[jv][ju] = C{0, 0};
+            __syncwarp();
           }
-#pragma unroll
-          for (int ju = 0; ju < J; ++ju) acc[jv][ju] = C{0, 0};
-          __syncwarp();
-        }
         lb += nw;
         if (!more) break;
         bt = bt_next;

@@ -121,7 +121,7 @@ Plan build_plan(const PlanRequest &rq) {
   const int K = rq.max_per_item;
   P.tile_tasks.assign(ntiles + 1, 0);
   std::vector<Item> items;
-  std::vector<int32_t> stamp;  // per row of the tile: last batch that took an item in it
+  std::vector<int32_t> stamp;  // per cell of the tile: last batch that took it
   std::vector<uint8_t> taken;
   // slot assignment collected per batch: (slot, sorted index) pairs
   std::vector<int64_t> slot_sorted;  // slot -> sorted index or -1
@@ -152,9 +152,9 @@ Plan build_plan(const PlanRequest &rq) {
       std::stable_sort(items.begin(), items.end(),
                        [](const Item &x, const Item &y) { return x.count > y.count; });
       // Greedy packing: scan the pending items in order and take one unless
-      // it clashes with the batch; the scan gives up 256 clashes past the
-      // first pending item.
-      stamp.assign(size_t(h), -1);
+      // its base cell is already in the batch; the scan gives up 256 clashes
+      // past the first pending item.
+      stamp.assign(size_t(h) * w, -1);
       taken.assign(items.size(), 0);
       size_t front = 0;
       int32_t batch_id = 0;
@@ -167,21 +167,11 @@ Plan build_plan(const PlanRequest &rq) {
         size_t skipped = 0;
         for (size_t k = front; k < items.size() && lanes.size() < size_t(kBatch); ++k) {
           if (taken[k]) continue;
-          // Two items of a batch never share a base row within Ju columns, so
-          // the row-by-row flush of the grid kernel touches disjoint cells
-          // within each row phase (this also makes base cells distinct).
-          bool clash = false;
-          if (stamp[items[k].lp] == batch_id)
-            for (size_t l : lanes)
-              if (items[l].lp == items[k].lp && std::abs(items[l].lq - items[k].lq) < rq.Ju) {
-                clash = true;
-                break;
-              }
-          if (clash) {
+          if (stamp[items[k].cell] == batch_id) {
             if (++skipped > 256) break;
             continue;
           }
-          stamp[items[k].lp] = batch_id;
+          stamp[items[k].cell] = batch_id;
           taken[k] = 1;
           lanes.push_back(k);
         }

@@ -3,8 +3,7 @@
 //
 // Visibilities are sorted by uv tile and base cell, grouped into work items
 // (one base cell, up to K visibilities) and packed into batches of 32 items,
-// one item per lane; two items of a batch never share a base row within Ju
-// columns (so never a base cell).  Each
+// one item per lane, no two items of a batch on the same base cell.  Each
 // batch owns 32 * kmax consecutive "slots" (kmax = its largest item): lane l's
 // k-th visibility sits in slot base + 32 k + l, so a warp that walks k reads
 // 256 contiguous bytes per access and every lane runs the same loop.  Lanes

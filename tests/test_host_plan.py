@@ -66,8 +66,7 @@ def replay_grid(plan, taps_u, taps_v, vis):
             for lane, lp, lq, cnt, sl in _lanes(plan, b):
                 if cnt == 0:
                     continue
-                # the row-phase flush needs: same base row => >= J columns apart
-                assert all(r != lp or abs(c - lq) >= J for (r, c) in cells), "batch clash"
+                assert (lp, lq) not in cells, "two items of one base cell in a batch"
                 cells.add((lp, lq))
                 for i in sl:
                     z = np.conj(plan.weight[i]) * slots[i]
