@@ -47,7 +47,9 @@ def parse():
                    help="visibilities in the CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
-    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--e2e-steps", type=int, default=5, help="0 skips the end-to-end leg")
+    p.add_argument("--power-iters", type=int, default=20,
+                   help="power-method rounds for the norm before timing (0: norm 1)")
     p.add_argument("--threads", type=int, default=0, help="CTA threads (tuning)")
     p.add_argument("--max-per-item", type=int, default=0)
     return p.parse_args()
@@ -229,7 +231,7 @@ def run_gb300(args):
     op = pgb.MeasurementOperator(u, v, None, None, power_iters=0, precision="fp32", **kw)
     t_create = time.perf_counter() - t0
     t0 = time.perf_counter()
-    norm = op.power_method(20, 1e-4)
+    norm = op.power_method(args.power_iters, 1e-4) if args.power_iters > 0 else 1.0
     t_power = time.perf_counter() - t0
     info = op.info()
 
@@ -366,6 +368,12 @@ def run_gb300(args):
         del op64
 
     # end to end through the host complex<double> entry points, pinned buffers
+    if args.e2e_steps <= 0:
+        if rank == 0:
+            print(json.dumps(out), flush=True)
+        if dist:
+            dist.destroy_process_group()
+        return
     xh = torch.from_numpy(x).pin_memory()
     yh = torch.empty(M, dtype=torch.complex128).pin_memory()
     xoh = torch.empty(N, dtype=torch.complex128).pin_memory()
