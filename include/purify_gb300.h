@@ -127,6 +127,24 @@ int purify_gb300_adjoint_host(purify_gb300_operator *op, const double *y, double
 int purify_gb300_degrid(purify_gb300_operator *op, const void *grid, void *vis, void *stream);
 int purify_gb300_grid(purify_gb300_operator *op, const void *vis, void *grid, void *stream);
 
+/* G^H that allocates nothing, for callers that may not call cudaMalloc once
+ * running (all device memory handed to a pool at start-up, or a hard memory
+ * cap on a shared GPU).  Same inputs, output and result as purify_gb300_grid;
+ * its scratch (accumulation windows and the slot-ordered visibility buffer)
+ * lives in one fixed array of PURIFY_GB300_STATIC_SCRATCH_BYTES that is part
+ * of the library and stays resident on every GPU that loads it.  An operator
+ * whose scratch would not fit is refused with PURIFY_GB300_INVALID_ARGUMENT
+ * (purify_gb300_grid_no_alloc_bytes tells the need).  The first call on a
+ * device looks up the array's address; make that first call before any
+ * stream capture.  Every call shares the array and leaves its contents
+ * behind, so calls that overlap on the GPU (any operator, any stream) race:
+ * order them.  Everything the kernels read from the array is written first
+ * in the same call.  No counterpart in the reference. */
+#define PURIFY_GB300_STATIC_SCRATCH_BYTES (32u << 20)
+int purify_gb300_grid_no_alloc(purify_gb300_operator *op, const void *vis, void *grid,
+                               void *stream);
+int purify_gb300_grid_no_alloc_bytes(const purify_gb300_operator *op, int64_t *bytes);
+
 /* Gridding correction S(j, i) as imsizey*imsizex complex<double> values
  * (row j, column i), as details::init_correction2d builds it
  * (operators.cc:101-121).  Host only. */

@@ -157,6 +157,22 @@ int purify_gb300_grid(purify_gb300_operator *op, const void *vis, void *grid, vo
     op->impl->grid(vis, grid, static_cast<cudaStream_t>(stream));
   });
 }
+// G^H for callers that may not allocate: scratch from the library's fixed
+// device array (see no_alloc.cu).
+int purify_gb300_grid_no_alloc(purify_gb300_operator *op, const void *vis, void *grid,
+                               void *stream) {
+  if (!op) return null_arg("operator");
+  return guard([&] {
+    const pg::OperatorInfo i = op->impl->info();
+    if (!grid || (!vis && i.M > 0)) throw pg::Error(pg::kInvalidArgument, "null buffer");
+    op->impl->grid_no_alloc(vis, grid, static_cast<cudaStream_t>(stream));
+  });
+}
+int purify_gb300_grid_no_alloc_bytes(const purify_gb300_operator *op, int64_t *bytes) {
+  if (!op) return null_arg("operator");
+  if (!bytes) return null_arg("bytes");
+  return guard([&] { *bytes = op->impl->no_alloc_bytes(); });
+}
 int purify_gb300_correction(int32_t kernel, uint32_t Ju, uint32_t Jv, uint32_t imsizey,
                             uint32_t imsizex, double os, double *S_out) {
   if (!S_out) return null_arg("S_out");

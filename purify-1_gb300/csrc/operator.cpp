@@ -11,6 +11,7 @@
 
 #include "device_kernels.h"
 #include "gridding_kernels.h"
+#include "no_alloc.h"
 #include "plan.h"
 
 namespace pg {
@@ -102,6 +103,8 @@ class OperatorT final : public Operator {
   void adjoint(const void *y, void *x, cudaStream_t stream) override;
   void degrid(const void *grid, void *vis, cudaStream_t stream) override;
   void grid(const void *vis, void *grid, cudaStream_t stream) override;
+  void grid_no_alloc(const void *vis, void *grid, cudaStream_t stream) override;
+  int64_t no_alloc_bytes() const override;
   void forward_host(const double *x, double *y) override;
   void adjoint_host(const double *y, double *x) override;
   double power_method(int iters, double tol) override;
@@ -520,6 +523,67 @@ void OperatorT<real>::grid(const void *vis, void *grid, cudaStream_t user) {
   std::lock_guard<std::mutex> lock(mu_);
   join(user);
   grid_on_stream(vis, grid);
+  release(user);
+}
+
+// Scratch layout in the fixed array: the task windows, then the slot buffer,
+// each starting on a 256-byte boundary.
+template <typename real>
+int64_t OperatorT<real>::no_alloc_bytes() const {
+  auto up = [](int64_t b) { return (b + 255) / 256 * 256; };
+  return up(int64_t(sizeof(C)) * slot_stride_ * std::max(ntasks_, 1)) +
+         up(int64_t(sizeof(C)) * std::max<int64_t>(S_, 1));
+}
+
+template <typename real>
+void OperatorT<real>::grid_no_alloc(const void *vis, void *grid, cudaStream_t user) {
+  DeviceGuard guard(device_);
+  const int64_t need = no_alloc_bytes();
+  if (need > int64_t(static_scratch_bytes()))
+    throw Error(kInvalidArgument,
+                "purify_gb300_grid_no_alloc: this operator needs " + std::to_string(need) +
+                    " bytes of scratch, the fixed array holds " +
+                    std::to_string(static_scratch_bytes()));
+  void *scratch = nullptr;
+  cuda_check(static_scratch_address(&scratch), "cudaGetSymbolAddress");
+  unsigned char *base = static_cast<unsigned char *>(scratch);
+  void *windows = base;
+  void *slots = base + (int64_t(sizeof(C)) * slot_stride_ * std::max(ntasks_, 1) + 255) / 256 * 256;
+  std::lock_guard<std::mutex> lock(mu_);
+  join(user);
+  // expand writes every slot (0 for null slots) and the grid kernel writes
+  // every cell of every task window, so nothing left in the array from an
+  // earlier call is read.
+  cuda_check(launch_expand<real>(vis, slot_user_.as<int32_t>(), slots, S_, stream_), "expand");
+  ApplyArgs<real> a;
+  a.tilebuf = windows;
+  a.tasks = tasks_.as<Task>();
+  a.batches = batches_.as<int2>();
+  a.lane_code = lane_code_.as<int32_t>();
+  a.frac = frac_.get();
+  a.weight = unit_weights_ ? nullptr : weight_.get();
+  a.slot_in = slots;
+  a.Nu = Nu_;
+  a.Nv = Nv_;
+  a.slot_stride = slot_stride_;
+  cuda_check(launch_grid<real>(a, poly_, J_, ntasks_, win_rows_, win_cols_, shape_, stream_),
+             "grid");
+  FoldArgs f;
+  f.tilebuf = windows;
+  f.slot_stride = slot_stride_;
+  f.tile_tasks = tile_tasks_.as<int32_t>();
+  f.tu_start = tu_start_.as<int32_t>();
+  f.tv_start = tv_start_.as<int32_t>();
+  f.tu_of = tu_of_.as<int32_t>();
+  f.tv_of = tv_of_.as<int32_t>();
+  f.ntu = ntu_;
+  f.ntv = ntv_;
+  f.Ju = J_;
+  f.Jv = J_;
+  f.Nu = Nu_;
+  f.Nv = Nv_;
+  f.grid = grid;
+  cuda_check(launch_fold<real>(f, stream_), "fold");
   release(user);
 }
 

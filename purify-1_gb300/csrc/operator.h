@@ -72,6 +72,9 @@ class Operator {
   // G and G^H alone (no correction, padding or FFT).
   virtual void degrid(const void *grid, void *vis, cudaStream_t stream) = 0;
   virtual void grid(const void *vis, void *grid, cudaStream_t stream) = 0;
+  // G^H with its scratch in the library's fixed device array (no allocation).
+  virtual void grid_no_alloc(const void *vis, void *grid, cudaStream_t stream) = 0;
+  virtual int64_t no_alloc_bytes() const = 0;
   // Host complex<double> buffers; synchronous.
   virtual void forward_host(const double *x, double *y) = 0;
   virtual void adjoint_host(const double *y, double *x) = 0;

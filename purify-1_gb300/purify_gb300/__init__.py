@@ -78,7 +78,8 @@ EXPORTS = [
     "purify_gb300_plan_sizes", "purify_gb300_plan_export", "purify_gb300_plan_destroy",
     "purify_gb300_kernel_taps", "purify_gb300_degrid", "purify_gb300_grid",
     "purify_gb300_correction", "purify_gb300_stage_timing", "purify_gb300_stage_times",
-    "purify_gb300_operator_create_tuned",
+    "purify_gb300_operator_create_tuned", "purify_gb300_grid_no_alloc",
+    "purify_gb300_grid_no_alloc_bytes",
 ]
 STAGES = ["pad", "fft_forward", "degrid", "grid", "fold", "fft_inverse", "crop", "compact",
           "expand"]
@@ -127,6 +128,8 @@ def load(path=None):
         f.argtypes = [vp, vp, vp, vp]
     L.purify_gb300_correction.argtypes = [ctypes.c_int32, ctypes.c_uint32, ctypes.c_uint32,
                                           ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double, vp]
+    L.purify_gb300_grid_no_alloc.argtypes = [vp, vp, vp, vp]
+    L.purify_gb300_grid_no_alloc_bytes.argtypes = [vp, P(ctypes.c_int64)]
     L.purify_gb300_stage_timing.argtypes = [vp, ctypes.c_int]
     L.purify_gb300_stage_times.argtypes = [vp, vp, vp]
     _lib = L
@@ -338,6 +341,20 @@ class MeasurementOperator:
         _check(load().purify_gb300_grid(self._h, ctypes.c_void_p(vis.data_ptr()),
                                         ctypes.c_void_p(grid.data_ptr()), self._stream(stream)))
         return grid
+
+    def grid_no_alloc_into(self, vis, grid, stream=None):
+        """G^H alone with no device allocation: the scratch is the library's
+        fixed array (purify_gb300_grid_no_alloc).  Same result as grid_into."""
+        _check(load().purify_gb300_grid_no_alloc(self._h, ctypes.c_void_p(vis.data_ptr()),
+                                                 ctypes.c_void_p(grid.data_ptr()),
+                                                 self._stream(stream)))
+        return grid
+
+    def grid_no_alloc_bytes(self):
+        """Scratch bytes the allocation-free G^H needs for this operator."""
+        n = ctypes.c_int64()
+        _check(load().purify_gb300_grid_no_alloc_bytes(self._h, ctypes.byref(n)))
+        return n.value
 
     def _check_device_tensor(self, t, n):
         if not t.is_cuda or t.dtype != self.complex_dtype or not t.is_contiguous() or t.numel() != n:
