@@ -79,6 +79,10 @@ typedef struct {
   double cellx, celly;     /* arcsec, default 1, 1 */
   int32_t precision;       /* purify_gb300_precision */
   int32_t device;          /* CUDA device ordinal */
+  /* Extension: per-row w-support (M values, Jw of each visibility) when
+   * w_term != 0, or NULL to use Jw for every row as the reference does.
+   * Supports Jw + J - 1 up to 32 taps per axis. */
+  const int32_t *jw_rows;
 } purify_gb300_create_args;
 
 /* Fills `args` with the reference's defaults (operators.h:373-380). */
@@ -229,6 +233,15 @@ int purify_gb300_plan_destroy(purify_gb300_plan *plan);
 int purify_gb300_kernel_taps(int32_t kernel, uint32_t J, double oversample_ratio,
                              int32_t precision, const double *t, int64_t n, double *out,
                              double *fit_error);
+
+/* One w-projection row as the device rebuilds it from its stored factors:
+ * the S x S values (S = Jw + J - 1, row-major, v then u) of the gridding
+ * matrix row of a visibility at (u, v) pixels with w - mean(w) = w_centered,
+ * weight 1, phase included (out: 2 S S doubles).  Host only; operators.cc:49-99,
+ * projection_kernels.cc:59-85. */
+int purify_gb300_wrow_taps(double u, double v, double w_centered, uint32_t Jw, uint32_t J,
+                           int32_t kernel, double oversample_ratio, uint32_t imsizey,
+                           uint32_t imsizex, double cellx, double celly, double *out);
 
 /* Message of the last failing call on this thread ("" when none). */
 const char *purify_gb300_last_error(void);

@@ -12,6 +12,7 @@
 #include "gridding_kernels.h"
 #include "operator.h"
 #include "plan.h"
+#include "wplan.h"
 
 struct purify_gb300_operator {
   std::unique_ptr<pg::Operator> impl;
@@ -96,6 +97,7 @@ int purify_gb300_operator_create_tuned(const purify_gb300_create_args *a,
     c.Jv = int(a->Jv);
     c.w_term = a->w_term != 0;
     c.Jw = int(a->Jw);
+    c.jw_rows = a->jw_rows;
     c.cellx = a->cellx;
     c.celly = a->celly;
     c.fp64 = a->precision == PURIFY_GB300_FP64;
@@ -173,6 +175,50 @@ int purify_gb300_grid_no_alloc_bytes(const purify_gb300_operator *op, int64_t *b
   if (!bytes) return null_arg("bytes");
   return guard([&] { *bytes = op->impl->no_alloc_bytes(); });
 }
+int purify_gb300_wrow_taps(double u, double v, double w_centered, uint32_t Jw, uint32_t J,
+                           int32_t kernel, double os, uint32_t imsizey, uint32_t imsizex,
+                           double cellx, double celly, double *out) {
+  if (!out) return null_arg("out");
+  return guard([&] {
+    // two rows with w and -w: their mean is 0, so row 0 sees w_centered
+    const double uu[2] = {u, u}, vv[2] = {v, v}, ww[2] = {w_centered, -w_centered};
+    pg::WPlanRequest rq;
+    rq.u = uu;
+    rq.v = vv;
+    rq.w = ww;
+    rq.M = 2;
+    rq.Nu = int(std::floor(imsizex * os));
+    rq.Nv = int(std::floor(imsizey * os));
+    rq.imsizex = int(imsizex);
+    rq.imsizey = int(imsizey);
+    rq.oversample_ratio = os;
+    rq.cellx = cellx;
+    rq.celly = celly;
+    rq.J = int(J);
+    rq.Jw = int(Jw);
+    rq.kernel = kernel;
+    pg::WPlan p;
+    try {
+      p = pg::build_wplan(rq);
+    } catch (const std::invalid_argument &e) {
+      throw pg::Error(pg::kInvalidArgument, e.what());
+    }
+    const int64_t i = p.user_slot[0];
+    const int S = (p.code[i] >> 16) & 0xff;
+    std::vector<std::complex<double>> f(6 * S);
+    pg::wplan_factors<double>(p, i, i + 1, f.data());
+    const std::complex<double> sgn = p.weight[i];  // +-1: (-1)^(kw_u + kw_v)
+    for (int jv = 0; jv < S; ++jv)
+      for (int ju = 0; ju < S; ++ju) {
+        std::complex<double> k = 0;
+        for (int r = 0; r < 3; ++r) k += f[r * S + jv] * f[(3 + r) * S + ju];
+        k *= sgn;
+        out[2 * (jv * S + ju)] = k.real();
+        out[2 * (jv * S + ju) + 1] = k.imag();
+      }
+  });
+}
+
 int purify_gb300_correction(int32_t kernel, uint32_t Ju, uint32_t Jv, uint32_t imsizey,
                             uint32_t imsizex, double os, double *S_out) {
   if (!S_out) return null_arg("S_out");

@@ -13,6 +13,8 @@
 #include "gridding_kernels.h"
 #include "no_alloc.h"
 #include "plan.h"
+#include "wkernels.h"
+#include "wplan.h"
 
 namespace pg {
 
@@ -136,6 +138,8 @@ class OperatorT final : public Operator {
   // G and G^H between the grid and the slot-ordered visibility buffer.
   void degrid_slots(const void *grid, void *caller_vis = nullptr);
   void grid_slots(void *grid, const void *caller_vis = nullptr);
+  void grid_core(void *grid, const void *vis, const int32_t *slot_user, void *windows);
+  void fold_into(void *grid, const void *windows);
   void degrid_on_stream(const void *grid, void *y);
   void grid_on_stream(const void *y, void *grid);
   // Phi' / Phi'^H with visibilities kept in slot order (power method).
@@ -150,6 +154,14 @@ class OperatorT final : public Operator {
   int device_ = 0;
   int Nx_ = 0, Ny_ = 0, Nu_ = 0, Nv_ = 0, x0_ = 0, y0_ = 0, J_ = 0;
   int64_t M_ = 0, N_ = 0, S_ = 0;
+  bool wmode_ = false;  // w-projection rows instead of separable taps
+  int fold_J_ = 0;      // halo of the task windows + 1 (J, or the largest w support)
+  DeviceBuffer wcode_, wfactor_, wfactors_;
+  int64_t nnz_ = 0, occupied_ = 0, work_items_ = 0;
+  void init_plain(const OperatorConfig &cfg, int64_t &bytes, AxisTiling &tu, AxisTiling &tv,
+                  std::vector<int32_t> &tile_tasks);
+  void init_w(const OperatorConfig &cfg, int64_t &bytes, AxisTiling &tu, AxisTiling &tv,
+              std::vector<int32_t> &tile_tasks);
   bool unit_weights_ = true;
   bool fused_forward_ = true, fused_adjoint_ = false;
   double norm_ = 1.0;
@@ -212,84 +224,40 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
   for (int j = 0; j < Ny_; ++j)
     sv_[j] = 1.0 / kern.correction((y0_ + j + 0.5) / Nv_ - 0.5);
 
-  // Coverage plan (FP64 coordinates, tile sort, work items).
-  PlanRequest rq;
-  rq.u = cfg.u;
-  rq.v = cfg.v;
-  rq.weights = reinterpret_cast<const std::complex<double> *>(cfg.weights);
-  rq.M = cfg.M;
-  rq.Nu = Nu_;
-  rq.Nv = Nv_;
-  rq.Ju = cfg.Ju;
-  rq.Jv = cfg.Jv;
-  rq.tile = cfg.tile > 0 ? cfg.tile : kTile;
-  rq.max_per_item = cfg.max_per_item > 0 ? cfg.max_per_item : 16;
-  Plan plan;
-  try {
-    plan = build_plan(rq);
-  } catch (const std::invalid_argument &e) {
-    throw Error(kInvalidArgument, e.what());
-  }
   shape_.threads = cfg.threads > 0 ? cfg.threads : 128;
+  wmode_ = cfg.w_term;
   // Measured on the 10^7-visibility benchmark: the forward is faster writing
   // caller order directly (scattered stores), the adjoint faster with a
-  // separate gather into slot order.
-  fused_forward_ = cfg.fused_permute != 0;
-  fused_adjoint_ = cfg.fused_permute == 1;
-  ntasks_ = int(plan.tasks.size());
-  win_rows_ = plan.win_rows;
-  win_cols_ = plan.win_cols;
-  ntu_ = plan.tu.n;
-  ntv_ = plan.tv.n;
-  slot_stride_ = int64_t(win_rows_) * win_cols_;
+  // separate gather into slot order.  The w-projection kernels always use
+  // the slot-ordered buffer.
+  fused_forward_ = !wmode_ && cfg.fused_permute != 0;
+  fused_adjoint_ = !wmode_ && cfg.fused_permute == 1;
 
   cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
   cuda_check(cudaEventCreateWithFlags(&ev_in_, cudaEventDisableTiming), "cudaEventCreate");
   cuda_check(cudaEventCreateWithFlags(&ev_out_, cudaEventDisableTiming), "cudaEventCreate");
 
   int64_t bytes = 0;
+  AxisTiling tu, tv;
+  std::vector<int32_t> tile_tasks;
+  if (wmode_)
+    init_w(cfg, bytes, tu, tv, tile_tasks);
+  else
+    init_plain(cfg, bytes, tu, tv, tile_tasks);
+  ntu_ = tu.n;
+  ntv_ = tv.n;
+  slot_stride_ = int64_t(win_rows_) * win_cols_;
   {
-    S_ = plan.S;
-    unit_weights_ = plan.unit_weights;
-    std::vector<C> fr(S_);
-    for (int64_t i = 0; i < S_; ++i) {
-      // unit weights: the phase sign (-1)^(k_u + k_v) rides in the sign of t_u
-      const double tu = (unit_weights_ && plan.flip[i]) ? -plan.frac_u[i] : plan.frac_u[i];
-      fr[i] = C(real(tu), real(plan.frac_v[i]));
-    }
-    frac_.alloc(sizeof(C) * S_, &bytes);
-    frac_.upload(fr.data(), sizeof(C) * S_, stream_);
-    if (!unit_weights_) {
-      std::vector<C> wt(S_);
-      for (int64_t i = 0; i < S_; ++i)
-        wt[i] = C(real(plan.weight[i].real()), real(plan.weight[i].imag()));
-      weight_.alloc(sizeof(C) * S_, &bytes);
-      weight_.upload(wt.data(), sizeof(C) * S_, stream_);
-      cuda_check(cudaStreamSynchronize(stream_), "upload");
-    }
-    slot_user_.alloc(sizeof(int32_t) * S_, &bytes);
-    slot_user_.upload(plan.slot_user.data(), sizeof(int32_t) * S_, stream_);
-    user_slot_.alloc(sizeof(int32_t) * M_, &bytes);
-    user_slot_.upload(plan.user_slot.data(), sizeof(int32_t) * M_, stream_);
-    const size_t nb = plan.batch_base.size();
-    std::vector<int2> bt(nb);
-    for (size_t k = 0; k < nb; ++k) bt[k] = int2{plan.batch_base[k], plan.batch_kmax[k]};
-    batches_.alloc(sizeof(int2) * nb, &bytes);
-    batches_.upload(bt.data(), sizeof(int2) * nb, stream_);
-    lane_code_.alloc(sizeof(int32_t) * plan.lane_code.size(), &bytes);
-    lane_code_.upload(plan.lane_code.data(), sizeof(int32_t) * plan.lane_code.size(), stream_);
-    tasks_.alloc(sizeof(Task) * plan.tasks.size(), &bytes);
-    tasks_.upload(plan.tasks.data(), sizeof(Task) * plan.tasks.size(), stream_);
-    tile_tasks_.alloc(sizeof(int32_t) * plan.tile_tasks.size(), &bytes);
-    tile_tasks_.upload(plan.tile_tasks.data(), sizeof(int32_t) * plan.tile_tasks.size(), stream_);
-    tu_start_.alloc(sizeof(int32_t) * plan.tu.start.size(), &bytes);
-    tu_start_.upload(plan.tu.start.data(), sizeof(int32_t) * plan.tu.start.size(), stream_);
-    tv_start_.alloc(sizeof(int32_t) * plan.tv.start.size(), &bytes);
-    tv_start_.upload(plan.tv.start.data(), sizeof(int32_t) * plan.tv.start.size(), stream_);
-    tu_of_.alloc(sizeof(int32_t) * plan.tu.of.size(), &bytes);
-    tu_of_.upload(plan.tu.of.data(), sizeof(int32_t) * plan.tu.of.size(), stream_);
-    tv_of_.alloc(sizeof(int32_t) * plan.tv.of.size(), &bytes);
-    tv_of_.upload(plan.tv.of.data(), sizeof(int32_t) * plan.tv.of.size(), stream_);
+    tile_tasks_.alloc(sizeof(int32_t) * tile_tasks.size(), &bytes);
+    tile_tasks_.upload(tile_tasks.data(), sizeof(int32_t) * tile_tasks.size(), stream_);
+    tu_start_.alloc(sizeof(int32_t) * tu.start.size(), &bytes);
+    tu_start_.upload(tu.start.data(), sizeof(int32_t) * tu.start.size(), stream_);
+    tv_start_.alloc(sizeof(int32_t) * tv.start.size(), &bytes);
+    tv_start_.upload(tv.start.data(), sizeof(int32_t) * tv.start.size(), stream_);
+    tu_of_.alloc(sizeof(int32_t) * tu.of.size(), &bytes);
+    tu_of_.upload(tu.of.data(), sizeof(int32_t) * tu.of.size(), stream_);
+    tv_of_.alloc(sizeof(int32_t) * tv.of.size(), &bytes);
+    tv_of_.upload(tv.of.data(), sizeof(int32_t) * tv.of.size(), stream_);
     su_d_.alloc(sizeof(real) * Nx_, &bytes);
     sv_d_.alloc(sizeof(real) * Ny_, &bytes);
     const size_t gbytes = sizeof(C) * size_t(Nu_) * Nv_;
@@ -297,7 +265,7 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
     cuda_check(cudaMemsetAsync(pad_.get(), 0, gbytes, stream_), "cudaMemset");
     work_.alloc(gbytes, &bytes);
     tilebuf_.alloc(sizeof(C) * size_t(slot_stride_) * std::max(ntasks_, 1), &bytes);
-    slots_.alloc(sizeof(C) * S_, &bytes);
+    slots_.alloc(sizeof(C) * std::max<int64_t>(S_, 1), &bytes);
     norm_partial_.alloc(sizeof(double) * kNormBlocks, &bytes);
     norm_out_.alloc(sizeof(double), &bytes);
     // The staging vectors above are pageable; wait before they go out of scope.
@@ -319,15 +287,154 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
   info_.fp64 = cfg.fp64;
   info_.kernel = cfg.kernel;
   info_.w_term = cfg.w_term;
-  info_.nnz = M_ * int64_t(cfg.Ju) * cfg.Jv;
-  info_.occupied_cells = plan.occupied_cells;
-  info_.work_items = int64_t(plan.lane_code.size());
   info_.tasks = ntasks_;
   info_.device_bytes = bytes;
-  info_.kernel_fit_error = fit.max_error;
+  info_.kernel_fit_error = wmode_ ? 0.0 : fit.max_error;
+  info_.nnz = nnz_;
+  info_.occupied_cells = occupied_;
+  info_.work_items = work_items_;
 
   set_norm(1.0);
   if (cfg.power_iters > 0) power_method(cfg.power_iters, cfg.power_tol);
+}
+
+template <typename real>
+void OperatorT<real>::init_plain(const OperatorConfig &cfg, int64_t &bytes, AxisTiling &tu,
+                                 AxisTiling &tv, std::vector<int32_t> &tile_tasks) {
+  // Coverage plan (FP64 coordinates, tile sort, work items, slots).
+  PlanRequest rq;
+  rq.u = cfg.u;
+  rq.v = cfg.v;
+  rq.weights = reinterpret_cast<const std::complex<double> *>(cfg.weights);
+  rq.M = cfg.M;
+  rq.Nu = Nu_;
+  rq.Nv = Nv_;
+  rq.Ju = cfg.Ju;
+  rq.Jv = cfg.Jv;
+  rq.tile = cfg.tile > 0 ? cfg.tile : kTile;
+  rq.max_per_item = cfg.max_per_item > 0 ? cfg.max_per_item : 16;
+  Plan plan;
+  try {
+    plan = build_plan(rq);
+  } catch (const std::invalid_argument &e) {
+    throw Error(kInvalidArgument, e.what());
+  }
+  ntasks_ = int(plan.tasks.size());
+  win_rows_ = plan.win_rows;
+  win_cols_ = plan.win_cols;
+  fold_J_ = J_;
+  S_ = plan.S;
+  unit_weights_ = plan.unit_weights;
+  nnz_ = M_ * int64_t(cfg.Ju) * cfg.Jv;
+  occupied_ = plan.occupied_cells;
+  work_items_ = int64_t(plan.lane_code.size());
+  std::vector<C> fr(S_);
+  for (int64_t i = 0; i < S_; ++i) {
+    // unit weights: the phase sign (-1)^(k_u + k_v) rides in the sign of t_u
+    const double t = (unit_weights_ && plan.flip[i]) ? -plan.frac_u[i] : plan.frac_u[i];
+    fr[i] = C(real(t), real(plan.frac_v[i]));
+  }
+  frac_.alloc(sizeof(C) * S_, &bytes);
+  frac_.upload(fr.data(), sizeof(C) * S_, stream_);
+  std::vector<C> wt;
+  if (!unit_weights_) {
+    wt.resize(S_);
+    for (int64_t i = 0; i < S_; ++i)
+      wt[i] = C(real(plan.weight[i].real()), real(plan.weight[i].imag()));
+    weight_.alloc(sizeof(C) * S_, &bytes);
+    weight_.upload(wt.data(), sizeof(C) * S_, stream_);
+  }
+  slot_user_.alloc(sizeof(int32_t) * S_, &bytes);
+  slot_user_.upload(plan.slot_user.data(), sizeof(int32_t) * S_, stream_);
+  user_slot_.alloc(sizeof(int32_t) * M_, &bytes);
+  user_slot_.upload(plan.user_slot.data(), sizeof(int32_t) * M_, stream_);
+  const size_t nb = plan.batch_base.size();
+  std::vector<int2> bt(nb);
+  for (size_t k = 0; k < nb; ++k) bt[k] = int2{plan.batch_base[k], plan.batch_kmax[k]};
+  batches_.alloc(sizeof(int2) * nb, &bytes);
+  batches_.upload(bt.data(), sizeof(int2) * nb, stream_);
+  lane_code_.alloc(sizeof(int32_t) * plan.lane_code.size(), &bytes);
+  lane_code_.upload(plan.lane_code.data(), sizeof(int32_t) * plan.lane_code.size(), stream_);
+  tasks_.alloc(sizeof(Task) * plan.tasks.size(), &bytes);
+  tasks_.upload(plan.tasks.data(), sizeof(Task) * plan.tasks.size(), stream_);
+  // the staging vectors are pageable: wait before they go out of scope
+  cuda_check(cudaStreamSynchronize(stream_), "upload");
+  tu = plan.tu;
+  tv = plan.tv;
+  tile_tasks = plan.tile_tasks;
+}
+
+template <typename real>
+void OperatorT<real>::init_w(const OperatorConfig &cfg, int64_t &bytes, AxisTiling &tu,
+                             AxisTiling &tv, std::vector<int32_t> &tile_tasks) {
+  WPlanRequest rq;
+  rq.u = cfg.u;
+  rq.v = cfg.v;
+  rq.w = cfg.w;
+  rq.weights = reinterpret_cast<const std::complex<double> *>(cfg.weights);
+  rq.jw_rows = cfg.jw_rows;
+  rq.M = cfg.M;
+  rq.Nu = Nu_;
+  rq.Nv = Nv_;
+  rq.imsizex = Nx_;
+  rq.imsizey = Ny_;
+  rq.oversample_ratio = cfg.oversample_ratio;
+  rq.cellx = cfg.cellx;
+  rq.celly = cfg.celly;
+  rq.J = cfg.Ju;
+  rq.Jw = cfg.Jw;
+  rq.kernel = cfg.kernel;
+  rq.tile = cfg.tile > 0 ? cfg.tile : kTile;
+  WPlan plan;
+  try {
+    plan = build_wplan(rq);
+  } catch (const std::invalid_argument &e) {
+    throw Error(kInvalidArgument, e.what());
+  }
+  if (plan.Smax > kMaxWSupport)
+    throw Error(kUnsupported, "w-projection support above 32 taps per axis");
+  ntasks_ = int(plan.tasks.size());
+  win_rows_ = plan.win_rows;
+  win_cols_ = plan.win_cols;
+  fold_J_ = plan.Smax;
+  S_ = M_;
+  unit_weights_ = false;
+  nnz_ = plan.taps;
+  occupied_ = 0;
+  work_items_ = M_;
+  std::vector<C> wt(M_);
+  for (int64_t i = 0; i < M_; ++i)
+    wt[i] = C(real(plan.weight[i].real()), real(plan.weight[i].imag()));
+  weight_.alloc(sizeof(C) * std::max<int64_t>(M_, 1), &bytes);
+  weight_.upload(wt.data(), sizeof(C) * M_, stream_);
+  wcode_.alloc(sizeof(int32_t) * std::max<int64_t>(M_, 1), &bytes);
+  wcode_.upload(plan.code.data(), sizeof(int32_t) * M_, stream_);
+  wfactor_.alloc(sizeof(int64_t) * std::max<int64_t>(M_, 1), &bytes);
+  wfactor_.upload(plan.factor.data(), sizeof(int64_t) * M_, stream_);
+  slot_user_.alloc(sizeof(int32_t) * std::max<int64_t>(M_, 1), &bytes);
+  slot_user_.upload(plan.slot_user.data(), sizeof(int32_t) * M_, stream_);
+  user_slot_.alloc(sizeof(int32_t) * std::max<int64_t>(M_, 1), &bytes);
+  user_slot_.upload(plan.user_slot.data(), sizeof(int32_t) * M_, stream_);
+  tasks_.alloc(sizeof(Task) * std::max<size_t>(plan.tasks.size(), 1), &bytes);
+  tasks_.upload(plan.tasks.data(), sizeof(Task) * plan.tasks.size(), stream_);
+  cuda_check(cudaStreamSynchronize(stream_), "upload");
+  // Row factors, FP64-generated, uploaded in chunks of rows.
+  wfactors_.alloc(sizeof(C) * std::max<int64_t>(plan.factor_count, 1), &bytes);
+  const int64_t chunk_rows = 1 << 20;
+  std::vector<std::complex<real>> buf;
+  for (int64_t i0 = 0; i0 < M_; i0 += chunk_rows) {
+    const int64_t i1 = std::min(M_, i0 + chunk_rows);
+    const int64_t f0 = plan.factor[i0];
+    const int64_t f1 = i1 < M_ ? plan.factor[i1] : plan.factor_count;
+    buf.resize(size_t(f1 - f0));
+    wplan_factors<real>(plan, i0, i1, buf.data());
+    cuda_check(cudaMemcpy(wfactors_.as<C>() + f0, buf.data(), sizeof(C) * (f1 - f0),
+                          cudaMemcpyHostToDevice),
+               "factor upload");
+  }
+  tu = plan.tu;
+  tv = plan.tv;
+  tile_tasks = plan.tile_tasks;
 }
 
 template <typename real>
@@ -376,6 +483,24 @@ void OperatorT<real>::release(cudaStream_t user) {
 
 template <typename real>
 void OperatorT<real>::degrid_slots(const void *grid, void *caller_vis) {
+  if (wmode_) {
+    WArgs<real> w;
+    w.grid = grid;
+    w.tasks = tasks_.as<Task>();
+    w.code = wcode_.as<int32_t>();
+    w.factor = wfactor_.as<int64_t>();
+    w.factors = wfactors_.get();
+    w.weight = weight_.get();
+    w.slot_out = slots_.get();
+    w.Nu = Nu_;
+    w.Nv = Nv_;
+    w.Smax = fold_J_;
+    mark_begin(kDegrid);
+    cuda_check(launch_wdegrid<real>(w, ntasks_, win_rows_, win_cols_, shape_.threads, stream_),
+               "w degrid");
+    mark_end(kDegrid);
+    return;
+  }
   ApplyArgs<real> a;
   a.grid = grid;
   a.tasks = tasks_.as<Task>();
@@ -395,15 +520,44 @@ void OperatorT<real>::degrid_slots(const void *grid, void *caller_vis) {
 
 template <typename real>
 void OperatorT<real>::grid_slots(void *grid, const void *caller_vis) {
+  grid_core(grid, caller_vis ? caller_vis : slots_.get(),
+            caller_vis ? slot_user_.as<int32_t>() : nullptr, tilebuf_.get());
+}
+
+// G^H from visibilities in slot order (or caller order through slot_user)
+// into `grid`, accumulating in the task windows at `windows`.
+template <typename real>
+void OperatorT<real>::grid_core(void *grid, const void *vis, const int32_t *slot_user,
+                                void *windows) {
+  if (wmode_) {
+    WArgs<real> w;
+    w.tilebuf = windows;
+    w.tasks = tasks_.as<Task>();
+    w.code = wcode_.as<int32_t>();
+    w.factor = wfactor_.as<int64_t>();
+    w.factors = wfactors_.get();
+    w.weight = weight_.get();
+    w.slot_in = vis;
+    w.Nu = Nu_;
+    w.Nv = Nv_;
+    w.Smax = fold_J_;
+    w.slot_stride = slot_stride_;
+    mark_begin(kGrid);
+    cuda_check(launch_wgrid<real>(w, ntasks_, win_rows_, win_cols_, shape_.threads, stream_),
+               "w grid");
+    mark_end(kGrid);
+    fold_into(grid, windows);
+    return;
+  }
   ApplyArgs<real> a;
-  a.tilebuf = tilebuf_.get();
+  a.tilebuf = windows;
   a.tasks = tasks_.as<Task>();
   a.batches = batches_.as<int2>();
   a.lane_code = lane_code_.as<int32_t>();
   a.frac = frac_.get();
   a.weight = unit_weights_ ? nullptr : weight_.get();
-  a.slot_in = caller_vis ? caller_vis : slots_.get();
-  a.slot_user = caller_vis ? slot_user_.as<int32_t>() : nullptr;
+  a.slot_in = vis;
+  a.slot_user = slot_user;
   a.Nu = Nu_;
   a.Nv = Nv_;
   a.slot_stride = slot_stride_;
@@ -411,8 +565,13 @@ void OperatorT<real>::grid_slots(void *grid, const void *caller_vis) {
   cuda_check(launch_grid<real>(a, poly_, J_, ntasks_, win_rows_, win_cols_, shape_, stream_),
              "grid");
   mark_end(kGrid);
+  fold_into(grid, windows);
+}
+
+template <typename real>
+void OperatorT<real>::fold_into(void *grid, const void *windows) {
   FoldArgs f;
-  f.tilebuf = tilebuf_.get();
+  f.tilebuf = windows;
   f.slot_stride = slot_stride_;
   f.tile_tasks = tile_tasks_.as<int32_t>();
   f.tu_start = tu_start_.as<int32_t>();
@@ -421,8 +580,8 @@ void OperatorT<real>::grid_slots(void *grid, const void *caller_vis) {
   f.tv_of = tv_of_.as<int32_t>();
   f.ntu = ntu_;
   f.ntv = ntv_;
-  f.Ju = J_;
-  f.Jv = J_;
+  f.Ju = fold_J_;
+  f.Jv = fold_J_;
   f.Nu = Nu_;
   f.Nv = Nv_;
   f.grid = grid;
@@ -551,39 +710,11 @@ void OperatorT<real>::grid_no_alloc(const void *vis, void *grid, cudaStream_t us
   void *slots = base + (int64_t(sizeof(C)) * slot_stride_ * std::max(ntasks_, 1) + 255) / 256 * 256;
   std::lock_guard<std::mutex> lock(mu_);
   join(user);
-  // expand writes every slot (0 for null slots) and the grid kernel writes
+  // expand writes every slot (0 for null slots) and the grid kernels write
   // every cell of every task window, so nothing left in the array from an
   // earlier call is read.
   cuda_check(launch_expand<real>(vis, slot_user_.as<int32_t>(), slots, S_, stream_), "expand");
-  ApplyArgs<real> a;
-  a.tilebuf = windows;
-  a.tasks = tasks_.as<Task>();
-  a.batches = batches_.as<int2>();
-  a.lane_code = lane_code_.as<int32_t>();
-  a.frac = frac_.get();
-  a.weight = unit_weights_ ? nullptr : weight_.get();
-  a.slot_in = slots;
-  a.Nu = Nu_;
-  a.Nv = Nv_;
-  a.slot_stride = slot_stride_;
-  cuda_check(launch_grid<real>(a, poly_, J_, ntasks_, win_rows_, win_cols_, shape_, stream_),
-             "grid");
-  FoldArgs f;
-  f.tilebuf = windows;
-  f.slot_stride = slot_stride_;
-  f.tile_tasks = tile_tasks_.as<int32_t>();
-  f.tu_start = tu_start_.as<int32_t>();
-  f.tv_start = tv_start_.as<int32_t>();
-  f.tu_of = tu_of_.as<int32_t>();
-  f.tv_of = tv_of_.as<int32_t>();
-  f.ntu = ntu_;
-  f.ntv = ntv_;
-  f.Ju = J_;
-  f.Jv = J_;
-  f.Nu = Nu_;
-  f.Nv = Nv_;
-  f.grid = grid;
-  cuda_check(launch_fold<real>(f, stream_), "fold");
+  grid_core(grid, slots, nullptr, windows);
   release(user);
 }
 
@@ -808,7 +939,10 @@ std::unique_ptr<Operator> Operator::create(const OperatorConfig &cfg) {
     throw Error(kUnsupported, "the GB300 operator requires Ju == Jv");
   if (cfg.Ju < 1 || cfg.Ju > kMaxJ)
     throw Error(kUnsupported, "kernel support must be between 1 and 8 taps");
-  if (cfg.w_term) throw Error(kUnsupported, "w-projection is served by the w-stack operator");
+  if (cfg.w_term && (cfg.M > 0 && !cfg.w))
+    throw Error(kInvalidArgument, "w-projection needs the w coordinates");
+  if (cfg.w_term && (cfg.Jw < 1 || cfg.Jw + cfg.Ju - 1 > kMaxWSupport) && !cfg.jw_rows)
+    throw Error(kUnsupported, "w-projection support Jw + J - 1 must be between 1 and 32");
   if (cfg.threads != 0 && (cfg.threads % 32 != 0 || cfg.threads < 32 || cfg.threads > 256))
     throw Error(kInvalidArgument, "threads must be a multiple of 32 in [32, 256]");
   if (cfg.fp64) return std::unique_ptr<Operator>(new OperatorT<double>(cfg));

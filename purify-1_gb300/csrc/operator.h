@@ -33,6 +33,7 @@ struct OperatorConfig {
   int Ju = 4, Jv = 4;
   bool w_term = false;
   int Jw = 6;
+  const int32_t *jw_rows = nullptr;  // per-row w-support, or null for Jw
   double cellx = 1.0, celly = 1.0;
   bool fp64 = false;
   int device = 0;

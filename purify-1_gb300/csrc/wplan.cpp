@@ -1,0 +1,223 @@
+#include "wplan.h"
+
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+#include <stdexcept>
+
+#include "gridding_kernels.h"
+
+namespace pg {
+namespace {
+constexpr double kPi = 3.14159265358979323846;
+
+double wrap(double x, double y) {
+  double r = std::fmod(x, y);
+  if (r < 0) r += y;
+  return r;
+}
+
+// projection_kernels::pixel_to_lambda (projection_kernels.cc:28-30)
+double pixel_to_lambda(double cell, int imsize, double os) {
+  return 60. * 60. * 180. / cell / std::floor(os * imsize) / kPi;
+}
+
+// The zero-padded linear convolution of convolution.h:42-52,
+// out(j) = sum_k f(k) g_pad(n_out - 1 - j + k), n_out = Jg + Jf - 1.
+void conv1d(const double *f, int Jf, const std::complex<double> *g, int Jg,
+            std::complex<double> *out) {
+  const int n_out = Jg + Jf - 1;
+  for (int j = 0; j < n_out; ++j) {
+    std::complex<double> acc = 0;
+    for (int k = 0; k < Jf; ++k) {
+      const int idx = n_out - 1 - j + k - (Jf - 1);  // index into the unpadded g
+      if (idx >= 0 && idx < Jg) acc += f[k] * g[idx];
+    }
+    out[j] = acc;
+  }
+}
+}  // namespace
+
+WPlan build_wplan(const WPlanRequest &rq) {
+  if (rq.M < 0) throw std::invalid_argument("negative number of visibilities");
+  if (rq.M > 0 && (!rq.u || !rq.v || !rq.w)) throw std::invalid_argument("u, v and w must be given");
+  if (rq.J < 1 || rq.Jw < 1) throw std::invalid_argument("kernel supports must be >= 1");
+  if (rq.M > int64_t(INT32_MAX) - 1) throw std::invalid_argument("too many visibilities");
+  WPlan P;
+  P.M = rq.M;
+  P.Nu = rq.Nu;
+  P.Nv = rq.Nv;
+  P.J = rq.J;
+  const int64_t M = rq.M;
+  std::vector<int32_t> jw(M);
+  int Smax = 1;
+  for (int64_t m = 0; m < M; ++m) {
+    jw[m] = rq.jw_rows ? rq.jw_rows[m] : rq.Jw;
+    if (jw[m] < 1 || jw[m] + rq.J - 1 > 255) throw std::invalid_argument("w-support out of range");
+    Smax = std::max(Smax, int(jw[m] + rq.J - 1));
+  }
+  P.Smax = Smax;
+  P.tu = make_tiling(rq.Nu, rq.tile);
+  P.tv = make_tiling(rq.Nv, rq.tile);
+  if (rq.Nu < Smax || rq.Nv < Smax)
+    throw std::invalid_argument("grid is smaller than the largest w-projection support");
+  for (int b = 0; b < P.tu.n; ++b)
+    if (P.tu.start[b + 1] - P.tu.start[b] < Smax - 1)
+      throw std::invalid_argument("grid width is too small for the w-projection support");
+  for (int b = 0; b < P.tv.n; ++b)
+    if (P.tv.start[b + 1] - P.tv.start[b] < Smax - 1)
+      throw std::invalid_argument("grid height is too small for the w-projection support");
+  const int ntu = P.tu.n, ntv = P.tv.n, ntiles = ntu * ntv;
+
+  // The kernel sees w - mean(w) (operators.h:323).
+  double wmean = 0;
+  for (int64_t m = 0; m < M; ++m) wmean += rq.w[m];
+  if (M > 0) wmean /= double(M);
+
+  // Placement per row (operators.cc:85-96): kw = floor(u - S/2), taps at
+  // kw + 1 .. kw + S (mod N); the phase (-1)^(kw_u + kw_v) goes with the weight.
+  std::vector<int32_t> tile(M), local(M);
+  std::vector<uint8_t> flip(M);
+  for (int64_t m = 0; m < M; ++m) {
+    const int S = jw[m] + rq.J - 1;
+    const double kwu = std::floor(rq.u[m] - S * 0.5), kwv = std::floor(rq.v[m] - S * 0.5);
+    const int q0 = int(wrap(kwu + 1, rq.Nu)), p0 = int(wrap(kwv + 1, rq.Nv));
+    const int a = P.tv.of[p0], b = P.tu.of[q0];
+    tile[m] = a * ntu + b;
+    local[m] = ((p0 - P.tv.start[a]) << 8) | (q0 - P.tu.start[b]);
+    flip[m] = uint8_t((int64_t(kwu) + int64_t(kwv)) & 1);
+  }
+  // Plan order: tile, then support descending (warps take visibilities in
+  // turn, so neighbours in this order cost about the same), then caller order.
+  std::vector<int32_t> order(M);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
+    if (tile[x] != tile[y]) return tile[x] < tile[y];
+    return jw[x] > jw[y];
+  });
+  P.code.resize(M);
+  P.factor.resize(M);
+  P.weight.resize(M);
+  P.slot_user.resize(M);
+  P.user_slot.resize(M);
+  int64_t off = 0;
+  for (int64_t i = 0; i < M; ++i) {
+    const int32_t m = order[i];
+    const int S = jw[m] + rq.J - 1;
+    const int lp = local[m] >> 8, lq = local[m] & 0xff;  // item_pack layout below
+    P.code[i] = lp | (lq << 8) | (S << 16);
+    P.factor[i] = off;
+    off += int64_t(6) * S;
+    const std::complex<double> wgt = rq.weights ? rq.weights[m] : std::complex<double>(1.0, 0.0);
+    P.weight[i] = flip[m] ? -wgt : wgt;
+    P.slot_user[i] = m;
+    P.user_slot[m] = int32_t(i);
+    P.taps += int64_t(S) * S;
+  }
+  P.factor_count = off;
+  P.kernel = rq.kernel;
+  P.oversample_ratio = rq.oversample_ratio;
+  P.du_lambda = pixel_to_lambda(rq.cellx, rq.imsizex, rq.oversample_ratio);
+  P.dv_lambda = pixel_to_lambda(rq.celly, rq.imsizey, rq.oversample_ratio);
+  P.gen_u.resize(M);
+  P.gen_v.resize(M);
+  P.gen_w.resize(M);
+  P.gen_jw.resize(M);
+  for (int64_t i = 0; i < M; ++i) {
+    const int32_t m = order[i];
+    P.gen_u[i] = rq.u[m];
+    P.gen_v[i] = rq.v[m];
+    P.gen_w[i] = rq.w[m] - wmean;
+    P.gen_jw[i] = jw[m];
+  }
+
+  // Tasks: consecutive visibilities of one tile, bounded in taps.
+  P.tile_tasks.assign(ntiles + 1, 0);
+  int64_t i = 0;
+  for (int t = 0; t < ntiles; ++t) {
+    const int a = t / ntu, b = t % ntu;
+    int64_t e = i;
+    while (e < M && tile[order[e]] == t) ++e;
+    int64_t s = i;
+    while (s < e) {
+      int64_t k = s, taps = 0;
+      while (k < e && (k == s || taps + (P.code[k] >> 16) * (P.code[k] >> 16) <= rq.max_taps_per_task)) {
+        taps += int64_t(P.code[k] >> 16) * (P.code[k] >> 16);
+        ++k;
+      }
+      Task tk{};
+      tk.P = P.tv.start[a];
+      tk.Q = P.tu.start[b];
+      tk.H = P.tv.start[a + 1] - P.tv.start[a];
+      tk.W = P.tu.start[b + 1] - P.tu.start[b];
+      tk.batch_begin = int32_t(s);
+      tk.batch_end = int32_t(k);
+      tk.tile = t;
+      P.tasks.push_back(tk);
+      s = k;
+    }
+    P.tile_tasks[t + 1] = int32_t(P.tasks.size());
+    P.win_rows = std::max(P.win_rows, P.tv.start[a + 1] - P.tv.start[a] + Smax - 1);
+    P.win_cols = std::max(P.win_cols, P.tu.start[b + 1] - P.tu.start[b] + Smax - 1);
+    i = e;
+  }
+  return P;
+}
+
+template <typename T>
+void wplan_factors(const WPlan &P, int64_t i0, int64_t i1, std::complex<T> *out) {
+  const int J = P.J;
+  const GriddingKernel kern(P.kernel, J, P.oversample_ratio);
+  const double dul = P.du_lambda, dvl = P.dv_lambda;
+  const int64_t base = i0 < int64_t(P.factor.size()) ? P.factor[i0] : 0;
+#pragma omp parallel
+  {
+    std::vector<double> fu(J), fv(J);
+    std::vector<std::complex<double>> alpha(3 * 256), beta(3 * 256), row(6 * 256);
+#pragma omp for schedule(dynamic, 1024)
+    for (int64_t i = i0; i < i1; ++i) {
+      const double u = P.gen_u[i], v = P.gen_v[i], w = P.gen_w[i];
+      const int Jw = P.gen_jw[i], S = Jw + J - 1;
+      // Kaiser-Bessel (or other) taps: projection_kernels.cc:66-75
+      const double du = u - std::floor(u - J * 0.5), dv = v - std::floor(v - J * 0.5);
+      for (int k = 0; k < J; ++k) {
+        fu[k] = kern.value(du - k - 1);
+        fv[k] = kern.value(dv - k - 1);
+      }
+      // w-kernel samples: sample (row jv, column ju) = kernelw(dwu - ju - 1,
+      // dwv - jv - 1, w) (projection_kernels.cc:76-82, 31-47)
+      const double dwu = u - std::floor(u - Jw * 0.5), dwv = v - std::floor(v - Jw * 0.5);
+      std::complex<double> *a1 = &alpha[0], *a2 = &alpha[256], *a3 = &alpha[512];
+      std::complex<double> *b1 = &beta[0], *b2 = &beta[256], *b3 = &beta[512];
+      const std::complex<double> c = std::complex<double>(1.0 / w, 0.0) / std::complex<double>(0, 1);
+      // g = (a~ / (w i)) b~^T + (1 - chi_v) 1^T + chi_v (1 - chi_u)^T: every
+      // sample comes from exactly one term, so no term cancels another.
+      for (int k = 0; k < Jw; ++k) {
+        const double U = dwu - k - 1, V = dwv - k - 1;
+        const bool ok_u = std::abs(U * dul / w) < 1, ok_v = std::abs(V * dvl / w) < 1;
+        const double uu = U * dul, vv = V * dvl;
+        a1[k] = ok_v ? c * std::exp(std::complex<double>(0, -kPi * vv * vv / w)) : 0.0;
+        b1[k] = ok_u ? std::exp(std::complex<double>(0, -kPi * uu * uu / w)) : 0.0;
+        a2[k] = ok_v ? 0.0 : 1.0;
+        b2[k] = 1.0;
+        a3[k] = ok_v ? 1.0 : 0.0;
+        b3[k] = ok_u ? 0.0 : 1.0;
+      }
+      for (int r = 0; r < 3; ++r) {
+        conv1d(fv.data(), J, &alpha[256 * r], Jw, &row[r * S]);
+        conv1d(fu.data(), J, &beta[256 * r], Jw, &row[(3 + r) * S]);
+      }
+      std::complex<T> *dst = out + (P.factor[i] - base);
+      for (int r = 0; r < 6; ++r)
+        for (int k = 0; k < S; ++k) {
+          const std::complex<double> z = (k & 1) ? -row[r * S + k] : row[r * S + k];
+          dst[r * S + k] = std::complex<T>(T(z.real()), T(z.imag()));
+        }
+    }
+  }
+}
+
+template void wplan_factors<float>(const WPlan &, int64_t, int64_t, std::complex<float> *);
+template void wplan_factors<double>(const WPlan &, int64_t, int64_t, std::complex<double> *);
+
+}  // namespace pg

@@ -47,7 +47,7 @@ class CreateArgs(ctypes.Structure):
         ("power_tol", ctypes.c_double), ("kernel", ctypes.c_int32),
         ("Ju", ctypes.c_uint32), ("Jv", ctypes.c_uint32), ("w_term", ctypes.c_int32),
         ("Jw", ctypes.c_uint32), ("cellx", ctypes.c_double), ("celly", ctypes.c_double),
-        ("precision", ctypes.c_int32), ("device", ctypes.c_int32),
+        ("precision", ctypes.c_int32), ("device", ctypes.c_int32), ("jw_rows", ctypes.c_void_p),
     ]
 
 
@@ -79,7 +79,7 @@ EXPORTS = [
     "purify_gb300_kernel_taps", "purify_gb300_degrid", "purify_gb300_grid",
     "purify_gb300_correction", "purify_gb300_stage_timing", "purify_gb300_stage_times",
     "purify_gb300_operator_create_tuned", "purify_gb300_grid_no_alloc",
-    "purify_gb300_grid_no_alloc_bytes",
+    "purify_gb300_grid_no_alloc_bytes", "purify_gb300_wrow_taps",
 ]
 STAGES = ["pad", "fft_forward", "degrid", "grid", "fold", "fft_inverse", "crop", "compact",
           "expand"]
@@ -130,6 +130,10 @@ def load(path=None):
                                           ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double, vp]
     L.purify_gb300_grid_no_alloc.argtypes = [vp, vp, vp, vp]
     L.purify_gb300_grid_no_alloc_bytes.argtypes = [vp, P(ctypes.c_int64)]
+    L.purify_gb300_wrow_taps.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int32,
+                                         ctypes.c_double, ctypes.c_uint32, ctypes.c_uint32,
+                                         ctypes.c_double, ctypes.c_double, vp]
     L.purify_gb300_stage_timing.argtypes = [vp, ctypes.c_int]
     L.purify_gb300_stage_times.argtypes = [vp, vp, vp]
     _lib = L
@@ -173,6 +177,18 @@ def kernel_taps(kernel, J, t, oversample_ratio=2.0, precision="fp32"):
                                            PRECISIONS[precision], _np_ptr(t), t.size,
                                            _np_ptr(out), ctypes.byref(err)))
     return out, err.value
+
+
+def wrow_taps(u, v, w_centered, Jw, J, kernel="kb", oversample_ratio=2.0, imsizey=64,
+              imsizex=64, cellx=1.0, celly=1.0):
+    """One w-projection gridding-matrix row (S x S, phase included, weight 1)
+    as the device rebuilds it from its factors (purify_gb300_wrow_taps)."""
+    S = int(Jw) + int(J) - 1
+    out = np.empty(S * S, dtype=np.complex128)
+    _check(load().purify_gb300_wrow_taps(float(u), float(v), float(w_centered), int(Jw), int(J),
+                                         KERNELS[kernel], float(oversample_ratio), int(imsizey),
+                                         int(imsizex), float(cellx), float(celly), _np_ptr(out)))
+    return out.reshape(S, S)
 
 
 class CoveragePlan:
@@ -222,7 +238,7 @@ class MeasurementOperator:
     def __init__(self, u, v, w=None, weights=None, imsizey=256, imsizex=256,
                  oversample_ratio=2.0, power_iters=100, power_tol=1e-4, kernel="kb", Ju=4, Jv=4,
                  w_term=False, Jw=6, cellx=1.0, celly=1.0, precision="fp32", device=0,
-                 tuning=None):
+                 tuning=None, jw_rows=None):
         L = load()
         u = np.ascontiguousarray(u, dtype=np.float64).ravel()
         v = np.ascontiguousarray(v, dtype=np.float64).ravel()
@@ -245,6 +261,9 @@ class MeasurementOperator:
         a.Ju, a.Jv = int(Ju), int(Jv)
         a.w_term = 1 if w_term else 0
         a.Jw = int(Jw)
+        jw = None if jw_rows is None else np.ascontiguousarray(jw_rows, dtype=np.int32).ravel()
+        self._jw = jw
+        a.jw_rows = _np_ptr(jw)
         a.cellx, a.celly = float(cellx), float(celly)
         a.precision = PRECISIONS[precision]
         a.device = int(device)

@@ -77,3 +77,27 @@ def config_large(M=10_000_000, seed=0):
     u, v = mixed_uv(M, 2048, 2048, 0.7, 0.15, seed=seed)
     return dict(u=u, v=v, imsizey=1024, imsizex=1024, kernel="kb", Ju=6, Jv=6,
                 x=sky_image(1024, 1024, seed=seed))
+
+
+def wproj_supports(w, w_max, J=4, s_min=4, s_max=24):
+    """Per-row w-supports for the w-projection workload: the total support
+    S = Jw + J - 1 grows affinely with |w - mean(w)| from s_min at w = 0 to
+    s_max at |w| = w_max; returns Jw per row."""
+    wc = np.abs(np.asarray(w) - np.mean(w))
+    S = np.clip(np.rint(s_min + (s_max - s_min) * wc / w_max), s_min, s_max).astype(np.int32)
+    return S - (J - 1)
+
+
+def config_wproj(M=20_000_000, imsize=2048, cell=1.0, seed=0):
+    """2048^2 image, 4096^2 grid, 70% core + 30% uniform uv, w ~ U(-w_max,
+    w_max) with w_max = 12 grid pixels in wavelengths (so the validity region
+    of the small-angle w-kernel spans about 24 taps at |w| = w_max), KB J=4,
+    per-row support 4..24 taps per axis."""
+    N = 2 * imsize
+    u, v = mixed_uv(M, N, N, 0.7, 0.15, seed=seed)
+    du = 60.0 * 60.0 * 180.0 / cell / N / np.pi
+    w_max = 12.0 * du
+    w = np.random.default_rng(seed + 17).uniform(-w_max, w_max, M)
+    return dict(u=u, v=v, w=w, jw_rows=wproj_supports(w, w_max), imsizey=imsize, imsizex=imsize,
+                cellx=cell, celly=cell, kernel="kb", Ju=4, Jv=4, w_max=w_max,
+                x=sky_image(imsize, imsize, seed=seed))
