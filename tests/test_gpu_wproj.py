@@ -85,6 +85,7 @@ def test_w_power_method_and_determinism(pg, oracle_mod, cuda):
     n_gpu = ops[0].power_method(50, 0.0)
     n_ref = oop.power_method(50, 0.0)
     assert abs(n_gpu - n_ref) / n_ref < 1e-12
+    assert ops[1].power_method(50, 0.0) == n_gpu
     x = _to(torch, np.random.default_rng(1).standard_normal(n * n), "fp64")
     a = ops[0].adjoint(ops[0].forward(x))
     b = ops[1].adjoint(ops[1].forward(x))
