@@ -40,8 +40,10 @@ def parse():
     p.add_argument("--steps", type=int, default=50)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    p.add_argument("--workload", choices=["imaging", "wproj"], default="imaging",
-                   help="imaging: the 1024^2 / 1e7 headline; wproj: 2048^2 / 2e7 w-projection")
+    p.add_argument("--workload", choices=["imaging", "wproj", "batch"], default="imaging",
+                   help="imaging: the 1024^2 / 1e7 headline; wproj: 2048^2 / 2e7 w-projection; "
+                        "batch: 64 channels in one graph-replayed grouped step")
+    p.add_argument("--channels", type=int, default=64, help="channels of the batch workload")
     p.add_argument("--M", type=int, default=0, help="visibilities (0: the workload's own)")
     p.add_argument("--imsize", type=int, default=1024)
     p.add_argument("--J", type=int, default=6)
@@ -530,9 +532,219 @@ def run_wproj(args):
     print(json.dumps(out), flush=True)
 
 
+BATCH_WORKLOAD = ("64 channels, image %s^2 drawn per channel, M log-uniform in [1e4, 2e6], "
+                  "70% Gaussian core sigma = 0.15 N (1 + 0.01 k) + 30% uniform, KB J=4, FP32")
+
+
+def run_batch(args):
+    """Batched channels: one step = Phi then Phi^H of every channel, replayed
+    from one CUDA graph; compared with the same applies made channel by
+    channel through single operators."""
+    import torch
+    import purify_gb300 as pgb
+    from purify_gb300 import synthetic
+    pgb.build()
+    dev = torch.device("cuda", 0)
+    t0 = time.perf_counter()
+    chans = synthetic.config_batch(args.channels, seed=0)
+    t_gen = time.perf_counter() - t0
+    Ms = [c["u"].size for c in chans]
+    Mtot = int(sum(Ms))
+    npix = [c["imsizey"] * c["imsizex"] for c in chans]
+    t0 = time.perf_counter()
+    b = pgb.Batch(chans, J=4, precision="fp32")
+    t_create = time.perf_counter() - t0
+    tuning = b.tuning
+    t0 = time.perf_counter()
+    norms = b.power_method(args.power_iters, 1e-4) if args.power_iters > 0 else np.ones(len(chans))
+    t_power = time.perf_counter() - t0
+    info = b.info()
+    stream = torch.cuda.current_stream(dev)
+    xs = [torch.from_numpy(c["x"]).to(torch.complex64).to(dev) for c in chans]
+    vis = [torch.empty(m, dtype=torch.complex64, device=dev) for m in Ms]
+    xo = [torch.empty(n, dtype=torch.complex64, device=dev) for n in npix]
+    b.bind(xs, vis, xo, stream)
+    for _ in range(args.warmup):
+        b.apply(3, stream)
+    torch.cuda.synchronize(dev)
+    sampler = ClockSampler(0)
+    time.sleep(0.5)
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    torch.cuda.synchronize(dev)
+    w0 = time.time()
+    evs[0].record(stream)
+    for k in range(args.steps):
+        b.apply(3, stream)
+        evs[k + 1].record(stream)
+    torch.cuda.synchronize(dev)
+    w1 = time.time()
+    time.sleep(0.3)
+    sampler.stop()
+    clocks = sampler.summary(sampler.window(w0 - 0.25, w1 + 0.25)) or sampler.summary(sampler.rows)
+    per_step = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
+    ms = evs[0].elapsed_time(evs[-1]) / args.steps
+    # grouped gridding launches alone (same kernels as inside the step)
+    t_deg = b.time(8, 10)
+    t_grd = b.time(16, 10)
+    t_fwd = b.time(1, 10)
+    t_adj = b.time(2, 10)
+    s8 = 8
+    NuNv = [4 * n for n in npix]
+    alg_deg = sum(m * (16 + 2 * s8) for m in Ms) + s8 * sum(NuNv)
+    peak, peak_kind = measured_peak()
+    kern, dur = ("degrid", t_deg) if t_deg >= t_grd else ("grid", t_grd)
+    b_step = sum(2 * m * (16 + 2 * s8) for m in Ms) + s8 * sum(7 * g + 3 * n
+                                                               for g, n in zip(NuNv, npix))
+    out = {
+        "metric": "batched degrid+grid Mvis/s (Phi then Phi^H of every channel per step), FP32",
+        "value": Mtot / (ms * 1e-3) / 1e6, "unit": "Mvis/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic: seeded (PCG64)",
+        "config": {"workload": BATCH_WORKLOAD % "{256,512,1024}", "channels": len(chans),
+                   "visibilities": Mtot, "pixels": int(sum(npix)),
+                   "sizes": {str(n): int(sum(1 for c in chans if c["imsizex"] == n))
+                             for n in (256, 512, 1024)},
+                   "l2": "inputs larger than L2 (%.0f MB of coverage state and visibilities "
+                         "per step)" % (Mtot * 24 / 1e6)},
+        "tuning": tuning, "latency_ms": {"p50": float(np.percentile(per_step, 50)),
+                                         "p99": float(np.percentile(per_step, 99))},
+        "stage_ms": {"forward": t_fwd, "adjoint": t_adj, "degrid_launch": t_deg,
+                     "grid_launch": t_grd},
+        "create_s": t_create, "generate_s": t_gen, "power_method_s": t_power,
+        "power_iters": args.power_iters, "device_bytes": info["device_bytes"],
+        "gpu_launches": 6 * args.steps, "clocks": clocks,
+        "roofline": {"bound": "hbm", "kernel": kern, "algorithmic_bytes": alg_deg,
+                     "achieved": alg_deg / (dur * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": alg_deg / (dur * 1e-3) / 1e9 / peak, "peak_source": peak_kind,
+                     "traffic": None},
+        "step_roofline": {"algorithmic_bytes": b_step,
+                          "achieved_gbs": b_step / (ms * 1e-3) / 1e9,
+                          "frac": b_step / (ms * 1e-3) / 1e9 / peak},
+    }
+    # the same work as single-channel applies, one channel after another
+    ops = [pgb.MeasurementOperator(c["u"], c["v"], None, None, c["imsizey"], c["imsizex"], 2.0,
+                                   power_iters=0, kernel="kb", Ju=4, Jv=4, precision="fp32")
+           for c in chans]
+    for op, nrm in zip(ops, norms):
+        op.set_norm(float(nrm))
+    vis1 = [torch.empty_like(t) for t in vis]
+    xo1 = [torch.empty_like(t) for t in xo]
+
+    def seq_step():
+        for k, op in enumerate(ops):
+            op.forward_into(xs[k], vis1[k], stream)
+            op.adjoint_into(vis1[k], xo1[k], stream)
+    for _ in range(max(1, args.warmup)):
+        seq_step()
+    ks = max(3, args.steps // 5)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    for _ in range(ks):
+        seq_step()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms_seq = e0.elapsed_time(e1) / ks
+    b.apply(3, stream)
+    torch.cuda.synchronize(dev)
+    err_v = max(rel_l2(vis[k].cpu().numpy(), vis1[k].cpu().numpy()) for k in range(len(chans)))
+    err_x = max(rel_l2(xo[k].cpu().numpy(), xo1[k].cpu().numpy()) for k in range(len(chans)))
+    out["sequential_single_channel"] = {
+        "value": Mtot / (ms_seq * 1e-3) / 1e6, "ms_per_step": ms_seq,
+        "speedup_batch_over_sequential": ms_seq / ms,
+        "max_rel_l2_batch_vs_single": {"forward": err_v, "adjoint": err_x}}
+    del ops, vis1, xo1
+    # FP64 batch: same channels, same tuning
+    if not args.no_fp64:
+        b64 = pgb.Batch(chans, J=4, precision="fp64", tuning=tuning)
+        b64.set_norms(norms)
+        xs64 = [torch.from_numpy(c["x"]).to(dev) for c in chans]
+        vis64 = [torch.empty(m, dtype=torch.complex128, device=dev) for m in Ms]
+        xo64 = [torch.empty(n, dtype=torch.complex128, device=dev) for n in npix]
+        b64.bind(xs64, vis64, xo64, stream)
+        for _ in range(max(1, args.warmup)):
+            b64.apply(3, stream)
+        k64 = max(3, args.steps // 5)
+        e0.record(stream)
+        for _ in range(k64):
+            b64.apply(3, stream)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms64 = e0.elapsed_time(e1) / k64
+        b.apply(3, stream)
+        torch.cuda.synchronize(dev)
+        fwd_err = max(rel_l2(vis[k].cpu().numpy(), vis64[k].cpu().numpy())
+                      for k in range(len(chans)))
+        adj_err = max(rel_l2(xo[k].cpu().numpy(), xo64[k].cpu().numpy())
+                      for k in range(len(chans)))
+        out["fp64"] = {"value": Mtot / (ms64 * 1e-3) / 1e6, "ms_per_step": ms64,
+                       "speedup_fp32_over_fp64": ms64 / ms}
+        out["rel_l2_fp32_vs_fp64_max_channel"] = {"forward": fwd_err, "adjoint": adj_err}
+        del b64, xs64, vis64, xo64
+    # end to end: pinned host images in, visibilities and adjoint images out
+    if args.e2e_steps > 0:
+        xh = [x.cpu().pin_memory() for x in xs]
+        vh = [torch.empty(m, dtype=torch.complex64).pin_memory() for m in Ms]
+        xoh = [torch.empty(n, dtype=torch.complex64).pin_memory() for n in npix]
+
+        def e2e_step():
+            for k in range(len(chans)):
+                xs[k].copy_(xh[k], non_blocking=True)
+            b.apply(3, stream)
+            for k in range(len(chans)):
+                vh[k].copy_(vis[k], non_blocking=True)
+                xoh[k].copy_(xo[k], non_blocking=True)
+            torch.cuda.synchronize(dev)
+        e2e_step()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            e2e_step()
+        t_e2e = (time.perf_counter() - t0) / args.e2e_steps
+        out["e2e"] = {"value": Mtot / t_e2e / 1e6, "unit": "Mvis/s", "ms_per_step": t_e2e * 1e3,
+                      "h2d_bytes_per_step": 8 * int(sum(npix)),
+                      "d2h_bytes_per_step": 8 * (Mtot + int(sum(npix))),
+                      "api": "Batch.bind once + Batch.apply(3) per step, c64 pinned host copies"}
+    if not args.no_cpu_baseline:
+        # FP64 oracle: fixed cost (pad + FFT + crop) per image size, per-visibility
+        # cost from a sample of the largest channel, summed over the channels
+        try:
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import oracle
+            oracle.build()
+            fixed = {}
+            for n in sorted({c["imsizex"] for c in chans}):
+                op0 = oracle.Operator(np.zeros(0), np.zeros(0), None, None, n, n, 2.0,
+                                      kernel="kb", Ju=4, Jv=4)
+                x0 = synthetic.sky_image(n, n)
+                t0 = time.perf_counter()
+                op0.adjoint(op0.forward(x0))
+                fixed[n] = time.perf_counter() - t0
+            big = int(np.argmax(Ms))
+            c = chans[big]
+            Msmp = min(args.cpu_sample, Ms[big])
+            ops_ = oracle.Operator(c["u"][:Msmp], c["v"][:Msmp], None, None, c["imsizey"],
+                                   c["imsizex"], 2.0, kernel="kb", Ju=4, Jv=4)
+            t0 = time.perf_counter()
+            ops_.adjoint(ops_.forward(c["x"]))
+            t_s = time.perf_counter() - t0
+            per_vis = max(t_s - fixed[c["imsizex"]], 0.0) / Msmp
+            t_full = sum(fixed[ch["imsizex"]] for ch in chans) + per_vis * Mtot
+            out["cpu_baseline"] = {
+                "value": Mtot / t_full / 1e6, "unit": "Mvis/s", "cores": oracle.get_threads(),
+                "kind": "port",
+                "sample": "FP64 oracle: pad+FFT+crop timed once per image size with M=0, "
+                          "per-visibility cost from %d visibilities of channel %d; summed over "
+                          "the %d channels" % (Msmp, big, len(chans))}
+        except Exception as e:
+            out["cpu_baseline"] = {"error": str(e)}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
-    if args.workload == "wproj" and args.impl == "gb300":
+    if args.workload == "batch" and args.impl == "gb300":
+        run_batch(args)
+    elif args.workload == "wproj" and args.impl == "gb300":
         run_wproj(args)
     elif args.impl == "reference":
         run_reference(args)

@@ -243,6 +243,72 @@ int purify_gb300_wrow_taps(double u, double v, double w_centered, uint32_t Jw, u
                            int32_t kernel, double oversample_ratio, uint32_t imsizey,
                            uint32_t imsizex, double cellx, double celly, double *out);
 
+/* ---- Multi-channel batch -------------------------------------------------
+ * Many operators (frequency channels or snapshots, each with its own coverage,
+ * visibility count and image size; one kernel, support and oversampling)
+ * applied together.  A step over all channels is a fixed set of grouped
+ * launches -- one degrid and one grid launch over every channel's tasks,
+ * element-wise kernels over all channels, one batched cuFFT per grid size --
+ * recorded once into a CUDA graph and replayed.  Each channel's result is
+ * that of a single operator built from its coverage (within the precision's
+ * rounding).  The reference applies such a set one operator after another
+ * (init_combine_operators / init_super_operator, operators.h:513-578). */
+typedef struct purify_gb300_batch purify_gb300_batch;
+typedef struct {
+  const double *u, *v;    /* M coordinates in grid pixels */
+  const double *weights;  /* M complex<double>, or NULL for ones */
+  int64_t M;
+  uint32_t imsizey, imsizex;
+} purify_gb300_channel;
+/* Tile edge and CTA sizes of a batch.  No counterpart in the reference. */
+typedef struct {
+  int32_t tile;            /* uv tile edge in grid cells */
+  int32_t max_per_item;    /* visibilities of one base cell given to one lane */
+  int32_t degrid_threads;  /* CTA threads of the grouped degrid launch */
+  int32_t grid_threads;    /* CTA threads of the grouped grid launch */
+} purify_gb300_batch_tuning;
+/* Builds the batch (plans every channel, uploads the coverage state).  With
+ * tuning == NULL the autotuner picks the tile edge and CTA sizes by timing
+ * candidates on the GPU (a sample of up to 8 channels; cached per process).
+ * Norms start at 1; see purify_gb300_batch_power_method. */
+int purify_gb300_batch_create(const purify_gb300_channel *channels, int32_t nch,
+                              double oversample_ratio, int32_t kernel, uint32_t J,
+                              int32_t precision, int32_t device,
+                              const purify_gb300_batch_tuning *tuning, purify_gb300_batch **out);
+int purify_gb300_batch_destroy(purify_gb300_batch *b);
+/* The tuning the batch runs with (the autotuner's pick when it chose). */
+int purify_gb300_batch_get_tuning(const purify_gb300_batch *b, purify_gb300_batch_tuning *t);
+/* Binds per-channel device buffers (arrays of nch pointers; complex of the
+ * batch's precision): x_in (imsizey*imsizex, forward input), vis (M, forward
+ * output and adjoint input), x_out (imsizey*imsizex, adjoint output).  Any
+ * array may be NULL when the directions that use it are not applied.  The
+ * pointers live in device tables read by the recorded graph, so rebinding
+ * needs no new recording.  Ordered on `stream` like an apply. */
+int purify_gb300_batch_bind(purify_gb300_batch *b, const void *const *x_in, void *const *vis,
+                            void *const *x_out, void *stream);
+/* One step over every channel: directions 1 = Phi (x_in -> vis), 2 = Phi^H
+ * (vis -> x_out), 3 = both in turn (x_out = Phi^H Phi x_in).  Ordered after
+ * prior work on `stream`; later work on `stream` sees the results. */
+int purify_gb300_batch_apply(purify_gb300_batch *b, int32_t directions, void *stream);
+/* Power method of every channel together, each channel with the
+ * single-operator rule (operators.h:390-391); sets the per-channel norms and
+ * writes them to norms (nch doubles) when not NULL.  Synchronous. */
+int purify_gb300_batch_power_method(purify_gb300_batch *b, uint32_t iters, double tol,
+                                    double *norms);
+int purify_gb300_batch_set_norms(purify_gb300_batch *b, const double *norms);
+int purify_gb300_batch_get_norms(const purify_gb300_batch *b, double *norms);
+typedef struct {
+  int32_t channels, size_groups;
+  int64_t visibilities, pixels, tasks, device_bytes;
+} purify_gb300_batch_info;
+int purify_gb300_batch_info_get(const purify_gb300_batch *b, purify_gb300_batch_info *info);
+/* Average device milliseconds of one replay over `reps` replays (after two
+ * untimed ones) on the batch's own scratch buffers: what = 1, 2, 3 as in
+ * purify_gb300_batch_apply, 8 = the grouped degrid launch alone, 16 = the
+ * grouped grid launch alone.  The binding is kept.  No counterpart in the
+ * reference; used by the autotuner and the benchmark. */
+int purify_gb300_batch_time(purify_gb300_batch *b, int32_t what, uint32_t reps, double *ms);
+
 /* Message of the last failing call on this thread ("" when none). */
 const char *purify_gb300_last_error(void);
 /* Library version string. */

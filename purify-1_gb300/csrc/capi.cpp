@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "../../include/purify_gb300.h"
+#include "batch.h"
 #include "gridding_kernels.h"
 #include "operator.h"
 #include "plan.h"
@@ -19,6 +20,11 @@ struct purify_gb300_operator {
 };
 struct purify_gb300_plan {
   pg::Plan plan;
+};
+struct purify_gb300_batch {
+  std::unique_ptr<pg::Batch> impl;
+  pg::BatchTuning tuning;
+  int nch = 0;
 };
 
 namespace {
@@ -428,6 +434,109 @@ int purify_gb300_kernel_taps(int32_t kernel, uint32_t J, double os, int32_t prec
       }
     }
   });
+}
+
+int purify_gb300_batch_create(const purify_gb300_channel *channels, int32_t nch,
+                              double oversample_ratio, int32_t kernel, uint32_t J,
+                              int32_t precision, int32_t device,
+                              const purify_gb300_batch_tuning *tuning, purify_gb300_batch **out) {
+  if (!out) return null_arg("out");
+  if (!channels) return null_arg("channels");
+  return guard([&] {
+    if (nch < 1) throw pg::Error(pg::kInvalidArgument, "a batch needs at least one channel");
+    if (precision != PURIFY_GB300_FP32 && precision != PURIFY_GB300_FP64)
+      throw pg::Error(pg::kInvalidArgument, "unknown precision");
+    pg::BatchConfig cfg;
+    cfg.channels.resize(nch);
+    for (int c = 0; c < nch; ++c) {
+      pg::ChannelSpec &s = cfg.channels[c];
+      s.u = channels[c].u;
+      s.v = channels[c].v;
+      s.weights = reinterpret_cast<const std::complex<double> *>(channels[c].weights);
+      s.M = channels[c].M;
+      s.imsizey = int(channels[c].imsizey);
+      s.imsizex = int(channels[c].imsizex);
+    }
+    cfg.oversample_ratio = oversample_ratio;
+    cfg.kernel = kernel;
+    cfg.J = int(J);
+    cfg.fp64 = precision == PURIFY_GB300_FP64;
+    cfg.device = device;
+    pg::BatchTuning t;
+    if (tuning) {
+      t.tile = tuning->tile > 0 ? tuning->tile : pg::kTile;
+      t.max_per_item = tuning->max_per_item > 0 ? tuning->max_per_item : 16;
+      t.degrid_threads = tuning->degrid_threads > 0 ? tuning->degrid_threads : 128;
+      t.grid_threads = tuning->grid_threads > 0 ? tuning->grid_threads : 128;
+    } else {
+      t = pg::autotune_batch(cfg);
+    }
+    cfg.tile = t.tile;
+    cfg.max_per_item = t.max_per_item;
+    cfg.threads = 128;
+    cfg.degrid_threads = t.degrid_threads;
+    cfg.grid_threads = t.grid_threads;
+    std::unique_ptr<purify_gb300_batch> b(new purify_gb300_batch);
+    b->impl = pg::Batch::create(cfg);
+    b->tuning = t;
+    b->nch = nch;
+    *out = b.release();
+  });
+}
+int purify_gb300_batch_destroy(purify_gb300_batch *b) {
+  delete b;
+  return PURIFY_GB300_OK;
+}
+int purify_gb300_batch_get_tuning(const purify_gb300_batch *b, purify_gb300_batch_tuning *t) {
+  if (!b) return null_arg("batch");
+  if (!t) return null_arg("tuning");
+  t->tile = b->tuning.tile;
+  t->max_per_item = b->tuning.max_per_item;
+  t->degrid_threads = b->tuning.degrid_threads;
+  t->grid_threads = b->tuning.grid_threads;
+  return PURIFY_GB300_OK;
+}
+int purify_gb300_batch_bind(purify_gb300_batch *b, const void *const *x_in, void *const *vis,
+                            void *const *x_out, void *stream) {
+  if (!b) return null_arg("batch");
+  return guard([&] { b->impl->bind(x_in, vis, x_out, static_cast<cudaStream_t>(stream)); });
+}
+int purify_gb300_batch_apply(purify_gb300_batch *b, int32_t directions, void *stream) {
+  if (!b) return null_arg("batch");
+  return guard([&] { b->impl->apply(directions, static_cast<cudaStream_t>(stream)); });
+}
+int purify_gb300_batch_power_method(purify_gb300_batch *b, uint32_t iters, double tol,
+                                    double *norms) {
+  if (!b) return null_arg("batch");
+  return guard([&] { b->impl->power_method(int(iters), tol, norms); });
+}
+int purify_gb300_batch_set_norms(purify_gb300_batch *b, const double *norms) {
+  if (!b) return null_arg("batch");
+  if (!norms) return null_arg("norms");
+  return guard([&] { b->impl->set_norms(norms); });
+}
+int purify_gb300_batch_get_norms(const purify_gb300_batch *b, double *norms) {
+  if (!b) return null_arg("batch");
+  if (!norms) return null_arg("norms");
+  b->impl->get_norms(norms);
+  return PURIFY_GB300_OK;
+}
+int purify_gb300_batch_time(purify_gb300_batch *b, int32_t what, uint32_t reps, double *ms) {
+  if (!b) return null_arg("batch");
+  if (!ms) return null_arg("ms");
+  return guard([&] { *ms = b->impl->time_apply(what, int(reps)); });
+}
+int purify_gb300_batch_info_get(const purify_gb300_batch *b, purify_gb300_batch_info *info) {
+  if (!b) return null_arg("batch");
+  if (!info) return null_arg("info");
+  const pg::BatchInfo i = b->impl->info();
+  info->channels = i.channels;
+  info->size_groups = i.size_groups;
+  info->visibilities = i.visibilities;
+  info->pixels = i.pixels;
+  info->tasks = i.tasks;
+  info->device_bytes = i.device_bytes;
+  return PURIFY_GB300_OK;
 }
 
 }  // extern "C"

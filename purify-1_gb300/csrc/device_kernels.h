@@ -31,7 +31,15 @@ struct ApplyArgs {
   int Nu = 0, Nv = 0;
   int64_t slot_stride = 0;          // complex elements per tilebuf slot
   int win_bytes = 0;  // set by the launchers: shared bytes before the batch headers
+  // Grouped launch over several operators: a device array of per-operator
+  // ApplyArgs (indexed by Task::channel) and the first task of each operator
+  // in the grouped task list (its tilebuf holds windows from that index on).
+  const void *group = nullptr;
+  const int32_t *group_task_base = nullptr;
 };
+
+// Blocks of the first stage of the deterministic norm reductions.
+constexpr int kNormBlocks = 512;
 
 struct LaunchShape {
   int threads = 128;  // 32 x warps per CTA
@@ -54,6 +62,19 @@ cudaError_t launch_grid(const ApplyArgs<real> &a, const PolyTable<real> &poly, i
                         int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
                         cudaStream_t s);
 
+// Grouped forms: `a.tasks` lists the tasks of several operators (Task::channel
+// names the operator), `a.group` points at a device array of their ApplyArgs
+// and `a.group_task_base` at the first grouped task of each; win_rows /
+// win_cols are the largest over the group.
+template <typename real>
+cudaError_t launch_degrid_group(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
+                                int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
+                                cudaStream_t s);
+template <typename real>
+cudaError_t launch_grid_group(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
+                              int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
+                              cudaStream_t s);
+
 // G^H, second half: sums the task windows that cover each grid cell, in a
 // fixed order, into the grid.
 struct FoldArgs {
@@ -67,6 +88,46 @@ struct FoldArgs {
 };
 template <typename real>
 cudaError_t launch_fold(const FoldArgs &f, cudaStream_t s);
+
+// Per-operator arguments of the grouped element-wise kernels (batch of
+// channels, one CTA row per channel).
+template <typename real>
+struct ChannelIO {
+  const void *x_in = nullptr;   // image in (forward)
+  void *x_out = nullptr;        // image out (adjoint)
+  const real *su = nullptr, *sv = nullptr;
+  void *pad = nullptr;          // zero-padded grid (forward FFT input)
+  void *work = nullptr;         // FFT output / adjoint grid
+  const void *vis_in = nullptr; // caller-ordered visibilities in (adjoint)
+  void *vis_out = nullptr;      // caller-ordered visibilities out (forward)
+  void *slots = nullptr;        // slot-ordered buffer
+  const int32_t *slot_user = nullptr, *user_slot = nullptr;
+  int Nx = 0, Ny = 0, Nu = 0, Nv = 0, x0 = 0, y0 = 0;
+  int64_t M = 0, S = 0;
+};
+
+template <typename real>
+cudaError_t launch_pad_group(const ChannelIO<real> *chans, int nch, int64_t max_pixels,
+                             cudaStream_t s);
+template <typename real>
+cudaError_t launch_crop_group(const ChannelIO<real> *chans, int nch, int64_t max_pixels,
+                              cudaStream_t s);
+template <typename real>
+cudaError_t launch_compact_group(const ChannelIO<real> *chans, int nch, int64_t max_vis,
+                                 cudaStream_t s);
+template <typename real>
+cudaError_t launch_expand_group(const ChannelIO<real> *chans, int nch, int64_t max_slots,
+                                cudaStream_t s);
+// Per-channel deterministic FP64 sum of |x_out|^2 into out[c] (partial holds
+// nch * kNormBlocks doubles), and x_out <- x_out * inv[c].
+template <typename real>
+cudaError_t launch_sq_norm_group(const ChannelIO<real> *chans, int nch, double *partial,
+                                 double *out, cudaStream_t s);
+template <typename real>
+cudaError_t launch_scale_group(const ChannelIO<real> *chans, int nch, int64_t max_pixels,
+                               const double *inv, cudaStream_t s);
+template <typename real>
+cudaError_t launch_fold_group(const FoldArgs *folds, int nch, int max_tiles, cudaStream_t s);
 
 // Z S: scaled gridding correction and zero padding.  su[i] sv[j] x[j Nx + i]
 // lands at grid[(y0 + j) Nu + x0 + i]; other grid cells are left untouched.
@@ -95,7 +156,6 @@ cudaError_t launch_to_c128(const void *src, void *dst, int64_t n, cudaStream_t s
 
 // Deterministic FP64 sum of |x|^2 over n complex values into *out (device).
 // `partial` must hold kNormBlocks doubles.
-constexpr int kNormBlocks = 512;
 template <typename real>
 cudaError_t launch_sq_norm(const void *x, int64_t n, double *partial, double *out,
                            cudaStream_t s);

@@ -57,7 +57,7 @@ struct Task {
   int32_t P, Q, H, W;
   int32_t batch_begin, batch_end;  // [begin, end) in units of 32-item batches
   int32_t tile;                    // tile id (tile_row * ntu + tile_col)
-  int32_t pad_;
+  int32_t channel;                 // operator of a grouped (multi-channel) launch, else 0
 };
 
 // Work item encoding: .x = first visibility (plan order), .y = lp | lq << 8 |

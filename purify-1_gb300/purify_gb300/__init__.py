@@ -68,6 +68,22 @@ class Info(ctypes.Structure):
     ]
 
 
+class Channel(ctypes.Structure):
+    _fields_ = [("u", ctypes.c_void_p), ("v", ctypes.c_void_p), ("weights", ctypes.c_void_p),
+                ("M", ctypes.c_int64), ("imsizey", ctypes.c_uint32), ("imsizex", ctypes.c_uint32)]
+
+
+class BatchTuning(ctypes.Structure):
+    _fields_ = [("tile", ctypes.c_int32), ("max_per_item", ctypes.c_int32),
+                ("degrid_threads", ctypes.c_int32), ("grid_threads", ctypes.c_int32)]
+
+
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("channels", ctypes.c_int32), ("size_groups", ctypes.c_int32),
+                ("visibilities", ctypes.c_int64), ("pixels", ctypes.c_int64),
+                ("tasks", ctypes.c_int64), ("device_bytes", ctypes.c_int64)]
+
+
 # Every symbol include/purify_gb300.h declares (checked by the CPU tests).
 EXPORTS = [
     "purify_gb300_default_args", "purify_gb300_operator_create", "purify_gb300_operator_destroy",
@@ -80,6 +96,10 @@ EXPORTS = [
     "purify_gb300_correction", "purify_gb300_stage_timing", "purify_gb300_stage_times",
     "purify_gb300_operator_create_tuned", "purify_gb300_grid_no_alloc",
     "purify_gb300_grid_no_alloc_bytes", "purify_gb300_wrow_taps",
+    "purify_gb300_batch_create", "purify_gb300_batch_destroy", "purify_gb300_batch_get_tuning",
+    "purify_gb300_batch_bind", "purify_gb300_batch_apply", "purify_gb300_batch_power_method",
+    "purify_gb300_batch_set_norms", "purify_gb300_batch_get_norms", "purify_gb300_batch_info_get",
+    "purify_gb300_batch_time",
 ]
 STAGES = ["pad", "fft_forward", "degrid", "grid", "fold", "fft_inverse", "crop", "compact",
           "expand"]
@@ -136,6 +156,19 @@ def load(path=None):
                                          ctypes.c_double, ctypes.c_double, vp]
     L.purify_gb300_stage_timing.argtypes = [vp, ctypes.c_int]
     L.purify_gb300_stage_times.argtypes = [vp, vp, vp]
+    L.purify_gb300_batch_create.argtypes = [P(Channel), ctypes.c_int32, ctypes.c_double,
+                                            ctypes.c_int32, ctypes.c_uint32, ctypes.c_int32,
+                                            ctypes.c_int32, P(BatchTuning), P(vp)]
+    L.purify_gb300_batch_destroy.argtypes = [vp]
+    L.purify_gb300_batch_get_tuning.argtypes = [vp, P(BatchTuning)]
+    L.purify_gb300_batch_bind.argtypes = [vp, vp, vp, vp, vp]
+    L.purify_gb300_batch_apply.argtypes = [vp, ctypes.c_int32, vp]
+    L.purify_gb300_batch_power_method.argtypes = [vp, ctypes.c_uint32, ctypes.c_double, vp]
+    L.purify_gb300_batch_set_norms.argtypes = [vp, vp]
+    L.purify_gb300_batch_get_norms.argtypes = [vp, vp]
+    L.purify_gb300_batch_info_get.argtypes = [vp, P(BatchInfo)]
+    L.purify_gb300_batch_time.argtypes = [vp, ctypes.c_int32, ctypes.c_uint32,
+                                          P(ctypes.c_double)]
     _lib = L
     return L
 
@@ -420,3 +453,137 @@ def init_degrid_operator_2d(u, v, w, weights, imsizey, imsizex, oversample_ratio
     return MeasurementOperator(u, v, w, weights, imsizey, imsizex, oversample_ratio, power_iters,
                                power_tol, kernel, Ju, Jv, w_term, Jw, cellx, celly, precision,
                                device)
+
+
+class Batch:
+    """Many channels (each its own coverage and image size; one kernel, J and
+    oversampling) applied together: grouped launches recorded once into a
+    CUDA graph and replayed.  The reference applies such a set operator by
+    operator (init_combine_operators, cpp/purify/operators.h:513-527).
+
+    ``channels`` is a list of dicts with keys u, v (grid pixels), imsizey,
+    imsizex and optionally weights.  ``tuning`` None runs the autotuner; a dict
+    with tile / max_per_item / degrid_threads / grid_threads fixes it."""
+
+    def __init__(self, channels, oversample_ratio=2.0, kernel="kb", J=4, precision="fp32",
+                 device=0, tuning=None):
+        L = load()
+        n = len(channels)
+        arr = (Channel * max(n, 1))()
+        self._keep = []
+        self.M, self.imsizes = [], []
+        for k, ch in enumerate(channels):
+            u = np.ascontiguousarray(ch["u"], dtype=np.float64).ravel()
+            v = np.ascontiguousarray(ch["v"], dtype=np.float64).ravel()
+            if u.size != v.size:
+                raise PurifyError(1, "channel %d: u and v differ in length" % k)
+            wt = ch.get("weights")
+            wt = None if wt is None else np.ascontiguousarray(wt, dtype=np.complex128).ravel()
+            self._keep += [u, v, wt]
+            arr[k] = Channel(_np_ptr(u), _np_ptr(v), _np_ptr(wt), u.size, int(ch["imsizey"]),
+                             int(ch["imsizex"]))
+            self.M.append(int(u.size))
+            self.imsizes.append((int(ch["imsizey"]), int(ch["imsizex"])))
+        h = ctypes.c_void_p()
+        t = None
+        if tuning:
+            t = BatchTuning(int(tuning.get("tile", 0)), int(tuning.get("max_per_item", 0)),
+                            int(tuning.get("degrid_threads", 0)),
+                            int(tuning.get("grid_threads", 0)))
+        _check(L.purify_gb300_batch_create(arr, n, float(oversample_ratio),
+                                           KERNELS[kernel] if isinstance(kernel, str) else int(kernel),
+                                           int(J), PRECISIONS[precision], int(device),
+                                           ctypes.byref(t) if t is not None else None,
+                                           ctypes.byref(h)))
+        self._keep = None
+        self._h = h
+        self.nch = n
+        self.precision = precision
+        self.device = int(device)
+        self._bound = None
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            load().purify_gb300_batch_destroy(h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def complex_dtype(self):
+        import torch
+        return torch.complex64 if self.precision == "fp32" else torch.complex128
+
+    @property
+    def tuning(self):
+        t = BatchTuning()
+        _check(load().purify_gb300_batch_get_tuning(self._h, ctypes.byref(t)))
+        return {"tile": t.tile, "max_per_item": t.max_per_item,
+                "degrid_threads": t.degrid_threads, "grid_threads": t.grid_threads}
+
+    def info(self):
+        i = BatchInfo()
+        _check(load().purify_gb300_batch_info_get(self._h, ctypes.byref(i)))
+        return {f: getattr(i, f) for f, _ in BatchInfo._fields_}
+
+    def _stream(self, stream):
+        import torch
+        if stream is None:
+            stream = torch.cuda.current_stream(self.device)
+        return ctypes.c_void_p(stream.cuda_stream)
+
+    def _ptrs(self, tensors, sizes, what):
+        if tensors is None:
+            return None
+        if len(tensors) != self.nch:
+            raise PurifyError(1, "%s: expected %d tensors" % (what, self.nch))
+        out = (ctypes.c_void_p * self.nch)()
+        for k, (t, n) in enumerate(zip(tensors, sizes)):
+            if (not t.is_cuda or t.dtype != self.complex_dtype or not t.is_contiguous()
+                    or t.numel() != n):
+                raise PurifyError(1, "%s[%d]: expected a contiguous CUDA %s tensor of %d values"
+                                  % (what, k, self.complex_dtype, n))
+            out[k] = t.data_ptr()
+        return out
+
+    def bind(self, x_in=None, vis=None, x_out=None, stream=None):
+        """Binds per-channel device tensors (lists of nch tensors)."""
+        npix = [a * b for a, b in self.imsizes]
+        xi = self._ptrs(x_in, npix, "x_in")
+        vi = self._ptrs(vis, self.M, "vis")
+        xo = self._ptrs(x_out, npix, "x_out")
+        _check(load().purify_gb300_batch_bind(self._h, xi, vi, xo, self._stream(stream)))
+        self._bound = (x_in, vis, x_out)  # keep the tensors alive while bound
+
+    def apply(self, directions=3, stream=None):
+        """1: vis = Phi x_in; 2: x_out = Phi^H vis; 3: both in turn."""
+        _check(load().purify_gb300_batch_apply(self._h, int(directions), self._stream(stream)))
+
+    def time(self, what=3, reps=10):
+        """Average device ms of one replay (1, 2, 3 as apply; 8 / 16 the
+        grouped degrid / grid launch alone) on the batch's own buffers."""
+        ms = ctypes.c_double()
+        _check(load().purify_gb300_batch_time(self._h, int(what), int(reps), ctypes.byref(ms)))
+        return ms.value
+
+    def power_method(self, iters=100, tol=1e-4):
+        n = np.zeros(self.nch)
+        _check(load().purify_gb300_batch_power_method(self._h, int(iters), float(tol), _np_ptr(n)))
+        return n
+
+    def set_norms(self, norms):
+        n = np.ascontiguousarray(norms, dtype=np.float64)
+        if n.size != self.nch:
+            raise PurifyError(1, "expected %d norms" % self.nch)
+        _check(load().purify_gb300_batch_set_norms(self._h, _np_ptr(n)))
+
+    @property
+    def norms(self):
+        n = np.zeros(self.nch)
+        _check(load().purify_gb300_batch_get_norms(self._h, _np_ptr(n)))
+        return n

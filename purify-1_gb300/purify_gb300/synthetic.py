@@ -101,3 +101,18 @@ def config_wproj(M=20_000_000, imsize=2048, cell=1.0, seed=0):
     return dict(u=u, v=v, w=w, jw_rows=wproj_supports(w, w_max), imsizey=imsize, imsizex=imsize,
                 cellx=cell, celly=cell, kernel="kb", Ju=4, Jv=4, w_max=w_max,
                 x=sky_image(imsize, imsize, seed=seed))
+
+
+def config_batch(nch=64, seed=0, m_lo=1e4, m_hi=2e6, sizes=(256, 512, 1024)):
+    """nch frequency channels: image size drawn from `sizes`, visibility count
+    log-uniform in [m_lo, m_hi], coverage 70% Gaussian core with sigma =
+    0.15 N (1 + 0.01 k) (channel frequency) + 30% uniform, KB J=4."""
+    rng = np.random.default_rng(seed)
+    sz = rng.choice(np.asarray(sizes), nch)
+    Ms = np.exp(rng.uniform(np.log(m_lo), np.log(m_hi), nch)).astype(np.int64)
+    chans = []
+    for k in range(nch):
+        n = int(sz[k])
+        u, v = mixed_uv(int(Ms[k]), 2 * n, 2 * n, 0.7, 0.15 * (1 + 0.01 * k), seed=seed + 1000 + k)
+        chans.append(dict(u=u, v=v, imsizey=n, imsizex=n, x=sky_image(n, n, seed=seed + k)))
+    return chans
