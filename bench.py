@@ -40,9 +40,15 @@ def parse():
     p.add_argument("--steps", type=int, default=50)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    p.add_argument("--workload", choices=["imaging", "wproj", "batch"], default="imaging",
+    p.add_argument("--workload", choices=["imaging", "wproj", "batch", "serve"],
+                   default="imaging",
                    help="imaging: the 1024^2 / 1e7 headline; wproj: 2048^2 / 2e7 w-projection; "
-                        "batch: 64 channels in one graph-replayed grouped step")
+                        "batch: 64 channels in one graph-replayed grouped step; serve: Poisson "
+                        "request stream on 16 resident coverages")
+    p.add_argument("--rate", type=float, default=100.0, help="serve: requests per second")
+    p.add_argument("--requests", type=int, default=400, help="serve: timed requests")
+    p.add_argument("--slots", type=int, default=8, help="serve: requests in flight at most")
+    p.add_argument("--budget-gb", type=float, default=24.0, help="serve: HBM budget of requests")
     p.add_argument("--channels", type=int, default=64, help="channels of the batch workload")
     p.add_argument("--M", type=int, default=0, help="visibilities (0: the workload's own)")
     p.add_argument("--imsize", type=int, default=1024)
@@ -532,8 +538,9 @@ def run_wproj(args):
     print(json.dumps(out), flush=True)
 
 
-BATCH_WORKLOAD = ("64 channels, image %s^2 drawn per channel, M log-uniform in [1e4, 2e6], "
-                  "70% Gaussian core sigma = 0.15 N (1 + 0.01 k) + 30% uniform, KB J=4, FP32")
+BATCH_WORKLOAD = ("64 channels, image {256,512,1024}^2 drawn per channel, M log-uniform in "
+                  "[1e4, 2e6], 70% Gaussian core sigma = 0.15 N (1 + 0.01 k) + 30% uniform, "
+                  "KB J=4, FP32")
 
 
 def run_batch(args):
@@ -600,7 +607,7 @@ def run_batch(args):
         "value": Mtot / (ms * 1e-3) / 1e6, "unit": "Mvis/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic: seeded (PCG64)",
-        "config": {"workload": BATCH_WORKLOAD % "{256,512,1024}", "channels": len(chans),
+        "config": {"workload": BATCH_WORKLOAD, "channels": len(chans),
                    "visibilities": Mtot, "pixels": int(sum(npix)),
                    "sizes": {str(n): int(sum(1 for c in chans if c["imsizex"] == n))
                              for n in (256, 512, 1024)},
@@ -740,9 +747,119 @@ def run_batch(args):
     print(json.dumps(out), flush=True)
 
 
+SERVE_WORKLOAD = ("Poisson request stream: 70% forward+adjoint, 25% adjoint-only, 5% norm "
+                  "(50 power-method rounds); 16 resident coverages, image {256,512,1024}^2, "
+                  "M log-uniform in [1e4, 5e6], 70% Gaussian core + 30% uniform, KB J=4")
+
+
+def serve_stream(pgb, covs, precision, args, t_arr, kinds, cov_idx, xs, vs):
+    """Runs the request stream on a fresh server; returns per-request results,
+    the server statistics and the wall time of the timed part."""
+    srv = pgb.Server(device=0, slots=args.slots, hbm_budget=int(args.budget_gb * (1 << 30)))
+    t0 = time.perf_counter()
+    ids = [srv.add_coverage(c["u"], c["v"], None, None, c["imsizey"], c["imsizex"],
+                            power_iters=10, precision=precision) for c in covs]
+    t_setup = time.perf_counter() - t0
+    # warm-up: one request of each kind on every coverage
+    for k in ids:
+        for kind in ("forward_adjoint", "adjoint"):
+            srv.wait(srv.submit(k, kind, xs[k], vs[k]))
+    srv.wait(srv.submit(ids[0], "norm", iters=5))
+    base = srv.stats()
+    tickets = [None] * len(t_arr)
+
+    def producer():
+        start = time.perf_counter()
+        for r in range(len(t_arr)):
+            delay = start + t_arr[r] - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            c = int(cov_idx[r])
+            tickets[r] = srv.submit(ids[c], str(kinds[r]), xs[c], vs[c], iters=50, tol=0.0)
+    w0 = time.perf_counter()
+    th = threading.Thread(target=producer)
+    th.start()
+    results = []
+    for r in range(len(t_arr)):
+        while tickets[r] is None:
+            time.sleep(0.0002)
+        res = srv.wait(tickets[r])
+        if r >= 48:  # outputs of the first requests are kept for the FP32/FP64 comparison
+            res.pop("vis", None)
+            res.pop("x", None)
+        results.append(res)
+    th.join()
+    wall = time.perf_counter() - w0
+    st = srv.stats()
+    srv.close()
+    return results, st, base, wall, t_setup
+
+
+def run_serve(args):
+    """Request serving: a Poisson stream of forward+adjoint, adjoint-only and
+    norm requests on 16 resident coverages; latency from submit to the end of
+    the request's device work."""
+    import purify_gb300 as pgb
+    from purify_gb300 import synthetic
+    pgb.build()
+    covs = synthetic.config_serve_pool(16, seed=0)
+    t_arr, kinds, cov_idx = synthetic.request_stream(args.requests, args.rate, len(covs), seed=1)
+    xs = [synthetic.sky_image(c["imsizey"], c["imsizex"], seed=k) for k, c in enumerate(covs)]
+    vs = [synthetic.random_vis(c["u"].size, seed=100 + k) for k, c in enumerate(covs)]
+    out = None
+    per_prec = {}
+    for prec in (["fp32"] if args.no_fp64 else ["fp32", "fp64"]):
+        res, st, base, wall, t_setup = serve_stream(pgb, covs, prec, args, t_arr, kinds, cov_idx,
+                                                    xs, vs)
+        lat = np.array([r["latency_ms"] for r in res])
+        ok = sum(1 for r in res if r["status"] == 0)
+        passes = st["visibility_passes"] - base["visibility_passes"]
+        by_kind = {}
+        for kind in ("forward_adjoint", "adjoint", "norm"):
+            sel = [r["latency_ms"] for r, k in zip(res, kinds) if str(k) == kind]
+            if sel:
+                by_kind[kind] = {"n": len(sel), "p50": float(np.percentile(sel, 50)),
+                                 "p99": float(np.percentile(sel, 99))}
+        per_prec[prec] = {
+            "value": passes / 2 / wall / 1e6, "requests_ok": ok, "wall_s": wall,
+            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                           "mean": float(lat.mean()), "by_kind": by_kind},
+            "queue_ms_p99": float(np.percentile([r["queue_ms"] for r in res], 99)),
+            "inflight_peak": st["inflight_peak"], "bytes_peak": st["bytes_peak"],
+            "setup_s": t_setup}
+        per_prec[prec]["_res"] = res
+    f32 = per_prec["fp32"]
+    out = {
+        "metric": "served degrid+grid Mvis/s and p50/p99 request latency (Poisson stream), FP32",
+        "value": f32["value"], "unit": "Mvis/s", "n_gpus": 1, "steps": args.requests,
+        "warmup": 33, "ms_per_step": f32["wall_s"] * 1e3 / args.requests,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded (PCG64)",
+        "config": {"workload": SERVE_WORKLOAD, "rate_per_s": args.rate, "requests": args.requests,
+                   "slots": args.slots, "hbm_budget_gb": args.budget_gb,
+                   "latency": "submit to end of the request's device work (D2H included)"},
+        "latency_ms": f32["latency_ms"], "serving": {k: {kk: vv for kk, vv in v.items()
+                                                          if kk != "_res"}
+                                                      for k, v in per_prec.items()},
+        "gpu_launches": None,
+    }
+    if "fp64" in per_prec:
+        r32, r64 = per_prec["fp32"]["_res"], per_prec["fp64"]["_res"]
+        ef = [rel_l2(a["vis"], b["vis"]) for a, b in zip(r32, r64) if "vis" in a]
+        ea = [rel_l2(a["x"], b["x"]) for a, b in zip(r32, r64) if "x" in a]
+        en = [abs(a["norm"] - b["norm"]) / b["norm"] for a, b in zip(r32, r64)
+              if a["norm"] and b["norm"]]
+        out["rel_l2_fp32_vs_fp64_max_request"] = {"forward": max(ef) if ef else None,
+                                                 "adjoint": max(ea) if ea else None,
+                                                 "norm_rel": max(en) if en else None}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
-    if args.workload == "batch" and args.impl == "gb300":
+    if args.workload == "serve" and args.impl == "gb300":
+        run_serve(args)
+    elif args.workload == "batch" and args.impl == "gb300":
         run_batch(args)
     elif args.workload == "wproj" and args.impl == "gb300":
         run_wproj(args)

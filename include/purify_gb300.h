@@ -309,6 +309,69 @@ int purify_gb300_batch_info_get(const purify_gb300_batch *b, purify_gb300_batch_
  * reference; used by the autotuner and the benchmark. */
 int purify_gb300_batch_time(purify_gb300_batch *b, int32_t what, uint32_t reps, double *ms);
 
+/* ---- Request server ------------------------------------------------------
+ * Forward, adjoint and operator-norm requests on coverages kept resident on
+ * the device, admitted by an HBM budget and run concurrently: each admitted
+ * request gets its own workspace (grids, task windows, I/O vectors) from a
+ * stream-ordered memory pool and one of `slots` CUDA streams, so requests
+ * that arrive while others run are admitted as streams and memory free up
+ * and their kernels overlap on the GPU.  A request shares no scratch with
+ * another, so its result is the same alone and in a mix.  No counterpart in
+ * the reference (its operators are applied by one solver at a time). */
+typedef struct purify_gb300_server purify_gb300_server;
+typedef struct {
+  int32_t device;
+  int32_t slots;             /* requests in flight at most (1..64) */
+  int64_t hbm_budget_bytes;  /* device bytes of the requests in flight */
+} purify_gb300_server_config;
+int purify_gb300_server_create(const purify_gb300_server_config *cfg, purify_gb300_server **out);
+/* Destroys after the requests already submitted have run. */
+int purify_gb300_server_destroy(purify_gb300_server *s);
+/* Builds a resident coverage from operator arguments (power_iters > 0 sets
+ * its norm) and returns its id. */
+int purify_gb300_server_add_coverage(purify_gb300_server *s, const purify_gb300_create_args *args,
+                                     int32_t *coverage);
+#define PURIFY_GB300_REQ_FORWARD 1         /* vis_out = Phi x_in */
+#define PURIFY_GB300_REQ_ADJOINT 2         /* x_out = Phi^H vis_in (dirty image) */
+#define PURIFY_GB300_REQ_FORWARD_ADJOINT 3 /* vis_out = Phi x_in, x_out = Phi^H vis_out */
+#define PURIFY_GB300_REQ_NORM 4            /* ||Phi'|| by iters power-method rounds */
+/* Host vectors are complex<double>; inputs are copied at submit, outputs
+ * written by purify_gb300_server_wait. */
+typedef struct {
+  int32_t coverage;
+  int32_t kind;
+  const double *x_in;
+  const double *vis_in;
+  double *vis_out;
+  double *x_out;
+  uint32_t iters; /* norm requests */
+  double tol;     /* norm requests: the power method's stopping rule */
+} purify_gb300_request;
+int purify_gb300_server_submit(purify_gb300_server *s, const purify_gb300_request *rq,
+                               int64_t *ticket);
+typedef struct {
+  int32_t status;      /* of the request: OK, REJECTED (never fits the budget), ... */
+  int32_t iterations;  /* norm requests: rounds until the stopping rule held */
+  double norm;
+  double queue_ms, run_ms, latency_ms; /* submit->admit, admit->done, submit->done */
+  int64_t device_bytes;
+} purify_gb300_result;
+/* Waits up to timeout_s seconds (< 0: no limit); returns
+ * PURIFY_GB300_TIMEOUT if the request is still running, else copies its
+ * outputs, fills *out and forgets the ticket. */
+int purify_gb300_server_wait(purify_gb300_server *s, int64_t ticket, double timeout_s,
+                             purify_gb300_result *out);
+/* Device bytes a request would hold while in flight. */
+int purify_gb300_server_request_bytes(const purify_gb300_server *s, const purify_gb300_request *rq,
+                                      int64_t *bytes);
+typedef struct {
+  int64_t submitted, completed, rejected, failed;
+  int64_t inflight_peak, bytes_peak, bytes_budget;
+  double latency_p50_ms, latency_p99_ms, latency_mean_ms; /* completed requests */
+  double visibility_passes; /* sum of M x (G and G^H passes) of completed requests */
+} purify_gb300_server_stats;
+int purify_gb300_server_get_stats(const purify_gb300_server *s, purify_gb300_server_stats *out);
+
 /* Message of the last failing call on this thread ("" when none). */
 const char *purify_gb300_last_error(void);
 /* Library version string. */

@@ -13,6 +13,7 @@
 #include "gridding_kernels.h"
 #include "operator.h"
 #include "plan.h"
+#include "server.h"
 #include "wplan.h"
 
 struct purify_gb300_operator {
@@ -20,6 +21,9 @@ struct purify_gb300_operator {
 };
 struct purify_gb300_plan {
   pg::Plan plan;
+};
+struct purify_gb300_server {
+  std::unique_ptr<pg::Server> impl;
 };
 struct purify_gb300_batch {
   std::unique_ptr<pg::Batch> impl;
@@ -80,6 +84,45 @@ int purify_gb300_operator_create(const purify_gb300_create_args *a, purify_gb300
   return purify_gb300_operator_create_tuned(a, nullptr, out);
 }
 
+}  // extern "C"
+
+namespace {
+pg::OperatorConfig to_config(const purify_gb300_create_args *a, const purify_gb300_tuning *t) {
+  pg::OperatorConfig c;
+  c.u = a->u;
+  c.v = a->v;
+  c.w = a->w;
+  c.weights = a->weights;
+  c.M = a->M;
+  c.imsizey = int(a->imsizey);
+  c.imsizex = int(a->imsizex);
+  c.oversample_ratio = a->oversample_ratio;
+  c.power_iters = int(a->power_iters);
+  c.power_tol = a->power_tol;
+  c.kernel = a->kernel;
+  c.Ju = int(a->Ju);
+  c.Jv = int(a->Jv);
+  c.w_term = a->w_term != 0;
+  c.Jw = int(a->Jw);
+  c.jw_rows = a->jw_rows;
+  c.cellx = a->cellx;
+  c.celly = a->celly;
+  c.fp64 = a->precision == PURIFY_GB300_FP64;
+  c.device = a->device;
+  if (t) {
+    c.threads = t->threads;
+    c.max_per_item = t->max_per_item;
+    c.tile = t->tile;
+    c.fused_permute = t->fused_permute;
+  }
+  if (a->precision != PURIFY_GB300_FP32 && a->precision != PURIFY_GB300_FP64)
+    throw pg::Error(pg::kInvalidArgument, "unknown precision");
+  return c;
+}
+}  // namespace
+
+extern "C" {
+
 int purify_gb300_operator_create_tuned(const purify_gb300_create_args *a,
                                        const purify_gb300_tuning *t,
                                        purify_gb300_operator **out) {
@@ -87,35 +130,7 @@ int purify_gb300_operator_create_tuned(const purify_gb300_create_args *a,
   if (!out) return null_arg("out");
   *out = nullptr;
   return guard([&] {
-    pg::OperatorConfig c;
-    c.u = a->u;
-    c.v = a->v;
-    c.w = a->w;
-    c.weights = a->weights;
-    c.M = a->M;
-    c.imsizey = int(a->imsizey);
-    c.imsizex = int(a->imsizex);
-    c.oversample_ratio = a->oversample_ratio;
-    c.power_iters = int(a->power_iters);
-    c.power_tol = a->power_tol;
-    c.kernel = a->kernel;
-    c.Ju = int(a->Ju);
-    c.Jv = int(a->Jv);
-    c.w_term = a->w_term != 0;
-    c.Jw = int(a->Jw);
-    c.jw_rows = a->jw_rows;
-    c.cellx = a->cellx;
-    c.celly = a->celly;
-    c.fp64 = a->precision == PURIFY_GB300_FP64;
-    c.device = a->device;
-    if (t) {
-      c.threads = t->threads;
-      c.max_per_item = t->max_per_item;
-      c.tile = t->tile;
-      c.fused_permute = t->fused_permute;
-    }
-    if (a->precision != PURIFY_GB300_FP32 && a->precision != PURIFY_GB300_FP64)
-      throw pg::Error(pg::kInvalidArgument, "unknown precision");
+    const pg::OperatorConfig c = to_config(a, t);
     auto *h = new purify_gb300_operator();
     try {
       h->impl = pg::Operator::create(c);
@@ -536,6 +551,104 @@ int purify_gb300_batch_info_get(const purify_gb300_batch *b, purify_gb300_batch_
   info->pixels = i.pixels;
   info->tasks = i.tasks;
   info->device_bytes = i.device_bytes;
+  return PURIFY_GB300_OK;
+}
+
+int purify_gb300_server_create(const purify_gb300_server_config *cfg, purify_gb300_server **out) {
+  if (!cfg) return null_arg("config");
+  if (!out) return null_arg("out");
+  *out = nullptr;
+  return guard([&] {
+    pg::ServerConfig c;
+    c.device = cfg->device;
+    c.slots = cfg->slots;
+    c.hbm_budget = cfg->hbm_budget_bytes;
+    std::unique_ptr<purify_gb300_server> h(new purify_gb300_server);
+    h->impl.reset(new pg::Server(c));
+    *out = h.release();
+  });
+}
+int purify_gb300_server_destroy(purify_gb300_server *s) {
+  return guard([&] { delete s; });
+}
+int purify_gb300_server_add_coverage(purify_gb300_server *s, const purify_gb300_create_args *a,
+                                     int32_t *coverage) {
+  if (!s) return null_arg("server");
+  if (!a) return null_arg("args");
+  if (!coverage) return null_arg("coverage");
+  return guard([&] { *coverage = s->impl->add_coverage(to_config(a, nullptr)); });
+}
+}  // extern "C"
+
+namespace {
+pg::Request to_request(const purify_gb300_request *rq) {
+  pg::Request r;
+  r.coverage = rq->coverage;
+  r.kind = rq->kind;
+  r.x_in = rq->x_in;
+  r.vis_in = rq->vis_in;
+  r.vis_out = rq->vis_out;
+  r.x_out = rq->x_out;
+  r.iters = int(rq->iters);
+  r.tol = rq->tol;
+  return r;
+}
+}  // namespace
+
+extern "C" {
+int purify_gb300_server_submit(purify_gb300_server *s, const purify_gb300_request *rq,
+                               int64_t *ticket) {
+  if (!s) return null_arg("server");
+  if (!rq) return null_arg("request");
+  if (!ticket) return null_arg("ticket");
+  return guard([&] { *ticket = s->impl->submit(to_request(rq)); });
+}
+int purify_gb300_server_wait(purify_gb300_server *s, int64_t ticket, double timeout_s,
+                             purify_gb300_result *out) {
+  if (!s) return null_arg("server");
+  int rc = PURIFY_GB300_OK;
+  const int g = guard([&] {
+    pg::RequestResult r;
+    if (!s->impl->wait(ticket, timeout_s, &r)) {
+      rc = PURIFY_GB300_TIMEOUT;
+      return;
+    }
+    if (out) {
+      out->status = r.status;
+      out->iterations = r.iterations;
+      out->norm = r.norm;
+      out->queue_ms = r.queue_ms;
+      out->run_ms = r.run_ms;
+      out->latency_ms = r.latency_ms;
+      out->device_bytes = r.device_bytes;
+    }
+  });
+  if (g != PURIFY_GB300_OK) return g;
+  if (rc == PURIFY_GB300_TIMEOUT) g_last_error = "request still running";
+  return rc;
+}
+int purify_gb300_server_request_bytes(const purify_gb300_server *s, const purify_gb300_request *rq,
+                                      int64_t *bytes) {
+  if (!s) return null_arg("server");
+  if (!rq) return null_arg("request");
+  if (!bytes) return null_arg("bytes");
+  return guard([&] { *bytes = s->impl->request_bytes(to_request(rq)); });
+}
+int purify_gb300_server_get_stats(const purify_gb300_server *s, purify_gb300_server_stats *out) {
+  if (!s) return null_arg("server");
+  if (!out) return null_arg("stats");
+  const pg::ServerStats t = s->impl->stats();
+  out->submitted = t.submitted;
+  out->completed = t.completed;
+  out->rejected = t.rejected;
+  out->failed = t.failed;
+  out->inflight_peak = t.inflight_peak;
+  out->bytes_peak = t.bytes_peak;
+  out->bytes_budget = t.bytes_budget;
+  out->latency_p50_ms = t.latency_p50_ms;
+  out->latency_p99_ms = t.latency_p99_ms;
+  out->latency_mean_ms = t.latency_mean_ms;
+  out->visibility_passes = t.visibility_passes;
   return PURIFY_GB300_OK;
 }
 

@@ -141,6 +141,20 @@ __global__ void fill_kernel(cplx<real> *x, int64_t n, real value) {
     x[k] = cplx<real>{value, real(0)};
 }
 
+// x <- x * real(1 / sqrt(*sq)) (0 when *sq is not positive).
+template <typename real>
+__global__ void scale_rsqrt_kernel(cplx<real> *x, int64_t n, const double *__restrict__ sq) {
+  const double v = sqrt(*sq);
+  const real s = v > 0 ? real(1.0 / v) : real(0);
+  for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n;
+       k += int64_t(gridDim.x) * blockDim.x) {
+    cplx<real> w = x[k];
+    w.x *= s;
+    w.y *= s;
+    x[k] = w;
+  }
+}
+
 int stream_blocks(int64_t n, int threads) {
   const int64_t b = (n + threads - 1) / threads;
   return int(b < 1 ? 1 : (b > 152 * 32 ? 152 * 32 : b));
@@ -251,6 +265,13 @@ cudaError_t launch_scale(void *x, int64_t n, double scale, cudaStream_t s) {
   return cudaGetLastError();
 }
 template <typename real>
+cudaError_t launch_scale_rsqrt(void *x, int64_t n, const double *sq, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  scale_rsqrt_kernel<real><<<stream_blocks(n, 256), 256, 0, s>>>(static_cast<cplx<real> *>(x), n,
+                                                                 sq);
+  return cudaGetLastError();
+}
+template <typename real>
 cudaError_t launch_fill(void *x, int64_t n, double value, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   fill_kernel<real><<<stream_blocks(n, 256), 256, 0, s>>>(static_cast<cplx<real> *>(x), n,
@@ -277,7 +298,8 @@ cudaError_t launch_fill(void *x, int64_t n, double value, cudaStream_t s) {
   template cudaError_t launch_sq_norm<real>(const void *, int64_t, double *, double *,          \
                                             cudaStream_t);                                      \
   template cudaError_t launch_scale<real>(void *, int64_t, double, cudaStream_t);               \
-  template cudaError_t launch_fill<real>(void *, int64_t, double, cudaStream_t);
+  template cudaError_t launch_fill<real>(void *, int64_t, double, cudaStream_t);                 \
+  template cudaError_t launch_scale_rsqrt<real>(void *, int64_t, const double *, cudaStream_t);
 
 PG_INSTANTIATE(float)
 PG_INSTANTIATE(double)

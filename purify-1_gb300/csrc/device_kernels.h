@@ -162,6 +162,9 @@ cudaError_t launch_sq_norm(const void *x, int64_t n, double *partial, double *ou
 // x <- x * scale.
 template <typename real>
 cudaError_t launch_scale(void *x, int64_t n, double scale, cudaStream_t s);
+// x <- x * real(1 / sqrt(*sq)) with *sq on the device (0 when not positive).
+template <typename real>
+cudaError_t launch_scale_rsqrt(void *x, int64_t n, const double *sq, cudaStream_t s);
 // x <- value (complex, real part only).
 template <typename real>
 cudaError_t launch_fill(void *x, int64_t n, double value, cudaStream_t s);

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <complex>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <vector>
 
@@ -47,6 +48,10 @@ class OperatorT final : public Operator {
   OperatorInfo info() const override { return info_; }
   void set_stage_timing(bool on) override;
   void stage_times(double *total_ms, int64_t *launches) override;
+  WorkspaceSizes workspace_sizes() const override;
+  void forward_ws(const void *x, void *y, const Workspace &ws) override;
+  void adjoint_ws(const void *y, void *x, const Workspace &ws) override;
+  void power_ws(void *x, int iters, double *sq, double *partial, const Workspace &ws) override;
 
  private:
   enum Stage { kPad = 0, kFftF, kDegrid, kGrid, kFold, kFftI, kCrop, kCompact, kExpand };
@@ -115,6 +120,15 @@ class OperatorT final : public Operator {
       norm_partial_, norm_out_;
   DeviceBuffer x128_, y128_, xc_, yc_, pm_x_;
   bool staging_ = false, pm_ready_ = false;
+  // Scratch of the apply being enqueued: the operator's own (own_) or a
+  // caller's workspace (the *_ws entry points).
+  Workspace own_;
+  const Workspace *ws_ = &own_;
+  DeviceBuffer su_unit_d_;  // correction scaled for norm 1 (Phi')
+  const real *su_active() const {
+    return ws_->unit_norm ? su_unit_d_.as<real>() : su_d_.as<real>();
+  }
+  void with_workspace(const Workspace &ws, const std::function<void()> &f);
 };
 
 template <typename real>
@@ -192,6 +206,7 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
     tv_of_.upload(tv.of.data(), sizeof(int32_t) * tv.of.size(), stream_);
     su_d_.alloc(sizeof(real) * Nx_, &bytes);
     sv_d_.alloc(sizeof(real) * Ny_, &bytes);
+    su_unit_d_.alloc(sizeof(real) * Nx_, &bytes);
     const size_t gbytes = sizeof(C) * size_t(Nu_) * Nv_;
     pad_.alloc(gbytes, &bytes);
     cuda_check(cudaMemsetAsync(pad_.get(), 0, gbytes, stream_), "cudaMemset");
@@ -208,6 +223,20 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
   cufft_check(cufftSetStream(fft_, stream_), "cufftSetStream");
   size_t ws = 0;
   if (cufftGetSize(fft_, &ws) == CUFFT_SUCCESS) bytes += int64_t(ws);
+  own_.pad = pad_.get();
+  own_.work = work_.get();
+  own_.tilebuf = tilebuf_.get();
+  own_.slots = slots_.get();
+  own_.fft = fft_;
+  own_.stream = stream_;
+  {
+    // Phi' (norm 1) correction for power-method workspaces.
+    const double c = 1.0 / std::sqrt(double(Nu_) * double(Nv_));
+    std::vector<real> su1(Nx_);
+    for (int i = 0; i < Nx_; ++i) su1[i] = real(su_[i] * c);
+    su_unit_d_.upload(su1.data(), sizeof(real) * Nx_, stream_);
+    cuda_check(cudaStreamSynchronize(stream_), "correction upload");
+  }
 
   info_.M = M_;
   info_.imsizey = Ny_;
@@ -423,12 +452,12 @@ void OperatorT<real>::degrid_slots(const void *grid, void *caller_vis) {
     w.factor = wfactor_.as<int64_t>();
     w.factors = wfactors_.get();
     w.weight = weight_.get();
-    w.slot_out = slots_.get();
+    w.slot_out = ws_->slots;
     w.Nu = Nu_;
     w.Nv = Nv_;
     w.Smax = fold_J_;
     mark_begin(kDegrid);
-    cuda_check(launch_wdegrid<real>(w, ntasks_, win_rows_, win_cols_, shape_.threads, stream_),
+    cuda_check(launch_wdegrid<real>(w, ntasks_, win_rows_, win_cols_, shape_.threads, ws_->stream),
                "w degrid");
     mark_end(kDegrid);
     return;
@@ -440,20 +469,20 @@ void OperatorT<real>::degrid_slots(const void *grid, void *caller_vis) {
   a.lane_code = lane_code_.as<int32_t>();
   a.frac = frac_.get();
   a.weight = unit_weights_ ? nullptr : weight_.get();
-  a.slot_out = caller_vis ? caller_vis : slots_.get();
+  a.slot_out = caller_vis ? caller_vis : ws_->slots;
   a.slot_user = caller_vis ? slot_user_.as<int32_t>() : nullptr;
   a.Nu = Nu_;
   a.Nv = Nv_;
   mark_begin(kDegrid);
-  cuda_check(launch_degrid<real>(a, poly_, J_, ntasks_, win_rows_, win_cols_, shape_, stream_),
+  cuda_check(launch_degrid<real>(a, poly_, J_, ntasks_, win_rows_, win_cols_, shape_, ws_->stream),
              "degrid");
   mark_end(kDegrid);
 }
 
 template <typename real>
 void OperatorT<real>::grid_slots(void *grid, const void *caller_vis) {
-  grid_core(grid, caller_vis ? caller_vis : slots_.get(),
-            caller_vis ? slot_user_.as<int32_t>() : nullptr, tilebuf_.get());
+  grid_core(grid, caller_vis ? caller_vis : ws_->slots,
+            caller_vis ? slot_user_.as<int32_t>() : nullptr, ws_->tilebuf);
 }
 
 // G^H from visibilities in slot order (or caller order through slot_user)
@@ -475,7 +504,7 @@ void OperatorT<real>::grid_core(void *grid, const void *vis, const int32_t *slot
     w.Smax = fold_J_;
     w.slot_stride = slot_stride_;
     mark_begin(kGrid);
-    cuda_check(launch_wgrid<real>(w, ntasks_, win_rows_, win_cols_, shape_.threads, stream_),
+    cuda_check(launch_wgrid<real>(w, ntasks_, win_rows_, win_cols_, shape_.threads, ws_->stream),
                "w grid");
     mark_end(kGrid);
     fold_into(grid, windows);
@@ -494,7 +523,7 @@ void OperatorT<real>::grid_core(void *grid, const void *vis, const int32_t *slot
   a.Nv = Nv_;
   a.slot_stride = slot_stride_;
   mark_begin(kGrid);
-  cuda_check(launch_grid<real>(a, poly_, J_, ntasks_, win_rows_, win_cols_, shape_, stream_),
+  cuda_check(launch_grid<real>(a, poly_, J_, ntasks_, win_rows_, win_cols_, shape_, ws_->stream),
              "grid");
   mark_end(kGrid);
   fold_into(grid, windows);
@@ -518,7 +547,7 @@ void OperatorT<real>::fold_into(void *grid, const void *windows) {
   f.Nv = Nv_;
   f.grid = grid;
   mark_begin(kFold);
-  cuda_check(launch_fold<real>(f, stream_), "fold");
+  cuda_check(launch_fold<real>(f, ws_->stream), "fold");
   mark_end(kFold);
 }
 
@@ -530,7 +559,7 @@ void OperatorT<real>::degrid_on_stream(const void *grid, void *y) {
   }
   degrid_slots(grid);
   mark_begin(kCompact);
-  cuda_check(launch_compact<real>(slots_.get(), user_slot_.as<int32_t>(), y, M_, stream_),
+  cuda_check(launch_compact<real>(ws_->slots, user_slot_.as<int32_t>(), y, M_, ws_->stream),
              "compact");
   mark_end(kCompact);
 }
@@ -542,7 +571,7 @@ void OperatorT<real>::grid_on_stream(const void *y, void *grid) {
     return;
   }
   mark_begin(kExpand);
-  cuda_check(launch_expand<real>(y, slot_user_.as<int32_t>(), slots_.get(), S_, stream_),
+  cuda_check(launch_expand<real>(y, slot_user_.as<int32_t>(), ws_->slots, S_, ws_->stream),
              "expand");
   mark_end(kExpand);
   grid_slots(grid);
@@ -551,25 +580,25 @@ void OperatorT<real>::grid_on_stream(const void *y, void *grid) {
 template <typename real>
 void OperatorT<real>::forward_slots(const void *x, void *caller_vis) {
   mark_begin(kPad);
-  cuda_check(launch_pad<real>(x, su_d_.as<real>(), sv_d_.as<real>(), pad_.get(), Nx_, Ny_, Nu_,
-                              x0_, y0_, stream_),
+  cuda_check(launch_pad<real>(x, su_active(), sv_d_.as<real>(), ws_->pad, Nx_, Ny_, Nu_,
+                              x0_, y0_, ws_->stream),
              "pad");
   mark_end(kPad);
   mark_begin(kFftF);
-  cufft_check(Traits<real>::exec(fft_, pad_.get(), work_.get(), CUFFT_FORWARD), "cufftExec");
+  cufft_check(Traits<real>::exec(ws_->fft, ws_->pad, ws_->work, CUFFT_FORWARD), "cufftExec");
   mark_end(kFftF);
-  degrid_slots(work_.get(), caller_vis);
+  degrid_slots(ws_->work, caller_vis);
 }
 
 template <typename real>
 void OperatorT<real>::adjoint_slots(void *x, const void *caller_vis) {
-  grid_slots(work_.get(), caller_vis);
+  grid_slots(ws_->work, caller_vis);
   mark_begin(kFftI);
-  cufft_check(Traits<real>::exec(fft_, work_.get(), work_.get(), CUFFT_INVERSE), "cufftExec");
+  cufft_check(Traits<real>::exec(ws_->fft, ws_->work, ws_->work, CUFFT_INVERSE), "cufftExec");
   mark_end(kFftI);
   mark_begin(kCrop);
-  cuda_check(launch_crop<real>(work_.get(), su_d_.as<real>(), sv_d_.as<real>(), x, Nx_, Ny_, Nu_,
-                               x0_, y0_, stream_),
+  cuda_check(launch_crop<real>(ws_->work, su_active(), sv_d_.as<real>(), x, Nx_, Ny_, Nu_,
+                               x0_, y0_, ws_->stream),
              "crop");
   mark_end(kCrop);
 }
@@ -582,7 +611,7 @@ void OperatorT<real>::forward_on_stream(const void *x, void *y) {
   }
   forward_slots(x);
   mark_begin(kCompact);
-  cuda_check(launch_compact<real>(slots_.get(), user_slot_.as<int32_t>(), y, M_, stream_),
+  cuda_check(launch_compact<real>(ws_->slots, user_slot_.as<int32_t>(), y, M_, ws_->stream),
              "compact");
   mark_end(kCompact);
 }
@@ -594,10 +623,66 @@ void OperatorT<real>::adjoint_on_stream(const void *y, void *x) {
     return;
   }
   mark_begin(kExpand);
-  cuda_check(launch_expand<real>(y, slot_user_.as<int32_t>(), slots_.get(), S_, stream_),
+  cuda_check(launch_expand<real>(y, slot_user_.as<int32_t>(), ws_->slots, S_, ws_->stream),
              "expand");
   mark_end(kExpand);
   adjoint_slots(x);
+}
+
+template <typename real>
+WorkspaceSizes OperatorT<real>::workspace_sizes() const {
+  WorkspaceSizes w;
+  w.pad = int64_t(sizeof(C)) * Nu_ * Nv_;
+  w.work = w.pad;
+  w.tilebuf = int64_t(sizeof(C)) * slot_stride_ * std::max(ntasks_, 1);
+  w.slots = int64_t(sizeof(C)) * std::max<int64_t>(S_, 1);
+  return w;
+}
+
+// Enqueues f's launches on ws.stream with ws's scratch.  The coverage state
+// is only read, so applies on different workspaces may run concurrently.
+template <typename real>
+void OperatorT<real>::with_workspace(const Workspace &ws, const std::function<void()> &f) {
+  DeviceGuard guard(device_);
+  std::lock_guard<std::mutex> lock(mu_);
+  ws_ = &ws;
+  try {
+    f();
+  } catch (...) {
+    ws_ = &own_;
+    throw;
+  }
+  ws_ = &own_;
+}
+
+template <typename real>
+void OperatorT<real>::forward_ws(const void *x, void *y, const Workspace &ws) {
+  with_workspace(ws, [&] { forward_on_stream(x, y); });
+}
+template <typename real>
+void OperatorT<real>::adjoint_ws(const void *y, void *x, const Workspace &ws) {
+  with_workspace(ws, [&] { adjoint_on_stream(y, x); });
+}
+
+// The power iteration of power_method() with the normalisation done on the
+// device: after round i, sq[i] = ||x||^2 (FP64, same reduction) and x is
+// scaled by real(1 / sqrt(sq[i])), the host's arithmetic, so the estimates
+// sqrt(sq[i]) are those of power_method() bit for bit.  The stopping rule is
+// applied by the caller to the recorded estimates.
+template <typename real>
+void OperatorT<real>::power_ws(void *x, int iters, double *sq, double *partial,
+                               const Workspace &ws) {
+  Workspace w = ws;
+  w.unit_norm = true;
+  with_workspace(w, [&] {
+    cuda_check(launch_fill<real>(x, N_, 1.0 / std::sqrt(double(N_)), w.stream), "fill");
+    for (int i = 0; i < iters; ++i) {
+      forward_slots(x);
+      adjoint_slots(x);
+      cuda_check(launch_sq_norm<real>(x, N_, partial, sq + i, w.stream), "norm");
+      cuda_check(launch_scale_rsqrt<real>(x, N_, sq + i, w.stream), "scale");
+    }
+  });
 }
 
 template <typename real>
@@ -798,12 +883,12 @@ void OperatorT<real>::mark_begin(int stage) {
     }
   }
   marks_[marks_used_].stage = stage;
-  cuda_check(cudaEventRecord(marks_[marks_used_].a, stream_), "cudaEventRecord");
+  cuda_check(cudaEventRecord(marks_[marks_used_].a, ws_->stream), "cudaEventRecord");
 }
 template <typename real>
 void OperatorT<real>::mark_end(int) {
   if (!timing_) return;
-  cuda_check(cudaEventRecord(marks_[marks_used_].b, stream_), "cudaEventRecord");
+  cuda_check(cudaEventRecord(marks_[marks_used_].b, ws_->stream), "cudaEventRecord");
   ++marks_used_;
 }
 template <typename real>

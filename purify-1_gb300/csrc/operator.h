@@ -62,6 +62,21 @@ struct OperatorInfo {
   double kernel_fit_error = 0, norm = 1;
 };
 
+// Scratch of one apply held outside the operator, so that several applies of
+// one coverage can be in flight at once on different streams.
+struct Workspace {
+  void *pad = nullptr;      // Nv x Nu complex, zero outside the image region
+  void *work = nullptr;     // Nv x Nu complex
+  void *tilebuf = nullptr;  // accumulation windows of the tasks
+  void *slots = nullptr;    // slot-ordered visibilities
+  int fft = 0;              // cuFFT plan (cufftHandle) of Nv x Nu, bound to `stream`
+  cudaStream_t stream = nullptr;
+  bool unit_norm = false;   // apply Phi' (norm 1) instead of Phi
+};
+struct WorkspaceSizes {
+  int64_t pad = 0, work = 0, tilebuf = 0, slots = 0;  // bytes
+};
+
 class Operator {
  public:
   static std::unique_ptr<Operator> create(const OperatorConfig &cfg);
@@ -88,6 +103,16 @@ class Operator {
   static constexpr int kStages = 9;
   virtual void set_stage_timing(bool on) = 0;
   virtual void stage_times(double *total_ms, int64_t *launches) = 0;
+  // Applies on a caller's workspace: enqueued on ws.stream only (no wait on
+  // the operator's own stream), coverage state read-only.
+  virtual WorkspaceSizes workspace_sizes() const = 0;
+  virtual void forward_ws(const void *x, void *y, const Workspace &ws) = 0;
+  virtual void adjoint_ws(const void *y, void *x, const Workspace &ws) = 0;
+  // `iters` power-method rounds of Phi'^H Phi' from the normalised all-ones
+  // image in x (N complex scratch), the normalisation on the device; sq[i]
+  // (device) receives ||x||^2 of round i, partial is kNormBlocks doubles.
+  virtual void power_ws(void *x, int iters, double *sq, double *partial,
+                        const Workspace &ws) = 0;
 };
 
 }  // namespace pg

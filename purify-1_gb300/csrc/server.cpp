@@ -1,0 +1,473 @@
+#include "server.h"
+
+#include <cufft.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "device_kernels.h"
+#include "device_util.h"
+
+namespace pg {
+namespace {
+
+using Clock = std::chrono::steady_clock;
+double ms_between(Clock::time_point a, Clock::time_point b) {
+  return std::chrono::duration<double, std::milli>(b - a).count();
+}
+size_t up256(size_t b) { return (b + 255) / 256 * 256; }
+
+// A non-head request may overtake a head that does not fit the budget at
+// most this many times before admission waits for the head.
+constexpr int kMaxOvertakes = 16;
+
+}  // namespace
+
+struct Server::Coverage {
+  std::unique_ptr<Operator> op;
+  OperatorInfo info;
+  WorkspaceSizes ws;
+  int64_t M = 0, N = 0;
+  bool fp64 = false;
+};
+
+struct Server::Slot {
+  cudaStream_t stream = nullptr;
+  std::map<int64_t, cufftHandle> plans;  // key: fp64 | Nu << 1 | Nv << 32
+  bool busy = false;
+};
+
+struct Server::Job {
+  Server *server = nullptr;
+  int64_t ticket = 0;
+  Request rq;
+  int status = kOk;
+  bool done = false;
+  int overtaken = 0;
+  Clock::time_point t_submit, t_admit, t_done;
+  void *host_in = nullptr, *host_out = nullptr;
+  size_t in_bytes = 0, out_bytes = 0;
+  void *dev = nullptr;
+  int64_t bytes = 0;
+  Slot *slot = nullptr;
+  double norm = 0;
+  int iterations = 0;
+};
+
+static int64_t plan_key(bool fp64, int Nu, int Nv) {
+  return int64_t(fp64) | (int64_t(Nu) << 1) | (int64_t(Nv) << 32);
+}
+
+Server::Server(const ServerConfig &cfg) : cfg_(cfg) {
+  if (cfg.slots < 1 || cfg.slots > 64) throw Error(kInvalidArgument, "slots must be in [1, 64]");
+  if (cfg.hbm_budget <= 0) throw Error(kInvalidArgument, "the HBM budget must be positive");
+  DeviceGuard guard(cfg.device);
+  cudaMemPoolProps props{};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.handleTypes = cudaMemHandleTypeNone;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = cfg.device;
+  cuda_check(cudaMemPoolCreate(&pool_, &props), "cudaMemPoolCreate");
+  // Keep freed request memory in the pool (no return to the driver between
+  // requests); the budget bounds what is in use.
+  uint64_t keep = uint64_t(cfg.hbm_budget);
+  cuda_check(cudaMemPoolSetAttribute(pool_, cudaMemPoolAttrReleaseThreshold, &keep),
+             "cudaMemPoolSetAttribute");
+  for (int k = 0; k < cfg.slots; ++k) {
+    std::unique_ptr<Slot> s(new Slot);
+    cuda_check(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    slots_.push_back(std::move(s));
+  }
+  stats_.bytes_budget = cfg.hbm_budget;
+  thread_ = std::thread([this] { loop(); });
+}
+
+Server::~Server() {
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    stop_ = true;
+    dirty_ = true;
+  }
+  cv_.notify_all();
+  if (thread_.joinable()) thread_.join();
+  DeviceGuard guard(cfg_.device);
+  for (auto &s : slots_) {
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (auto &kv : s->plans) cufftDestroy(kv.second);
+    if (s->stream) cudaStreamDestroy(s->stream);
+  }
+  if (pool_) cudaMemPoolDestroy(pool_);
+  for (auto &kv : jobs_) {
+    Job &j = *kv.second;
+    if (j.host_in) unpin(j.host_in, j.in_bytes);
+    if (j.host_out) unpin(j.host_out, j.out_bytes);
+  }
+  for (auto &kv : pinned_free_) cudaFreeHost(kv.second);
+}
+
+int Server::add_coverage(const OperatorConfig &cfg_in) {
+  OperatorConfig cfg = cfg_in;
+  cfg.device = cfg_.device;
+  std::unique_ptr<Coverage> c(new Coverage);
+  c->op = Operator::create(cfg);
+  c->info = c->op->info();
+  c->ws = c->op->workspace_sizes();
+  c->M = c->info.M;
+  c->N = int64_t(c->info.imsizey) * c->info.imsizex;
+  c->fp64 = c->info.fp64;
+  // cuFFT plans of this grid size for every slot, made before any request
+  // needs them (plan creation allocates).
+  DeviceGuard guard(cfg_.device);
+  const int64_t key = plan_key(c->fp64, int(c->info.ftsizeu), int(c->info.ftsizev));
+  std::lock_guard<std::mutex> lk(mu_);
+  for (auto &s : slots_) {
+    if (s->plans.count(key)) continue;
+    cufftHandle h = 0;
+    cufft_check(cufftPlan2d(&h, int(c->info.ftsizev), int(c->info.ftsizeu),
+                            c->fp64 ? CUFFT_Z2Z : CUFFT_C2C),
+                "cufftPlan2d");
+    const cufftResult r = cufftSetStream(h, s->stream);
+    if (r != CUFFT_SUCCESS) {
+      cufftDestroy(h);
+      cufft_check(r, "cufftSetStream");
+    }
+    s->plans[key] = h;
+  }
+  coverages_.push_back(std::move(c));
+  return int(coverages_.size()) - 1;
+}
+
+// Device layout of a request, 256-byte aligned pieces: complex<double> I/O
+// vectors, their working-precision copies (FP32 only), the workspace, and the
+// power-method vectors.
+int64_t Server::request_bytes(const Request &rq) const {
+  if (rq.coverage < 0 || rq.coverage >= int(coverages_.size()))
+    throw Error(kInvalidArgument, "unknown coverage");
+  const Coverage &c = *coverages_[rq.coverage];
+  const size_t cs = c.fp64 ? 16 : 8;
+  size_t b = up256(size_t(c.ws.pad)) + up256(size_t(c.ws.work)) + up256(size_t(c.ws.tilebuf)) +
+             up256(size_t(c.ws.slots));
+  if (rq.kind == kReqNorm) {
+    b += up256(cs * size_t(c.N)) + up256(sizeof(double) * std::max(rq.iters, 1)) +
+         up256(sizeof(double) * kNormBlocks);
+    return int64_t(b);
+  }
+  b += up256(16 * size_t(c.N)) + up256(16 * size_t(std::max<int64_t>(c.M, 1)));
+  if (!c.fp64) b += up256(8 * size_t(c.N)) + up256(8 * size_t(std::max<int64_t>(c.M, 1)));
+  return int64_t(b);
+}
+
+void *Server::pinned(size_t bytes) {
+  size_t cls = 4096;
+  while (cls < bytes) cls <<= 1;
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    auto it = pinned_free_.find(cls);
+    if (it != pinned_free_.end()) {
+      void *p = it->second;
+      pinned_free_.erase(it);
+      return p;
+    }
+  }
+  void *p = nullptr;
+  cuda_check(cudaHostAlloc(&p, cls, cudaHostAllocPortable), "cudaHostAlloc");
+  return p;
+}
+void Server::unpin(void *p, size_t bytes) {
+  size_t cls = 4096;
+  while (cls < bytes) cls <<= 1;
+  pinned_free_.emplace(cls, p);  // caller holds mu_
+}
+
+int64_t Server::submit(const Request &rq) {
+  if (rq.kind < kReqForward || rq.kind > kReqNorm) throw Error(kInvalidArgument, "unknown request kind");
+  const int64_t need = request_bytes(rq);
+  const Coverage &c = *coverages_[rq.coverage];
+  const bool fwd = rq.kind == kReqForward || rq.kind == kReqForwardAdjoint;
+  const bool adj = rq.kind == kReqAdjoint || rq.kind == kReqForwardAdjoint;
+  if (fwd && (!rq.x_in || (c.M > 0 && !rq.vis_out)))
+    throw Error(kInvalidArgument, "a forward request needs x_in and vis_out");
+  if (rq.kind == kReqAdjoint && c.M > 0 && !rq.vis_in)
+    throw Error(kInvalidArgument, "an adjoint request needs vis_in");
+  if (adj && !rq.x_out) throw Error(kInvalidArgument, "an adjoint request needs x_out");
+  if (rq.kind == kReqNorm && rq.iters < 1) throw Error(kInvalidArgument, "iters must be >= 1");
+  std::shared_ptr<Job> j(new Job);
+  j->server = this;
+  j->rq = rq;
+  j->bytes = need;
+  j->t_submit = Clock::now();
+  switch (rq.kind) {
+    case kReqForward: j->in_bytes = 16 * size_t(c.N); j->out_bytes = 16 * size_t(c.M); break;
+    case kReqAdjoint: j->in_bytes = 16 * size_t(c.M); j->out_bytes = 16 * size_t(c.N); break;
+    case kReqForwardAdjoint:
+      j->in_bytes = 16 * size_t(c.N);
+      j->out_bytes = 16 * size_t(c.M + c.N);
+      break;
+    default: j->in_bytes = 0; j->out_bytes = sizeof(double) * size_t(rq.iters); break;
+  }
+  if (j->in_bytes) {
+    j->host_in = pinned(j->in_bytes);
+    std::memcpy(j->host_in, fwd ? rq.x_in : rq.vis_in, j->in_bytes);
+  }
+  if (j->out_bytes) j->host_out = pinned(j->out_bytes);
+  int64_t ticket;
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    ticket = next_ticket_++;
+    j->ticket = ticket;
+    jobs_[ticket] = j;
+    ++stats_.submitted;
+    if (need > cfg_.hbm_budget) {
+      j->status = kRejected;
+      j->done = true;
+      j->t_admit = j->t_done = j->t_submit;
+      ++stats_.rejected;
+    } else {
+      pending_.push_back(j);
+      dirty_ = true;
+    }
+  }
+  cv_.notify_one();
+  done_cv_.notify_all();
+  return ticket;
+}
+
+void CUDART_CB Server::on_done(void *p) {
+  Job *j = static_cast<Job *>(p);
+  Server *s = j->server;
+  {
+    std::lock_guard<std::mutex> lk(s->mu_);
+    j->t_done = Clock::now();
+    s->completed_.push_back(j);
+    s->dirty_ = true;
+  }
+  s->cv_.notify_one();
+}
+
+void Server::loop() {
+  cudaSetDevice(cfg_.device);
+  std::unique_lock<std::mutex> lk(mu_);
+  for (;;) {
+    cv_.wait(lk, [&] { return dirty_; });
+    dirty_ = false;
+    while (!completed_.empty()) {
+      Job *j = completed_.front();
+      completed_.pop_front();
+      finish(*j);
+    }
+    // Admission: first come first served, but a request that fits may
+    // overtake a head that does not (a bounded number of times).
+    auto it = pending_.begin();
+    while (it != pending_.end()) {
+      Slot *free = nullptr;
+      for (auto &s : slots_)
+        if (!s->busy) {
+          free = s.get();
+          break;
+        }
+      if (!free) break;
+      Job &j = **it;
+      if (bytes_in_use_ + j.bytes <= cfg_.hbm_budget) {
+        if (it != pending_.begin()) ++pending_.front()->overtaken;
+        launch(j, *free);
+        it = pending_.erase(it);
+        continue;
+      }
+      if (pending_.front()->overtaken >= kMaxOvertakes) break;
+      ++it;
+    }
+    if (stop_ && pending_.empty() && inflight_ == 0) break;
+  }
+}
+
+void Server::launch(Job &j, Slot &slot) {
+  const Coverage &c = *coverages_[j.rq.coverage];
+  j.slot = &slot;
+  j.t_admit = Clock::now();
+  slot.busy = true;
+  bytes_in_use_ += j.bytes;
+  ++inflight_;
+  stats_.bytes_peak = std::max(stats_.bytes_peak, bytes_in_use_);
+  stats_.inflight_peak = std::max(stats_.inflight_peak, inflight_);
+  cudaStream_t s = slot.stream;
+  try {
+    cuda_check(cudaMallocFromPoolAsync(&j.dev, size_t(j.bytes), pool_, s), "request memory");
+    char *p = static_cast<char *>(j.dev);
+    auto take = [&](size_t b) {
+      char *q = p;
+      p += up256(b);
+      return static_cast<void *>(q);
+    };
+    Workspace ws;
+    ws.pad = take(size_t(c.ws.pad));
+    ws.work = take(size_t(c.ws.work));
+    ws.tilebuf = take(size_t(c.ws.tilebuf));
+    ws.slots = take(size_t(c.ws.slots));
+    ws.fft = slot.plans.at(plan_key(c.fp64, int(c.info.ftsizeu), int(c.info.ftsizev)));
+    ws.stream = s;
+    // the padded grid must be zero outside the image region
+    cuda_check(cudaMemsetAsync(ws.pad, 0, size_t(c.ws.pad), s), "cudaMemsetAsync");
+    const size_t cs = c.fp64 ? 16 : 8;
+    if (j.rq.kind == kReqNorm) {
+      void *x = take(cs * size_t(c.N));
+      double *sq = static_cast<double *>(take(sizeof(double) * j.rq.iters));
+      double *partial = static_cast<double *>(take(sizeof(double) * kNormBlocks));
+      c.op->power_ws(x, j.rq.iters, sq, partial, ws);
+      cuda_check(cudaMemcpyAsync(j.host_out, sq, sizeof(double) * j.rq.iters,
+                                 cudaMemcpyDeviceToHost, s),
+                 "D2H");
+    } else {
+      void *x128 = take(16 * size_t(c.N));
+      void *y128 = take(16 * size_t(std::max<int64_t>(c.M, 1)));
+      void *xc = x128, *yc = y128;
+      if (!c.fp64) {
+        xc = take(8 * size_t(c.N));
+        yc = take(8 * size_t(std::max<int64_t>(c.M, 1)));
+      }
+      auto to_work = [&](void *src128, void *dst, int64_t n) {
+        if (!c.fp64) cuda_check(launch_from_c128<float>(src128, dst, n, s), "convert");
+      };
+      auto to_c128 = [&](void *src, void *dst128, int64_t n) {
+        if (!c.fp64) cuda_check(launch_to_c128<float>(src, dst128, n, s), "convert");
+      };
+      const bool fwd = j.rq.kind != kReqAdjoint;
+      if (fwd) {
+        cuda_check(cudaMemcpyAsync(x128, j.host_in, 16 * size_t(c.N), cudaMemcpyHostToDevice, s),
+                   "H2D");
+        to_work(x128, xc, c.N);
+        c.op->forward_ws(xc, yc, ws);
+      } else if (c.M > 0) {
+        cuda_check(cudaMemcpyAsync(y128, j.host_in, 16 * size_t(c.M), cudaMemcpyHostToDevice, s),
+                   "H2D");
+        to_work(y128, yc, c.M);
+      }
+      if (j.rq.kind != kReqForward) {
+        if (j.rq.kind == kReqAdjoint && c.M == 0)
+          cuda_check(cudaMemsetAsync(yc, 0, cs, s), "cudaMemsetAsync");
+        // x was read by the forward's first kernel, so its buffer takes the image
+        c.op->adjoint_ws(yc, xc, ws);
+      }
+      char *out = static_cast<char *>(j.host_out);
+      if (fwd && c.M > 0) {
+        to_c128(yc, y128, c.M);
+        cuda_check(cudaMemcpyAsync(out, y128, 16 * size_t(c.M), cudaMemcpyDeviceToHost, s), "D2H");
+        out += 16 * size_t(c.M);
+      }
+      if (j.rq.kind != kReqForward) {
+        to_c128(xc, x128, c.N);
+        cuda_check(cudaMemcpyAsync(out, x128, 16 * size_t(c.N), cudaMemcpyDeviceToHost, s), "D2H");
+      }
+    }
+    cuda_check(cudaLaunchHostFunc(s, &Server::on_done, &j), "cudaLaunchHostFunc");
+  } catch (const Error &e) {
+    // Nothing will call back: retire now.  Work already enqueued finishes
+    // before the stream-ordered free.
+    j.status = int(e.status);
+    j.t_done = Clock::now();
+    finish(j);
+  }
+}
+
+void Server::finish(Job &j) {
+  Slot &slot = *j.slot;
+  if (j.dev) cudaFreeAsync(j.dev, slot.stream);
+  j.dev = nullptr;
+  slot.busy = false;
+  bytes_in_use_ -= j.bytes;
+  --inflight_;
+  const Coverage &c = *coverages_[j.rq.coverage];
+  if (j.status == kOk && j.rq.kind == kReqNorm) {
+    // the single-operator stopping rule on the recorded estimates
+    const double *sq = static_cast<const double *>(j.host_out);
+    double old_value = 0;
+    for (int i = 0; i < j.rq.iters; ++i) {
+      const double value = std::sqrt(sq[i]);
+      j.iterations = i + 1;
+      if (!(value > 0)) {
+        j.status = kNormNotPositive;
+        break;
+      }
+      if (j.rq.tol * j.rq.tol > std::abs(old_value - value) / old_value) {
+        old_value = value;
+        break;
+      }
+      old_value = value;
+    }
+    j.norm = std::sqrt(old_value);
+  }
+  if (j.status == kOk) {
+    ++stats_.completed;
+    const double passes = j.rq.kind == kReqNorm ? 2.0 * j.rq.iters
+                          : j.rq.kind == kReqForwardAdjoint ? 2.0 : 1.0;
+    stats_.visibility_passes += passes * double(c.M);
+    latencies_.push_back(ms_between(j.t_submit, j.t_done));
+  } else {
+    ++stats_.failed;
+  }
+  j.done = true;
+  done_cv_.notify_all();
+}
+
+bool Server::wait(int64_t ticket, double timeout_s, RequestResult *out) {
+  std::shared_ptr<Job> j;
+  {
+    std::unique_lock<std::mutex> lk(mu_);
+    auto it = jobs_.find(ticket);
+    if (it == jobs_.end()) throw Error(kInvalidArgument, "unknown ticket");
+    j = it->second;
+    auto ready = [&] { return j->done; };
+    if (timeout_s < 0)
+      done_cv_.wait(lk, ready);
+    else if (!done_cv_.wait_for(lk, std::chrono::duration<double>(timeout_s), ready))
+      return false;
+    jobs_.erase(ticket);
+  }
+  const Coverage &c = *coverages_[j->rq.coverage];
+  if (j->status == kOk && j->rq.kind != kReqNorm) {
+    const char *src = static_cast<const char *>(j->host_out);
+    if (j->rq.kind != kReqAdjoint && c.M > 0) {
+      std::memcpy(j->rq.vis_out, src, 16 * size_t(c.M));
+      src += 16 * size_t(c.M);
+    }
+    if (j->rq.kind != kReqForward) std::memcpy(j->rq.x_out, src, 16 * size_t(c.N));
+  }
+  if (out) {
+    out->status = j->status;
+    out->norm = j->norm;
+    out->iterations = j->iterations;
+    out->queue_ms = ms_between(j->t_submit, j->t_admit);
+    out->run_ms = ms_between(j->t_admit, j->t_done);
+    out->latency_ms = ms_between(j->t_submit, j->t_done);
+    out->device_bytes = j->bytes;
+  }
+  std::lock_guard<std::mutex> lk(mu_);
+  if (j->host_in) unpin(j->host_in, j->in_bytes);
+  if (j->host_out) unpin(j->host_out, j->out_bytes);
+  j->host_in = j->host_out = nullptr;
+  return true;
+}
+
+ServerStats Server::stats() const {
+  std::lock_guard<std::mutex> lk(mu_);
+  ServerStats s = stats_;
+  if (!latencies_.empty()) {
+    std::vector<double> v = latencies_;
+    std::sort(v.begin(), v.end());
+    auto pct = [&](double q) {
+      // nearest-rank percentile
+      const size_t k = size_t(std::ceil(q * double(v.size())));
+      return v[std::min(v.size() - 1, k == 0 ? 0 : k - 1)];
+    };
+    s.latency_p50_ms = pct(0.50);
+    s.latency_p99_ms = pct(0.99);
+    double sum = 0;
+    for (double x : v) sum += x;
+    s.latency_mean_ms = sum / double(v.size());
+  }
+  return s;
+}
+
+}  // namespace pg

@@ -84,6 +84,36 @@ class BatchInfo(ctypes.Structure):
                 ("tasks", ctypes.c_int64), ("device_bytes", ctypes.c_int64)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("slots", ctypes.c_int32),
+                ("hbm_budget_bytes", ctypes.c_int64)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("coverage", ctypes.c_int32), ("kind", ctypes.c_int32), ("x_in", ctypes.c_void_p),
+                ("vis_in", ctypes.c_void_p), ("vis_out", ctypes.c_void_p),
+                ("x_out", ctypes.c_void_p), ("iters", ctypes.c_uint32), ("tol", ctypes.c_double)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("iterations", ctypes.c_int32),
+                ("norm", ctypes.c_double), ("queue_ms", ctypes.c_double),
+                ("run_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
+                ("device_bytes", ctypes.c_int64)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64),
+                ("rejected", ctypes.c_int64), ("failed", ctypes.c_int64),
+                ("inflight_peak", ctypes.c_int64), ("bytes_peak", ctypes.c_int64),
+                ("bytes_budget", ctypes.c_int64), ("latency_p50_ms", ctypes.c_double),
+                ("latency_p99_ms", ctypes.c_double), ("latency_mean_ms", ctypes.c_double),
+                ("visibility_passes", ctypes.c_double)]
+
+
+REQUEST_KINDS = {"forward": 1, "adjoint": 2, "forward_adjoint": 3, "norm": 4}
+
+
 # Every symbol include/purify_gb300.h declares (checked by the CPU tests).
 EXPORTS = [
     "purify_gb300_default_args", "purify_gb300_operator_create", "purify_gb300_operator_destroy",
@@ -100,6 +130,9 @@ EXPORTS = [
     "purify_gb300_batch_bind", "purify_gb300_batch_apply", "purify_gb300_batch_power_method",
     "purify_gb300_batch_set_norms", "purify_gb300_batch_get_norms", "purify_gb300_batch_info_get",
     "purify_gb300_batch_time",
+    "purify_gb300_server_create", "purify_gb300_server_destroy", "purify_gb300_server_add_coverage",
+    "purify_gb300_server_submit", "purify_gb300_server_wait", "purify_gb300_server_request_bytes",
+    "purify_gb300_server_get_stats",
 ]
 STAGES = ["pad", "fft_forward", "degrid", "grid", "fold", "fft_inverse", "crop", "compact",
           "expand"]
@@ -169,6 +202,13 @@ def load(path=None):
     L.purify_gb300_batch_info_get.argtypes = [vp, P(BatchInfo)]
     L.purify_gb300_batch_time.argtypes = [vp, ctypes.c_int32, ctypes.c_uint32,
                                           P(ctypes.c_double)]
+    L.purify_gb300_server_create.argtypes = [P(ServerConfig), P(vp)]
+    L.purify_gb300_server_destroy.argtypes = [vp]
+    L.purify_gb300_server_add_coverage.argtypes = [vp, P(CreateArgs), P(ctypes.c_int32)]
+    L.purify_gb300_server_submit.argtypes = [vp, P(Request), P(ctypes.c_int64)]
+    L.purify_gb300_server_wait.argtypes = [vp, ctypes.c_int64, ctypes.c_double, P(Result)]
+    L.purify_gb300_server_request_bytes.argtypes = [vp, P(Request), P(ctypes.c_int64)]
+    L.purify_gb300_server_get_stats.argtypes = [vp, P(ServerStats)]
     _lib = L
     return L
 
@@ -261,6 +301,39 @@ class CoveragePlan:
         self.Nu, self.Nv, self.J = int(ftsizeu), int(ftsizev), int(J)
 
 
+def _create_args(u, v, w, weights, imsizey, imsizex, oversample_ratio, power_iters, power_tol,
+                 kernel, Ju, Jv, w_term, Jw, cellx, celly, precision, device, jw_rows):
+    """CreateArgs of the reference's factory arguments; returns the struct and
+    the arrays it points into (keep them alive while it is used)."""
+    L = load()
+    u = np.ascontiguousarray(u, dtype=np.float64).ravel()
+    v = np.ascontiguousarray(v, dtype=np.float64).ravel()
+    if v.size != u.size:
+        raise PurifyError(1, "Size of u and v vectors are not the same for creating gridding matrix.")
+    w = None if w is None else np.ascontiguousarray(w, dtype=np.float64).ravel()
+    wt = None if weights is None else np.ascontiguousarray(weights, dtype=np.complex128).ravel()
+    jw = None if jw_rows is None else np.ascontiguousarray(jw_rows, dtype=np.int32).ravel()
+    a = CreateArgs()
+    L.purify_gb300_default_args(ctypes.byref(a))
+    a.u, a.v = _np_ptr(u), _np_ptr(v)
+    a.w = _np_ptr(w)
+    a.weights = _np_ptr(wt)
+    a.M = u.size
+    a.imsizey, a.imsizex = int(imsizey), int(imsizex)
+    a.oversample_ratio = float(oversample_ratio)
+    a.power_iters = int(power_iters)
+    a.power_tol = float(power_tol)
+    a.kernel = KERNELS[kernel] if isinstance(kernel, str) else int(kernel)
+    a.Ju, a.Jv = int(Ju), int(Jv)
+    a.w_term = 1 if w_term else 0
+    a.Jw = int(Jw)
+    a.jw_rows = _np_ptr(jw)
+    a.cellx, a.celly = float(cellx), float(celly)
+    a.precision = PRECISIONS[precision]
+    a.device = int(device)
+    return a, (u, v, w, wt, jw)
+
+
 def _is_torch(x):
     return type(x).__module__.startswith("torch")
 
@@ -273,33 +346,10 @@ class MeasurementOperator:
                  w_term=False, Jw=6, cellx=1.0, celly=1.0, precision="fp32", device=0,
                  tuning=None, jw_rows=None):
         L = load()
-        u = np.ascontiguousarray(u, dtype=np.float64).ravel()
-        v = np.ascontiguousarray(v, dtype=np.float64).ravel()
-        M = u.size
-        if v.size != M:
-            raise PurifyError(1, "Size of u and v vectors are not the same for creating gridding matrix.")
-        w = None if w is None else np.ascontiguousarray(w, dtype=np.float64).ravel()
-        wt = None if weights is None else np.ascontiguousarray(weights, dtype=np.complex128).ravel()
-        a = CreateArgs()
-        L.purify_gb300_default_args(ctypes.byref(a))
-        a.u, a.v = _np_ptr(u), _np_ptr(v)
-        a.w = _np_ptr(w)
-        a.weights = _np_ptr(wt)
-        a.M = M
-        a.imsizey, a.imsizex = int(imsizey), int(imsizex)
-        a.oversample_ratio = float(oversample_ratio)
-        a.power_iters = int(power_iters)
-        a.power_tol = float(power_tol)
-        a.kernel = KERNELS[kernel] if isinstance(kernel, str) else int(kernel)
-        a.Ju, a.Jv = int(Ju), int(Jv)
-        a.w_term = 1 if w_term else 0
-        a.Jw = int(Jw)
-        jw = None if jw_rows is None else np.ascontiguousarray(jw_rows, dtype=np.int32).ravel()
-        self._jw = jw
-        a.jw_rows = _np_ptr(jw)
-        a.cellx, a.celly = float(cellx), float(celly)
-        a.precision = PRECISIONS[precision]
-        a.device = int(device)
+        a, keep = _create_args(u, v, w, weights, imsizey, imsizex, oversample_ratio, power_iters,
+                               power_tol, kernel, Ju, Jv, w_term, Jw, cellx, celly, precision,
+                               device, jw_rows)
+        M = a.M
         h = ctypes.c_void_p()
         if tuning:
             t = Tuning(int(tuning.get("threads", 0)), int(tuning.get("max_per_item", 0)),
@@ -587,3 +637,107 @@ class Batch:
         n = np.zeros(self.nch)
         _check(load().purify_gb300_batch_get_norms(self._h, _np_ptr(n)))
         return n
+
+
+class Server:
+    """Request server on one GPU: coverages resident on the device, requests
+    admitted by an HBM budget and run concurrently on `slots` streams, each
+    with its own workspace (see include/purify_gb300.h).  Host vectors are
+    complex128 numpy arrays."""
+
+    def __init__(self, device=0, slots=8, hbm_budget=8 << 30):
+        L = load()
+        cfg = ServerConfig(int(device), int(slots), int(hbm_budget))
+        h = ctypes.c_void_p()
+        _check(L.purify_gb300_server_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self._cov = []       # (M, N) per coverage
+        self._out = {}       # ticket -> output arrays
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            load().purify_gb300_server_destroy(h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_coverage(self, u, v, w=None, weights=None, imsizey=256, imsizex=256,
+                     oversample_ratio=2.0, power_iters=0, power_tol=1e-4, kernel="kb", Ju=4,
+                     Jv=4, w_term=False, Jw=6, cellx=1.0, celly=1.0, precision="fp32",
+                     jw_rows=None):
+        a, keep = _create_args(u, v, w, weights, imsizey, imsizex, oversample_ratio, power_iters,
+                               power_tol, kernel, Ju, Jv, w_term, Jw, cellx, celly, precision, 0,
+                               jw_rows)
+        cid = ctypes.c_int32()
+        _check(load().purify_gb300_server_add_coverage(self._h, ctypes.byref(a), ctypes.byref(cid)))
+        del keep
+        self._cov.append((int(a.M), int(imsizey) * int(imsizex)))
+        return cid.value
+
+    def _request(self, coverage, kind, x=None, vis=None, iters=50, tol=1e-4):
+        M, N = self._cov[coverage]
+        k = REQUEST_KINDS[kind] if isinstance(kind, str) else int(kind)
+        rq = Request()
+        rq.coverage, rq.kind, rq.iters, rq.tol = int(coverage), k, int(iters), float(tol)
+        keep, outs = [], {}
+        if k in (1, 3):
+            x = np.ascontiguousarray(x, dtype=np.complex128).ravel()
+            if x.size != N:
+                raise PurifyError(1, "image vector has %d values, expected %d" % (x.size, N))
+            keep.append(x)
+            rq.x_in = _np_ptr(x)
+            outs["vis"] = np.empty(M, dtype=np.complex128)
+            rq.vis_out = _np_ptr(outs["vis"])
+        if k == 2:
+            vis = np.ascontiguousarray(vis, dtype=np.complex128).ravel()
+            if vis.size != M:
+                raise PurifyError(1, "visibility vector has %d values, expected %d" % (vis.size, M))
+            keep.append(vis)
+            rq.vis_in = _np_ptr(vis)
+        if k in (2, 3):
+            outs["x"] = np.empty(N, dtype=np.complex128)
+            rq.x_out = _np_ptr(outs["x"])
+        return rq, keep, outs
+
+    def request_bytes(self, coverage, kind, iters=50):
+        M, N = self._cov[coverage]
+        rq, _, _ = self._request(coverage, kind, np.zeros(N, np.complex128),
+                                 np.zeros(M, np.complex128), iters)
+        b = ctypes.c_int64()
+        _check(load().purify_gb300_server_request_bytes(self._h, ctypes.byref(rq), ctypes.byref(b)))
+        return b.value
+
+    def submit(self, coverage, kind, x=None, vis=None, iters=50, tol=1e-4):
+        """Queues a request ("forward", "adjoint", "forward_adjoint", "norm");
+        returns its ticket.  Inputs are copied before this returns."""
+        rq, keep, outs = self._request(coverage, kind, x, vis, iters, tol)
+        t = ctypes.c_int64()
+        _check(load().purify_gb300_server_submit(self._h, ctypes.byref(rq), ctypes.byref(t)))
+        del keep
+        self._out[t.value] = outs
+        return t.value
+
+    def wait(self, ticket, timeout=None):
+        """The request's result dict (status, norm, iterations, queue_ms,
+        run_ms, latency_ms, device_bytes, vis / x outputs), or None if it is
+        still running after `timeout` seconds."""
+        r = Result()
+        rc = load().purify_gb300_server_wait(self._h, int(ticket),
+                                             -1.0 if timeout is None else float(timeout),
+                                             ctypes.byref(r))
+        if rc == 7:
+            return None
+        _check(rc)
+        out = {f: getattr(r, f) for f, _ in Result._fields_}
+        out.update(self._out.pop(ticket, {}))
+        return out
+
+    def stats(self):
+        st = ServerStats()
+        _check(load().purify_gb300_server_get_stats(self._h, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in ServerStats._fields_}

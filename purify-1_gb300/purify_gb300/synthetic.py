@@ -116,3 +116,29 @@ def config_batch(nch=64, seed=0, m_lo=1e4, m_hi=2e6, sizes=(256, 512, 1024)):
         u, v = mixed_uv(int(Ms[k]), 2 * n, 2 * n, 0.7, 0.15 * (1 + 0.01 * k), seed=seed + 1000 + k)
         chans.append(dict(u=u, v=v, imsizey=n, imsizex=n, x=sky_image(n, n, seed=seed + k)))
     return chans
+
+
+def config_serve_pool(n=16, seed=0, m_lo=1e4, m_hi=5e6, sizes=(256, 512, 1024)):
+    """n resident coverages for the request server: image size drawn from
+    `sizes`, visibility count log-uniform in [m_lo, m_hi], 70% Gaussian core
+    (sigma = 0.15 N) + 30% uniform, KB J=4."""
+    rng = np.random.default_rng(seed)
+    sz = rng.choice(np.asarray(sizes), n)
+    Ms = np.exp(rng.uniform(np.log(m_lo), np.log(m_hi), n)).astype(np.int64)
+    out = []
+    for k in range(n):
+        m = int(sz[k])
+        u, v = mixed_uv(int(Ms[k]), 2 * m, 2 * m, 0.7, 0.15, seed=seed + 2000 + k)
+        out.append(dict(u=u, v=v, imsizey=m, imsizex=m))
+    return out
+
+
+def request_stream(n, rate, n_coverages, seed=0, mix=(0.70, 0.25, 0.05)):
+    """n requests of a Poisson stream at `rate` per second: arrival times,
+    kinds (forward_adjoint / adjoint / norm with probabilities `mix`) and
+    coverages (uniform over the pool)."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, n))
+    kinds = rng.choice(np.array(["forward_adjoint", "adjoint", "norm"]), n, p=np.asarray(mix))
+    cov = rng.integers(0, n_coverages, n)
+    return t, kinds, cov
