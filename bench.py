@@ -841,7 +841,11 @@ def run_serve(args):
         "latency_ms": f32["latency_ms"], "serving": {k: {kk: vv for kk, vv in v.items()
                                                           if kk != "_res"}
                                                       for k, v in per_prec.items()},
-        "gpu_launches": None,
+        # own kernels per request (FP32): conversions, pad, degrid, expand,
+        # grid, fold, crop; a norm round: pad, degrid, grid, fold, crop, two
+        # reduction kernels and the scale
+        "gpu_launches": int(sum({"forward_adjoint": 9, "adjoint": 6}.get(str(k), 1 + 8 * 50)
+                                for k in kinds)),
     }
     if "fp64" in per_prec:
         r32, r64 = per_prec["fp32"]["_res"], per_prec["fp64"]["_res"]

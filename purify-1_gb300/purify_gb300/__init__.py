@@ -680,6 +680,8 @@ class Server:
         return cid.value
 
     def _request(self, coverage, kind, x=None, vis=None, iters=50, tol=1e-4):
+        if not 0 <= int(coverage) < len(self._cov):
+            raise PurifyError(1, "unknown coverage %d" % coverage)
         M, N = self._cov[coverage]
         k = REQUEST_KINDS[kind] if isinstance(kind, str) else int(kind)
         rq = Request()
@@ -705,6 +707,8 @@ class Server:
         return rq, keep, outs
 
     def request_bytes(self, coverage, kind, iters=50):
+        if not 0 <= int(coverage) < len(self._cov):
+            raise PurifyError(1, "unknown coverage %d" % coverage)
         M, N = self._cov[coverage]
         rq, _, _ = self._request(coverage, kind, np.zeros(N, np.complex128),
                                  np.zeros(M, np.complex128), iters)
