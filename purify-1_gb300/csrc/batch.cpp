@@ -107,6 +107,7 @@ class BatchT final : public Batch {
   std::unique_ptr<Chan[]> chans_;
   std::vector<SizeGroup> groups_;
   int ntasks_ = 0, win_rows_ = 0, win_cols_ = 0, max_tiles_ = 0;
+  bool any_weight_ = false;  // some channel has a weight stream
   int64_t max_pixels_ = 0, max_slots_ = 0;
   Arena shared_;  // grouped task list, argument tables, padded and FFT grids
   size_t o_tasks_ = 0, o_task_base_ = 0, o_fwd_ = 0, o_adj_ = 0, o_folds_ = 0, o_io_ = 0,
@@ -191,6 +192,7 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     }
     ch.S = plan.S;
     ch.unit = plan.unit_weights;
+    if (!ch.unit) any_weight_ = true;
     ch.ntasks = int(plan.tasks.size());
     ch.ntu = plan.tu.n;
     ch.ntv = plan.tv.n;
@@ -464,9 +466,9 @@ void BatchT<real>::record(int mode) {
     const bool dg = mode == kDegridOnly;
     head.group = shared_.at<ApplyArgs<real>>(dg ? o_fwd_ : o_adj_);
     cuda_check(dg ? launch_degrid_group<real>(head, poly_, J_, ntasks_, win_rows_, win_cols_,
-                                              degrid_shape_, stream_)
+                                              degrid_shape_, true, any_weight_, stream_)
                   : launch_grid_group<real>(head, poly_, J_, ntasks_, win_rows_, win_cols_,
-                                            grid_shape_, stream_),
+                                            grid_shape_, false, any_weight_, stream_),
                dg ? "degrid" : "grid");
     return;
   }
@@ -478,14 +480,14 @@ void BatchT<real>::record(int mode) {
                   "cufftExec");
     head.group = shared_.at<ApplyArgs<real>>(o_fwd_);
     cuda_check(launch_degrid_group<real>(head, poly_, J_, ntasks_, win_rows_, win_cols_,
-                                         degrid_shape_, stream_),
+                                         degrid_shape_, true, any_weight_, stream_),
                "degrid");
   }
   if (mode & kAdjoint) {
     cuda_check(launch_expand_group<real>(io, nch_, max_slots_, stream_), "expand");
     head.group = shared_.at<ApplyArgs<real>>(o_adj_);
     cuda_check(launch_grid_group<real>(head, poly_, J_, ntasks_, win_rows_, win_cols_,
-                                       grid_shape_, stream_),
+                                       grid_shape_, false, any_weight_, stream_),
                "grid");
     cuda_check(launch_fold_group<real>(shared_.at<FoldArgs>(o_folds_), nch_, max_tiles_, stream_),
                "fold");

@@ -120,19 +120,21 @@ __global__ void scale_group_kernel(const ChannelIO<real> *__restrict__ chans,
 template <typename real>
 cudaError_t launch_degrid_group(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
                                 int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
-                                cudaStream_t s) {
-  const size_t smem = degrid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape);
+                                bool user, bool weight, cudaStream_t s) {
+  const size_t smem = degrid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, weight);
   ApplyArgs<real> b = a;
   b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, false));
+  b.stage_bytes = int(stage_bytes(sizeof(real), true, user, weight));
   return launch_apply<real, true>(true, b, poly, J, ntasks, smem, shape.threads, s);
 }
 template <typename real>
 cudaError_t launch_grid_group(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
                               int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
-                              cudaStream_t s) {
-  const size_t smem = grid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape);
+                              bool user, bool weight, cudaStream_t s) {
+  const size_t smem = grid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, weight);
   ApplyArgs<real> b = a;
   b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, true));
+  b.stage_bytes = int(stage_bytes(sizeof(real), false, user, weight));
   return launch_apply<real, true>(false, b, poly, J, ntasks, smem, shape.threads, s);
 }
 
@@ -192,11 +194,11 @@ cudaError_t launch_scale_group(const ChannelIO<real> *chans, int nch, int64_t ma
 
 #define PG_INSTANTIATE_GROUP(real)                                                               \
   template cudaError_t launch_degrid_group<real>(const ApplyArgs<real> &, const PolyTable<real> &,  \
-                                                 int, int, int, int, const LaunchShape &,          \
-                                                 cudaStream_t);                                    \
+                                                 int, int, int, int, const LaunchShape &, bool,    \
+                                                 bool, cudaStream_t);                              \
   template cudaError_t launch_grid_group<real>(const ApplyArgs<real> &, const PolyTable<real> &,    \
-                                               int, int, int, int, const LaunchShape &,            \
-                                               cudaStream_t);                                      \
+                                               int, int, int, int, const LaunchShape &, bool,      \
+                                               bool, cudaStream_t);                                \
   template cudaError_t launch_fold_group<real>(const FoldArgs *, int, int, cudaStream_t);          \
   template cudaError_t launch_pad_group<real>(const ChannelIO<real> *, int, int64_t, cudaStream_t); \
   template cudaError_t launch_crop_group<real>(const ChannelIO<real> *, int, int64_t,              \

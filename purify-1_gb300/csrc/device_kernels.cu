@@ -163,30 +163,36 @@ int stream_blocks(int64_t n, int threads) {
 }  // namespace
 
 size_t degrid_smem_bytes(int precision_bytes, int, int win_rows, int win_cols,
-                         const LaunchShape &shape) {
-  return window_bytes(precision_bytes, win_rows, win_cols, shape, false) + kHeaderBytes;
+                         const LaunchShape &shape, bool user, bool weight) {
+  return window_bytes(precision_bytes, win_rows, win_cols, shape, false) + kHeaderBytes +
+         size_t(shape.threads / 32) * stage_bytes(precision_bytes, true, user, weight);
 }
 size_t grid_smem_bytes(int precision_bytes, int, int win_rows, int win_cols,
-                       const LaunchShape &shape) {
-  return window_bytes(precision_bytes, win_rows, win_cols, shape, true) + kHeaderBytes;
+                       const LaunchShape &shape, bool user, bool weight) {
+  return window_bytes(precision_bytes, win_rows, win_cols, shape, true) + kHeaderBytes +
+         size_t(shape.threads / 32) * stage_bytes(precision_bytes, false, user, weight);
 }
 
 template <typename real>
 cudaError_t launch_degrid(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
                           int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
                           cudaStream_t s) {
-  const size_t smem = degrid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape);
+  const bool user = a.slot_user != nullptr, weight = a.weight != nullptr;
+  const size_t smem = degrid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, weight);
   ApplyArgs<real> b = a;
   b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, false));
+  b.stage_bytes = int(stage_bytes(sizeof(real), true, user, weight));
   return launch_apply<real, false>(true, b, poly, J, ntasks, smem, shape.threads, s);
 }
 template <typename real>
 cudaError_t launch_grid(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
                         int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
                         cudaStream_t s) {
-  const size_t smem = grid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape);
+  const bool user = a.slot_user != nullptr, weight = a.weight != nullptr;
+  const size_t smem = grid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, weight);
   ApplyArgs<real> b = a;
   b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, true));
+  b.stage_bytes = int(stage_bytes(sizeof(real), false, user, weight));
   return launch_apply<real, false>(false, b, poly, J, ntasks, smem, shape.threads, s);
 }
 

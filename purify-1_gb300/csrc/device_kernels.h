@@ -30,7 +30,8 @@ struct ApplyArgs {
   const int32_t *slot_user = nullptr;
   int Nu = 0, Nv = 0;
   int64_t slot_stride = 0;          // complex elements per tilebuf slot
-  int win_bytes = 0;  // set by the launchers: shared bytes before the batch headers
+  int win_bytes = 0;    // set by the launchers: shared bytes before the batch headers
+  int stage_bytes = 0;  // set by the launchers: per-warp staging stride
   // Grouped launch over several operators: a device array of per-operator
   // ApplyArgs (indexed by Task::channel) and the first task of each operator
   // in the grouped task list (its tilebuf holds windows from that index on).
@@ -45,11 +46,12 @@ struct LaunchShape {
   int threads = 128;  // 32 x warps per CTA
 };
 
-// Largest dynamic shared memory a launch of the given shape needs, in bytes.
+// Largest dynamic shared memory a launch of the given shape needs, in bytes:
+// user = visibilities in caller order, weight = a weight stream.
 size_t degrid_smem_bytes(int precision_bytes, int J, int win_rows, int win_cols,
-                         const LaunchShape &shape);
+                         const LaunchShape &shape, bool user = true, bool weight = true);
 size_t grid_smem_bytes(int precision_bytes, int J, int win_rows, int win_cols,
-                       const LaunchShape &shape);
+                       const LaunchShape &shape, bool user = false, bool weight = true);
 
 // G: tiles of the grid -> visibilities.
 template <typename real>
@@ -65,15 +67,16 @@ cudaError_t launch_grid(const ApplyArgs<real> &a, const PolyTable<real> &poly, i
 // Grouped forms: `a.tasks` lists the tasks of several operators (Task::channel
 // names the operator), `a.group` points at a device array of their ApplyArgs
 // and `a.group_task_base` at the first grouped task of each; win_rows /
-// win_cols are the largest over the group.
+// win_cols are the largest over the group; user / weight say whether any
+// operator of the group reads caller order / has a weight stream.
 template <typename real>
 cudaError_t launch_degrid_group(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
                                 int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
-                                cudaStream_t s);
+                                bool user, bool weight, cudaStream_t s);
 template <typename real>
 cudaError_t launch_grid_group(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
                               int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
-                              cudaStream_t s);
+                              bool user, bool weight, cudaStream_t s);
 
 // G^H, second half: sums the task windows that cover each grid cell, in a
 // fixed order, into the grid.

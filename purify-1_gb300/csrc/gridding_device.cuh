@@ -93,7 +93,9 @@ __device__ __forceinline__ void cp_async_wait_all() {
 }
 
 // Shared-memory layout of a task: the grid window(s), then the batch
-// headers {first slot, kmax} and the 32 lane codes of each batch.
+// headers {first slot, kmax} and the 32 lane codes of each batch, then the
+// per-warp staging buffers.
+constexpr size_t kHeaderBytes = kMaxTaskBatches * (sizeof(int2) + kBatch * sizeof(int));
 struct TaskHeaders {
   int2 *hdr;
   int *code;
@@ -116,18 +118,6 @@ __device__ __forceinline__ TaskHeaders load_headers(const A &a, const Task &tk,
   return h;
 }
 
-// Visibility read for the grid kernel: slot order, or caller order through
-// slot_user (0 for null slots).
-template <typename real>
-__device__ __forceinline__ cplx<real> read_vis(const ApplyArgs<real> &a, const cplx<real> *vin,
-                                              size_t i) {
-  if (a.slot_user) {
-    const int m = __ldcs(a.slot_user + i);
-    return m >= 0 ? vin[m] : cplx<real>{0, 0};
-  }
-  return vin[i];
-}
-
 // Operator arguments of a task.  A single-operator launch reads them from the
 // kernel parameters; a grouped launch (several operators in one grid) from
 // the device table at a0.group, indexed by the task's channel.
@@ -144,10 +134,44 @@ struct ArgsOf<real, true> {
   }
 };
 
+// Per-warp staging of the coverage stream.  A warp walks its batches in
+// chunks of up to kStage<real> k-steps; while it computes one chunk, the
+// next chunk's per-slot data (t, and the caller index, weight or visibility
+// as the launch needs) is on its way into shared memory by cp.async, so a
+// whole chunk of loads is in flight per warp instead of one step.  Each lane
+// copies and later reads only its own column, so the per-thread
+// cp.async.wait_group is the only wait.  Layout per warp, each [2][kStage][32]:
+// t, then caller index (int), then the second complex stream.
+template <typename real>
+struct StageDepth {
+  static constexpr int value = 8;
+};
+template <>
+struct StageDepth<double> {
+  static constexpr int value = 4;
+};
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+template <typename real>
+__device__ __forceinline__ void next_chunk(int &lb, int &k0, const int2 *hdr, int nw) {
+  k0 += StageDepth<real>::value;
+  if (k0 >= hdr[lb].y) {
+    k0 = 0;
+    lb += nw;
+  }
+}
+
 template <typename real, int J, bool SUB, bool GROUP>
 __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
                                                      const __grid_constant__ PolyTable<real> poly) {
   using C = cplx<real>;
+  constexpr int CH = StageDepth<real>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Task tk = a0.tasks[blockIdx.x];
   const auto &a = ArgsOf<real, GROUP>::get(a0, tk.channel);
@@ -170,94 +194,100 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
   const int nbt = tk.batch_end - tk.batch_begin;
   const C *frac = static_cast<const C *>(a.frac);
   const C *weight = static_cast<const C *>(a.weight);
+  const int32_t *user = a.slot_user;
   C *out = static_cast<C *>(a.slot_out);
   const bool unit = weight == nullptr;
-  int lb = warp;
-  if (lb >= nbt) return;
-  // One flattened loop over (batch, k) per warp; the next slot's coverage
-  // state is loaded one step ahead, across batch boundaries too.  Lanes past
-  // their item's end compute on null slots, whose results are never read.
-  int2 bt = th.hdr[lb];
-  int k = 0;
-  size_t i = size_t(bt.x) + lane;
-  int cnt = item_count(th.code[lb * kBatch + lane]);
-  C F[J][J];
-  auto load_F = [&](int code) {
-    const int lp = item_lp(code), lq = item_lq(code);
-#pragma unroll
-    for (int jv = 0; jv < J; ++jv)
-#pragma unroll
-      for (int ju = 0; ju < J; ++ju) F[jv][ju] = win[(lp + jv) * WW + lq + ju];
+  if (warp >= nbt) return;
+  unsigned char *stg = smem_raw + a0.win_bytes + kHeaderBytes + size_t(warp) * a0.stage_bytes;
+  C *st_t = reinterpret_cast<C *>(stg);
+  int *st_m = reinterpret_cast<int *>(stg + 2 * CH * 32 * sizeof(C));
+  C *st_w = reinterpret_cast<C *>(stg + 2 * CH * 32 * (sizeof(C) + (user ? 4 : 0)));
+  auto issue = [&](int lb, int k0, int buf) {
+    const int2 bt = th.hdr[lb];
+    const int n = min(CH, bt.y - k0);
+    for (int j = 0; j < n; ++j) {
+      const size_t i = size_t(bt.x) + size_t(k0 + j) * kBatch + lane;
+      const int e = (buf * CH + j) * 32 + lane;
+      cp_async<sizeof(C)>(st_t + e, frac + i);
+      if (user) cp_async<4>(st_m + e, user + i);
+      if (!unit) cp_async<sizeof(C)>(st_w + e, weight + i);
+    }
+    cp_async_commit();
   };
-  load_F(th.code[lb * kBatch + lane]);
-  C t_next = stream_load(frac + i);
-  int m_next = a.slot_user ? __ldcs(a.slot_user + i) : 0;
-  while (true) {
-    const C t = t_next;
-    const int m = m_next;
-    const size_t i_cur = i;
-    const bool real_slot = k < cnt;  // null slots (past the lane's item) get 0
-    // advance to the next slot of this warp
-    bool new_batch = false;
-    if (k + 1 < bt.y) {
-      ++k;
-      i += kBatch;
+  int ilb = warp, ik0 = 0;  // next chunk to issue
+  issue(ilb, ik0, 0);
+  next_chunk<real>(ilb, ik0, th.hdr, nw);
+  int lb = warp, k0 = 0, buf = 0, cnt = 0;
+  C F[J][J];
+  while (lb < nbt) {
+    if (ilb < nbt) {
+      issue(ilb, ik0, buf ^ 1);
+      next_chunk<real>(ilb, ik0, th.hdr, nw);
     } else {
-      lb += nw;
-      new_batch = true;
-      if (lb < nbt) {
-        bt = th.hdr[lb];
-        k = 0;
-        i = size_t(bt.x) + lane;
-      }
+      cp_async_commit();  // empty group: keeps "all but the newest group" meaning this chunk
     }
-    const bool more = !new_batch || lb < nbt;
-    if (more) {
-      t_next = stream_load(frac + i);
-      if (a.slot_user) m_next = __ldcs(a.slot_user + i);
-    }
-    real ku[J], kv[J];
-    tap_weights<real, J, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
-    tap_weights<real, J, SUB>(poly.v, poly.nsub_v, t.y, kv);
-    real sr = 0, si = 0;
-#pragma unroll
-    for (int jv = 0; jv < J; ++jv) {
-      real rr = 0, ri = 0;
-#pragma unroll
-      for (int ju = 0; ju < J; ++ju) {
-        rr = fma(ku[ju], F[jv][ju].x, rr);
-        ri = fma(ku[ju], F[jv][ju].y, ri);
-      }
-      sr = fma(kv[jv], rr, sr);
-      si = fma(kv[jv], ri, si);
-    }
-    C y;
-    if (unit) {
-      const real sg = copysign(real(1), t.x);
-      y.x = sg * sr;
-      y.y = sg * si;
-    } else {
-      const C w = stream_load(weight + i_cur);
-      y.x = sr * w.x - si * w.y;
-      y.y = sr * w.y + si * w.x;
-    }
-    if (!a.slot_user)
-      out[i_cur] = real_slot ? y : C{0, 0};
-    else if (m >= 0)
-      out[m] = y;
-    if (!more) break;
-    if (new_batch) {
+    const int2 bt = th.hdr[lb];
+    if (k0 == 0) {
+      // new batch: this lane's item and its J x J grid block
       const int code = th.code[lb * kBatch + lane];
       cnt = item_count(code);
-      load_F(code);
+      const int lp = item_lp(code), lq = item_lq(code);
+#pragma unroll
+      for (int jv = 0; jv < J; ++jv)
+#pragma unroll
+        for (int ju = 0; ju < J; ++ju) F[jv][ju] = win[(lp + jv) * WW + lq + ju];
     }
+    cp_async_wait_group<1>();
+    const int n = min(CH, bt.y - k0);
+    for (int j = 0; j < n; ++j) {
+      const int k = k0 + j;
+      const int e = (buf * CH + j) * 32 + lane;
+      const C t = st_t[e];
+      real ku[J], kv[J];
+      tap_weights<real, J, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
+      tap_weights<real, J, SUB>(poly.v, poly.nsub_v, t.y, kv);
+      real sr = 0, si = 0;
+#pragma unroll
+      for (int jv = 0; jv < J; ++jv) {
+        real rr = 0, ri = 0;
+#pragma unroll
+        for (int ju = 0; ju < J; ++ju) {
+          rr = fma(ku[ju], F[jv][ju].x, rr);
+          ri = fma(ku[ju], F[jv][ju].y, ri);
+        }
+        sr = fma(kv[jv], rr, sr);
+        si = fma(kv[jv], ri, si);
+      }
+      C y;
+      if (unit) {
+        const real sg = copysign(real(1), t.x);
+        y.x = sg * sr;
+        y.y = sg * si;
+      } else {
+        const C w = st_w[e];
+        y.x = sr * w.x - si * w.y;
+        y.y = sr * w.y + si * w.x;
+      }
+      // Lanes past their item's end compute on null slots: 0 in slot order,
+      // nothing in caller order.
+      if (!user) {
+        out[size_t(bt.x) + size_t(k) * kBatch + lane] = k < cnt ? y : C{0, 0};
+      } else {
+        const int m = st_m[e];
+        if (m >= 0) out[m] = y;
+      }
+    }
+    buf ^= 1;
+    next_chunk<real>(lb, k0, th.hdr, nw);
   }
+  cp_async_wait_all();
 }
 
 template <typename real, int J, bool SUB, bool GROUP>
 __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
                                                    const __grid_constant__ PolyTable<real> poly) {
   using C = cplx<real>;
+  constexpr int CH = StageDepth<real>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Task tk = a0.tasks[blockIdx.x];
   const auto &a = ArgsOf<real, GROUP>::get(a0, tk.channel);
@@ -273,70 +303,92 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
   const C *frac = static_cast<const C *>(a.frac);
   const C *weight = static_cast<const C *>(a.weight);
   const C *vin = static_cast<const C *>(a.slot_in);
+  const int32_t *user = a.slot_user;
   const bool unit = weight == nullptr;
-  int lb = warp;
-  if (lb < nbt) {
-    int2 bt = th.hdr[lb];
-    int code = th.code[lb * kBatch + lane];
-    int k = 0;
-    size_t i = size_t(bt.x) + lane;
+  if (warp < nbt) {
+    unsigned char *stg = smem_raw + a0.win_bytes + kHeaderBytes + size_t(warp) * a0.stage_bytes;
+    C *st_t = reinterpret_cast<C *>(stg);
+    int *st_m = reinterpret_cast<int *>(stg + 2 * CH * 32 * sizeof(C));
+    // the visibility (slot order) or, with caller order, nothing: it is
+    // gathered through the staged caller index
+    C *st_y = reinterpret_cast<C *>(stg + 2 * CH * 32 * (sizeof(C) + (user ? 4 : 0)));
+    C *st_w = st_y + (user ? 0 : 2 * CH * 32);
+    auto issue = [&](int lb, int k0, int buf) {
+      const int2 bt = th.hdr[lb];
+      const int n = min(CH, bt.y - k0);
+      for (int j = 0; j < n; ++j) {
+        const size_t i = size_t(bt.x) + size_t(k0 + j) * kBatch + lane;
+        const int e = (buf * CH + j) * 32 + lane;
+        cp_async<sizeof(C)>(st_t + e, frac + i);
+        if (user)
+          cp_async<4>(st_m + e, user + i);
+        else
+          cp_async<sizeof(C)>(st_y + e, vin + i);
+        if (!unit) cp_async<sizeof(C)>(st_w + e, weight + i);
+      }
+      cp_async_commit();
+    };
+    int ilb = warp, ik0 = 0;
+    issue(ilb, ik0, 0);
+    next_chunk<real>(ilb, ik0, th.hdr, nw);
+    int lb = warp, k0 = 0, buf = 0;
     C acc[J][J];
 #pragma unroll
     for (int jv = 0; jv < J; ++jv)
 #pragma unroll
       for (int ju = 0; ju < J; ++ju) acc[jv][ju] = C{0, 0};
-    C t_next = stream_load(frac + i);
-    C y_next = read_vis(a, vin, i);
-    while (true) {
-      const C t = t_next;
-      const C yv = y_next;
-      const size_t i_cur = i;
-      bool new_batch = false;
-      if (k + 1 < bt.y) {
-        ++k;
-        i += kBatch;
+    while (lb < nbt) {
+      if (ilb < nbt) {
+        issue(ilb, ik0, buf ^ 1);
+        next_chunk<real>(ilb, ik0, th.hdr, nw);
       } else {
-        new_batch = true;
+        cp_async_commit();
       }
-      int2 bt_next = bt;
-      if (new_batch && lb + nw < nbt) {
-        bt_next = th.hdr[lb + nw];
-        i = size_t(bt_next.x) + lane;
-      }
-      const bool more = !new_batch || lb + nw < nbt;
-      if (more) {
-        t_next = stream_load(frac + i);
-        y_next = read_vis(a, vin, i);
-      }
-      // Null slots hold a zero visibility, so they add nothing.
-      real zr, zi;
-      if (unit) {
-        const real sg = copysign(real(1), t.x);
-        zr = sg * yv.x;
-        zi = sg * yv.y;
-      } else {
-        // conj(weight) * y: G^H holds the conjugated entries of G.
-        const C w = stream_load(weight + i_cur);
-        zr = w.x * yv.x + w.y * yv.y;
-        zi = w.x * yv.y - w.y * yv.x;
-      }
-      real ku[J], kv[J];
-      tap_weights<real, J, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
-      tap_weights<real, J, SUB>(poly.v, poly.nsub_v, t.y, kv);
+      const int2 bt = th.hdr[lb];
+      cp_async_wait_group<1>();
+      const int n = min(CH, bt.y - k0);
+      for (int j = 0; j < n; ++j) {
+        const int e = (buf * CH + j) * 32 + lane;
+        const C t = st_t[e];
+        C yv;
+        if (user) {
+          const int m = st_m[e];
+          yv = m >= 0 ? vin[m] : C{0, 0};
+        } else {
+          yv = st_y[e];
+        }
+        // Null slots hold a zero visibility, so they add nothing.
+        real zr, zi;
+        if (unit) {
+          const real sg = copysign(real(1), t.x);
+          zr = sg * yv.x;
+          zi = sg * yv.y;
+        } else {
+          // conj(weight) * y: G^H holds the conjugated entries of G.
+          const C w = st_w[e];
+          zr = w.x * yv.x + w.y * yv.y;
+          zi = w.x * yv.y - w.y * yv.x;
+        }
+        real ku[J], kv[J];
+        tap_weights<real, J, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
+        tap_weights<real, J, SUB>(poly.v, poly.nsub_v, t.y, kv);
 #pragma unroll
-      for (int jv = 0; jv < J; ++jv) {
-        const real ar = zr * kv[jv], ai = zi * kv[jv];
+        for (int jv = 0; jv < J; ++jv) {
+          const real ar = zr * kv[jv], ai = zi * kv[jv];
 #pragma unroll
-        for (int ju = 0; ju < J; ++ju) {
-          acc[jv][ju].x = fma(ar, ku[ju], acc[jv][ju].x);
-          acc[jv][ju].y = fma(ai, ku[ju], acc[jv][ju].y);
+          for (int ju = 0; ju < J; ++ju) {
+            acc[jv][ju].x = fma(ar, ku[ju], acc[jv][ju].x);
+            acc[jv][ju].y = fma(ai, ku[ju], acc[jv][ju].y);
+          }
         }
       }
-      if (new_batch) {
-        // Flush.  The items of one batch have distinct base cells, so at each
-        // (jv, ju) step the 32 lanes update 32 distinct cells; steps are
-        // ordered by __syncwarp, which makes the summation order a function
-        // of the plan.
+      buf ^= 1;
+      if (k0 + CH >= bt.y) {
+        // Flush at the end of the batch.  The items of one batch have
+        // distinct base cells, so at each (jv, ju) step the 32 lanes update
+        // 32 distinct cells; steps are ordered by __syncwarp, which makes the
+        // summation order a function of the plan.
+        const int code = th.code[lb * kBatch + lane];
         const int cnt = item_count(code);
         const int lp = item_lp(code), lq = item_lq(code);
 #pragma unroll
@@ -353,13 +405,10 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
             acc[jv][ju] = C{0, 0};
             __syncwarp();
           }
-        lb += nw;
-        if (!more) break;
-        bt = bt_next;
-        code = th.code[lb * kBatch + lane];
-        k = 0;
       }
+      next_chunk<real>(lb, k0, th.hdr, nw);
     }
+    cp_async_wait_all();
   }
   __syncthreads();
   const int local_task = GROUP ? int(blockIdx.x) - a0.group_task_base[tk.channel] : int(blockIdx.x);
@@ -445,13 +494,22 @@ __device__ __forceinline__ void fold_tile(const FoldArgs &f, int t) {
   }
 }
 
+// Per-warp staging bytes (see StageDepth): t, then for degrid the caller
+// index if visibilities are written in caller order, for grid the caller
+// index or the slot-ordered visibility, then the weight if there is one.
+inline size_t stage_bytes(int precision_bytes, bool degrid, bool user, bool weight) {
+  const size_t CH = precision_bytes == 8 ? StageDepth<double>::value : StageDepth<float>::value;
+  const size_t c = 2 * size_t(precision_bytes);
+  const size_t per = c + (degrid ? (user ? 4 : 0) : (user ? 4 : c)) + (weight ? c : 0);
+  return 2 * CH * 32 * per;
+}
+
 inline size_t window_bytes(int precision_bytes, int win_rows, int win_cols, const LaunchShape &shape,
                     bool per_warp) {
   const size_t one = size_t(win_rows) * win_cols * 2 * precision_bytes;
   const size_t b = per_warp ? one * size_t(shape.threads / 32) : one;
   return (b + 15) / 16 * 16;
 }
-constexpr size_t kHeaderBytes = kMaxTaskBatches * (sizeof(int2) + kBatch * sizeof(int));
 
 // Dispatch on the support J (templated so the J x J block stays in registers)
 // and on whether the kernel polynomial has sub-segments (narrow kernels, PSWF).

@@ -193,6 +193,20 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
   ntu_ = tu.n;
   ntv_ = tv.n;
   slot_stride_ = int64_t(win_rows_) * win_cols_;
+  if (!wmode_) {
+    // Shared memory of the largest launch this operator makes (windows,
+    // batch headers, per-warp staging in the most demanding layout).
+    int optin = 0;
+    cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_),
+               "cudaDeviceGetAttribute");
+    const size_t need =
+        std::max(degrid_smem_bytes(sizeof(real), J_, win_rows_, win_cols_, shape_, true, true),
+                 grid_smem_bytes(sizeof(real), J_, win_rows_, win_cols_, shape_, true, true));
+    if (need > size_t(optin))
+      throw Error(kUnsupported, "tile / threads / support need " + std::to_string(need) +
+                                    " bytes of shared memory per CTA; the device allows " +
+                                    std::to_string(optin));
+  }
   {
     tile_tasks_.alloc(sizeof(int32_t) * tile_tasks.size(), &bytes);
     tile_tasks_.upload(tile_tasks.data(), sizeof(int32_t) * tile_tasks.size(), stream_);
