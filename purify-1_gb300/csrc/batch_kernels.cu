@@ -124,7 +124,7 @@ cudaError_t launch_degrid_group(const ApplyArgs<real> &a, const PolyTable<real> 
   const size_t smem = degrid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, weight);
   ApplyArgs<real> b = a;
   b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, false));
-  b.stage_bytes = int(stage_bytes(sizeof(real), true, user, weight));
+  b.stage_bytes = int(stage_bytes(sizeof(real), J, user, weight));
   return launch_apply<real, true>(true, b, poly, J, ntasks, smem, shape.threads, s);
 }
 template <typename real>
@@ -134,7 +134,6 @@ cudaError_t launch_grid_group(const ApplyArgs<real> &a, const PolyTable<real> &p
   const size_t smem = grid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, weight);
   ApplyArgs<real> b = a;
   b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, true));
-  b.stage_bytes = int(stage_bytes(sizeof(real), false, user, weight));
   return launch_apply<real, true>(false, b, poly, J, ntasks, smem, shape.threads, s);
 }
 

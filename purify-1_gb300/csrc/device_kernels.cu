@@ -162,15 +162,14 @@ int stream_blocks(int64_t n, int threads) {
 
 }  // namespace
 
-size_t degrid_smem_bytes(int precision_bytes, int, int win_rows, int win_cols,
+size_t degrid_smem_bytes(int precision_bytes, int J, int win_rows, int win_cols,
                          const LaunchShape &shape, bool user, bool weight) {
   return window_bytes(precision_bytes, win_rows, win_cols, shape, false) + kHeaderBytes +
-         size_t(shape.threads / 32) * stage_bytes(precision_bytes, true, user, weight);
+         size_t(shape.threads / 32) * stage_bytes(precision_bytes, J, user, weight);
 }
 size_t grid_smem_bytes(int precision_bytes, int, int win_rows, int win_cols,
-                       const LaunchShape &shape, bool user, bool weight) {
-  return window_bytes(precision_bytes, win_rows, win_cols, shape, true) + kHeaderBytes +
-         size_t(shape.threads / 32) * stage_bytes(precision_bytes, false, user, weight);
+                       const LaunchShape &shape, bool, bool) {
+  return window_bytes(precision_bytes, win_rows, win_cols, shape, true) + kHeaderBytes;
 }
 
 template <typename real>
@@ -181,7 +180,7 @@ cudaError_t launch_degrid(const ApplyArgs<real> &a, const PolyTable<real> &poly,
   const size_t smem = degrid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, weight);
   ApplyArgs<real> b = a;
   b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, false));
-  b.stage_bytes = int(stage_bytes(sizeof(real), true, user, weight));
+  b.stage_bytes = int(stage_bytes(sizeof(real), J, user, weight));
   return launch_apply<real, false>(true, b, poly, J, ntasks, smem, shape.threads, s);
 }
 template <typename real>
@@ -192,7 +191,6 @@ cudaError_t launch_grid(const ApplyArgs<real> &a, const PolyTable<real> &poly, i
   const size_t smem = grid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, weight);
   ApplyArgs<real> b = a;
   b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, true));
-  b.stage_bytes = int(stage_bytes(sizeof(real), false, user, weight));
   return launch_apply<real, false>(false, b, poly, J, ntasks, smem, shape.threads, s);
 }
 

@@ -47,7 +47,8 @@ struct LaunchShape {
 };
 
 // Largest dynamic shared memory a launch of the given shape needs, in bytes:
-// user = visibilities in caller order, weight = a weight stream.
+// user = visibilities in caller order, weight = a weight stream (they size
+// the degrid kernel's staging buffers; the grid kernel has none).
 size_t degrid_smem_bytes(int precision_bytes, int J, int win_rows, int win_cols,
                          const LaunchShape &shape, bool user = true, bool weight = true);
 size_t grid_smem_bytes(int precision_bytes, int J, int win_rows, int win_cols,

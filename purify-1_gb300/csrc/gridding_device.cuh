@@ -118,6 +118,18 @@ __device__ __forceinline__ TaskHeaders load_headers(const A &a, const Task &tk,
   return h;
 }
 
+// Visibility read for the grid kernel: slot order, or caller order through
+// slot_user (0 for null slots).
+template <typename real>
+__device__ __forceinline__ cplx<real> read_vis(const ApplyArgs<real> &a, const cplx<real> *vin,
+                                              size_t i) {
+  if (a.slot_user) {
+    const int m = __ldcs(a.slot_user + i);
+    return m >= 0 ? vin[m] : cplx<real>{0, 0};
+  }
+  return vin[i];
+}
+
 // Operator arguments of a task.  A single-operator launch reads them from the
 // kernel parameters; a grouped launch (several operators in one grid) from
 // the device table at a0.group, indexed by the task's channel.
@@ -134,22 +146,24 @@ struct ArgsOf<real, true> {
   }
 };
 
-// Per-warp staging of the coverage stream.  A warp walks its batches in
-// chunks of up to kStage<real> k-steps; while it computes one chunk, the
-// next chunk's per-slot data (t, and the caller index, weight or visibility
-// as the launch needs) is on its way into shared memory by cp.async, so a
-// whole chunk of loads is in flight per warp instead of one step.  Each lane
-// copies and later reads only its own column, so the per-thread
-// cp.async.wait_group is the only wait.  Layout per warp, each [2][kStage][32]:
-// t, then caller index (int), then the second complex stream.
-template <typename real>
+// Per-warp staging of the degrid kernel's coverage stream.  A warp walks its
+// batches in chunks of up to CH k-steps; while it computes one chunk, the
+// next chunk's per-slot data (t, and the caller index and weight when the
+// launch has them) is on its way into shared memory by cp.async, so a whole
+// chunk of loads is in flight per warp instead of one step.  Each lane copies
+// and later reads only its own column, so the per-thread
+// cp.async.wait_group is the only wait.  Layout per warp, each [2][CH][32]:
+// t, then the caller index (int), then the weight.  The grid kernel does not
+// stage: its per-warp windows already fill shared memory, and staging would
+// cost it resident CTAs.
+template <typename real, int J>
 struct StageDepth {
-  static constexpr int value = 8;
+  static constexpr int value = (J <= 4 ? 4 : 8) / (sizeof(real) == 8 ? 2 : 1);
 };
-template <>
-struct StageDepth<double> {
-  static constexpr int value = 4;
-};
+inline constexpr int stage_depth(int precision_bytes, int J) {
+  return (J <= 4 ? 4 : 8) / (precision_bytes == 8 ? 2 : 1);
+}
+
 __device__ __forceinline__ void cp_async_commit() {
   asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
@@ -158,9 +172,9 @@ __device__ __forceinline__ void cp_async_wait_group() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-template <typename real>
+template <int CH>
 __device__ __forceinline__ void next_chunk(int &lb, int &k0, const int2 *hdr, int nw) {
-  k0 += StageDepth<real>::value;
+  k0 += CH;
   if (k0 >= hdr[lb].y) {
     k0 = 0;
     lb += nw;
@@ -171,7 +185,7 @@ template <typename real, int J, bool SUB, bool GROUP>
 __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
                                                      const __grid_constant__ PolyTable<real> poly) {
   using C = cplx<real>;
-  constexpr int CH = StageDepth<real>::value;
+  constexpr int CH = StageDepth<real, J>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Task tk = a0.tasks[blockIdx.x];
   const auto &a = ArgsOf<real, GROUP>::get(a0, tk.channel);
@@ -216,13 +230,13 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
   };
   int ilb = warp, ik0 = 0;  // next chunk to issue
   issue(ilb, ik0, 0);
-  next_chunk<real>(ilb, ik0, th.hdr, nw);
+  next_chunk<CH>(ilb, ik0, th.hdr, nw);
   int lb = warp, k0 = 0, buf = 0, cnt = 0;
   C F[J][J];
   while (lb < nbt) {
     if (ilb < nbt) {
       issue(ilb, ik0, buf ^ 1);
-      next_chunk<real>(ilb, ik0, th.hdr, nw);
+      next_chunk<CH>(ilb, ik0, th.hdr, nw);
     } else {
       cp_async_commit();  // empty group: keeps "all but the newest group" meaning this chunk
     }
@@ -278,7 +292,7 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
       }
     }
     buf ^= 1;
-    next_chunk<real>(lb, k0, th.hdr, nw);
+    next_chunk<CH>(lb, k0, th.hdr, nw);
   }
   cp_async_wait_all();
 }
@@ -287,7 +301,6 @@ template <typename real, int J, bool SUB, bool GROUP>
 __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
                                                    const __grid_constant__ PolyTable<real> poly) {
   using C = cplx<real>;
-  constexpr int CH = StageDepth<real>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Task tk = a0.tasks[blockIdx.x];
   const auto &a = ArgsOf<real, GROUP>::get(a0, tk.channel);
@@ -303,92 +316,75 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
   const C *frac = static_cast<const C *>(a.frac);
   const C *weight = static_cast<const C *>(a.weight);
   const C *vin = static_cast<const C *>(a.slot_in);
-  const int32_t *user = a.slot_user;
   const bool unit = weight == nullptr;
   if (warp < nbt) {
-    unsigned char *stg = smem_raw + a0.win_bytes + kHeaderBytes + size_t(warp) * a0.stage_bytes;
-    C *st_t = reinterpret_cast<C *>(stg);
-    int *st_m = reinterpret_cast<int *>(stg + 2 * CH * 32 * sizeof(C));
-    // the visibility (slot order) or, with caller order, nothing: it is
-    // gathered through the staged caller index
-    C *st_y = reinterpret_cast<C *>(stg + 2 * CH * 32 * (sizeof(C) + (user ? 4 : 0)));
-    C *st_w = st_y + (user ? 0 : 2 * CH * 32);
-    auto issue = [&](int lb, int k0, int buf) {
-      const int2 bt = th.hdr[lb];
-      const int n = min(CH, bt.y - k0);
-      for (int j = 0; j < n; ++j) {
-        const size_t i = size_t(bt.x) + size_t(k0 + j) * kBatch + lane;
-        const int e = (buf * CH + j) * 32 + lane;
-        cp_async<sizeof(C)>(st_t + e, frac + i);
-        if (user)
-          cp_async<4>(st_m + e, user + i);
-        else
-          cp_async<sizeof(C)>(st_y + e, vin + i);
-        if (!unit) cp_async<sizeof(C)>(st_w + e, weight + i);
+    // Two cursors over this warp's (batch, k) steps, slot = hdr[lb].x +
+    // 32 k + lane: the compute cursor and, two steps ahead of it, the
+    // prefetch cursor, so two steps of coverage loads are in flight.
+    int clb = warp, ck = 0;
+    int plb = warp, pk = 0;
+    auto adv = [&](int &lb, int &k) {
+      if (k + 1 < th.hdr[lb].y) {
+        ++k;
+      } else {
+        k = 0;
+        lb += nw;
       }
-      cp_async_commit();
     };
-    int ilb = warp, ik0 = 0;
-    issue(ilb, ik0, 0);
-    next_chunk<real>(ilb, ik0, th.hdr, nw);
-    int lb = warp, k0 = 0, buf = 0;
+    auto slot = [&](int lb, int k) { return size_t(th.hdr[lb].x) + size_t(k) * kBatch + lane; };
+    C t0 = stream_load(frac + slot(plb, pk)), y0 = read_vis(a, vin, slot(plb, pk));
+    adv(plb, pk);
+    C t1{0, 0}, y1{0, 0};
+    if (plb < nbt) {
+      t1 = stream_load(frac + slot(plb, pk));
+      y1 = read_vis(a, vin, slot(plb, pk));
+      adv(plb, pk);
+    }
     C acc[J][J];
 #pragma unroll
     for (int jv = 0; jv < J; ++jv)
 #pragma unroll
       for (int ju = 0; ju < J; ++ju) acc[jv][ju] = C{0, 0};
-    while (lb < nbt) {
-      if (ilb < nbt) {
-        issue(ilb, ik0, buf ^ 1);
-        next_chunk<real>(ilb, ik0, th.hdr, nw);
+    while (clb < nbt) {
+      const C t = t0, yv = y0;
+      const size_t i_cur = slot(clb, ck);
+      t0 = t1;
+      y0 = y1;
+      if (plb < nbt) {
+        t1 = stream_load(frac + slot(plb, pk));
+        y1 = read_vis(a, vin, slot(plb, pk));
+        adv(plb, pk);
+      }
+      // Null slots hold a zero visibility, so they add nothing.
+      real zr, zi;
+      if (unit) {
+        const real sg = copysign(real(1), t.x);
+        zr = sg * yv.x;
+        zi = sg * yv.y;
       } else {
-        cp_async_commit();
+        // conj(weight) * y: G^H holds the conjugated entries of G.
+        const C w = stream_load(weight + i_cur);
+        zr = w.x * yv.x + w.y * yv.y;
+        zi = w.x * yv.y - w.y * yv.x;
       }
-      const int2 bt = th.hdr[lb];
-      cp_async_wait_group<1>();
-      const int n = min(CH, bt.y - k0);
-      for (int j = 0; j < n; ++j) {
-        const int e = (buf * CH + j) * 32 + lane;
-        const C t = st_t[e];
-        C yv;
-        if (user) {
-          const int m = st_m[e];
-          yv = m >= 0 ? vin[m] : C{0, 0};
-        } else {
-          yv = st_y[e];
-        }
-        // Null slots hold a zero visibility, so they add nothing.
-        real zr, zi;
-        if (unit) {
-          const real sg = copysign(real(1), t.x);
-          zr = sg * yv.x;
-          zi = sg * yv.y;
-        } else {
-          // conj(weight) * y: G^H holds the conjugated entries of G.
-          const C w = st_w[e];
-          zr = w.x * yv.x + w.y * yv.y;
-          zi = w.x * yv.y - w.y * yv.x;
-        }
-        real ku[J], kv[J];
-        tap_weights<real, J, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
-        tap_weights<real, J, SUB>(poly.v, poly.nsub_v, t.y, kv);
+      real ku[J], kv[J];
+      tap_weights<real, J, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
+      tap_weights<real, J, SUB>(poly.v, poly.nsub_v, t.y, kv);
 #pragma unroll
-        for (int jv = 0; jv < J; ++jv) {
-          const real ar = zr * kv[jv], ai = zi * kv[jv];
+      for (int jv = 0; jv < J; ++jv) {
+        const real ar = zr * kv[jv], ai = zi * kv[jv];
 #pragma unroll
-          for (int ju = 0; ju < J; ++ju) {
-            acc[jv][ju].x = fma(ar, ku[ju], acc[jv][ju].x);
-            acc[jv][ju].y = fma(ai, ku[ju], acc[jv][ju].y);
-          }
+        for (int ju = 0; ju < J; ++ju) {
+          acc[jv][ju].x = fma(ar, ku[ju], acc[jv][ju].x);
+          acc[jv][ju].y = fma(ai, ku[ju], acc[jv][ju].y);
         }
       }
-      buf ^= 1;
-      if (k0 + CH >= bt.y) {
+      if (ck + 1 >= th.hdr[clb].y) {
         // Flush at the end of the batch.  The items of one batch have
         // distinct base cells, so at each (jv, ju) step the 32 lanes update
         // 32 distinct cells; steps are ordered by __syncwarp, which makes the
         // summation order a function of the plan.
-        const int code = th.code[lb * kBatch + lane];
+        const int code = th.code[clb * kBatch + lane];
         const int cnt = item_count(code);
         const int lp = item_lp(code), lq = item_lq(code);
 #pragma unroll
@@ -406,9 +402,8 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
             __syncwarp();
           }
       }
-      next_chunk<real>(lb, k0, th.hdr, nw);
+      adv(clb, ck);
     }
-    cp_async_wait_all();
   }
   __syncthreads();
   const int local_task = GROUP ? int(blockIdx.x) - a0.group_task_base[tk.channel] : int(blockIdx.x);
@@ -494,14 +489,13 @@ __device__ __forceinline__ void fold_tile(const FoldArgs &f, int t) {
   }
 }
 
-// Per-warp staging bytes (see StageDepth): t, then for degrid the caller
-// index if visibilities are written in caller order, for grid the caller
-// index or the slot-ordered visibility, then the weight if there is one.
-inline size_t stage_bytes(int precision_bytes, bool degrid, bool user, bool weight) {
-  const size_t CH = precision_bytes == 8 ? StageDepth<double>::value : StageDepth<float>::value;
+// Per-warp staging bytes of the degrid kernel (see StageDepth): t, the caller
+// index if visibilities are written in caller order, the weight if there is
+// one.
+inline size_t stage_bytes(int precision_bytes, int J, bool user, bool weight) {
+  const size_t CH = size_t(stage_depth(precision_bytes, J));
   const size_t c = 2 * size_t(precision_bytes);
-  const size_t per = c + (degrid ? (user ? 4 : 0) : (user ? 4 : c)) + (weight ? c : 0);
-  return 2 * CH * 32 * per;
+  return 2 * CH * 32 * (c + (user ? 4 : 0) + (weight ? c : 0));
 }
 
 inline size_t window_bytes(int precision_bytes, int win_rows, int win_cols, const LaunchShape &shape,
