@@ -25,22 +25,46 @@ namespace pg {
 namespace {
 using namespace dev;
 
+// The permutations are random 8-byte gathers: each thread keeps four of them
+// in flight (indices first, then the gathered values), which is what bounds
+// them, not instructions.
+constexpr int kPermUnroll = 4;
 template <typename real>
 __global__ void compact_kernel(const cplx<real> *__restrict__ slots,
                                const int32_t *__restrict__ user_slot,
                                cplx<real> *__restrict__ out, int64_t M) {
-  for (int64_t m = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; m < M;
-       m += int64_t(gridDim.x) * blockDim.x)
-    __stcs(out + m, slots[__ldcs(user_slot + m)]);
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t m0 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; m0 < M;
+       m0 += kPermUnroll * stride) {
+    int32_t src[kPermUnroll];
+    cplx<real> v[kPermUnroll];
+#pragma unroll
+    for (int r = 0; r < kPermUnroll; ++r)
+      src[r] = m0 + r * stride < M ? __ldcs(user_slot + m0 + r * stride) : -1;
+#pragma unroll
+    for (int r = 0; r < kPermUnroll; ++r) v[r] = src[r] >= 0 ? slots[src[r]] : cplx<real>{0, 0};
+#pragma unroll
+    for (int r = 0; r < kPermUnroll; ++r)
+      if (m0 + r * stride < M) __stcs(out + m0 + r * stride, v[r]);
+  }
 }
 template <typename real>
 __global__ void expand_kernel(const cplx<real> *__restrict__ in,
                               const int32_t *__restrict__ slot_user,
                               cplx<real> *__restrict__ slots, int64_t S) {
-  for (int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; s < S;
-       s += int64_t(gridDim.x) * blockDim.x) {
-    const int32_t m = __ldcs(slot_user + s);
-    slots[s] = m >= 0 ? in[m] : cplx<real>{0, 0};
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t s0 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; s0 < S;
+       s0 += kPermUnroll * stride) {
+    int32_t m[kPermUnroll];
+    cplx<real> v[kPermUnroll];
+#pragma unroll
+    for (int r = 0; r < kPermUnroll; ++r)
+      m[r] = s0 + r * stride < S ? __ldcs(slot_user + s0 + r * stride) : -1;
+#pragma unroll
+    for (int r = 0; r < kPermUnroll; ++r) v[r] = m[r] >= 0 ? in[m[r]] : cplx<real>{0, 0};
+#pragma unroll
+    for (int r = 0; r < kPermUnroll; ++r)
+      if (s0 + r * stride < S) slots[s0 + r * stride] = v[r];
   }
 }
 
