@@ -65,7 +65,7 @@ class BatchT final : public Batch {
   struct Chan {
     int Nx = 0, Ny = 0, Nu = 0, Nv = 0, x0 = 0, y0 = 0;
     int64_t M = 0, S = 0, slot_stride = 0;
-    int ntasks = 0, ntu = 0, ntv = 0, win_rows = 0, win_cols = 0;
+    int ntasks = 0, ntu = 0, ntv = 0, win_rows = 0, win_cols = 0, win_stride = 0;
     int group = 0, in_group = 0;
     bool unit = true;
     double norm = 1.0;
@@ -198,6 +198,7 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     ch.ntv = plan.tv.n;
     ch.win_rows = plan.win_rows;
     ch.win_cols = plan.win_cols;
+    ch.win_stride = plan.win_stride;
     ch.slot_stride = int64_t(plan.win_rows) * plan.win_cols;
     for (Task tk : plan.tasks) {
       tk.channel = c;
@@ -339,6 +340,7 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     a.weight = ch.unit ? nullptr : m.at<char>(ch.o_weight);
     a.Nu = ch.Nu;
     a.Nv = ch.Nv;
+    a.win_stride = ch.win_stride;
     a.slot_stride = ch.slot_stride;
     // forward: degrid straight into the caller-ordered visibilities
     fwd_[c] = a;

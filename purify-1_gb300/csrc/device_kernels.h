@@ -29,6 +29,7 @@ struct ApplyArgs {
   // slot_in then point at caller-ordered M-vectors.
   const int32_t *slot_user = nullptr;
   int Nu = 0, Nv = 0;
+  int win_stride = 0;               // row stride of the shared-memory windows (plan's win_stride)
   int64_t slot_stride = 0;          // complex elements per tilebuf slot
   int win_bytes = 0;    // set by the launchers: shared bytes before the batch headers
   int stage_bytes = 0;  // set by the launchers: per-warp staging stride

@@ -189,7 +189,8 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Task tk = a0.tasks[blockIdx.x];
   const auto &a = ArgsOf<real, GROUP>::get(a0, tk.channel);
-  const int WW = tk.W + J - 1, WH = tk.H + J - 1;
+  // the window in shared memory: WH rows of WW cells at row stride WS
+  const int WW = tk.W + J - 1, WH = tk.H + J - 1, WS = a.win_stride;
   C *win = reinterpret_cast<C *>(smem_raw);
   const TaskHeaders th = load_headers(a, tk, smem_raw + a0.win_bytes);
   const C *grid = static_cast<const C *>(a.grid);
@@ -200,7 +201,7 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
     if (p >= a.Nv) p -= a.Nv;
     int q = tk.Q + lq;
     if (q >= a.Nu) q -= a.Nu;
-    cp_async<sizeof(C)>(win + idx, grid + size_t(p) * a.Nu + q);
+    cp_async<sizeof(C)>(win + lp * WS + lq, grid + size_t(p) * a.Nu + q);
   }
   cp_async_wait_all();
   __syncthreads();
@@ -249,7 +250,7 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
 #pragma unroll
       for (int jv = 0; jv < J; ++jv)
 #pragma unroll
-        for (int ju = 0; ju < J; ++ju) F[jv][ju] = win[(lp + jv) * WW + lq + ju];
+        for (int ju = 0; ju < J; ++ju) F[jv][ju] = win[(lp + jv) * WS + lq + ju];
     }
     cp_async_wait_group<1>();
     const int n = min(CH, bt.y - k0);
@@ -304,7 +305,9 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Task tk = a0.tasks[blockIdx.x];
   const auto &a = ArgsOf<real, GROUP>::get(a0, tk.channel);
-  const int WW = tk.W + J - 1, WH = tk.H + J - 1, WN = WW * WH;
+  // warp windows in shared memory: WH rows at row stride WS (WN cells each);
+  // the task window written out is WH x WW, packed
+  const int WW = tk.W + J - 1, WH = tk.H + J - 1, WS = a.win_stride, WN = WS * WH;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   C *wins = reinterpret_cast<C *>(smem_raw);
   const TaskHeaders th = load_headers(a, tk, smem_raw + a0.win_bytes);
@@ -392,7 +395,7 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
 #pragma unroll
           for (int ju = 0; ju < J; ++ju) {
             if (cnt > 0) {
-              C *cell = mine + (lp + jv) * WW + lq + ju;
+              C *cell = mine + (lp + jv) * WS + lq + ju;
               C c = *cell;
               c.x += acc[jv][ju].x;
               c.y += acc[jv][ju].y;
@@ -408,10 +411,11 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
   __syncthreads();
   const int local_task = GROUP ? int(blockIdx.x) - a0.group_task_base[tk.channel] : int(blockIdx.x);
   C *out = static_cast<C *>(a.tilebuf) + size_t(local_task) * a.slot_stride;
-  for (int idx = threadIdx.x; idx < WN; idx += blockDim.x) {
-    C s = wins[idx];
+  for (int idx = threadIdx.x; idx < WW * WH; idx += blockDim.x) {
+    const int lp = idx / WW, e = idx + lp * (WS - WW);
+    C s = wins[e];
     for (int w = 1; w < nw; ++w) {
-      const C o = wins[w * WN + idx];
+      const C o = wins[w * WN + e];
       s.x += o.x;
       s.y += o.y;
     }

@@ -106,7 +106,7 @@ class OperatorT final : public Operator {
   std::vector<real> su_scaled_, sv_real_;
   PolyTable<real> poly_{};
   LaunchShape shape_;
-  int ntasks_ = 0, win_rows_ = 0, win_cols_ = 0, ntu_ = 0, ntv_ = 0;
+  int ntasks_ = 0, win_rows_ = 0, win_cols_ = 0, win_stride_ = 0, ntu_ = 0, ntv_ = 0;
   int64_t slot_stride_ = 0;
 
   cudaStream_t stream_ = nullptr;
@@ -297,6 +297,7 @@ void OperatorT<real>::init_plain(const OperatorConfig &cfg, int64_t &bytes, Axis
   ntasks_ = int(plan.tasks.size());
   win_rows_ = plan.win_rows;
   win_cols_ = plan.win_cols;
+  win_stride_ = plan.win_stride;
   fold_J_ = J_;
   S_ = plan.S;
   unit_weights_ = plan.unit_weights;
@@ -487,6 +488,7 @@ void OperatorT<real>::degrid_slots(const void *grid, void *caller_vis) {
   a.slot_user = caller_vis ? slot_user_.as<int32_t>() : nullptr;
   a.Nu = Nu_;
   a.Nv = Nv_;
+  a.win_stride = win_stride_;
   mark_begin(kDegrid);
   cuda_check(launch_degrid<real>(a, poly_, J_, ntasks_, win_rows_, win_cols_, shape_, ws_->stream),
              "degrid");
@@ -535,6 +537,7 @@ void OperatorT<real>::grid_core(void *grid, const void *vis, const int32_t *slot
   a.slot_user = slot_user;
   a.Nu = Nu_;
   a.Nv = Nv_;
+  a.win_stride = win_stride_;
   a.slot_stride = slot_stride_;
   mark_begin(kGrid);
   cuda_check(launch_grid<real>(a, poly_, J_, ntasks_, win_rows_, win_cols_, shape_, ws_->stream),

@@ -69,6 +69,10 @@ Plan build_plan(const PlanRequest &rq) {
       throw std::invalid_argument("grid height is too small for the kernel support");
 
   const int ntu = P.tu.n, ntv = P.tv.n, ntiles = ntu * ntv;
+  // Row stride of the tasks' shared-memory windows: the widest window.
+  int WS = 0;
+  for (int b = 0; b < ntu; ++b) WS = std::max(WS, P.tu.start[b + 1] - P.tu.start[b] + rq.Ju - 1);
+  P.win_stride = WS;
   // Cell rank: tiles in row-major order, cells row-major inside a tile.
   std::vector<int64_t> tile_cell0(ntiles + 1, 0);
   for (int a = 0; a < ntv; ++a)
@@ -153,30 +157,46 @@ Plan build_plan(const PlanRequest &rq) {
                        [](const Item &x, const Item &y) { return x.count > y.count; });
       // Greedy packing: scan the pending items in order and take one unless
       // its base cell is already in the batch; the scan gives up 256 clashes
-      // past the first pending item.
+      // past the first pending item.  Lanes are chosen by bank class: an
+      // item whose window offset lp * WS + lq is r (mod 16) goes to lane r or
+      // 16 + r when free, so the lanes of a half-warp mostly touch distinct
+      // 8-byte bank pairs at every (jv, ju) offset of their blocks; otherwise
+      // it takes the first free lane (which items form a batch does not
+      // depend on the lanes).
       stamp.assign(size_t(h) * w, -1);
       taken.assign(items.size(), 0);
       size_t front = 0;
       int32_t batch_id = 0;
       const int64_t task_batch0 = int64_t(P.batch_base.size());
-      std::vector<size_t> lanes;
+      std::vector<int64_t> lane_item(kBatch);
       while (true) {
         while (front < items.size() && taken[front]) ++front;
         if (front == items.size()) break;
-        lanes.clear();
+        std::fill(lane_item.begin(), lane_item.end(), -1);
+        int filled = 0;
         size_t skipped = 0;
-        for (size_t k = front; k < items.size() && lanes.size() < size_t(kBatch); ++k) {
+        for (size_t k = front; k < items.size() && filled < kBatch; ++k) {
           if (taken[k]) continue;
-          if (stamp[items[k].cell] == batch_id) {
+          const int r = (items[k].lp * WS + items[k].lq) & 15;
+          int lane = lane_item[r] < 0 ? r : (lane_item[16 + r] < 0 ? 16 + r : -1);
+          if (lane < 0)
+            for (int l = 0; l < kBatch; ++l)
+              if (lane_item[l] < 0) {
+                lane = l;
+                break;
+              }
+          if (stamp[items[k].cell] == batch_id || lane < 0) {
             if (++skipped > 256) break;
             continue;
           }
           stamp[items[k].cell] = batch_id;
           taken[k] = 1;
-          lanes.push_back(k);
+          lane_item[lane] = int64_t(k);
+          ++filled;
         }
         int kmax = 0;
-        for (size_t k : lanes) kmax = std::max(kmax, int(items[k].count));
+        for (int l = 0; l < kBatch; ++l)
+          if (lane_item[l] >= 0) kmax = std::max(kmax, int(items[lane_item[l]].count));
         const int64_t base = P.S;
         P.batch_base.push_back(int32_t(base));
         P.batch_kmax.push_back(kmax);
@@ -184,8 +204,8 @@ Plan build_plan(const PlanRequest &rq) {
         if (P.S > int64_t(INT32_MAX)) throw std::invalid_argument("too many slots");
         slot_sorted.resize(P.S, -1);
         for (int l = 0; l < kBatch; ++l) {
-          if (l < int(lanes.size())) {
-            const Item &it = items[lanes[l]];
+          if (lane_item[l] >= 0) {
+            const Item &it = items[lane_item[l]];
             P.lane_code.push_back(item_pack(it.lp, it.lq, it.count));
             for (int k = 0; k < it.count; ++k)
               slot_sorted[base + int64_t(kBatch) * k + l] = it.first + k;

@@ -3,7 +3,9 @@
 //
 // Visibilities are sorted by uv tile and base cell, grouped into work items
 // (one base cell, up to K visibilities) and packed into batches of 32 items,
-// one item per lane, no two items of a batch on the same base cell.  Each
+// one item per lane, no two items of a batch on the same base cell, items on
+// the lanes of their shared-memory bank classes where free (see
+// Plan::win_stride).  Each
 // batch owns 32 * kmax consecutive "slots" (kmax = its largest item): lane l's
 // k-th visibility sits in slot base + 32 k + l, so a warp that walks k reads
 // 256 contiguous bytes per access and every lane runs the same loop.  Lanes
@@ -58,6 +60,9 @@ struct Plan {
   std::vector<Task> tasks;
   std::vector<int32_t> tile_tasks;  // ntiles + 1 offsets into tasks
   int win_rows = 0, win_cols = 0;   // largest window: (H + Jv - 1) x (W + Ju - 1)
+  // Row stride of the windows in shared memory (the widest window); a batch's
+  // lane l preferably holds an item with (lp * win_stride + lq) mod 16 == l mod 16.
+  int win_stride = 0;
   // statistics
   int64_t occupied_cells = 0;
   int64_t real_items = 0;

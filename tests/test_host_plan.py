@@ -154,3 +154,20 @@ def test_plan_balances_dense_cells(pg):
     counts = (p.lane_code >> 16) & 0xFFFF
     assert counts.sum() == 5000 and counts.max() <= 16
     assert (p.slot_user >= 0).sum() == 5000
+
+
+def test_batch_lanes_are_bank_classes(pg):
+    """Items sit on the lane of their bank class (window offset lp * stride +
+    lq = lane, mod 16) wherever that lane was free, so half-warps mostly touch
+    distinct shared-memory bank pairs at each tap offset; the stride is the
+    widest window.  Which items form a batch does not depend on the lanes."""
+    from purify_gb300 import synthetic
+    u, v = synthetic.mixed_uv(200_000, 512, 512, 0.7, 0.15, seed=3)
+    p = pg.CoveragePlan(u, v, 512, 512, 6)
+    lc = p.lane_code
+    lp, lq, cnt = lc & 0xFF, (lc >> 8) & 0xFF, lc >> 16
+    r = (lp * p.win_cols + lq) & 15
+    lane = np.arange(32)[None, :] & 15
+    on_class = ((r == lane) & (cnt > 0)).sum() / (cnt > 0).sum()
+    assert on_class > 0.6
+    assert (cnt > 0).mean() > 0.9
