@@ -140,7 +140,7 @@ cudaError_t launch_grid_group(const ApplyArgs<real> &a, const PolyTable<real> &p
 template <typename real>
 cudaError_t launch_fold_group(const FoldArgs *folds, int nch, int max_tiles, cudaStream_t s) {
   if (nch == 0 || max_tiles == 0) return cudaSuccess;
-  fold_group_kernel<real><<<dim3(max_tiles, nch), 256, 0, s>>>(folds);
+  fold_group_kernel<real><<<dim3(max_tiles, nch), dim3(32, 8), 0, s>>>(folds);
   return cudaGetLastError();
 }
 template <typename real>

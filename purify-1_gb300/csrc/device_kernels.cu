@@ -220,7 +220,7 @@ cudaError_t launch_grid(const ApplyArgs<real> &a, const PolyTable<real> &poly, i
 
 template <typename real>
 cudaError_t launch_fold(const FoldArgs &f, cudaStream_t s) {
-  fold_kernel<real><<<f.ntu * f.ntv, 256, 0, s>>>(f);
+  fold_kernel<real><<<f.ntu * f.ntv, dim3(32, 8), 0, s>>>(f);
   return cudaGetLastError();
 }
 

@@ -429,66 +429,62 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
 template <typename real>
 __device__ __forceinline__ void fold_tile(const FoldArgs &f, int t) {
   using C = cplx<real>;
-  const int a = t / f.ntu, b = t - (t / f.ntu) * f.ntu;
+  // Launched with 32 x 8 threads: x walks the columns, y the rows of the tile.
+  const int a = t / f.ntu, b = t - a * f.ntu;
   const int a2 = a == 0 ? f.ntv - 1 : a - 1;
   const int b2 = b == 0 ? f.ntu - 1 : b - 1;
-  const int P = f.tv_start[a], Q = f.tu_start[b];
-  const int H = f.tv_start[a + 1] - P, W = f.tu_start[b + 1] - Q;
-  const int Hu = f.tv_start[a2 + 1] - f.tv_start[a2];  // height of the tile above
-  const int Wl = f.tu_start[b2 + 1] - f.tu_start[b2];  // width of the tile to the left
-  const int WWo = W + f.Ju - 1, WWl = Wl + f.Ju - 1;
   const int tu = a2 * f.ntu + b, tl = a * f.ntu + b2, td = a2 * f.ntu + b2;
+  // independent broadcast loads of the tile's metadata
+  const int P = f.tv_start[a], P1 = f.tv_start[a + 1], Q = f.tu_start[b], Q1 = f.tu_start[b + 1];
+  const int Pu = f.tv_start[a2], Pu1 = f.tv_start[a2 + 1];
+  const int Ql = f.tu_start[b2], Ql1 = f.tu_start[b2 + 1];
   const int own0 = f.tile_tasks[t], own1 = f.tile_tasks[t + 1];
   const int up0 = f.tile_tasks[tu], up1 = f.tile_tasks[tu + 1];
   const int lf0 = f.tile_tasks[tl], lf1 = f.tile_tasks[tl + 1];
   const int dg0 = f.tile_tasks[td], dg1 = f.tile_tasks[td + 1];
+  const int H = P1 - P, W = Q1 - Q, Hu = Pu1 - Pu, Wl = Ql1 - Ql;
+  const int WWo = W + f.Ju - 1, WWl = Wl + f.Ju - 1;
+  const int64_t ss = f.slot_stride;
   const C *__restrict__ buf = static_cast<const C *>(f.tilebuf);
   C *__restrict__ grid = static_cast<C *>(f.grid);
-  auto cell_sum = [&](int idx) {
-    const int lp = idx / W, lq = idx - lp * W;
-    C s{0, 0};
-    for (int k = own0; k < own1; ++k) {
-      const C v = buf[size_t(k) * f.slot_stride + lp * WWo + lq];
-      s.x += v.x;
-      s.y += v.y;
-    }
-    const bool up = lp < f.Jv - 1, left = lq < f.Ju - 1;
-    if (up)
-      for (int k = up0; k < up1; ++k) {
-        const C v = buf[size_t(k) * f.slot_stride + (lp + Hu) * WWo + lq];
+  for (int lp = threadIdx.y; lp < H; lp += blockDim.y) {
+    const bool up = lp < f.Jv - 1;  // uniform across a warp (one row)
+    for (int lq = threadIdx.x; lq < W; lq += blockDim.x) {
+      // own tile's task windows, then the halos of the tiles above, to the
+      // left and above-left, each in task order
+      C s{0, 0};
+      const C *p = buf + own0 * ss + lp * WWo + lq;
+      for (int k = own0; k < own1; ++k, p += ss) {
+        const C v = *p;
         s.x += v.x;
         s.y += v.y;
       }
-    if (left)
-      for (int k = lf0; k < lf1; ++k) {
-        const C v = buf[size_t(k) * f.slot_stride + lp * WWl + lq + Wl];
-        s.x += v.x;
-        s.y += v.y;
+      const bool left = lq < f.Ju - 1;
+      if (up) {
+        p = buf + up0 * ss + (lp + Hu) * WWo + lq;
+        for (int k = up0; k < up1; ++k, p += ss) {
+          const C v = *p;
+          s.x += v.x;
+          s.y += v.y;
+        }
       }
-    if (up && left)
-      for (int k = dg0; k < dg1; ++k) {
-        const C v = buf[size_t(k) * f.slot_stride + (lp + Hu) * WWl + lq + Wl];
-        s.x += v.x;
-        s.y += v.y;
+      if (left) {
+        p = buf + lf0 * ss + lp * WWl + lq + Wl;
+        for (int k = lf0; k < lf1; ++k, p += ss) {
+          const C v = *p;
+          s.x += v.x;
+          s.y += v.y;
+        }
       }
-    return s;
-  };
-  // Four cells per thread per round, loads first, so their latencies overlap.
-  constexpr int R = 4;
-  for (int base = threadIdx.x; base < H * W; base += R * blockDim.x) {
-    C s[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const int idx = base + r * blockDim.x;
-      if (idx < H * W) s[r] = cell_sum(idx);
-    }
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const int idx = base + r * blockDim.x;
-      if (idx < H * W) {
-        const int lp = idx / W, lq = idx - lp * W;
-        grid[size_t(P + lp) * f.Nu + Q + lq] = s[r];
+      if (up && left) {
+        p = buf + dg0 * ss + (lp + Hu) * WWl + lq + Wl;
+        for (int k = dg0; k < dg1; ++k, p += ss) {
+          const C v = *p;
+          s.x += v.x;
+          s.y += v.y;
+        }
       }
+      grid[size_t(P + lp) * f.Nu + Q + lq] = s;
     }
   }
 }
