@@ -62,7 +62,15 @@ def parse():
                    help="power-method rounds for the norm before timing (0: norm 1)")
     p.add_argument("--threads", type=int, default=0, help="CTA threads (tuning)")
     p.add_argument("--max-per-item", type=int, default=0)
+    p.add_argument("--tile", type=int, default=0, help="uv tile edge (tuning)")
     return p.parse_args()
+
+
+def tuning_of(args):
+    """Tuning dict of the --threads / --max-per-item / --tile flags (None: defaults)."""
+    t = {k: v for k, v in (("threads", args.threads), ("max_per_item", args.max_per_item),
+                           ("tile", args.tile)) if v}
+    return t or None
 
 
 def dist_env():
@@ -240,7 +248,8 @@ def run_gb300(args):
     kw = dict(imsizey=n, imsizex=n, oversample_ratio=2.0, kernel="kb", Ju=args.J, Jv=args.J,
               device=local)
     t0 = time.perf_counter()
-    op = pgb.MeasurementOperator(u, v, None, None, power_iters=0, precision="fp32", **kw)
+    op = pgb.MeasurementOperator(u, v, None, None, power_iters=0, precision="fp32",
+                                 tuning=tuning_of(args), **kw)
     t_create = time.perf_counter() - t0
     t0 = time.perf_counter()
     norm = op.power_method(args.power_iters, 1e-4) if args.power_iters > 0 else 1.0
@@ -333,7 +342,8 @@ def run_gb300(args):
 
     # FP32 vs FP64 GPU, same coverage and norm
     if not args.no_fp64:
-        op64 = pgb.MeasurementOperator(u, v, None, None, power_iters=0, precision="fp64", **kw)
+        op64 = pgb.MeasurementOperator(u, v, None, None, power_iters=0, precision="fp64",
+                                       tuning=tuning_of(args), **kw)
         op64.set_norm(norm)
         x64 = torch.from_numpy(x).to(dev)
         y64 = torch.empty(M, dtype=torch.complex128, device=dev)
@@ -445,7 +455,7 @@ def run_wproj(args):
               w_term=True, Jw=6, cellx=c["cellx"], celly=c["celly"], jw_rows=c["jw_rows"])
     t0 = time.perf_counter()
     op = pgb.MeasurementOperator(c["u"], c["v"], c["w"], None, power_iters=0, precision="fp32",
-                                 **kw)
+                                 tuning=tuning_of(args), **kw)
     t_create = time.perf_counter() - t0
     norm = op.power_method(args.power_iters, 1e-4) if args.power_iters > 0 else 1.0
     info = op.info()

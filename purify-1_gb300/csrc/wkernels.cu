@@ -2,7 +2,8 @@
 // kernel row per visibility).  Row m's S x S taps are rebuilt on the fly from
 // its stored rank-3 factors, K = A_0 B_0^T + A_1 B_1^T + A_2 B_2^T
 // (wplan.h).  One warp handles one visibility at a time; lane l covers row
-// r = l / S of each group of R = 32 / S rows and column c = l % S.
+// r = l / S of each group of R = 32 / S rows and column c = l % S, two row
+// groups per step.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -48,12 +49,47 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
-// Stages the 6 S factors of a row into the warp's buffer.
-template <typename C>
-__device__ __forceinline__ void stage_factors(const C *src, C *buf, int S, int lane) {
-  for (int k = lane; k < 6 * S; k += 32) buf[k] = src[k];
-  __syncwarp();
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
+__device__ __forceinline__ void cp_async_wait_one() {
+  asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+}
+
+// Per-warp software pipeline over the visibilities i = first, first + nw, ...
+// of a task: while visibility i is computed, the row factors of the next one
+// are on their way into the other half of the warp's factor buffer
+// (cp.async), and the code, factor offset, weight and visibility of the one
+// after that are being loaded into registers.
+template <typename real>
+struct WPipe {
+  using C = cplx<real>;
+  const WArgs<real> &a;
+  C *fb;  // [2][6 * Smax]
+  int lane, nw, end;
+  int code1 = 0, code2 = 0;
+  int64_t off1 = 0, off2 = 0;
+  C w1{0, 0}, w2{0, 0}, y1{0, 0}, y2{0, 0};
+  __device__ WPipe(const WArgs<real> &args, C *buf, int l, int n, int e)
+      : a(args), fb(buf), lane(l), nw(n), end(e) {}
+  __device__ __forceinline__ void meta(int i, int &code, int64_t &off, C &w, C &y, bool vis_in) {
+    if (i < end) {
+      code = a.code[i];
+      off = a.factor[i];
+      w = static_cast<const C *>(a.weight)[i];
+      if (vis_in) y = static_cast<const C *>(a.slot_in)[i];
+    }
+  }
+  __device__ __forceinline__ void issue(int i, int code, int64_t off, int buf) {
+    if (i < end) {
+      const int S = (code >> 16) & 0xff;
+      const C *src = static_cast<const C *>(a.factors) + off;
+      C *dst = fb + buf * 6 * a.Smax;
+      for (int k = lane; k < 6 * S; k += 32) cp_async<sizeof(C)>(dst + k, src + k);
+    }
+    cp_async_commit();
+  }
+};
 
 template <typename real>
 __global__ void __launch_bounds__(128) wdegrid_kernel(const WArgs<real> a) {
@@ -63,7 +99,7 @@ __global__ void __launch_bounds__(128) wdegrid_kernel(const WArgs<real> a) {
   const int WW = tk.W + a.Smax - 1, WH = tk.H + a.Smax - 1;
   C *win = reinterpret_cast<C *>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  C *fbuf = reinterpret_cast<C *>(smem_raw + a.win_bytes) + warp * 6 * a.Smax;
+  C *fb = reinterpret_cast<C *>(smem_raw + a.win_bytes) + warp * 2 * 6 * a.Smax;
   const C *grid = static_cast<const C *>(a.grid);
   for (int idx = threadIdx.x; idx < WW * WH; idx += blockDim.x) {
     const int lp = idx / WW, lq = idx - lp * WW;
@@ -75,13 +111,23 @@ __global__ void __launch_bounds__(128) wdegrid_kernel(const WArgs<real> a) {
   }
   cp_async_wait_all();
   __syncthreads();
-  const C *factors = static_cast<const C *>(a.factors);
-  const C *weight = static_cast<const C *>(a.weight);
   C *out = static_cast<C *>(a.slot_out);
-  for (int i = tk.batch_begin + warp; i < tk.batch_end; i += nw) {
-    const int code = a.code[i];
-    const int lp = code & 0xff, lq = (code >> 8) & 0xff, S = (code >> 16) & 0xff;
-    stage_factors(factors + a.factor[i], fbuf, S, lane);
+  const int first = tk.batch_begin + warp;
+  WPipe<real> pp(a, fb, lane, nw, tk.batch_end);
+  int code0 = 0;
+  int64_t off0 = 0;
+  C w0{0, 0}, y0{0, 0};
+  pp.meta(first, code0, off0, w0, y0, false);
+  pp.meta(first + nw, pp.code1, pp.off1, pp.w1, pp.y1, false);
+  pp.issue(first, code0, off0, 0);
+  int buf = 0;
+  for (int i = first; i < tk.batch_end; i += nw) {
+    pp.issue(i + nw, pp.code1, pp.off1, buf ^ 1);
+    pp.meta(i + 2 * nw, pp.code2, pp.off2, pp.w2, pp.y2, false);
+    cp_async_wait_one();
+    __syncwarp();  // every lane's factor copies for visibility i have landed
+    const C *fbuf = fb + buf * 6 * a.Smax;
+    const int lp = code0 & 0xff, lq = (code0 >> 8) & 0xff, S = (code0 >> 16) & 0xff;
     const int R = 32 / S, r = lane / S, c = lane - r * S;
     const bool active = r < R;
     C b0{0, 0}, b1{0, 0}, b2{0, 0};
@@ -90,24 +136,40 @@ __global__ void __launch_bounds__(128) wdegrid_kernel(const WArgs<real> a) {
       b1 = fbuf[4 * S + c];
       b2 = fbuf[5 * S + c];
     }
-    C acc{0, 0};
-    for (int jv0 = 0; jv0 < S; jv0 += R) {
-      const int jv = jv0 + r;
-      if (active && jv < S) {
-        C k = cmul(fbuf[jv], b0);
-        cfma(k, fbuf[S + jv], b1);
-        cfma(k, fbuf[2 * S + jv], b2);
-        cfma(acc, k, win[(lp + jv) * WW + lq + c]);
+    C acc{0, 0}, acc2{0, 0};
+    for (int jv0 = 0; jv0 < S; jv0 += 2 * R) {
+      const int ja = jv0 + r, jb = jv0 + R + r;
+      if (active && ja < S) {
+        C k = cmul(fbuf[ja], b0);
+        cfma(k, fbuf[S + ja], b1);
+        cfma(k, fbuf[2 * S + ja], b2);
+        cfma(acc, k, win[(lp + ja) * WW + lq + c]);
+      }
+      if (active && jb < S) {
+        C k = cmul(fbuf[jb], b0);
+        cfma(k, fbuf[S + jb], b1);
+        cfma(k, fbuf[2 * S + jb], b2);
+        cfma(acc2, k, win[(lp + jb) * WW + lq + c]);
       }
     }
+    acc.x += acc2.x;
+    acc.y += acc2.y;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
       acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
     }
-    if (lane == 0) out[i] = cmul(acc, weight[i]);
-    __syncwarp();  // fbuf is reused by the next visibility
+    if (lane == 0) out[i] = cmul(acc, w0);
+    __syncwarp();  // this half of the factor buffer is refilled two visibilities on
+    code0 = pp.code1;
+    off0 = pp.off1;
+    w0 = pp.w1;
+    pp.code1 = pp.code2;
+    pp.off1 = pp.off2;
+    pp.w1 = pp.w2;
+    buf ^= 1;
   }
+  cp_async_wait_all();
 }
 
 template <typename real>
@@ -118,20 +180,28 @@ __global__ void __launch_bounds__(128) wgrid_kernel(const WArgs<real> a) {
   const int WW = tk.W + a.Smax - 1, WH = tk.H + a.Smax - 1, WN = WW * WH;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   C *wins = reinterpret_cast<C *>(smem_raw);
-  C *fbuf = reinterpret_cast<C *>(smem_raw + a.win_bytes) + warp * 6 * a.Smax;
+  C *fb = reinterpret_cast<C *>(smem_raw + a.win_bytes) + warp * 2 * 6 * a.Smax;
   for (int idx = threadIdx.x; idx < nw * WN; idx += blockDim.x) wins[idx] = C{0, 0};
   __syncthreads();
   C *mine = wins + warp * WN;
-  const C *factors = static_cast<const C *>(a.factors);
-  const C *weight = static_cast<const C *>(a.weight);
-  const C *vin = static_cast<const C *>(a.slot_in);
-  for (int i = tk.batch_begin + warp; i < tk.batch_end; i += nw) {
-    const int code = a.code[i];
-    const int lp = code & 0xff, lq = (code >> 8) & 0xff, S = (code >> 16) & 0xff;
-    stage_factors(factors + a.factor[i], fbuf, S, lane);
+  const int first = tk.batch_begin + warp;
+  WPipe<real> pp(a, fb, lane, nw, tk.batch_end);
+  int code0 = 0;
+  int64_t off0 = 0;
+  C w0{0, 0}, y0{0, 0};
+  pp.meta(first, code0, off0, w0, y0, true);
+  pp.meta(first + nw, pp.code1, pp.off1, pp.w1, pp.y1, true);
+  pp.issue(first, code0, off0, 0);
+  int buf = 0;
+  for (int i = first; i < tk.batch_end; i += nw) {
+    pp.issue(i + nw, pp.code1, pp.off1, buf ^ 1);
+    pp.meta(i + 2 * nw, pp.code2, pp.off2, pp.w2, pp.y2, true);
+    cp_async_wait_one();
+    __syncwarp();  // every lane's factor copies for visibility i have landed
+    const C *fbuf = fb + buf * 6 * a.Smax;
+    const int lp = code0 & 0xff, lq = (code0 >> 8) & 0xff, S = (code0 >> 16) & 0xff;
     // conj(weight) * y: G^H holds the conjugated entries of G
-    const C w = weight[i], y = vin[i];
-    const C z{w.x * y.x + w.y * y.y, w.x * y.y - w.y * y.x};
+    const C z{w0.x * y0.x + w0.y * y0.y, w0.x * y0.y - w0.y * y0.x};
     const int R = 32 / S, r = lane / S, c = lane - r * S;
     const bool active = r < R;
     C b0{0, 0}, b1{0, 0}, b2{0, 0};
@@ -141,23 +211,50 @@ __global__ void __launch_bounds__(128) wgrid_kernel(const WArgs<real> a) {
       b2 = fbuf[5 * S + c];
     }
     // All S^2 cells of one visibility are distinct, so the lanes never touch
-    // the same cell within it; visibilities are ordered by __syncwarp.
-    for (int jv0 = 0; jv0 < S; jv0 += R) {
-      const int jv = jv0 + r;
-      if (active && jv < S) {
-        C k = cmul(fbuf[jv], b0);
-        cfma(k, fbuf[S + jv], b1);
-        cfma(k, fbuf[2 * S + jv], b2);
-        // conj(K) z
-        C *cell = mine + (lp + jv) * WW + lq + c;
-        C v = *cell;
-        v.x = fma(k.x, z.x, fma(k.y, z.y, v.x));
-        v.y = fma(k.x, z.y, fma(-k.y, z.x, v.y));
-        *cell = v;
+    // the same cell within it, and the two rows a lane updates per step are
+    // different cells; visibilities are ordered by __syncwarp.
+    for (int jv0 = 0; jv0 < S; jv0 += 2 * R) {
+      const int ja = jv0 + r, jb = jv0 + R + r;
+      const bool oka = active && ja < S, okb = active && jb < S;
+      C ka{0, 0}, kb{0, 0}, va{0, 0}, vb{0, 0};
+      C *ca = mine + (lp + ja) * WW + lq + c;
+      C *cb = mine + (lp + jb) * WW + lq + c;
+      if (oka) {
+        ka = cmul(fbuf[ja], b0);
+        cfma(ka, fbuf[S + ja], b1);
+        cfma(ka, fbuf[2 * S + ja], b2);
+        va = *ca;
+      }
+      if (okb) {
+        kb = cmul(fbuf[jb], b0);
+        cfma(kb, fbuf[S + jb], b1);
+        cfma(kb, fbuf[2 * S + jb], b2);
+        vb = *cb;
+      }
+      // conj(K) z
+      if (oka) {
+        va.x = fma(ka.x, z.x, fma(ka.y, z.y, va.x));
+        va.y = fma(ka.x, z.y, fma(-ka.y, z.x, va.y));
+        *ca = va;
+      }
+      if (okb) {
+        vb.x = fma(kb.x, z.x, fma(kb.y, z.y, vb.x));
+        vb.y = fma(kb.x, z.y, fma(-kb.y, z.x, vb.y));
+        *cb = vb;
       }
     }
     __syncwarp();
+    code0 = pp.code1;
+    off0 = pp.off1;
+    w0 = pp.w1;
+    y0 = pp.y1;
+    pp.code1 = pp.code2;
+    pp.off1 = pp.off2;
+    pp.w1 = pp.w2;
+    pp.y1 = pp.y2;
+    buf ^= 1;
   }
+  cp_async_wait_all();
   __syncthreads();
   C *out = static_cast<C *>(a.tilebuf) + size_t(blockIdx.x) * a.slot_stride;
   for (int idx = threadIdx.x; idx < WN; idx += blockDim.x) {
@@ -182,12 +279,12 @@ size_t wwindow_bytes(int bytes_real, int win_rows, int win_cols, int threads, bo
 template <typename real>
 size_t wdegrid_smem_bytes(int win_rows, int win_cols, int Smax, int threads) {
   return wwindow_bytes(sizeof(real), win_rows, win_cols, threads, false) +
-         size_t(threads / 32) * 6 * Smax * 2 * sizeof(real);
+         size_t(threads / 32) * 2 * 6 * Smax * 2 * sizeof(real);
 }
 template <typename real>
 size_t wgrid_smem_bytes(int win_rows, int win_cols, int Smax, int threads) {
   return wwindow_bytes(sizeof(real), win_rows, win_cols, threads, true) +
-         size_t(threads / 32) * 6 * Smax * 2 * sizeof(real);
+         size_t(threads / 32) * 2 * 6 * Smax * 2 * sizeof(real);
 }
 
 template <typename real>
