@@ -125,6 +125,28 @@ int purify_gb300_adjoint(purify_gb300_operator *op, const void *y, void *x, void
 int purify_gb300_forward_host(purify_gb300_operator *op, const double *x, double *y);
 int purify_gb300_adjoint_host(purify_gb300_operator *op, const double *y, double *x);
 
+/* Phi^H Phi x on device buffers (x and out: imsizey*imsizex values; they may
+ * be the same buffer), the visibilities kept in the operator's internal order
+ * between the two halves.  This is the combined degridding/gridding operator
+ * of operators::init_grid_degrid_operator_2d (compact_operators.h:147-174):
+ * with the operator's norm from its power method it is Phi'^H Phi' /
+ * ||Phi'||^2, what the reference computes with the G^H G sparse matrix
+ * (pruned at 1e-7, compact_operators.h:103-116); here nothing is pruned. */
+int purify_gb300_normal(purify_gb300_operator *op, const void *x, void *out, void *stream);
+
+/* Convolution with the point-spread function, the image-domain approximation
+ * of Phi^H Phi (operators::init_psf_convolve_2d, compact_operators.h:279-307):
+ * psf = Phi^H Phi delta with delta at pixel (floor(imsizey/2) - 1,
+ * floor(imsizex/2) - 1); apply(x) = F^-1 (F psf . F x) / ||.||^2 with the
+ * unitary imsizey x imsizex FFT F (circular, no padding) and the norm from
+ * power_iters power-method rounds on the unnormalised convolution. */
+typedef struct purify_gb300_psf purify_gb300_psf;
+int purify_gb300_psf_create(purify_gb300_operator *op, uint32_t power_iters, double power_tol,
+                            purify_gb300_psf **out);
+int purify_gb300_psf_apply(purify_gb300_psf *p, const void *x, void *out, void *stream);
+int purify_gb300_psf_norm(const purify_gb300_psf *p, double *norm);
+int purify_gb300_psf_destroy(purify_gb300_psf *p);
+
 /* G and G^H alone on device buffers of the operator's precision: grid is
  * ftsizev*ftsizeu values (index p * ftsizeu + q), vis is M values.  Replaces
  * the closures of operators::init_gridding_matrix_2d (operators.h:123-145). */

@@ -203,3 +203,39 @@ class Operator:
         _check(lib().or_power_method(self.h, int(iters), float(tol), _ptr(x0), ctypes.byref(out)))
         self.norm = out.value
         return self.norm
+
+
+def psf_convolve(op, imsizey, imsizex, power_iters=100, power_tol=1e-4):
+    """operators::init_psf_convolve_2d (cpp/purify/compact_operators.h:279-307)
+    on an oracle operator: psf = Phi^H Phi delta with delta at sub2ind(floor(Ny/2)
+    - 1, floor(Nx/2) - 1) (utilities.cc:321-333, row * cols + col); A x =
+    F^-1(F psf . F x) with the unitary Ny x Nx FFT of init_FFT_2d
+    (operators.h:206-261; no padding, circular); the power method on {A, id}
+    from the normalised all-ones vector (the rule of Operator.power_method)
+    gives ||A||, and the operator is A / ||A||^2.  Returns (apply, norm)."""
+    N = imsizey * imsizex
+    delta = np.zeros(N, dtype=np.complex128)
+    delta[(imsizey // 2 - 1) * imsizex + (imsizex // 2 - 1)] = 1.0
+    psf = op.adjoint(op.forward(delta))
+    ft = fft2(psf.reshape(imsizey, imsizex)).ravel() / np.sqrt(N)
+
+    def raw(x):
+        fx = fft2(np.asarray(x, dtype=np.complex128).reshape(imsizey, imsizex)).ravel() / np.sqrt(N)
+        return fft2((ft * fx).reshape(imsizey, imsizex), inverse=True).ravel() / np.sqrt(N)
+
+    norm = 1.0
+    if power_iters > 0:
+        x = np.full(N, 1.0 / np.sqrt(N), dtype=np.complex128)
+        old = 0.0
+        for _ in range(power_iters):
+            x = raw(x)
+            value = float(np.sqrt(np.sum(np.abs(x) ** 2)))
+            if not value > 0:
+                raise RuntimeError("Operator norm is not greater than zero.")
+            x = x / value
+            if power_tol * power_tol > abs(old - value) / old if old else False:
+                old = value
+                break
+            old = value
+        norm = float(np.sqrt(old))
+    return (lambda x: raw(x) / norm ** 2), norm

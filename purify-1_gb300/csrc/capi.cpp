@@ -13,6 +13,7 @@
 #include "gridding_kernels.h"
 #include "operator.h"
 #include "plan.h"
+#include "psf.h"
 #include "server.h"
 #include "wplan.h"
 
@@ -21,6 +22,9 @@ struct purify_gb300_operator {
 };
 struct purify_gb300_plan {
   pg::Plan plan;
+};
+struct purify_gb300_psf {
+  std::unique_ptr<pg::PsfConvolve> impl;
 };
 struct purify_gb300_server {
   std::unique_ptr<pg::Server> impl;
@@ -164,6 +168,37 @@ int purify_gb300_adjoint(purify_gb300_operator *op, const void *y, void *x, void
     op->impl->adjoint(y, x, static_cast<cudaStream_t>(stream));
   });
 }
+int purify_gb300_normal(purify_gb300_operator *op, const void *x, void *out, void *stream) {
+  if (!op) return null_arg("operator");
+  if (!x || !out) return null_arg("buffer");
+  return guard([&] { op->impl->normal(x, out, static_cast<cudaStream_t>(stream)); });
+}
+int purify_gb300_psf_create(purify_gb300_operator *op, uint32_t power_iters, double power_tol,
+                            purify_gb300_psf **out) {
+  if (!op) return null_arg("operator");
+  if (!out) return null_arg("out");
+  *out = nullptr;
+  return guard([&] {
+    std::unique_ptr<purify_gb300_psf> h(new purify_gb300_psf);
+    h->impl = pg::PsfConvolve::create(*op->impl, int(power_iters), power_tol);
+    *out = h.release();
+  });
+}
+int purify_gb300_psf_apply(purify_gb300_psf *p, const void *x, void *out, void *stream) {
+  if (!p) return null_arg("psf");
+  if (!x || !out) return null_arg("buffer");
+  return guard([&] { p->impl->apply(x, out, static_cast<cudaStream_t>(stream)); });
+}
+int purify_gb300_psf_norm(const purify_gb300_psf *p, double *norm) {
+  if (!p) return null_arg("psf");
+  if (!norm) return null_arg("norm");
+  *norm = p->impl->norm();
+  return PURIFY_GB300_OK;
+}
+int purify_gb300_psf_destroy(purify_gb300_psf *p) {
+  return guard([&] { delete p; });
+}
+
 int purify_gb300_degrid(purify_gb300_operator *op, const void *grid, void *vis, void *stream) {
   if (!op) return null_arg("operator");
   return guard([&] {

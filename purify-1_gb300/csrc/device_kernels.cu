@@ -179,6 +179,24 @@ __global__ void scale_rsqrt_kernel(cplx<real> *x, int64_t n, const double *__res
   }
 }
 
+// a <- a * b * scale (complex, element-wise).
+template <typename real>
+__global__ void cmul_scale_kernel(cplx<real> *__restrict__ a, const cplx<real> *__restrict__ b,
+                                  int64_t n, real scale) {
+  for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n;
+       k += int64_t(gridDim.x) * blockDim.x) {
+    const cplx<real> x = a[k], y = b[k];
+    a[k] = cplx<real>{scale * (x.x * y.x - x.y * y.y), scale * (x.x * y.y + x.y * y.x)};
+  }
+}
+// x <- 0, x[index] <- 1.
+template <typename real>
+__global__ void delta_kernel(cplx<real> *x, int64_t n, int64_t index) {
+  for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n;
+       k += int64_t(gridDim.x) * blockDim.x)
+    x[k] = cplx<real>{k == index ? real(1) : real(0), real(0)};
+}
+
 int stream_blocks(int64_t n, int threads) {
   const int64_t b = (n + threads - 1) / threads;
   return int(b < 1 ? 1 : (b > 152 * 32 ? 152 * 32 : b));
@@ -293,6 +311,19 @@ cudaError_t launch_scale(void *x, int64_t n, double scale, cudaStream_t s) {
   return cudaGetLastError();
 }
 template <typename real>
+cudaError_t launch_cmul_scale(void *a, const void *b, int64_t n, double scale, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  cmul_scale_kernel<real><<<stream_blocks(n, 256), 256, 0, s>>>(
+      static_cast<cplx<real> *>(a), static_cast<const cplx<real> *>(b), n, real(scale));
+  return cudaGetLastError();
+}
+template <typename real>
+cudaError_t launch_delta(void *x, int64_t n, int64_t index, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  delta_kernel<real><<<stream_blocks(n, 256), 256, 0, s>>>(static_cast<cplx<real> *>(x), n, index);
+  return cudaGetLastError();
+}
+template <typename real>
 cudaError_t launch_scale_rsqrt(void *x, int64_t n, const double *sq, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   scale_rsqrt_kernel<real><<<stream_blocks(n, 256), 256, 0, s>>>(static_cast<cplx<real> *>(x), n,
@@ -327,7 +358,9 @@ cudaError_t launch_fill(void *x, int64_t n, double value, cudaStream_t s) {
                                             cudaStream_t);                                      \
   template cudaError_t launch_scale<real>(void *, int64_t, double, cudaStream_t);               \
   template cudaError_t launch_fill<real>(void *, int64_t, double, cudaStream_t);                 \
-  template cudaError_t launch_scale_rsqrt<real>(void *, int64_t, const double *, cudaStream_t);
+  template cudaError_t launch_scale_rsqrt<real>(void *, int64_t, const double *, cudaStream_t);   \
+  template cudaError_t launch_cmul_scale<real>(void *, const void *, int64_t, double, cudaStream_t); \
+  template cudaError_t launch_delta<real>(void *, int64_t, int64_t, cudaStream_t);
 
 PG_INSTANTIATE(float)
 PG_INSTANTIATE(double)

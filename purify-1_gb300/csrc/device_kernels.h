@@ -170,6 +170,12 @@ cudaError_t launch_scale(void *x, int64_t n, double scale, cudaStream_t s);
 // x <- x * real(1 / sqrt(*sq)) with *sq on the device (0 when not positive).
 template <typename real>
 cudaError_t launch_scale_rsqrt(void *x, int64_t n, const double *sq, cudaStream_t s);
+// a <- a * b * scale, complex element-wise.
+template <typename real>
+cudaError_t launch_cmul_scale(void *a, const void *b, int64_t n, double scale, cudaStream_t s);
+// x <- the unit vector e_index.
+template <typename real>
+cudaError_t launch_delta(void *x, int64_t n, int64_t index, cudaStream_t s);
 // x <- value (complex, real part only).
 template <typename real>
 cudaError_t launch_fill(void *x, int64_t n, double value, cudaStream_t s);

@@ -36,6 +36,7 @@ class OperatorT final : public Operator {
   ~OperatorT() override;
   void forward(const void *x, void *y, cudaStream_t stream) override;
   void adjoint(const void *y, void *x, cudaStream_t stream) override;
+  void normal(const void *x, void *out, cudaStream_t stream) override;
   void degrid(const void *grid, void *vis, cudaStream_t stream) override;
   void grid(const void *vis, void *grid, cudaStream_t stream) override;
   void grid_no_alloc(const void *vis, void *grid, cudaStream_t stream) override;
@@ -253,6 +254,7 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
   }
 
   info_.M = M_;
+  info_.device = device_;
   info_.imsizey = Ny_;
   info_.imsizex = Nx_;
   info_.ftsizev = Nv_;
@@ -700,6 +702,16 @@ void OperatorT<real>::power_ws(void *x, int iters, double *sq, double *partial,
       cuda_check(launch_scale_rsqrt<real>(x, N_, sq + i, w.stream), "scale");
     }
   });
+}
+
+template <typename real>
+void OperatorT<real>::normal(const void *x, void *out, cudaStream_t user) {
+  DeviceGuard guard(device_);
+  std::lock_guard<std::mutex> lock(mu_);
+  join(user);
+  forward_slots(x);
+  adjoint_slots(out);
+  release(user);
 }
 
 template <typename real>

@@ -60,6 +60,7 @@ struct OperatorInfo {
   bool w_term = false;
   int64_t nnz = 0, occupied_cells = 0, work_items = 0, tasks = 0, device_bytes = 0;
   double kernel_fit_error = 0, norm = 1;
+  int device = 0;
 };
 
 // Scratch of one apply held outside the operator, so that several applies of
@@ -85,6 +86,9 @@ class Operator {
   // Device buffers of the operator's precision; ordered after `stream`.
   virtual void forward(const void *x, void *y, cudaStream_t stream) = 0;
   virtual void adjoint(const void *y, void *x, cudaStream_t stream) = 0;
+  // Phi^H Phi x with the visibilities kept in slot order between the two
+  // halves (no caller-order permutation): the combined degrid/grid operator.
+  virtual void normal(const void *x, void *out, cudaStream_t stream) = 0;
   // G and G^H alone (no correction, padding or FFT).
   virtual void degrid(const void *grid, void *vis, cudaStream_t stream) = 0;
   virtual void grid(const void *vis, void *grid, cudaStream_t stream) = 0;

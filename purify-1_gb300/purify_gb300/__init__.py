@@ -132,7 +132,8 @@ EXPORTS = [
     "purify_gb300_batch_time",
     "purify_gb300_server_create", "purify_gb300_server_destroy", "purify_gb300_server_add_coverage",
     "purify_gb300_server_submit", "purify_gb300_server_wait", "purify_gb300_server_request_bytes",
-    "purify_gb300_server_get_stats",
+    "purify_gb300_server_get_stats", "purify_gb300_normal", "purify_gb300_psf_create",
+    "purify_gb300_psf_apply", "purify_gb300_psf_norm", "purify_gb300_psf_destroy",
 ]
 STAGES = ["pad", "fft_forward", "degrid", "grid", "fold", "fft_inverse", "crop", "compact",
           "expand"]
@@ -209,6 +210,11 @@ def load(path=None):
     L.purify_gb300_server_wait.argtypes = [vp, ctypes.c_int64, ctypes.c_double, P(Result)]
     L.purify_gb300_server_request_bytes.argtypes = [vp, P(Request), P(ctypes.c_int64)]
     L.purify_gb300_server_get_stats.argtypes = [vp, P(ServerStats)]
+    L.purify_gb300_normal.argtypes = [vp, vp, vp, vp]
+    L.purify_gb300_psf_create.argtypes = [vp, ctypes.c_uint32, ctypes.c_double, P(vp)]
+    L.purify_gb300_psf_apply.argtypes = [vp, vp, vp, vp]
+    L.purify_gb300_psf_norm.argtypes = [vp, P(ctypes.c_double)]
+    L.purify_gb300_psf_destroy.argtypes = [vp]
     _lib = L
     return L
 
@@ -431,6 +437,19 @@ class MeasurementOperator:
         _check(load().purify_gb300_adjoint(self._h, ctypes.c_void_p(y.data_ptr()),
                                            ctypes.c_void_p(x.data_ptr()), self._stream(stream)))
         return x
+
+    def normal(self, x, stream=None):
+        """Phi^H Phi x for a CUDA tensor x (imsizey*imsizex values), the
+        combined degrid/grid operator (init_grid_degrid_operator_2d)."""
+        import torch
+        self._check_device_tensor(x, self.imsizey * self.imsizex)
+        out = torch.empty_like(x)
+        return self.normal_into(x, out, stream)
+
+    def normal_into(self, x, out, stream=None):
+        _check(load().purify_gb300_normal(self._h, ctypes.c_void_p(x.data_ptr()),
+                                          ctypes.c_void_p(out.data_ptr()), self._stream(stream)))
+        return out
 
     def degrid_into(self, grid, vis, stream=None):
         """G alone: grid (ftsizev*ftsizeu) -> vis (M), device tensors."""
@@ -745,3 +764,44 @@ class Server:
         st = ServerStats()
         _check(load().purify_gb300_server_get_stats(self._h, ctypes.byref(st)))
         return {f: getattr(st, f) for f, _ in ServerStats._fields_}
+
+
+
+class PsfConvolve:
+    """Convolution with the operator's point-spread function, the
+    image-domain approximation of Phi^H Phi (init_psf_convolve_2d,
+    cpp/purify/compact_operators.h:279-307), on CUDA tensors."""
+
+    def __init__(self, op, power_iters=100, power_tol=1e-4):
+        h = ctypes.c_void_p()
+        _check(load().purify_gb300_psf_create(op.handle, int(power_iters), float(power_tol),
+                                              ctypes.byref(h)))
+        self._h = h
+        self.op = op
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            load().purify_gb300_psf_destroy(h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def norm(self):
+        n = ctypes.c_double()
+        _check(load().purify_gb300_psf_norm(self._h, ctypes.byref(n)))
+        return n.value
+
+    def __call__(self, x, out=None, stream=None):
+        import torch
+        self.op._check_device_tensor(x, self.op.imsizey * self.op.imsizex)
+        out = torch.empty_like(x) if out is None else out
+        _check(load().purify_gb300_psf_apply(self._h, ctypes.c_void_p(x.data_ptr()),
+                                             ctypes.c_void_p(out.data_ptr()),
+                                             self.op._stream(stream)))
+        return out

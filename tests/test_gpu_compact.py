@@ -1,0 +1,109 @@
+"""The combined degrid/grid operator Phi^H Phi (init_grid_degrid_operator_2d,
+compact_operators.h:147-174) and the PSF convolution approximation
+(init_psf_convolve_2d, compact_operators.h:279-307) against the FP64 oracle,
+and the reference's power-method checks of both (tests/operators.cc:171-215:
+the normalised operators have norm 1 within power_tol).
+
+Tolerances (relative L2): FP64 1e-10, FP32 1e-5 (the parity bars of the
+measurement operator); normal vs adjoint(forward): exact (same kernels on the
+same values, only the visibility order between the halves differs)."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from purify_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+TOL = {"fp32": 1e-5, "fp64": 1e-10}
+
+
+def case(n=64, M=6000, seed=4):
+    u, v = synthetic.gaussian_core_uv(M, 2 * n, 2 * n, 0.25, seed=seed)
+    return u, v, n
+
+
+def dev(torch, a, precision):
+    dt = torch.complex64 if precision == "fp32" else torch.complex128
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.complex128)).to(dt).cuda()
+
+
+def host(t):
+    return t.cpu().numpy().astype(np.complex128)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_normal_equals_forward_then_adjoint(pg, cuda, precision):
+    torch = cuda
+    u, v, n = case()
+    wt = np.random.default_rng(1).standard_normal(u.size) + 0.5j
+    op = pg.MeasurementOperator(u, v, None, wt, n, n, 2.0, power_iters=10, precision=precision)
+    x = dev(torch, synthetic.sky_image(n, n), precision)
+    a = op.normal(x)
+    b = op.adjoint(op.forward(x))
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)
+    # in place
+    y = x.clone()
+    op.normal_into(y, y)
+    torch.cuda.synchronize()
+    assert torch.equal(y, a)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_normal_vs_oracle_and_norm(pg, oracle_mod, cuda, precision):
+    torch = cuda
+    u, v, n = case()
+    op = pg.MeasurementOperator(u, v, None, None, n, n, 2.0, power_iters=100, power_tol=1e-4,
+                                precision=precision)
+    oop = oracle_mod.Operator(u, v, None, None, n, n, 2.0, kernel="kb", Ju=4, Jv=4)
+    oop.power_method(100, 1e-4)
+    x = synthetic.sky_image(n, n, seed=2)
+    got = host(op.normal(dev(torch, x, precision)))
+    assert rel_l2(got, oop.adjoint(oop.forward(x))) < TOL[precision]
+    # the normalised Phi^H Phi has norm 1 (tests/operators.cc:184-190)
+    z = torch.ones(n * n, dtype=op.complex_dtype, device="cuda") / n
+    old = 0.0
+    for _ in range(100):
+        z = op.normal(z)
+        value = float(torch.linalg.norm(z).item())
+        z = z / value
+        if abs(old - value) / value < 1e-8:
+            break
+        old = value
+    assert abs(np.sqrt(value) - 1.0) < 1e-3
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_psf_convolve_vs_oracle(pg, oracle_mod, cuda, precision):
+    torch = cuda
+    u, v, n = case(n=64, M=5000, seed=7)
+    op = pg.MeasurementOperator(u, v, None, None, n, n, 2.0, power_iters=100, power_tol=1e-4,
+                                precision=precision)
+    oop = oracle_mod.Operator(u, v, None, None, n, n, 2.0, kernel="kb", Ju=4, Jv=4)
+    oop.power_method(100, 1e-4)
+    psf = pg.PsfConvolve(op, power_iters=100, power_tol=1e-4)
+    apply_ref, norm_ref = oracle_mod.psf_convolve(oop, n, n, 100, 1e-4)
+    assert abs(psf.norm - norm_ref) / norm_ref < (1e-10 if precision == "fp64" else 1e-5)
+    x = synthetic.sky_image(n, n, seed=3)
+    got = host(psf(dev(torch, x, precision)))
+    assert rel_l2(got, apply_ref(x)) < TOL[precision]
+    # the normalised convolution has norm 1 (tests/operators.cc:201-214)
+    z = torch.ones(n * n, dtype=op.complex_dtype, device="cuda") / n
+    for _ in range(200):
+        z = psf(z)
+        value = float(torch.linalg.norm(z).item())
+        z = z / value
+    assert abs(np.sqrt(value) - 1.0) < 1e-3
+
+
+def test_psf_of_non_square_image(pg, oracle_mod, cuda):
+    torch = cuda
+    ny, nx = 48, 80
+    u, v = synthetic.gaussian_core_uv(3000, 2 * nx, 2 * ny, 0.25, seed=9)
+    op = pg.MeasurementOperator(u, v, None, None, ny, nx, 2.0, power_iters=50, precision="fp64")
+    oop = oracle_mod.Operator(u, v, None, None, ny, nx, 2.0, kernel="kb", Ju=4, Jv=4)
+    oop.power_method(50, 1e-4)
+    psf = pg.PsfConvolve(op, power_iters=50)
+    apply_ref, norm_ref = oracle_mod.psf_convolve(oop, ny, nx, 50, 1e-4)
+    x = synthetic.sky_image(ny, nx, seed=5)
+    assert rel_l2(host(psf(dev(torch, x, "fp64"))), apply_ref(x)) < 1e-10

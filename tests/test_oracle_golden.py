@@ -143,3 +143,24 @@ def test_lambda_to_pixels_round_trip(oracle_mod):
         up, vp = oracle_mod.lambda_to_pixels(u, u, cell, cell, 256, 256)
         scale = 60.0 * 60.0 * 180.0 / cell / 256 / np.pi
         assert is_approx(u, up * scale, 1e-6)
+
+
+def test_psf_convolve_normalised_norm_is_one(oracle_mod):
+    """init_psf_convolve_2d's operator is normalised by its own power method,
+    so a second power method gives norm 1 within power_tol
+    (cpp/tests/operators.cc:201-214)."""
+    rng = np.random.default_rng(0)
+    n = 16
+    u = rng.normal(0, 4, 200)
+    v = rng.normal(0, 4, 200)
+    op = oracle_mod.Operator(u, v, None, None, n, n, 2.0, kernel="kb", Ju=4, Jv=4)
+    op.power_method(100, 1e-4)
+    apply, norm = oracle_mod.psf_convolve(op, n, n, 100, 1e-4)
+    assert norm > 0
+    x = rng.standard_normal(n * n) + 1j * rng.standard_normal(n * n)
+    x /= np.linalg.norm(x)
+    for _ in range(300):
+        x = apply(x)
+        value = np.linalg.norm(x)
+        x /= value
+    assert abs(np.sqrt(value) - 1.0) < 1e-4
