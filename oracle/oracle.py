@@ -217,11 +217,12 @@ def psf_convolve(op, imsizey, imsizex, power_iters=100, power_tol=1e-4):
     delta = np.zeros(N, dtype=np.complex128)
     delta[(imsizey // 2 - 1) * imsizex + (imsizex // 2 - 1)] = 1.0
     psf = op.adjoint(op.forward(delta))
-    ft = fft2(psf.reshape(imsizey, imsizex)).ravel() / np.sqrt(N)
+    # fft2 is the oracle's unitary transform (each direction / sqrt(N))
+    ft = fft2(psf.reshape(imsizey, imsizex)).ravel()
 
     def raw(x):
-        fx = fft2(np.asarray(x, dtype=np.complex128).reshape(imsizey, imsizex)).ravel() / np.sqrt(N)
-        return fft2((ft * fx).reshape(imsizey, imsizex), inverse=True).ravel() / np.sqrt(N)
+        fx = fft2(np.asarray(x, dtype=np.complex128).reshape(imsizey, imsizex)).ravel()
+        return fft2((ft * fx).reshape(imsizey, imsizex), inverse=True).ravel()
 
     norm = 1.0
     if power_iters > 0:
