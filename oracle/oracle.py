@@ -211,7 +211,7 @@ def psf_convolve(op, imsizey, imsizex, power_iters=100, power_tol=1e-4):
     - 1, floor(Nx/2) - 1) (utilities.cc:321-333, row * cols + col); A x =
     F^-1(F psf . F x) with the unitary Ny x Nx FFT of init_FFT_2d
     (operators.h:206-261; no padding, circular); the power method on {A, id}
-    from the normalised all-ones vector (the rule of Operator.power_method)
+    (the rule of Operator.power_method, from a fixed pseudo-random image)
     gives ||A||, and the operator is A / ||A||^2.  Returns (apply, norm)."""
     N = imsizey * imsizex
     delta = np.zeros(N, dtype=np.complex128)
@@ -226,7 +226,13 @@ def psf_convolve(op, imsizey, imsizex, power_iters=100, power_tol=1e-4):
 
     norm = 1.0
     if power_iters > 0:
-        x = np.full(N, 1.0 / np.sqrt(N), dtype=np.complex128)
+        # start: x_k = h(k) / 2^32 - 1/2, h(k) = 2654435761 k mod 2^32 (Knuth's
+        # multiplicative hash), normalised -- the all-ones image is the
+        # zero-frequency eigenvector of a circular convolution, so the
+        # reference starts from a random image instead
+        k = np.arange(N, dtype=np.uint64)
+        x = ((k * np.uint64(2654435761)) % np.uint64(2 ** 32)).astype(np.float64) / 2.0 ** 32 - 0.5
+        x = (x / np.linalg.norm(x)).astype(np.complex128)
         old = 0.0
         for _ in range(power_iters):
             x = raw(x)

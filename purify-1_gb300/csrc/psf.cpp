@@ -5,6 +5,7 @@
 #include <cmath>
 #include <complex>
 #include <mutex>
+#include <vector>
 
 #include "device_kernels.h"
 #include "device_util.h"
@@ -64,9 +65,22 @@ PsfT<real>::PsfT(Operator &op, int power_iters, double power_tol) {
   // Power method on A (adjoint = identity): x <- A x, estimate ||A x||,
   // stop when its relative change is below tol^2, norm = sqrt(estimate).
   if (power_iters > 0) {
+    // The all-ones image is the zero-frequency eigenvector of a circular
+    // convolution, so the iteration starts from a fixed pseudo-random image
+    // (the reference starts from a random one): x_k = h(k) / 2^32 - 1/2 with
+    // Knuth's multiplicative hash h(k) = 2654435761 k mod 2^32, normalised.
+    std::vector<C> x0(N_);
+    double nn = 0;
+    for (int64_t k = 0; k < N_; ++k) {
+      const double r = double(uint32_t(uint64_t(k) * 2654435761ull)) / 4294967296.0 - 0.5;
+      x0[k] = C(real(r), real(0));
+      nn += r * r;
+    }
+    const double inv = 1.0 / std::sqrt(nn);
+    for (auto &c : x0) c *= real(inv);
     DeviceBuffer x;
     x.alloc(sizeof(C) * N_, nullptr);
-    cuda_check(launch_fill<real>(x.get(), N_, 1.0 / std::sqrt(double(N_)), stream_), "fill");
+    x.upload(x0.data(), sizeof(C) * N_, stream_);
     double old_value = 0;
     for (int i = 0; i < power_iters; ++i) {
       apply_raw(x.get(), x.get(), 1.0);

@@ -3,7 +3,7 @@
 // 279-307): psf = Phi^H Phi delta at pixel (floor(Ny/2) - 1, floor(Nx/2) - 1);
 // A x = F^-1 (F psf * F x) with the unitary image-size FFT F (circular
 // convolution, no padding); the operator is A / ||A|| ^ 2 with ||A|| from the
-// power method on A.
+// power method on A, started from a fixed pseudo-random image.
 #pragma once
 #include <cuda_runtime_api.h>
 
