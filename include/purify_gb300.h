@@ -394,6 +394,31 @@ typedef struct {
 } purify_gb300_server_stats;
 int purify_gb300_server_get_stats(const purify_gb300_server *s, purify_gb300_server_stats *out);
 
+/* ---- Coverage ingest -------------------------------------------------------
+ * The reference's .vis text format (utilities::read_visibility,
+ * utilities.cc:140-188): per row u v [w] re(V) im(V) sigma separated by white
+ * space, nan / inf accepted; v is negated on reading (utilities.cc:178) and
+ * the weight is 1 / sigma.  purify_gb300_vis_file_rows counts the rows;
+ * purify_gb300_read_visibility fills u, v, w (NULL allowed when !w_term),
+ * vis and weights (complex<double>, rows values each).  Host only. */
+int purify_gb300_vis_file_rows(const char *path, int64_t *rows);
+int purify_gb300_read_visibility(const char *path, int32_t w_term, int64_t rows, double *u,
+                                 double *v, double *w, double *vis, double *weights);
+/* utilities::init_weights (utilities.cc:569-608): none (all 1), natural and
+ * whiten (the weights unchanged), uniform (w / sqrt(n)) and robust
+ * (w / sqrt(1 + s n), s = sum w^2 / sum n^2 * 25 * 10^(-2R)), with n the
+ * number of visibilities in the ftsizev x ftsizeu cell of floor(u / oversample),
+ * floor(v / oversample) (periodic).  The histogram and the sums run on the
+ * device (integer atomics, fixed-order FP64 reductions); host buffers. */
+#define PURIFY_GB300_WEIGHT_NONE 0
+#define PURIFY_GB300_WEIGHT_NATURAL 1
+#define PURIFY_GB300_WEIGHT_WHITEN 2
+#define PURIFY_GB300_WEIGHT_UNIFORM 3
+#define PURIFY_GB300_WEIGHT_ROBUST 4
+int purify_gb300_init_weights(const double *u, const double *v, const double *weights, int64_t M,
+                              double oversample_factor, int32_t weighting, double R,
+                              uint32_t ftsizeu, uint32_t ftsizev, int32_t device, double *out);
+
 /* Message of the last failing call on this thread ("" when none). */
 const char *purify_gb300_last_error(void);
 /* Library version string. */

@@ -246,3 +246,47 @@ def psf_convolve(op, imsizey, imsizex, power_iters=100, power_tol=1e-4):
             old = value
         norm = float(np.sqrt(old))
     return (lambda x: raw(x) / norm ** 2), norm
+
+
+def read_visibility(path, w_term=False):
+    """utilities::read_visibility (cpp/purify/utilities.cc:140-188) restated:
+    rows of u v [w] re im sigma; v negated (utilities.cc:178), weight 1 / sigma."""
+    with open(path) as f:
+        rows = sum(1 for _ in f)
+    with open(path) as f:
+        toks = f.read().split()
+    per = 6 if w_term else 5
+    vals = np.array([float(t) for t in toks[:rows * per]], dtype=np.float64).reshape(rows, per)
+    u, v = vals[:, 0], -vals[:, 1]
+    w = vals[:, 2] if w_term else np.zeros(rows)
+    k = 3 if w_term else 2
+    vis = np.empty(rows, dtype=np.complex128)
+    vis.real, vis.imag = vals[:, k], vals[:, k + 1]
+    weights = np.zeros(rows, dtype=np.complex128)
+    weights.real = 1.0 / vals[:, k + 2]
+    return {"u": u.copy(), "v": v.copy(), "w": w.copy(), "vis": vis, "weights": weights}
+
+
+def init_weights(u, v, weights, oversample_factor, weighting, R, ftsizeu, ftsizev):
+    """utilities::init_weights (cpp/purify/utilities.cc:569-608) restated with
+    sequential loops; utilities::mod is fmod wrapped to [0, y)."""
+    weights = np.asarray(weights, dtype=np.complex128)
+    if weighting == "none":
+        return np.ones_like(weights)
+    if weighting in ("natural", "whiten"):
+        return weights.copy()
+    if weighting not in ("uniform", "robust"):
+        raise RuntimeError("Wrong weighting type, " + weighting + " not recognised.")
+    scale = 1.0 / oversample_factor
+    q = np.mod(np.floor(np.asarray(u) * scale), ftsizeu).astype(np.int64)
+    p = np.mod(np.floor(np.asarray(v) * scale), ftsizev).astype(np.int64)
+    grid = np.zeros((ftsizev, ftsizeu), dtype=np.complex128)
+    for a, b in zip(p, q):
+        grid[a, b] += 1
+    sum_weights = np.sum(weights * weights)
+    sum_grid2 = np.sum(grid * grid)
+    robust_scale = sum_weights / sum_grid2 * 25.0 * 10.0 ** (-2 * R)
+    g = np.sqrt(grid)
+    if weighting == "uniform":
+        return weights / g[p, q]
+    return weights / np.sqrt(1.0 + robust_scale * g[p, q] * g[p, q])

@@ -11,6 +11,7 @@
 #include "../../include/purify_gb300.h"
 #include "batch.h"
 #include "gridding_kernels.h"
+#include "ingest.h"
 #include "operator.h"
 #include "plan.h"
 #include "psf.h"
@@ -685,6 +686,33 @@ int purify_gb300_server_get_stats(const purify_gb300_server *s, purify_gb300_ser
   out->latency_mean_ms = t.latency_mean_ms;
   out->visibility_passes = t.visibility_passes;
   return PURIFY_GB300_OK;
+}
+
+int purify_gb300_vis_file_rows(const char *path, int64_t *rows) {
+  if (!path) return null_arg("path");
+  if (!rows) return null_arg("rows");
+  return guard([&] { *rows = pg::vis_file_rows(path); });
+}
+int purify_gb300_read_visibility(const char *path, int32_t w_term, int64_t rows, double *u,
+                                 double *v, double *w, double *vis, double *weights) {
+  if (!path) return null_arg("path");
+  if (!u || !v || !vis || !weights) return null_arg("output");
+  if (w_term && !w) return null_arg("w");
+  return guard([&] {
+    pg::read_visibility(path, w_term != 0, rows, u, v, w,
+                        reinterpret_cast<std::complex<double> *>(vis),
+                        reinterpret_cast<std::complex<double> *>(weights));
+  });
+}
+int purify_gb300_init_weights(const double *u, const double *v, const double *weights, int64_t M,
+                              double oversample_factor, int32_t weighting, double R,
+                              uint32_t ftsizeu, uint32_t ftsizev, int32_t device, double *out) {
+  if (M > 0 && (!u || !v || !weights || !out)) return null_arg("buffer");
+  return guard([&] {
+    pg::init_weights(u, v, reinterpret_cast<const std::complex<double> *>(weights), M,
+                     oversample_factor, weighting, R, int(ftsizeu), int(ftsizev), device,
+                     reinterpret_cast<std::complex<double> *>(out));
+  });
 }
 
 }  // extern "C"

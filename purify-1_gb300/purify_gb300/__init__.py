@@ -134,6 +134,7 @@ EXPORTS = [
     "purify_gb300_server_submit", "purify_gb300_server_wait", "purify_gb300_server_request_bytes",
     "purify_gb300_server_get_stats", "purify_gb300_normal", "purify_gb300_psf_create",
     "purify_gb300_psf_apply", "purify_gb300_psf_norm", "purify_gb300_psf_destroy",
+    "purify_gb300_vis_file_rows", "purify_gb300_read_visibility", "purify_gb300_init_weights",
 ]
 STAGES = ["pad", "fft_forward", "degrid", "grid", "fold", "fft_inverse", "crop", "compact",
           "expand"]
@@ -215,6 +216,12 @@ def load(path=None):
     L.purify_gb300_psf_apply.argtypes = [vp, vp, vp, vp]
     L.purify_gb300_psf_norm.argtypes = [vp, P(ctypes.c_double)]
     L.purify_gb300_psf_destroy.argtypes = [vp]
+    L.purify_gb300_vis_file_rows.argtypes = [ctypes.c_char_p, P(ctypes.c_int64)]
+    L.purify_gb300_read_visibility.argtypes = [ctypes.c_char_p, ctypes.c_int32, ctypes.c_int64,
+                                               vp, vp, vp, vp, vp]
+    L.purify_gb300_init_weights.argtypes = [vp, vp, vp, ctypes.c_int64, ctypes.c_double,
+                                            ctypes.c_int32, ctypes.c_double, ctypes.c_uint32,
+                                            ctypes.c_uint32, ctypes.c_int32, vp]
     _lib = L
     return L
 
@@ -338,6 +345,42 @@ def _create_args(u, v, w, weights, imsizey, imsizex, oversample_ratio, power_ite
     a.precision = PRECISIONS[precision]
     a.device = int(device)
     return a, (u, v, w, wt, jw)
+
+
+WEIGHTINGS = {"none": 0, "natural": 1, "whiten": 2, "uniform": 3, "robust": 4}
+
+
+def read_visibility(path, w_term=False):
+    """utilities::read_visibility (cpp/purify/utilities.cc:140-188): a .vis
+    text file of u v [w] re im sigma rows; v negated, weights = 1 / sigma."""
+    L = load()
+    p = os.fsencode(path)
+    rows = ctypes.c_int64()
+    _check(L.purify_gb300_vis_file_rows(p, ctypes.byref(rows)))
+    n = rows.value
+    u, v, w = np.empty(n), np.empty(n), np.zeros(n)
+    vis = np.empty(n, dtype=np.complex128)
+    weights = np.empty(n, dtype=np.complex128)
+    _check(L.purify_gb300_read_visibility(p, 1 if w_term else 0, n, _np_ptr(u), _np_ptr(v),
+                                          _np_ptr(w) if w_term else None, _np_ptr(vis),
+                                          _np_ptr(weights)))
+    return {"u": u, "v": v, "w": w, "vis": vis, "weights": weights}
+
+
+def init_weights(u, v, weights, oversample_factor, weighting, R, ftsizeu, ftsizev, device=0):
+    """utilities::init_weights (cpp/purify/utilities.cc:569-608): none,
+    natural, whiten, uniform or robust visibility weights."""
+    u = np.ascontiguousarray(u, dtype=np.float64).ravel()
+    v = np.ascontiguousarray(v, dtype=np.float64).ravel()
+    wt = np.ascontiguousarray(weights, dtype=np.complex128).ravel()
+    if not (u.size == v.size == wt.size):
+        raise PurifyError(1, "u, v and weights differ in length")
+    out = np.empty_like(wt)
+    _check(load().purify_gb300_init_weights(
+        _np_ptr(u), _np_ptr(v), _np_ptr(wt), u.size, float(oversample_factor),
+        WEIGHTINGS[weighting] if isinstance(weighting, str) else int(weighting), float(R),
+        int(ftsizeu), int(ftsizev), int(device), _np_ptr(out)))
+    return out
 
 
 def _is_torch(x):

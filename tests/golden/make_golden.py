@@ -104,6 +104,12 @@ def main(ref):
         m31=img,
         m31_naxis=np.array(naxis, dtype=np.int64),
     )
+    # The first 400 rows of the reference's PADMM test coverage, unchanged,
+    # as input for the .vis reader and the weighting tests.
+    with open(os.path.join(exp, "padmm", "input_data.vis")) as f:
+        head = [next(f) for _ in range(400)]
+    with open(os.path.join(HERE, "padmm_input_head.vis"), "w") as f:
+        f.writelines(head)
 
 
 if __name__ == "__main__":
