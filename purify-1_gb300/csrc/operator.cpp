@@ -362,7 +362,14 @@ void OperatorT<real>::init_w(const OperatorConfig &cfg, int64_t &bytes, AxisTili
   rq.J = cfg.Ju;
   rq.Jw = cfg.Jw;
   rq.kernel = cfg.kernel;
-  rq.tile = cfg.tile > 0 ? cfg.tile : kTile;
+  // Default tile edge: 24 (measured fastest on the w-projection workload),
+  // widened to the largest support - 1 (a window may reach one tile ahead).
+  int smax = cfg.Jw + cfg.Ju - 1;
+  if (cfg.jw_rows) {
+    smax = 1;
+    for (int64_t m = 0; m < cfg.M; ++m) smax = std::max(smax, cfg.jw_rows[m] + cfg.Ju - 1);
+  }
+  rq.tile = cfg.tile > 0 ? cfg.tile : std::max(24, smax - 1);
   WPlan plan;
   try {
     plan = build_wplan(rq);
