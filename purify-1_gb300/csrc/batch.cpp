@@ -111,7 +111,9 @@ class BatchT final : public Batch {
   int64_t max_pixels_ = 0, max_slots_ = 0;
   Arena shared_;  // grouped task list, argument tables, padded and FFT grids
   size_t o_tasks_ = 0, o_task_base_ = 0, o_fwd_ = 0, o_adj_ = 0, o_folds_ = 0, o_io_ = 0,
-         o_partial_ = 0, o_sq_ = 0, o_inv_ = 0;
+         o_partial_ = 0, o_sq_ = 0, o_inv_ = 0, o_map_pix_ = 0, o_map_slot_ = 0, o_map_tile_ = 0;
+  // block maps of the grouped element-wise launches: {channel, block}
+  std::vector<int2> map_pix_, map_slot_, map_tile_;
   std::vector<ApplyArgs<real>> fwd_, adj_;
   std::vector<FoldArgs> folds_;
   std::vector<ChannelIO<real>> io_;
@@ -292,6 +294,17 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     g.o_pad = shared_.reserve(gb);
     g.o_work = shared_.reserve(gb);
   }
+  for (int c = 0; c < nch_; ++c) {
+    const Chan &ch = chans_[c];
+    const int64_t npix = (int64_t(ch.Nx) * ch.Ny + kGroupPixels - 1) / kGroupPixels;
+    for (int64_t k = 0; k < npix; ++k) map_pix_.push_back(int2{c, int(k)});
+    const int64_t nsl = (ch.S + kGroupSlots - 1) / kGroupSlots;
+    for (int64_t k = 0; k < nsl; ++k) map_slot_.push_back(int2{c, int(k)});
+    for (int k = 0; k < ch.ntu * ch.ntv; ++k) map_tile_.push_back(int2{c, k});
+  }
+  o_map_pix_ = shared_.reserve(sizeof(int2) * map_pix_.size());
+  o_map_slot_ = shared_.reserve(sizeof(int2) * map_slot_.size());
+  o_map_tile_ = shared_.reserve(sizeof(int2) * map_tile_.size());
   o_tasks_ = shared_.reserve(sizeof(Task) * tasks.size());
   o_task_base_ = shared_.reserve(sizeof(int32_t) * nch_);
   o_fwd_ = shared_.reserve(sizeof(ApplyArgs<real>) * nch_);
@@ -313,6 +326,12 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
   cuda_check(cudaMemcpyAsync(shared_.at<char>(o_task_base_), task_base.data(),
                              sizeof(int32_t) * nch_, cudaMemcpyHostToDevice, stream_),
              "upload");
+  for (auto m : {std::make_pair(&map_pix_, o_map_pix_), std::make_pair(&map_slot_, o_map_slot_),
+                 std::make_pair(&map_tile_, o_map_tile_)})
+    if (!m.first->empty())
+      cuda_check(cudaMemcpyAsync(shared_.at<char>(m.second), m.first->data(),
+                                 sizeof(int2) * m.first->size(), cudaMemcpyHostToDevice, stream_),
+                 "upload");
   for (SizeGroup &g : groups_) {
     int n[2] = {g.Nv, g.Nu};
     const int dist = g.Nu * g.Nv;
@@ -475,7 +494,9 @@ void BatchT<real>::record(int mode) {
     return;
   }
   if (mode & kForward) {
-    cuda_check(launch_pad_group<real>(io, nch_, max_pixels_, stream_), "pad");
+    cuda_check(launch_pad_group<real>(io, shared_.at<int2>(o_map_pix_), int(map_pix_.size()),
+                                      stream_),
+               "pad");
     for (SizeGroup &g : groups_)
       cufft_check(Traits<real>::exec(g.fft, shared_.at<C>(g.o_pad), shared_.at<C>(g.o_work),
                                      CUFFT_FORWARD),
@@ -486,18 +507,23 @@ void BatchT<real>::record(int mode) {
                "degrid");
   }
   if (mode & kAdjoint) {
-    cuda_check(launch_expand_group<real>(io, nch_, max_slots_, stream_), "expand");
+    cuda_check(launch_expand_group<real>(io, shared_.at<int2>(o_map_slot_), int(map_slot_.size()),
+                                         stream_),
+               "expand");
     head.group = shared_.at<ApplyArgs<real>>(o_adj_);
     cuda_check(launch_grid_group<real>(head, poly_, J_, ntasks_, win_rows_, win_cols_,
                                        grid_shape_, false, any_weight_, stream_),
                "grid");
-    cuda_check(launch_fold_group<real>(shared_.at<FoldArgs>(o_folds_), nch_, max_tiles_, stream_),
+    cuda_check(launch_fold_group<real>(shared_.at<FoldArgs>(o_folds_), shared_.at<int2>(o_map_tile_),
+                                       int(map_tile_.size()), stream_),
                "fold");
     for (SizeGroup &g : groups_)
       cufft_check(Traits<real>::exec(g.fft, shared_.at<C>(g.o_work), shared_.at<C>(g.o_work),
                                      CUFFT_INVERSE),
                   "cufftExec");
-    cuda_check(launch_crop_group<real>(io, nch_, max_pixels_, stream_), "crop");
+    cuda_check(launch_crop_group<real>(io, shared_.at<int2>(o_map_pix_), int(map_pix_.size()),
+                                       stream_),
+               "crop");
   }
   if (mode == kPower)
     cuda_check(launch_sq_norm_group<real>(io, nch_, shared_.at<double>(o_partial_),
@@ -733,7 +759,8 @@ void BatchT<real>::power_method(int iters, double tol, double *norms_out) {
         cuda_check(cudaMemcpyAsync(shared_.at<char>(o_inv_), inv.data(), sizeof(double) * nch_,
                                    cudaMemcpyHostToDevice, stream_),
                    "H2D");
-        cuda_check(launch_scale_group<real>(shared_.at<ChannelIO<real>>(o_io_), nch_, max_pixels_,
+        cuda_check(launch_scale_group<real>(shared_.at<ChannelIO<real>>(o_io_),
+                                            shared_.at<int2>(o_map_pix_), int(map_pix_.size()),
                                             shared_.at<double>(o_inv_), stream_),
                    "scale");
       }

@@ -14,16 +14,21 @@ namespace pg {
 namespace {
 using namespace dev;
 
+// The element-wise grouped kernels run over a block map: block b works on
+// channel map[b].x, its block map[b].y, so no block is idle whatever the
+// spread of channel sizes.
 template <typename real>
-__global__ void fold_group_kernel(const FoldArgs *__restrict__ folds) {
-  const FoldArgs &f = folds[blockIdx.y];
-  if (int(blockIdx.x) < f.ntu * f.ntv) fold_tile<real>(f, blockIdx.x);
+__global__ void fold_group_kernel(const FoldArgs *__restrict__ folds, const int2 *__restrict__ map) {
+  const int2 m = map[blockIdx.x];
+  fold_tile<real>(folds[m.x], m.y);
 }
 
 template <typename real>
-__global__ void pad_group_kernel(const ChannelIO<real> *__restrict__ chans) {
-  const ChannelIO<real> &c = chans[blockIdx.y];
-  const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+__global__ void pad_group_kernel(const ChannelIO<real> *__restrict__ chans,
+                                 const int2 *__restrict__ map) {
+  const int2 m = map[blockIdx.x];
+  const ChannelIO<real> &c = chans[m.x];
+  const int64_t idx = int64_t(m.y) * blockDim.x + threadIdx.x;
   if (idx >= int64_t(c.Nx) * c.Ny) return;
   const int j = int(idx / c.Nx), i = int(idx - int64_t(j) * c.Nx);
   const real s = c.su[i] * c.sv[j];
@@ -32,34 +37,36 @@ __global__ void pad_group_kernel(const ChannelIO<real> *__restrict__ chans) {
       cplx<real>{s * v.x, s * v.y};
 }
 template <typename real>
-__global__ void crop_group_kernel(const ChannelIO<real> *__restrict__ chans) {
-  const ChannelIO<real> &c = chans[blockIdx.y];
-  const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+__global__ void crop_group_kernel(const ChannelIO<real> *__restrict__ chans,
+                                  const int2 *__restrict__ map) {
+  const int2 m = map[blockIdx.x];
+  const ChannelIO<real> &c = chans[m.x];
+  const int64_t idx = int64_t(m.y) * blockDim.x + threadIdx.x;
   if (idx >= int64_t(c.Nx) * c.Ny) return;
   const int j = int(idx / c.Nx), i = int(idx - int64_t(j) * c.Nx);
   const real s = c.su[i] * c.sv[j];
   const cplx<real> v = static_cast<const cplx<real> *>(c.work)[int64_t(c.y0 + j) * c.Nu + c.x0 + i];
   static_cast<cplx<real> *>(c.x_out)[idx] = cplx<real>{s * v.x, s * v.y};
 }
+// slots[s] = in[slot_user[s]] (0 for null slots): a block covers 4 * 256
+// consecutive slots, four gathers in flight per thread.
 template <typename real>
-__global__ void compact_group_kernel(const ChannelIO<real> *__restrict__ chans) {
-  const ChannelIO<real> &c = chans[blockIdx.y];
-  const cplx<real> *slots = static_cast<const cplx<real> *>(c.slots);
-  cplx<real> *out = static_cast<cplx<real> *>(c.vis_out);
-  for (int64_t m = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; m < c.M;
-       m += int64_t(gridDim.x) * blockDim.x)
-    __stcs(out + m, slots[__ldcs(c.user_slot + m)]);
-}
-template <typename real>
-__global__ void expand_group_kernel(const ChannelIO<real> *__restrict__ chans) {
-  const ChannelIO<real> &c = chans[blockIdx.y];
+__global__ void expand_group_kernel(const ChannelIO<real> *__restrict__ chans,
+                                    const int2 *__restrict__ map) {
+  const int2 mm = map[blockIdx.x];
+  const ChannelIO<real> &c = chans[mm.x];
   const cplx<real> *in = static_cast<const cplx<real> *>(c.vis_in);
   cplx<real> *slots = static_cast<cplx<real> *>(c.slots);
-  for (int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; s < c.S;
-       s += int64_t(gridDim.x) * blockDim.x) {
-    const int32_t m = __ldcs(c.slot_user + s);
-    slots[s] = m >= 0 ? in[m] : cplx<real>{0, 0};
-  }
+  const int64_t s0 = int64_t(mm.y) * kGroupSlots + threadIdx.x;
+  int32_t m[4];
+  cplx<real> v[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) m[r] = s0 + r * 256 < c.S ? __ldcs(c.slot_user + s0 + r * 256) : -1;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) v[r] = m[r] >= 0 ? in[m[r]] : cplx<real>{0, 0};
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+    if (s0 + r * 256 < c.S) slots[s0 + r * 256] = v[r];
 }
 
 // Per-channel FP64 |x|^2 of the adjoint output, with the same fixed
@@ -101,18 +108,17 @@ __global__ void sq_norm_group_final(const double *__restrict__ partial, int n,
 // x_out of channel c <- x_out * inv[c].
 template <typename real>
 __global__ void scale_group_kernel(const ChannelIO<real> *__restrict__ chans,
-                                   const double *__restrict__ inv) {
-  const ChannelIO<real> &c = chans[blockIdx.y];
+                                   const int2 *__restrict__ map, const double *__restrict__ inv) {
+  const int2 m = map[blockIdx.x];
+  const ChannelIO<real> &c = chans[m.x];
+  const int64_t k = int64_t(m.y) * blockDim.x + threadIdx.x;
+  if (k >= int64_t(c.Nx) * c.Ny) return;
   cplx<real> *x = static_cast<cplx<real> *>(c.x_out);
-  const int64_t n = int64_t(c.Nx) * c.Ny;
-  const real s = real(inv[blockIdx.y]);
-  for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n;
-       k += int64_t(gridDim.x) * blockDim.x) {
-    cplx<real> v = x[k];
-    v.x *= s;
-    v.y *= s;
-    x[k] = v;
-  }
+  const real s = real(inv[m.x]);
+  cplx<real> w = x[k];
+  w.x *= s;
+  w.y *= s;
+  x[k] = w;
 }
 
 }  // namespace
@@ -138,42 +144,32 @@ cudaError_t launch_grid_group(const ApplyArgs<real> &a, const PolyTable<real> &p
 }
 
 template <typename real>
-cudaError_t launch_fold_group(const FoldArgs *folds, int nch, int max_tiles, cudaStream_t s) {
-  if (nch == 0 || max_tiles == 0) return cudaSuccess;
-  fold_group_kernel<real><<<dim3(max_tiles, nch), dim3(32, 8), 0, s>>>(folds);
+cudaError_t launch_fold_group(const FoldArgs *folds, const int2 *map, int nblocks, cudaStream_t s) {
+  if (nblocks == 0) return cudaSuccess;
+  fold_group_kernel<real><<<nblocks, dim3(32, 8), 0, s>>>(folds, map);
   return cudaGetLastError();
 }
 template <typename real>
-cudaError_t launch_pad_group(const ChannelIO<real> *chans, int nch, int64_t max_pixels,
+cudaError_t launch_pad_group(const ChannelIO<real> *chans, const int2 *map, int nblocks,
                              cudaStream_t s) {
-  if (nch == 0 || max_pixels == 0) return cudaSuccess;
-  pad_group_kernel<real><<<dim3(unsigned((max_pixels + 255) / 256), nch), 256, 0, s>>>(chans);
+  if (nblocks == 0) return cudaSuccess;
+  pad_group_kernel<real><<<nblocks, kGroupPixels, 0, s>>>(chans, map);
   return cudaGetLastError();
 }
 template <typename real>
-cudaError_t launch_crop_group(const ChannelIO<real> *chans, int nch, int64_t max_pixels,
+cudaError_t launch_crop_group(const ChannelIO<real> *chans, const int2 *map, int nblocks,
                               cudaStream_t s) {
-  if (nch == 0 || max_pixels == 0) return cudaSuccess;
-  crop_group_kernel<real><<<dim3(unsigned((max_pixels + 255) / 256), nch), 256, 0, s>>>(chans);
+  if (nblocks == 0) return cudaSuccess;
+  crop_group_kernel<real><<<nblocks, kGroupPixels, 0, s>>>(chans, map);
   return cudaGetLastError();
 }
 template <typename real>
-cudaError_t launch_compact_group(const ChannelIO<real> *chans, int nch, int64_t max_vis,
-                                 cudaStream_t s) {
-  if (nch == 0 || max_vis == 0) return cudaSuccess;
-  const int bx = std::max(1, std::min(int((max_vis + 255) / 256), 2048));
-  compact_group_kernel<real><<<dim3(bx, nch), 256, 0, s>>>(chans);
-  return cudaGetLastError();
-}
-template <typename real>
-cudaError_t launch_expand_group(const ChannelIO<real> *chans, int nch, int64_t max_slots,
+cudaError_t launch_expand_group(const ChannelIO<real> *chans, const int2 *map, int nblocks,
                                 cudaStream_t s) {
-  if (nch == 0 || max_slots == 0) return cudaSuccess;
-  const int bx = std::max(1, std::min(int((max_slots + 255) / 256), 2048));
-  expand_group_kernel<real><<<dim3(bx, nch), 256, 0, s>>>(chans);
+  if (nblocks == 0) return cudaSuccess;
+  expand_group_kernel<real><<<nblocks, 256, 0, s>>>(chans, map);
   return cudaGetLastError();
 }
-
 template <typename real>
 cudaError_t launch_sq_norm_group(const ChannelIO<real> *chans, int nch, double *partial,
                                  double *out, cudaStream_t s) {
@@ -183,11 +179,10 @@ cudaError_t launch_sq_norm_group(const ChannelIO<real> *chans, int nch, double *
   return cudaGetLastError();
 }
 template <typename real>
-cudaError_t launch_scale_group(const ChannelIO<real> *chans, int nch, int64_t max_pixels,
+cudaError_t launch_scale_group(const ChannelIO<real> *chans, const int2 *map, int nblocks,
                                const double *inv, cudaStream_t s) {
-  if (nch == 0 || max_pixels == 0) return cudaSuccess;
-  const int bx = std::max(1, std::min(int((max_pixels + 255) / 256), 2048));
-  scale_group_kernel<real><<<dim3(bx, nch), 256, 0, s>>>(chans, inv);
+  if (nblocks == 0) return cudaSuccess;
+  scale_group_kernel<real><<<nblocks, kGroupPixels, 0, s>>>(chans, map, inv);
   return cudaGetLastError();
 }
 
@@ -198,17 +193,16 @@ cudaError_t launch_scale_group(const ChannelIO<real> *chans, int nch, int64_t ma
   template cudaError_t launch_grid_group<real>(const ApplyArgs<real> &, const PolyTable<real> &,    \
                                                int, int, int, int, const LaunchShape &, bool,      \
                                                bool, cudaStream_t);                                \
-  template cudaError_t launch_fold_group<real>(const FoldArgs *, int, int, cudaStream_t);          \
-  template cudaError_t launch_pad_group<real>(const ChannelIO<real> *, int, int64_t, cudaStream_t); \
-  template cudaError_t launch_crop_group<real>(const ChannelIO<real> *, int, int64_t,              \
+  template cudaError_t launch_fold_group<real>(const FoldArgs *, const int2 *, int, cudaStream_t);  \
+  template cudaError_t launch_pad_group<real>(const ChannelIO<real> *, const int2 *, int,          \
+                                              cudaStream_t);                                       \
+  template cudaError_t launch_crop_group<real>(const ChannelIO<real> *, const int2 *, int,         \
                                                cudaStream_t);                                      \
-  template cudaError_t launch_compact_group<real>(const ChannelIO<real> *, int, int64_t,           \
-                                                  cudaStream_t);                                   \
-  template cudaError_t launch_expand_group<real>(const ChannelIO<real> *, int, int64_t,            \
+  template cudaError_t launch_expand_group<real>(const ChannelIO<real> *, const int2 *, int,       \
                                                  cudaStream_t);                                    \
   template cudaError_t launch_sq_norm_group<real>(const ChannelIO<real> *, int, double *, double *, \
                                                   cudaStream_t);                                   \
-  template cudaError_t launch_scale_group<real>(const ChannelIO<real> *, int, int64_t,             \
+  template cudaError_t launch_scale_group<real>(const ChannelIO<real> *, const int2 *, int,        \
                                                 const double *, cudaStream_t);
 
 PG_INSTANTIATE_GROUP(float)

@@ -111,17 +111,19 @@ struct ChannelIO {
   int64_t M = 0, S = 0;
 };
 
+// Grouped element-wise launches run over a block map (one int2 {channel,
+// block of that channel} per CTA): pad / crop / scale take kGroupPixels
+// pixels per block, expand kGroupSlots slots, fold one tile.
+constexpr int kGroupPixels = 256;
+constexpr int kGroupSlots = 4 * 256;
 template <typename real>
-cudaError_t launch_pad_group(const ChannelIO<real> *chans, int nch, int64_t max_pixels,
+cudaError_t launch_pad_group(const ChannelIO<real> *chans, const int2 *map, int nblocks,
                              cudaStream_t s);
 template <typename real>
-cudaError_t launch_crop_group(const ChannelIO<real> *chans, int nch, int64_t max_pixels,
+cudaError_t launch_crop_group(const ChannelIO<real> *chans, const int2 *map, int nblocks,
                               cudaStream_t s);
 template <typename real>
-cudaError_t launch_compact_group(const ChannelIO<real> *chans, int nch, int64_t max_vis,
-                                 cudaStream_t s);
-template <typename real>
-cudaError_t launch_expand_group(const ChannelIO<real> *chans, int nch, int64_t max_slots,
+cudaError_t launch_expand_group(const ChannelIO<real> *chans, const int2 *map, int nblocks,
                                 cudaStream_t s);
 // Per-channel deterministic FP64 sum of |x_out|^2 into out[c] (partial holds
 // nch * kNormBlocks doubles), and x_out <- x_out * inv[c].
@@ -129,10 +131,10 @@ template <typename real>
 cudaError_t launch_sq_norm_group(const ChannelIO<real> *chans, int nch, double *partial,
                                  double *out, cudaStream_t s);
 template <typename real>
-cudaError_t launch_scale_group(const ChannelIO<real> *chans, int nch, int64_t max_pixels,
+cudaError_t launch_scale_group(const ChannelIO<real> *chans, const int2 *map, int nblocks,
                                const double *inv, cudaStream_t s);
 template <typename real>
-cudaError_t launch_fold_group(const FoldArgs *folds, int nch, int max_tiles, cudaStream_t s);
+cudaError_t launch_fold_group(const FoldArgs *folds, const int2 *map, int nblocks, cudaStream_t s);
 
 // Z S: scaled gridding correction and zero padding.  su[i] sv[j] x[j Nx + i]
 // lands at grid[(y0 + j) Nu + x0 + i]; other grid cells are left untouched.

@@ -429,7 +429,9 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
 template <typename real>
 __device__ __forceinline__ void fold_tile(const FoldArgs &f, int t) {
   using C = cplx<real>;
-  // Launched with 32 x 8 threads: x walks the columns, y the rows of the tile.
+  // Launched with 32 x 8 threads: a thread owns column lq of a 32-column
+  // chunk and rows ty, ty + 8, ty + 16, ty + 24 of a 32-row chunk, kept in
+  // registers while the task windows are walked (outer loop over tasks).
   const int a = t / f.ntu, b = t - a * f.ntu;
   const int a2 = a == 0 ? f.ntv - 1 : a - 1;
   const int b2 = b == 0 ? f.ntu - 1 : b - 1;
@@ -447,44 +449,70 @@ __device__ __forceinline__ void fold_tile(const FoldArgs &f, int t) {
   const int64_t ss = f.slot_stride;
   const C *__restrict__ buf = static_cast<const C *>(f.tilebuf);
   C *__restrict__ grid = static_cast<C *>(f.grid);
-  for (int lp = threadIdx.y; lp < H; lp += blockDim.y) {
-    const bool up = lp < f.Jv - 1;  // uniform across a warp (one row)
-    for (int lq = threadIdx.x; lq < W; lq += blockDim.x) {
-      // own tile's task windows, then the halos of the tiles above, to the
-      // left and above-left, each in task order
-      C s{0, 0};
-      const C *p = buf + own0 * ss + lp * WWo + lq;
-      for (int k = own0; k < own1; ++k, p += ss) {
-        const C v = *p;
-        s.x += v.x;
-        s.y += v.y;
+  constexpr int R = 4;
+  for (int c0 = 0; c0 < W; c0 += 32) {
+    const int lq = c0 + int(threadIdx.x);
+    const bool col = lq < W, left = lq < f.Ju - 1;
+    for (int r0 = 0; r0 < H; r0 += 8 * R) {
+      C s[R];
+      int lp[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        s[r] = C{0, 0};
+        lp[r] = r0 + int(threadIdx.y) + 8 * r;
       }
-      const bool left = lq < f.Ju - 1;
-      if (up) {
-        p = buf + up0 * ss + (lp + Hu) * WWo + lq;
-        for (int k = up0; k < up1; ++k, p += ss) {
-          const C v = *p;
-          s.x += v.x;
-          s.y += v.y;
+      // own tile's task windows, in task order
+      for (int k = own0; k < own1; ++k) {
+        const C *w = buf + k * ss + lq;
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+          if (col && lp[r] < H) {
+            const C v = w[lp[r] * WWo];
+            s[r].x += v.x;
+            s[r].y += v.y;
+          }
+      }
+      // halo rows of the tile above, then halo columns of the tile to the
+      // left, then the corner of the tile above-left, each in task order
+      if (r0 < f.Jv - 1)
+        for (int k = up0; k < up1; ++k) {
+          const C *w = buf + k * ss + Hu * WWo + lq;
+#pragma unroll
+          for (int r = 0; r < R; ++r)
+            if (col && lp[r] < f.Jv - 1 && lp[r] < H) {
+              const C v = w[lp[r] * WWo];
+              s[r].x += v.x;
+              s[r].y += v.y;
+            }
         }
-      }
-      if (left) {
-        p = buf + lf0 * ss + lp * WWl + lq + Wl;
-        for (int k = lf0; k < lf1; ++k, p += ss) {
-          const C v = *p;
-          s.x += v.x;
-          s.y += v.y;
+      if (left)
+        for (int k = lf0; k < lf1; ++k) {
+          const C *w = buf + k * ss + lq + Wl;
+#pragma unroll
+          for (int r = 0; r < R; ++r)
+            if (lp[r] < H) {
+              const C v = w[lp[r] * WWl];
+              s[r].x += v.x;
+              s[r].y += v.y;
+            }
         }
-      }
-      if (up && left) {
-        p = buf + dg0 * ss + (lp + Hu) * WWl + lq + Wl;
-        for (int k = dg0; k < dg1; ++k, p += ss) {
-          const C v = *p;
-          s.x += v.x;
-          s.y += v.y;
+      if (left && r0 < f.Jv - 1)
+        for (int k = dg0; k < dg1; ++k) {
+          const C *w = buf + k * ss + Hu * WWl + lq + Wl;
+#pragma unroll
+          for (int r = 0; r < R; ++r)
+            if (lp[r] < f.Jv - 1 && lp[r] < H) {
+              const C v = w[lp[r] * WWl];
+              s[r].x += v.x;
+              s[r].y += v.y;
+            }
         }
+      if (col) {
+        C *g = grid + size_t(P) * f.Nu + Q + lq;
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+          if (lp[r] < H) g[size_t(lp[r]) * f.Nu] = s[r];
       }
-      grid[size_t(P + lp) * f.Nu + Q + lq] = s;
     }
   }
 }
