@@ -124,3 +124,26 @@ def test_request_errors(pg, cuda):
         srv.wait(123456)  # unknown ticket
     with pytest.raises(pg.PurifyError):
         pg.Server(slots=0)
+
+
+def test_w_projection_coverage(pg, cuda):
+    """A w-projection coverage served: the same result as the operator's host
+    entry points (the server runs the same row kernels on its workspace)."""
+    rng = np.random.default_rng(8)
+    n, M = 64, 3000
+    u = rng.normal(0, 16, M)
+    v = rng.normal(0, 16, M)
+    du = 60.0 * 60.0 * 180.0 / 1.0 / (2 * n) / np.pi
+    w = rng.uniform(-12 * du, 12 * du, M)
+    srv = pg.Server(slots=2, hbm_budget=1 << 30)
+    cid = srv.add_coverage(u, v, w, None, n, n, power_iters=5, w_term=True, Jw=6,
+                           precision="fp32")
+    op = pg.MeasurementOperator(u, v, w, None, n, n, 2.0, power_iters=5, w_term=True, Jw=6,
+                                precision="fp32")
+    x = synthetic.sky_image(n, n, seed=3)
+    r = srv.wait(srv.submit(cid, "forward_adjoint", x))
+    y = op.forward(x)
+    assert np.array_equal(r["vis"], y)
+    assert np.array_equal(r["x"], op.adjoint(y))
+    r = srv.wait(srv.submit(cid, "norm", iters=10, tol=0.0))
+    assert r["norm"] == op.power_method(10, 0.0)
