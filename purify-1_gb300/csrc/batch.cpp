@@ -106,9 +106,8 @@ class BatchT final : public Batch {
   LaunchShape degrid_shape_, grid_shape_;
   std::unique_ptr<Chan[]> chans_;
   std::vector<SizeGroup> groups_;
-  int ntasks_ = 0, win_rows_ = 0, win_cols_ = 0, max_tiles_ = 0;
+  int ntasks_ = 0, win_rows_ = 0, win_cols_ = 0;
   bool any_weight_ = false;  // some channel has a weight stream
-  int64_t max_pixels_ = 0, max_slots_ = 0;
   Arena shared_;  // grouped task list, argument tables, padded and FFT grids
   size_t o_tasks_ = 0, o_task_base_ = 0, o_fwd_ = 0, o_adj_ = 0, o_folds_ = 0, o_io_ = 0,
          o_partial_ = 0, o_sq_ = 0, o_inv_ = 0, o_map_pix_ = 0, o_map_slot_ = 0, o_map_tile_ = 0;
@@ -261,9 +260,6 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
 
     win_rows_ = std::max(win_rows_, ch.win_rows);
     win_cols_ = std::max(win_cols_, ch.win_cols);
-    max_tiles_ = std::max(max_tiles_, ch.ntu * ch.ntv);
-    max_pixels_ = std::max(max_pixels_, int64_t(ch.Nx) * ch.Ny);
-    max_slots_ = std::max(max_slots_, ch.S);
     info_.visibilities += ch.M;
     info_.pixels += int64_t(ch.Nx) * ch.Ny;
   }
