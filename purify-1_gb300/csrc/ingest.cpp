@@ -76,6 +76,10 @@ void init_weights(const double *u, const double *v, const std::complex<double> *
   }
   if (ftsizeu < 1 || ftsizev < 1) throw Error(kInvalidArgument, "empty grid");
   if (!(oversample_factor > 0)) throw Error(kInvalidArgument, "oversample_factor must be > 0");
+  for (int64_t i = 0; i < M; ++i)
+    if (!std::isfinite(u[i]) || !std::isfinite(v[i]))
+      throw Error(kInvalidArgument, "visibility " + std::to_string(i) +
+                                        " has a non-finite u or v coordinate");
   if (M == 0) return;
   DeviceGuard guard(device);
   cudaStream_t s = nullptr;

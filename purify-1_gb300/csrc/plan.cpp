@@ -47,6 +47,10 @@ Plan build_plan(const PlanRequest &rq) {
   if (rq.tile < 1 || rq.tile > 255) throw std::invalid_argument("tile edge out of range");
   if (rq.max_batches_per_task < 1 || rq.max_batches_per_task > kMaxTaskBatches)
     throw std::invalid_argument("max_batches_per_task out of range");
+  for (int64_t m = 0; m < rq.M; ++m)
+    if (!std::isfinite(rq.u[m]) || !std::isfinite(rq.v[m]))
+      throw std::invalid_argument("visibility " + std::to_string(m) +
+                                  " has a non-finite u or v coordinate");
 
   Plan P;
   P.M = rq.M;

@@ -4,6 +4,7 @@
 #include <cmath>
 #include <numeric>
 #include <stdexcept>
+#include <string>
 
 #include "gridding_kernels.h"
 
@@ -43,6 +44,10 @@ WPlan build_wplan(const WPlanRequest &rq) {
   if (rq.M > 0 && (!rq.u || !rq.v || !rq.w)) throw std::invalid_argument("u, v and w must be given");
   if (rq.J < 1 || rq.Jw < 1) throw std::invalid_argument("kernel supports must be >= 1");
   if (rq.M > int64_t(INT32_MAX) - 1) throw std::invalid_argument("too many visibilities");
+  for (int64_t m = 0; m < rq.M; ++m)
+    if (!std::isfinite(rq.u[m]) || !std::isfinite(rq.v[m]) || !std::isfinite(rq.w[m]))
+      throw std::invalid_argument("visibility " + std::to_string(m) +
+                                  " has a non-finite u, v or w coordinate");
   WPlan P;
   P.M = rq.M;
   P.Nu = rq.Nu;

@@ -171,3 +171,15 @@ def test_batch_lanes_are_bank_classes(pg):
     on_class = ((r == lane) & (cnt > 0)).sum() / (cnt > 0).sum()
     assert on_class > 0.6
     assert (cnt > 0).mean() > 0.9
+
+
+@pytest.mark.parametrize("bad", [np.nan, np.inf, -np.inf])
+def test_plan_rejects_non_finite_coordinates(pg, bad):
+    u = np.zeros(10)
+    v = np.zeros(10)
+    u[3] = bad
+    with pytest.raises(pg.PurifyError) as e:
+        pg.CoveragePlan(u, v, 64, 64, 4)
+    assert e.value.status == 1
+    with pytest.raises(pg.PurifyError):
+        pg.CoveragePlan(v, u, 64, 64, 4)

@@ -60,3 +60,10 @@ def test_host_weightings(pg, oracle_mod, kind):
     assert np.array_equal(got, ref)
     with pytest.raises(pg.PurifyError):
         pg.init_weights(d["u"], d["v"], d["weights"], 2.0, 9, 0.0, 64, 64)
+
+
+def test_weights_reject_non_finite(pg):
+    u = np.zeros(5)
+    u[2] = np.nan
+    with pytest.raises(pg.PurifyError):
+        pg.init_weights(u, np.zeros(5), np.ones(5), 2.0, "uniform", 0.0, 16, 16)
