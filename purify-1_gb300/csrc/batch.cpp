@@ -110,7 +110,8 @@ class BatchT final : public Batch {
   bool any_weight_ = false;  // some channel has a weight stream
   Arena shared_;  // grouped task list, argument tables, padded and FFT grids
   size_t o_tasks_ = 0, o_task_base_ = 0, o_fwd_ = 0, o_adj_ = 0, o_folds_ = 0, o_io_ = 0,
-         o_partial_ = 0, o_sq_ = 0, o_inv_ = 0, o_map_pix_ = 0, o_map_slot_ = 0, o_map_tile_ = 0;
+         o_partial_ = 0, o_sq_ = 0, o_inv_ = 0, o_map_pix_ = 0, o_map_slot_ = 0, o_map_tile_ = 0,
+         o_order_ = 0;
   // block maps of the grouped element-wise launches: {channel, block}
   std::vector<int2> map_pix_, map_slot_, map_tile_;
   std::vector<ApplyArgs<real>> fwd_, adj_;
@@ -156,6 +157,7 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
 
   chans_.reset(new Chan[nch_]);
   std::vector<Task> tasks;
+  std::vector<int64_t> task_cost;  // slots of each grouped task
   std::vector<int32_t> task_base(nch_);
   for (int c = 0; c < nch_; ++c) {
     const ChannelSpec &spec = cfg.channels[c];
@@ -204,6 +206,9 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     for (Task tk : plan.tasks) {
       tk.channel = c;
       tasks.push_back(tk);
+      int64_t cost = 0;
+      for (int b = tk.batch_begin; b < tk.batch_end; ++b) cost += plan.batch_kmax[b];
+      task_cost.push_back(cost);
     }
     const size_t nb = plan.batch_base.size();
     Arena &m = ch.mem;
@@ -301,6 +306,12 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
   o_map_pix_ = shared_.reserve(sizeof(int2) * map_pix_.size());
   o_map_slot_ = shared_.reserve(sizeof(int2) * map_slot_.size());
   o_map_tile_ = shared_.reserve(sizeof(int2) * map_tile_.size());
+  // Longest tasks of all channels first: the last wave of CTAs is short.
+  std::vector<int32_t> order(tasks.size());
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int32_t x, int32_t y) { return task_cost[x] > task_cost[y]; });
+  o_order_ = shared_.reserve(sizeof(int32_t) * order.size());
   o_tasks_ = shared_.reserve(sizeof(Task) * tasks.size());
   o_task_base_ = shared_.reserve(sizeof(int32_t) * nch_);
   o_fwd_ = shared_.reserve(sizeof(ApplyArgs<real>) * nch_);
@@ -315,10 +326,14 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     cuda_check(cudaMemsetAsync(shared_.at<char>(g.o_pad), 0,
                                sizeof(C) * size_t(g.Nu) * g.Nv * g.chans.size(), stream_),
                "cudaMemset");
-  if (!tasks.empty())
+  if (!tasks.empty()) {
     cuda_check(cudaMemcpyAsync(shared_.at<char>(o_tasks_), tasks.data(), sizeof(Task) * tasks.size(),
                                cudaMemcpyHostToDevice, stream_),
                "upload");
+    cuda_check(cudaMemcpyAsync(shared_.at<char>(o_order_), order.data(),
+                               sizeof(int32_t) * order.size(), cudaMemcpyHostToDevice, stream_),
+               "upload");
+  }
   cuda_check(cudaMemcpyAsync(shared_.at<char>(o_task_base_), task_base.data(),
                              sizeof(int32_t) * nch_, cudaMemcpyHostToDevice, stream_),
              "upload");
@@ -478,6 +493,7 @@ void BatchT<real>::record(int mode) {
   const ChannelIO<real> *io = shared_.at<ChannelIO<real>>(o_io_);
   ApplyArgs<real> head;
   head.tasks = shared_.at<Task>(o_tasks_);
+  head.order = shared_.at<int32_t>(o_order_);
   head.group_task_base = shared_.at<int32_t>(o_task_base_);
   if (mode == kDegridOnly || mode == kGridOnly) {  // one gridding launch alone (timing)
     const bool dg = mode == kDegridOnly;

@@ -37,6 +37,9 @@ struct ApplyArgs {
   // ApplyArgs (indexed by Task::channel) and the first task of each operator
   // in the grouped task list (its tilebuf holds windows from that index on).
   const void *group = nullptr;
+  // Launch order: CTA b runs task order[b] (longest tasks first, so the last
+  // wave is short), or task b when null.
+  const int32_t *order = nullptr;
   const int32_t *group_task_base = nullptr;
 };
 

@@ -187,7 +187,8 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
   using C = cplx<real>;
   constexpr int CH = StageDepth<real, J>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const Task tk = a0.tasks[blockIdx.x];
+  const int task_id = a0.order ? a0.order[blockIdx.x] : int(blockIdx.x);
+  const Task tk = a0.tasks[task_id];
   const auto &a = ArgsOf<real, GROUP>::get(a0, tk.channel);
   // the window in shared memory: WH rows of WW cells at row stride WS
   const int WW = tk.W + J - 1, WH = tk.H + J - 1, WS = a.win_stride;
@@ -303,7 +304,8 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
                                                    const __grid_constant__ PolyTable<real> poly) {
   using C = cplx<real>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const Task tk = a0.tasks[blockIdx.x];
+  const int task_id = a0.order ? a0.order[blockIdx.x] : int(blockIdx.x);
+  const Task tk = a0.tasks[task_id];
   const auto &a = ArgsOf<real, GROUP>::get(a0, tk.channel);
   // warp windows in shared memory: WH rows at row stride WS (WN cells each);
   // the task window written out is WH x WW, packed
@@ -409,7 +411,7 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
     }
   }
   __syncthreads();
-  const int local_task = GROUP ? int(blockIdx.x) - a0.group_task_base[tk.channel] : int(blockIdx.x);
+  const int local_task = GROUP ? task_id - a0.group_task_base[tk.channel] : task_id;
   C *out = static_cast<C *>(a.tilebuf) + size_t(local_task) * a.slot_stride;
   for (int idx = threadIdx.x; idx < WW * WH; idx += blockDim.x) {
     const int lp = idx / WW, e = idx + lp * (WS - WW);

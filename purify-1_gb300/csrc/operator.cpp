@@ -116,7 +116,7 @@ class OperatorT final : public Operator {
   bool fft_ok_ = false;
   std::mutex mu_;
 
-  DeviceBuffer frac_, weight_, slot_user_, user_slot_, batches_, lane_code_, tasks_, tile_tasks_,
+  DeviceBuffer task_order_, frac_, weight_, slot_user_, user_slot_, batches_, lane_code_, tasks_, tile_tasks_,
       tu_start_, tv_start_, tu_of_, tv_of_, su_d_, sv_d_, pad_, work_, tilebuf_, slots_,
       norm_partial_, norm_out_;
   DeviceBuffer x128_, y128_, xc_, yc_, pm_x_;
@@ -335,6 +335,8 @@ void OperatorT<real>::init_plain(const OperatorConfig &cfg, int64_t &bytes, Axis
   lane_code_.upload(plan.lane_code.data(), sizeof(int32_t) * plan.lane_code.size(), stream_);
   tasks_.alloc(sizeof(Task) * plan.tasks.size(), &bytes);
   tasks_.upload(plan.tasks.data(), sizeof(Task) * plan.tasks.size(), stream_);
+  task_order_.alloc(sizeof(int32_t) * plan.task_order.size(), &bytes);
+  task_order_.upload(plan.task_order.data(), sizeof(int32_t) * plan.task_order.size(), stream_);
   // the staging vectors are pageable: wait before they go out of scope
   cuda_check(cudaStreamSynchronize(stream_), "upload");
   tu = plan.tu;
@@ -402,6 +404,8 @@ void OperatorT<real>::init_w(const OperatorConfig &cfg, int64_t &bytes, AxisTili
   user_slot_.upload(plan.user_slot.data(), sizeof(int32_t) * M_, stream_);
   tasks_.alloc(sizeof(Task) * std::max<size_t>(plan.tasks.size(), 1), &bytes);
   tasks_.upload(plan.tasks.data(), sizeof(Task) * plan.tasks.size(), stream_);
+  task_order_.alloc(sizeof(int32_t) * std::max<size_t>(plan.task_order.size(), 1), &bytes);
+  task_order_.upload(plan.task_order.data(), sizeof(int32_t) * plan.task_order.size(), stream_);
   cuda_check(cudaStreamSynchronize(stream_), "upload");
   // Row factors, FP64-generated, uploaded in chunks of rows.
   wfactors_.alloc(sizeof(C) * std::max<int64_t>(plan.factor_count, 1), &bytes);
@@ -472,6 +476,7 @@ void OperatorT<real>::degrid_slots(const void *grid, void *caller_vis) {
     WArgs<real> w;
     w.grid = grid;
     w.tasks = tasks_.as<Task>();
+    w.order = task_order_.as<int32_t>();
     w.code = wcode_.as<int32_t>();
     w.factor = wfactor_.as<int64_t>();
     w.factors = wfactors_.get();
@@ -498,6 +503,7 @@ void OperatorT<real>::degrid_slots(const void *grid, void *caller_vis) {
   a.Nu = Nu_;
   a.Nv = Nv_;
   a.win_stride = win_stride_;
+  a.order = task_order_.as<int32_t>();
   mark_begin(kDegrid);
   cuda_check(launch_degrid<real>(a, poly_, J_, ntasks_, win_rows_, win_cols_, shape_, ws_->stream),
              "degrid");
@@ -519,6 +525,7 @@ void OperatorT<real>::grid_core(void *grid, const void *vis, const int32_t *slot
     WArgs<real> w;
     w.tilebuf = windows;
     w.tasks = tasks_.as<Task>();
+    w.order = task_order_.as<int32_t>();
     w.code = wcode_.as<int32_t>();
     w.factor = wfactor_.as<int64_t>();
     w.factors = wfactors_.get();
@@ -547,6 +554,7 @@ void OperatorT<real>::grid_core(void *grid, const void *vis, const int32_t *slot
   a.Nu = Nu_;
   a.Nv = Nv_;
   a.win_stride = win_stride_;
+  a.order = task_order_.as<int32_t>();
   a.slot_stride = slot_stride_;
   mark_begin(kGrid);
   cuda_check(launch_grid<real>(a, poly_, J_, ntasks_, win_rows_, win_cols_, shape_, ws_->stream),

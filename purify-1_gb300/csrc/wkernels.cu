@@ -95,7 +95,8 @@ template <typename real>
 __global__ void __launch_bounds__(128) wdegrid_kernel(const WArgs<real> a) {
   using C = cplx<real>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const Task tk = a.tasks[blockIdx.x];
+  const int task_id = a.order ? a.order[blockIdx.x] : int(blockIdx.x);
+  const Task tk = a.tasks[task_id];
   const int WW = tk.W + a.Smax - 1, WH = tk.H + a.Smax - 1;
   C *win = reinterpret_cast<C *>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
@@ -176,7 +177,8 @@ template <typename real>
 __global__ void __launch_bounds__(128) wgrid_kernel(const WArgs<real> a) {
   using C = cplx<real>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const Task tk = a.tasks[blockIdx.x];
+  const int task_id = a.order ? a.order[blockIdx.x] : int(blockIdx.x);
+  const Task tk = a.tasks[task_id];
   const int WW = tk.W + a.Smax - 1, WH = tk.H + a.Smax - 1, WN = WW * WH;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   C *wins = reinterpret_cast<C *>(smem_raw);
@@ -256,7 +258,7 @@ __global__ void __launch_bounds__(128) wgrid_kernel(const WArgs<real> a) {
   }
   cp_async_wait_all();
   __syncthreads();
-  C *out = static_cast<C *>(a.tilebuf) + size_t(blockIdx.x) * a.slot_stride;
+  C *out = static_cast<C *>(a.tilebuf) + size_t(task_id) * a.slot_stride;
   for (int idx = threadIdx.x; idx < WN; idx += blockDim.x) {
     C s = wins[idx];
     for (int w2 = 1; w2 < nw; ++w2) {

@@ -17,6 +17,7 @@ struct WArgs {
   const void *grid = nullptr;      // degrid input, Nv x Nu complex
   void *tilebuf = nullptr;         // grid output: one window per task
   const Task *tasks = nullptr;     // batch_begin / batch_end = visibility range
+  const int32_t *order = nullptr;  // CTA b runs task order[b], or task b when null
   const int32_t *code = nullptr;   // per visibility: lp | lq << 8 | S << 16
   const int64_t *factor = nullptr; // per visibility: first factor (complex index)
   const void *factors = nullptr;   // complex factors A_0..A_2, B_0..B_2 per row
