@@ -157,7 +157,7 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
 
   chans_.reset(new Chan[nch_]);
   std::vector<Task> tasks;
-  std::vector<int64_t> task_cost;  // slots of each grouped task
+  std::vector<int32_t> order;  // launch order of the grouped tasks
   std::vector<int32_t> task_base(nch_);
   for (int c = 0; c < nch_; ++c) {
     const ChannelSpec &spec = cfg.channels[c];
@@ -206,10 +206,10 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     for (Task tk : plan.tasks) {
       tk.channel = c;
       tasks.push_back(tk);
-      int64_t cost = 0;
-      for (int b = tk.batch_begin; b < tk.batch_end; ++b) cost += plan.batch_kmax[b];
-      task_cost.push_back(cost);
     }
+    // each channel's own launch order, channels one after the other (the
+    // tasks of one grid stay together, so its windows share L2)
+    for (int32_t k : plan.task_order) order.push_back(task_base[c] + k);
     const size_t nb = plan.batch_base.size();
     Arena &m = ch.mem;
     ch.o_frac = m.reserve(sizeof(C) * ch.S);
@@ -306,11 +306,6 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
   o_map_pix_ = shared_.reserve(sizeof(int2) * map_pix_.size());
   o_map_slot_ = shared_.reserve(sizeof(int2) * map_slot_.size());
   o_map_tile_ = shared_.reserve(sizeof(int2) * map_tile_.size());
-  // Longest tasks of all channels first: the last wave of CTAs is short.
-  std::vector<int32_t> order(tasks.size());
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int32_t x, int32_t y) { return task_cost[x] > task_cost[y]; });
   o_order_ = shared_.reserve(sizeof(int32_t) * order.size());
   o_tasks_ = shared_.reserve(sizeof(Task) * tasks.size());
   o_task_base_ = shared_.reserve(sizeof(int32_t) * nch_);

@@ -49,6 +49,9 @@ constexpr int kTile = 32;
 constexpr int kBatch = 32;
 // Most batches one CTA task may hold (its headers are staged in shared memory).
 constexpr int kMaxTaskBatches = 64;
+// Grids up to this many bytes (as complex<float>) launch their tasks longest
+// first; larger ones in spatial order (see plan.h).
+constexpr int64_t kLptGridBytes = int64_t(64) << 20;
 
 // One CTA work unit.  A tile is the rectangle [P, P+H) x [Q, Q+W) of base
 // cells; its grid window is (H + J - 1) x (W + J - 1) cells starting at (P, Q),

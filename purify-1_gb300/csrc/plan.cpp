@@ -246,13 +246,16 @@ Plan build_plan(const PlanRequest &rq) {
       P.win_cols = std::max(P.win_cols, w + rq.Ju - 1);
     }
 
-  // Longest tasks first: the last wave of CTAs is then short.
-  {
+  // Launch order.  Longest tasks first makes the last wave of CTAs short;
+  // that pays while the grid stays in L2 (<= kLptGridBytes as complex<float>).
+  // A larger grid keeps the spatial (tile) order, which reuses the halos of
+  // neighbouring windows from L2.
+  P.task_order.resize(P.tasks.size());
+  std::iota(P.task_order.begin(), P.task_order.end(), 0);
+  if (int64_t(rq.Nu) * rq.Nv * 8 <= kLptGridBytes) {
     std::vector<int64_t> cost(P.tasks.size(), 0);
     for (size_t k = 0; k < P.tasks.size(); ++k)
       for (int b = P.tasks[k].batch_begin; b < P.tasks[k].batch_end; ++b) cost[k] += P.batch_kmax[b];
-    P.task_order.resize(P.tasks.size());
-    std::iota(P.task_order.begin(), P.task_order.end(), 0);
     std::stable_sort(P.task_order.begin(), P.task_order.end(),
                      [&](int32_t x, int32_t y) { return cost[x] > cost[y]; });
   }

@@ -58,7 +58,8 @@ struct Plan {
   std::vector<int32_t> batch_base, batch_kmax;
   std::vector<int32_t> lane_code;  // batch * 32 + lane -> item_pack(lp, lq, count)
   std::vector<Task> tasks;
-  // Launch order of the tasks: by decreasing slot count (longest first).
+  // Launch order of the tasks: by decreasing slot count (longest first) when
+  // the grid is at most kLptGridBytes, else the tile order.
   std::vector<int32_t> task_order;
   std::vector<int32_t> tile_tasks;  // ntiles + 1 offsets into tasks
   int win_rows = 0, win_cols = 0;   // largest window: (H + Jv - 1) x (W + Ju - 1)

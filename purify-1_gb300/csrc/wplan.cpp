@@ -166,16 +166,17 @@ WPlan build_wplan(const WPlanRequest &rq) {
     P.win_cols = std::max(P.win_cols, P.tu.start[b + 1] - P.tu.start[b] + Smax - 1);
     i = e;
   }
-  // Longest tasks (in taps) first: the last wave of CTAs is short.
-  {
+  // Launch order: longest tasks (in taps) first while the grid stays in L2,
+  // else the spatial order (see build_plan).
+  P.task_order.resize(P.tasks.size());
+  std::iota(P.task_order.begin(), P.task_order.end(), 0);
+  if (int64_t(rq.Nu) * rq.Nv * 8 <= kLptGridBytes) {
     std::vector<int64_t> cost(P.tasks.size(), 0);
     for (size_t k = 0; k < P.tasks.size(); ++k)
       for (int i = P.tasks[k].batch_begin; i < P.tasks[k].batch_end; ++i) {
         const int64_t S = P.code[i] >> 16;
         cost[k] += S * S;
       }
-    P.task_order.resize(P.tasks.size());
-    std::iota(P.task_order.begin(), P.task_order.end(), 0);
     std::stable_sort(P.task_order.begin(), P.task_order.end(),
                      [&](int32_t x, int32_t y) { return cost[x] > cost[y]; });
   }

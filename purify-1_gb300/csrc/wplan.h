@@ -50,7 +50,7 @@ struct WPlan {
   int kernel = kKB;
   double oversample_ratio = 2.0, du_lambda = 0.0, dv_lambda = 0.0;
   std::vector<Task> tasks;  // batch_begin / batch_end = visibility range in plan order
-  std::vector<int32_t> task_order;  // launch order: by decreasing taps (longest first)
+  std::vector<int32_t> task_order;  // launch order: by decreasing taps, or tile order (see plan.h)
   std::vector<int32_t> tile_tasks;
   int win_rows = 0, win_cols = 0;
   int64_t taps = 0;  // sum of S^2
