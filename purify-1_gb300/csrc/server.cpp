@@ -6,6 +6,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <new>
 #include <string>
 
 #include "device_kernels.h"
@@ -366,6 +367,14 @@ void Server::launch(Job &j, Slot &slot) {
     // Nothing will call back: retire now.  Work already enqueued finishes
     // before the stream-ordered free.
     j.status = int(e.status);
+    j.t_done = Clock::now();
+    finish(j);
+  } catch (const std::bad_alloc &) {
+    j.status = kOutOfMemory;
+    j.t_done = Clock::now();
+    finish(j);
+  } catch (...) {
+    j.status = kInternal;
     j.t_done = Clock::now();
     finish(j);
   }
