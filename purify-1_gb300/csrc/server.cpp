@@ -137,17 +137,24 @@ int Server::add_coverage(const OperatorConfig &cfg_in) {
     }
     s->plans[key] = h;
   }
+  std::lock_guard<std::mutex> ck(cov_mu_);
   coverages_.push_back(std::move(c));
   return int(coverages_.size()) - 1;
+}
+
+// Coverages are only ever appended and live as long as the server, so the
+// reference stays valid after the lock is released.
+const Server::Coverage &Server::coverage(int id) const {
+  std::lock_guard<std::mutex> ck(cov_mu_);
+  if (id < 0 || id >= int(coverages_.size())) throw Error(kInvalidArgument, "unknown coverage");
+  return *coverages_[size_t(id)];
 }
 
 // Device layout of a request, 256-byte aligned pieces: complex<double> I/O
 // vectors, their working-precision copies (FP32 only), the workspace, and the
 // power-method vectors.
 int64_t Server::request_bytes(const Request &rq) const {
-  if (rq.coverage < 0 || rq.coverage >= int(coverages_.size()))
-    throw Error(kInvalidArgument, "unknown coverage");
-  const Coverage &c = *coverages_[rq.coverage];
+  const Coverage &c = coverage(rq.coverage);
   const size_t cs = c.fp64 ? 16 : 8;
   size_t b = up256(size_t(c.ws.pad)) + up256(size_t(c.ws.work)) + up256(size_t(c.ws.tilebuf)) +
              up256(size_t(c.ws.slots));
@@ -186,7 +193,7 @@ void Server::unpin(void *p, size_t bytes) {
 int64_t Server::submit(const Request &rq) {
   if (rq.kind < kReqForward || rq.kind > kReqNorm) throw Error(kInvalidArgument, "unknown request kind");
   const int64_t need = request_bytes(rq);
-  const Coverage &c = *coverages_[rq.coverage];
+  const Coverage &c = coverage(rq.coverage);
   const bool fwd = rq.kind == kReqForward || rq.kind == kReqForwardAdjoint;
   const bool adj = rq.kind == kReqAdjoint || rq.kind == kReqForwardAdjoint;
   if (fwd && (!rq.x_in || (c.M > 0 && !rq.vis_out)))
@@ -285,7 +292,7 @@ void Server::loop() {
 }
 
 void Server::launch(Job &j, Slot &slot) {
-  const Coverage &c = *coverages_[j.rq.coverage];
+  const Coverage &c = coverage(j.rq.coverage);
   j.slot = &slot;
   j.t_admit = Clock::now();
   slot.busy = true;
@@ -387,7 +394,7 @@ void Server::finish(Job &j) {
   slot.busy = false;
   bytes_in_use_ -= j.bytes;
   --inflight_;
-  const Coverage &c = *coverages_[j.rq.coverage];
+  const Coverage &c = coverage(j.rq.coverage);
   if (j.status == kOk && j.rq.kind == kReqNorm) {
     // the single-operator stopping rule on the recorded estimates
     const double *sq = static_cast<const double *>(j.host_out);
@@ -434,7 +441,7 @@ bool Server::wait(int64_t ticket, double timeout_s, RequestResult *out) {
       return false;
     jobs_.erase(ticket);
   }
-  const Coverage &c = *coverages_[j->rq.coverage];
+  const Coverage &c = coverage(j->rq.coverage);
   if (j->status == kOk && j->rq.kind != kReqNorm) {
     const char *src = static_cast<const char *>(j->host_out);
     if (j->rq.kind != kReqAdjoint && c.M > 0) {

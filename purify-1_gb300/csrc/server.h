@@ -99,7 +99,9 @@ class Server {
   void unpin(void *p, size_t bytes);
 
   ServerConfig cfg_;
-  std::vector<std::unique_ptr<Coverage>> coverages_;
+  const Coverage &coverage(int id) const;
+  std::vector<std::unique_ptr<Coverage>> coverages_;  // appended under cov_mu_
+  mutable std::mutex cov_mu_;
   std::vector<std::unique_ptr<Slot>> slots_;
   cudaMemPool_t pool_ = nullptr;
   std::map<int64_t, std::shared_ptr<Job>> jobs_;
