@@ -91,7 +91,6 @@ class Server {
   struct Slot;
   struct Coverage;
   void loop();
-  bool try_admit(Job &job);
   void launch(Job &job, Slot &slot);
   void finish(Job &job);
   static void CUDART_CB on_done(void *job);
