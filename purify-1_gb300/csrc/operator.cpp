@@ -7,7 +7,10 @@
 #include <complex>
 #include <cstring>
 #include <functional>
+#include <map>
 #include <mutex>
+#include <set>
+#include <tuple>
 #include <vector>
 
 #include "device_kernels.h"
@@ -130,6 +133,12 @@ class OperatorT final : public Operator {
     return ws_->unit_norm ? su_unit_d_.as<real>() : su_d_.as<real>();
   }
   void with_workspace(const Workspace &ws, const std::function<void()> &f);
+  // Recorded applies on the operator's own scratch (see run_recorded).
+  using GraphKey = std::tuple<int, const void *, const void *>;
+  std::map<GraphKey, cudaGraphExec_t> graphs_;
+  std::set<GraphKey> seen_;
+  void run_recorded(int kind, const void *in, void *out, const std::function<void()> &enqueue);
+  void drop_graphs();
 };
 
 template <typename real>
@@ -429,6 +438,7 @@ void OperatorT<real>::init_w(const OperatorConfig &cfg, int64_t &bytes, AxisTili
 template <typename real>
 OperatorT<real>::~OperatorT() {
   if (stream_) cudaStreamSynchronize(stream_);
+  drop_graphs();
   for (cudaEvent_t e : event_pool_) cudaEventDestroy(e);
   if (fft_ok_) cufftDestroy(fft_);
   if (ev_in_) cudaEventDestroy(ev_in_);
@@ -724,8 +734,10 @@ void OperatorT<real>::normal(const void *x, void *out, cudaStream_t user) {
   DeviceGuard guard(device_);
   std::lock_guard<std::mutex> lock(mu_);
   join(user);
-  forward_slots(x);
-  adjoint_slots(out);
+  run_recorded(3, x, out, [&] {
+    forward_slots(x);
+    adjoint_slots(out);
+  });
   release(user);
 }
 
@@ -779,12 +791,61 @@ void OperatorT<real>::grid_no_alloc(const void *vis, void *grid, cudaStream_t us
   release(user);
 }
 
+// Applies on the operator's own scratch are recorded into a CUDA graph the
+// second time they are made with the same buffers and replayed from then on:
+// the chain's launches are then one graph launch.  The graph holds the
+// buffer addresses only; everything else it reads (coverage state, the
+// correction and norm) is read from device memory when it runs.
+template <typename real>
+void OperatorT<real>::run_recorded(int kind, const void *in, void *out,
+                                   const std::function<void()> &enqueue) {
+  if (timing_ || ws_ != &own_) {
+    enqueue();
+    return;
+  }
+  const GraphKey key{kind, in, out};
+  auto it = graphs_.find(key);
+  if (it != graphs_.end()) {
+    cuda_check(cudaGraphLaunch(it->second, stream_), "cudaGraphLaunch");
+    return;
+  }
+  if (!seen_.count(key)) {
+    seen_.insert(key);
+    if (seen_.size() > 64) seen_.clear();
+    enqueue();
+    return;
+  }
+  if (graphs_.size() >= 16) drop_graphs();
+  cudaGraph_t g = nullptr;
+  cuda_check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "capture");
+  try {
+    enqueue();
+  } catch (...) {
+    cudaStreamEndCapture(stream_, &g);
+    if (g) cudaGraphDestroy(g);
+    throw;
+  }
+  cuda_check(cudaStreamEndCapture(stream_, &g), "capture");
+  cudaGraphExec_t e = nullptr;
+  const cudaError_t r = cudaGraphInstantiate(&e, g, 0);
+  cudaGraphDestroy(g);
+  cuda_check(r, "cudaGraphInstantiate");
+  graphs_[key] = e;
+  cuda_check(cudaGraphLaunch(e, stream_), "cudaGraphLaunch");
+}
+
+template <typename real>
+void OperatorT<real>::drop_graphs() {
+  for (auto &kv : graphs_) cudaGraphExecDestroy(kv.second);
+  graphs_.clear();
+}
+
 template <typename real>
 void OperatorT<real>::forward(const void *x, void *y, cudaStream_t user) {
   DeviceGuard guard(device_);
   std::lock_guard<std::mutex> lock(mu_);
   join(user);
-  forward_on_stream(x, y);
+  run_recorded(1, x, y, [&] { forward_on_stream(x, y); });
   release(user);
 }
 template <typename real>
@@ -792,7 +853,7 @@ void OperatorT<real>::adjoint(const void *y, void *x, cudaStream_t user) {
   DeviceGuard guard(device_);
   std::lock_guard<std::mutex> lock(mu_);
   join(user);
-  adjoint_on_stream(y, x);
+  run_recorded(2, y, x, [&] { adjoint_on_stream(y, x); });
   release(user);
 }
 

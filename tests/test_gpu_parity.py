@@ -269,3 +269,36 @@ def test_operators_with_different_kernels_interleaved(pg, oracle_mod, cuda):
     torch.cuda.synchronize()
     for k, y, _ in outs:
         assert rel_l2(to_np(y), refs[k].forward(x)) < 1e-5
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_recorded_applies(pg, cuda, precision):
+    """Repeated applies on the same buffers are recorded into a CUDA graph and
+    replayed: the results stay bit-identical to the first (direct) apply, and
+    a later set_norm is honoured by the replays."""
+    torch = cuda
+    from purify_gb300 import synthetic
+    c = synthetic.config_small()
+    op = pg.MeasurementOperator(c["u"][:20000], c["v"][:20000], None, None, 256, 256, 2.0,
+                                power_iters=0, precision=precision)
+    x = to_dev(torch, c["x"], precision)
+    y = torch.empty(20000, dtype=op.complex_dtype, device="cuda")
+    xo = torch.empty_like(x)
+    nz = torch.empty_like(x)
+    first_y = first_x = first_n = None
+    for k in range(5):
+        op.forward_into(x, y)
+        op.adjoint_into(y, xo)
+        op.normal_into(x, nz)
+        torch.cuda.synchronize()
+        if k == 0:
+            first_y, first_x, first_n = y.clone(), xo.clone(), nz.clone()
+        else:
+            assert torch.equal(y, first_y) and torch.equal(xo, first_x) and torch.equal(nz, first_n)
+    op.set_norm(2.0)
+    for _ in range(3):
+        op.forward_into(x, y)
+        op.normal_into(x, nz)
+    torch.cuda.synchronize()
+    assert rel_l2(to_np(y), to_np(first_y) / 2.0) < 1e-6
+    assert rel_l2(to_np(nz), to_np(first_n) / 4.0) < 1e-6
