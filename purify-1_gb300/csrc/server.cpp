@@ -267,7 +267,10 @@ void Server::loop() {
       finish(*j);
     }
     // Admission: first come first served, but a request that fits may
-    // overtake a head that does not (a bounded number of times).
+    // overtake a head that does not (a bounded number of times).  Slots and
+    // bytes are reserved under the lock; the launches are enqueued without
+    // it, so submit() and completions are not held up by a long request.
+    std::vector<Job *> admitted;
     auto it = pending_.begin();
     while (it != pending_.end()) {
       Slot *free = nullptr;
@@ -280,19 +283,27 @@ void Server::loop() {
       Job &j = **it;
       if (bytes_in_use_ + j.bytes <= cfg_.hbm_budget) {
         if (it != pending_.begin()) ++pending_.front()->overtaken;
-        launch(j, *free);
+        reserve(j, *free);
+        admitted.push_back(&j);
         it = pending_.erase(it);
         continue;
       }
       if (pending_.front()->overtaken >= kMaxOvertakes) break;
       ++it;
     }
+    if (!admitted.empty()) {
+      lk.unlock();
+      std::vector<Job *> failed;
+      for (Job *j : admitted)
+        if (!enqueue(*j)) failed.push_back(j);
+      lk.lock();
+      for (Job *j : failed) finish(*j);
+    }
     if (stop_ && pending_.empty() && inflight_ == 0) break;
   }
 }
 
-void Server::launch(Job &j, Slot &slot) {
-  const Coverage &c = coverage(j.rq.coverage);
+void Server::reserve(Job &j, Slot &slot) {
   j.slot = &slot;
   j.t_admit = Clock::now();
   slot.busy = true;
@@ -300,6 +311,14 @@ void Server::launch(Job &j, Slot &slot) {
   ++inflight_;
   stats_.bytes_peak = std::max(stats_.bytes_peak, bytes_in_use_);
   stats_.inflight_peak = std::max(stats_.inflight_peak, inflight_);
+}
+
+// Enqueues the request's copies and kernels on its slot's stream (called
+// without the server lock).  Returns false if enqueueing failed; the caller
+// then retires the job.
+bool Server::enqueue(Job &j) {
+  const Coverage &c = coverage(j.rq.coverage);
+  Slot &slot = *j.slot;
   cudaStream_t s = slot.stream;
   try {
     cuda_check(cudaMallocFromPoolAsync(&j.dev, size_t(j.bytes), pool_, s), "request memory");
@@ -370,21 +389,18 @@ void Server::launch(Job &j, Slot &slot) {
       }
     }
     cuda_check(cudaLaunchHostFunc(s, &Server::on_done, &j), "cudaLaunchHostFunc");
+    return true;
   } catch (const Error &e) {
-    // Nothing will call back: retire now.  Work already enqueued finishes
-    // before the stream-ordered free.
+    // Nothing will call back: the caller retires the job.  Work already
+    // enqueued finishes before the stream-ordered free.
     j.status = int(e.status);
-    j.t_done = Clock::now();
-    finish(j);
   } catch (const std::bad_alloc &) {
     j.status = kOutOfMemory;
-    j.t_done = Clock::now();
-    finish(j);
   } catch (...) {
     j.status = kInternal;
-    j.t_done = Clock::now();
-    finish(j);
   }
+  j.t_done = Clock::now();
+  return false;
 }
 
 void Server::finish(Job &j) {

@@ -91,7 +91,8 @@ class Server {
   struct Slot;
   struct Coverage;
   void loop();
-  void launch(Job &job, Slot &slot);
+  void reserve(Job &job, Slot &slot);
+  bool enqueue(Job &job);
   void finish(Job &job);
   static void CUDART_CB on_done(void *job);
   void *pinned(size_t bytes);
