@@ -28,6 +28,27 @@ struct Cplx<double> {
 template <typename real>
 using cplx = typename Cplx<real>::type;
 
+// Component-wise complex arithmetic.  For float these are Blackwell's paired
+// FP32 instructions (one instruction for both components, each component
+// rounded exactly as fmaf / fadd / fmul), for double two scalar operations:
+// either way the result is bit-identical to the scalar form.
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ double2 fma2(double2 a, double2 b, double2 c) {
+  return make_double2(fma(a.x, b.x, c.x), fma(a.y, b.y, c.y));
+}
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ double2 add2(double2 a, double2 b) {
+  return make_double2(a.x + b.x, a.y + b.y);
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ double2 mul2(double2 a, double2 b) {
+  return make_double2(a.x * b.x, a.y * b.y);
+}
+template <typename real>
+__device__ __forceinline__ cplx<real> splat(real k) {
+  return cplx<real>{k, k};
+}
+
 // Tap weights of one axis by Horner's rule.  With SUB = false every lane
 // reads the same coefficient at the same time, so the coefficients come
 // straight from the constant bank of the kernel parameters.  Every kernel of
@@ -262,18 +283,15 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
       real ku[J], kv[J];
       tap_weights<real, J, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
       tap_weights<real, J, SUB>(poly.v, poly.nsub_v, t.y, kv);
-      real sr = 0, si = 0;
+      C sum{0, 0};
 #pragma unroll
       for (int jv = 0; jv < J; ++jv) {
-        real rr = 0, ri = 0;
+        C row{0, 0};
 #pragma unroll
-        for (int ju = 0; ju < J; ++ju) {
-          rr = fma(ku[ju], F[jv][ju].x, rr);
-          ri = fma(ku[ju], F[jv][ju].y, ri);
-        }
-        sr = fma(kv[jv], rr, sr);
-        si = fma(kv[jv], ri, si);
+        for (int ju = 0; ju < J; ++ju) row = fma2(splat(ku[ju]), F[jv][ju], row);
+        sum = fma2(splat(kv[jv]), row, sum);
       }
+      const real sr = sum.x, si = sum.y;
       C y;
       if (unit) {
         const real sg = copysign(real(1), t.x);
@@ -375,14 +393,12 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
       real ku[J], kv[J];
       tap_weights<real, J, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
       tap_weights<real, J, SUB>(poly.v, poly.nsub_v, t.y, kv);
+      const C z{zr, zi};
 #pragma unroll
       for (int jv = 0; jv < J; ++jv) {
-        const real ar = zr * kv[jv], ai = zi * kv[jv];
+        const C az = mul2(z, splat(kv[jv]));
 #pragma unroll
-        for (int ju = 0; ju < J; ++ju) {
-          acc[jv][ju].x = fma(ar, ku[ju], acc[jv][ju].x);
-          acc[jv][ju].y = fma(ai, ku[ju], acc[jv][ju].y);
-        }
+        for (int ju = 0; ju < J; ++ju) acc[jv][ju] = fma2(az, splat(ku[ju]), acc[jv][ju]);
       }
       if (ck + 1 >= th.hdr[clb].y) {
         // Flush at the end of the batch.  The items of one batch have
@@ -398,10 +414,7 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
           for (int ju = 0; ju < J; ++ju) {
             if (cnt > 0) {
               C *cell = mine + (lp + jv) * WS + lq + ju;
-              C c = *cell;
-              c.x += acc[jv][ju].x;
-              c.y += acc[jv][ju].y;
-              *cell = c;
+              *cell = add2(*cell, acc[jv][ju]);
             }
             acc[jv][ju] = C{0, 0};
             __syncwarp();
