@@ -261,14 +261,14 @@ int purify_gb300_wrow_taps(double u, double v, double w_centered, uint32_t Jw, u
       throw pg::Error(pg::kInvalidArgument, e.what());
     }
     const int64_t i = p.user_slot[0];
-    const int S = (p.code[i] >> 16) & 0xff;
-    std::vector<std::complex<double>> f(6 * S);
+    const int S = pg::wrow_support(p.code[i]), rank = pg::wrow_rank(p.code[i]);
+    std::vector<std::complex<double>> f(2 * rank * S);
     pg::wplan_factors<double>(p, i, i + 1, f.data());
     const std::complex<double> sgn = p.weight[i];  // +-1: (-1)^(kw_u + kw_v)
     for (int jv = 0; jv < S; ++jv)
       for (int ju = 0; ju < S; ++ju) {
         std::complex<double> k = 0;
-        for (int r = 0; r < 3; ++r) k += f[r * S + jv] * f[(3 + r) * S + ju];
+        for (int r = 0; r < rank; ++r) k += f[r * S + jv] * f[(rank + r) * S + ju];
         k *= sgn;
         out[2 * (jv * S + ju)] = k.real();
         out[2 * (jv * S + ju) + 1] = k.imag();

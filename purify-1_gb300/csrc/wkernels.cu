@@ -1,7 +1,8 @@
 // sm_103a kernels of the w-projection gridding operator (G and G^H with one
 // kernel row per visibility).  Row m's S x S taps are rebuilt on the fly from
 // its stored rank-3 factors, K = A_0 B_0^T + A_1 B_1^T + A_2 B_2^T
-// (wplan.h).  One warp handles one visibility at a time; lane l covers row
+// (wplan.h), over the row's nonzero terms only (rank 1 to 3, from the row
+// code).  One warp handles one visibility at a time; lane l covers row
 // r = l / S of each group of R = 32 / S rows and column c = l % S, two row
 // groups per step.
 #include <cuda_runtime.h>
@@ -61,6 +62,29 @@ __device__ __forceinline__ void cp_async_wait_one() {
 // are on their way into the other half of the warp's factor buffer
 // (cp.async), and the code, factor offset, weight and visibility of the one
 // after that are being loaded into registers.
+// Stored factor terms of a row: the popcount of the code's term mask.
+__device__ __forceinline__ int row_rank(int code) { return __popc((code >> 24) & 7); }
+
+// Tap (row j, the lane's column) of a row: sum over the stored terms of
+// A_e[j] b[e], with b[e] = B_e[column] held by the lane.  The rank is the same
+// for the whole warp (one visibility).
+template <typename C>
+__device__ __forceinline__ C row_tap(const C *fbuf, int S, int rank, int j, const C (&b)[3]) {
+  C k = cmul(fbuf[j], b[0]);
+  if (rank > 1) cfma(k, fbuf[S + j], b[1]);
+  if (rank > 2) cfma(k, fbuf[2 * S + j], b[2]);
+  return k;
+}
+template <typename C>
+__device__ __forceinline__ void column_factors(const C *fbuf, int S, int rank, int c, bool active,
+                                               C (&b)[3]) {
+  b[0] = b[1] = b[2] = C{0, 0};
+  if (!active) return;
+  b[0] = fbuf[rank * S + c];
+  if (rank > 1) b[1] = fbuf[(rank + 1) * S + c];
+  if (rank > 2) b[2] = fbuf[(rank + 2) * S + c];
+}
+
 template <typename real>
 struct WPipe {
   using C = cplx<real>;
@@ -82,10 +106,10 @@ struct WPipe {
   }
   __device__ __forceinline__ void issue(int i, int code, int64_t off, int buf) {
     if (i < end) {
-      const int S = (code >> 16) & 0xff;
+      const int n = 2 * row_rank(code) * ((code >> 16) & 0xff);
       const C *src = static_cast<const C *>(a.factors) + off;
       C *dst = fb + buf * 6 * a.Smax;
-      for (int k = lane; k < 6 * S; k += 32) cp_async<sizeof(C)>(dst + k, src + k);
+      for (int k = lane; k < n; k += 32) cp_async<sizeof(C)>(dst + k, src + k);
     }
     cp_async_commit();
   }
@@ -129,29 +153,16 @@ __global__ void __launch_bounds__(128) wdegrid_kernel(const WArgs<real> a) {
     __syncwarp();  // every lane's factor copies for visibility i have landed
     const C *fbuf = fb + buf * 6 * a.Smax;
     const int lp = code0 & 0xff, lq = (code0 >> 8) & 0xff, S = (code0 >> 16) & 0xff;
+    const int rank = row_rank(code0);
     const int R = 32 / S, r = lane / S, c = lane - r * S;
     const bool active = r < R;
-    C b0{0, 0}, b1{0, 0}, b2{0, 0};
-    if (active) {
-      b0 = fbuf[3 * S + c];
-      b1 = fbuf[4 * S + c];
-      b2 = fbuf[5 * S + c];
-    }
+    C b[3];
+    column_factors(fbuf, S, rank, c, active, b);
     C acc{0, 0}, acc2{0, 0};
     for (int jv0 = 0; jv0 < S; jv0 += 2 * R) {
       const int ja = jv0 + r, jb = jv0 + R + r;
-      if (active && ja < S) {
-        C k = cmul(fbuf[ja], b0);
-        cfma(k, fbuf[S + ja], b1);
-        cfma(k, fbuf[2 * S + ja], b2);
-        cfma(acc, k, win[(lp + ja) * WW + lq + c]);
-      }
-      if (active && jb < S) {
-        C k = cmul(fbuf[jb], b0);
-        cfma(k, fbuf[S + jb], b1);
-        cfma(k, fbuf[2 * S + jb], b2);
-        cfma(acc2, k, win[(lp + jb) * WW + lq + c]);
-      }
+      if (active && ja < S) cfma(acc, row_tap(fbuf, S, rank, ja, b), win[(lp + ja) * WW + lq + c]);
+      if (active && jb < S) cfma(acc2, row_tap(fbuf, S, rank, jb, b), win[(lp + jb) * WW + lq + c]);
     }
     acc.x += acc2.x;
     acc.y += acc2.y;
@@ -202,16 +213,13 @@ __global__ void __launch_bounds__(128) wgrid_kernel(const WArgs<real> a) {
     __syncwarp();  // every lane's factor copies for visibility i have landed
     const C *fbuf = fb + buf * 6 * a.Smax;
     const int lp = code0 & 0xff, lq = (code0 >> 8) & 0xff, S = (code0 >> 16) & 0xff;
+    const int rank = row_rank(code0);
     // conj(weight) * y: G^H holds the conjugated entries of G
     const C z{w0.x * y0.x + w0.y * y0.y, w0.x * y0.y - w0.y * y0.x};
     const int R = 32 / S, r = lane / S, c = lane - r * S;
     const bool active = r < R;
-    C b0{0, 0}, b1{0, 0}, b2{0, 0};
-    if (active) {
-      b0 = fbuf[3 * S + c];
-      b1 = fbuf[4 * S + c];
-      b2 = fbuf[5 * S + c];
-    }
+    C b[3];
+    column_factors(fbuf, S, rank, c, active, b);
     // All S^2 cells of one visibility are distinct, so the lanes never touch
     // the same cell within it, and the two rows a lane updates per step are
     // different cells; visibilities are ordered by __syncwarp.
@@ -222,15 +230,11 @@ __global__ void __launch_bounds__(128) wgrid_kernel(const WArgs<real> a) {
       C *ca = mine + (lp + ja) * WW + lq + c;
       C *cb = mine + (lp + jb) * WW + lq + c;
       if (oka) {
-        ka = cmul(fbuf[ja], b0);
-        cfma(ka, fbuf[S + ja], b1);
-        cfma(ka, fbuf[2 * S + ja], b2);
+        ka = row_tap(fbuf, S, rank, ja, b);
         va = *ca;
       }
       if (okb) {
-        kb = cmul(fbuf[jb], b0);
-        cfma(kb, fbuf[S + jb], b1);
-        cfma(kb, fbuf[2 * S + jb], b2);
+        kb = row_tap(fbuf, S, rank, jb, b);
         vb = *cb;
       }
       // conj(K) z

@@ -37,6 +37,25 @@ void conv1d(const double *f, int Jf, const std::complex<double> *g, int Jg,
     out[j] = acc;
   }
 }
+
+// Which of the three terms of a row's sample matrix
+//   g = (a~ / (w i)) b~^T + (1 - chi_v) 1^T + chi_v (1 - chi_u)^T
+// are nonzero (bit r for term r), from the validity masks chi of
+// projection_kernels.cc:38-45 at the row's Jw sample offsets.  A term that is
+// zero here is exactly zero, so leaving it out changes no tap.
+int row_terms(double u, double v, double w, int Jw, double dul, double dvl) {
+  const double dwu = u - std::floor(u - Jw * 0.5), dwv = v - std::floor(v - Jw * 0.5);
+  bool any_u = false, all_u = true, any_v = false, all_v = true;
+  for (int k = 0; k < Jw; ++k) {
+    const double U = dwu - k - 1, V = dwv - k - 1;
+    const bool ok_u = std::abs(U * dul / w) < 1, ok_v = std::abs(V * dvl / w) < 1;
+    any_u |= ok_u;
+    all_u &= ok_u;
+    any_v |= ok_v;
+    all_v &= ok_v;
+  }
+  return int(any_v && any_u) | int(!all_v) << 1 | int(any_v && !all_u) << 2;
+}
 }  // namespace
 
 WPlan build_wplan(const WPlanRequest &rq) {
@@ -100,6 +119,8 @@ WPlan build_wplan(const WPlanRequest &rq) {
     if (tile[x] != tile[y]) return tile[x] < tile[y];
     return jw[x] > jw[y];
   });
+  P.du_lambda = pixel_to_lambda(rq.cellx, rq.imsizex, rq.oversample_ratio);
+  P.dv_lambda = pixel_to_lambda(rq.celly, rq.imsizey, rq.oversample_ratio);
   P.code.resize(M);
   P.factor.resize(M);
   P.weight.resize(M);
@@ -110,9 +131,10 @@ WPlan build_wplan(const WPlanRequest &rq) {
     const int32_t m = order[i];
     const int S = jw[m] + rq.J - 1;
     const int lp = local[m] >> 8, lq = local[m] & 0xff;  // item_pack layout below
-    P.code[i] = lp | (lq << 8) | (S << 16);
+    const int terms = row_terms(rq.u[m], rq.v[m], rq.w[m] - wmean, jw[m], P.du_lambda, P.dv_lambda);
+    P.code[i] = lp | (lq << 8) | (S << 16) | (terms << 24);
     P.factor[i] = off;
-    off += int64_t(6) * S;
+    off += int64_t(2) * wrow_rank(P.code[i]) * S;
     const std::complex<double> wgt = rq.weights ? rq.weights[m] : std::complex<double>(1.0, 0.0);
     P.weight[i] = flip[m] ? -wgt : wgt;
     P.slot_user[i] = m;
@@ -122,8 +144,6 @@ WPlan build_wplan(const WPlanRequest &rq) {
   P.factor_count = off;
   P.kernel = rq.kernel;
   P.oversample_ratio = rq.oversample_ratio;
-  P.du_lambda = pixel_to_lambda(rq.cellx, rq.imsizex, rq.oversample_ratio);
-  P.dv_lambda = pixel_to_lambda(rq.celly, rq.imsizey, rq.oversample_ratio);
   P.gen_u.resize(M);
   P.gen_v.resize(M);
   P.gen_w.resize(M);
@@ -146,8 +166,8 @@ WPlan build_wplan(const WPlanRequest &rq) {
     int64_t s = i;
     while (s < e) {
       int64_t k = s, taps = 0;
-      while (k < e && (k == s || taps + (P.code[k] >> 16) * (P.code[k] >> 16) <= rq.max_taps_per_task)) {
-        taps += int64_t(P.code[k] >> 16) * (P.code[k] >> 16);
+      while (k < e && (k == s || taps + wrow_taps(P.code[k]) <= rq.max_taps_per_task)) {
+        taps += wrow_taps(P.code[k]);
         ++k;
       }
       Task tk{};
@@ -174,8 +194,7 @@ WPlan build_wplan(const WPlanRequest &rq) {
     std::vector<int64_t> cost(P.tasks.size(), 0);
     for (size_t k = 0; k < P.tasks.size(); ++k)
       for (int i = P.tasks[k].batch_begin; i < P.tasks[k].batch_end; ++i) {
-        const int64_t S = P.code[i] >> 16;
-        cost[k] += S * S;
+        cost[k] += wrow_taps(P.code[i]);
       }
     std::stable_sort(P.task_order.begin(), P.task_order.end(),
                      [&](int32_t x, int32_t y) { return cost[x] > cost[y]; });
@@ -222,12 +241,17 @@ void wplan_factors(const WPlan &P, int64_t i0, int64_t i1, std::complex<T> *out)
         a3[k] = ok_v ? 1.0 : 0.0;
         b3[k] = ok_u ? 0.0 : 1.0;
       }
-      for (int r = 0; r < 3; ++r) {
-        conv1d(fv.data(), J, &alpha[256 * r], Jw, &row[r * S]);
-        conv1d(fu.data(), J, &beta[256 * r], Jw, &row[(3 + r) * S]);
-      }
+      // the nonzero terms only (the row code's term mask): A of each, then B
+      const int terms = wrow_terms(P.code[i]), rank = wrow_rank(P.code[i]);
+      int e = 0;
+      for (int r = 0; r < 3; ++r)
+        if (terms >> r & 1) {
+          conv1d(fv.data(), J, &alpha[256 * r], Jw, &row[e * S]);
+          conv1d(fu.data(), J, &beta[256 * r], Jw, &row[(rank + e) * S]);
+          ++e;
+        }
       std::complex<T> *dst = out + (P.factor[i] - base);
-      for (int r = 0; r < 6; ++r)
+      for (int r = 0; r < 2 * rank; ++r)
         for (int k = 0; k < S; ++k) {
           const std::complex<double> z = (k & 1) ? -row[r * S + k] : row[r * S + k];
           dst[r * S + k] = std::complex<T>(T(z.real()), T(z.imag()));

@@ -9,9 +9,10 @@
 //   g = (a~ / (w i)) b~^T + (1 - chi_v) 1^T + chi_v (1 - chi_u)^T
 // (a~, b~ the masked 1-D chirps, chi the validity masks; every sample comes
 // from exactly one term, so no term cancels another in finite precision).
-// The convolution is bilinear, so K_m = sum_r A_r B_r^T with six length-S
-// factor vectors, which is what is stored (FP64-generated, in the operator's
-// precision).
+// The convolution is bilinear, so K_m = sum_r A_r B_r^T with up to six
+// length-S factor vectors, which is what is stored (FP64-generated, in the
+// operator's precision).  Terms whose masks make them zero are not stored:
+// where the validity rectangle covers all of a row's samples K_m has rank 1.
 #pragma once
 #include <complex>
 #include <cstdint>
@@ -39,7 +40,7 @@ struct WPlan {
   int Nu = 0, Nv = 0, J = 0, Smax = 0;
   AxisTiling tu, tv;
   // per visibility in plan order (tile, then support descending)
-  std::vector<int32_t> code;     // lp | lq << 8 | S << 16
+  std::vector<int32_t> code;     // lp | lq << 8 | S << 16 | terms << 24 (see wrow_terms)
   std::vector<int64_t> factor;   // offset of the row's factors, in complex values
   std::vector<std::complex<double>> weight;  // weight with (-1)^(kw_u + kw_v) folded in
   std::vector<int32_t> slot_user, user_slot;
@@ -58,9 +59,23 @@ struct WPlan {
 
 WPlan build_wplan(const WPlanRequest &rq);
 
+// Fields of a row code: the support S and the mask of stored terms (bit r:
+// term r of the sample matrix is nonzero); the rank is the mask's popcount.
+inline int wrow_support(int32_t code) { return (code >> 16) & 0xff; }
+inline int wrow_terms(int32_t code) { return (code >> 24) & 7; }
+inline int wrow_rank(int32_t code) {
+  const int t = wrow_terms(code);
+  return (t & 1) + ((t >> 1) & 1) + ((t >> 2) & 1);
+}
+inline int64_t wrow_taps(int32_t code) {
+  const int64_t S = wrow_support(code);
+  return S * S;
+}
+
 // Factors of rows [i0, i1) of the plan, FP64-generated, written in T to
-// out[factor[i] - factor[i0] ...]: per row A_0..A_2 then B_0..B_2 (S complex
-// each, (-1)^j of the phase folded in) with K = sum_r A_r B_r^T.
+// out[factor[i] - factor[i0] ...]: per row A_0..A_{rank-1} then
+// B_0..B_{rank-1} over the row's nonzero terms (S complex each, (-1)^j of the
+// phase folded in) with K = sum_r A_r B_r^T.
 template <typename T>
 void wplan_factors(const WPlan &plan, int64_t i0, int64_t i1, std::complex<T> *out);
 
