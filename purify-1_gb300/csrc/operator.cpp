@@ -97,7 +97,8 @@ class OperatorT final : public Operator {
   int64_t M_ = 0, N_ = 0, S_ = 0;
   bool wmode_ = false;  // w-projection rows instead of separable taps
   int fold_J_ = 0;      // halo of the task windows + 1 (J, or the largest w support)
-  DeviceBuffer wcode_, wfactor_, wfactors_;
+  DeviceBuffer wcode_, wfactor_, wfactors_, wchunks_, wtask_chunk_;
+  int wchunk_values_ = 0;
   int64_t nnz_ = 0, occupied_ = 0, work_items_ = 0;
   void init_plain(const OperatorConfig &cfg, int64_t &bytes, AxisTiling &tu, AxisTiling &tv,
                   std::vector<int32_t> &tile_tasks);
@@ -415,9 +416,16 @@ void OperatorT<real>::init_w(const OperatorConfig &cfg, int64_t &bytes, AxisTili
   tasks_.upload(plan.tasks.data(), sizeof(Task) * plan.tasks.size(), stream_);
   task_order_.alloc(sizeof(int32_t) * std::max<size_t>(plan.task_order.size(), 1), &bytes);
   task_order_.upload(plan.task_order.data(), sizeof(int32_t) * plan.task_order.size(), stream_);
+  wchunks_.alloc(sizeof(WChunk) * std::max<size_t>(plan.chunks.size(), 1), &bytes);
+  wchunks_.upload(plan.chunks.data(), sizeof(WChunk) * plan.chunks.size(), stream_);
+  wtask_chunk_.alloc(sizeof(int32_t) * plan.task_chunk.size(), &bytes);
+  wtask_chunk_.upload(plan.task_chunk.data(), sizeof(int32_t) * plan.task_chunk.size(), stream_);
+  wchunk_values_ = plan.chunk_values;
   cuda_check(cudaStreamSynchronize(stream_), "upload");
-  // Row factors, FP64-generated, uploaded in chunks of rows.
-  wfactors_.alloc(sizeof(C) * std::max<int64_t>(plan.factor_count, 1), &bytes);
+  // Row factors, FP64-generated, uploaded in chunks of rows.  Two values of
+  // tail: the G^H staging copies read whole 16-byte pieces.
+  wfactors_.alloc(sizeof(C) * (plan.factor_count + 2), &bytes);
+  cuda_check(cudaMemset(wfactors_.get(), 0, sizeof(C) * (plan.factor_count + 2)), "memset");
   const int64_t chunk_rows = 1 << 20;
   std::vector<std::complex<real>> buf;
   for (int64_t i0 = 0; i0 < M_; i0 += chunk_rows) {
@@ -492,11 +500,14 @@ void OperatorT<real>::degrid_slots(const void *grid, void *caller_vis) {
     w.factors = wfactors_.get();
     w.weight = weight_.get();
     w.slot_out = ws_->slots;
+    w.chunks = wchunks_.as<WChunk>();
+    w.task_chunk = wtask_chunk_.as<int32_t>();
+    w.chunk_values = wchunk_values_;
     w.Nu = Nu_;
     w.Nv = Nv_;
     w.Smax = fold_J_;
     mark_begin(kDegrid);
-    cuda_check(launch_wdegrid<real>(w, ntasks_, win_rows_, win_cols_, shape_.threads, ws_->stream),
+    cuda_check(launch_wdegrid<real>(w, ntasks_, win_rows_, win_cols_, ws_->stream),
                "w degrid");
     mark_end(kDegrid);
     return;
@@ -541,12 +552,15 @@ void OperatorT<real>::grid_core(void *grid, const void *vis, const int32_t *slot
     w.factors = wfactors_.get();
     w.weight = weight_.get();
     w.slot_in = vis;
+    w.chunks = wchunks_.as<WChunk>();
+    w.task_chunk = wtask_chunk_.as<int32_t>();
+    w.chunk_values = wchunk_values_;
     w.Nu = Nu_;
     w.Nv = Nv_;
     w.Smax = fold_J_;
     w.slot_stride = slot_stride_;
     mark_begin(kGrid);
-    cuda_check(launch_wgrid<real>(w, ntasks_, win_rows_, win_cols_, shape_.threads, ws_->stream),
+    cuda_check(launch_wgrid<real>(w, ntasks_, win_rows_, win_cols_, ws_->stream),
                "w grid");
     mark_end(kGrid);
     fold_into(grid, windows);

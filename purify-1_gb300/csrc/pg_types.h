@@ -63,6 +63,18 @@ struct Task {
   int32_t channel;                 // operator of a grouped (multi-channel) launch, else 0
 };
 
+// A run of consecutive visibilities (plan order) of one w-projection task
+// whose row factors, [fbegin, fend) in complex values, are staged in shared
+// memory together.
+struct WChunk {
+  int64_t fbegin, fend;
+  int32_t vis_begin, vis_end;
+};
+// Bounds of a w-projection chunk: visibilities, and factor values (raised to
+// 6 Smax when one row needs more).
+constexpr int kWChunkVis = 64;
+constexpr int kWChunkValues = 1024;
+
 // Work item encoding: .x = first visibility (plan order), .y = lp | lq << 8 |
 // count << 16 with (lp, lq) the base cell relative to the tile origin.  An
 // item with count 0 is padding.

@@ -57,11 +57,6 @@ __device__ __forceinline__ void cp_async_wait_one() {
   asm volatile("cp.async.wait_group 1;\n" ::: "memory");
 }
 
-// Per-warp software pipeline over the visibilities i = first, first + nw, ...
-// of a task: while visibility i is computed, the row factors of the next one
-// are on their way into the other half of the warp's factor buffer
-// (cp.async), and the code, factor offset, weight and visibility of the one
-// after that are being loaded into registers.
 // Stored factor terms of a row: the popcount of the code's term mask.
 __device__ __forceinline__ int row_rank(int code) { return __popc((code >> 24) & 7); }
 
@@ -76,55 +71,115 @@ __device__ __forceinline__ C row_tap(const C *fbuf, int S, int rank, int j, cons
   return k;
 }
 template <typename C>
-__device__ __forceinline__ void column_factors(const C *fbuf, int S, int rank, int c, bool active,
-                                               C (&b)[3]) {
-  b[0] = b[1] = b[2] = C{0, 0};
-  if (!active) return;
+__device__ __forceinline__ void column_factors(const C *fbuf, int S, int rank, int c, C (&b)[3]) {
   b[0] = fbuf[rank * S + c];
-  if (rank > 1) b[1] = fbuf[(rank + 1) * S + c];
-  if (rank > 2) b[2] = fbuf[(rank + 2) * S + c];
+  b[1] = rank > 1 ? fbuf[(rank + 1) * S + c] : C{0, 0};
+  b[2] = rank > 2 ? fbuf[(rank + 2) * S + c] : C{0, 0};
 }
 
+// G^H of the w-projection rows with one window per CTA.  The window's rows
+// are dealt to the kBandWarps warps in turn (row p to warp p mod kBandWarps)
+// and every warp walks all of the task's visibilities in plan order, updating
+// only its own rows: each cell has one writer, which adds the visibilities in
+// plan order.  The rows' factors, codes, weights and visibilities are staged
+// in shared memory one chunk (WChunk) at a time, the next chunk's copies in
+// flight (cp.async) while the current one is gridded.
+constexpr int kBandWarps = 8;
+
 template <typename real>
-struct WPipe {
+struct BandStage {
   using C = cplx<real>;
-  const WArgs<real> &a;
-  C *fb;  // [2][6 * Smax]
-  int lane, nw, end;
-  int code1 = 0, code2 = 0;
-  int64_t off1 = 0, off2 = 0;
-  C w1{0, 0}, w2{0, 0}, y1{0, 0}, y2{0, 0};
-  __device__ WPipe(const WArgs<real> &args, C *buf, int l, int n, int e)
-      : a(args), fb(buf), lane(l), nw(n), end(e) {}
-  __device__ __forceinline__ void meta(int i, int &code, int64_t &off, C &w, C &y, bool vis_in) {
-    if (i < end) {
-      code = a.code[i];
-      off = a.factor[i];
-      w = static_cast<const C *>(a.weight)[i];
-      if (vis_in) y = static_cast<const C *>(a.slot_in)[i];
-    }
-  }
-  __device__ __forceinline__ void issue(int i, int code, int64_t off, int buf) {
-    if (i < end) {
-      const int n = 2 * row_rank(code) * ((code >> 16) & 0xff);
-      const C *src = static_cast<const C *>(a.factors) + off;
-      C *dst = fb + buf * 6 * a.Smax;
-      for (int k = lane; k < n; k += 32) cp_async<sizeof(C)>(dst + k, src + k);
-    }
-    cp_async_commit();
-  }
+  C *f;         // factor values [chunk_values + 2], from the chunk's aligned start
+  int64_t *fo;  // factor offsets [kWChunkVis]
+  int *code;    // [kWChunkVis]
+  C *w, *y;     // weights, visibilities [kWChunkVis]
 };
 
 template <typename real>
-__global__ void __launch_bounds__(128) wdegrid_kernel(const WArgs<real> a) {
+__host__ __device__ inline size_t band_stage_bytes(int chunk_values) {
+  const size_t c = 2 * sizeof(real);
+  auto up = [](size_t b) { return (b + 15) / 16 * 16; };
+  return up(c * (chunk_values + 2)) + up(8 * kWChunkVis) + up(4 * kWChunkVis) +
+         2 * up(c * kWChunkVis);
+}
+
+template <typename real>
+__device__ __forceinline__ BandStage<real> band_stage(unsigned char *base, int chunk_values) {
+  using C = cplx<real>;
+  auto up = [](size_t b) { return (b + 15) / 16 * 16; };
+  BandStage<real> st;
+  st.f = reinterpret_cast<C *>(base);
+  base += up(sizeof(C) * (chunk_values + 2));
+  st.fo = reinterpret_cast<int64_t *>(base);
+  base += up(8 * kWChunkVis);
+  st.code = reinterpret_cast<int *>(base);
+  base += up(4 * kWChunkVis);
+  st.w = reinterpret_cast<C *>(base);
+  base += up(sizeof(C) * kWChunkVis);
+  st.y = reinterpret_cast<C *>(base);
+  return st;
+}
+
+// First factor value a chunk's staging copies start at: the chunk's first
+// value rounded down to a 16-byte boundary.
+template <typename real>
+__device__ __forceinline__ int64_t band_base(const WChunk &c) {
+  return sizeof(real) == 4 ? (c.fbegin & ~int64_t(1)) : c.fbegin;
+}
+
+template <typename real, bool VIS>
+__device__ __forceinline__ void band_issue(const WArgs<real> &a, const WChunk &c,
+                                           const BandStage<real> &st) {
+  using C = cplx<real>;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  // factors in 16-byte pieces over [base, fend rounded up): the factor
+  // buffer is allocated with a 16-byte tail, so the last piece stays inside
+  const int64_t f0 = band_base<real>(c);
+  const int64_t nbytes = (c.fend - f0) * int64_t(sizeof(C));
+  const int pieces = int((nbytes + 15) / 16);
+  const char *src = reinterpret_cast<const char *>(static_cast<const C *>(a.factors) + f0);
+  char *dst = reinterpret_cast<char *>(st.f);
+  for (int k = tid; k < pieces; k += nt) cp_async<16>(dst + 16 * k, src + 16 * k);
+  const int nv = c.vis_end - c.vis_begin;
+  for (int k = tid; k < nv; k += nt) {
+    const int i = c.vis_begin + k;
+    cp_async<8>(st.fo + k, a.factor + i);
+    cp_async<4>(st.code + k, a.code + i);
+    cp_async<sizeof(C)>(st.w + k, static_cast<const C *>(a.weight) + i);
+    if (VIS) cp_async<sizeof(C)>(st.y + k, static_cast<const C *>(a.slot_in) + i);
+  }
+  cp_async_commit();
+}
+
+// Lane layout of a row of support S: R = 32 / S row slots of S columns, lane
+// l at row slot r = l / S, column c = l % S.  (l + 0.5) / S is at least 1/64
+// from an integer, so the rounded reciprocal gives the exact quotients.
+__device__ __forceinline__ void lane_layout(int S, int lane, int &R, int &r, int &c) {
+  const float rcp = __frcp_rn(float(S));
+  R = int(32.5f * rcp);
+  r = int((float(lane) + 0.5f) * rcp);
+  c = lane - r * S;
+}
+
+// G of the w-projection rows: the task's grid window is staged once per CTA,
+// the rows' factors, codes and weights one chunk at a time (the next chunk
+// in flight while the current one is used), and each warp takes whole
+// visibilities of the chunk in turn.  For visibility m, lane (r, c) sums
+// A_e[jv] g[jv][c] over its rows jv for each stored term e, then applies
+// B_e[c]; a butterfly over the warp adds the lanes.
+template <typename real>
+__global__ void __launch_bounds__(kBandWarps * 32, 4) wdegrid_band_kernel(const WArgs<real> a) {
   using C = cplx<real>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int task_id = a.order ? a.order[blockIdx.x] : int(blockIdx.x);
   const Task tk = a.tasks[task_id];
   const int WW = tk.W + a.Smax - 1, WH = tk.H + a.Smax - 1;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   C *win = reinterpret_cast<C *>(smem_raw);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  C *fb = reinterpret_cast<C *>(smem_raw + a.win_bytes) + warp * 2 * 6 * a.Smax;
+  const size_t sb = band_stage_bytes<real>(a.chunk_values);
+  auto stage = [&](int buf) {
+    return band_stage<real>(smem_raw + a.win_bytes + buf * sb, a.chunk_values);
+  };
   const C *grid = static_cast<const C *>(a.grid);
   for (int idx = threadIdx.x; idx < WW * WH; idx += blockDim.x) {
     const int lp = idx / WW, lq = idx - lp * WW;
@@ -134,203 +189,178 @@ __global__ void __launch_bounds__(128) wdegrid_kernel(const WArgs<real> a) {
     if (q >= a.Nu) q -= a.Nu;
     cp_async<sizeof(C)>(win + idx, grid + size_t(p) * a.Nu + q);
   }
-  cp_async_wait_all();
-  __syncthreads();
+  cp_async_commit();  // the window travels with the first chunk's group
   C *out = static_cast<C *>(a.slot_out);
-  const int first = tk.batch_begin + warp;
-  WPipe<real> pp(a, fb, lane, nw, tk.batch_end);
-  int code0 = 0;
-  int64_t off0 = 0;
-  C w0{0, 0}, y0{0, 0};
-  pp.meta(first, code0, off0, w0, y0, false);
-  pp.meta(first + nw, pp.code1, pp.off1, pp.w1, pp.y1, false);
-  pp.issue(first, code0, off0, 0);
-  int buf = 0;
-  for (int i = first; i < tk.batch_end; i += nw) {
-    pp.issue(i + nw, pp.code1, pp.off1, buf ^ 1);
-    pp.meta(i + 2 * nw, pp.code2, pp.off2, pp.w2, pp.y2, false);
+  const int c0 = a.task_chunk[task_id], c1 = a.task_chunk[task_id + 1];
+  if (c0 < c1) band_issue<real, false>(a, a.chunks[c0], stage(0));
+  for (int ch = c0; ch < c1; ++ch) {
+    const int buf = (ch - c0) & 1;
+    if (ch + 1 < c1)
+      band_issue<real, false>(a, a.chunks[ch + 1], stage(buf ^ 1));
+    else
+      cp_async_commit();
     cp_async_wait_one();
-    __syncwarp();  // every lane's factor copies for visibility i have landed
-    const C *fbuf = fb + buf * 6 * a.Smax;
-    const int lp = code0 & 0xff, lq = (code0 >> 8) & 0xff, S = (code0 >> 16) & 0xff;
-    const int rank = row_rank(code0);
-    const int R = 32 / S, r = lane / S, c = lane - r * S;
-    const bool active = r < R;
-    C b[3];
-    column_factors(fbuf, S, rank, c, active, b);
-    C acc{0, 0}, acc2{0, 0};
-    for (int jv0 = 0; jv0 < S; jv0 += 2 * R) {
-      const int ja = jv0 + r, jb = jv0 + R + r;
-      if (active && ja < S) cfma(acc, row_tap(fbuf, S, rank, ja, b), win[(lp + ja) * WW + lq + c]);
-      if (active && jb < S) cfma(acc2, row_tap(fbuf, S, rank, jb, b), win[(lp + jb) * WW + lq + c]);
-    }
-    acc.x += acc2.x;
-    acc.y += acc2.y;
+    __syncthreads();
+    const WChunk cr = a.chunks[ch];
+    const BandStage<real> sg = stage(buf);
+    const int64_t f0 = band_base<real>(cr);
+    const int nv = cr.vis_end - cr.vis_begin;
+    for (int v = warp; v < nv; v += kBandWarps) {
+      const int code = sg.code[v];
+      const int lp = code & 0xff, lq = (code >> 8) & 0xff, S = (code >> 16) & 0xff;
+      const int rank = row_rank(code);
+      const C *fr = sg.f + (sg.fo[v] - f0);
+      int R, r, c;
+      lane_layout(S, lane, R, r, c);
+      C y{0, 0};
+      if (r < R) {
+        C s0{0, 0}, s1{0, 0}, s2{0, 0};
+        const C *g = win + (lp + r) * WW + lq + c;
+        for (int jv = r; jv < S; jv += R, g += R * WW) {
+          const C gv = *g;
+          cfma(s0, fr[jv], gv);
+          if (rank > 1) cfma(s1, fr[S + jv], gv);
+          if (rank > 2) cfma(s2, fr[2 * S + jv], gv);
+        }
+        y = cmul(fr[rank * S + c], s0);
+        if (rank > 1) cfma(y, fr[(rank + 1) * S + c], s1);
+        if (rank > 2) cfma(y, fr[(rank + 2) * S + c], s2);
+      }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
-      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+      for (int o = 16; o > 0; o >>= 1) {
+        y.x += __shfl_xor_sync(0xffffffffu, y.x, o);
+        y.y += __shfl_xor_sync(0xffffffffu, y.y, o);
+      }
+      if (lane == 0) out[cr.vis_begin + v] = cmul(y, sg.w[v]);
     }
-    if (lane == 0) out[i] = cmul(acc, w0);
-    __syncwarp();  // this half of the factor buffer is refilled two visibilities on
-    code0 = pp.code1;
-    off0 = pp.off1;
-    w0 = pp.w1;
-    pp.code1 = pp.code2;
-    pp.off1 = pp.off2;
-    pp.w1 = pp.w2;
-    buf ^= 1;
+    __syncthreads();  // every warp is done with this buffer before it is refilled
   }
   cp_async_wait_all();
 }
 
 template <typename real>
-__global__ void __launch_bounds__(128) wgrid_kernel(const WArgs<real> a) {
+__global__ void __launch_bounds__(kBandWarps * 32, 4) wgrid_band_kernel(const WArgs<real> a) {
   using C = cplx<real>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int task_id = a.order ? a.order[blockIdx.x] : int(blockIdx.x);
   const Task tk = a.tasks[task_id];
   const int WW = tk.W + a.Smax - 1, WH = tk.H + a.Smax - 1, WN = WW * WH;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  C *wins = reinterpret_cast<C *>(smem_raw);
-  C *fb = reinterpret_cast<C *>(smem_raw + a.win_bytes) + warp * 2 * 6 * a.Smax;
-  for (int idx = threadIdx.x; idx < nw * WN; idx += blockDim.x) wins[idx] = C{0, 0};
-  __syncthreads();
-  C *mine = wins + warp * WN;
-  const int first = tk.batch_begin + warp;
-  WPipe<real> pp(a, fb, lane, nw, tk.batch_end);
-  int code0 = 0;
-  int64_t off0 = 0;
-  C w0{0, 0}, y0{0, 0};
-  pp.meta(first, code0, off0, w0, y0, true);
-  pp.meta(first + nw, pp.code1, pp.off1, pp.w1, pp.y1, true);
-  pp.issue(first, code0, off0, 0);
-  int buf = 0;
-  for (int i = first; i < tk.batch_end; i += nw) {
-    pp.issue(i + nw, pp.code1, pp.off1, buf ^ 1);
-    pp.meta(i + 2 * nw, pp.code2, pp.off2, pp.w2, pp.y2, true);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  C *win = reinterpret_cast<C *>(smem_raw);
+  const size_t sb = band_stage_bytes<real>(a.chunk_values);
+  auto stage = [&](int buf) {
+    return band_stage<real>(smem_raw + a.win_bytes + buf * sb, a.chunk_values);
+  };
+  for (int idx = threadIdx.x; idx < WN; idx += blockDim.x) win[idx] = C{0, 0};
+  const int c0 = a.task_chunk[task_id], c1 = a.task_chunk[task_id + 1];
+  if (c0 < c1) band_issue<real, true>(a, a.chunks[c0], stage(0));
+  for (int ch = c0; ch < c1; ++ch) {
+    const int buf = (ch - c0) & 1;
+    if (ch + 1 < c1)
+      band_issue<real, true>(a, a.chunks[ch + 1], stage(buf ^ 1));
+    else
+      cp_async_commit();  // empty group: "all but the newest" still means this chunk
     cp_async_wait_one();
-    __syncwarp();  // every lane's factor copies for visibility i have landed
-    const C *fbuf = fb + buf * 6 * a.Smax;
-    const int lp = code0 & 0xff, lq = (code0 >> 8) & 0xff, S = (code0 >> 16) & 0xff;
-    const int rank = row_rank(code0);
-    // conj(weight) * y: G^H holds the conjugated entries of G
-    const C z{w0.x * y0.x + w0.y * y0.y, w0.x * y0.y - w0.y * y0.x};
-    const int R = 32 / S, r = lane / S, c = lane - r * S;
-    const bool active = r < R;
-    C b[3];
-    column_factors(fbuf, S, rank, c, active, b);
-    // All S^2 cells of one visibility are distinct, so the lanes never touch
-    // the same cell within it, and the two rows a lane updates per step are
-    // different cells; visibilities are ordered by __syncwarp.
-    for (int jv0 = 0; jv0 < S; jv0 += 2 * R) {
-      const int ja = jv0 + r, jb = jv0 + R + r;
-      const bool oka = active && ja < S, okb = active && jb < S;
-      C ka{0, 0}, kb{0, 0}, va{0, 0}, vb{0, 0};
-      C *ca = mine + (lp + ja) * WW + lq + c;
-      C *cb = mine + (lp + jb) * WW + lq + c;
-      if (oka) {
-        ka = row_tap(fbuf, S, rank, ja, b);
-        va = *ca;
+    __syncthreads();  // the chunk's copies (and the zeroed window) are visible
+    const WChunk cr = a.chunks[ch];
+    const BandStage<real> sg = stage(buf);
+    const int64_t f0 = band_base<real>(cr);
+    const int nv = cr.vis_end - cr.vis_begin;
+    for (int v = 0; v < nv; ++v) {
+      const int code = sg.code[v];
+      const int lp = code & 0xff, lq = (code >> 8) & 0xff, S = (code >> 16) & 0xff;
+      // this warp's first row of the visibility: (lp + jv0) = warp (mod kBandWarps)
+      const int jv0 = (warp - lp) & (kBandWarps - 1);
+      if (jv0 < S) {
+        const int rank = row_rank(code);
+        const C *fr = sg.f + (sg.fo[v] - f0);
+        const C w = sg.w[v], y = sg.y[v];
+        // conj(weight) * y: G^H holds the conjugated entries of G
+        const C z{w.x * y.x + w.y * y.y, w.x * y.y - w.y * y.x};
+        const int nrows = (S - 1 - jv0) / kBandWarps + 1;
+        int R, r, c;
+        lane_layout(S, lane, R, r, c);
+        if (r < R) {
+          C b[3];
+          column_factors(fr, S, rank, c, b);
+          for (int t = r; t < nrows; t += R) {
+            const int jv = jv0 + kBandWarps * t;
+            const C k = row_tap(fr, S, rank, jv, b);
+            C *cell = win + (lp + jv) * WW + lq + c;
+            C cv = *cell;
+            // conj(K) z
+            cv.x = fma(k.x, z.x, fma(k.y, z.y, cv.x));
+            cv.y = fma(k.x, z.y, fma(-k.y, z.x, cv.y));
+            *cell = cv;
+          }
+        }
       }
-      if (okb) {
-        kb = row_tap(fbuf, S, rank, jb, b);
-        vb = *cb;
-      }
-      // conj(K) z
-      if (oka) {
-        va.x = fma(ka.x, z.x, fma(ka.y, z.y, va.x));
-        va.y = fma(ka.x, z.y, fma(-ka.y, z.x, va.y));
-        *ca = va;
-      }
-      if (okb) {
-        vb.x = fma(kb.x, z.x, fma(kb.y, z.y, vb.x));
-        vb.y = fma(kb.x, z.y, fma(-kb.y, z.x, vb.y));
-        *cb = vb;
-      }
+      __syncwarp();  // this warp's cells of visibility v are written before v + 1
     }
-    __syncwarp();
-    code0 = pp.code1;
-    off0 = pp.off1;
-    w0 = pp.w1;
-    y0 = pp.y1;
-    pp.code1 = pp.code2;
-    pp.off1 = pp.off2;
-    pp.w1 = pp.w2;
-    pp.y1 = pp.y2;
-    buf ^= 1;
+    __syncthreads();  // every warp is done with this buffer before it is refilled
   }
   cp_async_wait_all();
   __syncthreads();
   C *out = static_cast<C *>(a.tilebuf) + size_t(task_id) * a.slot_stride;
-  for (int idx = threadIdx.x; idx < WN; idx += blockDim.x) {
-    C s = wins[idx];
-    for (int w2 = 1; w2 < nw; ++w2) {
-      const C o = wins[w2 * WN + idx];
-      s.x += o.x;
-      s.y += o.y;
-    }
-    out[idx] = s;
-  }
+  for (int idx = threadIdx.x; idx < WN; idx += blockDim.x) out[idx] = win[idx];
 }
 
-size_t wwindow_bytes(int bytes_real, int win_rows, int win_cols, int threads, bool per_warp) {
-  const size_t one = size_t(win_rows) * win_cols * 2 * bytes_real;
-  const size_t b = per_warp ? one * size_t(threads / 32) : one;
+// One task window (win_rows x win_cols complex), rounded to 16 bytes.
+size_t wwindow_bytes(int bytes_real, int win_rows, int win_cols) {
+  const size_t b = size_t(win_rows) * win_cols * 2 * bytes_real;
   return (b + 15) / 16 * 16;
 }
 
 }  // namespace
 
 template <typename real>
-size_t wdegrid_smem_bytes(int win_rows, int win_cols, int Smax, int threads) {
-  return wwindow_bytes(sizeof(real), win_rows, win_cols, threads, false) +
-         size_t(threads / 32) * 2 * 6 * Smax * 2 * sizeof(real);
+size_t wdegrid_smem_bytes(int win_rows, int win_cols, int chunk_values) {
+  return wwindow_bytes(sizeof(real), win_rows, win_cols) + 2 * band_stage_bytes<real>(chunk_values);
 }
 template <typename real>
-size_t wgrid_smem_bytes(int win_rows, int win_cols, int Smax, int threads) {
-  return wwindow_bytes(sizeof(real), win_rows, win_cols, threads, true) +
-         size_t(threads / 32) * 2 * 6 * Smax * 2 * sizeof(real);
+size_t wgrid_smem_bytes(int win_rows, int win_cols, int chunk_values) {
+  return wwindow_bytes(sizeof(real), win_rows, win_cols) +
+         2 * band_stage_bytes<real>(chunk_values);
 }
 
 template <typename real>
 cudaError_t launch_wdegrid(const WArgs<real> &a0, int ntasks, int win_rows, int win_cols,
-                           int threads, cudaStream_t s) {
+                           cudaStream_t s) {
   if (ntasks == 0) return cudaSuccess;
   WArgs<real> a = a0;
-  a.win_bytes = int(wwindow_bytes(sizeof(real), win_rows, win_cols, threads, false));
-  const size_t smem = wdegrid_smem_bytes<real>(win_rows, win_cols, a.Smax, threads);
+  a.win_bytes = int(wwindow_bytes(sizeof(real), win_rows, win_cols));
+  const size_t smem = wdegrid_smem_bytes<real>(win_rows, win_cols, a.chunk_values);
   if (smem > 48 * 1024) {
     const cudaError_t e = cudaFuncSetAttribute(
-        wdegrid_kernel<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        wdegrid_band_kernel<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
   }
-  wdegrid_kernel<real><<<ntasks, threads, smem, s>>>(a);
+  wdegrid_band_kernel<real><<<ntasks, kBandWarps * 32, smem, s>>>(a);
   return cudaGetLastError();
 }
 template <typename real>
 cudaError_t launch_wgrid(const WArgs<real> &a0, int ntasks, int win_rows, int win_cols,
-                         int threads, cudaStream_t s) {
+                         cudaStream_t s) {
   if (ntasks == 0) return cudaSuccess;
   WArgs<real> a = a0;
-  a.win_bytes = int(wwindow_bytes(sizeof(real), win_rows, win_cols, threads, true));
-  const size_t smem = wgrid_smem_bytes<real>(win_rows, win_cols, a.Smax, threads);
+  a.win_bytes = int(wwindow_bytes(sizeof(real), win_rows, win_cols));
+  const size_t smem = wgrid_smem_bytes<real>(win_rows, win_cols, a.chunk_values);
   if (smem > 48 * 1024) {
     const cudaError_t e = cudaFuncSetAttribute(
-        wgrid_kernel<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        wgrid_band_kernel<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
   }
-  wgrid_kernel<real><<<ntasks, threads, smem, s>>>(a);
+  wgrid_band_kernel<real><<<ntasks, kBandWarps * 32, smem, s>>>(a);
   return cudaGetLastError();
 }
 
-template size_t wdegrid_smem_bytes<float>(int, int, int, int);
-template size_t wdegrid_smem_bytes<double>(int, int, int, int);
-template size_t wgrid_smem_bytes<float>(int, int, int, int);
-template size_t wgrid_smem_bytes<double>(int, int, int, int);
-template cudaError_t launch_wdegrid<float>(const WArgs<float> &, int, int, int, int, cudaStream_t);
-template cudaError_t launch_wdegrid<double>(const WArgs<double> &, int, int, int, int, cudaStream_t);
-template cudaError_t launch_wgrid<float>(const WArgs<float> &, int, int, int, int, cudaStream_t);
-template cudaError_t launch_wgrid<double>(const WArgs<double> &, int, int, int, int, cudaStream_t);
+template size_t wdegrid_smem_bytes<float>(int, int, int);
+template size_t wdegrid_smem_bytes<double>(int, int, int);
+template size_t wgrid_smem_bytes<float>(int, int, int);
+template size_t wgrid_smem_bytes<double>(int, int, int);
+template cudaError_t launch_wdegrid<float>(const WArgs<float> &, int, int, int, cudaStream_t);
+template cudaError_t launch_wdegrid<double>(const WArgs<double> &, int, int, int, cudaStream_t);
+template cudaError_t launch_wgrid<float>(const WArgs<float> &, int, int, int, cudaStream_t);
+template cudaError_t launch_wgrid<double>(const WArgs<double> &, int, int, int, cudaStream_t);
 
 }  // namespace pg

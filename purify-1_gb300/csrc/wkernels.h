@@ -24,20 +24,25 @@ struct WArgs {
   const void *weight = nullptr;    // per visibility, complex, phase sign folded in
   void *slot_out = nullptr;        // degrid output in plan order
   const void *slot_in = nullptr;   // grid input in plan order
+  const WChunk *chunks = nullptr;  // staging chunks (wplan.h)
+  const int32_t *task_chunk = nullptr;
+  int chunk_values = 0;
   int Nu = 0, Nv = 0, Smax = 0;
   int64_t slot_stride = 0;
   int win_bytes = 0;               // set by the launchers
 };
 
+// Both kernels run 256 threads per CTA with one window per CTA and the row
+// data staged chunk by chunk (WArgs::chunks).
 template <typename real>
-size_t wdegrid_smem_bytes(int win_rows, int win_cols, int Smax, int threads);
+size_t wdegrid_smem_bytes(int win_rows, int win_cols, int chunk_values);
 template <typename real>
-size_t wgrid_smem_bytes(int win_rows, int win_cols, int Smax, int threads);
+size_t wgrid_smem_bytes(int win_rows, int win_cols, int chunk_values);
 template <typename real>
 cudaError_t launch_wdegrid(const WArgs<real> &a, int ntasks, int win_rows, int win_cols,
-                           int threads, cudaStream_t s);
+                           cudaStream_t s);
 template <typename real>
 cudaError_t launch_wgrid(const WArgs<real> &a, int ntasks, int win_rows, int win_cols,
-                         int threads, cudaStream_t s);
+                         cudaStream_t s);
 
 }  // namespace pg

@@ -186,6 +186,24 @@ WPlan build_wplan(const WPlanRequest &rq) {
     P.win_cols = std::max(P.win_cols, P.tu.start[b + 1] - P.tu.start[b] + Smax - 1);
     i = e;
   }
+  // Staging chunks (the factor ranges of consecutive rows are contiguous).
+  P.chunk_values = std::max(kWChunkValues, 6 * Smax);
+  P.task_chunk.assign(P.tasks.size() + 1, 0);
+  for (size_t k = 0; k < P.tasks.size(); ++k) {
+    const int32_t b = P.tasks[k].batch_begin, e = P.tasks[k].batch_end;
+    auto fend = [&](int32_t r) { return r + 1 < M ? P.factor[r + 1] : P.factor_count; };
+    for (int32_t r = b; r < e;) {
+      WChunk c{P.factor[r], fend(r), r, r + 1};
+      while (c.vis_end < e && c.vis_end - c.vis_begin < kWChunkVis &&
+             fend(c.vis_end) - c.fbegin <= P.chunk_values) {
+        c.fend = fend(c.vis_end);
+        ++c.vis_end;
+      }
+      P.chunks.push_back(c);
+      r = c.vis_end;
+    }
+    P.task_chunk[k + 1] = int32_t(P.chunks.size());
+  }
   // Launch order: longest tasks (in taps) first while the grid stays in L2,
   // else the spatial order (see build_plan).
   P.task_order.resize(P.tasks.size());

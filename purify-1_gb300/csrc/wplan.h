@@ -53,6 +53,12 @@ struct WPlan {
   std::vector<Task> tasks;  // batch_begin / batch_end = visibility range in plan order
   std::vector<int32_t> task_order;  // launch order: by decreasing taps, or tile order (see plan.h)
   std::vector<int32_t> tile_tasks;
+  // Staging chunks of the G^H kernel: task k owns chunks
+  // [task_chunk[k], task_chunk[k + 1]), each at most kWChunkVis rows and
+  // chunk_values factor values (plus one value of alignment slack).
+  std::vector<WChunk> chunks;
+  std::vector<int32_t> task_chunk;
+  int chunk_values = 0;
   int win_rows = 0, win_cols = 0;
   int64_t taps = 0;  // sum of S^2
 };
