@@ -1,31 +1,34 @@
 // sm_103a kernels of the w-projection gridding operator (G and G^H with one
-// kernel row per visibility).  Row m's S x S taps are rebuilt on the fly from
-// its stored rank-3 factors, K = A_0 B_0^T + A_1 B_1^T + A_2 B_2^T
-// (wplan.h), over the row's nonzero terms only (rank 1 to 3, from the row
-// code).  One warp handles one visibility at a time; lane l covers row
-// r = l / S of each group of R = 32 / S rows and column c = l % S, two row
-// groups per step.
+// kernel row per visibility).  Row m's S x S taps come from its stored
+// factors, K = sum_e A_e B_e^T over the row's nonzero terms (rank 1 to 3,
+// from the row code; wplan.h).  Within a visibility, lane l covers row slot
+// r = l / S of R = 32 / S and column c = l % S.
 #include <cuda_runtime.h>
 
 #include <cstdint>
 
+#include "cplx_ops.cuh"
 #include "wkernels.h"
 
 namespace pg {
 namespace {
 
-template <typename real>
-struct Cplx;
-template <>
-struct Cplx<float> {
-  using type = float2;
-};
-template <>
-struct Cplx<double> {
-  using type = double2;
-};
-template <typename real>
-using cplx = typename Cplx<real>::type;
+using dev::cplx;
+using dev::fma2;
+using dev::splat;
+
+// ceil(2^16 / S): for lanes l < 32 and S <= 32, (l m) >> 16 = l / S and
+// (32 m) >> 16 = 32 / S exactly (the rounding error is below 1/2048, the
+// distance to the next integer at least 1/32).
+#define PG_MAGIC(S) ((65535 + (S)) / (S))
+__constant__ int kLaneMagic[33] = {
+    0,            PG_MAGIC(1),  PG_MAGIC(2),  PG_MAGIC(3),  PG_MAGIC(4),  PG_MAGIC(5),
+    PG_MAGIC(6),  PG_MAGIC(7),  PG_MAGIC(8),  PG_MAGIC(9),  PG_MAGIC(10), PG_MAGIC(11),
+    PG_MAGIC(12), PG_MAGIC(13), PG_MAGIC(14), PG_MAGIC(15), PG_MAGIC(16), PG_MAGIC(17),
+    PG_MAGIC(18), PG_MAGIC(19), PG_MAGIC(20), PG_MAGIC(21), PG_MAGIC(22), PG_MAGIC(23),
+    PG_MAGIC(24), PG_MAGIC(25), PG_MAGIC(26), PG_MAGIC(27), PG_MAGIC(28), PG_MAGIC(29),
+    PG_MAGIC(30), PG_MAGIC(31), PG_MAGIC(32)};
+#undef PG_MAGIC
 
 template <typename C>
 __device__ __forceinline__ C cmul(C a, C b) {
@@ -35,6 +38,17 @@ template <typename C>
 __device__ __forceinline__ void cfma(C &acc, C a, C b) {
   acc.x = fma(a.x, b.x, fma(-a.y, b.y, acc.x));
   acc.y = fma(a.x, b.y, fma(a.y, b.x, acc.y));
+}
+
+// conj(a) b, and acc += conj(a) b
+template <typename C>
+__device__ __forceinline__ C cmul_conj(C a, C b) {
+  return C{a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x};
+}
+template <typename C>
+__device__ __forceinline__ void cfma_conj(C &acc, C a, C b) {
+  acc.x = fma(a.x, b.x, fma(a.y, b.y, acc.x));
+  acc.y = fma(a.x, b.y, fma(-a.y, b.x, acc.y));
 }
 
 template <int BYTES>
@@ -60,22 +74,6 @@ __device__ __forceinline__ void cp_async_wait_one() {
 // Stored factor terms of a row: the popcount of the code's term mask.
 __device__ __forceinline__ int row_rank(int code) { return __popc((code >> 24) & 7); }
 
-// Tap (row j, the lane's column) of a row: sum over the stored terms of
-// A_e[j] b[e], with b[e] = B_e[column] held by the lane.  The rank is the same
-// for the whole warp (one visibility).
-template <typename C>
-__device__ __forceinline__ C row_tap(const C *fbuf, int S, int rank, int j, const C (&b)[3]) {
-  C k = cmul(fbuf[j], b[0]);
-  if (rank > 1) cfma(k, fbuf[S + j], b[1]);
-  if (rank > 2) cfma(k, fbuf[2 * S + j], b[2]);
-  return k;
-}
-template <typename C>
-__device__ __forceinline__ void column_factors(const C *fbuf, int S, int rank, int c, C (&b)[3]) {
-  b[0] = fbuf[rank * S + c];
-  b[1] = rank > 1 ? fbuf[(rank + 1) * S + c] : C{0, 0};
-  b[2] = rank > 2 ? fbuf[(rank + 2) * S + c] : C{0, 0};
-}
 
 // G^H of the w-projection rows with one window per CTA.  The window's rows
 // are dealt to the kBandWarps warps in turn (row p to warp p mod kBandWarps)
@@ -91,15 +89,16 @@ struct BandStage {
   using C = cplx<real>;
   C *f;         // factor values [chunk_values + 2], from the chunk's aligned start
   int64_t *fo;  // factor offsets [kWChunkVis]
+  int *rel;     // factor offsets relative to the staged start [kWChunkVis]
   int *code;    // [kWChunkVis]
-  C *w, *y;     // weights, visibilities [kWChunkVis]
+  C *w, *y;     // weights (G^H: conj(weight) y after the prep pass), visibilities
 };
 
 template <typename real>
 __host__ __device__ inline size_t band_stage_bytes(int chunk_values) {
   const size_t c = 2 * sizeof(real);
   auto up = [](size_t b) { return (b + 15) / 16 * 16; };
-  return up(c * (chunk_values + 2)) + up(8 * kWChunkVis) + up(4 * kWChunkVis) +
+  return up(c * (chunk_values + 2)) + up(8 * kWChunkVis) + 2 * up(4 * kWChunkVis) +
          2 * up(c * kWChunkVis);
 }
 
@@ -112,6 +111,8 @@ __device__ __forceinline__ BandStage<real> band_stage(unsigned char *base, int c
   base += up(sizeof(C) * (chunk_values + 2));
   st.fo = reinterpret_cast<int64_t *>(base);
   base += up(8 * kWChunkVis);
+  st.rel = reinterpret_cast<int *>(base);
+  base += up(4 * kWChunkVis);
   st.code = reinterpret_cast<int *>(base);
   base += up(4 * kWChunkVis);
   st.w = reinterpret_cast<C *>(base);
@@ -152,13 +153,19 @@ __device__ __forceinline__ void band_issue(const WArgs<real> &a, const WChunk &c
 }
 
 // Lane layout of a row of support S: R = 32 / S row slots of S columns, lane
-// l at row slot r = l / S, column c = l % S.  (l + 0.5) / S is at least 1/64
-// from an integer, so the rounded reciprocal gives the exact quotients.
+// l at row slot r = l / S, column c = l % S.
 __device__ __forceinline__ void lane_layout(int S, int lane, int &R, int &r, int &c) {
-  const float rcp = __frcp_rn(float(S));
-  R = int(32.5f * rcp);
-  r = int((float(lane) + 0.5f) * rcp);
+  const int m = kLaneMagic[S];
+  R = (32 * m) >> 16;
+  r = (lane * m) >> 16;
   c = lane - r * S;
+}
+
+// Packed complex products.  With P = sum g.x A and Q = sum g.y A over taps,
+// sum A g = P + i Q; conj(A) b = A.x b + A.y (b.y, -b.x).
+template <typename C>
+__device__ __forceinline__ C plus_i(C p, C q) {
+  return C{p.x - q.y, p.y + q.x};
 }
 
 // G of the w-projection rows: the task's grid window is staged once per CTA,
@@ -214,17 +221,29 @@ __global__ void __launch_bounds__(kBandWarps * 32, 4) wdegrid_band_kernel(const 
       lane_layout(S, lane, R, r, c);
       C y{0, 0};
       if (r < R) {
-        C s0{0, 0}, s1{0, 0}, s2{0, 0};
         const C *g = win + (lp + r) * WW + lq + c;
-        for (int jv = r; jv < S; jv += R, g += R * WW) {
-          const C gv = *g;
-          cfma(s0, fr[jv], gv);
-          if (rank > 1) cfma(s1, fr[S + jv], gv);
-          if (rank > 2) cfma(s2, fr[2 * S + jv], gv);
+        const int gs = R * WW;
+        if (rank == 1) {
+          C p{0, 0}, q{0, 0};
+#pragma unroll 2
+          for (int jv = r; jv < S; jv += R, g += gs) {
+            const C gv = *g, A = fr[jv];
+            p = fma2(splat(gv.x), A, p);
+            q = fma2(splat(gv.y), A, q);
+          }
+          y = cmul(fr[S + c], plus_i(p, q));
+        } else {
+          C s0{0, 0}, s1{0, 0}, s2{0, 0};
+          for (int jv = r; jv < S; jv += R, g += gs) {
+            const C gv = *g;
+            cfma(s0, fr[jv], gv);
+            cfma(s1, fr[S + jv], gv);
+            if (rank > 2) cfma(s2, fr[2 * S + jv], gv);
+          }
+          y = cmul(fr[rank * S + c], s0);
+          cfma(y, fr[(rank + 1) * S + c], s1);
+          if (rank > 2) cfma(y, fr[(rank + 2) * S + c], s2);
         }
-        y = cmul(fr[rank * S + c], s0);
-        if (rank > 1) cfma(y, fr[(rank + 1) * S + c], s1);
-        if (rank > 2) cfma(y, fr[(rank + 2) * S + c], s2);
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
@@ -264,34 +283,49 @@ __global__ void __launch_bounds__(kBandWarps * 32, 4) wgrid_band_kernel(const WA
     __syncthreads();  // the chunk's copies (and the zeroed window) are visible
     const WChunk cr = a.chunks[ch];
     const BandStage<real> sg = stage(buf);
-    const int64_t f0 = band_base<real>(cr);
     const int nv = cr.vis_end - cr.vis_begin;
+    // prep, once per visibility: conj(weight) y (G^H holds the conjugated
+    // entries of G) and the staged factor offset
+    for (int v = threadIdx.x; v < nv; v += blockDim.x) {
+      sg.w[v] = cmul_conj(sg.w[v], sg.y[v]);
+      sg.rel[v] = int(sg.fo[v] - band_base<real>(cr));
+    }
+    __syncthreads();
     for (int v = 0; v < nv; ++v) {
       const int code = sg.code[v];
-      const int lp = code & 0xff, lq = (code >> 8) & 0xff, S = (code >> 16) & 0xff;
+      const int lp = code & 0xff, S = (code >> 16) & 0xff;
       // this warp's first row of the visibility: (lp + jv0) = warp (mod kBandWarps)
       const int jv0 = (warp - lp) & (kBandWarps - 1);
       if (jv0 < S) {
-        const int rank = row_rank(code);
-        const C *fr = sg.f + (sg.fo[v] - f0);
-        const C w = sg.w[v], y = sg.y[v];
-        // conj(weight) * y: G^H holds the conjugated entries of G
-        const C z{w.x * y.x + w.y * y.y, w.x * y.y - w.y * y.x};
+        const int lq = (code >> 8) & 0xff, rank = row_rank(code);
+        const C *fr = sg.f + sg.rel[v];
         const int nrows = (S - 1 - jv0) / kBandWarps + 1;
         int R, r, c;
         lane_layout(S, lane, R, r, c);
         if (r < R) {
-          C b[3];
-          column_factors(fr, S, rank, c, b);
-          for (int t = r; t < nrows; t += R) {
-            const int jv = jv0 + kBandWarps * t;
-            const C k = row_tap(fr, S, rank, jv, b);
-            C *cell = win + (lp + jv) * WW + lq + c;
-            C cv = *cell;
-            // conj(K) z
-            cv.x = fma(k.x, z.x, fma(k.y, z.y, cv.x));
-            cv.y = fma(k.x, z.y, fma(-k.y, z.x, cv.y));
-            *cell = cv;
+          // conj(K[jv][c]) z = sum_e conj(A_e[jv]) (conj(B_e[c]) z): the
+          // column part bz_e is formed once per visibility
+          const C z = sg.w[v];
+          C *cell = win + (lp + jv0 + kBandWarps * r) * WW + lq + c;
+          const int cs = kBandWarps * R * WW;
+          const C *A = fr + jv0;
+          if (rank == 1) {
+            const C bz = cmul_conj(fr[S + c], z), bzr{bz.y, -bz.x};
+            for (int t = r; t < nrows; t += R, cell += cs) {
+              const C Av = A[kBandWarps * t];
+              *cell = fma2(splat(Av.y), bzr, fma2(splat(Av.x), bz, *cell));
+            }
+          } else {
+            const C b0 = cmul_conj(fr[rank * S + c], z), b1 = cmul_conj(fr[(rank + 1) * S + c], z);
+            const C b2 = rank > 2 ? cmul_conj(fr[(rank + 2) * S + c], z) : C{0, 0};
+            for (int t = r; t < nrows; t += R, cell += cs) {
+              const int j = kBandWarps * t;
+              C cv = *cell;
+              cfma_conj(cv, A[j], b0);
+              cfma_conj(cv, A[S + j], b1);
+              if (rank > 2) cfma_conj(cv, A[2 * S + j], b2);
+              *cell = cv;
+            }
           }
         }
       }
