@@ -284,11 +284,17 @@ __global__ void __launch_bounds__(kBandWarps * 32, 4) wgrid_band_kernel(const WA
     const WChunk cr = a.chunks[ch];
     const BandStage<real> sg = stage(buf);
     const int nv = cr.vis_end - cr.vis_begin;
-    // prep, once per visibility: conj(weight) y (G^H holds the conjugated
-    // entries of G) and the staged factor offset
-    for (int v = threadIdx.x; v < nv; v += blockDim.x) {
-      sg.w[v] = cmul_conj(sg.w[v], sg.y[v]);
-      sg.rel[v] = int(sg.fo[v] - band_base<real>(cr));
+    // prep, one warp per visibility: the staged factor offset, and the column
+    // factors replaced in place by conj(B_e[c]) z with z = conj(weight) y
+    // (G^H holds the conjugated entries of G), so
+    // conj(K[jv][c]) z = sum_e conj(A_e[jv]) B'_e[c]
+    for (int v = warp; v < nv; v += kBandWarps) {
+      const int code = sg.code[v], S = (code >> 16) & 0xff, rank = row_rank(code);
+      const int rel = int(sg.fo[v] - band_base<real>(cr));
+      const C z = cmul_conj(sg.w[v], sg.y[v]);
+      C *B = sg.f + rel + rank * S;
+      for (int k = lane; k < rank * S; k += 32) B[k] = cmul_conj(B[k], z);
+      if (lane == 0) sg.rel[v] = rel;
     }
     __syncthreads();
     for (int v = 0; v < nv; ++v) {
@@ -303,21 +309,18 @@ __global__ void __launch_bounds__(kBandWarps * 32, 4) wgrid_band_kernel(const WA
         int R, r, c;
         lane_layout(S, lane, R, r, c);
         if (r < R) {
-          // conj(K[jv][c]) z = sum_e conj(A_e[jv]) (conj(B_e[c]) z): the
-          // column part bz_e is formed once per visibility
-          const C z = sg.w[v];
           C *cell = win + (lp + jv0 + kBandWarps * r) * WW + lq + c;
           const int cs = kBandWarps * R * WW;
           const C *A = fr + jv0;
           if (rank == 1) {
-            const C bz = cmul_conj(fr[S + c], z), bzr{bz.y, -bz.x};
+            const C bz = fr[S + c], bzr{bz.y, -bz.x};
             for (int t = r; t < nrows; t += R, cell += cs) {
               const C Av = A[kBandWarps * t];
               *cell = fma2(splat(Av.y), bzr, fma2(splat(Av.x), bz, *cell));
             }
           } else {
-            const C b0 = cmul_conj(fr[rank * S + c], z), b1 = cmul_conj(fr[(rank + 1) * S + c], z);
-            const C b2 = rank > 2 ? cmul_conj(fr[(rank + 2) * S + c], z) : C{0, 0};
+            const C b0 = fr[rank * S + c], b1 = fr[(rank + 1) * S + c];
+            const C b2 = rank > 2 ? fr[(rank + 2) * S + c] : C{0, 0};
             for (int t = r; t < nrows; t += R, cell += cs) {
               const int j = kBandWarps * t;
               C cv = *cell;
