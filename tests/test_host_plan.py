@@ -160,7 +160,9 @@ def test_batch_lanes_are_bank_classes(pg):
     """Items sit on the lane of their bank class (window offset lp * stride +
     lq = lane, mod 16) wherever that lane was free, so half-warps mostly touch
     distinct shared-memory bank pairs at each tap offset; the stride is the
-    widest window.  Which items form a batch does not depend on the lanes."""
+    widest window.  A batch holds at most 4 items of a class, spread over the
+    two half-warps, so a half-warp's lane-block access mostly costs at most
+    two wavefronts per class."""
     from purify_gb300 import synthetic
     u, v = synthetic.mixed_uv(200_000, 512, 512, 0.7, 0.15, seed=3)
     p = pg.CoveragePlan(u, v, 512, 512, 6)
@@ -168,9 +170,19 @@ def test_batch_lanes_are_bank_classes(pg):
     lp, lq, cnt = lc & 0xFF, (lc >> 8) & 0xFF, lc >> 16
     r = (lp * p.win_cols + lq) & 15
     lane = np.arange(32)[None, :] & 15
-    on_class = ((r == lane) & (cnt > 0)).sum() / (cnt > 0).sum()
+    valid = cnt > 0
+    on_class = ((r == lane) & valid).sum() / valid.sum()
     assert on_class > 0.6
-    assert (cnt > 0).mean() > 0.9
+    assert valid.mean() > 0.9
+    per_batch, per_half = [], []
+    for b in range(lc.shape[0]):
+        per_batch.append(np.bincount(r[b][valid[b]], minlength=16).max())
+        for h in range(2):
+            sel = slice(16 * h, 16 * h + 16)
+            if valid[b][sel].any():
+                per_half.append(np.bincount(r[b][sel][valid[b][sel]], minlength=16).max())
+    assert max(per_batch) <= 4
+    assert np.mean(per_half) < 2.3
 
 
 @pytest.mark.parametrize("bad", [np.nan, np.inf, -np.inf])
