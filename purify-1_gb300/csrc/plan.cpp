@@ -28,9 +28,10 @@ double wrap(double x, double y) {
 }
 
 // Most items of one shared-memory bank class in a batch (see the packing).
-// At the 10^7-visibility workload, 4 costs 0.8% more slots and leaves a
-// lane-block access about 4.2 wavefronts instead of 5.0; 3 costs 3.4% slots
-// and measured slower, 2 costs 16%.
+// At the 10^7-visibility workload a lane-block access then costs about 3.2
+// shared-memory wavefronts instead of 5.0 (2 is the floor) for 2% more
+// slots; a cap of 3 over the whole batch cost 3.4% slots and measured
+// slower, a cap of 2 cost 16%.
 constexpr int kClassCap = 4;
 
 struct Item {
@@ -167,8 +168,10 @@ Plan build_plan(const PlanRequest &rq) {
                        [](const Item &x, const Item &y) { return x.count > y.count; });
       // Greedy packing: scan the pending items in order and take one unless
       // its base cell is already in the batch or the batch already holds
-      // kClassCap items of its bank class; the scan gives up 256 clashes past
-      // the first pending item.  The bank class of an item is its window
+      // too many items of its bank class; a scan gives up 256 clashes past
+      // the first pending item.  The first scan takes only items of the front
+      // item's count, at most two per class; the second fills the batch from
+      // the front at kClassCap per class.  The bank class of an item is its window
       // offset lp * WS + lq mod 16: at every (jv, ju) offset of their blocks,
       // the lanes of a half-warp that share a class hit the same 8-byte bank
       // pair, and each extra one costs a shared-memory wavefront.  An item of
@@ -188,35 +191,44 @@ Plan build_plan(const PlanRequest &rq) {
         int class_count[16] = {0};
         int half_class[2][16] = {{0}};
         int filled = 0;
-        size_t skipped = 0;
-        for (size_t k = front; k < items.size() && filled < kBatch; ++k) {
-          if (taken[k]) continue;
-          const int r = (items[k].lp * WS + items[k].lq) & 15;
-          int lane = lane_item[r] < 0 ? r : (lane_item[16 + r] < 0 ? 16 + r : -1);
-          if (lane < 0) {
-            // both class lanes taken: a free lane in the half-warp holding
-            // fewer items of this class
-            const int h0 = half_class[0][r] <= half_class[1][r] ? 0 : 1;
-            for (int hh = 0; hh < 2 && lane < 0; ++hh) {
-              const int h = hh == 0 ? h0 : 1 - h0;
-              for (int l = 16 * h; l < 16 * h + 16; ++l)
-                if (lane_item[l] < 0) {
-                  lane = l;
-                  break;
-                }
+        // one scan from the front: cap items per class; with same_count >= 0
+        // only the items of that count (a contiguous run of the sorted list)
+        auto scan = [&](int cap, int same_count) {
+          size_t skipped = 0;
+          for (size_t k = front; k < items.size() && filled < kBatch; ++k) {
+            if (same_count >= 0 && items[k].count != same_count) break;
+            if (taken[k]) continue;
+            const int r = (items[k].lp * WS + items[k].lq) & 15;
+            int lane = lane_item[r] < 0 ? r : (lane_item[16 + r] < 0 ? 16 + r : -1);
+            if (lane < 0) {
+              // both class lanes taken: a free lane in the half-warp holding
+              // fewer items of this class
+              const int h0 = half_class[0][r] <= half_class[1][r] ? 0 : 1;
+              for (int hh = 0; hh < 2 && lane < 0; ++hh) {
+                const int h = hh == 0 ? h0 : 1 - h0;
+                for (int l = 16 * h; l < 16 * h + 16; ++l)
+                  if (lane_item[l] < 0) {
+                    lane = l;
+                    break;
+                  }
+              }
             }
+            if (stamp[items[k].cell] == batch_id || lane < 0 || class_count[r] >= cap) {
+              if (++skipped > 256) break;
+              continue;
+            }
+            ++class_count[r];
+            ++half_class[lane >> 4][r];
+            stamp[items[k].cell] = batch_id;
+            taken[k] = 1;
+            lane_item[lane] = int64_t(k);
+            ++filled;
           }
-          if (stamp[items[k].cell] == batch_id || lane < 0 || class_count[r] >= kClassCap) {
-            if (++skipped > 256) break;
-            continue;
-          }
-          ++class_count[r];
-          ++half_class[lane >> 4][r];
-          stamp[items[k].cell] = batch_id;
-          taken[k] = 1;
-          lane_item[lane] = int64_t(k);
-          ++filled;
-        }
+        };
+        // first the items of the front item's count (no null slots among
+        // them) at two per class, then the rest of the batch at kClassCap
+        scan(2, items[front].count);
+        scan(kClassCap, -1);
         int kmax = 0;
         for (int l = 0; l < kBatch; ++l)
           if (lane_item[l] >= 0) kmax = std::max(kmax, int(items[lane_item[l]].count));
