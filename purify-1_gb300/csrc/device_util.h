@@ -81,5 +81,24 @@ struct Traits<double> {
   }
 };
 
+// cuFFT plan of the Nu columns of an Nv x Nu row-major grid (length Nv,
+// stride Nu, one column after the other), bound to `s`; its work area is
+// added to *bytes.
+template <typename real>
+inline cufftHandle make_column_plan(int Nu, int Nv, cudaStream_t s, int64_t *bytes) {
+  cufftHandle h = 0;
+  int n[1] = {Nv}, embed[1] = {Nv};
+  cufft_check(cufftPlanMany(&h, 1, n, embed, Nu, 1, embed, Nu, 1, Traits<real>::kType, Nu),
+              "cufftPlanMany");
+  const cufftResult r = cufftSetStream(h, s);
+  if (r != CUFFT_SUCCESS) {
+    cufftDestroy(h);
+    cufft_check(r, "cufftSetStream");
+  }
+  size_t ws = 0;
+  if (bytes && cufftGetSize(h, &ws) == CUFFT_SUCCESS) *bytes += int64_t(ws);
+  return h;
+}
+
 
 }  // namespace pg

@@ -15,6 +15,7 @@
 
 #include "device_kernels.h"
 #include "device_util.h"
+#include "fft_kernels.h"
 #include "gridding_kernels.h"
 #include "no_alloc.h"
 #include "plan.h"
@@ -84,6 +85,7 @@ class OperatorT final : public Operator {
   void degrid_on_stream(const void *grid, void *y);
   void grid_on_stream(const void *y, void *grid);
   // Phi' / Phi'^H with visibilities kept in slot order (power method).
+  FftArgs fft_args() const;
   void forward_slots(const void *x, void *caller_vis = nullptr);
   void adjoint_slots(void *x, const void *caller_vis = nullptr);
   void join(cudaStream_t user);
@@ -118,6 +120,12 @@ class OperatorT final : public Operator {
   cudaEvent_t ev_in_ = nullptr, ev_out_ = nullptr;
   cufftHandle fft_ = 0;
   bool fft_ok_ = false;
+  // FP32 with a power-of-two grid width: fused row passes + a cuFFT column
+  // transform (fft_kernels.h) replace Z S + 2-D FFT and 2-D FFT + S^H Z^H.
+  bool fused_fft_ = false;
+  cufftHandle fft_cols_ = 0;
+  DeviceBuffer tw_u_;
+  bool use_fused_fft() const { return fused_fft_ && ws_->fft_cols != 0; }
   std::mutex mu_;
 
   DeviceBuffer task_order_, frac_, weight_, slot_user_, user_slot_, batches_, lane_code_, tasks_, tile_tasks_,
@@ -245,6 +253,14 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
   }
   cufft_check(cufftPlan2d(&fft_, Nv_, Nu_, Traits<real>::kType), "cufftPlan2d");
   fft_ok_ = true;
+  if (sizeof(real) == 4 && fft_rows_supported(Nu_)) {
+    const std::vector<float> twu = fft_twiddles(Nu_);
+    tw_u_.alloc(sizeof(float) * twu.size(), &bytes);
+    tw_u_.upload(twu.data(), sizeof(float) * twu.size(), stream_);
+    cuda_check(cudaStreamSynchronize(stream_), "twiddle upload");
+    fft_cols_ = make_column_plan<real>(Nu_, Nv_, stream_, &bytes);
+    fused_fft_ = true;
+  }
   cufft_check(cufftSetStream(fft_, stream_), "cufftSetStream");
   size_t ws = 0;
   if (cufftGetSize(fft_, &ws) == CUFFT_SUCCESS) bytes += int64_t(ws);
@@ -253,6 +269,7 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
   own_.tilebuf = tilebuf_.get();
   own_.slots = slots_.get();
   own_.fft = fft_;
+  own_.fft_cols = fft_cols_;
   own_.stream = stream_;
   {
     // Phi' (norm 1) correction for power-method workspaces.
@@ -449,6 +466,7 @@ OperatorT<real>::~OperatorT() {
   drop_graphs();
   for (cudaEvent_t e : event_pool_) cudaEventDestroy(e);
   if (fft_ok_) cufftDestroy(fft_);
+  if (fft_cols_) cufftDestroy(fft_cols_);
   if (ev_in_) cudaEventDestroy(ev_in_);
   if (ev_out_) cudaEventDestroy(ev_out_);
   if (stream_) cudaStreamDestroy(stream_);
@@ -636,7 +654,32 @@ void OperatorT<real>::grid_on_stream(const void *y, void *grid) {
 }
 
 template <typename real>
+FftArgs OperatorT<real>::fft_args() const {
+  FftArgs f;
+  f.Nx = Nx_;
+  f.Ny = Ny_;
+  f.Nu = Nu_;
+  f.Nv = Nv_;
+  f.x0 = x0_;
+  f.y0 = y0_;
+  f.su = reinterpret_cast<const float *>(su_active());
+  f.sv = reinterpret_cast<const float *>(sv_d_.get());
+  f.tw_u = tw_u_.get();
+  return f;
+}
+
+template <typename real>
 void OperatorT<real>::forward_slots(const void *x, void *caller_vis) {
+  if (use_fused_fft()) {
+    // row transforms of the image rows into ws->pad (its other rows stay
+    // zero), then the column transform into ws->work
+    mark_begin(kFftF);
+    cuda_check(launch_fft_rows_forward(fft_args(), x, ws_->pad, ws_->stream), "fft rows");
+    cufft_check(Traits<real>::exec(ws_->fft_cols, ws_->pad, ws_->work, CUFFT_FORWARD), "cufftExec");
+    mark_end(kFftF);
+    degrid_slots(ws_->work, caller_vis);
+    return;
+  }
   mark_begin(kPad);
   cuda_check(launch_pad<real>(x, su_active(), sv_d_.as<real>(), ws_->pad, Nx_, Ny_, Nu_,
                               x0_, y0_, ws_->stream),
@@ -651,6 +694,13 @@ void OperatorT<real>::forward_slots(const void *x, void *caller_vis) {
 template <typename real>
 void OperatorT<real>::adjoint_slots(void *x, const void *caller_vis) {
   grid_slots(ws_->work, caller_vis);
+  if (use_fused_fft()) {
+    mark_begin(kFftI);
+    cufft_check(Traits<real>::exec(ws_->fft_cols, ws_->work, ws_->work, CUFFT_INVERSE), "cufftExec");
+    cuda_check(launch_fft_rows_inverse(fft_args(), ws_->work, x, ws_->stream), "fft rows");
+    mark_end(kFftI);
+    return;
+  }
   mark_begin(kFftI);
   cufft_check(Traits<real>::exec(ws_->fft, ws_->work, ws_->work, CUFFT_INVERSE), "cufftExec");
   mark_end(kFftI);

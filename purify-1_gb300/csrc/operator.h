@@ -71,6 +71,10 @@ struct Workspace {
   void *tilebuf = nullptr;  // accumulation windows of the tasks
   void *slots = nullptr;    // slot-ordered visibilities
   int fft = 0;              // cuFFT plan (cufftHandle) of Nv x Nu, bound to `stream`
+  // FP32 grids with power-of-two widths: a cuFFT plan of the Nu columns
+  // (length Nv, stride Nu), bound to `stream`; with it the operator runs the
+  // fused row passes (fft_kernels.h) instead of pad + 2-D FFT + crop.
+  int fft_cols = 0;
   cudaStream_t stream = nullptr;
   bool unit_norm = false;   // apply Phi' (norm 1) instead of Phi
 };

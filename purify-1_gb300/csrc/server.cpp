@@ -11,6 +11,7 @@
 
 #include "device_kernels.h"
 #include "device_util.h"
+#include "fft_kernels.h"
 
 namespace pg {
 namespace {
@@ -38,6 +39,7 @@ struct Server::Coverage {
 struct Server::Slot {
   cudaStream_t stream = nullptr;
   std::map<int64_t, cufftHandle> plans;  // key: fp64 | Nu << 1 | Nv << 32
+  std::map<int64_t, cufftHandle> col_plans;  // FP32 column transforms, same key
   bool busy = false;
 };
 
@@ -98,6 +100,7 @@ Server::~Server() {
   for (auto &s : slots_) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     for (auto &kv : s->plans) cufftDestroy(kv.second);
+    for (auto &kv : s->col_plans) cufftDestroy(kv.second);
     if (s->stream) cudaStreamDestroy(s->stream);
   }
   if (pool_) cudaMemPoolDestroy(pool_);
@@ -136,6 +139,10 @@ int Server::add_coverage(const OperatorConfig &cfg_in) {
       cufft_check(r, "cufftSetStream");
     }
     s->plans[key] = h;
+    // the column transform of the fused FFT path (fft_kernels.h)
+    if (!c->fp64 && fft_rows_supported(int(c->info.ftsizeu)))
+      s->col_plans[key] =
+          make_column_plan<float>(int(c->info.ftsizeu), int(c->info.ftsizev), s->stream, nullptr);
   }
   std::lock_guard<std::mutex> ck(cov_mu_);
   coverages_.push_back(std::move(c));
@@ -333,7 +340,10 @@ bool Server::enqueue(Job &j) {
     ws.work = take(size_t(c.ws.work));
     ws.tilebuf = take(size_t(c.ws.tilebuf));
     ws.slots = take(size_t(c.ws.slots));
-    ws.fft = slot.plans.at(plan_key(c.fp64, int(c.info.ftsizeu), int(c.info.ftsizev)));
+    const int64_t key = plan_key(c.fp64, int(c.info.ftsizeu), int(c.info.ftsizev));
+    ws.fft = slot.plans.at(key);
+    const auto cp = slot.col_plans.find(key);
+    ws.fft_cols = cp == slot.col_plans.end() ? 0 : cp->second;
     ws.stream = s;
     // the padded grid must be zero outside the image region
     cuda_check(cudaMemsetAsync(ws.pad, 0, size_t(c.ws.pad), s), "cudaMemsetAsync");

@@ -111,6 +111,36 @@ def test_kernels_and_supports(pg, oracle_mod, cuda, kernel, J, precision):
     assert rel_l2(xx, oop.adjoint(yy)) < TOL[precision]
 
 
+@pytest.mark.parametrize("ny,nx,os", [
+    (32, 32, 2.0),       # 64^2 grid, the smallest fused size
+    (64, 128, 2.0),      # 128 x 256, non-square
+    (80, 40, 1.6),       # 128 x 64 grid around a non-power-of-two image (x0 = 12, y0 = 24)
+    (256, 256, 2.0),     # 512^2
+    (1024, 2048, 2.0),   # 2048 x 4096: the largest row and column lengths
+])
+def test_fused_fft_grids(pg, oracle_mod, cuda, ny, nx, os):
+    """FP32 operators on grids of power-of-two width run the fused row passes
+    (correction + padding + row FFT, row FFT + cropping + correction) with a
+    column FFT instead of pad + 2-D FFT + crop; both directions against the
+    oracle and the adjoint dot-product test."""
+    torch = cuda
+    rng = np.random.default_rng(ny + nx)
+    M = 5000
+    Nu, Nv = int(np.floor(os * nx)), int(np.floor(os * ny))
+    u = rng.uniform(-Nu / 2, Nu / 2, M)
+    v = rng.uniform(-Nv / 2, Nv / 2, M)
+    gop, oop = make_pair(pg, oracle_mod, u, v, ny, nx, "kb", 4, None, "fp32", os)
+    x = rng.standard_normal(ny * nx) + 1j * rng.standard_normal(ny * nx)
+    y = to_np(gop.forward(to_dev(torch, x, "fp32")))
+    assert rel_l2(y, oop.forward(x)) < TOL["fp32"]
+    yy = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    xx = to_np(gop.adjoint(to_dev(torch, yy, "fp32")))
+    assert rel_l2(xx, oop.adjoint(yy)) < TOL["fp32"]
+    lhs = np.vdot(yy, y)
+    rhs = np.vdot(xx, x)
+    assert abs(lhs - rhs) <= DOT_TOL["fp32"] * np.linalg.norm(y) * np.linalg.norm(yy)
+
+
 @pytest.mark.parametrize("precision", ["fp32", "fp64"])
 @pytest.mark.parametrize("ny,nx,os,spread", [
     (20, 36, 2.0, 30.0),     # non-square, non power of two grid (40 x 72)
