@@ -324,7 +324,9 @@ def run_gb300(args):
                        "p99": float(np.percentile(per_step, 99))},
         "create_s": t_create, "power_method_s": t_power, "norm": norm,
         "stages_ms_per_launch": {k: (ms / nl if nl else None) for k, (ms, nl) in stages.items()},
-        "gpu_launches": 5 * args.steps,
+        # own kernels per step: the forward row pass (or pad), degrid, expand,
+        # grid, fold, the inverse row pass (or crop)
+        "gpu_launches": 6 * args.steps,
         "clocks": clocks,
     }
 
@@ -862,9 +864,10 @@ def run_serve(args):
         "latency_ms": f32["latency_ms"], "serving": {k: {kk: vv for kk, vv in v.items()
                                                           if kk != "_res"}
                                                       for k, v in per_prec.items()},
-        # own kernels per request (FP32): conversions, pad, degrid, expand,
-        # grid, fold, crop; a norm round: pad, degrid, grid, fold, crop, two
-        # reduction kernels and the scale
+        # own kernels per request (FP32): conversions, the forward row pass
+        # (or pad), degrid, expand, grid, fold, the inverse row pass (or crop);
+        # a norm round: both row passes, degrid, grid, fold, two reduction
+        # kernels and the scale
         "gpu_launches": int(sum({"forward_adjoint": 9, "adjoint": 6}.get(str(k), 1 + 8 * 50)
                                 for k in kinds)),
     }
