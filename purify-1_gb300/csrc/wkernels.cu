@@ -76,10 +76,10 @@ __device__ __forceinline__ int row_rank(int code) { return __popc((code >> 24) &
 
 
 // G^H of the w-projection rows with one window per CTA.  The window's rows
-// are dealt to the kBandWarps warps in turn (row p to warp p mod kBandWarps)
-// and every warp walks all of the task's visibilities in plan order, updating
-// only its own rows: each cell has one writer, which adds the visibilities in
-// plan order.  The rows' factors, codes, weights and visibilities are staged
+// are cut into kBandWarps contiguous bands, one per warp, and every warp walks
+// the task's visibilities in plan order, updating only the rows of its band
+// (a visibility whose rows miss the band costs the warp a comparison): each
+// cell has one writer, which adds the visibilities in plan order.  The rows' factors, codes, weights and visibilities are staged
 // in shared memory one chunk (WChunk) at a time, the next chunk's copies in
 // flight (cp.async) while the current one is gridded.
 constexpr int kBandWarps = 8;
@@ -265,6 +265,9 @@ __global__ void __launch_bounds__(kBandWarps * 32, 4) wgrid_band_kernel(const WA
   const Task tk = a.tasks[task_id];
   const int WW = tk.W + a.Smax - 1, WH = tk.H + a.Smax - 1, WN = WW * WH;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // this warp's band of window rows
+  const int band_h = (WH + kBandWarps - 1) / kBandWarps;
+  const int band0 = min(warp * band_h, WH), band1 = min(band0 + band_h, WH);
   C *win = reinterpret_cast<C *>(smem_raw);
   const size_t sb = band_stage_bytes<real>(a.chunk_values);
   auto stage = [&](int buf) {
@@ -300,29 +303,29 @@ __global__ void __launch_bounds__(kBandWarps * 32, 4) wgrid_band_kernel(const WA
     for (int v = 0; v < nv; ++v) {
       const int code = sg.code[v];
       const int lp = code & 0xff, S = (code >> 16) & 0xff;
-      // this warp's first row of the visibility: (lp + jv0) = warp (mod kBandWarps)
-      const int jv0 = (warp - lp) & (kBandWarps - 1);
-      if (jv0 < S) {
+      // the rows of the visibility inside this warp's band
+      const int lo = max(lp, band0), hi = min(lp + S, band1);
+      if (lo < hi) {
         const int lq = (code >> 8) & 0xff, rank = row_rank(code);
         const C *fr = sg.f + sg.rel[v];
-        const int nrows = (S - 1 - jv0) / kBandWarps + 1;
+        const int jv0 = lo - lp, nrows = hi - lo;
         int R, r, c;
         lane_layout(S, lane, R, r, c);
         if (r < R) {
-          C *cell = win + (lp + jv0 + kBandWarps * r) * WW + lq + c;
-          const int cs = kBandWarps * R * WW;
+          C *cell = win + (lo + r) * WW + lq + c;
+          const int cs = R * WW;
           const C *A = fr + jv0;
           if (rank == 1) {
             const C bz = fr[S + c], bzr{bz.y, -bz.x};
             for (int t = r; t < nrows; t += R, cell += cs) {
-              const C Av = A[kBandWarps * t];
+              const C Av = A[t];
               *cell = fma2(splat(Av.y), bzr, fma2(splat(Av.x), bz, *cell));
             }
           } else {
             const C b0 = fr[rank * S + c], b1 = fr[(rank + 1) * S + c];
             const C b2 = rank > 2 ? fr[(rank + 2) * S + c] : C{0, 0};
             for (int t = r; t < nrows; t += R, cell += cs) {
-              const int j = kBandWarps * t;
+              const int j = t;
               C cv = *cell;
               cfma_conj(cv, A[j], b0);
               cfma_conj(cv, A[S + j], b1);
