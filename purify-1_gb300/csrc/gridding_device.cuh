@@ -76,6 +76,26 @@ __device__ __forceinline__ void cp_async(void *smem, const void *gmem) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem), "n"(BYTES)
                  : "memory");
 }
+// The same copy with an L2 evict-first policy, for streams read once (the
+// coverage state): their lines leave L2 before those of the kernel's output.
+template <int BYTES>
+__device__ __forceinline__ void cp_async_stream(void *smem, const void *gmem,
+                                                unsigned long long pol) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  if (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;\n" ::"r"(s),
+                 "l"(gmem), "l"(pol)
+                 : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], %2, %3;\n" ::"r"(s),
+                 "l"(gmem), "n"(BYTES), "l"(pol)
+                 : "memory");
+}
+__device__ __forceinline__ unsigned long long l2_stream_policy() {
+  unsigned long long p;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
@@ -206,15 +226,16 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
   C *st_t = reinterpret_cast<C *>(stg);
   int *st_m = reinterpret_cast<int *>(stg + 2 * CH * 32 * sizeof(C));
   C *st_w = reinterpret_cast<C *>(stg + 2 * CH * 32 * (sizeof(C) + (user ? 4 : 0)));
+  const unsigned long long pol = l2_stream_policy();
   auto issue = [&](int lb, int k0, int buf) {
     const int2 bt = th.hdr[lb];
     const int n = min(CH, bt.y - k0);
     for (int j = 0; j < n; ++j) {
       const size_t i = size_t(bt.x) + size_t(k0 + j) * kBatch + lane;
       const int e = (buf * CH + j) * 32 + lane;
-      cp_async<sizeof(C)>(st_t + e, frac + i);
-      if (user) cp_async<4>(st_m + e, user + i);
-      if (!unit) cp_async<sizeof(C)>(st_w + e, weight + i);
+      cp_async_stream<sizeof(C)>(st_t + e, frac + i, pol);
+      if (user) cp_async_stream<4>(st_m + e, user + i, pol);
+      if (!unit) cp_async_stream<sizeof(C)>(st_w + e, weight + i, pol);
     }
     cp_async_commit();
   };
