@@ -135,7 +135,7 @@ __device__ __forceinline__ cplx<real> read_vis(const ApplyArgs<real> &a, const c
     const int m = __ldcs(a.slot_user + i);
     return m >= 0 ? vin[m] : cplx<real>{0, 0};
   }
-  return vin[i];
+  return __ldcs(vin + i);  // read once: streaming
 }
 
 // Operator arguments of a task.  A single-operator launch reads them from the
