@@ -64,7 +64,7 @@ __global__ void expand_kernel(const cplx<real> *__restrict__ in,
     for (int r = 0; r < kPermUnroll; ++r) v[r] = m[r] >= 0 ? in[m[r]] : cplx<real>{0, 0};
 #pragma unroll
     for (int r = 0; r < kPermUnroll; ++r)
-      if (s0 + r * stride < S) slots[s0 + r * stride] = v[r];
+      if (s0 + r * stride < S) __stcs(slots + s0 + r * stride, v[r]);
   }
 }
 
