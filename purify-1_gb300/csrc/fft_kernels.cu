@@ -1,7 +1,7 @@
 // Fused row passes of the padded-grid FFT (see fft_kernels.h).
 //
-// Each pass is a Stockham auto-sort FFT of length N = 8^a * {1, 2, 4} over V
-// rows per CTA, 256 threads.  Stage s with radix R and sub-transform length
+// Each pass is a Stockham auto-sort FFT of length N = 16^a * {1, 2, 4, 8} over
+// V rows per CTA, 256 threads.  Stage s with radix R and sub-transform length
 // Ns takes, for butterfly j < N / R, the inputs j + r N / R, multiplies input
 // r by w^(r (j mod Ns)) with w = exp(-+2 pi i / (Ns R)), does an R-point DFT
 // in registers and writes output r to (j / Ns) Ns R + (j mod Ns) + r Ns; after
@@ -45,10 +45,53 @@ __device__ __forceinline__ float2 mul_w8_3(float2 a) {
   return INV ? make_float2(-h * (a.x + a.y), h * (a.x - a.y)) : make_float2(h * (a.y - a.x), -h * (a.x + a.y));
 }
 
+// exp(-+2 pi i m / 16) for the 16-point DFT's inner twiddles (m = n2 k1).
+template <bool INV>
+__device__ __forceinline__ float2 w16(int m) {
+  constexpr float c1 = 0.92387953251128676f, s1 = 0.38268343236508977f,
+                  h = 0.70710678118654752f;
+  float c = 1.f, sn = 0.f;  // cos, sin of 2 pi m / 16
+  switch (m) {
+    case 1: c = c1; sn = s1; break;
+    case 2: c = h; sn = h; break;
+    case 3: c = s1; sn = c1; break;
+    case 4: c = 0.f; sn = 1.f; break;
+    case 6: c = -h; sn = h; break;
+    case 9: c = -c1; sn = -s1; break;
+  }
+  return make_float2(c, INV ? sn : -sn);
+}
+
+template <int R, bool INV>
+__device__ __forceinline__ void dft(float2 *v);
+
+// 16-point DFT as 4 x 4: DFT-4 over n1 of v[4 n1 + n2] for each n2, times
+// w16^(n2 k1), then DFT-4 over n2 for each k1 into X[k1 + 4 k2].
+template <bool INV>
+__device__ __forceinline__ void dft16(float2 *v) {
+  float2 a[4][4];
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) {
+    float2 t[4] = {v[n2], v[4 + n2], v[8 + n2], v[12 + n2]};
+    dft<4, INV>(t);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) a[n2][k1] = (n2 && k1) ? cmulf(t[k1], w16<INV>(n2 * k1)) : t[k1];
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    float2 t[4] = {a[0][k1], a[1][k1], a[2][k1], a[3][k1]};
+    dft<4, INV>(t);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = t[k2];
+  }
+}
+
 // Natural-order R-point DFT in registers, X_k = sum_m v_m exp(-+2 pi i m k / R).
 template <int R, bool INV>
 __device__ __forceinline__ void dft(float2 *v) {
-  if constexpr (R == 2) {
+  if constexpr (R == 16) {
+    dft16<INV>(v);
+  } else if constexpr (R == 2) {
     const float2 a = v[0], b = v[1];
     v[0] = cadd(a, b);
     v[1] = csub(a, b);
@@ -60,7 +103,7 @@ __device__ __forceinline__ void dft(float2 *v) {
     v[1] = cadd(t1, t3);
     v[3] = csub(t1, t3);
   } else {
-    static_assert(R == 8, "radix 2, 4 or 8");
+    static_assert(R == 8, "radix 2, 4, 8 or 16");
     float2 e[4] = {v[0], v[2], v[4], v[6]}, o[4] = {v[1], v[3], v[5], v[7]};
     dft<4, INV>(e);
     dft<4, INV>(o);
@@ -117,31 +160,37 @@ __device__ __forceinline__ int sidx(int row, int n) {
 // Twiddles w^r, r = 1 ... R-1, of w = exp(-+2 pi i k / (Ns R)) from w, w^2
 // and w^4 (loaded from the table): the others as one product of two of them.
 template <int R>
-__device__ __forceinline__ void twiddle(float2 *v, const float2 (&w)[3]) {
-  v[1] = cmulf(v[1], w[0]);
-  if constexpr (R >= 4) {
-    v[2] = cmulf(v[2], w[1]);
-    v[3] = cmulf(v[3], cmulf(w[0], w[1]));
-    if constexpr (R == 8) {
-      v[4] = cmulf(v[4], w[2]);
-      v[5] = cmulf(v[5], cmulf(w[0], w[2]));
-      v[6] = cmulf(v[6], cmulf(w[1], w[2]));
-      v[7] = cmulf(v[7], cmulf(cmulf(w[0], w[1]), w[2]));
-    }
+__device__ __forceinline__ void twiddle(float2 *v, const float2 (&w)[4]) {
+  // w^r from the loaded powers w^(2^e): the product over the set bits of r
+  float2 p[R];
+  p[1] = w[0];
+#pragma unroll
+  for (int r = 2; r < R; ++r) {
+    const int top = 31 - __clz(r), low = r - (1 << top);  // compile-time after unrolling
+    p[r] = low ? cmulf(p[low], w[top]) : w[top];
   }
+#pragma unroll
+  for (int r = 1; r < R; ++r) v[r] = cmulf(v[r], p[r]);
 }
 
 // The twiddles of every stage after the first, loaded in the prologue
 // together with the first stage's data so that one load latency covers them.
-constexpr int kMaxStages = 4, kMaxQ = 4;
+constexpr int kMaxStages = 4, kMaxQ = 8, kMaxPow = 4;
 struct TwiddleCache {
-  float2 w[kMaxStages][kMaxQ][3];
+  float2 w[kMaxStages][kMaxQ][kMaxPow];
+};
+
+// Radix of the stage with sub-transform length Ns: 16 while it divides the
+// rest, then the remainder (2, 4 or 8).
+template <int N, int Ns>
+struct StageRadix {
+  static constexpr int rem = N / Ns;
+  static constexpr int value = rem % 16 == 0 ? 16 : rem;
 };
 
 template <int N, int V, int Ns, int S, bool INV>
 __device__ __forceinline__ void load_twiddles(TwiddleCache &c, const float2 *__restrict__ tw) {
-  constexpr int rem = N / Ns;
-  constexpr int R = rem % 8 == 0 ? 8 : rem;
+  constexpr int R = StageRadix<N, Ns>::value;
   constexpr int NB = V * (N / R);
   constexpr int Q = (NB + kFftThreads - 1) / kFftThreads;
   static_assert(S < kMaxStages && Q <= kMaxQ, "twiddle cache size");
@@ -152,7 +201,7 @@ __device__ __forceinline__ void load_twiddles(TwiddleCache &c, const float2 *__r
       const int j = flat % (N / R);
       const int step = (j % Ns) * (N / (Ns * R));
 #pragma unroll
-      for (int e = 0; e < 3; ++e) {
+      for (int e = 0; e < kMaxPow; ++e) {
         if ((1 << e) < R && flat < NB) {
           float2 w = __ldg(tw + (step << e));
           if (INV) w.y = -w.y;
@@ -169,8 +218,7 @@ template <int N, int V, int Ns, int S, bool INV>
 __device__ __forceinline__ void run_stages(const FftArgs &a, const float2 *__restrict__ in,
                                            float2 *__restrict__ out, float2 *sm,
                                            const TwiddleCache &tc, int row0) {
-  constexpr int rem = N / Ns;
-  constexpr int R = rem % 8 == 0 ? 8 : rem;
+  constexpr int R = StageRadix<N, Ns>::value;
   constexpr bool FIRST = Ns == 1, LAST = Ns * R == N;
   constexpr int NB = V * (N / R);  // butterflies of the stage
   constexpr int Q = (NB + kFftThreads - 1) / kFftThreads;
@@ -218,7 +266,7 @@ __device__ __forceinline__ void run_stages(const FftArgs &a, const float2 *__res
 }
 
 template <int N, int V, bool INV>
-__global__ void __launch_bounds__(kFftThreads) fft_row_kernel(const FftArgs a,
+__global__ void __launch_bounds__(kFftThreads, 4) fft_row_kernel(const FftArgs a,
                                                               const float2 *__restrict__ in,
                                                               float2 *__restrict__ out) {
   extern __shared__ float2 fft_sm[];
@@ -227,8 +275,9 @@ __global__ void __launch_bounds__(kFftThreads) fft_row_kernel(const FftArgs a,
   run_stages<N, V, 1, 0, INV>(a, in, out, fft_sm, tc, int(blockIdx.x) * V);
 }
 
-// Rows per CTA: enough to give every thread a butterfly in the first stage.
-constexpr int rows_per_cta(int N) { return N >= 2048 ? 1 : 2048 / N; }
+// Rows per CTA: enough to give every thread a butterfly in the first
+// (radix-16) stage.
+constexpr int rows_per_cta(int N) { return N >= 4096 ? 1 : 4096 / N; }
 
 template <int N, bool INV>
 cudaError_t launch_rows(const FftArgs &a, const void *in, void *out, cudaStream_t s) {
