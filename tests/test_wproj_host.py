@@ -1,6 +1,8 @@
-"""w-projection rows on the CPU: the rank-3 factors the device stores rebuild
-the reference's row values (operators.cc:49-99 with projection_kernels.cc:
-16-85), compared with the oracle's explicit CSR rows."""
+"""w-projection rows on the CPU: the factors the device stores (only the
+nonzero terms of the rank-3 split: rank 1 where the validity rectangle covers
+all samples or none, up to 3 otherwise) rebuild the reference's row values
+(operators.cc:49-99 with projection_kernels.cc:16-85), compared with the
+oracle's explicit CSR rows."""
 import numpy as np
 import pytest
 
