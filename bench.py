@@ -291,6 +291,35 @@ def run_gb300(args):
         dist.barrier()
     total_ms = evs[0].elapsed_time(evs[-1])
     per_step = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
+    # forward and adjoint alone, each over the same number of steps (after
+    # the timed steps, so the headline number is unaffected)
+    directions = {}
+    for name, fn in (("forward", lambda: op.forward_into(xd, yd, stream)),
+                     ("adjoint", lambda: op.adjoint_into(yd, xo, stream))):
+        fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / args.steps
+        directions[name] = {"ms": ms, "mvis_s": M / (ms * 1e-3) / 1e6}
+    # adjoint dot-product test at full size, |<Phi x, y> - <x, Phi^H y>| /
+    # (||Phi x|| ||y||), with a seeded random y; FP64 sums on the device
+    gen = torch.Generator(device=dev).manual_seed(11)
+    yr = torch.complex(torch.randn(M, device=dev, generator=gen),
+                       torch.randn(M, device=dev, generator=gen)).to(torch.complex64)
+    xa = torch.empty(N, dtype=torch.complex64, device=dev)
+    op.forward_into(xd, yd, stream)
+    op.adjoint_into(yr, xa, stream)
+    torch.cuda.synchronize(dev)
+    lhs = torch.vdot(yr.to(torch.complex128), yd.to(torch.complex128))
+    rhs = torch.vdot(xa.to(torch.complex128), xd.to(torch.complex128))
+    adjoint_test = float(abs(lhs - rhs) / (torch.linalg.vector_norm(yd.to(torch.complex128)) *
+                                         torch.linalg.vector_norm(yr.to(torch.complex128))))
+    del yr, xa
     # per-stage breakdown in a separate pass (the events between stages are
     # not in the timed steps)
     op.stage_timing(True)
@@ -324,6 +353,8 @@ def run_gb300(args):
                        "p99": float(np.percentile(per_step, 99))},
         "create_s": t_create, "power_method_s": t_power, "norm": norm,
         "stages_ms_per_launch": {k: (ms / nl if nl else None) for k, (ms, nl) in stages.items()},
+        "directions": directions,
+        "adjoint_dot_test_fp32": adjoint_test,
         # own kernels per step: the forward row pass (or pad), degrid, expand,
         # grid, fold, the inverse row pass (or crop)
         "gpu_launches": 6 * args.steps,
