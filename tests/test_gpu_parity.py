@@ -3,7 +3,7 @@ golden vectors.  Every call goes through the C ABI (libpurify_gb300.so).
 
 Tolerances (relative L2 unless stated):
   FP64 GPU path vs oracle        1e-10
-  FP32 GPU path vs oracle        1e-5   (the BASELINE target for FP32)
+  FP32 GPU path vs oracle        1e-5   (the stated FP32 tolerance of the path)
   golden G / G^H (operators.cc)  1e-5   isApprox, as the reference test
   golden M31 Phi x               1e-6   isApprox after max-normalisation
   adjoint dot-product test       1e-6 (FP32), 1e-12 (FP64), relative to ||Phi x|| ||y||
