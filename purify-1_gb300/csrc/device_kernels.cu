@@ -48,11 +48,34 @@ __global__ void compact_kernel(const cplx<real> *__restrict__ slots,
       if (m0 + r * stride < M) __stcs(out + m0 + r * stride, v[r]);
   }
 }
+// Gathered loads of the caller-ordered visibilities at L2 evict-last
+// priority (launch_expand's keep_in).
+__device__ __forceinline__ unsigned long long l2_keep_policy() {
+  unsigned long long p;
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ float2 load_keep(const float2 *p, unsigned long long pol) {
+  float2 v;
+  asm volatile("ld.global.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;"
+               : "=f"(v.x), "=f"(v.y)
+               : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ double2 load_keep(const double2 *p, unsigned long long pol) {
+  double2 v;
+  asm volatile("ld.global.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;"
+               : "=d"(v.x), "=d"(v.y)
+               : "l"(p), "l"(pol));
+  return v;
+}
+
 template <typename real>
 __global__ void expand_kernel(const cplx<real> *__restrict__ in,
                               const int32_t *__restrict__ slot_user,
-                              cplx<real> *__restrict__ slots, int64_t S) {
+                              cplx<real> *__restrict__ slots, int64_t S, bool keep) {
   const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  const unsigned long long pol = l2_keep_policy();
   for (int64_t s0 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; s0 < S;
        s0 += kPermUnroll * stride) {
     int32_t m[kPermUnroll];
@@ -61,7 +84,8 @@ __global__ void expand_kernel(const cplx<real> *__restrict__ in,
     for (int r = 0; r < kPermUnroll; ++r)
       m[r] = s0 + r * stride < S ? __ldcs(slot_user + s0 + r * stride) : -1;
 #pragma unroll
-    for (int r = 0; r < kPermUnroll; ++r) v[r] = m[r] >= 0 ? in[m[r]] : cplx<real>{0, 0};
+    for (int r = 0; r < kPermUnroll; ++r)
+      v[r] = m[r] < 0 ? cplx<real>{0, 0} : keep ? load_keep(in + m[r], pol) : in[m[r]];
 #pragma unroll
     for (int r = 0; r < kPermUnroll; ++r)
       if (s0 + r * stride < S) __stcs(slots + s0 + r * stride, v[r]);
@@ -273,10 +297,11 @@ cudaError_t launch_compact(const void *slots, const int32_t *user_slot, void *ou
 }
 template <typename real>
 cudaError_t launch_expand(const void *in, const int32_t *slot_user, void *slots, int64_t S,
-                          cudaStream_t s) {
+                          cudaStream_t s, bool keep_in) {
   if (S == 0) return cudaSuccess;
   expand_kernel<real><<<stream_blocks(S, 256), 256, 0, s>>>(
-      static_cast<const cplx<real> *>(in), slot_user, static_cast<cplx<real> *>(slots), S);
+      static_cast<const cplx<real> *>(in), slot_user, static_cast<cplx<real> *>(slots), S,
+      keep_in);
   return cudaGetLastError();
 }
 
@@ -351,7 +376,7 @@ cudaError_t launch_fill(void *x, int64_t n, double value, cudaStream_t s) {
   template cudaError_t launch_compact<real>(const void *, const int32_t *, void *, int64_t,      \
                                            cudaStream_t);                                      \
   template cudaError_t launch_expand<real>(const void *, const int32_t *, void *, int64_t,       \
-                                          cudaStream_t);                                       \
+                                          cudaStream_t, bool);                                 \
   template cudaError_t launch_from_c128<real>(const void *, void *, int64_t, cudaStream_t);     \
   template cudaError_t launch_to_c128<real>(const void *, void *, int64_t, cudaStream_t);       \
   template cudaError_t launch_sq_norm<real>(const void *, int64_t, double *, double *,          \

@@ -151,12 +151,15 @@ cudaError_t launch_crop(const void *grid, const real *su, const real *sv, void *
 
 // Caller order <-> slot order.  compact: out[m] = slots[user_slot[m]], m < M.
 // expand: slots[s] = in[slot_user[s]] (0 where slot_user[s] < 0), s < S.
+// With keep_in, expand reads `in` at L2 evict-last priority, so the
+// caller-ordered vector stays in L2 afterwards (for a vector that fits in it:
+// the next degrid's scattered stores into it then hit L2).
 template <typename real>
 cudaError_t launch_compact(const void *slots, const int32_t *user_slot, void *out, int64_t M,
                            cudaStream_t s);
 template <typename real>
 cudaError_t launch_expand(const void *in, const int32_t *slot_user, void *slots, int64_t S,
-                          cudaStream_t s);
+                          cudaStream_t s, bool keep_in = false);
 
 // complex<double> <-> complex<real> conversion of n values.
 template <typename real>

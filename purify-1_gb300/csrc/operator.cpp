@@ -33,6 +33,12 @@ void cuda_check(cudaError_t e, const char *what) {
 
 namespace {
 
+// Largest caller-ordered visibility vector the adjoint's gather keeps in L2
+// at evict-last priority: three quarters of the GB300's 126 MB L2, so the
+// other streams of a step keep some room (the 10^7-visibility FP32 vector is
+// 80 MB).
+constexpr int64_t kKeepVisL2Bytes = int64_t(96) << 20;
+
 template <typename real>
 class OperatorT final : public Operator {
  public:
@@ -108,6 +114,10 @@ class OperatorT final : public Operator {
               std::vector<int32_t> &tile_tasks);
   bool unit_weights_ = true;
   bool fused_forward_ = true, fused_adjoint_ = false;
+  // The adjoint's gather keeps the caller-ordered visibilities in L2
+  // (evict-last) when they fit in kKeepVisL2Bytes: in a forward / adjoint
+  // loop the next degrid's scattered stores into them then hit L2.
+  bool keep_vis_l2_ = false;
   double norm_ = 1.0;
   std::vector<double> su_, sv_;  // 1 / ft kernel at the image pixels (unscaled)
   std::vector<real> su_scaled_, sv_real_;
@@ -196,6 +206,7 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
   // separate gather into slot order.  The w-projection kernels always use
   // the slot-ordered buffer.
   fused_forward_ = !wmode_ && cfg.fused_permute != 0;
+  keep_vis_l2_ = int64_t(sizeof(C)) * M_ <= kKeepVisL2Bytes;
   fused_adjoint_ = !wmode_ && cfg.fused_permute == 1;
 
   cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
@@ -647,7 +658,8 @@ void OperatorT<real>::grid_on_stream(const void *y, void *grid) {
     return;
   }
   mark_begin(kExpand);
-  cuda_check(launch_expand<real>(y, slot_user_.as<int32_t>(), ws_->slots, S_, ws_->stream),
+  cuda_check(launch_expand<real>(y, slot_user_.as<int32_t>(), ws_->slots, S_, ws_->stream,
+                                 keep_vis_l2_),
              "expand");
   mark_end(kExpand);
   grid_slots(grid);
@@ -731,7 +743,8 @@ void OperatorT<real>::adjoint_on_stream(const void *y, void *x) {
     return;
   }
   mark_begin(kExpand);
-  cuda_check(launch_expand<real>(y, slot_user_.as<int32_t>(), ws_->slots, S_, ws_->stream),
+  cuda_check(launch_expand<real>(y, slot_user_.as<int32_t>(), ws_->slots, S_, ws_->stream,
+                                 keep_vis_l2_),
              "expand");
   mark_end(kExpand);
   adjoint_slots(x);
