@@ -116,7 +116,9 @@ class OperatorT final : public Operator {
   bool fused_forward_ = true, fused_adjoint_ = false;
   // The adjoint's gather keeps the caller-ordered visibilities in L2
   // (evict-last) when they fit in kKeepVisL2Bytes: in a forward / adjoint
-  // loop the next degrid's scattered stores into them then hit L2.
+  // loop the next degrid's scattered stores into them then hit L2.  Only on
+  // the operator's own scratch: applies on other workspaces run concurrently
+  // (the server), and several kept vectors would crowd each other out.
   bool keep_vis_l2_ = false;
   double norm_ = 1.0;
   std::vector<double> su_, sv_;  // 1 / ft kernel at the image pixels (unscaled)
@@ -659,7 +661,7 @@ void OperatorT<real>::grid_on_stream(const void *y, void *grid) {
   }
   mark_begin(kExpand);
   cuda_check(launch_expand<real>(y, slot_user_.as<int32_t>(), ws_->slots, S_, ws_->stream,
-                                 keep_vis_l2_),
+                                 keep_vis_l2_ && ws_ == &own_),
              "expand");
   mark_end(kExpand);
   grid_slots(grid);
@@ -744,7 +746,7 @@ void OperatorT<real>::adjoint_on_stream(const void *y, void *x) {
   }
   mark_begin(kExpand);
   cuda_check(launch_expand<real>(y, slot_user_.as<int32_t>(), ws_->slots, S_, ws_->stream,
-                                 keep_vis_l2_),
+                                 keep_vis_l2_ && ws_ == &own_),
              "expand");
   mark_end(kExpand);
   adjoint_slots(x);
