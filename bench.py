@@ -347,7 +347,10 @@ def run_gb300(args):
         "data": "synthetic: seeded (PCG64) coverage and point-source + Gaussian-blob sky",
         "config": {"workload": WORKLOAD, "global_visibilities": world * M,
                    "l2": "inputs larger than L2 (about 300 MB of coverage state and "
-                         "visibilities read per step vs 129 MB L2)",
+                         "visibilities read per step vs 129 MB L2); the 80 MB caller-ordered "
+                         "visibility vector, Phi's output and Phi^H's input, is read by the "
+                         "adjoint's gather at L2 evict-last priority and so stays in L2 for "
+                         "the next step's degrid, as in a solver's Phi / Phi^H loop",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "latency_ms": {"p50": float(np.percentile(per_step, 50)),
                        "p99": float(np.percentile(per_step, 99))},
