@@ -291,11 +291,13 @@ def run_gb300(args):
         dist.barrier()
     total_ms = evs[0].elapsed_time(evs[-1])
     per_step = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
-    # forward and adjoint alone, each over the same number of steps (after
-    # the timed steps, so the headline number is unaffected)
+    # forward and adjoint alone, and the normal operator Phi^H Phi (slot
+    # order between its halves, no permutations), each over the same number
+    # of steps (after the timed steps, so the headline number is unaffected)
     directions = {}
     for name, fn in (("forward", lambda: op.forward_into(xd, yd, stream)),
-                     ("adjoint", lambda: op.adjoint_into(yd, xo, stream))):
+                     ("adjoint", lambda: op.adjoint_into(yd, xo, stream)),
+                     ("normal", lambda: op.normal_into(xd, xo, stream))):
         fn()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize(dev)
