@@ -161,8 +161,11 @@ int purify_gb300_grid(purify_gb300_operator *op, const void *vis, void *grid, vo
  * of the library and stays resident on every GPU that loads it.  An operator
  * whose scratch would not fit is refused with PURIFY_GB300_INVALID_ARGUMENT
  * (purify_gb300_grid_no_alloc_bytes tells the need).  The first call on a
- * device looks up the array's address; make that first call before any
- * stream capture.  Every call shares the array and leaves its contents
+ * device looks up the array's address and keeps it for the life of the
+ * process; make that first call before any stream capture.  The kept
+ * address dies with the device's context, so cudaDeviceReset after the
+ * first call is not supported (it also frees every operator's device
+ * state).  Every call shares the array and leaves its contents
  * behind, so calls that overlap on the GPU (any operator, any stream) race:
  * order them.  Everything the kernels read from the array is written first
  * in the same call.  No counterpart in the reference. */

@@ -32,7 +32,11 @@ size_t static_scratch_bytes() { return kBytes; }
 
 // In host code `g_static_scratch` only names the symbol; the device address
 // comes from cudaGetSymbolAddress, asked once per device with that device
-// current.  The first call on a device does this set-up.
+// current.  The first call on a device does this set-up and the address is
+// kept for the life of the process.  It belongs to the device's primary
+// context: after cudaDeviceReset the module may load at another address, so
+// a reset after the first call is not supported (the reset also frees every
+// operator's device state, which makes the operators unusable anyway).
 cudaError_t static_scratch_address(void **out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);

@@ -6,7 +6,10 @@ of cpp/tests/data.in.h:14-48 and the FITS layout of cpp/purify/pfitsio.cc:186-20
 and stores the same numbers, unchanged, as compressed ``.npz`` fixtures so the
 tests can run where the reference tree is not mounted.
 
-Usage:  python tests/golden/make_golden.py [REFERENCE_ROOT]
+Usage:  python tests/golden/make_golden.py REFERENCE_ROOT
+
+REFERENCE_ROOT is the root of the reference checkout (the folder holding
+``data/expected`` and ``data/images``); it has no default.
 """
 import os
 import re
@@ -113,4 +116,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python %s REFERENCE_ROOT" % os.path.basename(sys.argv[0]))
+    main(sys.argv[1])
