@@ -224,6 +224,23 @@ int purify_gb300_lambda_to_pixels(const double *u, const double *v, int64_t M, d
                                   double celly, uint32_t ftsizeu, uint32_t ftsizev,
                                   double *u_out, double *v_out);
 
+/* Units of visibility coordinates, in the order of utilities::vis_units
+ * (cpp/purify/utilities.h:14). */
+typedef enum {
+  PURIFY_GB300_UNITS_LAMBDA = 0,  /* wavelengths */
+  PURIFY_GB300_UNITS_RADIANS = 1, /* units of 2 pi across the grid */
+  PURIFY_GB300_UNITS_PIXELS = 2   /* grid pixels */
+} purify_gb300_units;
+/* The unit pipeline of the vis_params overload of init_degrid_operator_2d
+ * (operators.h:405-410): wavelengths go through set_cell_size (to radians)
+ * and then uv_scale (to pixels, utilities.cc:258-278); radians go through
+ * uv_scale alone; pixels are copied unchanged.  Cell sizes in arcsec, used
+ * for wavelengths only (0 derives them from max |u|, |v|).  An unknown unit
+ * is PURIFY_GB300_INVALID_ARGUMENT. */
+int purify_gb300_uv_to_pixels(const double *u, const double *v, int64_t M, int32_t units,
+                              double cellx, double celly, uint32_t ftsizeu, uint32_t ftsizev,
+                              double *u_out, double *v_out);
+
 /* ---- Host-side introspection (no GPU work) --------------------------------
  * The coverage plan the operator uploads.  Visibilities are sorted by uv tile
  * and base cell and grouped into work items (one base cell, up to 16

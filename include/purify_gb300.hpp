@@ -24,6 +24,7 @@
 #define PURIFY_GB300_HPP
 
 #include <array>
+#include <cmath>
 #include <complex>
 #include <cstdint>
 #include <functional>
@@ -139,14 +140,25 @@ std::shared_ptr<sopt::LinearTransform<T> const> init_degrid_operator_2d(
     const std::uint32_t Jv = 4, const bool w_term = false, const std::uint32_t Jw = 6,
     const double &cellx = 1, const double &celly = 1, const precision prec = precision::fp32,
     const int device = 0) {
+  // Size checks of details::init_gridding_matrix_2d (operators.cc:18-20,
+  // 63-71).  An empty weights vector stands for unit weights (the reference
+  // needs M of them); any other size is an error, as in the reference.  w is
+  // read only with w_term, where it must hold M values; without w_term the
+  // reference reads no w either.
   if (u.size() != v.size())
     throw std::runtime_error(
         "Size of u and v vectors are not the same for creating gridding matrix.");
+  if (w_term && w.size() != u.size())
+    throw std::runtime_error(
+        "Size of u and w vectors are not the same for creating gridding matrix.");
+  if (weights.size() != 0 && weights.size() != u.size())
+    throw std::runtime_error(
+        "Size of u and weights vectors are not the same for creating gridding matrix.");
   purify_gb300_create_args a;
   purify_gb300_default_args(&a);
   a.u = u.data();
   a.v = v.data();
-  a.w = w.size() == u.size() ? w.data() : nullptr;
+  a.w = w_term ? w.data() : nullptr;
   a.weights = weights.size() == u.size() ? reinterpret_cast<const double *>(weights.data())
                                          : nullptr;
   a.M = std::int64_t(u.size());
@@ -186,11 +198,50 @@ std::shared_ptr<sopt::LinearTransform<T> const> init_degrid_operator_2d_lambda(
   std::vector<double> up(u_lambda.size()), vp(v_lambda.size());
   check(purify_gb300_lambda_to_pixels(
       u_lambda.data(), v_lambda.data(), std::int64_t(u_lambda.size()), cell_x, cell_y,
-      std::uint32_t(oversample_ratio * imsizex), std::uint32_t(oversample_ratio * imsizey),
-      up.data(), vp.data()));
+      std::uint32_t(std::floor(oversample_ratio * imsizex)),
+      std::uint32_t(std::floor(oversample_ratio * imsizey)), up.data(), vp.data()));
   return init_degrid_operator_2d<T>(up, vp, w, weights, imsizey, imsizex, oversample_ratio,
                                     power_iters, power_tol, kern, Ju, Jv, w_term, Jw, cell_x,
                                     cell_y, prec);
+}
+
+// utilities::vis_units and the fields of utilities::vis_params that the
+// operator reads (cpp/purify/utilities.h:14-55), for callers without the
+// reference's headers.  The overload below accepts any type with these
+// fields, the reference's vis_params included (its units enum has the same
+// order).
+enum class vis_units { lambda = PURIFY_GB300_UNITS_LAMBDA, radians = PURIFY_GB300_UNITS_RADIANS,
+                       pixels = PURIFY_GB300_UNITS_PIXELS };
+template <class RealVec, class ComplexVec>
+struct vis_params {
+  RealVec u, v, w;
+  ComplexVec weights;
+  vis_units units = vis_units::lambda;
+};
+
+// The vis_params overload (operators.h:398-414): wavelengths are converted
+// by set_cell_size + uv_scale, radians by uv_scale, pixels pass unchanged
+// (utilities.cc:208-278); the cell sizes also reach the w-projection rows.
+template <class T, class VisParams>
+std::shared_ptr<sopt::LinearTransform<T> const> init_degrid_operator_2d(
+    const VisParams &uv_vis, const std::uint32_t &imsizey, const std::uint32_t &imsizex,
+    const double &cell_x, const double &cell_y, const double &oversample_ratio = 2,
+    const std::uint32_t &power_iters = 100, const double &power_tol = 1e-4,
+    const kernel kern = kernel::kb, const std::uint32_t Ju = 4, const std::uint32_t Jv = 4,
+    const bool w_term = false, const std::uint32_t Jw = 6,
+    const precision prec = precision::fp32, const int device = 0) {
+  if (uv_vis.u.size() != uv_vis.v.size())
+    throw std::runtime_error(
+        "Size of u and v vectors are not the same for creating gridding matrix.");
+  std::vector<double> up(uv_vis.u.size()), vp(uv_vis.v.size());
+  check(purify_gb300_uv_to_pixels(
+      uv_vis.u.data(), uv_vis.v.data(), std::int64_t(uv_vis.u.size()),
+      static_cast<std::int32_t>(uv_vis.units), cell_x, cell_y,
+      std::uint32_t(std::floor(oversample_ratio * imsizex)),
+      std::uint32_t(std::floor(oversample_ratio * imsizey)), up.data(), vp.data()));
+  return init_degrid_operator_2d<T>(up, vp, uv_vis.w, uv_vis.weights, imsizey, imsizex,
+                                    oversample_ratio, power_iters, power_tol, kern, Ju, Jv,
+                                    w_term, Jw, cell_x, cell_y, prec, device);
 }
 
 }  // namespace measurementoperator

@@ -378,6 +378,38 @@ int purify_gb300_lambda_to_pixels(const double *u, const double *v, int64_t M, d
   });
 }
 
+int purify_gb300_uv_to_pixels(const double *u, const double *v, int64_t M, int32_t units,
+                              double cellx, double celly, uint32_t ftsizeu, uint32_t ftsizev,
+                              double *u_out, double *v_out) {
+  if (M > 0 && (!u || !v || !u_out || !v_out)) return null_arg("coordinate buffer");
+  switch (units) {
+    case PURIFY_GB300_UNITS_LAMBDA:
+      return purify_gb300_lambda_to_pixels(u, v, M, cellx, celly, ftsizeu, ftsizev, u_out, v_out);
+    case PURIFY_GB300_UNITS_RADIANS:
+      // uv_scale alone (utilities.cc:258-278)
+      return guard([&] {
+        constexpr double pi = 3.14159265358979323846;
+        for (int64_t m = 0; m < M; ++m) {
+          u_out[m] = u[m] / (2 * pi) * ftsizeu;
+          v_out[m] = v[m] / (2 * pi) * ftsizev;
+        }
+      });
+    case PURIFY_GB300_UNITS_PIXELS:
+      return guard([&] {
+        for (int64_t m = 0; m < M; ++m) {
+          u_out[m] = u[m];
+          v_out[m] = v[m];
+        }
+      });
+    default:
+      return guard([&] {
+        throw pg::Error(pg::kInvalidArgument,
+                        "unknown visibility units " + std::to_string(units) +
+                            " (0 lambda, 1 radians, 2 pixels)");
+      });
+  }
+}
+
 int purify_gb300_plan_create(const double *u, const double *v, const double *weights, int64_t M,
                              uint32_t ftsizeu, uint32_t ftsizev, uint32_t J,
                              purify_gb300_plan **out) {

@@ -120,6 +120,7 @@ EXPORTS = [
     "purify_gb300_forward", "purify_gb300_adjoint", "purify_gb300_forward_host",
     "purify_gb300_adjoint_host", "purify_gb300_power_method", "purify_gb300_set_norm",
     "purify_gb300_get_norm", "purify_gb300_operator_info", "purify_gb300_lambda_to_pixels",
+    "purify_gb300_uv_to_pixels",
     "purify_gb300_last_error", "purify_gb300_version", "purify_gb300_plan_create",
     "purify_gb300_plan_sizes", "purify_gb300_plan_export", "purify_gb300_plan_destroy",
     "purify_gb300_kernel_taps", "purify_gb300_degrid", "purify_gb300_grid",
@@ -171,6 +172,9 @@ def load(path=None):
     L.purify_gb300_lambda_to_pixels.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_double,
                                                 ctypes.c_double, ctypes.c_uint32,
                                                 ctypes.c_uint32, vp, vp]
+    L.purify_gb300_uv_to_pixels.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_int32,
+                                            ctypes.c_double, ctypes.c_double, ctypes.c_uint32,
+                                            ctypes.c_uint32, vp, vp]
     L.purify_gb300_plan_create.argtypes = [vp, vp, vp, ctypes.c_int64, ctypes.c_uint32,
                                            ctypes.c_uint32, ctypes.c_uint32, P(vp)]
     L.purify_gb300_plan_sizes.argtypes = [vp, vp]
@@ -242,6 +246,21 @@ def lambda_to_pixels(u, v, cellx, celly, ftsizeu, ftsizev):
     uo, vo = np.empty_like(u), np.empty_like(v)
     _check(load().purify_gb300_lambda_to_pixels(_np_ptr(u), _np_ptr(v), u.size, cellx, celly,
                                                 ftsizeu, ftsizev, _np_ptr(uo), _np_ptr(vo)))
+    return uo, vo
+
+
+UNITS = {"lambda": 0, "radians": 1, "pixels": 2}
+
+
+def uv_to_pixels(u, v, units, cellx, celly, ftsizeu, ftsizev):
+    """Coordinates in `units` ("lambda", "radians" or "pixels") -> grid pixels,
+    the unit pipeline of the vis_params overload (operators.h:405-410)."""
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    uo, vo = np.empty_like(u), np.empty_like(v)
+    _check(load().purify_gb300_uv_to_pixels(_np_ptr(u), _np_ptr(v), u.size,
+                                            UNITS.get(units, units), cellx, celly, ftsizeu,
+                                            ftsizev, _np_ptr(uo), _np_ptr(vo)))
     return uo, vo
 
 

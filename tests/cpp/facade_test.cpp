@@ -3,6 +3,7 @@
 // *op * x and op->adjoint() * y.  Reads u, v, x, y from argv[1] (binary:
 // int64 M, int64 n, then u[M], v[M], x[2 n n], y[2 M] as doubles) and writes
 // norm, Phi x and Phi^H y to argv[2].
+#include <cmath>
 #include <complex>
 #include <cstdint>
 #include <cstdio>
@@ -39,6 +40,37 @@ int main(int argc, char **argv) {
     } catch (const std::runtime_error &) {
       threw = true;
     }
+    // the vis_params overload: pixels pass unchanged (bit-identical operator),
+    // radians go through uv_scale (operators.h:405-410)
+    namespace mo = purify::gb300::measurementoperator;
+    mo::vis_params<std::vector<double>, Vec> px;
+    px.u = u;
+    px.v = v;
+    px.units = mo::vis_units::pixels;
+    const auto op_px = mo::init_degrid_operator_2d<Vec>(px, uint32_t(n), uint32_t(n), 1.0, 1.0,
+                                                         2.0, 50, 1e-4, purify::gb300::kernel::kb,
+                                                         4, 4, false, 6,
+                                                         purify::gb300::precision::fp64);
+    mo::vis_params<std::vector<double>, Vec> rad = px;
+    const double two_pi = 6.283185307179586;
+    for (int64_t m = 0; m < M; ++m) {
+      rad.u[m] = u[m] * two_pi / double(2 * n);
+      rad.v[m] = v[m] * two_pi / double(2 * n);
+    }
+    rad.units = mo::vis_units::radians;
+    const auto op_rad = mo::init_degrid_operator_2d<Vec>(rad, uint32_t(n), uint32_t(n), 1.0, 1.0,
+                                                          2.0, 50, 1e-4, purify::gb300::kernel::kb,
+                                                          4, 4, false, 6,
+                                                          purify::gb300::precision::fp64);
+    const Vec fx_px = *op_px * x, fx_rad = *op_rad * x;
+    double e_px = 0, e_rad = 0, nrm = 0;
+    for (int64_t m = 0; m < M; ++m) {
+      e_px += std::norm(fx_px[m] - fx[m]);
+      e_rad += std::norm(fx_rad[m] - fx[m]);
+      nrm += std::norm(fx[m]);
+    }
+    std::printf("units pixels %.3e radians %.3e\n", std::sqrt(e_px / nrm), std::sqrt(e_rad / nrm));
+    if (e_px != 0 || !(std::sqrt(e_rad / nrm) < 1e-10)) return 4;
     std::ofstream out(argv[2], std::ios::binary);
     const double norm = 0.0;
     out.write(reinterpret_cast<const char *>(&norm), 8);
