@@ -54,7 +54,10 @@ def parse():
     p.add_argument("--imsize", type=int, default=1024)
     p.add_argument("--J", type=int, default=6)
     p.add_argument("--cpu-sample", type=int, default=1_000_000,
-                   help="visibilities in the CPU-baseline sample")
+                   help="visibilities of the extrapolated CPU sample kept beside the full-size "
+                        "CPU figure (0: none)")
+    p.add_argument("--cpu-pairs", type=int, default=10,
+                   help="timed Phi / Phi^H pairs of the full-size CPU baseline")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--e2e-steps", type=int, default=5, help="0 skips the end-to-end leg")
@@ -175,42 +178,77 @@ def rel_l2(a, b):
 
 
 # --------------------------------------------------------------- CPU oracle --
-def cpu_reference(u, v, x, imsize, J, sample, steps=2, warmup=1):
-    """Times the FP64 oracle on a bounded sample of the same coverage and
-    extrapolates the per-visibility cost to the full M."""
+def cpu_reference(u, v, x, imsize, J, pairs=10, warmup=1, sample=1_000_000):
+    """Times the FP64 oracle (the reference algorithm restated: explicit CSR G
+    and G^H, row-parallel OpenMP SpMV, unitary FFT) on the full workload:
+    construction once, then `warmup` untimed and `pairs` timed Phi / Phi^H
+    pairs; the value is M over the median pair.  A `sample`-visibility
+    subsample with a per-visibility extrapolation is kept beside it for
+    comparison with earlier figures (0 skips it)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
     threads = oracle.get_threads()
     M = u.size
-    Ms = min(sample, M)
-    idx = np.random.default_rng(123).choice(M, Ms, replace=False) if Ms < M else np.arange(M)
-    op0 = oracle.Operator(u[:0], v[:0], None, None, imsize, imsize, 2.0, kernel="kb", Ju=J, Jv=J)
-    ops = oracle.Operator(u[idx], v[idx], None, None, imsize, imsize, 2.0, kernel="kb", Ju=J,
-                          Jv=J)
-
-    def pair_time(op):
-        ts = []
-        for k in range(warmup + steps):
-            t0 = time.perf_counter()
-            y = op.forward(x)
-            op.adjoint(y)
-            if k >= warmup:
-                ts.append(time.perf_counter() - t0)
-        return statistics.median(ts)
-
-    t_fixed = pair_time(op0)
-    t_sample = pair_time(ops)
-    per_vis = max(t_sample - t_fixed, 0.0) / Ms
-    t_full = t_fixed + per_vis * M
-    return {
-        "value": M / t_full / 1e6, "unit": "Mvis/s", "cores": threads, "kind": "port",
-        "sample": ("Phi then Phi^H of the FP64 oracle (CSR G/G^H, OpenMP SpMV, radix-2 FFT) on "
-                   "%d of the %d visibilities with the full %d^2 grid; median of %d pairs; "
-                   "per-visibility cost extrapolated linearly to M=%d (fixed pad+FFT+crop part "
-                   "%.3f s timed with M=0)" % (Ms, M, 2 * imsize, steps, M, t_fixed)),
-        "t_pair_sample_s": t_sample, "t_fixed_s": t_fixed,
+    t0 = time.perf_counter()
+    op = oracle.Operator(u, v, None, None, imsize, imsize, 2.0, kernel="kb", Ju=J, Jv=J)
+    t_create = time.perf_counter() - t0
+    tf, ta, tp = [], [], []
+    for k in range(warmup + pairs):
+        t0 = time.perf_counter()
+        y = op.forward(x)
+        t1 = time.perf_counter()
+        op.adjoint(y)
+        t2 = time.perf_counter()
+        if k >= warmup:
+            tf.append(t1 - t0)
+            ta.append(t2 - t1)
+            tp.append(t2 - t0)
+    nnz = op.nnz
+    del op
+    t_pair = statistics.median(tp)
+    out = {
+        "value": M / t_pair / 1e6, "unit": "Mvis/s", "cores": threads, "kind": "port",
+        "sample": ("the full workload (M=%d, %d^2 grid, %d non-zeros in G and again in G^H): "
+                   "Phi then Phi^H of the FP64 oracle (CSR G/G^H, OpenMP SpMV, radix-2 FFT), "
+                   "median of %d timed pairs after %d untimed; construction %.1f s not timed"
+                   % (M, 2 * imsize, nnz, pairs, warmup, t_create)),
+        "ms_per_pair": t_pair * 1e3, "ms_forward": statistics.median(tf) * 1e3,
+        "ms_adjoint": statistics.median(ta) * 1e3, "create_s": t_create,
+        "host_bytes_G_and_GH": 2 * nnz * 20, "timed": True,
     }
+    if sample and sample < M:
+        idx = np.random.default_rng(123).choice(M, sample, replace=False)
+        op0 = oracle.Operator(u[:0], v[:0], None, None, imsize, imsize, 2.0, kernel="kb", Ju=J,
+                              Jv=J)
+        ops = oracle.Operator(u[idx], v[idx], None, None, imsize, imsize, 2.0, kernel="kb",
+                              Ju=J, Jv=J)
+
+        def pair_time(o):
+            ts = []
+            for k in range(3):
+                t0 = time.perf_counter()
+                o.adjoint(o.forward(x))
+                if k >= 1:
+                    ts.append(time.perf_counter() - t0)
+            return statistics.median(ts)
+        t_fixed, t_s = pair_time(op0), pair_time(ops)
+        t_ext = t_fixed + max(t_s - t_fixed, 0.0) / sample * M
+        out["sample_extrapolated"] = {
+            "value": M / t_ext / 1e6, "visibilities": sample,
+            "how": "per-visibility cost of a %d-visibility sample extrapolated to M" % sample}
+    return out
+
+
+def host_memory_gb():
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemTotal:"):
+                    return int(line.split()[1]) / 2**20
+    except Exception:
+        pass
+    return None
 
 
 def run_reference(args):
@@ -218,15 +256,16 @@ def run_reference(args):
     if rank != 0:
         return
     u, v, x = workload(args, seed=0)
-    # each step: one pair on the bounded sample (see cpu_reference)
-    cb = cpu_reference(u, v, x, args.imsize, args.J, args.cpu_sample, steps=max(1, args.steps),
-                       warmup=max(1, args.warmup))
+    # each step: one Phi / Phi^H pair of the full workload
+    cb = cpu_reference(u, v, x, args.imsize, args.J, pairs=max(1, args.steps),
+                       warmup=max(1, args.warmup), sample=0)
     line = {
         "metric": METRIC, "value": cb["value"], "unit": "Mvis/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": args.M / cb["value"] / 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": cb["ms_per_pair"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: seeded (PCG64) coverage and point-source + Gaussian-blob sky",
-        "config": {"workload": WORKLOAD, "parallelism": "host threads"},
+        "config": {"workload": WORKLOAD, "global_visibilities": args.M,
+                   "parallelism": "host threads", "host_memory_gb": host_memory_gb()},
         "impl": "reference", "cpu_baseline": cb,
         "e2e": {"value": cb["value"], "unit": "Mvis/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
@@ -235,6 +274,48 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------- GPU ----
+def kernel_bytes(info, s, caller_order_out=True, unit_weights=True):
+    """Bytes each gridding-chain kernel's own arguments carry per launch
+    (complex values of s bytes): what the kernel must read or write at least
+    once, independent of how it does it.
+
+    degrid: the grid once, per slot t (s) [+ weight (s)] [+ caller index (4)
+            when it writes caller order], lane codes and batch headers, and
+            the M visibilities it writes;
+    grid:   per slot t and the slot-ordered visibility (2 s) [+ weight],
+            lane codes and headers, and the task windows it writes;
+    expand: per slot the caller index (4) and the slot written (s), and the M
+            caller-ordered visibilities read;
+    fold:   the task windows read and the grid written."""
+    S, M = info["slots"], info["M"]
+    NuNv = info["ftsizeu"] * info["ftsizev"]
+    items = info["work_items"]
+    lanes = 4 * items + 8 * (items // 32)
+    windows = s * info["tasks"] * info["window_cells"]
+    wt = 0 if unit_weights else s * S
+    return {
+        "degrid": s * NuNv + s * S + wt + (4 * S if caller_order_out else 0) + lanes + s * M,
+        "grid": 2 * s * S + wt + lanes + windows,
+        "expand": 4 * S + s * S + s * M,
+        "fold": windows + s * NuNv,
+    }
+
+
+def roofline_entry(kern, alg, dur_s, peak, peak_kind, traffic, survey_bytes=None):
+    """achieved / frac on the kernel's own bytes, frac_dram on its profiled
+    DRAM traffic, and (when given) the survey formula's bytes beside them."""
+    achieved = alg / dur_s / 1e9
+    r = {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
+         "frac": achieved / peak, "peak_source": peak_kind, "algorithmic_bytes": alg,
+         "duration_ms": dur_s * 1e3, "traffic": traffic,
+         "frac_dram": (traffic / dur_s / 1e9 / peak) if traffic else None}
+    if survey_bytes:
+        r["survey_bytes"] = survey_bytes
+        r["frac_survey_bytes"] = survey_bytes / dur_s / 1e9 / peak
+    return r
+
+
+
 def run_gb300(args):
     import torch
     import purify_gb300 as pgb
@@ -366,21 +447,21 @@ def run_gb300(args):
         "clocks": clocks,
     }
 
-    # roofline of the dominant kernel (degrid or grid), algorithmic bytes:
-    # per visibility u,v (2 x 8 B) + weight + visibility (2 x 8 B); the grid once (8 B/cell)
+    # roofline of the dominant kernel (degrid or grid): the bytes its own
+    # arguments carry (kernel_bytes), the survey's per-visibility formula
+    # beside it, and the profiled DRAM traffic per launch
     s = 8
-    alg = {"degrid": M * (16 + 2 * s) + s * info["ftsizeu"] * info["ftsizev"],
-           "grid": M * (16 + 2 * s) + s * info["ftsizeu"] * info["ftsizev"]}
+    kb = kernel_bytes(info, s, caller_order_out=True)
     kern = max(("degrid", "grid"), key=lambda k: stages[k][0] / max(stages[k][1], 1))
     dur = stages[kern][0] / max(stages[kern][1], 1) * 1e-3
     peak, peak_kind = measured_peak()
-    achieved = alg[kern] / dur / 1e9
-    traffic = profiled_traffic().get(kern)
-    out["roofline"] = {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak,
-                       "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                       "algorithmic_bytes": alg[kern],
-                       "traffic": (traffic * M / 1e7) if traffic else None}
-    # whole-step HBM view: B_fwd + B_adj (algorithmic, c64)
+    # the profiled traffic belongs to the headline workload only
+    headline = (M == 10_000_000 and n == 1024 and args.J == 6 and not tuning_of(args))
+    traffic = profiled_traffic().get(kern) if headline else None
+    out["roofline"] = roofline_entry(kern, kb[kern], dur, peak, peak_kind, traffic,
+                                     M * (16 + 2 * s) + s * info["ftsizeu"] * info["ftsizev"])
+    out["kernel_bytes"] = kb
+    # whole-step HBM view: B_fwd + B_adj of the survey's formula (c64)
     NuNv = info["ftsizeu"] * info["ftsizev"]
     b_step = 2 * M * (16 + 2 * s) + s * (7 * NuNv + 3 * N)
     out["step_roofline"] = {"algorithmic_bytes": b_step,
@@ -472,7 +553,9 @@ def run_gb300(args):
                          "(complex<double> host vectors)"}
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_reference(u, v, x, n, args.J, args.cpu_sample)
+        out["cpu_baseline"] = cpu_reference(u, v, x, n, args.J, pairs=args.cpu_pairs,
+                                            sample=args.cpu_sample)
+        out["cpu_baseline"]["host_memory_gb"] = host_memory_gb()
     out["info"] = {k: info[k] for k in ("occupied_cells", "work_items", "tasks", "device_bytes",
                                         "kernel_fit_error")}
     if rank == 0:
@@ -518,12 +601,19 @@ def run_wproj(args):
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize(dev)
+    sampler = ClockSampler(0)
+    time.sleep(0.5)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    w0 = time.time()
     e0.record(stream)
     for _ in range(args.steps):
         step()
     e1.record(stream)
     torch.cuda.synchronize(dev)
+    w1 = time.time()
+    time.sleep(0.3)
+    sampler.stop()
+    clocks = sampler.summary(sampler.window(w0 - 0.25, w1 + 0.25)) or sampler.summary(sampler.rows)
     ms = e0.elapsed_time(e1) / args.steps
     op.stage_timing(True)
     for _ in range(max(2, min(args.steps, 5))):
@@ -533,9 +623,16 @@ def run_wproj(args):
     taps = info["nnz"]
     NuNv = info["ftsizeu"] * info["ftsizev"]
     s8 = 8
-    # algorithmic bytes per direction with stored FP32 rows (taps * s) as the
-    # w-projection estimate counts them, plus M(16 + 2s) and the grid once
-    alg = M * (16 + 2 * s8) + taps * s8 + s8 * NuNv
+    # Bytes the row-factor kernels' own arguments carry per launch: the
+    # stored factors (info factor_values complex values, 2 rank S per row,
+    # not the S^2 taps of explicit rows), per row its code (4), factor offset
+    # (8) and weight (s), the M slot-ordered visibilities, and the grid once
+    # (degrid) or the task windows (grid).  The survey's estimate with
+    # explicit FP32 rows (taps * s) is kept beside it.
+    rows = info["factor_values"] * s8 + M * (4 + 8 + s8) + M * s8
+    wbytes = {"degrid": rows + s8 * NuNv,
+              "grid": rows + s8 * info["tasks"] * info["window_cells"]}
+    survey = M * (16 + 2 * s8) + taps * s8 + s8 * NuNv
     kern = max(("degrid", "grid"), key=lambda k: stages[k][0] / max(stages[k][1], 1))
     dur = stages[kern][0] / max(stages[kern][1], 1) * 1e-3
     peak, peak_kind = measured_peak()
@@ -548,10 +645,12 @@ def run_wproj(args):
         "gtaps_per_s": 2 * taps / (ms * 1e-3) / 1e9,
         "stages_ms_per_launch": {k: (ms_ / nl if nl else None) for k, (ms_, nl) in stages.items()},
         "create_s": t_create, "generate_s": t_gen, "norm": norm,
-        "device_bytes": info["device_bytes"],
-        "roofline": {"bound": "hbm", "kernel": kern, "algorithmic_bytes": alg,
-                     "achieved": alg / dur / 1e9, "peak": peak, "unit": "GB/s",
-                     "frac": alg / dur / 1e9 / peak, "peak_source": peak_kind},
+        "device_bytes": info["device_bytes"], "factor_values": info["factor_values"],
+        "clocks": clocks, "kernel_bytes": wbytes,
+        "roofline": roofline_entry(kern, wbytes[kern], dur, peak, peak_kind, None, survey),
+        # own kernels per step: the forward row pass, w degrid, w grid, fold,
+        # the inverse row pass
+        "gpu_launches": 5 * args.steps,
     }
     # FP32 rows against the FP64 oracle on a row sample (rows are independent)
     try:
@@ -867,9 +966,17 @@ def run_serve(args):
     vs = [synthetic.random_vis(c["u"].size, seed=100 + k) for k, c in enumerate(covs)]
     out = None
     per_prec = {}
+    clocks = {}
     for prec in (["fp32"] if args.no_fp64 else ["fp32", "fp64"]):
+        sampler = ClockSampler(0)
+        w0 = time.time()
         res, st, base, wall, t_setup = serve_stream(pgb, covs, prec, args, t_arr, kinds, cov_idx,
                                                     xs, vs)
+        w1 = time.time()
+        sampler.stop()
+        # the timed stream is the last `wall` seconds of the call
+        clocks[prec] = (sampler.summary(sampler.window(w1 - wall - 0.25, w1 + 0.25)) or
+                        sampler.summary(sampler.rows))
         lat = np.array([r["latency_ms"] for r in res])
         ok = sum(1 for r in res if r["status"] == 0)
         passes = st["visibility_passes"] - base["visibility_passes"]
@@ -897,6 +1004,7 @@ def run_serve(args):
         "config": {"workload": SERVE_WORKLOAD, "rate_per_s": args.rate, "requests": args.requests,
                    "slots": args.slots, "hbm_budget_gb": args.budget_gb,
                    "latency": "submit to end of the request's device work (D2H included)"},
+        "clocks": clocks.get("fp32"), "clocks_fp64": clocks.get("fp64"),
         "latency_ms": f32["latency_ms"], "serving": {k: {kk: vv for kk, vv in v.items()
                                                           if kk != "_res"}
                                                       for k, v in per_prec.items()},

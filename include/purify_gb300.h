@@ -214,6 +214,9 @@ typedef struct {
   int64_t device_bytes;    /* device memory held by the operator */
   double kernel_fit_error; /* max |poly - kernel| of the tap weights (abs) */
   double norm;
+  int64_t slots;           /* per-slot coverage entries (M plus null slots; M with w_term) */
+  int64_t window_cells;    /* grid cells of one task's accumulation window */
+  int64_t factor_values;   /* w_term: complex row-factor values stored (0 otherwise) */
 } purify_gb300_info;
 int purify_gb300_operator_info(const purify_gb300_operator *op, purify_gb300_info *info);
 

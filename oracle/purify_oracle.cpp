@@ -300,22 +300,53 @@ struct CSR {
     }
   }
   // Conjugate transpose, the explicit copy that operators.h:135-136 keeps.
+  // Every adjoint row lists its source rows in ascending order, as a serial
+  // counting transpose would: the rows are cut into one contiguous block per
+  // thread, each block's entries go to a column segment after those of the
+  // blocks before it.
   CSR adjoint() const {
     CSR a;
     a.rows = cols;
     a.cols = rows;
     a.offsets.assign(cols + 1, 0);
-    for (t_int e = 0; e < offsets[rows]; ++e) a.offsets[index[e] + 1]++;
-    for (t_int c = 0; c < cols; ++c) a.offsets[c + 1] += a.offsets[c];
-    a.index.resize(offsets[rows]);
-    a.value.resize(offsets[rows]);
-    std::vector<t_int> fill(a.offsets.begin(), a.offsets.end() - 1);
-    for (t_int r = 0; r < rows; ++r)  // ascending r keeps every adjoint row sorted
-      for (t_int e = offsets[r]; e < offsets[r + 1]; ++e) {
-        const t_int d = fill[index[e]]++;
-        a.index[d] = static_cast<std::int32_t>(r);
-        a.value[d] = std::conj(value[e]);
+    const t_int nnz = offsets[rows];
+    a.index.resize(nnz);
+    a.value.resize(nnz);
+#ifdef _OPENMP
+    const int T = omp_get_max_threads();
+#else
+    const int T = 1;
+#endif
+    // at[t * cols + c]: entries of block t in column c, then their first slot
+    std::vector<t_int> at(size_t(T) * cols, 0);
+    auto block = [&](int t) { return std::make_pair(rows * t / T, rows * (t + 1) / T); };
+#pragma omp parallel for schedule(static, 1)
+    for (int t = 0; t < T; ++t) {
+      t_int *cnt = at.data() + size_t(t) * cols;
+      const auto br = block(t);
+      for (t_int e = offsets[br.first]; e < offsets[br.second]; ++e) cnt[index[e]]++;
+    }
+    t_int pos = 0;
+    for (t_int c = 0; c < cols; ++c) {
+      a.offsets[c] = pos;
+      for (int t = 0; t < T; ++t) {
+        const t_int n = at[size_t(t) * cols + c];
+        at[size_t(t) * cols + c] = pos;
+        pos += n;
       }
+    }
+    a.offsets[cols] = pos;
+#pragma omp parallel for schedule(static, 1)
+    for (int t = 0; t < T; ++t) {
+      t_int *fill = at.data() + size_t(t) * cols;
+      const auto br = block(t);
+      for (t_int r = br.first; r < br.second; ++r)
+        for (t_int e = offsets[r]; e < offsets[r + 1]; ++e) {
+          const t_int d = fill[index[e]]++;
+          a.index[d] = static_cast<std::int32_t>(r);
+          a.value[d] = std::conj(value[e]);
+        }
+    }
     return a;
   }
 };
@@ -436,16 +467,20 @@ CSR init_gridding_matrix_2d(const GriddingArgs &a, const std::function<t_real(t_
     for (t_int m = 0; m < a.M; ++m) {
       std::vector<std::pair<std::int32_t, t_complex>> row;
       row.reserve(per);
+      const t_real k_u = std::floor(a.u[m] - ju_max * 0.5);
+      const t_real k_v = std::floor(a.v[m] - jv_max * 0.5);
+      // The reference evaluates kernelu / kernelv inside the (ju, jv) loop;
+      // their J + J distinct values are computed once here (same values).
+      std::vector<t_real> ku(ju_max + 1), kv(jv_max + 1);
+      for (t_int ju = 1; ju < ju_max + 1; ++ju) ku[ju] = kernelu(a.u[m] - (k_u + ju));
+      for (t_int jv = 1; jv < jv_max + 1; ++jv) kv[jv] = kernelv(a.v[m] - (k_v + jv));
       for (t_int ju = 1; ju < ju_max + 1; ++ju)
         for (t_int jv = 1; jv < jv_max + 1; ++jv) {
-          const t_real k_u = std::floor(a.u[m] - ju_max * 0.5);
-          const t_real k_v = std::floor(a.v[m] - jv_max * 0.5);
           const t_int q = static_cast<t_int>(mod(k_u + ju, ftsizeu));
           const t_int p = static_cast<t_int>(mod(k_v + jv, ftsizev));
           const t_int index = p * ftsizeu + q;  // utilities::sub2ind (utilities.cc:321-333)
           const t_complex val = std::exp(-2 * pi * I * ((k_u + ju) * 0.5 + (k_v + jv) * 0.5)) *
-                                kernelu(a.u[m] - (k_u + ju)) * kernelv(a.v[m] - (k_v + jv)) *
-                                a.weights[m];
+                                ku[ju] * kv[jv] * a.weights[m];
           row.emplace_back(static_cast<std::int32_t>(index), val);
         }
       std::sort(row.begin(), row.end(),

@@ -347,6 +347,9 @@ int purify_gb300_operator_info(const purify_gb300_operator *op, purify_gb300_inf
     info->device_bytes = i.device_bytes;
     info->kernel_fit_error = i.kernel_fit_error;
     info->norm = i.norm;
+    info->slots = i.slots;
+    info->window_cells = i.window_cells;
+    info->factor_values = i.factor_values;
   });
 }
 

@@ -107,7 +107,7 @@ class OperatorT final : public Operator {
   int fold_J_ = 0;      // halo of the task windows + 1 (J, or the largest w support)
   DeviceBuffer wcode_, wfactor_, wfactors_, wchunks_, wtask_chunk_;
   int wchunk_values_ = 0;
-  int64_t nnz_ = 0, occupied_ = 0, work_items_ = 0;
+  int64_t nnz_ = 0, occupied_ = 0, work_items_ = 0, factor_values_ = 0;
   void init_plain(const OperatorConfig &cfg, int64_t &bytes, AxisTiling &tu, AxisTiling &tv,
                   std::vector<int32_t> &tile_tasks);
   void init_w(const OperatorConfig &cfg, int64_t &bytes, AxisTiling &tu, AxisTiling &tv,
@@ -310,6 +310,9 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
   info_.nnz = nnz_;
   info_.occupied_cells = occupied_;
   info_.work_items = work_items_;
+  info_.slots = S_;
+  info_.window_cells = slot_stride_;
+  info_.factor_values = factor_values_;
 
   set_norm(1.0);
   if (cfg.power_iters > 0) power_method(cfg.power_iters, cfg.power_tol);
@@ -451,6 +454,7 @@ void OperatorT<real>::init_w(const OperatorConfig &cfg, int64_t &bytes, AxisTili
   wtask_chunk_.alloc(sizeof(int32_t) * plan.task_chunk.size(), &bytes);
   wtask_chunk_.upload(plan.task_chunk.data(), sizeof(int32_t) * plan.task_chunk.size(), stream_);
   wchunk_values_ = plan.chunk_values;
+  factor_values_ = plan.factor_count;
   cuda_check(cudaStreamSynchronize(stream_), "upload");
   // Row factors, FP64-generated, uploaded in chunks of rows.  Two values of
   // tail: the G^H staging copies read whole 16-byte pieces.

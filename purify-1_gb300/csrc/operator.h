@@ -61,6 +61,7 @@ struct OperatorInfo {
   int64_t nnz = 0, occupied_cells = 0, work_items = 0, tasks = 0, device_bytes = 0;
   double kernel_fit_error = 0, norm = 1;
   int device = 0;
+  int64_t slots = 0, window_cells = 0, factor_values = 0;
 };
 
 // Scratch of one apply held outside the operator, so that several applies of

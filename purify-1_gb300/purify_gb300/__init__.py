@@ -64,7 +64,8 @@ class Info(ctypes.Structure):
         ("w_term", ctypes.c_int32), ("nnz", ctypes.c_int64), ("occupied_cells", ctypes.c_int64),
         ("work_items", ctypes.c_int64), ("tasks", ctypes.c_int64),
         ("device_bytes", ctypes.c_int64), ("kernel_fit_error", ctypes.c_double),
-        ("norm", ctypes.c_double),
+        ("norm", ctypes.c_double), ("slots", ctypes.c_int64), ("window_cells", ctypes.c_int64),
+        ("factor_values", ctypes.c_int64),
     ]
 
 
