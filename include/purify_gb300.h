@@ -105,6 +105,11 @@ typedef struct {
   int32_t fused_permute; /* 1: degrid/grid touch caller-ordered visibilities directly,
                             0: via a slot-ordered buffer and gather kernels, -1: default
                             (direct for Phi, gather for Phi^H) */
+  int32_t cell_group;    /* base cells per work item along each axis: 1, 2 (complex<float>
+                            with J <= 6: 2 x 2 cells share a (J + 1)^2 register block),
+                            or 0: 2 where allowed, else 1 */
+  int32_t class_cap;     /* most items of one shared-memory bank class in a batch of 32
+                            (1 .. 16), or 0 for the default */
 } purify_gb300_tuning;
 int purify_gb300_operator_create_tuned(const purify_gb300_create_args *args,
                                        const purify_gb300_tuning *tuning,
@@ -217,6 +222,7 @@ typedef struct {
   int64_t slots;           /* per-slot coverage entries (M plus null slots; M with w_term) */
   int64_t window_cells;    /* grid cells of one task's accumulation window */
   int64_t factor_values;   /* w_term: complex row-factor values stored (0 otherwise) */
+  int64_t cell_group;      /* base cells per work item along each axis (1 or 2) */
 } purify_gb300_info;
 int purify_gb300_operator_info(const purify_gb300_operator *op, purify_gb300_info *info);
 
@@ -256,8 +262,15 @@ typedef struct purify_gb300_plan purify_gb300_plan;
 int purify_gb300_plan_create(const double *u, const double *v, const double *weights, int64_t M,
                              uint32_t ftsizeu, uint32_t ftsizev, uint32_t J,
                              purify_gb300_plan **out);
-/* sizes[0..8] = M, slots, batches, tasks, tiles along u, tiles along v,
- * window rows, window columns, unit-weight flag. */
+/* The same plan with work items of group x group base cells (group 1 or 2;
+ * with 2 an item is an aligned 2 x 2 cell group of its tile, lp and lq are
+ * its anchor and each fraction carries the visibility's cell in the group
+ * as its integer part: frac = t + d, d in {0, 1}). */
+int purify_gb300_plan_create_grouped(const double *u, const double *v, const double *weights,
+                                     int64_t M, uint32_t ftsizeu, uint32_t ftsizev, uint32_t J,
+                                     int32_t group, purify_gb300_plan **out);
+/* sizes[0..10] = M, slots, batches, tasks, tiles along u, tiles along v,
+ * window rows, window columns, unit-weight flag, group, window row stride. */
 int purify_gb300_plan_sizes(const purify_gb300_plan *plan, int64_t *sizes);
 /* Per slot: frac (2 doubles t_u, t_v), weight (2 doubles, the weight times the
  * phase sign (-1)^(k_u + k_v); 0 for null slots), slot_user (caller index or
@@ -311,6 +324,7 @@ typedef struct {
   int32_t max_per_item;    /* visibilities of one base cell given to one lane */
   int32_t degrid_threads;  /* CTA threads of the grouped degrid launch */
   int32_t grid_threads;    /* CTA threads of the grouped grid launch */
+  int32_t cell_group;      /* base cells per work item along each axis (1, or 2 for FP32, J <= 6) */
 } purify_gb300_batch_tuning;
 /* Builds the batch (plans every channel, uploads the coverage state).  With
  * tuning == NULL the autotuner picks the tile edge and CTA sizes by timing

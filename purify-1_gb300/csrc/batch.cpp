@@ -1,4 +1,5 @@
 #include "batch.h"
+#include "operator.h"
 
 #include <cufft.h>
 
@@ -102,6 +103,7 @@ class BatchT final : public Batch {
   }
 
   int device_ = 0, J_ = 0, nch_ = 0;
+  int cfg_group_ = 1;  // cells per work item along each axis (every channel's plan)
   PolyTable<real> poly_{};
   LaunchShape degrid_shape_, grid_shape_;
   std::unique_ptr<Chan[]> chans_;
@@ -133,6 +135,7 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
   DeviceGuard guard(device_);
   nch_ = int(cfg.channels.size());
   J_ = cfg.J;
+  cfg_group_ = cfg.cell_group;
   degrid_shape_.threads = cfg.degrid_threads > 0 ? cfg.degrid_threads : cfg.threads;
   grid_shape_.threads = cfg.grid_threads > 0 ? cfg.grid_threads : cfg.threads;
 
@@ -187,6 +190,7 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     rq.Ju = rq.Jv = J_;
     rq.tile = cfg.tile;
     rq.max_per_item = cfg.max_per_item;
+    rq.group = cfg.cell_group;
     Plan plan;
     try {
       plan = build_plan(rq);
@@ -233,8 +237,8 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     std::vector<C> fr(ch.S);
     for (int64_t i = 0; i < ch.S; ++i) {
       // unit weights: the phase sign (-1)^(k_u + k_v) rides in the sign of t_u
-      const double t = (ch.unit && plan.flip[i]) ? -plan.frac_u[i] : plan.frac_u[i];
-      fr[i] = C(real(t), real(plan.frac_v[i]));
+      const real tu = fraction_in_cell<real>(plan.frac_u[i]);
+      fr[i] = C((ch.unit && plan.flip[i]) ? -tu : tu, fraction_in_cell<real>(plan.frac_v[i]));
     }
     auto put = [&](size_t off, const void *src, size_t bytes) {
       if (bytes)
@@ -366,6 +370,7 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     a.Nu = ch.Nu;
     a.Nv = ch.Nv;
     a.win_stride = ch.win_stride;
+    a.group_cells = cfg_group_;
     a.slot_stride = ch.slot_stride;
     // forward: degrid straight into the caller-ordered visibilities
     fwd_[c] = a;
@@ -385,7 +390,7 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     f.tv_of = m.at<int32_t>(ch.o_tv_of);
     f.ntu = ch.ntu;
     f.ntv = ch.ntv;
-    f.Ju = f.Jv = J_;
+    f.Ju = f.Jv = J_ + cfg_group_ - 1;  // windows reach JB - 1 cells into the next tiles
     f.Nu = ch.Nu;
     f.Nv = ch.Nv;
     f.grid = work_of(c);
@@ -487,6 +492,7 @@ template <typename real>
 void BatchT<real>::record(int mode) {
   const ChannelIO<real> *io = shared_.at<ChannelIO<real>>(o_io_);
   ApplyArgs<real> head;
+  head.group_cells = cfg_group_;
   head.tasks = shared_.at<Task>(o_tasks_);
   head.order = shared_.at<int32_t>(o_order_);
   head.group_task_base = shared_.at<int32_t>(o_task_base_);
@@ -800,6 +806,10 @@ std::unique_ptr<Batch> Batch::create(const BatchConfig &cfg) {
   if (cfg.tile < 8 || cfg.tile > 128) throw Error(kInvalidArgument, "tile must be in [8, 128]");
   if (cfg.max_per_item < 1 || cfg.max_per_item > 64)
     throw Error(kInvalidArgument, "max_per_item must be in [1, 64]");
+  if (cfg.cell_group != 1 && cfg.cell_group != 2)
+    throw Error(kInvalidArgument, "cell_group must be 1 or 2");
+  if (cfg.cell_group == 2 && (cfg.fp64 || cfg.J > kMaxGroupJ))
+    throw Error(kUnsupported, "2 x 2 work items need complex<float> and J <= 6");
   for (size_t c = 0; c < cfg.channels.size(); ++c) {
     const ChannelSpec &s = cfg.channels[c];
     if (s.imsizex <= 0 || s.imsizey <= 0)
@@ -850,8 +860,11 @@ BatchTuning autotune_batch(const BatchConfig &cfg) {
   const int prec = cfg.fp64 ? 8 : 4;
   BatchTuning best;
   double best_ms = -1;
+  const int max_group = (!cfg.fp64 && cfg.J <= kMaxGroupJ) ? 2 : 1;
+  for (int group = 1; group <= max_group; ++group)
   for (int tile : {24, 32, 48}) {
     sub.tile = tile;
+    sub.cell_group = group;
     sub.threads = 128;
     sub.degrid_threads = sub.grid_threads = 0;
     std::unique_ptr<Batch> b = Batch::create(sub);
@@ -861,10 +874,10 @@ BatchTuning autotune_batch(const BatchConfig &cfg) {
     for (int threads : {64, 128, 256}) {
       LaunchShape shape;
       shape.threads = threads;
-      const bool degrid_fits =
-          degrid_smem_bytes(prec, cfg.J, bi.win_rows, bi.win_cols, shape) <= size_t(optin);
-      const bool grid_fits =
-          grid_smem_bytes(prec, cfg.J, bi.win_rows, bi.win_cols, shape) <= size_t(optin);
+      const bool degrid_fits = degrid_smem_bytes(prec, cfg.J, bi.win_rows, bi.win_cols, shape,
+                                                 true, true, group) <= size_t(optin);
+      const bool grid_fits = grid_smem_bytes(prec, cfg.J, bi.win_rows, bi.win_cols, shape,
+                                             false, true, group) <= size_t(optin);
       if (!degrid_fits || !grid_fits) continue;
       b->set_launch_shapes(threads, threads);
       const double f = b->time_apply(1, 5), a = b->time_apply(2, 5);
@@ -881,6 +894,7 @@ BatchTuning autotune_batch(const BatchConfig &cfg) {
     if (best_ms < 0 || fwd_best + adj_best < best_ms) {
       best_ms = fwd_best + adj_best;
       best.tile = tile;
+      best.cell_group = group;
       best.max_per_item = cfg.max_per_item;
       best.degrid_threads = fwd_t;
       best.grid_threads = adj_t;

@@ -35,6 +35,7 @@ struct BatchConfig {
   int grid_threads = 0;     // 0: threads
   int max_per_item = 16;
   int tile = kTile;
+  int cell_group = 1;       // cells per work item along each axis (1, or 2 for FP32, J <= 6)
 };
 
 struct BatchInfo {
@@ -75,12 +76,14 @@ class Batch {
 // Launch and layout parameters of a batch.
 struct BatchTuning {
   int tile = kTile, max_per_item = 16, degrid_threads = 128, grid_threads = 128;
+  int cell_group = 1;
 };
 
-// Picks the uv tile edge and the CTA sizes of the two gridding kernels for
-// this batch by timing candidates on the GPU: a sample of up to eight
-// channels (evenly spaced in visibility count) is planned for each tile
-// edge, and each plan is timed with each CTA size, forward and adjoint apart.
+// Picks the uv tile edge, the work-item shape (single cells or 2 x 2 groups)
+// and the CTA sizes of the two gridding kernels for this batch by timing
+// candidates on the GPU: a sample of up to eight channels (evenly spaced in
+// visibility count) is planned for each tile edge and item shape, and each
+// plan is timed with each CTA size, forward and adjoint apart.
 // Results are cached per process, keyed by precision, kernel, support,
 // oversampling and the sample's sizes.
 BatchTuning autotune_batch(const BatchConfig &cfg);

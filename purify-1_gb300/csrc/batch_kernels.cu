@@ -127,9 +127,10 @@ template <typename real>
 cudaError_t launch_degrid_group(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
                                 int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
                                 bool user, bool weight, cudaStream_t s) {
-  const size_t smem = degrid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, weight);
+  const size_t smem =
+      degrid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, weight, a.group_cells);
   ApplyArgs<real> b = a;
-  b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, false));
+  b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, false, a.group_cells));
   b.stage_bytes = int(stage_bytes(sizeof(real), J, user, weight));
   return launch_apply<real, true>(true, b, poly, J, ntasks, smem, shape.threads, s);
 }
@@ -137,9 +138,10 @@ template <typename real>
 cudaError_t launch_grid_group(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
                               int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
                               bool user, bool weight, cudaStream_t s) {
-  const size_t smem = grid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, weight);
+  const size_t smem =
+      grid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, weight, a.group_cells);
   ApplyArgs<real> b = a;
-  b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, true));
+  b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, true, a.group_cells));
   return launch_apply<real, true>(false, b, poly, J, ntasks, smem, shape.threads, s);
 }
 

@@ -119,6 +119,8 @@ pg::OperatorConfig to_config(const purify_gb300_create_args *a, const purify_gb3
     c.max_per_item = t->max_per_item;
     c.tile = t->tile;
     c.fused_permute = t->fused_permute;
+    c.cell_group = t->cell_group;
+    c.class_cap = t->class_cap;
   }
   if (a->precision != PURIFY_GB300_FP32 && a->precision != PURIFY_GB300_FP64)
     throw pg::Error(pg::kInvalidArgument, "unknown precision");
@@ -350,6 +352,7 @@ int purify_gb300_operator_info(const purify_gb300_operator *op, purify_gb300_inf
     info->slots = i.slots;
     info->window_cells = i.window_cells;
     info->factor_values = i.factor_values;
+    info->cell_group = i.cell_group;
   });
 }
 
@@ -416,6 +419,11 @@ int purify_gb300_uv_to_pixels(const double *u, const double *v, int64_t M, int32
 int purify_gb300_plan_create(const double *u, const double *v, const double *weights, int64_t M,
                              uint32_t ftsizeu, uint32_t ftsizev, uint32_t J,
                              purify_gb300_plan **out) {
+  return purify_gb300_plan_create_grouped(u, v, weights, M, ftsizeu, ftsizev, J, 1, out);
+}
+int purify_gb300_plan_create_grouped(const double *u, const double *v, const double *weights,
+                                     int64_t M, uint32_t ftsizeu, uint32_t ftsizev, uint32_t J,
+                                     int32_t group, purify_gb300_plan **out) {
   if (!out) return null_arg("out");
   *out = nullptr;
   return guard([&] {
@@ -427,6 +435,7 @@ int purify_gb300_plan_create(const double *u, const double *v, const double *wei
     rq.Nu = int(ftsizeu);
     rq.Nv = int(ftsizev);
     rq.Ju = rq.Jv = int(J);
+    rq.group = group;
     auto *p = new purify_gb300_plan();
     try {
       p->plan = pg::build_plan(rq);
@@ -450,6 +459,8 @@ int purify_gb300_plan_sizes(const purify_gb300_plan *p, int64_t *sizes) {
   sizes[6] = P.win_rows;
   sizes[7] = P.win_cols;
   sizes[8] = P.unit_weights ? 1 : 0;
+  sizes[9] = P.group;
+  sizes[10] = P.win_stride;
   return PURIFY_GB300_OK;
 }
 
@@ -554,10 +565,12 @@ int purify_gb300_batch_create(const purify_gb300_channel *channels, int32_t nch,
       t.max_per_item = tuning->max_per_item > 0 ? tuning->max_per_item : 16;
       t.degrid_threads = tuning->degrid_threads > 0 ? tuning->degrid_threads : 128;
       t.grid_threads = tuning->grid_threads > 0 ? tuning->grid_threads : 128;
+      t.cell_group = tuning->cell_group > 0 ? tuning->cell_group : 1;
     } else {
       t = pg::autotune_batch(cfg);
     }
     cfg.tile = t.tile;
+    cfg.cell_group = t.cell_group;
     cfg.max_per_item = t.max_per_item;
     cfg.threads = 128;
     cfg.degrid_threads = t.degrid_threads;
@@ -580,6 +593,7 @@ int purify_gb300_batch_get_tuning(const purify_gb300_batch *b, purify_gb300_batc
   t->max_per_item = b->tuning.max_per_item;
   t->degrid_threads = b->tuning.degrid_threads;
   t->grid_threads = b->tuning.grid_threads;
+  t->cell_group = b->tuning.cell_group;
   return PURIFY_GB300_OK;
 }
 int purify_gb300_batch_bind(purify_gb300_batch *b, const void *const *x_in, void *const *vis,

@@ -229,13 +229,13 @@ int stream_blocks(int64_t n, int threads) {
 }  // namespace
 
 size_t degrid_smem_bytes(int precision_bytes, int J, int win_rows, int win_cols,
-                         const LaunchShape &shape, bool user, bool weight) {
-  return window_bytes(precision_bytes, win_rows, win_cols, shape, false) + kHeaderBytes +
+                         const LaunchShape &shape, bool user, bool weight, int group) {
+  return window_bytes(precision_bytes, win_rows, win_cols, shape, false, group) + kHeaderBytes +
          size_t(shape.threads / 32) * stage_bytes(precision_bytes, J, user, weight);
 }
 size_t grid_smem_bytes(int precision_bytes, int, int win_rows, int win_cols,
-                       const LaunchShape &shape, bool, bool) {
-  return window_bytes(precision_bytes, win_rows, win_cols, shape, true) + kHeaderBytes;
+                       const LaunchShape &shape, bool, bool, int group) {
+  return window_bytes(precision_bytes, win_rows, win_cols, shape, true, group) + kHeaderBytes;
 }
 
 template <typename real>
@@ -243,9 +243,10 @@ cudaError_t launch_degrid(const ApplyArgs<real> &a, const PolyTable<real> &poly,
                           int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
                           cudaStream_t s) {
   const bool user = a.slot_user != nullptr, weight = a.weight != nullptr;
-  const size_t smem = degrid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, weight);
+  const size_t smem =
+      degrid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, weight, a.group_cells);
   ApplyArgs<real> b = a;
-  b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, false));
+  b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, false, a.group_cells));
   b.stage_bytes = int(stage_bytes(sizeof(real), J, user, weight));
   return launch_apply<real, false>(true, b, poly, J, ntasks, smem, shape.threads, s);
 }
@@ -254,9 +255,10 @@ cudaError_t launch_grid(const ApplyArgs<real> &a, const PolyTable<real> &poly, i
                         int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
                         cudaStream_t s) {
   const bool user = a.slot_user != nullptr, weight = a.weight != nullptr;
-  const size_t smem = grid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, weight);
+  const size_t smem =
+      grid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, weight, a.group_cells);
   ApplyArgs<real> b = a;
-  b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, true));
+  b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, true, a.group_cells));
   return launch_apply<real, false>(false, b, poly, J, ntasks, smem, shape.threads, s);
 }
 

@@ -30,6 +30,7 @@ struct ApplyArgs {
   const int32_t *slot_user = nullptr;
   int Nu = 0, Nv = 0;
   int win_stride = 0;               // row stride of the shared-memory windows (plan's win_stride)
+  int group_cells = 1;              // cells per work item along each axis (plan's group)
   int64_t slot_stride = 0;          // complex elements per tilebuf slot
   int win_bytes = 0;    // set by the launchers: shared bytes before the batch headers
   int stage_bytes = 0;  // set by the launchers: per-warp staging stride
@@ -54,9 +55,11 @@ struct LaunchShape {
 // user = visibilities in caller order, weight = a weight stream (they size
 // the degrid kernel's staging buffers; the grid kernel has none).
 size_t degrid_smem_bytes(int precision_bytes, int J, int win_rows, int win_cols,
-                         const LaunchShape &shape, bool user = true, bool weight = true);
+                         const LaunchShape &shape, bool user = true, bool weight = true,
+                         int group = 1);
 size_t grid_smem_bytes(int precision_bytes, int J, int win_rows, int win_cols,
-                       const LaunchShape &shape, bool user = false, bool weight = true);
+                       const LaunchShape &shape, bool user = false, bool weight = true,
+                       int group = 1);
 
 // G: tiles of the grid -> visibilities.
 template <typename real>

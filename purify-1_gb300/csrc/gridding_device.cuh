@@ -12,6 +12,7 @@
 
 #include "cplx_ops.cuh"
 #include "device_kernels.h"
+#include "plan.h"
 
 namespace pg {
 namespace dev {
@@ -54,6 +55,26 @@ __device__ __forceinline__ void tap_weights(const PolyAxis<real, NC> &P, int nsu
       const real mirror = fma(-x, o, e);
       k[J - 1 - j] = (J % 2 == 1) ? mirror : -mirror;
     }
+  }
+}
+
+// Tap weights of one axis over the register block of an item of G x G base
+// cells (G = 1 or 2; block JB = J + G - 1 cells).  With G = 2 the stored
+// fraction x = t + d carries the visibility's cell d in {0, 1} inside the
+// group: its J taps start at block cell d and the other block cell is 0.
+template <typename real, int J, int G, bool SUB, int NC>
+__device__ __forceinline__ void block_taps(const PolyAxis<real, NC> &P, int nsub, real x,
+                                           real (&k)[J + G - 1]) {
+  if constexpr (G == 1) {
+    tap_weights<real, J, SUB>(P, nsub, x, k);
+  } else {
+    const bool d = x >= real(1);
+    real kk[J];
+    tap_weights<real, J, SUB>(P, nsub, d ? x - real(1) : x, kk);
+    k[0] = d ? real(0) : kk[0];
+#pragma unroll
+    for (int j = 1; j < J; ++j) k[j] = d ? kk[j - 1] : kk[j];
+    k[J] = d ? kk[J - 1] : real(0);
   }
 }
 
@@ -189,17 +210,19 @@ __device__ __forceinline__ void next_chunk(int &lb, int &k0, const int2 *hdr, in
   }
 }
 
-template <typename real, int J, bool SUB, bool GROUP>
+template <typename real, int J, int G, bool SUB, bool GROUP>
 __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
                                                      const __grid_constant__ PolyTable<real> poly) {
   using C = cplx<real>;
   constexpr int CH = StageDepth<real, J>::value;
+  constexpr int JB = J + G - 1;  // register block of an item (G x G base cells)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int task_id = a0.order ? a0.order[blockIdx.x] : int(blockIdx.x);
   const Task tk = a0.tasks[task_id];
   const auto &a = ArgsOf<real, GROUP>::get(a0, tk.channel);
-  // the window in shared memory: WH rows of WW cells at row stride WS
-  const int WW = tk.W + J - 1, WH = tk.H + J - 1, WS = a.win_stride;
+  // the window in shared memory: WH rows of WW cells at row stride WS,
+  // cell (r, c) at win_offset(r, c, WS, G)
+  const int WW = tk.W + JB - 1, WH = tk.H + JB - 1, WS = a.win_stride;
   C *win = reinterpret_cast<C *>(smem_raw);
   const TaskHeaders th = load_headers(a, tk, smem_raw + a0.win_bytes);
   const C *grid = static_cast<const C *>(a.grid);
@@ -210,7 +233,7 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
     if (p >= a.Nv) p -= a.Nv;
     int q = tk.Q + lq;
     if (q >= a.Nu) q -= a.Nu;
-    cp_async<sizeof(C)>(win + lp * WS + lq, grid + size_t(p) * a.Nu + q);
+    cp_async<sizeof(C)>(win + win_offset(lp, lq, WS, G), grid + size_t(p) * a.Nu + q);
   }
   cp_async_wait_all();
   __syncthreads();
@@ -243,7 +266,7 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
   issue(ilb, ik0, 0);
   next_chunk<CH>(ilb, ik0, th.hdr, nw);
   int lb = warp, k0 = 0, buf = 0, cnt = 0;
-  C F[J][J];
+  C F[JB][JB];
   while (lb < nbt) {
     if (ilb < nbt) {
       issue(ilb, ik0, buf ^ 1);
@@ -256,11 +279,11 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
       // new batch: this lane's item and its J x J grid block
       const int code = th.code[lb * kBatch + lane];
       cnt = item_count(code);
-      const int lp = item_lp(code), lq = item_lq(code);
+      const C *blk = win + win_offset(item_lp(code), item_lq(code), WS, G);
 #pragma unroll
-      for (int jv = 0; jv < J; ++jv)
+      for (int jv = 0; jv < JB; ++jv)
 #pragma unroll
-        for (int ju = 0; ju < J; ++ju) F[jv][ju] = win[(lp + jv) * WS + lq + ju];
+        for (int ju = 0; ju < JB; ++ju) F[jv][ju] = blk[win_offset(jv, ju, WS, G)];
     }
     cp_async_wait_group<1>();
     const int n = min(CH, bt.y - k0);
@@ -268,15 +291,15 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
       const int k = k0 + j;
       const int e = (buf * CH + j) * 32 + lane;
       const C t = st_t[e];
-      real ku[J], kv[J];
-      tap_weights<real, J, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
-      tap_weights<real, J, SUB>(poly.v, poly.nsub_v, t.y, kv);
+      real ku[JB], kv[JB];
+      block_taps<real, J, G, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
+      block_taps<real, J, G, SUB>(poly.v, poly.nsub_v, t.y, kv);
       C sum{0, 0};
 #pragma unroll
-      for (int jv = 0; jv < J; ++jv) {
+      for (int jv = 0; jv < JB; ++jv) {
         C row{0, 0};
 #pragma unroll
-        for (int ju = 0; ju < J; ++ju) row = fma2(splat(ku[ju]), F[jv][ju], row);
+        for (int ju = 0; ju < JB; ++ju) row = fma2(splat(ku[ju]), F[jv][ju], row);
         sum = fma2(splat(kv[jv]), row, sum);
       }
       const real sr = sum.x, si = sum.y;
@@ -305,17 +328,20 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
   cp_async_wait_all();
 }
 
-template <typename real, int J, bool SUB, bool GROUP>
+template <typename real, int J, int G, bool SUB, bool GROUP>
 __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
                                                    const __grid_constant__ PolyTable<real> poly) {
   using C = cplx<real>;
+  constexpr int JB = J + G - 1;  // register block of an item (G x G base cells)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int task_id = a0.order ? a0.order[blockIdx.x] : int(blockIdx.x);
   const Task tk = a0.tasks[task_id];
   const auto &a = ArgsOf<real, GROUP>::get(a0, tk.channel);
-  // warp windows in shared memory: WH rows at row stride WS (WN cells each);
-  // the task window written out is WH x WW, packed
-  const int WW = tk.W + J - 1, WH = tk.H + J - 1, WS = a.win_stride, WN = WS * WH;
+  // warp windows in shared memory: WH rows at row stride WS (WN cells each,
+  // cell (r, c) at win_offset(r, c, WS, G)); the task window written out is
+  // WH x WW, packed
+  const int WW = tk.W + JB - 1, WH = tk.H + JB - 1, WS = a.win_stride,
+            WN = win_cells(WH, WS, G);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   C *wins = reinterpret_cast<C *>(smem_raw);
   const TaskHeaders th = load_headers(a, tk, smem_raw + a0.win_bytes);
@@ -351,11 +377,11 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
       y1 = read_vis(a, vin, slot(plb, pk));
       adv(plb, pk);
     }
-    C acc[J][J];
+    C acc[JB][JB];
 #pragma unroll
-    for (int jv = 0; jv < J; ++jv)
+    for (int jv = 0; jv < JB; ++jv)
 #pragma unroll
-      for (int ju = 0; ju < J; ++ju) acc[jv][ju] = C{0, 0};
+      for (int ju = 0; ju < JB; ++ju) acc[jv][ju] = C{0, 0};
     while (clb < nbt) {
       const C t = t0, yv = y0;
       const size_t i_cur = slot(clb, ck);
@@ -378,15 +404,15 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
         zr = w.x * yv.x + w.y * yv.y;
         zi = w.x * yv.y - w.y * yv.x;
       }
-      real ku[J], kv[J];
-      tap_weights<real, J, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
-      tap_weights<real, J, SUB>(poly.v, poly.nsub_v, t.y, kv);
+      real ku[JB], kv[JB];
+      block_taps<real, J, G, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
+      block_taps<real, J, G, SUB>(poly.v, poly.nsub_v, t.y, kv);
       const C z{zr, zi};
 #pragma unroll
-      for (int jv = 0; jv < J; ++jv) {
+      for (int jv = 0; jv < JB; ++jv) {
         const C az = mul2(z, splat(kv[jv]));
 #pragma unroll
-        for (int ju = 0; ju < J; ++ju) acc[jv][ju] = fma2(az, splat(ku[ju]), acc[jv][ju]);
+        for (int ju = 0; ju < JB; ++ju) acc[jv][ju] = fma2(az, splat(ku[ju]), acc[jv][ju]);
       }
       if (ck + 1 >= th.hdr[clb].y) {
         // Flush at the end of the batch.  The items of one batch have
@@ -395,13 +421,13 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
         // summation order a function of the plan.
         const int code = th.code[clb * kBatch + lane];
         const int cnt = item_count(code);
-        const int lp = item_lp(code), lq = item_lq(code);
+        C *blk = mine + win_offset(item_lp(code), item_lq(code), WS, G);
 #pragma unroll
-        for (int jv = 0; jv < J; ++jv)
+        for (int jv = 0; jv < JB; ++jv)
 #pragma unroll
-          for (int ju = 0; ju < J; ++ju) {
+          for (int ju = 0; ju < JB; ++ju) {
             if (cnt > 0) {
-              C *cell = mine + (lp + jv) * WS + lq + ju;
+              C *cell = blk + win_offset(jv, ju, WS, G);
               *cell = add2(*cell, acc[jv][ju]);
             }
             acc[jv][ju] = C{0, 0};
@@ -415,7 +441,7 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
   const int local_task = GROUP ? task_id - a0.group_task_base[tk.channel] : task_id;
   C *out = static_cast<C *>(a.tilebuf) + size_t(local_task) * a.slot_stride;
   for (int idx = threadIdx.x; idx < WW * WH; idx += blockDim.x) {
-    const int lp = idx / WW, e = idx + lp * (WS - WW);
+    const int lp = idx / WW, e = win_offset(lp, idx - lp * WW, WS, G);
     C s = wins[e];
     for (int w = 1; w < nw; ++w) {
       const C o = wins[w * WN + e];
@@ -530,8 +556,8 @@ inline size_t stage_bytes(int precision_bytes, int J, bool user, bool weight) {
 }
 
 inline size_t window_bytes(int precision_bytes, int win_rows, int win_cols, const LaunchShape &shape,
-                    bool per_warp) {
-  const size_t one = size_t(win_rows) * win_cols * 2 * precision_bytes;
+                           bool per_warp, int group = 1) {
+  const size_t one = size_t(win_cells(win_rows, win_cols, group)) * 2 * precision_bytes;
   const size_t b = per_warp ? one * size_t(shape.threads / 32) : one;
   return (b + 15) / 16 * 16;
 }
@@ -539,10 +565,10 @@ inline size_t window_bytes(int precision_bytes, int win_rows, int win_cols, cons
 // Dispatch on the support J (templated so the J x J block stays in registers)
 // and on whether the kernel polynomial has sub-segments (narrow kernels, PSWF).
 
-template <typename real, int J, bool SUB, bool GROUP>
+template <typename real, int J, int G, bool SUB, bool GROUP>
 cudaError_t launch_one(bool degrid, const ApplyArgs<real> &a, const PolyTable<real> &poly,
                        int ntasks, size_t smem, int threads, cudaStream_t s) {
-  auto fn = degrid ? degrid_kernel<real, J, SUB, GROUP> : grid_kernel<real, J, SUB, GROUP>;
+  auto fn = degrid ? degrid_kernel<real, J, G, SUB, GROUP> : grid_kernel<real, J, G, SUB, GROUP>;
   if (smem > 48 * 1024) {
     const cudaError_t e =
         cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
@@ -557,19 +583,34 @@ cudaError_t launch_apply(bool degrid, const ApplyArgs<real> &a, const PolyTable<
                          int J, int ntasks, size_t smem, int threads, cudaStream_t s) {
   if (ntasks == 0) return cudaSuccess;
   const bool sub = poly.nsub_u > 1 || poly.nsub_v > 1;
-#define PG_CASE(JJ)                                                                    \
-  case JJ:                                                                             \
-    return sub ? launch_one<real, JJ, true, GROUP>(degrid, a, poly, ntasks, smem, threads, s) \
-               : launch_one<real, JJ, false, GROUP>(degrid, a, poly, ntasks, smem, threads, s);
+#define PG_CASE(JJ, GG)                                                                  \
+  case JJ:                                                                               \
+    return sub ? launch_one<real, JJ, GG, true, GROUP>(degrid, a, poly, ntasks, smem, threads, s) \
+               : launch_one<real, JJ, GG, false, GROUP>(degrid, a, poly, ntasks, smem, threads, s);
+  if (a.group_cells == 2) {
+    // 2 x 2 groups: complex<float> with J <= kMaxGroupJ (the (J + 1)^2
+    // block stays in registers)
+    if constexpr (sizeof(real) == 4) {
+      switch (J) {
+        PG_CASE(1, 2)
+        PG_CASE(2, 2)
+        PG_CASE(3, 2)
+        PG_CASE(4, 2)
+        PG_CASE(5, 2)
+        PG_CASE(6, 2)
+      }
+    }
+    return cudaErrorInvalidValue;
+  }
   switch (J) {
-    PG_CASE(1)
-    PG_CASE(2)
-    PG_CASE(3)
-    PG_CASE(4)
-    PG_CASE(5)
-    PG_CASE(6)
-    PG_CASE(7)
-    PG_CASE(8)
+    PG_CASE(1, 1)
+    PG_CASE(2, 1)
+    PG_CASE(3, 1)
+    PG_CASE(4, 1)
+    PG_CASE(5, 1)
+    PG_CASE(6, 1)
+    PG_CASE(7, 1)
+    PG_CASE(8, 1)
   }
 #undef PG_CASE
   return cudaErrorInvalidValue;

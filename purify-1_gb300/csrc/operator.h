@@ -45,7 +45,17 @@ struct OperatorConfig {
   // 0: through a slot-ordered buffer and separate gather kernels;
   // -1: default (direct for the forward, gather for the adjoint).
   int fused_permute = -1;
+  // cells per work item along each axis: 0 picks 2 for complex<float> with
+  // J <= kMaxGroupJ (2 x 2 groups of base cells, a (J + 1)^2 block), else 1
+  int cell_group = 0;
+  // most items of one bank class per batch (0: the planner's default)
+  int class_cap = 0;
 };
+
+// A plan fraction t + d (see PlanRequest::group) in precision `real`, kept
+// below d + 1 after rounding.
+template <typename real>
+real fraction_in_cell(double x);
 
 // S(j, i) = 1 / (ftv(y0 + j + 0.5) ftu(x0 + i + 0.5)) for the kernel, as
 // row-major imsizey x imsizex reals.
@@ -61,7 +71,7 @@ struct OperatorInfo {
   int64_t nnz = 0, occupied_cells = 0, work_items = 0, tasks = 0, device_bytes = 0;
   double kernel_fit_error = 0, norm = 1;
   int device = 0;
-  int64_t slots = 0, window_cells = 0, factor_values = 0;
+  int64_t slots = 0, window_cells = 0, factor_values = 0, cell_group = 1;
 };
 
 // Scratch of one apply held outside the operator, so that several applies of

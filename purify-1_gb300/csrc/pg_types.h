@@ -38,6 +38,9 @@ enum KernelId : int { kKB = 0, kGauss = 1, kBox = 2, kPSWF = 3, kKBMin = 4, kGau
 
 // Largest separable support handled by the plain (non w-projection) kernels.
 constexpr int kMaxJ = 8;
+// Largest support whose items may group 2 x 2 base cells (complex<float>
+// only: the (J + 1)^2 register block must stay in registers).
+constexpr int kMaxGroupJ = 6;
 // Largest number of sub-segments per tap of a piecewise kernel polynomial.
 constexpr int kMaxSub = 4;
 // Polynomial coefficient counts (degree + 1) per precision.

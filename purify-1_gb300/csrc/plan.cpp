@@ -54,6 +54,8 @@ Plan build_plan(const PlanRequest &rq) {
   if (rq.tile < 1 || rq.tile > 255) throw std::invalid_argument("tile edge out of range");
   if (rq.max_batches_per_task < 1 || rq.max_batches_per_task > kMaxTaskBatches)
     throw std::invalid_argument("max_batches_per_task out of range");
+  if (rq.group != 1 && rq.group != 2) throw std::invalid_argument("group must be 1 or 2");
+  if (rq.class_cap < 0 || rq.class_cap > 16) throw std::invalid_argument("class_cap out of range");
   for (int64_t m = 0; m < rq.M; ++m)
     if (!std::isfinite(rq.u[m]) || !std::isfinite(rq.v[m]))
       throw std::invalid_argument("visibility " + std::to_string(m) +
@@ -65,24 +67,29 @@ Plan build_plan(const PlanRequest &rq) {
   P.Nv = rq.Nv;
   P.Ju = rq.Ju;
   P.Jv = rq.Jv;
+  P.group = rq.group;
+  const int G = rq.group;
+  const int class_cap = rq.class_cap > 0 ? rq.class_cap : kClassCap;
+  // register block of an item: the support plus the extra cell of a group
+  const int JBu = rq.Ju + G - 1, JBv = rq.Jv + G - 1;
   P.tu = make_tiling(rq.Nu, rq.tile);
   P.tv = make_tiling(rq.Nv, rq.tile);
-  // A window reaches J - 1 cells into the next tile; it must not reach two
-  // tiles ahead, so every tile must be at least J - 1 cells wide, and the
+  // A window reaches JB - 1 cells into the next tile; it must not reach two
+  // tiles ahead, so every tile must be at least JB - 1 cells wide, and the
   // grid must hold the support.
   if (rq.Nu < rq.Ju || rq.Nv < rq.Jv)
     throw std::invalid_argument("grid is smaller than the kernel support");
   for (int b = 0; b < P.tu.n; ++b)
-    if (P.tu.start[b + 1] - P.tu.start[b] < rq.Ju - 1)
+    if (P.tu.start[b + 1] - P.tu.start[b] < JBu - 1)
       throw std::invalid_argument("grid width is too small for the kernel support");
   for (int b = 0; b < P.tv.n; ++b)
-    if (P.tv.start[b + 1] - P.tv.start[b] < rq.Jv - 1)
+    if (P.tv.start[b + 1] - P.tv.start[b] < JBv - 1)
       throw std::invalid_argument("grid height is too small for the kernel support");
 
   const int ntu = P.tu.n, ntv = P.tv.n, ntiles = ntu * ntv;
   // Row stride of the tasks' shared-memory windows: the widest window.
   int WS = 0;
-  for (int b = 0; b < ntu; ++b) WS = std::max(WS, P.tu.start[b + 1] - P.tu.start[b] + rq.Ju - 1);
+  for (int b = 0; b < ntu; ++b) WS = std::max(WS, P.tu.start[b + 1] - P.tu.start[b] + JBu - 1);
   P.win_stride = WS;
   // Cell rank: tiles in row-major order, cells row-major inside a tile.
   std::vector<int64_t> tile_cell0(ntiles + 1, 0);
@@ -102,6 +109,9 @@ Plan build_plan(const PlanRequest &rq) {
   std::vector<double> tu(M), tv(M);
   std::vector<int64_t> rank(M);
   std::vector<uint8_t> flip(M);
+  // With groups, a visibility's base cell inside its group (dx, dy) is added
+  // to its fractions and the item is keyed by the group's anchor cell.
+  const int gmask = ~(G - 1);
 #pragma omp parallel for schedule(static)
   for (int64_t m = 0; m < M; ++m) {
     const double su = rq.u[m] - rq.Ju * 0.5, sv = rq.v[m] - rq.Jv * 0.5;
@@ -116,7 +126,11 @@ Plan build_plan(const PlanRequest &rq) {
     const int a = P.tv.of[p0], b = P.tu.of[q0];
     const int t = a * ntu + b;
     const int w = P.tu.start[b + 1] - P.tu.start[b];
-    rank[m] = tile_cell0[t] + int64_t(p0 - P.tv.start[a]) * w + (q0 - P.tu.start[b]);
+    const int lp = p0 - P.tv.start[a], lq = q0 - P.tu.start[b];
+    const int ap = lp & gmask, aq = lq & gmask;
+    tu[m] += double(lq - aq);
+    tv[m] += double(lp - ap);
+    rank[m] = tile_cell0[t] + int64_t(ap) * w + aq;
   }
   if (rq.weights)
     for (int64_t m = 0; m < M && P.unit_weights; ++m)
@@ -198,7 +212,7 @@ Plan build_plan(const PlanRequest &rq) {
           for (size_t k = front; k < items.size() && filled < kBatch; ++k) {
             if (same_count >= 0 && items[k].count != same_count) break;
             if (taken[k]) continue;
-            const int r = (items[k].lp * WS + items[k].lq) & 15;
+            const int r = win_offset(items[k].lp, items[k].lq, WS, G) & 15;
             int lane = lane_item[r] < 0 ? r : (lane_item[16 + r] < 0 ? 16 + r : -1);
             if (lane < 0) {
               // both class lanes taken: a free lane in the half-warp holding
@@ -227,8 +241,8 @@ Plan build_plan(const PlanRequest &rq) {
         };
         // first the items of the front item's count (no null slots among
         // them) at two per class, then the rest of the batch at kClassCap
-        scan(2, items[front].count);
-        scan(kClassCap, -1);
+        scan(std::min(2, class_cap), items[front].count);
+        scan(class_cap, -1);
         int kmax = 0;
         for (int l = 0; l < kBatch; ++l)
           if (lane_item[l] >= 0) kmax = std::max(kmax, int(items[lane_item[l]].count));
@@ -273,8 +287,8 @@ Plan build_plan(const PlanRequest &rq) {
         s = e;
       }
       P.tile_tasks[t + 1] = int32_t(P.tasks.size());
-      P.win_rows = std::max(P.win_rows, h + rq.Jv - 1);
-      P.win_cols = std::max(P.win_cols, w + rq.Ju - 1);
+      P.win_rows = std::max(P.win_rows, h + JBv - 1);
+      P.win_cols = std::max(P.win_cols, w + JBu - 1);
     }
 
   // Launch order.  Longest tasks first makes the last wave of CTAs short;

@@ -28,6 +28,14 @@ struct PlanRequest {
   int Ju = 4, Jv = 4;  // taps per axis
   int tile = kTile;
   int max_per_item = 16;         // visibilities of one cell handled by one lane
+  // Cells per work item along each axis (1 or 2).  With 2, an item is an
+  // aligned 2 x 2 group of base cells of its tile (anchored at even local
+  // row and column); its visibilities share one (J + 1) x (J + 1) register
+  // block, and each carries its cell inside the group in the integer part of
+  // its fractions (t_u + dx, t_v + dy with dx, dy in {0, 1}).
+  int group = 1;
+  // Most items of one bank class per batch (0: the default, see plan.cpp).
+  int class_cap = 0;
   int max_batches_per_task = kMaxTaskBatches;
   int64_t max_slots_per_task = 16384;
 };
@@ -48,7 +56,7 @@ struct Plan {
   // by the phase sign alone.
   bool unit_weights = true;
   // per slot
-  std::vector<double> frac_u, frac_v;        // in [0, 1); 0 for null slots
+  std::vector<double> frac_u, frac_v;        // t + d in [0, group); 0 for null slots
   std::vector<uint8_t> flip;                 // (-1)^(k_u + k_v) == -1
   std::vector<std::complex<double>> weight;  // weight with the sign folded in (empty when unit)
   std::vector<int32_t> slot_user;            // caller index, -1 for null slots
@@ -62,15 +70,32 @@ struct Plan {
   // the grid is at most kLptGridBytes, else the tile order.
   std::vector<int32_t> task_order;
   std::vector<int32_t> tile_tasks;  // ntiles + 1 offsets into tasks
-  int win_rows = 0, win_cols = 0;   // largest window: (H + Jv - 1) x (W + Ju - 1)
+  int win_rows = 0, win_cols = 0;   // largest window: (H + JBv - 1) x (W + JBu - 1)
   // Row stride of the windows in shared memory (the widest window); a batch's
-  // lane l preferably holds an item with (lp * win_stride + lq) mod 16 == l mod 16.
+  // lane l preferably holds an item whose window offset (win_offset) is l
+  // mod 16.
   int win_stride = 0;
+  // Cells per item along each axis (PlanRequest::group); the register block
+  // of an item is JB = J + group - 1 cells wide.
+  int group = 1;
   // statistics
   int64_t occupied_cells = 0;
   int64_t real_items = 0;
   int max_cell_count = 0;
 };
+
+// Offset of window cell (r, c) in a shared-memory window of row stride WS.
+// Items of 2 x 2 groups sit at even rows and columns, which would leave
+// their offsets r WS + c on even cells only (8 of the 16 bank pairs); one
+// extra cell per two rows spreads them over all 16 while keeping the offset
+// of (r + jv, c + ju) from (r, c) independent of r for even r.
+PG_HD inline int win_offset(int r, int c, int WS, int group) {
+  return r * WS + c + (group == 2 ? (r >> 1) : 0);
+}
+// Cells of a window of `rows` rows at row stride WS in that layout.
+PG_HD inline int win_cells(int rows, int WS, int group) {
+  return rows * WS + (group == 2 ? (rows + 1) / 2 : 0);
+}
 
 // Builds the plan.  Throws std::invalid_argument on bad input.
 Plan build_plan(const PlanRequest &req);

@@ -53,7 +53,8 @@ class CreateArgs(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("threads", ctypes.c_int32), ("max_per_item", ctypes.c_int32),
-                ("tile", ctypes.c_int32), ("fused_permute", ctypes.c_int32)]
+                ("tile", ctypes.c_int32), ("fused_permute", ctypes.c_int32),
+                ("cell_group", ctypes.c_int32), ("class_cap", ctypes.c_int32)]
 
 
 class Info(ctypes.Structure):
@@ -65,7 +66,7 @@ class Info(ctypes.Structure):
         ("work_items", ctypes.c_int64), ("tasks", ctypes.c_int64),
         ("device_bytes", ctypes.c_int64), ("kernel_fit_error", ctypes.c_double),
         ("norm", ctypes.c_double), ("slots", ctypes.c_int64), ("window_cells", ctypes.c_int64),
-        ("factor_values", ctypes.c_int64),
+        ("factor_values", ctypes.c_int64), ("cell_group", ctypes.c_int64),
     ]
 
 
@@ -76,7 +77,8 @@ class Channel(ctypes.Structure):
 
 class BatchTuning(ctypes.Structure):
     _fields_ = [("tile", ctypes.c_int32), ("max_per_item", ctypes.c_int32),
-                ("degrid_threads", ctypes.c_int32), ("grid_threads", ctypes.c_int32)]
+                ("degrid_threads", ctypes.c_int32), ("grid_threads", ctypes.c_int32),
+                ("cell_group", ctypes.c_int32)]
 
 
 class BatchInfo(ctypes.Structure):
@@ -124,6 +126,7 @@ EXPORTS = [
     "purify_gb300_uv_to_pixels",
     "purify_gb300_last_error", "purify_gb300_version", "purify_gb300_plan_create",
     "purify_gb300_plan_sizes", "purify_gb300_plan_export", "purify_gb300_plan_destroy",
+    "purify_gb300_plan_create_grouped",
     "purify_gb300_kernel_taps", "purify_gb300_degrid", "purify_gb300_grid",
     "purify_gb300_correction", "purify_gb300_stage_timing", "purify_gb300_stage_times",
     "purify_gb300_operator_create_tuned", "purify_gb300_grid_no_alloc",
@@ -178,6 +181,9 @@ def load(path=None):
                                             ctypes.c_uint32, vp, vp]
     L.purify_gb300_plan_create.argtypes = [vp, vp, vp, ctypes.c_int64, ctypes.c_uint32,
                                            ctypes.c_uint32, ctypes.c_uint32, P(vp)]
+    L.purify_gb300_plan_create_grouped.argtypes = [vp, vp, vp, ctypes.c_int64, ctypes.c_uint32,
+                                                   ctypes.c_uint32, ctypes.c_uint32,
+                                                   ctypes.c_int32, P(vp)]
     L.purify_gb300_plan_sizes.argtypes = [vp, vp]
     L.purify_gb300_plan_export.argtypes = [vp] + [vp] * 10
     L.purify_gb300_plan_destroy.argtypes = [vp]
@@ -300,18 +306,19 @@ def wrow_taps(u, v, w_centered, Jw, J, kernel="kb", oversample_ratio=2.0, imsize
 class CoveragePlan:
     """Host-side copy of the coverage plan (purify_gb300_plan_*)."""
 
-    def __init__(self, u, v, ftsizeu, ftsizev, J, weights=None):
+    def __init__(self, u, v, ftsizeu, ftsizev, J, weights=None, group=1):
         L = load()
         u = np.ascontiguousarray(u, dtype=np.float64).ravel()
         v = np.ascontiguousarray(v, dtype=np.float64).ravel()
         wt = None if weights is None else np.ascontiguousarray(weights, dtype=np.complex128)
         h = ctypes.c_void_p()
-        _check(L.purify_gb300_plan_create(_np_ptr(u), _np_ptr(v), _np_ptr(wt), u.size,
-                                          int(ftsizeu), int(ftsizev), int(J), ctypes.byref(h)))
+        _check(L.purify_gb300_plan_create_grouped(_np_ptr(u), _np_ptr(v), _np_ptr(wt), u.size,
+                                                  int(ftsizeu), int(ftsizev), int(J), int(group),
+                                                  ctypes.byref(h)))
         try:
-            sz = np.zeros(9, dtype=np.int64)
+            sz = np.zeros(11, dtype=np.int64)
             _check(L.purify_gb300_plan_sizes(h, _np_ptr(sz)))
-            M, S, nb, nt, ntu, ntv, wr, wc, unit = (int(s) for s in sz)
+            M, S, nb, nt, ntu, ntv, wr, wc, unit, grp, ws = (int(s) for s in sz)
             self.frac = np.empty((S, 2))
             self.weight = np.empty(S, dtype=np.complex128)
             self.slot_user = np.empty(S, dtype=np.int32)
@@ -331,6 +338,7 @@ class CoveragePlan:
             L.purify_gb300_plan_destroy(h)
         self.M, self.S, self.ntu, self.ntv = M, S, ntu, ntv
         self.win_rows, self.win_cols, self.unit_weights = wr, wc, bool(unit)
+        self.group, self.win_stride = grp, ws
         self.Nu, self.Nv, self.J = int(ftsizeu), int(ftsizev), int(J)
 
 
@@ -422,7 +430,8 @@ class MeasurementOperator:
         h = ctypes.c_void_p()
         if tuning:
             t = Tuning(int(tuning.get("threads", 0)), int(tuning.get("max_per_item", 0)),
-                       int(tuning.get("tile", 0)), int(tuning.get("fused_permute", -1)))
+                       int(tuning.get("tile", 0)), int(tuning.get("fused_permute", -1)),
+                       int(tuning.get("cell_group", 0)), int(tuning.get("class_cap", 0)))
             _check(L.purify_gb300_operator_create_tuned(ctypes.byref(a), ctypes.byref(t),
                                                         ctypes.byref(h)))
         else:
@@ -621,7 +630,7 @@ class Batch:
         if tuning:
             t = BatchTuning(int(tuning.get("tile", 0)), int(tuning.get("max_per_item", 0)),
                             int(tuning.get("degrid_threads", 0)),
-                            int(tuning.get("grid_threads", 0)))
+                            int(tuning.get("grid_threads", 0)), int(tuning.get("cell_group", 0)))
         _check(L.purify_gb300_batch_create(arr, n, float(oversample_ratio),
                                            KERNELS[kernel] if isinstance(kernel, str) else int(kernel),
                                            int(J), PRECISIONS[precision], int(device),
@@ -656,7 +665,8 @@ class Batch:
         t = BatchTuning()
         _check(load().purify_gb300_batch_get_tuning(self._h, ctypes.byref(t)))
         return {"tile": t.tile, "max_per_item": t.max_per_item,
-                "degrid_threads": t.degrid_threads, "grid_threads": t.grid_threads}
+                "degrid_threads": t.degrid_threads, "grid_threads": t.grid_threads,
+                "cell_group": t.cell_group}
 
     def info(self):
         i = BatchInfo()

@@ -332,3 +332,45 @@ def test_recorded_applies(pg, cuda, precision):
     torch.cuda.synchronize()
     assert rel_l2(to_np(y), to_np(first_y) / 2.0) < 1e-6
     assert rel_l2(to_np(nz), to_np(first_n) / 4.0) < 1e-6
+
+
+@pytest.mark.parametrize("kernel,J", [("kb", 1), ("kb", 2), ("kb", 4), ("kb", 6), ("pswf", 6),
+                                      ("gauss", 3), ("box", 5)])
+@pytest.mark.parametrize("group", [1, 2])
+def test_work_item_shapes(pg, oracle_mod, cuda, kernel, J, group):
+    """FP32 work items of single base cells (group 1) and of aligned 2 x 2
+    cell groups sharing a (J + 1)^2 register block (group 2): both against
+    the oracle, with complex weights, a dense core and a sparse tail, wrap-
+    around, and bit-identical repeats; the plan reports the shape it used."""
+    torch = cuda
+    rng = np.random.default_rng(10 * J + group)
+    M, n = 6000, 50  # 100 x 100 grid: tiles of 25 cells, odd groups at tile edges
+    u = np.concatenate([rng.normal(0, 6, M // 2), rng.uniform(-70, 70, M - M // 2)])
+    v = np.concatenate([rng.normal(0, 6, M // 2), rng.uniform(-70, 70, M - M // 2)])
+    wt = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    gop = pg.MeasurementOperator(u, v, None, wt, n, n, 2.0, power_iters=0, kernel=kernel, Ju=J,
+                                 Jv=J, precision="fp32", tuning={"cell_group": group})
+    assert gop.info()["cell_group"] == group
+    oop = oracle_mod.Operator(u, v, None, wt, n, n, 2.0, kernel=kernel, Ju=J, Jv=J)
+    x = rng.standard_normal(n * n) + 1j * rng.standard_normal(n * n)
+    xd = to_dev(torch, x, "fp32")
+    y1 = gop.forward(xd)
+    y2 = gop.forward(xd)
+    assert torch.equal(y1, y2)
+    assert rel_l2(to_np(y1), oop.forward(x)) < TOL["fp32"]
+    yy = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    yd = to_dev(torch, yy, "fp32")
+    a1 = gop.adjoint(yd)
+    a2 = gop.adjoint(yd)
+    assert torch.equal(a1, a2)
+    assert rel_l2(to_np(a1), oop.adjoint(yy)) < TOL["fp32"]
+
+
+def test_default_work_items_are_grouped_for_fp32(pg, cuda):
+    """The default plan groups 2 x 2 base cells for complex<float> with
+    J <= 6 and keeps single cells for J > 6 and for complex<double>."""
+    u = np.zeros(10)
+    for prec, J, want in (("fp32", 6, 2), ("fp32", 7, 1), ("fp64", 4, 1)):
+        op = pg.MeasurementOperator(u, u, None, None, 32, 32, 2.0, power_iters=0, kernel="kb",
+                                    Ju=J, Jv=J, precision=prec)
+        assert op.info()["cell_group"] == want, (prec, J)

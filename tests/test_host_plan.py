@@ -35,17 +35,38 @@ def _lanes(plan, b):
         yield lane, lp, lq, cnt, [base + 32 * k + lane for k in range(kmax)]
 
 
+def block_taps(plan, kernel="kb"):
+    """Tap vectors of every slot over its item's register block (JB = J +
+    group - 1 cells): the J taps at the fraction's cell d inside the group
+    (frac = t + d), zeros elsewhere — what block_taps evaluates on the device."""
+    import purify_gb300 as pg
+    J, G = plan.J, plan.group
+    out = []
+    for axis in (0, 1):
+        f = plan.frac[:, axis]
+        d = np.floor(f).astype(int) if G == 2 else np.zeros(f.size, dtype=int)
+        assert d.min() >= 0 and d.max() <= G - 1
+        taps, _ = pg.kernel_taps(kernel, J, f - d, precision="fp64")
+        blk = np.zeros((f.size, J + G - 1))
+        for k in range(G):
+            sel = d == k
+            blk[sel, k:k + J] = taps[sel]
+        out.append(blk)
+    return out
+
+
 def replay_degrid(plan, taps_u, taps_v, grid):
     """Slot values as degrid_kernel writes them, then compact_kernel."""
-    J, Nu, Nv = plan.J, plan.Nu, plan.Nv
+    JB, Nu, Nv = plan.J + plan.group - 1, plan.Nu, plan.Nv
     slots = np.zeros(plan.S, dtype=np.complex128)
     g = grid.reshape(Nv, Nu)
     for (P, Q, H, W, b0, b1, tile, _) in plan.tasks:
         for b in range(b0, b1):
             for lane, lp, lq, cnt, sl in _lanes(plan, b):
                 assert lp < H and lq < W
-                rows = (P + lp + np.arange(J)) % Nv
-                cols = (Q + lq + np.arange(J)) % Nu
+                assert lp % plan.group == 0 and lq % plan.group == 0
+                rows = (P + lp + np.arange(JB)) % Nv
+                cols = (Q + lq + np.arange(JB)) % Nu
                 F = g[np.ix_(rows, cols)]
                 for k, i in enumerate(sl):
                     assert (plan.slot_user[i] >= 0) == (k < cnt)
@@ -56,7 +77,7 @@ def replay_degrid(plan, taps_u, taps_v, grid):
 def replay_grid(plan, taps_u, taps_v, vis):
     """expand_kernel, task windows as grid_kernel writes them, then
     fold_kernel's fixed-order sum."""
-    J, Nu, Nv = plan.J, plan.Nu, plan.Nv
+    J, Nu, Nv = plan.J + plan.group - 1, plan.Nu, plan.Nv  # J: the block width
     slots = np.where(plan.slot_user >= 0, vis[np.maximum(plan.slot_user, 0)], 0)
     windows = []
     for (P, Q, H, W, b0, b1, tile, _) in plan.tasks:
@@ -95,25 +116,30 @@ def replay_grid(plan, taps_u, taps_v, vis):
     return grid.ravel()
 
 
-@pytest.mark.parametrize("n,J,M,spread,seed", [
-    (16, 4, 10, 1.0, 0),     # the reference's golden operator shape
-    (24, 6, 300, 12.0, 1),   # grid 48: two uneven tiles per axis
-    (40, 3, 500, 40.0, 2),   # u, v well outside the grid: periodic wrap
-    (20, 8, 200, 3.0, 3),    # dense: many visibilities per cell, several layers
-    (18, 5, 64, 9.0, 4),     # odd support, 36-cell grid
+@pytest.mark.parametrize("n,J,M,spread,seed,group", [
+    (16, 4, 10, 1.0, 0, 1),     # the reference's golden operator shape
+    (24, 6, 300, 12.0, 1, 1),   # grid 48: two uneven tiles per axis
+    (40, 3, 500, 40.0, 2, 1),   # u, v well outside the grid: periodic wrap
+    (20, 8, 200, 3.0, 3, 1),    # dense: many visibilities per cell, several layers
+    (18, 5, 64, 9.0, 4, 1),     # odd support, 36-cell grid
+    (16, 4, 10, 1.0, 0, 2),     # 2 x 2 cell groups: the same shapes
+    (24, 6, 300, 12.0, 1, 2),
+    (40, 3, 500, 40.0, 2, 2),
+    (20, 5, 200, 3.0, 3, 2),
+    (18, 5, 64, 9.0, 4, 2),     # 36-cell grid: tiles of 18, odd halo
+    (25, 2, 400, 8.0, 5, 2),    # odd grid width (50): tiles of 25, a last group of one cell
 ])
-def test_plan_replay_matches_oracle_G(pg, oracle_mod, n, J, M, spread, seed):
+def test_plan_replay_matches_oracle_G(pg, oracle_mod, n, J, M, spread, seed, group):
     rng = np.random.default_rng(seed)
     u = rng.normal(0, spread, M)
     v = rng.normal(0, spread, M)
     wt = rng.standard_normal(M) + 1j * rng.standard_normal(M)
     Nu = Nv = 2 * n
-    plan = pg.CoveragePlan(u, v, Nu, Nv, J, weights=wt)
-    assert not plan.unit_weights
+    plan = pg.CoveragePlan(u, v, Nu, Nv, J, weights=wt, group=group)
+    assert plan.group == group and not plan.unit_weights
     assert sorted(plan.user_slot.tolist()) == sorted(np.flatnonzero(plan.slot_user >= 0).tolist())
     assert np.array_equal(plan.slot_user[plan.user_slot], np.arange(M))
-    taps_u, _ = pg.kernel_taps("kb", J, plan.frac[:, 0], precision="fp64")
-    taps_v, _ = pg.kernel_taps("kb", J, plan.frac[:, 1], precision="fp64")
+    taps_u, taps_v = block_taps(plan)
     op = oracle_mod.Operator(u, v, None, wt, n, n, 2.0, kernel="kb", Ju=J, Jv=J)
     grid = rng.standard_normal(Nu * Nv) + 1j * rng.standard_normal(Nu * Nv)
     y = replay_degrid(plan, taps_u, taps_v, grid)
@@ -130,8 +156,7 @@ def test_unit_weights_plan_matches_oracle(pg, oracle_mod):
     v = rng.normal(0, 10, M)
     plan = pg.CoveragePlan(u, v, 2 * n, 2 * n, J)
     assert plan.unit_weights
-    taps_u, _ = pg.kernel_taps("kb", J, plan.frac[:, 0], precision="fp64")
-    taps_v, _ = pg.kernel_taps("kb", J, plan.frac[:, 1], precision="fp64")
+    taps_u, taps_v = block_taps(plan)
     op = oracle_mod.Operator(u, v, None, None, n, n, 2.0, kernel="kb", Ju=J, Jv=J)
     grid = rng.standard_normal(4 * n * n) + 1j * rng.standard_normal(4 * n * n)
     assert rel_l2(replay_degrid(plan, taps_u, taps_v, grid), op.G_forward(grid)) < 1e-12
@@ -156,19 +181,24 @@ def test_plan_balances_dense_cells(pg):
     assert (p.slot_user >= 0).sum() == 5000
 
 
-def test_batch_lanes_are_bank_classes(pg):
+@pytest.mark.parametrize("group", [1, 2])
+def test_batch_lanes_are_bank_classes(pg, group):
     """Items sit on the lane of their bank class (window offset lp * stride +
     lq = lane, mod 16) wherever that lane was free, so half-warps mostly touch
     distinct shared-memory bank pairs at each tap offset; the stride is the
     widest window.  A batch holds at most 4 items of a class, spread over the
     two half-warps, and its items of the leading count at most 2, so a
-    half-warp's lane-block access mostly costs one or two wavefronts."""
+    half-warp's lane-block access mostly costs one or two wavefronts.  With
+    2 x 2 cell groups the anchors sit on even rows and columns; the window's
+    extra cell per two rows keeps their offsets on all 16 classes."""
     from purify_gb300 import synthetic
     u, v = synthetic.mixed_uv(200_000, 512, 512, 0.7, 0.15, seed=3)
-    p = pg.CoveragePlan(u, v, 512, 512, 6)
+    p = pg.CoveragePlan(u, v, 512, 512, 6, group=group)
     lc = p.lane_code
     lp, lq, cnt = lc & 0xFF, (lc >> 8) & 0xFF, lc >> 16
-    r = (lp * p.win_cols + lq) & 15
+    # window offset of the item's anchor (one extra cell per two rows with
+    # 2 x 2 groups, whose anchors sit on even rows and columns)
+    r = (lp * p.win_stride + lq + (lp >> 1) * (group - 1)) & 15
     lane = np.arange(32)[None, :] & 15
     valid = cnt > 0
     on_class = ((r == lane) & valid).sum() / valid.sum()
