@@ -810,6 +810,23 @@ std::unique_ptr<Batch> Batch::create(const BatchConfig &cfg) {
     throw Error(kInvalidArgument, "cell_group must be 1 or 2");
   if (cfg.cell_group == 2 && (cfg.fp64 || cfg.J > kMaxGroupJ))
     throw Error(kUnsupported, "2 x 2 work items need complex<float> and J <= 6");
+  {
+    // Kernels with sub-segmented taps run without a weight stream (the
+    // single operator applies such weights in separate passes, which the
+    // grouped launches do not have).
+    const GriddingKernel kern(cfg.kernel, cfg.J, cfg.oversample_ratio);
+    const bool sub = fit_axis(kern, cfg.J, cfg.fp64 ? kCoefF64 : kCoefF32).nsub > 1;
+    for (size_t c = 0; sub && c < cfg.channels.size(); ++c) {
+      const ChannelSpec &ch = cfg.channels[c];
+      if (!ch.weights) continue;
+      for (int64_t m = 0; m < ch.M; ++m)
+        if (ch.weights[m] != std::complex<double>(1.0, 0.0))
+          throw Error(kUnsupported, "channel " + std::to_string(c) +
+                                        ": weights with a sub-segmented kernel fit (this kernel "
+                                        "and support) are not supported in a batch; use single "
+                                        "operators");
+    }
+  }
   for (size_t c = 0; c < cfg.channels.size(); ++c) {
     const ChannelSpec &s = cfg.channels[c];
     if (s.imsizex <= 0 || s.imsizey <= 0)

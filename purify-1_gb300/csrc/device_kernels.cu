@@ -213,6 +213,18 @@ __global__ void cmul_scale_kernel(cplx<real> *__restrict__ a, const cplx<real> *
     a[k] = cplx<real>{scale * (x.x * y.x - x.y * y.y), scale * (x.x * y.y + x.y * y.x)};
   }
 }
+// a <- a * b or a * conj(b) (complex, element-wise).
+template <typename real, bool CONJ>
+__global__ void cmul_kernel(cplx<real> *__restrict__ a, const cplx<real> *__restrict__ b,
+                            int64_t n) {
+  for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n;
+       k += int64_t(gridDim.x) * blockDim.x) {
+    const cplx<real> x = a[k], y = b[k];
+    const real yi = CONJ ? -y.y : y.y;
+    a[k] = cplx<real>{x.x * y.x - x.y * yi, x.x * yi + x.y * y.x};
+  }
+}
+
 // x <- 0, x[index] <- 1.
 template <typename real>
 __global__ void delta_kernel(cplx<real> *x, int64_t n, int64_t index) {
@@ -345,6 +357,17 @@ cudaError_t launch_cmul_scale(void *a, const void *b, int64_t n, double scale, c
   return cudaGetLastError();
 }
 template <typename real>
+cudaError_t launch_cmul(void *a, const void *b, int64_t n, bool conj_b, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  auto *pa = static_cast<cplx<real> *>(a);
+  auto *pb = static_cast<const cplx<real> *>(b);
+  if (conj_b)
+    cmul_kernel<real, true><<<stream_blocks(n, 256), 256, 0, s>>>(pa, pb, n);
+  else
+    cmul_kernel<real, false><<<stream_blocks(n, 256), 256, 0, s>>>(pa, pb, n);
+  return cudaGetLastError();
+}
+template <typename real>
 cudaError_t launch_delta(void *x, int64_t n, int64_t index, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   delta_kernel<real><<<stream_blocks(n, 256), 256, 0, s>>>(static_cast<cplx<real> *>(x), n, index);
@@ -387,7 +410,8 @@ cudaError_t launch_fill(void *x, int64_t n, double value, cudaStream_t s) {
   template cudaError_t launch_fill<real>(void *, int64_t, double, cudaStream_t);                 \
   template cudaError_t launch_scale_rsqrt<real>(void *, int64_t, const double *, cudaStream_t);   \
   template cudaError_t launch_cmul_scale<real>(void *, const void *, int64_t, double, cudaStream_t); \
-  template cudaError_t launch_delta<real>(void *, int64_t, int64_t, cudaStream_t);
+  template cudaError_t launch_delta<real>(void *, int64_t, int64_t, cudaStream_t);              \
+  template cudaError_t launch_cmul<real>(void *, const void *, int64_t, bool, cudaStream_t);
 
 PG_INSTANTIATE(float)
 PG_INSTANTIATE(double)

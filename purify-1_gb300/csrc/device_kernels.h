@@ -184,6 +184,9 @@ cudaError_t launch_scale_rsqrt(void *x, int64_t n, const double *sq, cudaStream_
 // a <- a * b * scale, complex element-wise.
 template <typename real>
 cudaError_t launch_cmul_scale(void *a, const void *b, int64_t n, double scale, cudaStream_t s);
+// a <- a * b, or a * conj(b) with conj_b, complex element-wise.
+template <typename real>
+cudaError_t launch_cmul(void *a, const void *b, int64_t n, bool conj_b, cudaStream_t s);
 // x <- the unit vector e_index.
 template <typename real>
 cudaError_t launch_delta(void *x, int64_t n, int64_t index, cudaStream_t s);

@@ -243,7 +243,10 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
   const C *weight = static_cast<const C *>(a.weight);
   const int32_t *user = a.slot_user;
   C *out = static_cast<C *>(a.slot_out);
-  const bool unit = weight == nullptr;
+  // Kernels with sub-segmented taps have no weight stream: operators that
+  // need both apply their weights in separate element-wise passes (the host
+  // never passes a weight stream to these instantiations).
+  const bool unit = SUB || weight == nullptr;
   if (warp >= nbt) return;
   unsigned char *stg = smem_raw + a0.win_bytes + kHeaderBytes + size_t(warp) * a0.stage_bytes;
   C *st_t = reinterpret_cast<C *>(stg);
@@ -353,7 +356,7 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
   const C *frac = static_cast<const C *>(a.frac);
   const C *weight = static_cast<const C *>(a.weight);
   const C *vin = static_cast<const C *>(a.slot_in);
-  const bool unit = weight == nullptr;
+  const bool unit = SUB || weight == nullptr;  // see degrid_kernel
   if (warp < nbt) {
     // Two cursors over this warp's (batch, k) steps, slot = hdr[lb].x +
     // 32 k + lane: the compute cursor and, two steps ahead of it, the
@@ -583,6 +586,8 @@ cudaError_t launch_apply(bool degrid, const ApplyArgs<real> &a, const PolyTable<
                          int J, int ntasks, size_t smem, int threads, cudaStream_t s) {
   if (ntasks == 0) return cudaSuccess;
   const bool sub = poly.nsub_u > 1 || poly.nsub_v > 1;
+  // sub-segmented instantiations carry no weight stream (see degrid_kernel)
+  if (sub && a.weight) return cudaErrorInvalidValue;
 #define PG_CASE(JJ, GG)                                                                  \
   case JJ:                                                                               \
     return sub ? launch_one<real, JJ, GG, true, GROUP>(degrid, a, poly, ntasks, smem, threads, s) \

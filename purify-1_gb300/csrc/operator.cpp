@@ -126,6 +126,12 @@ class OperatorT final : public Operator {
   void init_w(const OperatorConfig &cfg, int64_t &bytes, AxisTiling &tu, AxisTiling &tv,
               std::vector<int32_t> &tile_tasks);
   bool unit_weights_ = true;
+  // Weights with sub-segmented taps: the gridding kernels run without a
+  // weight stream (the phase sign rides in t_u as for unit weights) and the
+  // weights are applied by element-wise passes: caller order after G, slot
+  // order (conjugated) before G^H.
+  bool split_weights_ = false;
+  DeviceBuffer wcaller_;  // caller-ordered weights of split_weights_
   bool fused_forward_ = true, fused_adjoint_ = false;
   // The adjoint's gather keeps the caller-ordered visibilities in L2
   // (evict-last) when they fit in kKeepVisL2Bytes: in a forward / adjoint
@@ -236,6 +242,8 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
     init_w(cfg, bytes, tu, tv, tile_tasks);
   else
     init_plain(cfg, bytes, tu, tv, tile_tasks);
+  // split weights are applied to the slot-ordered buffer before G^H
+  if (split_weights_) fused_adjoint_ = false;
   ntu_ = tu.n;
   ntv_ = tv.n;
   slot_stride_ = int64_t(win_rows_) * win_cols_;
@@ -348,25 +356,17 @@ void OperatorT<real>::init_plain(const OperatorConfig &cfg, int64_t &bytes, Axis
   rq.Jv = cfg.Jv;
   rq.tile = cfg.tile > 0 ? cfg.tile : kTile;
   rq.max_per_item = cfg.max_per_item > 0 ? cfg.max_per_item : 16;
-  // Work items of 2 x 2 base cells: measured faster on the 10^7-visibility
-  // workload, where a third of the occupied cells hold one visibility and a
-  // J x J block flushed per cell dominated G^H.  The (J + 1)^2 block fits
-  // the registers for complex<float> up to kMaxGroupJ; when the tiling is
-  // too narrow for it the plan falls back to single cells.
-  const bool group_ok = sizeof(real) == 4 && cfg.Ju <= kMaxGroupJ;
-  rq.group = cfg.cell_group == 0 ? (group_ok ? 2 : 1) : cfg.cell_group;
+  // Work items of single base cells by default: 2 x 2 groups (a (J + 1)^2
+  // block, complex<float> up to kMaxGroupJ) flush fewer blocks but spend
+  // more FMAs and registers per visibility, and measured slower on the
+  // 10^7-visibility workload (G^H 224 against 172 us, G 160 against 139).
+  rq.group = cfg.cell_group == 0 ? 1 : cfg.cell_group;
   rq.class_cap = cfg.class_cap;
   Plan plan;
   try {
     plan = build_plan(rq);
   } catch (const std::invalid_argument &e) {
-    if (cfg.cell_group != 0 || rq.group == 1) throw Error(kInvalidArgument, e.what());
-    rq.group = 1;
-    try {
-      plan = build_plan(rq);
-    } catch (const std::invalid_argument &e2) {
-      throw Error(kInvalidArgument, e2.what());
-    }
+    throw Error(kInvalidArgument, e.what());
   }
   group_ = plan.group;
   ntasks_ = int(plan.tasks.size());
@@ -376,6 +376,7 @@ void OperatorT<real>::init_plain(const OperatorConfig &cfg, int64_t &bytes, Axis
   fold_J_ = J_ + group_ - 1;  // task windows reach JB - 1 cells into the next tiles
   S_ = plan.S;
   unit_weights_ = plan.unit_weights;
+  split_weights_ = !unit_weights_ && (poly_.nsub_u > 1 || poly_.nsub_v > 1);
   nnz_ = M_ * int64_t(cfg.Ju) * cfg.Jv;
   occupied_ = plan.occupied_cells;
   work_items_ = int64_t(plan.lane_code.size());
@@ -383,17 +384,30 @@ void OperatorT<real>::init_plain(const OperatorConfig &cfg, int64_t &bytes, Axis
   for (int64_t i = 0; i < S_; ++i) {
     // unit weights: the phase sign (-1)^(k_u + k_v) rides in the sign of t_u
     const real tu = fraction_in_cell<real>(plan.frac_u[i]);
-    fr[i] = C((unit_weights_ && plan.flip[i]) ? -tu : tu, fraction_in_cell<real>(plan.frac_v[i]));
+    const bool sign_in_t = unit_weights_ || split_weights_;
+    fr[i] = C((sign_in_t && plan.flip[i]) ? -tu : tu, fraction_in_cell<real>(plan.frac_v[i]));
   }
   frac_.alloc(sizeof(C) * S_, &bytes);
   frac_.upload(fr.data(), sizeof(C) * S_, stream_);
   std::vector<C> wt;
   if (!unit_weights_) {
     wt.resize(S_);
-    for (int64_t i = 0; i < S_; ++i)
-      wt[i] = C(real(plan.weight[i].real()), real(plan.weight[i].imag()));
+    for (int64_t i = 0; i < S_; ++i) {
+      // split weights: the sign is in t_u, so the stream holds the weight itself
+      const std::complex<double> w = (split_weights_ && plan.flip[i]) ? -plan.weight[i]
+                                                                      : plan.weight[i];
+      wt[i] = C(real(w.real()), real(w.imag()));
+    }
     weight_.alloc(sizeof(C) * S_, &bytes);
     weight_.upload(wt.data(), sizeof(C) * S_, stream_);
+  }
+  std::vector<C> wc;
+  if (split_weights_) {
+    const auto *w = reinterpret_cast<const std::complex<double> *>(cfg.weights);
+    wc.resize(M_);
+    for (int64_t m = 0; m < M_; ++m) wc[m] = C(real(w[m].real()), real(w[m].imag()));
+    wcaller_.alloc(sizeof(C) * std::max<int64_t>(M_, 1), &bytes);
+    wcaller_.upload(wc.data(), sizeof(C) * M_, stream_);
   }
   slot_user_.alloc(sizeof(int32_t) * S_, &bytes);
   slot_user_.upload(plan.slot_user.data(), sizeof(int32_t) * S_, stream_);
@@ -583,7 +597,7 @@ void OperatorT<real>::degrid_slots(const void *grid, void *caller_vis) {
   a.batches = batches_.as<int2>();
   a.lane_code = lane_code_.as<int32_t>();
   a.frac = frac_.get();
-  a.weight = unit_weights_ ? nullptr : weight_.get();
+  a.weight = (unit_weights_ || split_weights_) ? nullptr : weight_.get();
   a.slot_out = caller_vis ? caller_vis : ws_->slots;
   a.slot_user = caller_vis ? slot_user_.as<int32_t>() : nullptr;
   a.Nu = Nu_;
@@ -594,11 +608,19 @@ void OperatorT<real>::degrid_slots(const void *grid, void *caller_vis) {
   mark_begin(kDegrid);
   cuda_check(launch_degrid<real>(a, poly_, J_, ntasks_, win_rows_, win_cols_, shape_, ws_->stream),
              "degrid");
+  if (split_weights_) {
+    if (caller_vis)
+      cuda_check(launch_cmul<real>(caller_vis, wcaller_.get(), M_, false, ws_->stream), "weights");
+    else
+      cuda_check(launch_cmul<real>(ws_->slots, weight_.get(), S_, false, ws_->stream), "weights");
+  }
   mark_end(kDegrid);
 }
 
 template <typename real>
 void OperatorT<real>::grid_slots(void *grid, const void *caller_vis) {
+  if (split_weights_ && !caller_vis)
+    cuda_check(launch_cmul<real>(ws_->slots, weight_.get(), S_, true, ws_->stream), "weights");
   grid_core(grid, caller_vis ? caller_vis : ws_->slots,
             caller_vis ? slot_user_.as<int32_t>() : nullptr, ws_->tilebuf);
 }
@@ -638,7 +660,7 @@ void OperatorT<real>::grid_core(void *grid, const void *vis, const int32_t *slot
   a.batches = batches_.as<int2>();
   a.lane_code = lane_code_.as<int32_t>();
   a.frac = frac_.get();
-  a.weight = unit_weights_ ? nullptr : weight_.get();
+  a.weight = (unit_weights_ || split_weights_) ? nullptr : weight_.get();
   a.slot_in = vis;
   a.slot_user = slot_user;
   a.Nu = Nu_;
@@ -902,6 +924,8 @@ void OperatorT<real>::grid_no_alloc(const void *vis, void *grid, cudaStream_t us
   // every cell of every task window, so nothing left in the array from an
   // earlier call is read.
   cuda_check(launch_expand<real>(vis, slot_user_.as<int32_t>(), slots, S_, stream_), "expand");
+  if (split_weights_)
+    cuda_check(launch_cmul<real>(slots, weight_.get(), S_, true, stream_), "weights");
   grid_core(grid, slots, nullptr, windows);
   release(user);
 }

@@ -216,3 +216,10 @@ def test_batch_errors(pg, cuda):
         pg.Batch([], J=4)
     with pytest.raises(pg.PurifyError):
         pg.Batch([dict(u=np.zeros(3), v=np.zeros(3), imsizey=0, imsizex=8)], J=4, tuning=TUNING)
+    # weights with a sub-segmented tap fit (KB J = 2) have no grouped form
+    rng = np.random.default_rng(0)
+    w = dict(u=rng.normal(0, 5, 50), v=rng.normal(0, 5, 50), imsizey=16, imsizex=16,
+             weights=rng.standard_normal(50) + 1j * rng.standard_normal(50))
+    with pytest.raises(pg.PurifyError) as e:
+        pg.Batch([w], J=2, precision="fp32", tuning=TUNING)
+    assert e.value.status == 2 and "sub-segmented" in str(e.value)

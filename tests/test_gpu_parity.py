@@ -366,11 +366,56 @@ def test_work_item_shapes(pg, oracle_mod, cuda, kernel, J, group):
     assert rel_l2(to_np(a1), oop.adjoint(yy)) < TOL["fp32"]
 
 
-def test_default_work_items_are_grouped_for_fp32(pg, cuda):
-    """The default plan groups 2 x 2 base cells for complex<float> with
-    J <= 6 and keeps single cells for J > 6 and for complex<double>."""
+def test_work_item_shape_requests(pg, cuda):
+    """Single base cells by default; 2 x 2 groups on request for complex<float>
+    with J <= 6, refused (UNSUPPORTED) for complex<double> and J > 6."""
     u = np.zeros(10)
-    for prec, J, want in (("fp32", 6, 2), ("fp32", 7, 1), ("fp64", 4, 1)):
+    for prec, J in (("fp32", 6), ("fp32", 8), ("fp64", 4)):
         op = pg.MeasurementOperator(u, u, None, None, 32, 32, 2.0, power_iters=0, kernel="kb",
                                     Ju=J, Jv=J, precision=prec)
-        assert op.info()["cell_group"] == want, (prec, J)
+        assert op.info()["cell_group"] == 1
+    op = pg.MeasurementOperator(u, u, None, None, 32, 32, 2.0, power_iters=0, kernel="kb", Ju=6,
+                                Jv=6, precision="fp32", tuning={"cell_group": 2})
+    assert op.info()["cell_group"] == 2
+    for prec, J in (("fp32", 7), ("fp64", 4)):
+        with pytest.raises(pg.PurifyError) as e:
+            pg.MeasurementOperator(u, u, None, None, 32, 32, 2.0, power_iters=0, kernel="kb",
+                                   Ju=J, Jv=J, precision=prec, tuning={"cell_group": 2})
+        assert e.value.status == 2
+
+
+@pytest.mark.parametrize("kernel,J", [("kb", 1), ("kb", 2), ("gauss", 2), ("pswf", 6)])
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_weights_with_sub_segmented_taps(pg, oracle_mod, cuda, kernel, J, precision):
+    """Kernels whose tap fit has sub-segments (narrow supports, the PSWF)
+    run without a weight stream; their operators apply complex weights in
+    element-wise passes (caller order after G, slot order before G^H).
+    Every path is checked against the oracle: forward and adjoint through
+    caller order, the normal operator and the power method through slot
+    order, and the allocation-free G^H against the ordinary one."""
+    torch = cuda
+    rng = np.random.default_rng(J + (0 if precision == "fp32" else 100))
+    M, n = 5000, 40
+    u = rng.normal(0, 15, M)
+    v = rng.normal(0, 15, M)
+    wt = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    gop, oop = make_pair(pg, oracle_mod, u, v, n, n, kernel, J, wt, precision)
+    x = rng.standard_normal(n * n) + 1j * rng.standard_normal(n * n)
+    y = to_np(gop.forward(to_dev(torch, x, precision)))
+    assert rel_l2(y, oop.forward(x)) < TOL[precision]
+    yy = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    xx = to_np(gop.adjoint(to_dev(torch, yy, precision)))
+    assert rel_l2(xx, oop.adjoint(yy)) < TOL[precision]
+    nx = to_np(gop.normal(to_dev(torch, x, precision)))
+    assert rel_l2(nx, oop.adjoint(oop.forward(x))) < TOL[precision]
+    n_gpu, n_ref = gop.power_method(20, 0.0), oop.power_method(20, 0.0)
+    assert abs(n_gpu - n_ref) / n_ref < TOL[precision]
+    cells = 4 * n * n
+    yd = to_dev(torch, yy, precision)
+    g1 = torch.empty(cells, dtype=gop.complex_dtype, device="cuda")
+    g2 = torch.empty(cells, dtype=gop.complex_dtype, device="cuda")
+    gop.grid_into(yd, g1)
+    gop.grid_no_alloc_into(yd, g2)
+    torch.cuda.synchronize()
+    assert torch.equal(g1, g2)
+    assert rel_l2(to_np(g1), oop.G_adjoint(yy)) < TOL[precision]
