@@ -74,7 +74,8 @@ class BatchT final : public Batch {
     Arena mem;                   // coverage state and scratch of this channel
     size_t o_frac = 0, o_weight = 0, o_slot_user = 0, o_user_slot = 0, o_batches = 0,
            o_lane = 0, o_tile_tasks = 0, o_tu_start = 0, o_tv_start = 0, o_tu_of = 0,
-           o_tv_of = 0, o_su = 0, o_sv = 0, o_tilebuf = 0, o_slots = 0, o_pm_x = 0, o_pm_vis = 0;
+           o_tv_of = 0, o_su = 0, o_sv = 0, o_tilebuf = 0, o_slots = 0, o_pm_x = 0, o_pm_vis = 0,
+           o_wvis = 0;
   };
   struct SizeGroup {
     int Nu = 0, Nv = 0;
@@ -109,13 +110,14 @@ class BatchT final : public Batch {
   std::unique_ptr<Chan[]> chans_;
   std::vector<SizeGroup> groups_;
   int ntasks_ = 0, win_rows_ = 0, win_cols_ = 0;
-  bool any_weight_ = false;  // some channel has a weight stream
   Arena shared_;  // grouped task list, argument tables, padded and FFT grids
   size_t o_tasks_ = 0, o_task_base_ = 0, o_fwd_ = 0, o_adj_ = 0, o_folds_ = 0, o_io_ = 0,
          o_partial_ = 0, o_sq_ = 0, o_inv_ = 0, o_map_pix_ = 0, o_map_slot_ = 0, o_map_tile_ = 0,
+         o_map_wvis_ = 0,
          o_order_ = 0;
   // block maps of the grouped element-wise launches: {channel, block}
   std::vector<int2> map_pix_, map_slot_, map_tile_;
+  std::vector<int2> map_wvis_;  // caller-ordered visibilities of the channels with weights
   std::vector<ApplyArgs<real>> fwd_, adj_;
   std::vector<FoldArgs> folds_;
   std::vector<ChannelIO<real>> io_;
@@ -199,7 +201,6 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     }
     ch.S = plan.S;
     ch.unit = plan.unit_weights;
-    if (!ch.unit) any_weight_ = true;
     ch.ntasks = int(plan.tasks.size());
     ch.ntu = plan.tu.n;
     ch.ntv = plan.tv.n;
@@ -218,6 +219,7 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     Arena &m = ch.mem;
     ch.o_frac = m.reserve(sizeof(C) * ch.S);
     ch.o_weight = ch.unit ? 0 : m.reserve(sizeof(C) * ch.S);
+    ch.o_wvis = ch.unit ? 0 : m.reserve(sizeof(C) * ch.M);
     ch.o_slot_user = m.reserve(sizeof(int32_t) * ch.S);
     ch.o_user_slot = m.reserve(sizeof(int32_t) * ch.M);
     ch.o_batches = m.reserve(sizeof(int2) * nb);
@@ -236,9 +238,9 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     m.allocate(&info_.device_bytes);
     std::vector<C> fr(ch.S);
     for (int64_t i = 0; i < ch.S; ++i) {
-      // unit weights: the phase sign (-1)^(k_u + k_v) rides in the sign of t_u
+      // the phase sign (-1)^(k_u + k_v) rides in the sign of t_u
       const real tu = fraction_in_cell<real>(plan.frac_u[i]);
-      fr[i] = C((ch.unit && plan.flip[i]) ? -tu : tu, fraction_in_cell<real>(plan.frac_v[i]));
+      fr[i] = C(plan.flip[i] ? -tu : tu, fraction_in_cell<real>(plan.frac_v[i]));
     }
     auto put = [&](size_t off, const void *src, size_t bytes) {
       if (bytes)
@@ -247,11 +249,20 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     };
     put(ch.o_frac, fr.data(), sizeof(C) * ch.S);
     std::vector<C> wt;
+    std::vector<C> wv;
     if (!ch.unit) {
+      // the weights themselves (the plan folds the phase sign into them; it
+      // rides in t_u here), in slot order for G^H and caller order for G
       wt.resize(ch.S);
-      for (int64_t i = 0; i < ch.S; ++i)
-        wt[i] = C(real(plan.weight[i].real()), real(plan.weight[i].imag()));
+      for (int64_t i = 0; i < ch.S; ++i) {
+        const std::complex<double> w = plan.flip[i] ? -plan.weight[i] : plan.weight[i];
+        wt[i] = C(real(w.real()), real(w.imag()));
+      }
       put(ch.o_weight, wt.data(), sizeof(C) * ch.S);
+      wv.resize(ch.M);
+      for (int64_t k = 0; k < ch.M; ++k)
+        wv[k] = C(real(spec.weights[k].real()), real(spec.weights[k].imag()));
+      put(ch.o_wvis, wv.data(), sizeof(C) * ch.M);
     }
     put(ch.o_slot_user, plan.slot_user.data(), sizeof(int32_t) * ch.S);
     put(ch.o_user_slot, plan.user_slot.data(), sizeof(int32_t) * ch.M);
@@ -306,10 +317,14 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     const int64_t nsl = (ch.S + kGroupSlots - 1) / kGroupSlots;
     for (int64_t k = 0; k < nsl; ++k) map_slot_.push_back(int2{c, int(k)});
     for (int k = 0; k < ch.ntu * ch.ntv; ++k) map_tile_.push_back(int2{c, k});
+    if (!ch.unit)
+      for (int64_t k = 0; k < (ch.M + kGroupSlots - 1) / kGroupSlots; ++k)
+        map_wvis_.push_back(int2{c, int(k)});
   }
   o_map_pix_ = shared_.reserve(sizeof(int2) * map_pix_.size());
   o_map_slot_ = shared_.reserve(sizeof(int2) * map_slot_.size());
   o_map_tile_ = shared_.reserve(sizeof(int2) * map_tile_.size());
+  o_map_wvis_ = shared_.reserve(sizeof(int2) * map_wvis_.size());
   o_order_ = shared_.reserve(sizeof(int32_t) * order.size());
   o_tasks_ = shared_.reserve(sizeof(Task) * tasks.size());
   o_task_base_ = shared_.reserve(sizeof(int32_t) * nch_);
@@ -337,7 +352,7 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
                              sizeof(int32_t) * nch_, cudaMemcpyHostToDevice, stream_),
              "upload");
   for (auto m : {std::make_pair(&map_pix_, o_map_pix_), std::make_pair(&map_slot_, o_map_slot_),
-                 std::make_pair(&map_tile_, o_map_tile_)})
+                 std::make_pair(&map_tile_, o_map_tile_), std::make_pair(&map_wvis_, o_map_wvis_)})
     if (!m.first->empty())
       cuda_check(cudaMemcpyAsync(shared_.at<char>(m.second), m.first->data(),
                                  sizeof(int2) * m.first->size(), cudaMemcpyHostToDevice, stream_),
@@ -366,7 +381,6 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     a.batches = m.at<int2>(ch.o_batches);
     a.lane_code = m.at<int32_t>(ch.o_lane);
     a.frac = m.at<char>(ch.o_frac);
-    a.weight = ch.unit ? nullptr : m.at<char>(ch.o_weight);
     a.Nu = ch.Nu;
     a.Nv = ch.Nv;
     a.win_stride = ch.win_stride;
@@ -402,6 +416,8 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     io.slots = m.at<char>(ch.o_slots);
     io.slot_user = m.at<int32_t>(ch.o_slot_user);
     io.user_slot = m.at<int32_t>(ch.o_user_slot);
+    io.w_slot = ch.unit ? nullptr : m.at<char>(ch.o_weight);
+    io.w_vis = ch.unit ? nullptr : m.at<char>(ch.o_wvis);
     io.Nx = ch.Nx;
     io.Ny = ch.Ny;
     io.Nu = ch.Nu;
@@ -500,9 +516,9 @@ void BatchT<real>::record(int mode) {
     const bool dg = mode == kDegridOnly;
     head.group = shared_.at<ApplyArgs<real>>(dg ? o_fwd_ : o_adj_);
     cuda_check(dg ? launch_degrid_group<real>(head, poly_, J_, ntasks_, win_rows_, win_cols_,
-                                              degrid_shape_, true, any_weight_, stream_)
+                                              degrid_shape_, true, stream_)
                   : launch_grid_group<real>(head, poly_, J_, ntasks_, win_rows_, win_cols_,
-                                            grid_shape_, false, any_weight_, stream_),
+                                            grid_shape_, false, stream_),
                dg ? "degrid" : "grid");
     return;
   }
@@ -516,8 +532,11 @@ void BatchT<real>::record(int mode) {
                   "cufftExec");
     head.group = shared_.at<ApplyArgs<real>>(o_fwd_);
     cuda_check(launch_degrid_group<real>(head, poly_, J_, ntasks_, win_rows_, win_cols_,
-                                         degrid_shape_, true, any_weight_, stream_),
+                                         degrid_shape_, true, stream_),
                "degrid");
+    cuda_check(launch_weigh_vis_group<real>(io, shared_.at<int2>(o_map_wvis_),
+                                            int(map_wvis_.size()), stream_),
+               "weights");
   }
   if (mode & kAdjoint) {
     cuda_check(launch_expand_group<real>(io, shared_.at<int2>(o_map_slot_), int(map_slot_.size()),
@@ -525,7 +544,7 @@ void BatchT<real>::record(int mode) {
                "expand");
     head.group = shared_.at<ApplyArgs<real>>(o_adj_);
     cuda_check(launch_grid_group<real>(head, poly_, J_, ntasks_, win_rows_, win_cols_,
-                                       grid_shape_, false, any_weight_, stream_),
+                                       grid_shape_, false, stream_),
                "grid");
     cuda_check(launch_fold_group<real>(shared_.at<FoldArgs>(o_folds_), shared_.at<int2>(o_map_tile_),
                                        int(map_tile_.size()), stream_),
@@ -810,23 +829,6 @@ std::unique_ptr<Batch> Batch::create(const BatchConfig &cfg) {
     throw Error(kInvalidArgument, "cell_group must be 1 or 2");
   if (cfg.cell_group == 2 && (cfg.fp64 || cfg.J > kMaxGroupJ))
     throw Error(kUnsupported, "2 x 2 work items need complex<float> and J <= 6");
-  {
-    // Kernels with sub-segmented taps run without a weight stream (the
-    // single operator applies such weights in separate passes, which the
-    // grouped launches do not have).
-    const GriddingKernel kern(cfg.kernel, cfg.J, cfg.oversample_ratio);
-    const bool sub = fit_axis(kern, cfg.J, cfg.fp64 ? kCoefF64 : kCoefF32).nsub > 1;
-    for (size_t c = 0; sub && c < cfg.channels.size(); ++c) {
-      const ChannelSpec &ch = cfg.channels[c];
-      if (!ch.weights) continue;
-      for (int64_t m = 0; m < ch.M; ++m)
-        if (ch.weights[m] != std::complex<double>(1.0, 0.0))
-          throw Error(kUnsupported, "channel " + std::to_string(c) +
-                                        ": weights with a sub-segmented kernel fit (this kernel "
-                                        "and support) are not supported in a batch; use single "
-                                        "operators");
-    }
-  }
   for (size_t c = 0; c < cfg.channels.size(); ++c) {
     const ChannelSpec &s = cfg.channels[c];
     if (s.imsizex <= 0 || s.imsizey <= 0)
@@ -891,10 +893,12 @@ BatchTuning autotune_batch(const BatchConfig &cfg) {
     for (int threads : {64, 128, 256}) {
       LaunchShape shape;
       shape.threads = threads;
-      const bool degrid_fits = degrid_smem_bytes(prec, cfg.J, bi.win_rows, bi.win_cols, shape,
-                                                 true, true, group) <= size_t(optin);
-      const bool grid_fits = grid_smem_bytes(prec, cfg.J, bi.win_rows, bi.win_cols, shape,
-                                             false, true, group) <= size_t(optin);
+      const bool degrid_fits =
+          degrid_smem_bytes(prec, cfg.J, bi.win_rows, bi.win_cols, shape, true, group) <=
+          size_t(optin);
+      const bool grid_fits =
+          grid_smem_bytes(prec, cfg.J, bi.win_rows, bi.win_cols, shape, false, group) <=
+          size_t(optin);
       if (!degrid_fits || !grid_fits) continue;
       b->set_launch_shapes(threads, threads);
       const double f = b->time_apply(1, 5), a = b->time_apply(2, 5);

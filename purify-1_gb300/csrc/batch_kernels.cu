@@ -64,9 +64,38 @@ __global__ void expand_group_kernel(const ChannelIO<real> *__restrict__ chans,
   for (int r = 0; r < 4; ++r) m[r] = s0 + r * 256 < c.S ? __ldcs(c.slot_user + s0 + r * 256) : -1;
 #pragma unroll
   for (int r = 0; r < 4; ++r) v[r] = m[r] >= 0 ? in[m[r]] : cplx<real>{0, 0};
+  if (c.w_slot) {
+    // conj(w) v: G^H holds the conjugated entries of G
+    const cplx<real> *w = static_cast<const cplx<real> *>(c.w_slot);
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+      if (s0 + r * 256 < c.S) {
+        const cplx<real> a = __ldcs(w + s0 + r * 256);
+        v[r] = cplx<real>{a.x * v[r].x + a.y * v[r].y, a.x * v[r].y - a.y * v[r].x};
+      }
+  }
 #pragma unroll
   for (int r = 0; r < 4; ++r)
     if (s0 + r * 256 < c.S) slots[s0 + r * 256] = v[r];
+}
+// vis_out[m] <- vis_out[m] w_vis[m]: a block covers 4 * 256 consecutive
+// caller-ordered visibilities of a channel with weights.
+template <typename real>
+__global__ void weigh_vis_group_kernel(const ChannelIO<real> *__restrict__ chans,
+                                       const int2 *__restrict__ map) {
+  const int2 mm = map[blockIdx.x];
+  const ChannelIO<real> &c = chans[mm.x];
+  cplx<real> *vis = static_cast<cplx<real> *>(c.vis_out);
+  const cplx<real> *w = static_cast<const cplx<real> *>(c.w_vis);
+  const int64_t m0 = int64_t(mm.y) * kGroupSlots + threadIdx.x;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int64_t m = m0 + r * 256;
+    if (m < c.M) {
+      const cplx<real> a = vis[m], b = __ldcs(w + m);
+      vis[m] = cplx<real>{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+    }
+  }
 }
 
 // Per-channel FP64 |x|^2 of the adjoint output, with the same fixed
@@ -126,20 +155,19 @@ __global__ void scale_group_kernel(const ChannelIO<real> *__restrict__ chans,
 template <typename real>
 cudaError_t launch_degrid_group(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
                                 int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
-                                bool user, bool weight, cudaStream_t s) {
+                                bool user, cudaStream_t s) {
   const size_t smem =
-      degrid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, weight, a.group_cells);
+      degrid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, a.group_cells);
   ApplyArgs<real> b = a;
   b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, false, a.group_cells));
-  b.stage_bytes = int(stage_bytes(sizeof(real), J, user, weight));
+  b.stage_bytes = int(stage_bytes(sizeof(real), J, user));
   return launch_apply<real, true>(true, b, poly, J, ntasks, smem, shape.threads, s);
 }
 template <typename real>
 cudaError_t launch_grid_group(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
                               int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
-                              bool user, bool weight, cudaStream_t s) {
-  const size_t smem =
-      grid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, weight, a.group_cells);
+                              bool user, cudaStream_t s) {
+  const size_t smem = grid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, a.group_cells);
   ApplyArgs<real> b = a;
   b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, true, a.group_cells));
   return launch_apply<real, true>(false, b, poly, J, ntasks, smem, shape.threads, s);
@@ -173,6 +201,13 @@ cudaError_t launch_expand_group(const ChannelIO<real> *chans, const int2 *map, i
   return cudaGetLastError();
 }
 template <typename real>
+cudaError_t launch_weigh_vis_group(const ChannelIO<real> *chans, const int2 *map, int nblocks,
+                                   cudaStream_t s) {
+  if (nblocks == 0) return cudaSuccess;
+  weigh_vis_group_kernel<real><<<nblocks, 256, 0, s>>>(chans, map);
+  return cudaGetLastError();
+}
+template <typename real>
 cudaError_t launch_sq_norm_group(const ChannelIO<real> *chans, int nch, double *partial,
                                  double *out, cudaStream_t s) {
   if (nch == 0) return cudaSuccess;
@@ -191,10 +226,10 @@ cudaError_t launch_scale_group(const ChannelIO<real> *chans, const int2 *map, in
 #define PG_INSTANTIATE_GROUP(real)                                                               \
   template cudaError_t launch_degrid_group<real>(const ApplyArgs<real> &, const PolyTable<real> &,  \
                                                  int, int, int, int, const LaunchShape &, bool,    \
-                                                 bool, cudaStream_t);                              \
+                                                 cudaStream_t);                                    \
   template cudaError_t launch_grid_group<real>(const ApplyArgs<real> &, const PolyTable<real> &,    \
                                                int, int, int, int, const LaunchShape &, bool,      \
-                                               bool, cudaStream_t);                                \
+                                               cudaStream_t);                                      \
   template cudaError_t launch_fold_group<real>(const FoldArgs *, const int2 *, int, cudaStream_t);  \
   template cudaError_t launch_pad_group<real>(const ChannelIO<real> *, const int2 *, int,          \
                                               cudaStream_t);                                       \
@@ -202,6 +237,8 @@ cudaError_t launch_scale_group(const ChannelIO<real> *chans, const int2 *map, in
                                                cudaStream_t);                                      \
   template cudaError_t launch_expand_group<real>(const ChannelIO<real> *, const int2 *, int,       \
                                                  cudaStream_t);                                    \
+  template cudaError_t launch_weigh_vis_group<real>(const ChannelIO<real> *, const int2 *, int,    \
+                                                    cudaStream_t);                                 \
   template cudaError_t launch_sq_norm_group<real>(const ChannelIO<real> *, int, double *, double *, \
                                                   cudaStream_t);                                   \
   template cudaError_t launch_scale_group<real>(const ChannelIO<real> *, const int2 *, int,        \

@@ -73,7 +73,8 @@ __device__ __forceinline__ double2 load_keep(const double2 *p, unsigned long lon
 template <typename real>
 __global__ void expand_kernel(const cplx<real> *__restrict__ in,
                               const int32_t *__restrict__ slot_user,
-                              cplx<real> *__restrict__ slots, int64_t S, bool keep) {
+                              cplx<real> *__restrict__ slots, int64_t S, bool keep,
+                              const cplx<real> *__restrict__ w) {
   const int64_t stride = int64_t(gridDim.x) * blockDim.x;
   const unsigned long long pol = l2_keep_policy();
   for (int64_t s0 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; s0 < S;
@@ -86,6 +87,15 @@ __global__ void expand_kernel(const cplx<real> *__restrict__ in,
 #pragma unroll
     for (int r = 0; r < kPermUnroll; ++r)
       v[r] = m[r] < 0 ? cplx<real>{0, 0} : keep ? load_keep(in + m[r], pol) : in[m[r]];
+    if (w) {
+      // conj(w) v: G^H holds the conjugated entries of G
+#pragma unroll
+      for (int r = 0; r < kPermUnroll; ++r)
+        if (s0 + r * stride < S) {
+          const cplx<real> c = __ldcs(w + s0 + r * stride);
+          v[r] = cplx<real>{c.x * v[r].x + c.y * v[r].y, c.x * v[r].y - c.y * v[r].x};
+        }
+    }
 #pragma unroll
     for (int r = 0; r < kPermUnroll; ++r)
       if (s0 + r * stride < S) __stcs(slots + s0 + r * stride, v[r]);
@@ -241,12 +251,12 @@ int stream_blocks(int64_t n, int threads) {
 }  // namespace
 
 size_t degrid_smem_bytes(int precision_bytes, int J, int win_rows, int win_cols,
-                         const LaunchShape &shape, bool user, bool weight, int group) {
+                         const LaunchShape &shape, bool user, int group) {
   return window_bytes(precision_bytes, win_rows, win_cols, shape, false, group) + kHeaderBytes +
-         size_t(shape.threads / 32) * stage_bytes(precision_bytes, J, user, weight);
+         size_t(shape.threads / 32) * stage_bytes(precision_bytes, J, user);
 }
 size_t grid_smem_bytes(int precision_bytes, int, int win_rows, int win_cols,
-                       const LaunchShape &shape, bool, bool, int group) {
+                       const LaunchShape &shape, bool, int group) {
   return window_bytes(precision_bytes, win_rows, win_cols, shape, true, group) + kHeaderBytes;
 }
 
@@ -254,21 +264,20 @@ template <typename real>
 cudaError_t launch_degrid(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
                           int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
                           cudaStream_t s) {
-  const bool user = a.slot_user != nullptr, weight = a.weight != nullptr;
+  const bool user = a.slot_user != nullptr;
   const size_t smem =
-      degrid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, weight, a.group_cells);
+      degrid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, a.group_cells);
   ApplyArgs<real> b = a;
   b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, false, a.group_cells));
-  b.stage_bytes = int(stage_bytes(sizeof(real), J, user, weight));
+  b.stage_bytes = int(stage_bytes(sizeof(real), J, user));
   return launch_apply<real, false>(true, b, poly, J, ntasks, smem, shape.threads, s);
 }
 template <typename real>
 cudaError_t launch_grid(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
                         int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
                         cudaStream_t s) {
-  const bool user = a.slot_user != nullptr, weight = a.weight != nullptr;
-  const size_t smem =
-      grid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, weight, a.group_cells);
+  const bool user = a.slot_user != nullptr;
+  const size_t smem = grid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, a.group_cells);
   ApplyArgs<real> b = a;
   b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, true, a.group_cells));
   return launch_apply<real, false>(false, b, poly, J, ntasks, smem, shape.threads, s);
@@ -311,11 +320,11 @@ cudaError_t launch_compact(const void *slots, const int32_t *user_slot, void *ou
 }
 template <typename real>
 cudaError_t launch_expand(const void *in, const int32_t *slot_user, void *slots, int64_t S,
-                          cudaStream_t s, bool keep_in) {
+                          cudaStream_t s, bool keep_in, const void *w) {
   if (S == 0) return cudaSuccess;
   expand_kernel<real><<<stream_blocks(S, 256), 256, 0, s>>>(
       static_cast<const cplx<real> *>(in), slot_user, static_cast<cplx<real> *>(slots), S,
-      keep_in);
+      keep_in, static_cast<const cplx<real> *>(w));
   return cudaGetLastError();
 }
 
@@ -401,7 +410,7 @@ cudaError_t launch_fill(void *x, int64_t n, double value, cudaStream_t s) {
   template cudaError_t launch_compact<real>(const void *, const int32_t *, void *, int64_t,      \
                                            cudaStream_t);                                      \
   template cudaError_t launch_expand<real>(const void *, const int32_t *, void *, int64_t,       \
-                                          cudaStream_t, bool);                                 \
+                                          cudaStream_t, bool, const void *);                   \
   template cudaError_t launch_from_c128<real>(const void *, void *, int64_t, cudaStream_t);     \
   template cudaError_t launch_to_c128<real>(const void *, void *, int64_t, cudaStream_t);       \
   template cudaError_t launch_sq_norm<real>(const void *, int64_t, double *, double *,          \

@@ -20,8 +20,7 @@ struct ApplyArgs {
   const Task *tasks = nullptr;
   const int2 *batches = nullptr;    // {first slot, kmax}
   const int32_t *lane_code = nullptr;  // item_pack per batch lane
-  const void *frac = nullptr;       // S x (t_u, t_v); sign of t_u = phase flip if unit weights
-  const void *weight = nullptr;     // S complex weights with the flip folded in, or null
+  const void *frac = nullptr;       // S x (t_u, t_v); sign of t_u = the phase flip (-1)^(k_u + k_v)
   void *slot_out = nullptr;         // degrid output, S complex
   const void *slot_in = nullptr;    // grid input, S complex
   // When set, visibilities are read / written in caller order directly:
@@ -52,14 +51,12 @@ struct LaunchShape {
 };
 
 // Largest dynamic shared memory a launch of the given shape needs, in bytes:
-// user = visibilities in caller order, weight = a weight stream (they size
-// the degrid kernel's staging buffers; the grid kernel has none).
+// user = visibilities in caller order (it sizes the degrid kernel's staging
+// buffers; the grid kernel has none).
 size_t degrid_smem_bytes(int precision_bytes, int J, int win_rows, int win_cols,
-                         const LaunchShape &shape, bool user = true, bool weight = true,
-                         int group = 1);
+                         const LaunchShape &shape, bool user = true, int group = 1);
 size_t grid_smem_bytes(int precision_bytes, int J, int win_rows, int win_cols,
-                       const LaunchShape &shape, bool user = false, bool weight = true,
-                       int group = 1);
+                       const LaunchShape &shape, bool user = false, int group = 1);
 
 // G: tiles of the grid -> visibilities.
 template <typename real>
@@ -75,16 +72,16 @@ cudaError_t launch_grid(const ApplyArgs<real> &a, const PolyTable<real> &poly, i
 // Grouped forms: `a.tasks` lists the tasks of several operators (Task::channel
 // names the operator), `a.group` points at a device array of their ApplyArgs
 // and `a.group_task_base` at the first grouped task of each; win_rows /
-// win_cols are the largest over the group; user / weight say whether any
-// operator of the group reads caller order / has a weight stream.
+// win_cols are the largest over the group; user says whether any operator
+// of the group reads or writes caller order.
 template <typename real>
 cudaError_t launch_degrid_group(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
                                 int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
-                                bool user, bool weight, cudaStream_t s);
+                                bool user, cudaStream_t s);
 template <typename real>
 cudaError_t launch_grid_group(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
                               int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
-                              bool user, bool weight, cudaStream_t s);
+                              bool user, cudaStream_t s);
 
 // G^H, second half: sums the task windows that cover each grid cell, in a
 // fixed order, into the grid.
@@ -113,6 +110,10 @@ struct ChannelIO {
   void *vis_out = nullptr;      // caller-ordered visibilities out (forward)
   void *slots = nullptr;        // slot-ordered buffer
   const int32_t *slot_user = nullptr, *user_slot = nullptr;
+  // weights (null for unit weights): w_slot in slot order (S values), used
+  // conjugated by the gather before G^H; w_vis in caller order (M values),
+  // multiplied into the forward's output
+  const void *w_slot = nullptr, *w_vis = nullptr;
   int Nx = 0, Ny = 0, Nu = 0, Nv = 0, x0 = 0, y0 = 0;
   int64_t M = 0, S = 0;
 };
@@ -131,6 +132,11 @@ cudaError_t launch_crop_group(const ChannelIO<real> *chans, const int2 *map, int
 template <typename real>
 cudaError_t launch_expand_group(const ChannelIO<real> *chans, const int2 *map, int nblocks,
                                 cudaStream_t s);
+// vis_out <- vis_out * w_vis over a block map of kGroupSlots visibilities
+// per block (channels with weights only).
+template <typename real>
+cudaError_t launch_weigh_vis_group(const ChannelIO<real> *chans, const int2 *map, int nblocks,
+                                   cudaStream_t s);
 // Per-channel deterministic FP64 sum of |x_out|^2 into out[c] (partial holds
 // nch * kNormBlocks doubles), and x_out <- x_out * inv[c].
 template <typename real>
@@ -160,9 +166,11 @@ cudaError_t launch_crop(const void *grid, const real *su, const real *sv, void *
 template <typename real>
 cudaError_t launch_compact(const void *slots, const int32_t *user_slot, void *out, int64_t M,
                            cudaStream_t s);
+// With w (S complex values in slot order), slots[s] = conj(w[s]) in[...]:
+// the conjugated weights of G^H applied in the same pass.
 template <typename real>
 cudaError_t launch_expand(const void *in, const int32_t *slot_user, void *slots, int64_t S,
-                          cudaStream_t s, bool keep_in = false);
+                          cudaStream_t s, bool keep_in = false, const void *w = nullptr);
 
 // complex<double> <-> complex<real> conversion of n values.
 template <typename real>

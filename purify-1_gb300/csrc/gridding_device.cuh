@@ -177,14 +177,20 @@ struct ArgsOf<real, true> {
 
 // Per-warp staging of the degrid kernel's coverage stream.  A warp walks its
 // batches in chunks of up to CH k-steps; while it computes one chunk, the
-// next chunk's per-slot data (t, and the caller index and weight when the
-// launch has them) is on its way into shared memory by cp.async, so a whole
-// chunk of loads is in flight per warp instead of one step.  Each lane copies
-// and later reads only its own column, so the per-thread
+// next chunk's per-slot data (t, and the caller index when the launch
+// writes caller order) is on its way into shared memory by cp.async, so a
+// whole chunk of loads is in flight per warp instead of one step.  Each lane
+// copies and later reads only its own column, so the per-thread
 // cp.async.wait_group is the only wait.  Layout per warp, each [2][CH][32]:
-// t, then the caller index (int), then the weight.  The grid kernel does not
-// stage: its per-warp windows already fill shared memory, and staging would
-// cost it resident CTAs.
+// t, then the caller index (int).  The grid kernel does not stage: its
+// per-warp windows already fill shared memory, and staging would cost it
+// resident CTAs.
+//
+// Weights are not applied in these kernels: the phase sign rides in t_u and
+// operators with weights multiply by them in element-wise passes around the
+// kernels.  (Instantiations that staged and applied a weight stream here
+// raised "illegal instruction" on the GPU for some supports; see the design
+// notes.)
 template <typename real, int J>
 struct StageDepth {
   static constexpr int value = (J <= 4 ? 4 : 8) / (sizeof(real) == 8 ? 2 : 1);
@@ -240,18 +246,12 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const int nbt = tk.batch_end - tk.batch_begin;
   const C *frac = static_cast<const C *>(a.frac);
-  const C *weight = static_cast<const C *>(a.weight);
   const int32_t *user = a.slot_user;
   C *out = static_cast<C *>(a.slot_out);
-  // Kernels with sub-segmented taps have no weight stream: operators that
-  // need both apply their weights in separate element-wise passes (the host
-  // never passes a weight stream to these instantiations).
-  const bool unit = SUB || weight == nullptr;
   if (warp >= nbt) return;
   unsigned char *stg = smem_raw + a0.win_bytes + kHeaderBytes + size_t(warp) * a0.stage_bytes;
   C *st_t = reinterpret_cast<C *>(stg);
   int *st_m = reinterpret_cast<int *>(stg + 2 * CH * 32 * sizeof(C));
-  C *st_w = reinterpret_cast<C *>(stg + 2 * CH * 32 * (sizeof(C) + (user ? 4 : 0)));
   const unsigned long long pol = l2_stream_policy();
   auto issue = [&](int lb, int k0, int buf) {
     const int2 bt = th.hdr[lb];
@@ -261,7 +261,6 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
       const int e = (buf * CH + j) * 32 + lane;
       cp_async_stream<sizeof(C)>(st_t + e, frac + i, pol);
       if (user) cp_async_stream<4>(st_m + e, user + i, pol);
-      if (!unit) cp_async_stream<sizeof(C)>(st_w + e, weight + i, pol);
     }
     cp_async_commit();
   };
@@ -305,17 +304,9 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
         for (int ju = 0; ju < JB; ++ju) row = fma2(splat(ku[ju]), F[jv][ju], row);
         sum = fma2(splat(kv[jv]), row, sum);
       }
-      const real sr = sum.x, si = sum.y;
-      C y;
-      if (unit) {
-        const real sg = copysign(real(1), t.x);
-        y.x = sg * sr;
-        y.y = sg * si;
-      } else {
-        const C w = st_w[e];
-        y.x = sr * w.x - si * w.y;
-        y.y = sr * w.y + si * w.x;
-      }
+      // the phase sign (-1)^(k_u + k_v) rides in the sign of t_u
+      const real sg = copysign(real(1), t.x);
+      const C y{sg * sum.x, sg * sum.y};
       // Lanes past their item's end compute on null slots: 0 in slot order,
       // nothing in caller order.
       if (!user) {
@@ -354,9 +345,7 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
   C *mine = wins + warp * WN;
   const int nbt = tk.batch_end - tk.batch_begin;
   const C *frac = static_cast<const C *>(a.frac);
-  const C *weight = static_cast<const C *>(a.weight);
   const C *vin = static_cast<const C *>(a.slot_in);
-  const bool unit = SUB || weight == nullptr;  // see degrid_kernel
   if (warp < nbt) {
     // Two cursors over this warp's (batch, k) steps, slot = hdr[lb].x +
     // 32 k + lane: the compute cursor and, two steps ahead of it, the
@@ -387,7 +376,6 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
       for (int ju = 0; ju < JB; ++ju) acc[jv][ju] = C{0, 0};
     while (clb < nbt) {
       const C t = t0, yv = y0;
-      const size_t i_cur = slot(clb, ck);
       t0 = t1;
       y0 = y1;
       if (plb < nbt) {
@@ -395,18 +383,10 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
         y1 = read_vis(a, vin, slot(plb, pk));
         adv(plb, pk);
       }
-      // Null slots hold a zero visibility, so they add nothing.
-      real zr, zi;
-      if (unit) {
-        const real sg = copysign(real(1), t.x);
-        zr = sg * yv.x;
-        zi = sg * yv.y;
-      } else {
-        // conj(weight) * y: G^H holds the conjugated entries of G.
-        const C w = stream_load(weight + i_cur);
-        zr = w.x * yv.x + w.y * yv.y;
-        zi = w.x * yv.y - w.y * yv.x;
-      }
+      // Null slots hold a zero visibility, so they add nothing.  The phase
+      // sign (-1)^(k_u + k_v) rides in the sign of t_u.
+      const real sg = copysign(real(1), t.x);
+      const real zr = sg * yv.x, zi = sg * yv.y;
       real ku[JB], kv[JB];
       block_taps<real, J, G, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
       block_taps<real, J, G, SUB>(poly.v, poly.nsub_v, t.y, kv);
@@ -549,13 +529,12 @@ __device__ __forceinline__ void fold_tile(const FoldArgs &f, int t) {
   }
 }
 
-// Per-warp staging bytes of the degrid kernel (see StageDepth): t, the caller
-// index if visibilities are written in caller order, the weight if there is
-// one.
-inline size_t stage_bytes(int precision_bytes, int J, bool user, bool weight) {
+// Per-warp staging bytes of the degrid kernel (see StageDepth): t, and the
+// caller index if visibilities are written in caller order.
+inline size_t stage_bytes(int precision_bytes, int J, bool user) {
   const size_t CH = size_t(stage_depth(precision_bytes, J));
   const size_t c = 2 * size_t(precision_bytes);
-  return 2 * CH * 32 * (c + (user ? 4 : 0) + (weight ? c : 0));
+  return 2 * CH * 32 * (c + (user ? 4 : 0));
 }
 
 inline size_t window_bytes(int precision_bytes, int win_rows, int win_cols, const LaunchShape &shape,
@@ -586,8 +565,6 @@ cudaError_t launch_apply(bool degrid, const ApplyArgs<real> &a, const PolyTable<
                          int J, int ntasks, size_t smem, int threads, cudaStream_t s) {
   if (ntasks == 0) return cudaSuccess;
   const bool sub = poly.nsub_u > 1 || poly.nsub_v > 1;
-  // sub-segmented instantiations carry no weight stream (see degrid_kernel)
-  if (sub && a.weight) return cudaErrorInvalidValue;
 #define PG_CASE(JJ, GG)                                                                  \
   case JJ:                                                                               \
     return sub ? launch_one<real, JJ, GG, true, GROUP>(degrid, a, poly, ntasks, smem, threads, s) \

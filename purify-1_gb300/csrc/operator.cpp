@@ -107,6 +107,11 @@ class OperatorT final : public Operator {
   FftArgs fft_args() const;
   void forward_slots(const void *x, void *caller_vis = nullptr);
   void adjoint_slots(void *x, const void *caller_vis = nullptr);
+  // Phi'^H Phi' x with the visibilities kept in slot order between G and G^H
+  // (power method, normal operator); the weights' conjugates are applied there.
+  void normal_slots(const void *x, void *out);
+  // Slot-ordered weights for the gather before G^H, or null for unit weights.
+  const void *slot_weights() const { return split_weights_ ? weight_.get() : nullptr; }
   void join(cudaStream_t user);
   void release(cudaStream_t user);
   void upload_correction();
@@ -126,12 +131,12 @@ class OperatorT final : public Operator {
   void init_w(const OperatorConfig &cfg, int64_t &bytes, AxisTiling &tu, AxisTiling &tv,
               std::vector<int32_t> &tile_tasks);
   bool unit_weights_ = true;
-  // Weights with sub-segmented taps: the gridding kernels run without a
-  // weight stream (the phase sign rides in t_u as for unit weights) and the
-  // weights are applied by element-wise passes: caller order after G, slot
-  // order (conjugated) before G^H.
+  // Weights (plain rows): the gridding kernels have no weight stream (the
+  // phase sign rides in t_u) and the weights are applied around them: in
+  // caller order after G (wcaller_), conjugated in slot order before G^H
+  // (weight_; by the gather where there is one).
   bool split_weights_ = false;
-  DeviceBuffer wcaller_;  // caller-ordered weights of split_weights_
+  DeviceBuffer wcaller_;  // caller-ordered weights
   bool fused_forward_ = true, fused_adjoint_ = false;
   // The adjoint's gather keeps the caller-ordered visibilities in L2
   // (evict-last) when they fit in kKeepVisL2Bytes: in a forward / adjoint
@@ -254,8 +259,8 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
     cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_),
                "cudaDeviceGetAttribute");
     const size_t need = std::max(
-        degrid_smem_bytes(sizeof(real), J_, win_rows_, win_cols_, shape_, true, true, group_),
-        grid_smem_bytes(sizeof(real), J_, win_rows_, win_cols_, shape_, true, true, group_));
+        degrid_smem_bytes(sizeof(real), J_, win_rows_, win_cols_, shape_, true, group_),
+        grid_smem_bytes(sizeof(real), J_, win_rows_, win_cols_, shape_, true, group_));
     if (need > size_t(optin))
       throw Error(kUnsupported, "tile / threads / support need " + std::to_string(need) +
                                     " bytes of shared memory per CTA; the device allows " +
@@ -376,7 +381,7 @@ void OperatorT<real>::init_plain(const OperatorConfig &cfg, int64_t &bytes, Axis
   fold_J_ = J_ + group_ - 1;  // task windows reach JB - 1 cells into the next tiles
   S_ = plan.S;
   unit_weights_ = plan.unit_weights;
-  split_weights_ = !unit_weights_ && (poly_.nsub_u > 1 || poly_.nsub_v > 1);
+  split_weights_ = !unit_weights_;
   nnz_ = M_ * int64_t(cfg.Ju) * cfg.Jv;
   occupied_ = plan.occupied_cells;
   work_items_ = int64_t(plan.lane_code.size());
@@ -384,8 +389,8 @@ void OperatorT<real>::init_plain(const OperatorConfig &cfg, int64_t &bytes, Axis
   for (int64_t i = 0; i < S_; ++i) {
     // unit weights: the phase sign (-1)^(k_u + k_v) rides in the sign of t_u
     const real tu = fraction_in_cell<real>(plan.frac_u[i]);
-    const bool sign_in_t = unit_weights_ || split_weights_;
-    fr[i] = C((sign_in_t && plan.flip[i]) ? -tu : tu, fraction_in_cell<real>(plan.frac_v[i]));
+    // the phase sign (-1)^(k_u + k_v) rides in the sign of t_u
+    fr[i] = C(plan.flip[i] ? -tu : tu, fraction_in_cell<real>(plan.frac_v[i]));
   }
   frac_.alloc(sizeof(C) * S_, &bytes);
   frac_.upload(fr.data(), sizeof(C) * S_, stream_);
@@ -393,9 +398,8 @@ void OperatorT<real>::init_plain(const OperatorConfig &cfg, int64_t &bytes, Axis
   if (!unit_weights_) {
     wt.resize(S_);
     for (int64_t i = 0; i < S_; ++i) {
-      // split weights: the sign is in t_u, so the stream holds the weight itself
-      const std::complex<double> w = (split_weights_ && plan.flip[i]) ? -plan.weight[i]
-                                                                      : plan.weight[i];
+      // the sign is in t_u, so this holds the weight itself
+      const std::complex<double> w = plan.flip[i] ? -plan.weight[i] : plan.weight[i];
       wt[i] = C(real(w.real()), real(w.imag()));
     }
     weight_.alloc(sizeof(C) * S_, &bytes);
@@ -597,7 +601,6 @@ void OperatorT<real>::degrid_slots(const void *grid, void *caller_vis) {
   a.batches = batches_.as<int2>();
   a.lane_code = lane_code_.as<int32_t>();
   a.frac = frac_.get();
-  a.weight = (unit_weights_ || split_weights_) ? nullptr : weight_.get();
   a.slot_out = caller_vis ? caller_vis : ws_->slots;
   a.slot_user = caller_vis ? slot_user_.as<int32_t>() : nullptr;
   a.Nu = Nu_;
@@ -619,8 +622,6 @@ void OperatorT<real>::degrid_slots(const void *grid, void *caller_vis) {
 
 template <typename real>
 void OperatorT<real>::grid_slots(void *grid, const void *caller_vis) {
-  if (split_weights_ && !caller_vis)
-    cuda_check(launch_cmul<real>(ws_->slots, weight_.get(), S_, true, ws_->stream), "weights");
   grid_core(grid, caller_vis ? caller_vis : ws_->slots,
             caller_vis ? slot_user_.as<int32_t>() : nullptr, ws_->tilebuf);
 }
@@ -660,7 +661,6 @@ void OperatorT<real>::grid_core(void *grid, const void *vis, const int32_t *slot
   a.batches = batches_.as<int2>();
   a.lane_code = lane_code_.as<int32_t>();
   a.frac = frac_.get();
-  a.weight = (unit_weights_ || split_weights_) ? nullptr : weight_.get();
   a.slot_in = vis;
   a.slot_user = slot_user;
   a.Nu = Nu_;
@@ -719,7 +719,7 @@ void OperatorT<real>::grid_on_stream(const void *y, void *grid) {
   }
   mark_begin(kExpand);
   cuda_check(launch_expand<real>(y, slot_user_.as<int32_t>(), ws_->slots, S_, ws_->stream,
-                                 keep_vis_l2_ && ws_ == &own_),
+                                 keep_vis_l2_ && ws_ == &own_, slot_weights()),
              "expand");
   mark_end(kExpand);
   grid_slots(grid);
@@ -784,6 +784,14 @@ void OperatorT<real>::adjoint_slots(void *x, const void *caller_vis) {
 }
 
 template <typename real>
+void OperatorT<real>::normal_slots(const void *x, void *out) {
+  forward_slots(x);
+  if (split_weights_)
+    cuda_check(launch_cmul<real>(ws_->slots, weight_.get(), S_, true, ws_->stream), "weights");
+  adjoint_slots(out);
+}
+
+template <typename real>
 void OperatorT<real>::forward_on_stream(const void *x, void *y) {
   if (fused_forward_) {
     forward_slots(x, y);
@@ -804,7 +812,7 @@ void OperatorT<real>::adjoint_on_stream(const void *y, void *x) {
   }
   mark_begin(kExpand);
   cuda_check(launch_expand<real>(y, slot_user_.as<int32_t>(), ws_->slots, S_, ws_->stream,
-                                 keep_vis_l2_ && ws_ == &own_),
+                                 keep_vis_l2_ && ws_ == &own_, slot_weights()),
              "expand");
   mark_end(kExpand);
   adjoint_slots(x);
@@ -858,8 +866,7 @@ void OperatorT<real>::power_ws(void *x, int iters, double *sq, double *partial,
   with_workspace(w, [&] {
     cuda_check(launch_fill<real>(x, N_, 1.0 / std::sqrt(double(N_)), w.stream), "fill");
     for (int i = 0; i < iters; ++i) {
-      forward_slots(x);
-      adjoint_slots(x);
+      normal_slots(x, x);
       cuda_check(launch_sq_norm<real>(x, N_, partial, sq + i, w.stream), "norm");
       cuda_check(launch_scale_rsqrt<real>(x, N_, sq + i, w.stream), "scale");
     }
@@ -872,8 +879,7 @@ void OperatorT<real>::normal(const void *x, void *out, cudaStream_t user) {
   std::lock_guard<std::mutex> lock(mu_);
   join(user);
   run_recorded(3, x, out, [&] {
-    forward_slots(x);
-    adjoint_slots(out);
+    normal_slots(x, out);
   });
   release(user);
 }
@@ -923,9 +929,9 @@ void OperatorT<real>::grid_no_alloc(const void *vis, void *grid, cudaStream_t us
   // expand writes every slot (0 for null slots) and the grid kernels write
   // every cell of every task window, so nothing left in the array from an
   // earlier call is read.
-  cuda_check(launch_expand<real>(vis, slot_user_.as<int32_t>(), slots, S_, stream_), "expand");
-  if (split_weights_)
-    cuda_check(launch_cmul<real>(slots, weight_.get(), S_, true, stream_), "weights");
+  cuda_check(launch_expand<real>(vis, slot_user_.as<int32_t>(), slots, S_, stream_, false,
+                                 slot_weights()),
+             "expand");
   grid_core(grid, slots, nullptr, windows);
   release(user);
 }
@@ -1081,8 +1087,7 @@ double OperatorT<real>::power_method(int iters, double tol) {
       double old_value = 0;
       for (int i = 0; i < iters; ++i) {
         // visibilities stay in slot order between the two halves
-        forward_slots(pm_x_.get());
-        adjoint_slots(pm_x_.get());
+        normal_slots(pm_x_.get(), pm_x_.get());
         cuda_check(launch_sq_norm<real>(pm_x_.get(), N_, norm_partial_.as<double>(),
                                         norm_out_.as<double>(), stream_),
                    "norm");

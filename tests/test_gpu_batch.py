@@ -216,10 +216,33 @@ def test_batch_errors(pg, cuda):
         pg.Batch([], J=4)
     with pytest.raises(pg.PurifyError):
         pg.Batch([dict(u=np.zeros(3), v=np.zeros(3), imsizey=0, imsizex=8)], J=4, tuning=TUNING)
-    # weights with a sub-segmented tap fit (KB J = 2) have no grouped form
-    rng = np.random.default_rng(0)
-    w = dict(u=rng.normal(0, 5, 50), v=rng.normal(0, 5, 50), imsizey=16, imsizex=16,
-             weights=rng.standard_normal(50) + 1j * rng.standard_normal(50))
-    with pytest.raises(pg.PurifyError) as e:
-        pg.Batch([w], J=2, precision="fp32", tuning=TUNING)
-    assert e.value.status == 2 and "sub-segmented" in str(e.value)
+
+
+@pytest.mark.parametrize("J", [2, 6])
+def test_batch_weights_any_kernel_fit(pg, cuda, J):
+    """Channels with complex weights, for a sub-segmented tap fit (KB J = 2)
+    and a plain one (J = 6): the grouped launches apply the weights around
+    the gridding kernels (caller order after G, conjugated by the gather
+    before G^H), as the single operator does."""
+    torch = cuda
+    rng = np.random.default_rng(J)
+    chans = []
+    for k, M in enumerate((3000, 5000)):
+        chans.append(dict(u=rng.normal(0, 12, M), v=rng.normal(0, 12, M), imsizey=48, imsizex=48,
+                          weights=rng.standard_normal(M) + 1j * rng.standard_normal(M)))
+    b = pg.Batch(chans, J=J, precision="fp32", tuning=TUNING)
+    ops = [pg.MeasurementOperator(c["u"], c["v"], None, c["weights"], 48, 48, 2.0, power_iters=0,
+                                  kernel="kb", Ju=J, Jv=J, precision="fp32",
+                                  tuning={"threads": 128, "tile": 32, "max_per_item": 16})
+           for c in chans]
+    xs = [dev(torch, rng.standard_normal(48 * 48) + 1j * rng.standard_normal(48 * 48), "fp32")
+          for _ in chans]
+    vis = [torch.empty(c["u"].size, dtype=torch.complex64, device="cuda") for c in chans]
+    xo = [torch.empty(48 * 48, dtype=torch.complex64, device="cuda") for _ in chans]
+    b.bind(xs, vis, xo)
+    b.apply(3)
+    torch.cuda.synchronize()
+    for k, op in enumerate(ops):
+        y = op.forward(xs[k])
+        assert rel_l2(host(vis[k]), host(y)) < TOL["fp32"], k
+        assert rel_l2(host(xo[k]), host(op.adjoint(vis[k]))) < TOL["fp32"], k
