@@ -368,6 +368,37 @@ int purify_gb300_batch_info_get(const purify_gb300_batch *b, purify_gb300_batch_
  * reference; used by the autotuner and the benchmark. */
 int purify_gb300_batch_time(purify_gb300_batch *b, int32_t what, uint32_t reps, double *ms);
 
+/* ---- Solver-side consumer ---------------------------------------------------
+ * Forward-backward (proximal gradient) iterations of
+ *   min_x 1/2 ||y - Phi x||^2 + gamma ||x||_1  (x real and >= 0 optionally)
+ * on the device: b = Phi^H y, then per iteration
+ *   x <- soft_{step gamma}(x - step (Phi^H Phi x - b))
+ * through purify_gb300_normal, followed by the reference's step-size update
+ * of gamma (cpp/purify/update_factory.h:46-54: gamma' = update_scale
+ * max |Re x|, taken when |gamma - gamma'| > update_tol during the first
+ * update_iters iterations).  gamma starts at gamma_scale max |Phi^H y|, as
+ * the reference's PADMM factory sets it (cpp/purify/algorithm_factory.h:
+ * 73-76).  This stands in for the reference's solvers (sopt's proximal ADMM,
+ * absent here) as the caller that applies Phi^H Phi many times per solve. */
+typedef struct {
+  uint32_t iterations;
+  double step;              /* gradient step; 1 for a normalised operator */
+  double gamma_scale;       /* default 1e-3 */
+  double update_scale;      /* default 1e-3 (step_size_scale) */
+  double update_tol;        /* default 1e-3 */
+  uint32_t update_iters;    /* default 0: gamma keeps its start value */
+  int32_t real_constraint;  /* default 1 */
+  int32_t positive_constraint; /* default 1 */
+} purify_gb300_fb_params;
+void purify_gb300_fb_default_params(purify_gb300_fb_params *p);
+/* y: M device values, x: imsizey * imsizex device values (start on entry,
+ * solution on exit), both of the operator's precision; gammas: host array of
+ * `iterations` doubles receiving the gamma each iteration used, or NULL.
+ * Ordered after `stream`; returns when the solve has finished. */
+int purify_gb300_forward_backward(purify_gb300_operator *op, const void *y, void *x,
+                                  const purify_gb300_fb_params *params, double *gammas,
+                                  void *stream);
+
 /* ---- Request server ------------------------------------------------------
  * Forward, adjoint and operator-norm requests on coverages kept resident on
  * the device, admitted by an HBM budget and run concurrently: each admitted

@@ -16,6 +16,7 @@
 #include "plan.h"
 #include "psf.h"
 #include "server.h"
+#include "solver.h"
 #include "wplan.h"
 
 struct purify_gb300_operator {
@@ -175,6 +176,37 @@ int purify_gb300_normal(purify_gb300_operator *op, const void *x, void *out, voi
   if (!op) return null_arg("operator");
   if (!x || !out) return null_arg("buffer");
   return guard([&] { op->impl->normal(x, out, static_cast<cudaStream_t>(stream)); });
+}
+void purify_gb300_fb_default_params(purify_gb300_fb_params *p) {
+  if (!p) return;
+  const pg::FbParams d;
+  p->iterations = uint32_t(d.iterations);
+  p->step = d.step;
+  p->gamma_scale = d.gamma_scale;
+  p->update_scale = d.update_scale;
+  p->update_tol = d.update_tol;
+  p->update_iters = uint32_t(d.update_iters);
+  p->real_constraint = d.real_constraint ? 1 : 0;
+  p->positive_constraint = d.positive_constraint ? 1 : 0;
+}
+int purify_gb300_forward_backward(purify_gb300_operator *op, const void *y, void *x,
+                                  const purify_gb300_fb_params *params, double *gammas,
+                                  void *stream) {
+  if (!op) return null_arg("operator");
+  if (!params) return null_arg("params");
+  if (!x || (!y && op->impl->info().M > 0)) return null_arg("buffer");
+  return guard([&] {
+    pg::FbParams p;
+    p.iterations = int(params->iterations);
+    p.step = params->step;
+    p.gamma_scale = params->gamma_scale;
+    p.update_scale = params->update_scale;
+    p.update_tol = params->update_tol;
+    p.update_iters = int(params->update_iters);
+    p.real_constraint = params->real_constraint != 0;
+    p.positive_constraint = params->positive_constraint != 0;
+    pg::forward_backward(*op->impl, y, x, p, gammas, static_cast<cudaStream_t>(stream));
+  });
 }
 int purify_gb300_psf_create(purify_gb300_operator *op, uint32_t power_iters, double power_tol,
                             purify_gb300_psf **out) {

@@ -75,6 +75,13 @@ class Channel(ctypes.Structure):
                 ("M", ctypes.c_int64), ("imsizey", ctypes.c_uint32), ("imsizex", ctypes.c_uint32)]
 
 
+class FbParams(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_uint32), ("step", ctypes.c_double),
+                ("gamma_scale", ctypes.c_double), ("update_scale", ctypes.c_double),
+                ("update_tol", ctypes.c_double), ("update_iters", ctypes.c_uint32),
+                ("real_constraint", ctypes.c_int32), ("positive_constraint", ctypes.c_int32)]
+
+
 class BatchTuning(ctypes.Structure):
     _fields_ = [("tile", ctypes.c_int32), ("max_per_item", ctypes.c_int32),
                 ("degrid_threads", ctypes.c_int32), ("grid_threads", ctypes.c_int32),
@@ -123,7 +130,7 @@ EXPORTS = [
     "purify_gb300_forward", "purify_gb300_adjoint", "purify_gb300_forward_host",
     "purify_gb300_adjoint_host", "purify_gb300_power_method", "purify_gb300_set_norm",
     "purify_gb300_get_norm", "purify_gb300_operator_info", "purify_gb300_lambda_to_pixels",
-    "purify_gb300_uv_to_pixels",
+    "purify_gb300_uv_to_pixels", "purify_gb300_fb_default_params", "purify_gb300_forward_backward",
     "purify_gb300_last_error", "purify_gb300_version", "purify_gb300_plan_create",
     "purify_gb300_plan_sizes", "purify_gb300_plan_export", "purify_gb300_plan_destroy",
     "purify_gb300_plan_create_grouped",
@@ -176,6 +183,9 @@ def load(path=None):
     L.purify_gb300_lambda_to_pixels.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_double,
                                                 ctypes.c_double, ctypes.c_uint32,
                                                 ctypes.c_uint32, vp, vp]
+    L.purify_gb300_fb_default_params.argtypes = [P(FbParams)]
+    L.purify_gb300_fb_default_params.restype = None
+    L.purify_gb300_forward_backward.argtypes = [vp, vp, vp, P(FbParams), vp, vp]
     L.purify_gb300_uv_to_pixels.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_int32,
                                             ctypes.c_double, ctypes.c_double, ctypes.c_uint32,
                                             ctypes.c_uint32, vp, vp]
@@ -522,6 +532,28 @@ class MeasurementOperator:
         _check(load().purify_gb300_normal(self._h, ctypes.c_void_p(x.data_ptr()),
                                           ctypes.c_void_p(out.data_ptr()), self._stream(stream)))
         return out
+
+    def forward_backward(self, y, x0=None, stream=None, **params):
+        """Forward-backward iterations of min 1/2 ||y - Phi x||^2 + gamma ||x||_1
+        on the device (purify_gb300_forward_backward).  y: CUDA tensor of M
+        values; x0: start (zeros when None).  Keyword parameters: iterations,
+        step, gamma_scale, update_scale, update_tol, update_iters,
+        real_constraint, positive_constraint.  Returns (x, gammas)."""
+        import torch
+        self._check_device_tensor(y, self.M)
+        n = self.imsizey * self.imsizex
+        x = torch.zeros(n, dtype=self.complex_dtype, device=y.device) if x0 is None else x0.clone()
+        p = FbParams()
+        load().purify_gb300_fb_default_params(ctypes.byref(p))
+        for k, v in params.items():
+            if not hasattr(p, k):
+                raise PurifyError(1, "unknown forward-backward parameter %s" % k)
+            setattr(p, k, type(getattr(p, k))(v))
+        gammas = np.zeros(max(int(p.iterations), 1))
+        _check(load().purify_gb300_forward_backward(self._h, ctypes.c_void_p(y.data_ptr()),
+                                                    ctypes.c_void_p(x.data_ptr()), ctypes.byref(p),
+                                                    _np_ptr(gammas), self._stream(stream)))
+        return x, gammas[:int(p.iterations)]
 
     def degrid_into(self, grid, vis, stream=None):
         """G alone: grid (ftsizev*ftsizeu) -> vis (M), device tensors."""
