@@ -49,27 +49,8 @@ __global__ void compact_kernel(const cplx<real> *__restrict__ slots,
   }
 }
 // Gathered loads of the caller-ordered visibilities at L2 evict-last
-// priority (launch_expand's keep_in).
-__device__ __forceinline__ unsigned long long l2_keep_policy() {
-  unsigned long long p;
-  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ float2 load_keep(const float2 *p, unsigned long long pol) {
-  float2 v;
-  asm volatile("ld.global.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;"
-               : "=f"(v.x), "=f"(v.y)
-               : "l"(p), "l"(pol));
-  return v;
-}
-__device__ __forceinline__ double2 load_keep(const double2 *p, unsigned long long pol) {
-  double2 v;
-  asm volatile("ld.global.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;"
-               : "=d"(v.x), "=d"(v.y)
-               : "l"(p), "l"(pol));
-  return v;
-}
-
+// priority (launch_expand's keep_in): l2_keep_policy / load_keep of
+// gridding_device.cuh.
 template <typename real>
 __global__ void expand_kernel(const cplx<real> *__restrict__ in,
                               const int32_t *__restrict__ slot_user,

@@ -147,16 +147,34 @@ __device__ __forceinline__ TaskHeaders load_headers(const A &a, const Task &tk,
   return h;
 }
 
-// Visibility read for the grid kernel: slot order, or caller order through
-// slot_user (0 for null slots).
+// Visibility reads of the grid kernel.  Slot order: a streaming load of
+// slot i.  Caller order: the gather of visibility m = slot_user[i] (0 for
+// null slots, m < 0), at L2 evict-last priority when the launch keeps the
+// caller-ordered vector in L2 (ApplyArgs::keep_in).
+__device__ __forceinline__ unsigned long long l2_keep_policy() {
+  unsigned long long p;
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ float2 load_keep(const float2 *p, unsigned long long pol) {
+  float2 v;
+  asm volatile("ld.global.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;"
+               : "=f"(v.x), "=f"(v.y)
+               : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ double2 load_keep(const double2 *p, unsigned long long pol) {
+  double2 v;
+  asm volatile("ld.global.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;"
+               : "=d"(v.x), "=d"(v.y)
+               : "l"(p), "l"(pol));
+  return v;
+}
 template <typename real>
-__device__ __forceinline__ cplx<real> read_vis(const ApplyArgs<real> &a, const cplx<real> *vin,
-                                              size_t i) {
-  if (a.slot_user) {
-    const int m = __ldcs(a.slot_user + i);
-    return m >= 0 ? vin[m] : cplx<real>{0, 0};
-  }
-  return __ldcs(vin + i);  // read once: streaming
+__device__ __forceinline__ cplx<real> gather_vis(const cplx<real> *vin, int m, bool keep,
+                                                unsigned long long pol) {
+  if (m < 0) return cplx<real>{0, 0};
+  return keep ? load_keep(vin + m, pol) : vin[m];
 }
 
 // Operator arguments of a task.  A single-operator launch reads them from the
@@ -349,7 +367,10 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
   if (warp < nbt) {
     // Two cursors over this warp's (batch, k) steps, slot = hdr[lb].x +
     // 32 k + lane: the compute cursor and, two steps ahead of it, the
-    // prefetch cursor, so two steps of coverage loads are in flight.
+    // prefetch cursor, so two steps of coverage loads are in flight.  In
+    // caller order the prefetch gathers vin[slot_user[slot]]; the caller
+    // index of the prefetch cursor's slot is loaded one step before its
+    // gather (mq), so a gather never waits on its index load.
     int clb = warp, ck = 0;
     int plb = warp, pk = 0;
     auto adv = [&](int &lb, int &k) {
@@ -361,13 +382,23 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
       }
     };
     auto slot = [&](int lb, int k) { return size_t(th.hdr[lb].x) + size_t(k) * kBatch + lane; };
-    C t0 = stream_load(frac + slot(plb, pk)), y0 = read_vis(a, vin, slot(plb, pk));
+    const int32_t *user = a.slot_user;
+    const bool keep = a.keep_in != 0;
+    const unsigned long long kpol = l2_keep_policy();
+    auto index_at = [&](int lb, int k) { return lb < nbt ? __ldcs(user + slot(lb, k)) : -1; };
+    auto value_at = [&](int lb, int k, int m) {
+      return user ? gather_vis<real>(vin, m, keep, kpol) : __ldcs(vin + slot(lb, k));
+    };
+    int mq = user ? index_at(plb, pk) : -1;
+    C t0 = stream_load(frac + slot(plb, pk)), y0 = value_at(plb, pk, mq);
     adv(plb, pk);
+    if (user) mq = index_at(plb, pk);
     C t1{0, 0}, y1{0, 0};
     if (plb < nbt) {
       t1 = stream_load(frac + slot(plb, pk));
-      y1 = read_vis(a, vin, slot(plb, pk));
+      y1 = value_at(plb, pk, mq);
       adv(plb, pk);
+      if (user) mq = index_at(plb, pk);
     }
     C acc[JB][JB];
 #pragma unroll
@@ -380,8 +411,9 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
       y0 = y1;
       if (plb < nbt) {
         t1 = stream_load(frac + slot(plb, pk));
-        y1 = read_vis(a, vin, slot(plb, pk));
+        y1 = value_at(plb, pk, mq);
         adv(plb, pk);
+        if (user) mq = index_at(plb, pk);
       }
       // Null slots hold a zero visibility, so they add nothing.  The phase
       // sign (-1)^(k_u + k_v) rides in the sign of t_u.

@@ -663,6 +663,9 @@ void OperatorT<real>::grid_core(void *grid, const void *vis, const int32_t *slot
   a.frac = frac_.get();
   a.slot_in = vis;
   a.slot_user = slot_user;
+  // reading caller order on the operator's own scratch: keep the vector in
+  // L2 for the next forward's scattered stores (see kKeepVisL2Bytes)
+  a.keep_in = (slot_user && keep_vis_l2_ && ws_ == &own_) ? 1 : 0;
   a.Nu = Nu_;
   a.Nv = Nv_;
   a.win_stride = win_stride_;
