@@ -121,7 +121,8 @@ class OperatorT final : public Operator {
   int device_ = 0;
   int Nx_ = 0, Ny_ = 0, Nu_ = 0, Nv_ = 0, x0_ = 0, y0_ = 0, J_ = 0;
   int64_t M_ = 0, N_ = 0, S_ = 0;
-  bool wmode_ = false;  // w-projection rows instead of separable taps
+  bool wmode_ = false;  // row-factor kernels (w-projection rows, or plain rows)
+  bool rows_mode_ = false;  // plain separable rows on the row-factor kernels
   int fold_J_ = 0;      // halo of the task windows + 1 (J, or the largest w support)
   DeviceBuffer wcode_, wfactor_, wfactors_, wchunks_, wtask_chunk_;
   int wchunk_values_ = 0;
@@ -204,30 +205,40 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
   // Kernel state, FP64 fit.  The reference builds G with (kernelv, kernelu)
   // in its (u, v) slots (operators.h:322-324); with Ju == Jv both are the same
   // function, which is the only case accepted here.
+  // Supports above the register-block kernels' limit, and Ju != Jv, run as
+  // plain rows on the row-factor kernels (see WPlanRequest::plain).
+  rows_mode_ = !cfg.w_term && (cfg.Ju != cfg.Jv || cfg.Ju > kMaxJ);
+  wmode_ = cfg.w_term || rows_mode_;
   GriddingKernel kern(cfg.kernel, J_, cfg.oversample_ratio);
   const int nc = PolyCount<real>::value;
-  const AxisFit fit = fit_axis(kern, J_, nc);
+  AxisFit fit;
   std::memset(&poly_, 0, sizeof(poly_));
-  for (int j = 0; j < J_; ++j)
-    for (int s = 0; s < fit.nsub; ++s)
-      for (int k = 0; k < nc; ++k) {
-        const real c = real(fit.coef[(size_t(j) * fit.nsub + s) * nc + k]);
-        poly_.u.c[j][s][k] = c;
-        poly_.v.c[j][s][k] = c;
-      }
-  poly_.nsub_u = poly_.nsub_v = fit.nsub;
+  if (!wmode_) {
+    fit = fit_axis(kern, J_, nc);
+    for (int j = 0; j < J_; ++j)
+      for (int s = 0; s < fit.nsub; ++s)
+        for (int k = 0; k < nc; ++k) {
+          const real c = real(fit.coef[(size_t(j) * fit.nsub + s) * nc + k]);
+          poly_.u.c[j][s][k] = c;
+          poly_.v.c[j][s][k] = c;
+        }
+    poly_.nsub_u = poly_.nsub_v = fit.nsub;
+  }
 
   // Gridding correction S(j, i) = 1 / (ftv(y0 + j + 0.5) ftu(x0 + i + 0.5))
-  // (operators.cc:101-121; the w = 0 chirp times Nx Ny is 1).
+  // (operators.cc:101-121; the w = 0 chirp times Nx Ny is 1), ftu of support
+  // Ju along x and ftv of support Jv along y (create_kernels, kernels.cc:
+  // 233-323).
+  const GriddingKernel kern_x(cfg.kernel, cfg.Ju, cfg.oversample_ratio);
+  const GriddingKernel kern_y(cfg.kernel, cfg.Jv, cfg.oversample_ratio);
   su_.resize(Nx_);
   sv_.resize(Ny_);
   for (int i = 0; i < Nx_; ++i)
-    su_[i] = 1.0 / kern.correction((x0_ + i + 0.5) / Nu_ - 0.5);
+    su_[i] = 1.0 / kern_x.correction((x0_ + i + 0.5) / Nu_ - 0.5);
   for (int j = 0; j < Ny_; ++j)
-    sv_[j] = 1.0 / kern.correction((y0_ + j + 0.5) / Nv_ - 0.5);
+    sv_[j] = 1.0 / kern_y.correction((y0_ + j + 0.5) / Nv_ - 0.5);
 
   shape_.threads = cfg.threads > 0 ? cfg.threads : 128;
-  wmode_ = cfg.w_term;
   // Measured on the 10^7-visibility benchmark: the forward is faster writing
   // caller order directly (scattered stores), the adjoint faster with a
   // separate gather into slot order.  The w-projection kernels always use
@@ -455,10 +466,13 @@ void OperatorT<real>::init_w(const OperatorConfig &cfg, int64_t &bytes, AxisTili
   rq.J = cfg.Ju;
   rq.Jw = cfg.Jw;
   rq.kernel = cfg.kernel;
+  rq.plain = rows_mode_;
+  rq.Ju = cfg.Ju;
+  rq.Jv = cfg.Jv;
   // Default tile edge: 24 (measured fastest on the w-projection workload),
   // widened to the largest support - 1 (a window may reach one tile ahead).
-  int smax = cfg.Jw + cfg.Ju - 1;
-  if (cfg.jw_rows) {
+  int smax = rows_mode_ ? std::max(cfg.Ju, cfg.Jv) : cfg.Jw + cfg.Ju - 1;
+  if (cfg.jw_rows && !rows_mode_) {
     smax = 1;
     for (int64_t m = 0; m < cfg.M; ++m) smax = std::max(smax, cfg.jw_rows[m] + cfg.Ju - 1);
   }
@@ -477,7 +491,8 @@ void OperatorT<real>::init_w(const OperatorConfig &cfg, int64_t &bytes, AxisTili
   fold_J_ = plan.Smax;
   S_ = M_;
   unit_weights_ = false;
-  nnz_ = plan.taps;
+  // the reference's non-zeros (Ju Jv per plain row; the stored rows pad to S^2)
+  nnz_ = rows_mode_ ? M_ * int64_t(cfg.Ju) * cfg.Jv : plan.taps;
   occupied_ = 0;
   work_items_ = M_;
   std::vector<C> wt(M_);
@@ -1204,15 +1219,23 @@ std::unique_ptr<Operator> Operator::create(const OperatorConfig &cfg) {
   if (cfg.M > 0 && (!cfg.u || !cfg.v)) throw Error(kInvalidArgument, "u and v must be given");
   const std::string why = check_kernel_request(cfg.kernel, cfg.Ju, cfg.Jv);
   if (!why.empty()) throw Error(kInvalidArgument, why);
-  if (cfg.Ju != cfg.Jv)
-    throw Error(kUnsupported, "the GB300 operator requires Ju == Jv");
-  if (cfg.Ju < 1 || cfg.Ju > kMaxJ)
-    throw Error(kUnsupported, "kernel support must be between 1 and 8 taps");
+  if (cfg.Ju < 1 || cfg.Jv < 1) throw Error(kInvalidArgument, "kernel support must be >= 1");
+  if (cfg.Ju != cfg.Jv && (cfg.kernel == kKB || cfg.kernel == kKBMin))
+    throw Error(kInvalidArgument,
+                "Ju != Jv with a Kaiser-Bessel kernel: the reference builds G with the Jv kernel "
+                "on the u axis and the Ju kernel on the v axis (operators.h:322-324), so one "
+                "axis is evaluated outside its support, where the kernel is not a number");
+  if (cfg.Ju != cfg.Jv && cfg.w_term)
+    throw Error(kUnsupported, "w-projection with Ju != Jv (non-square rows) is not supported");
+  if (!cfg.w_term && std::max(cfg.Ju, cfg.Jv) > kMaxWSupport)
+    throw Error(kUnsupported, "kernel support must be between 1 and 32 taps");
+  if (cfg.w_term && cfg.Ju > kMaxWSupport)
+    throw Error(kUnsupported, "kernel support must be between 1 and 32 taps");
   if (cfg.class_cap < 0 || cfg.class_cap > 16)
     throw Error(kInvalidArgument, "class_cap must be 0 (default) or in [1, 16]");
   if (cfg.cell_group < 0 || cfg.cell_group > 2)
     throw Error(kInvalidArgument, "cell_group must be 0 (automatic), 1 or 2");
-  if (cfg.cell_group == 2 && (cfg.fp64 || cfg.Ju > kMaxGroupJ || cfg.w_term))
+  if (cfg.cell_group == 2 && (cfg.fp64 || cfg.Ju > kMaxGroupJ || cfg.w_term || cfg.Ju != cfg.Jv))
     throw Error(kUnsupported, "2 x 2 work items need complex<float>, J <= 6 and no w-projection");
   if (cfg.w_term && (cfg.M > 0 && !cfg.w))
     throw Error(kInvalidArgument, "w-projection needs the w coordinates");

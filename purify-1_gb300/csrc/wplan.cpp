@@ -60,25 +60,33 @@ int row_terms(double u, double v, double w, int Jw, double dul, double dvl) {
 
 WPlan build_wplan(const WPlanRequest &rq) {
   if (rq.M < 0) throw std::invalid_argument("negative number of visibilities");
-  if (rq.M > 0 && (!rq.u || !rq.v || !rq.w)) throw std::invalid_argument("u, v and w must be given");
+  if (rq.M > 0 && (!rq.u || !rq.v || (!rq.w && !rq.plain)))
+    throw std::invalid_argument("u, v and w must be given");
   if (rq.J < 1 || rq.Jw < 1) throw std::invalid_argument("kernel supports must be >= 1");
+  if (rq.plain && (rq.Ju < 1 || rq.Jv < 1)) throw std::invalid_argument("kernel supports must be >= 1");
   if (rq.M > int64_t(INT32_MAX) - 1) throw std::invalid_argument("too many visibilities");
   for (int64_t m = 0; m < rq.M; ++m)
-    if (!std::isfinite(rq.u[m]) || !std::isfinite(rq.v[m]) || !std::isfinite(rq.w[m]))
+    if (!std::isfinite(rq.u[m]) || !std::isfinite(rq.v[m]) || (!rq.plain && !std::isfinite(rq.w[m])))
       throw std::invalid_argument("visibility " + std::to_string(m) +
                                   " has a non-finite u, v or w coordinate");
   WPlan P;
   P.M = rq.M;
   P.Nu = rq.Nu;
   P.Nv = rq.Nv;
-  P.J = rq.J;
+  P.plain = rq.plain;
+  P.Ju = rq.Ju;
+  P.Jv = rq.Jv;
+  // plain rows: S = max(Ju, Jv) for every row (a w-support of 1 on a support
+  // of S cells)
+  const int Jrow = rq.plain ? std::max(rq.Ju, rq.Jv) : rq.J;
+  P.J = Jrow;
   const int64_t M = rq.M;
   std::vector<int32_t> jw(M);
   int Smax = 1;
   for (int64_t m = 0; m < M; ++m) {
-    jw[m] = rq.jw_rows ? rq.jw_rows[m] : rq.Jw;
-    if (jw[m] < 1 || jw[m] + rq.J - 1 > 255) throw std::invalid_argument("w-support out of range");
-    Smax = std::max(Smax, int(jw[m] + rq.J - 1));
+    jw[m] = rq.plain ? 1 : (rq.jw_rows ? rq.jw_rows[m] : rq.Jw);
+    if (jw[m] < 1 || jw[m] + Jrow - 1 > 255) throw std::invalid_argument("w-support out of range");
+    Smax = std::max(Smax, int(jw[m] + Jrow - 1));
   }
   P.Smax = Smax;
   P.tu = make_tiling(rq.Nu, rq.tile);
@@ -95,15 +103,18 @@ WPlan build_wplan(const WPlanRequest &rq) {
 
   // The kernel sees w - mean(w) (operators.h:323).
   double wmean = 0;
-  for (int64_t m = 0; m < M; ++m) wmean += rq.w[m];
-  if (M > 0) wmean /= double(M);
+  if (!rq.plain) {
+    for (int64_t m = 0; m < M; ++m) wmean += rq.w[m];
+    if (M > 0) wmean /= double(M);
+  }
+  auto w_of = [&](int64_t m) { return rq.plain ? 0.0 : rq.w[m] - wmean; };
 
   // Placement per row (operators.cc:85-96): kw = floor(u - S/2), taps at
   // kw + 1 .. kw + S (mod N); the phase (-1)^(kw_u + kw_v) goes with the weight.
   std::vector<int32_t> tile(M), local(M);
   std::vector<uint8_t> flip(M);
   for (int64_t m = 0; m < M; ++m) {
-    const int S = jw[m] + rq.J - 1;
+    const int S = jw[m] + Jrow - 1;
     const double kwu = std::floor(rq.u[m] - S * 0.5), kwv = std::floor(rq.v[m] - S * 0.5);
     const int q0 = int(wrap(kwu + 1, rq.Nu)), p0 = int(wrap(kwv + 1, rq.Nv));
     const int a = P.tv.of[p0], b = P.tu.of[q0];
@@ -129,9 +140,11 @@ WPlan build_wplan(const WPlanRequest &rq) {
   int64_t off = 0;
   for (int64_t i = 0; i < M; ++i) {
     const int32_t m = order[i];
-    const int S = jw[m] + rq.J - 1;
+    const int S = jw[m] + Jrow - 1;
     const int lp = local[m] >> 8, lq = local[m] & 0xff;  // item_pack layout below
-    const int terms = row_terms(rq.u[m], rq.v[m], rq.w[m] - wmean, jw[m], P.du_lambda, P.dv_lambda);
+    // plain rows: one term (the separable taps)
+    const int terms =
+        rq.plain ? 1 : row_terms(rq.u[m], rq.v[m], w_of(m), jw[m], P.du_lambda, P.dv_lambda);
     P.code[i] = lp | (lq << 8) | (S << 16) | (terms << 24);
     P.factor[i] = off;
     off += int64_t(2) * wrow_rank(P.code[i]) * S;
@@ -152,7 +165,7 @@ WPlan build_wplan(const WPlanRequest &rq) {
     const int32_t m = order[i];
     P.gen_u[i] = rq.u[m];
     P.gen_v[i] = rq.v[m];
-    P.gen_w[i] = rq.w[m] - wmean;
+    P.gen_w[i] = w_of(m);
     P.gen_jw[i] = jw[m];
   }
 
@@ -224,6 +237,11 @@ template <typename T>
 void wplan_factors(const WPlan &P, int64_t i0, int64_t i1, std::complex<T> *out) {
   const int J = P.J;
   const GriddingKernel kern(P.kernel, J, P.oversample_ratio);
+  // plain rows: details::init_gridding_matrix_2d receives (kernelv, kernelu)
+  // in its (u, v) slots (operators.h:322-324), so the u-axis taps use the
+  // kernel of support Jv and the v-axis taps the kernel of support Ju
+  const GriddingKernel kern_uslot(P.kernel, P.plain ? P.Jv : J, P.oversample_ratio);
+  const GriddingKernel kern_vslot(P.kernel, P.plain ? P.Ju : J, P.oversample_ratio);
   const double dul = P.du_lambda, dvl = P.dv_lambda;
   const int64_t base = i0 < int64_t(P.factor.size()) ? P.factor[i0] : 0;
 #pragma omp parallel
@@ -233,6 +251,25 @@ void wplan_factors(const WPlan &P, int64_t i0, int64_t i1, std::complex<T> *out)
 #pragma omp for schedule(dynamic, 1024)
     for (int64_t i = i0; i < i1; ++i) {
       const double u = P.gen_u[i], v = P.gen_v[i], w = P.gen_w[i];
+      if (P.plain) {
+        // operators.cc:8-46: taps at k + 1 .. k + Ju with k = floor(u - Ju / 2),
+        // which sit at offset k - kw inside the row of S = J cells placed at
+        // kw = floor(u - S / 2); zero elsewhere; the phase (-1)^j as below
+        const int S = J;
+        const double kwu = std::floor(u - S * 0.5), kwv = std::floor(v - S * 0.5);
+        const double ku = std::floor(u - P.Ju * 0.5), kv = std::floor(v - P.Jv * 0.5);
+        const int ou = int(ku - kwu), ov = int(kv - kwv);
+        for (int k = 0; k < 2 * S; ++k) row[k] = 0.0;
+        for (int j = 1; j <= P.Jv; ++j) row[ov + j - 1] = kern_vslot.value(v - (kv + j));
+        for (int j = 1; j <= P.Ju; ++j) row[S + ou + j - 1] = kern_uslot.value(u - (ku + j));
+        std::complex<T> *dst = out + (P.factor[i] - base);
+        for (int r = 0; r < 2; ++r)
+          for (int k = 0; k < S; ++k) {
+            const std::complex<double> z = (k & 1) ? -row[r * S + k] : row[r * S + k];
+            dst[r * S + k] = std::complex<T>(T(z.real()), T(z.imag()));
+          }
+        continue;
+      }
       const int Jw = P.gen_jw[i], S = Jw + J - 1;
       // Kaiser-Bessel (or other) taps: projection_kernels.cc:66-75
       const double du = u - std::floor(u - J * 0.5), dv = v - std::floor(v - J * 0.5);

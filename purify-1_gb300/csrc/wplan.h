@@ -33,11 +33,20 @@ struct WPlanRequest {
   int kernel = kKB;
   int tile = kTile;
   int64_t max_taps_per_task = 1 << 18;
+  // Plain separable rows (no w-term): each row is the Ju u-axis taps times
+  // the Jv v-axis taps, placed as details::init_gridding_matrix_2d places
+  // them (operators.cc:8-46) inside a square row of S = max(Ju, Jv) cells,
+  // rank 1.  Used for supports above the register-block kernels' limit and
+  // for Ju != Jv.  w and Jw are ignored.
+  bool plain = false;
+  int Ju = 4, Jv = 4;
 };
 
 struct WPlan {
   int64_t M = 0;
   int Nu = 0, Nv = 0, J = 0, Smax = 0;
+  bool plain = false;  // plain separable rows (WPlanRequest::plain)
+  int Ju = 0, Jv = 0;
   AxisTiling tu, tv;
   // per visibility in plan order (tile, then support descending)
   std::vector<int32_t> code;     // lp | lq << 8 | S << 16 | terms << 24 (see wrow_terms)

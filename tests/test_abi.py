@@ -53,8 +53,10 @@ def _create(pg, **kw):
 @pytest.mark.parametrize("kw,status", [
     (dict(kernel="pswf", Ju=4, Jv=4), 1),   # kernels.cc:241-244
     (dict(kernel=17), 1),                   # kernels.cc:320-321
-    (dict(Ju=4, Jv=6), 2),
-    (dict(Ju=9, Jv=9), 2),
+    (dict(Ju=4, Jv=6), 1),                  # KB: one axis outside its support (operators.h:322-324)
+    (dict(kernel="kbmin", Ju=6, Jv=4), 1),
+    (dict(kernel="gauss", Ju=4, Jv=6, w_term=True, w=np.zeros(4)), 2),
+    (dict(Ju=33, Jv=33), 2),
     (dict(imsizex=0), 1),
     (dict(oversample_ratio=0.0), 1),
 ])

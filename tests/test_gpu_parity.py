@@ -440,3 +440,33 @@ def test_caller_order_grid_is_bit_identical(pg, cuda, small_config, precision):
     f0, f1 = ops[0].forward(x), ops[1].forward(x)
     torch.cuda.synchronize()
     assert torch.equal(a0, a1) and torch.equal(f0, f1)
+
+
+@pytest.mark.parametrize("kernel,Ju,Jv", [("gauss", 4, 6), ("gauss", 6, 3), ("box", 3, 5),
+                                          ("gauss_alt", 2, 4), ("kb", 10, 10), ("gauss", 12, 12),
+                                          ("box", 16, 16), ("kbmin", 9, 9)])
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_unequal_and_wide_supports(pg, oracle_mod, cuda, kernel, Ju, Jv, precision):
+    """Ju != Jv and supports above 8 taps run as plain separable rows on the
+    row-factor kernels.  The reference builds G with the Jv kernel on the u
+    axis and the Ju kernel on the v axis (operators.h:322-324), which the
+    oracle restates; S uses ftu of Ju along x and ftv of Jv along y.  Forward,
+    adjoint (complex weights) and the power method against the oracle."""
+    torch = cuda
+    rng = np.random.default_rng(Ju * 10 + Jv)
+    M, n = 4000, 48
+    u = rng.normal(0, 15, M)
+    v = rng.normal(0, 15, M)
+    wt = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    gop = pg.MeasurementOperator(u, v, None, wt, n, n, 2.0, power_iters=0, kernel=kernel, Ju=Ju,
+                                 Jv=Jv, precision=precision)
+    oop = oracle_mod.Operator(u, v, None, wt, n, n, 2.0, kernel=kernel, Ju=Ju, Jv=Jv)
+    assert gop.info()["nnz"] == oop.nnz == M * Ju * Jv
+    x = rng.standard_normal(n * n) + 1j * rng.standard_normal(n * n)
+    y = to_np(gop.forward(to_dev(torch, x, precision)))
+    assert rel_l2(y, oop.forward(x)) < TOL[precision]
+    yy = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    xx = to_np(gop.adjoint(to_dev(torch, yy, precision)))
+    assert rel_l2(xx, oop.adjoint(yy)) < TOL[precision]
+    n_gpu, n_ref = gop.power_method(20, 0.0), oop.power_method(20, 0.0)
+    assert abs(n_gpu - n_ref) / n_ref < TOL[precision]
