@@ -413,6 +413,9 @@ typedef struct {
   int32_t device;
   int32_t slots;             /* requests in flight at most (1..64) */
   int64_t hbm_budget_bytes;  /* device bytes of the requests in flight */
+  int32_t norm_slots;        /* slots norm requests may hold (0: slots / 4, at least 1); they
+                                run on the lowest stream priority, other requests on the
+                                highest, so short requests are scheduled first */
 } purify_gb300_server_config;
 int purify_gb300_server_create(const purify_gb300_server_config *cfg, purify_gb300_server **out);
 /* Destroys after the requests already submitted have run. */

@@ -680,6 +680,7 @@ int purify_gb300_server_create(const purify_gb300_server_config *cfg, purify_gb3
     c.device = cfg->device;
     c.slots = cfg->slots;
     c.hbm_budget = cfg->hbm_budget_bytes;
+    c.norm_slots = cfg->norm_slots;
     std::unique_ptr<purify_gb300_server> h(new purify_gb300_server);
     h->impl.reset(new pg::Server(c));
     *out = h.release();

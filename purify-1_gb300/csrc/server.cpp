@@ -41,6 +41,7 @@ struct Server::Slot {
   std::map<int64_t, cufftHandle> plans;  // key: fp64 | Nu << 1 | Nv << 32
   std::map<int64_t, cufftHandle> col_plans;  // FP32 column transforms, same key
   bool busy = false;
+  bool long_slot = false;  // serves norm requests (lowest stream priority)
 };
 
 struct Server::Job {
@@ -59,6 +60,24 @@ struct Server::Job {
   double norm = 0;
   int iterations = 0;
 };
+
+// Host copies between the caller's vectors and pinned staging.  Large ones
+// are split over host threads: a single thread's memcpy is well below the
+// host memory bandwidth, and the submitting thread pays for it.
+static void copy_bytes(void *dst, const void *src, size_t bytes) {
+  constexpr size_t kParallelBytes = size_t(4) << 20;
+  if (bytes < kParallelBytes) {
+    std::memcpy(dst, src, bytes);
+    return;
+  }
+  const int64_t pieces = int64_t((bytes + (size_t(1) << 20) - 1) >> 20);
+#pragma omp parallel for schedule(static) num_threads(8)
+  for (int64_t k = 0; k < pieces; ++k) {
+    const size_t off = size_t(k) << 20;
+    std::memcpy(static_cast<char *>(dst) + off, static_cast<const char *>(src) + off,
+                std::min(size_t(1) << 20, bytes - off));
+  }
+}
 
 static int64_t plan_key(bool fp64, int Nu, int Nv) {
   return int64_t(fp64) | (int64_t(Nu) << 1) | (int64_t(Nv) << 32);
@@ -79,9 +98,19 @@ Server::Server(const ServerConfig &cfg) : cfg_(cfg) {
   uint64_t keep = uint64_t(cfg.hbm_budget);
   cuda_check(cudaMemPoolSetAttribute(pool_, cudaMemPoolAttrReleaseThreshold, &keep),
              "cudaMemPoolSetAttribute");
+  if (cfg.norm_slots < 0 || cfg.norm_slots > cfg.slots)
+    throw Error(kInvalidArgument, "norm_slots must be in [0, slots]");
+  norm_slots_ = cfg.norm_slots > 0 ? cfg.norm_slots : std::max(1, cfg.slots / 4);
+  // The first norm_slots_ slots are the long-request (norm) slots, on the
+  // lowest stream priority; the others on the highest.
+  int lo = 0, hi = 0;
+  cuda_check(cudaDeviceGetStreamPriorityRange(&lo, &hi), "cudaDeviceGetStreamPriorityRange");
   for (int k = 0; k < cfg.slots; ++k) {
     std::unique_ptr<Slot> s(new Slot);
-    cuda_check(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    s->long_slot = k < norm_slots_;
+    cuda_check(cudaStreamCreateWithPriority(&s->stream, cudaStreamNonBlocking,
+                                            s->long_slot ? lo : hi),
+               "cudaStreamCreateWithPriority");
     slots_.push_back(std::move(s));
   }
   stats_.bytes_budget = cfg.hbm_budget;
@@ -225,7 +254,7 @@ int64_t Server::submit(const Request &rq) {
   }
   if (j->in_bytes) {
     j->host_in = pinned(j->in_bytes);
-    std::memcpy(j->host_in, fwd ? rq.x_in : rq.vis_in, j->in_bytes);
+    copy_bytes(j->host_in, fwd ? rq.x_in : rq.vis_in, j->in_bytes);
   }
   if (j->out_bytes) j->host_out = pinned(j->out_bytes);
   int64_t ticket;
@@ -279,17 +308,33 @@ void Server::loop() {
     // it, so submit() and completions are not held up by a long request.
     std::vector<Job *> admitted;
     auto it = pending_.begin();
+    // the head waits for a slot of its class (not for the budget): other
+    // requests passing it then do not count as overtakes
+    bool head_class_blocked = false;
     while (it != pending_.end()) {
-      Slot *free = nullptr;
-      for (auto &s : slots_)
-        if (!s->busy) {
-          free = s.get();
-          break;
-        }
-      if (!free) break;
       Job &j = **it;
+      // norm requests: a free long slot only; others: a free short slot,
+      // else a free long slot
+      const bool long_job = j.rq.kind == kReqNorm;
+      Slot *free = nullptr;
+      for (int pass = 0; pass < 2 && !free; ++pass)
+        for (auto &s : slots_)
+          if (!s->busy && s->long_slot == (long_job || pass == 1)) {
+            free = s.get();
+            break;
+          }
+      if (!free) {
+        bool any = false;
+        for (auto &s : slots_) any |= !s->busy;
+        if (!any) break;
+        // only slots of the other class are free: look further down the queue
+        if (it == pending_.begin()) head_class_blocked = true;
+        if (!head_class_blocked && pending_.front()->overtaken >= kMaxOvertakes) break;
+        ++it;
+        continue;
+      }
       if (bytes_in_use_ + j.bytes <= cfg_.hbm_budget) {
-        if (it != pending_.begin()) ++pending_.front()->overtaken;
+        if (it != pending_.begin() && !head_class_blocked) ++pending_.front()->overtaken;
         reserve(j, *free);
         admitted.push_back(&j);
         it = pending_.erase(it);
@@ -471,10 +516,10 @@ bool Server::wait(int64_t ticket, double timeout_s, RequestResult *out) {
   if (j->status == kOk && j->rq.kind != kReqNorm) {
     const char *src = static_cast<const char *>(j->host_out);
     if (j->rq.kind != kReqAdjoint && c.M > 0) {
-      std::memcpy(j->rq.vis_out, src, 16 * size_t(c.M));
+      copy_bytes(j->rq.vis_out, src, 16 * size_t(c.M));
       src += 16 * size_t(c.M);
     }
-    if (j->rq.kind != kReqForward) std::memcpy(j->rq.x_out, src, 16 * size_t(c.N));
+    if (j->rq.kind != kReqForward) copy_bytes(j->rq.x_out, src, 16 * size_t(c.N));
   }
   if (out) {
     out->status = j->status;

@@ -36,6 +36,11 @@ struct ServerConfig {
   int device = 0;
   int slots = 8;                  // requests in flight at most (one stream each)
   int64_t hbm_budget = 8LL << 30; // device bytes of the requests in flight
+  // Slots norm requests (many rounds each) may hold at once; 0: a quarter of
+  // the slots, at least one.  They run on low-priority streams, the other
+  // requests on high-priority ones, so the block scheduler serves short
+  // requests first when both wait.
+  int norm_slots = 0;
 };
 
 // Host buffers are complex<double> (interleaved), as the host entry points.
@@ -112,6 +117,7 @@ class Server {
   std::vector<double> latencies_;
   std::multimap<size_t, void *> pinned_free_;
   mutable std::mutex mu_;
+  int norm_slots_ = 1;  // slots that take norm requests (the first ones)
   std::condition_variable cv_;       // scheduler wake-ups
   std::condition_variable done_cv_;  // request completions
   bool stop_ = false, dirty_ = false;

@@ -96,7 +96,7 @@ class BatchInfo(ctypes.Structure):
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("slots", ctypes.c_int32),
-                ("hbm_budget_bytes", ctypes.c_int64)]
+                ("hbm_budget_bytes", ctypes.c_int64), ("norm_slots", ctypes.c_int32)]
 
 
 class Request(ctypes.Structure):
@@ -769,9 +769,9 @@ class Server:
     with its own workspace (see include/purify_gb300.h).  Host vectors are
     complex128 numpy arrays."""
 
-    def __init__(self, device=0, slots=8, hbm_budget=8 << 30):
+    def __init__(self, device=0, slots=8, hbm_budget=8 << 30, norm_slots=0):
         L = load()
-        cfg = ServerConfig(int(device), int(slots), int(hbm_budget))
+        cfg = ServerConfig(int(device), int(slots), int(hbm_budget), int(norm_slots))
         h = ctypes.c_void_p()
         _check(L.purify_gb300_server_create(ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h

@@ -147,3 +147,23 @@ def test_w_projection_coverage(pg, cuda):
     assert np.array_equal(r["x"], op.adjoint(y))
     r = srv.wait(srv.submit(cid, "norm", iters=10, tol=0.0))
     assert r["norm"] == op.power_method(10, 0.0)
+
+
+def test_norm_slots_and_priorities(pg, cuda):
+    """Norm requests hold at most norm_slots slots (low stream priority);
+    short requests take the high-priority slots first, else any free slot.
+    A mix submitted in one burst completes, each result equal to the same
+    request alone; norm_slots outside [0, slots] is refused."""
+    covs = coverages()
+    srv = pg.Server(slots=4, hbm_budget=4 << 30, norm_slots=1)
+    ids = add_all(srv, covs)
+    reqs = requests(covs, ids, n=20, seed=21)
+    # the norms first, so short requests pass norms that wait for the one long slot
+    reqs.sort(key=lambda q: q["kind"] != "norm")
+    mix = run_mix(srv, reqs)
+    assert all(r["status"] == 0 for r in mix)
+    assert srv.stats()["completed"] == len(reqs)
+    for q, m in zip(reqs, mix):
+        same(srv.wait(srv.submit(q["coverage"], q["kind"], q["x"], q["vis"], q["iters"])), m)
+    with pytest.raises(pg.PurifyError):
+        pg.Server(slots=2, norm_slots=3)
