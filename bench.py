@@ -70,6 +70,8 @@ def parse():
                    help="base cells per work item along each axis: 1, 2, or 0 for the default")
     p.add_argument("--class-cap", type=int, default=0,
                    help="most items of one bank class per batch (0: default; tuning)")
+    p.add_argument("--keep-store", type=int, default=0,
+                   help="1: Phi stores its caller-ordered output at L2 evict-last priority (tuning)")
     p.add_argument("--fused-permute", type=int, default=-1,
                    help="1: degrid/grid touch caller order directly, 0: gather kernels, "
                         "-1: default per direction (tuning)")
@@ -80,7 +82,7 @@ def tuning_of(args):
     """Tuning dict of the --threads / --max-per-item / --tile flags (None: defaults)."""
     t = {k: v for k, v in (("threads", args.threads), ("max_per_item", args.max_per_item),
                            ("tile", args.tile), ("cell_group", args.cell_group),
-                           ("class_cap", args.class_cap)) if v}
+                           ("class_cap", args.class_cap), ("keep_store", args.keep_store)) if v}
     if args.fused_permute >= 0:
         t["fused_permute"] = args.fused_permute
     return t or None

@@ -110,6 +110,8 @@ typedef struct {
                             or 0: 2 where allowed, else 1 */
   int32_t class_cap;     /* most items of one shared-memory bank class in a batch of 32
                             (1 .. 16), or 0 for the default */
+  int32_t keep_store;    /* 1: Phi's caller-ordered output is stored at L2 evict-last
+                            priority (when it fits the L2 share), for a following Phi^H */
 } purify_gb300_tuning;
 int purify_gb300_operator_create_tuned(const purify_gb300_create_args *args,
                                        const purify_gb300_tuning *tuning,

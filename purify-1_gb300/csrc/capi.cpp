@@ -122,6 +122,7 @@ pg::OperatorConfig to_config(const purify_gb300_create_args *a, const purify_gb3
     c.fused_permute = t->fused_permute;
     c.cell_group = t->cell_group;
     c.class_cap = t->class_cap;
+    c.keep_store = t->keep_store;
   }
   if (a->precision != PURIFY_GB300_FP32 && a->precision != PURIFY_GB300_FP64)
     throw pg::Error(pg::kInvalidArgument, "unknown precision");

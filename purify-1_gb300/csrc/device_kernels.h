@@ -30,8 +30,9 @@ struct ApplyArgs {
   int Nu = 0, Nv = 0;
   int win_stride = 0;               // row stride of the shared-memory windows (plan's win_stride)
   int group_cells = 1;              // cells per work item along each axis (plan's group)
-  // grid kernel reading caller order (slot_user set): gather at L2
-  // evict-last priority, so the caller-ordered vector stays in L2
+  // caller order (slot_user set): the grid kernel gathers and the degrid
+  // kernel stores the caller-ordered vector at L2 evict-last priority, so it
+  // stays in L2 between the two
   int keep_in = 0;
   int64_t slot_stride = 0;          // complex elements per tilebuf slot
   int win_bytes = 0;    // set by the launchers: shared bytes before the batch headers

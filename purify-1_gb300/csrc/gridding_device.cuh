@@ -170,6 +170,16 @@ __device__ __forceinline__ double2 load_keep(const double2 *p, unsigned long lon
                : "l"(p), "l"(pol));
   return v;
 }
+__device__ __forceinline__ void store_keep(float2 *p, float2 v, unsigned long long pol) {
+  asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(p), "f"(v.x), "f"(v.y),
+               "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ void store_keep(double2 *p, double2 v, unsigned long long pol) {
+  asm volatile("st.global.L2::cache_hint.v2.f64 [%0], {%1, %2}, %3;" ::"l"(p), "d"(v.x), "d"(v.y),
+               "l"(pol)
+               : "memory");
+}
 template <typename real>
 __device__ __forceinline__ cplx<real> gather_vis(const cplx<real> *vin, int m, bool keep,
                                                 unsigned long long pol) {
@@ -266,11 +276,14 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
   const C *frac = static_cast<const C *>(a.frac);
   const int32_t *user = a.slot_user;
   C *out = static_cast<C *>(a.slot_out);
+  // caller-ordered output kept in L2 (evict-last) for the adjoint's gather
+  const bool keep = a.keep_in != 0;
   if (warp >= nbt) return;
   unsigned char *stg = smem_raw + a0.win_bytes + kHeaderBytes + size_t(warp) * a0.stage_bytes;
   C *st_t = reinterpret_cast<C *>(stg);
   int *st_m = reinterpret_cast<int *>(stg + 2 * CH * 32 * sizeof(C));
   const unsigned long long pol = l2_stream_policy();
+  const unsigned long long kpol = l2_keep_policy();
   auto issue = [&](int lb, int k0, int buf) {
     const int2 bt = th.hdr[lb];
     const int n = min(CH, bt.y - k0);
@@ -331,7 +344,12 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
         out[size_t(bt.x) + size_t(k) * kBatch + lane] = k < cnt ? y : C{0, 0};
       } else {
         const int m = st_m[e];
-        if (m >= 0) out[m] = y;
+        if (m >= 0) {
+          if (keep)
+            store_keep(out + m, y, kpol);
+          else
+            out[m] = y;
+        }
       }
     }
     buf ^= 1;

@@ -145,6 +145,8 @@ class OperatorT final : public Operator {
   // the operator's own scratch: applies on other workspaces run concurrently
   // (the server), and several kept vectors would crowd each other out.
   bool keep_vis_l2_ = false;
+  // degrid stores the caller-ordered output at evict-last priority too
+  bool keep_store_ = false;
   double norm_ = 1.0;
   std::vector<double> su_, sv_;  // 1 / ft kernel at the image pixels (unscaled)
   std::vector<real> su_scaled_, sv_real_;
@@ -245,6 +247,7 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
   // the slot-ordered buffer.
   fused_forward_ = !wmode_ && cfg.fused_permute != 0;
   keep_vis_l2_ = int64_t(sizeof(C)) * M_ <= kKeepVisL2Bytes;
+  keep_store_ = cfg.keep_store != 0;
   fused_adjoint_ = !wmode_ && cfg.fused_permute == 1;
 
   cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
@@ -618,6 +621,7 @@ void OperatorT<real>::degrid_slots(const void *grid, void *caller_vis) {
   a.frac = frac_.get();
   a.slot_out = caller_vis ? caller_vis : ws_->slots;
   a.slot_user = caller_vis ? slot_user_.as<int32_t>() : nullptr;
+  a.keep_in = (caller_vis && keep_store_ && keep_vis_l2_ && ws_ == &own_) ? 1 : 0;
   a.Nu = Nu_;
   a.Nv = Nv_;
   a.win_stride = win_stride_;

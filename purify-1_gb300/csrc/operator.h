@@ -50,6 +50,8 @@ struct OperatorConfig {
   int cell_group = 0;
   // most items of one bank class per batch (0: the planner's default)
   int class_cap = 0;
+  // 1: the forward's caller-ordered output is stored at L2 evict-last priority
+  int keep_store = 0;
 };
 
 // A plan fraction t + d (see PlanRequest::group) in precision `real`, kept

@@ -54,7 +54,8 @@ class CreateArgs(ctypes.Structure):
 class Tuning(ctypes.Structure):
     _fields_ = [("threads", ctypes.c_int32), ("max_per_item", ctypes.c_int32),
                 ("tile", ctypes.c_int32), ("fused_permute", ctypes.c_int32),
-                ("cell_group", ctypes.c_int32), ("class_cap", ctypes.c_int32)]
+                ("cell_group", ctypes.c_int32), ("class_cap", ctypes.c_int32),
+                ("keep_store", ctypes.c_int32)]
 
 
 class Info(ctypes.Structure):
@@ -441,7 +442,8 @@ class MeasurementOperator:
         if tuning:
             t = Tuning(int(tuning.get("threads", 0)), int(tuning.get("max_per_item", 0)),
                        int(tuning.get("tile", 0)), int(tuning.get("fused_permute", -1)),
-                       int(tuning.get("cell_group", 0)), int(tuning.get("class_cap", 0)))
+                       int(tuning.get("cell_group", 0)), int(tuning.get("class_cap", 0)),
+                       int(tuning.get("keep_store", 0)))
             _check(L.purify_gb300_operator_create_tuned(ctypes.byref(a), ctypes.byref(t),
                                                         ctypes.byref(h)))
         else:
