@@ -281,16 +281,17 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------- GPU ----
-def kernel_bytes(info, s, caller_order_out=True, unit_weights=True):
+def kernel_bytes(info, s, caller_order_out=True):
     """Bytes each gridding-chain kernel's own arguments carry per launch
     (complex values of s bytes): what the kernel must read or write at least
-    once, independent of how it does it.
+    once, independent of how it does it.  Weights are not among them: a
+    weighted operator applies them in separate elementwise passes.
 
-    degrid: the grid once, per slot t (s) [+ weight (s)] [+ caller index (4)
-            when it writes caller order], lane codes and batch headers, and
-            the M visibilities it writes;
-    grid:   per slot t and the slot-ordered visibility (2 s) [+ weight],
-            lane codes and headers, and the task windows it writes;
+    degrid: the grid once, per slot t (s) [+ caller index (4) when it writes
+            caller order], lane codes and batch headers, and the M
+            visibilities it writes;
+    grid:   per slot t and the slot-ordered visibility (2 s), lane codes and
+            headers, and the task windows it writes;
     expand: per slot the caller index (4) and the slot written (s), and the M
             caller-ordered visibilities read;
     fold:   the task windows read and the grid written."""
@@ -299,10 +300,9 @@ def kernel_bytes(info, s, caller_order_out=True, unit_weights=True):
     items = info["work_items"]
     lanes = 4 * items + 8 * (items // 32)
     windows = s * info["tasks"] * info["window_cells"]
-    wt = 0 if unit_weights else s * S
     return {
-        "degrid": s * NuNv + s * S + wt + (4 * S if caller_order_out else 0) + lanes + s * M,
-        "grid": 2 * s * S + wt + lanes + windows,
+        "degrid": s * NuNv + s * S + (4 * S if caller_order_out else 0) + lanes + s * M,
+        "grid": 2 * s * S + lanes + windows,
         "expand": 4 * S + s * S + s * M,
         "fold": windows + s * NuNv,
     }
@@ -522,6 +522,23 @@ def run_gb300(args):
                                                     "rows": 20000}
         except Exception as e:  # the oracle is a checker only
             out["rel_l2_vs_oracle_forward_rows"] = {"error": str(e)}
+        # the full-size adjoint of a y that is zero outside the row sample
+        # equals the sampled operator's adjoint (G^H is linear in y)
+        try:
+            rng = np.random.default_rng(8)
+            ys = rng.standard_normal(idx.size) + 1j * rng.standard_normal(idx.size)
+            yfull = torch.zeros(M, dtype=torch.complex128)
+            yfull[torch.from_numpy(idx)] = torch.from_numpy(ys)
+            y64.copy_(yfull.to(dev))
+            op64.adjoint_into(y64, xo64, stream)
+            op.adjoint_into(y64.to(torch.complex64), xo, stream)
+            torch.cuda.synchronize(dev)
+            xr = ref.adjoint(ys)
+            out["rel_l2_vs_oracle_adjoint_sample"] = {"fp32": rel_l2(xo.cpu().numpy(), xr),
+                                                      "fp64": rel_l2(xo64.cpu().numpy(), xr),
+                                                      "rows": int(idx.size)}
+        except Exception as e:
+            out["rel_l2_vs_oracle_adjoint_sample"] = {"error": str(e)}
         del op64
 
     # end to end through the host complex<double> entry points, pinned buffers
