@@ -70,6 +70,8 @@ def parse():
                    help="base cells per work item along each axis: 1, 2, or 0 for the default")
     p.add_argument("--class-cap", type=int, default=0,
                    help="most items of one bank class per batch (0: default; tuning)")
+    p.add_argument("--fft-columns", type=int, default=0,
+                   help="1: cuFFT's column plan instead of the column pass (tuning)")
     p.add_argument("--keep-store", type=int, default=0,
                    help="1: Phi stores its caller-ordered output at L2 evict-last priority (tuning)")
     p.add_argument("--fused-permute", type=int, default=-1,
@@ -82,7 +84,8 @@ def tuning_of(args):
     """Tuning dict of the --threads / --max-per-item / --tile flags (None: defaults)."""
     t = {k: v for k, v in (("threads", args.threads), ("max_per_item", args.max_per_item),
                            ("tile", args.tile), ("cell_group", args.cell_group),
-                           ("class_cap", args.class_cap), ("keep_store", args.keep_store)) if v}
+                           ("class_cap", args.class_cap), ("keep_store", args.keep_store),
+                           ("fft_columns", args.fft_columns)) if v}
     if args.fused_permute >= 0:
         t["fused_permute"] = args.fused_permute
     return t or None
@@ -744,6 +747,11 @@ def run_batch(args):
     b = pgb.Batch(chans, J=4, precision="fp32")
     t_create = time.perf_counter() - t0
     tuning = b.tuning
+    if args.fft_columns:
+        # the autotuned shapes with the other column transform (A/B)
+        b.close()
+        tuning["fft_columns"] = args.fft_columns
+        b = pgb.Batch(chans, J=4, precision="fp32", tuning=tuning)
     t0 = time.perf_counter()
     norms = b.power_method(args.power_iters, 1e-4) if args.power_iters > 0 else np.ones(len(chans))
     t_power = time.perf_counter() - t0

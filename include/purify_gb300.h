@@ -112,6 +112,9 @@ typedef struct {
                             (1 .. 16), or 0 for the default */
   int32_t keep_store;    /* 1: Phi's caller-ordered output is stored at L2 evict-last
                             priority (when it fits the L2 share), for a following Phi^H */
+  int32_t fft_columns;   /* column transforms of the FP32 power-of-two FFT path: 0 = the
+                            library's column pass (grid height <= 2048), 1 = cuFFT's
+                            strided column plan */
 } purify_gb300_tuning;
 int purify_gb300_operator_create_tuned(const purify_gb300_create_args *args,
                                        const purify_gb300_tuning *tuning,
@@ -327,6 +330,8 @@ typedef struct {
   int32_t degrid_threads;  /* CTA threads of the grouped degrid launch */
   int32_t grid_threads;    /* CTA threads of the grouped grid launch */
   int32_t cell_group;      /* base cells per work item along each axis (1, or 2 for FP32, J <= 6) */
+  int32_t fft_columns;     /* column transforms of FP32 power-of-two grids: 0 = the library's
+                              column pass (grid height <= 2048), 1 = cuFFT's strided plan */
 } purify_gb300_batch_tuning;
 /* Builds the batch (plans every channel, uploads the coverage state).  With
  * tuning == NULL the autotuner picks the tile edge and CTA sizes by timing

@@ -10,11 +10,13 @@
 #include <mutex>
 #include <numeric>
 #include <sstream>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
 #include "device_kernels.h"
 #include "device_util.h"
+#include "fft_kernels.h"
 #include "gridding_kernels.h"
 #include "plan.h"
 
@@ -77,13 +79,26 @@ class BatchT final : public Batch {
            o_tv_of = 0, o_su = 0, o_sv = 0, o_tilebuf = 0, o_slots = 0, o_pm_x = 0, o_pm_vis = 0,
            o_wvis = 0;
   };
+  // Channels of one grid size.  FP32 groups of a power-of-two width are
+  // "fused": their grids are interleaved by rows (row r of the group holds
+  // row r of every member, member k at columns k Nu ..., row stride
+  // ld = members x Nu), the padding and the row FFTs of all members run as
+  // one row-pass launch, and one column pass (launch_fft_cols; a strided
+  // cuFFT plan where that does not apply) transforms every member's columns.
+  // The other groups keep contiguous grids (ld = Nu), a batched 2-D plan and
+  // the grouped pad / crop kernels.
   struct SizeGroup {
     int Nu = 0, Nv = 0;
     std::vector<int> chans;
     size_t o_pad = 0, o_work = 0;
-    cufftHandle fft = 0;
+    cufftHandle fft = 0;  // fused: the cuFFT column plan (if any); else the batched 2-D plan
     bool fft_ok = false;
+    bool fused = false, own_cols = false;
+    int ld = 0, max_ny = 0;
+    // fused: member channel indices, row and column twiddles
+    size_t o_members = 0, o_tw = 0, o_twv = 0;
   };
+  FftColArgs col_args(const SizeGroup &g, bool inverse) const;
   void upload_corrections();
   void upload_tables(cudaStream_t s);
   void record(int mode);
@@ -94,13 +109,16 @@ class BatchT final : public Batch {
   void bind_internal();
   void join(cudaStream_t user);
   void release(cudaStream_t user);
-  void *pad_of(int c) const {
+  // a channel's grids inside its group's buffers
+  size_t grid_offset(int c) const {
     const SizeGroup &g = groups_[chans_[c].group];
-    return shared_.at<C>(g.o_pad) + size_t(chans_[c].in_group) * g.Nu * g.Nv;
+    return size_t(chans_[c].in_group) * size_t(g.Nu) * (g.fused ? 1 : size_t(g.Nv));
+  }
+  void *pad_of(int c) const {
+    return shared_.at<C>(groups_[chans_[c].group].o_pad) + grid_offset(c);
   }
   void *work_of(int c) const {
-    const SizeGroup &g = groups_[chans_[c].group];
-    return shared_.at<C>(g.o_work) + size_t(chans_[c].in_group) * g.Nu * g.Nv;
+    return shared_.at<C>(groups_[chans_[c].group].o_work) + grid_offset(c);
   }
 
   int device_ = 0, J_ = 0, nch_ = 0;
@@ -112,11 +130,13 @@ class BatchT final : public Batch {
   int ntasks_ = 0, win_rows_ = 0, win_cols_ = 0;
   Arena shared_;  // grouped task list, argument tables, padded and FFT grids
   size_t o_tasks_ = 0, o_task_base_ = 0, o_fwd_ = 0, o_adj_ = 0, o_folds_ = 0, o_io_ = 0,
-         o_partial_ = 0, o_sq_ = 0, o_inv_ = 0, o_map_pix_ = 0, o_map_slot_ = 0, o_map_tile_ = 0,
+         o_partial_ = 0, o_sq_ = 0, o_inv_ = 0, o_map_pix_ = 0, o_map_pad_ = 0, o_map_slot_ = 0,
+         o_map_tile_ = 0,
          o_map_wvis_ = 0,
          o_order_ = 0;
   // block maps of the grouped element-wise launches: {channel, block}
   std::vector<int2> map_pix_, map_slot_, map_tile_;
+  std::vector<int2> map_pad_;  // pixels of the channels of unfused size groups (pad / crop)
   std::vector<int2> map_wvis_;  // caller-ordered visibilities of the channels with weights
   std::vector<ApplyArgs<real>> fwd_, adj_;
   std::vector<FoldArgs> folds_;
@@ -306,14 +326,25 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
   }
   info_.size_groups = int(groups_.size());
   for (SizeGroup &g : groups_) {
+    g.fused = std::is_same<real, float>::value && fft_rows_supported(g.Nu);
+    g.ld = g.fused ? g.Nu * int(g.chans.size()) : g.Nu;
+    for (int c : g.chans) g.max_ny = std::max(g.max_ny, chans_[c].Ny);
     const size_t gb = sizeof(C) * size_t(g.Nu) * g.Nv * g.chans.size();
     g.o_pad = shared_.reserve(gb);
     g.o_work = shared_.reserve(gb);
+    if (g.fused) {
+      g.own_cols = cfg.fft_columns != 1 && fft_cols_supported(g.Nv, g.ld);
+      g.o_members = shared_.reserve(sizeof(int) * g.chans.size());
+      g.o_tw = shared_.reserve(2 * sizeof(float) * size_t(g.Nu));
+      g.o_twv = shared_.reserve(2 * sizeof(float) * size_t(g.Nv));
+    }
   }
   for (int c = 0; c < nch_; ++c) {
     const Chan &ch = chans_[c];
     const int64_t npix = (int64_t(ch.Nx) * ch.Ny + kGroupPixels - 1) / kGroupPixels;
     for (int64_t k = 0; k < npix; ++k) map_pix_.push_back(int2{c, int(k)});
+    if (!groups_[ch.group].fused)
+      for (int64_t k = 0; k < npix; ++k) map_pad_.push_back(int2{c, int(k)});
     const int64_t nsl = (ch.S + kGroupSlots - 1) / kGroupSlots;
     for (int64_t k = 0; k < nsl; ++k) map_slot_.push_back(int2{c, int(k)});
     for (int k = 0; k < ch.ntu * ch.ntv; ++k) map_tile_.push_back(int2{c, k});
@@ -322,6 +353,7 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
         map_wvis_.push_back(int2{c, int(k)});
   }
   o_map_pix_ = shared_.reserve(sizeof(int2) * map_pix_.size());
+  o_map_pad_ = shared_.reserve(sizeof(int2) * map_pad_.size());
   o_map_slot_ = shared_.reserve(sizeof(int2) * map_slot_.size());
   o_map_tile_ = shared_.reserve(sizeof(int2) * map_tile_.size());
   o_map_wvis_ = shared_.reserve(sizeof(int2) * map_wvis_.size());
@@ -351,13 +383,35 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
   cuda_check(cudaMemcpyAsync(shared_.at<char>(o_task_base_), task_base.data(),
                              sizeof(int32_t) * nch_, cudaMemcpyHostToDevice, stream_),
              "upload");
-  for (auto m : {std::make_pair(&map_pix_, o_map_pix_), std::make_pair(&map_slot_, o_map_slot_),
+  for (auto m : {std::make_pair(&map_pix_, o_map_pix_), std::make_pair(&map_pad_, o_map_pad_),
+                 std::make_pair(&map_slot_, o_map_slot_),
                  std::make_pair(&map_tile_, o_map_tile_), std::make_pair(&map_wvis_, o_map_wvis_)})
     if (!m.first->empty())
       cuda_check(cudaMemcpyAsync(shared_.at<char>(m.second), m.first->data(),
                                  sizeof(int2) * m.first->size(), cudaMemcpyHostToDevice, stream_),
                  "upload");
   for (SizeGroup &g : groups_) {
+    if (g.fused) {
+      // columns of the interleaved group: ld columns of Nv cells, stride ld
+      if (!g.own_cols) {
+        g.fft = make_column_plan<real>(g.ld, g.Nv, stream_, &info_.device_bytes);
+        g.fft_ok = true;
+      }
+      const std::vector<float> twv = fft_twiddles(g.Nv);
+      cuda_check(cudaMemcpyAsync(shared_.at<char>(g.o_twv), twv.data(), sizeof(float) * twv.size(),
+                                 cudaMemcpyHostToDevice, stream_),
+                 "upload");
+      cuda_check(cudaMemcpyAsync(shared_.at<char>(g.o_members), g.chans.data(),
+                                 sizeof(int) * g.chans.size(), cudaMemcpyHostToDevice, stream_),
+                 "upload");
+      const std::vector<float> tw = fft_twiddles(g.Nu);
+      cuda_check(cudaMemcpyAsync(shared_.at<char>(g.o_tw), tw.data(), sizeof(float) * tw.size(),
+                                 cudaMemcpyHostToDevice, stream_),
+                 "upload");
+      // the pageable sources above must outlive their staging
+      cuda_check(cudaStreamSynchronize(stream_), "upload");
+      continue;
+    }
     int n[2] = {g.Nv, g.Nu};
     const int dist = g.Nu * g.Nv;
     cufft_check(cufftPlanMany(&g.fft, 2, n, nullptr, 1, dist, nullptr, 1, dist,
@@ -383,6 +437,7 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     a.frac = m.at<char>(ch.o_frac);
     a.Nu = ch.Nu;
     a.Nv = ch.Nv;
+    a.ld = groups_[ch.group].ld;
     a.win_stride = ch.win_stride;
     a.group_cells = cfg_group_;
     a.slot_stride = ch.slot_stride;
@@ -407,6 +462,7 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     f.Ju = f.Jv = J_ + cfg_group_ - 1;  // windows reach JB - 1 cells into the next tiles
     f.Nu = ch.Nu;
     f.Nv = ch.Nv;
+    f.ld = groups_[ch.group].ld;
     f.grid = work_of(c);
     ChannelIO<real> &io = io_[c];
     io.su = m.at<real>(ch.o_su);
@@ -422,6 +478,7 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     io.Ny = ch.Ny;
     io.Nu = ch.Nu;
     io.Nv = ch.Nv;
+    io.ld = groups_[ch.group].ld;
     io.x0 = ch.x0;
     io.y0 = ch.y0;
     io.M = ch.M;
@@ -523,13 +580,27 @@ void BatchT<real>::record(int mode) {
     return;
   }
   if (mode & kForward) {
-    cuda_check(launch_pad_group<real>(io, shared_.at<int2>(o_map_pix_), int(map_pix_.size()),
-                                      stream_),
-               "pad");
-    for (SizeGroup &g : groups_)
+    if (!map_pad_.empty())
+      cuda_check(launch_pad_group<real>(io, shared_.at<int2>(o_map_pad_), int(map_pad_.size()),
+                                        stream_),
+                 "pad");
+    for (SizeGroup &g : groups_) {
+      if (g.fused) {
+        // S, padding and the row FFT of every member's image rows into the
+        // group's padded grid (its other rows stay zero), then the columns
+        cuda_check(launch_fft_rows_group(false, io, shared_.at<int>(g.o_members),
+                                         int(g.chans.size()), g.Nu, g.max_ny, g.ld,
+                                         shared_.at<char>(g.o_tw), stream_),
+                   "row pass");
+        if (g.own_cols) {
+          cuda_check(launch_fft_cols(false, col_args(g, false), stream_), "column pass");
+          continue;
+        }
+      }
       cufft_check(Traits<real>::exec(g.fft, shared_.at<C>(g.o_pad), shared_.at<C>(g.o_work),
                                      CUFFT_FORWARD),
                   "cufftExec");
+    }
     head.group = shared_.at<ApplyArgs<real>>(o_fwd_);
     cuda_check(launch_degrid_group<real>(head, poly_, J_, ntasks_, win_rows_, win_cols_,
                                          degrid_shape_, true, stream_),
@@ -549,18 +620,45 @@ void BatchT<real>::record(int mode) {
     cuda_check(launch_fold_group<real>(shared_.at<FoldArgs>(o_folds_), shared_.at<int2>(o_map_tile_),
                                        int(map_tile_.size()), stream_),
                "fold");
-    for (SizeGroup &g : groups_)
-      cufft_check(Traits<real>::exec(g.fft, shared_.at<C>(g.o_work), shared_.at<C>(g.o_work),
-                                     CUFFT_INVERSE),
-                  "cufftExec");
-    cuda_check(launch_crop_group<real>(io, shared_.at<int2>(o_map_pix_), int(map_pix_.size()),
-                                       stream_),
-               "crop");
+    for (SizeGroup &g : groups_) {
+      if (g.own_cols)
+        cuda_check(launch_fft_cols(true, col_args(g, true), stream_), "column pass");
+      else
+        cufft_check(Traits<real>::exec(g.fft, shared_.at<C>(g.o_work), shared_.at<C>(g.o_work),
+                                       CUFFT_INVERSE),
+                    "cufftExec");
+      if (g.fused)
+        cuda_check(launch_fft_rows_group(true, io, shared_.at<int>(g.o_members),
+                                         int(g.chans.size()), g.Nu, g.max_ny, g.ld,
+                                         shared_.at<char>(g.o_tw), stream_),
+                   "row pass");
+    }
+    if (!map_pad_.empty())
+      cuda_check(launch_crop_group<real>(io, shared_.at<int2>(o_map_pad_), int(map_pad_.size()),
+                                         stream_),
+                 "crop");
   }
   if (mode == kPower)
     cuda_check(launch_sq_norm_group<real>(io, nch_, shared_.at<double>(o_partial_),
                                           shared_.at<double>(o_sq_), stream_),
                "norm");
+}
+
+// The column pass of a fused size group: forward pad -> work (reading each
+// member's image rows only), inverse work -> work in place (writing them only).
+template <typename real>
+FftColArgs BatchT<real>::col_args(const SizeGroup &g, bool inverse) const {
+  FftColArgs c;
+  c.in = shared_.at<C>(inverse ? g.o_work : g.o_pad);
+  c.out = shared_.at<C>(g.o_work);
+  c.Nv = g.Nv;
+  c.W = g.ld;
+  c.ld = g.ld;
+  c.tw_v = shared_.at<char>(g.o_twv);
+  c.chans = shared_.at<char>(o_io_);
+  c.members = shared_.at<int>(g.o_members);
+  c.Nu = g.Nu;
+  return c;
 }
 
 template <typename real>

@@ -36,6 +36,9 @@ struct BatchConfig {
   int max_per_item = 16;
   int tile = kTile;
   int cell_group = 1;       // cells per work item along each axis (1, or 2 for FP32, J <= 6)
+  // column transforms of the fused size groups: 0 = launch_fft_cols where it
+  // applies, 1 = a strided cuFFT plan
+  int fft_columns = 0;
 };
 
 struct BatchInfo {
@@ -77,6 +80,7 @@ class Batch {
 struct BatchTuning {
   int tile = kTile, max_per_item = 16, degrid_threads = 128, grid_threads = 128;
   int cell_group = 1;
+  int fft_columns = 0;
 };
 
 // Picks the uv tile edge, the work-item shape (single cells or 2 x 2 groups)

@@ -33,7 +33,7 @@ __global__ void pad_group_kernel(const ChannelIO<real> *__restrict__ chans,
   const int j = int(idx / c.Nx), i = int(idx - int64_t(j) * c.Nx);
   const real s = c.su[i] * c.sv[j];
   const cplx<real> v = static_cast<const cplx<real> *>(c.x_in)[idx];
-  static_cast<cplx<real> *>(c.pad)[int64_t(c.y0 + j) * c.Nu + c.x0 + i] =
+  static_cast<cplx<real> *>(c.pad)[int64_t(c.y0 + j) * (c.ld ? c.ld : c.Nu) + c.x0 + i] =
       cplx<real>{s * v.x, s * v.y};
 }
 template <typename real>
@@ -45,7 +45,8 @@ __global__ void crop_group_kernel(const ChannelIO<real> *__restrict__ chans,
   if (idx >= int64_t(c.Nx) * c.Ny) return;
   const int j = int(idx / c.Nx), i = int(idx - int64_t(j) * c.Nx);
   const real s = c.su[i] * c.sv[j];
-  const cplx<real> v = static_cast<const cplx<real> *>(c.work)[int64_t(c.y0 + j) * c.Nu + c.x0 + i];
+  const cplx<real> v =
+      static_cast<const cplx<real> *>(c.work)[int64_t(c.y0 + j) * (c.ld ? c.ld : c.Nu) + c.x0 + i];
   static_cast<cplx<real> *>(c.x_out)[idx] = cplx<real>{s * v.x, s * v.y};
 }
 // slots[s] = in[slot_user[s]] (0 for null slots): a block covers 4 * 256

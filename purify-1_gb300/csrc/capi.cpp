@@ -123,6 +123,7 @@ pg::OperatorConfig to_config(const purify_gb300_create_args *a, const purify_gb3
     c.cell_group = t->cell_group;
     c.class_cap = t->class_cap;
     c.keep_store = t->keep_store;
+    c.fft_columns = t->fft_columns;
   }
   if (a->precision != PURIFY_GB300_FP32 && a->precision != PURIFY_GB300_FP64)
     throw pg::Error(pg::kInvalidArgument, "unknown precision");
@@ -599,11 +600,13 @@ int purify_gb300_batch_create(const purify_gb300_channel *channels, int32_t nch,
       t.degrid_threads = tuning->degrid_threads > 0 ? tuning->degrid_threads : 128;
       t.grid_threads = tuning->grid_threads > 0 ? tuning->grid_threads : 128;
       t.cell_group = tuning->cell_group > 0 ? tuning->cell_group : 1;
+      t.fft_columns = tuning->fft_columns;
     } else {
       t = pg::autotune_batch(cfg);
     }
     cfg.tile = t.tile;
     cfg.cell_group = t.cell_group;
+    cfg.fft_columns = t.fft_columns;
     cfg.max_per_item = t.max_per_item;
     cfg.threads = 128;
     cfg.degrid_threads = t.degrid_threads;
@@ -627,6 +630,7 @@ int purify_gb300_batch_get_tuning(const purify_gb300_batch *b, purify_gb300_batc
   t->degrid_threads = b->tuning.degrid_threads;
   t->grid_threads = b->tuning.grid_threads;
   t->cell_group = b->tuning.cell_group;
+  t->fft_columns = b->tuning.fft_columns;
   return PURIFY_GB300_OK;
 }
 int purify_gb300_batch_bind(purify_gb300_batch *b, const void *const *x_in, void *const *vis,

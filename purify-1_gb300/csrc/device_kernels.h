@@ -28,6 +28,7 @@ struct ApplyArgs {
   // slot_in then point at caller-ordered M-vectors.
   const int32_t *slot_user = nullptr;
   int Nu = 0, Nv = 0;
+  int ld = 0;                       // row stride of the grid in cells (0: Nu)
   int win_stride = 0;               // row stride of the shared-memory windows (plan's win_stride)
   int group_cells = 1;              // cells per work item along each axis (plan's group)
   // caller order (slot_user set): the grid kernel gathers and the degrid
@@ -97,6 +98,7 @@ struct FoldArgs {
   const int32_t *tu_of, *tv_of;      // Nu, Nv
   int ntu, ntv, Ju, Jv, Nu, Nv;
   void *grid;
+  int ld = 0;  // row stride of the grid in cells (0: Nu)
 };
 template <typename real>
 cudaError_t launch_fold(const FoldArgs &f, cudaStream_t s);
@@ -119,6 +121,7 @@ struct ChannelIO {
   // multiplied into the forward's output
   const void *w_slot = nullptr, *w_vis = nullptr;
   int Nx = 0, Ny = 0, Nu = 0, Nv = 0, x0 = 0, y0 = 0;
+  int ld = 0;  // row stride of pad and work in cells (0: Nu)
   int64_t M = 0, S = 0;
 };
 

@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstdint>
 
+#include "device_kernels.h"
 #include "fft_kernels.h"
 
 namespace pg {
@@ -132,7 +133,7 @@ __device__ __forceinline__ float2 load_in(const FftArgs &a, const float2 *__rest
     const float2 x = in[size_t(j) * a.Nx + i];
     return make_float2(s * x.x, s * x.y);
   } else {
-    return in[size_t(a.y0 + j) * a.Nu + n];
+    return in[size_t(a.y0 + j) * a.ld + n];
   }
 }
 
@@ -141,7 +142,7 @@ __device__ __forceinline__ void store_out(const FftArgs &a, float2 *__restrict__
                                           float2 v) {
   if (j >= a.Ny) return;
   if constexpr (!INV) {
-    out[size_t(a.y0 + j) * a.Nu + n] = v;
+    out[size_t(a.y0 + j) * a.ld + n] = v;
   } else {
     const int i = n - a.x0;
     if (i >= 0 && i < a.Nx) {
@@ -151,9 +152,12 @@ __device__ __forceinline__ void store_out(const FftArgs &a, float2 *__restrict__
   }
 }
 
-template <int N>
+// Shared-memory slot of element n of row `row`: one pad element every 32,
+// and rows PAD elements further apart (the column pass picks PAD so that the
+// V rows it reads at one n fall on different banks).
+template <int N, int PAD = 0>
 __device__ __forceinline__ int sidx(int row, int n) {
-  constexpr int NP = N + N / 32;
+  constexpr int NP = N + N / 32 + PAD;
   return row * NP + n + (n >> 5);
 }
 
@@ -188,16 +192,16 @@ struct StageRadix {
   static constexpr int value = rem % 16 == 0 ? 16 : rem;
 };
 
-template <int N, int V, int Ns, int S, bool INV>
+template <int N, int V, int Ns, int S, bool INV, int T = kFftThreads>
 __device__ __forceinline__ void load_twiddles(TwiddleCache &c, const float2 *__restrict__ tw) {
   constexpr int R = StageRadix<N, Ns>::value;
   constexpr int NB = V * (N / R);
-  constexpr int Q = (NB + kFftThreads - 1) / kFftThreads;
+  constexpr int Q = (NB + T - 1) / T;
   static_assert(S < kMaxStages && Q <= kMaxQ, "twiddle cache size");
   if constexpr (Ns > 1) {
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-      const int flat = int(threadIdx.x) + q * kFftThreads;
+      const int flat = int(threadIdx.x) + q * T;
       const int j = flat % (N / R);
       const int step = (j % Ns) * (N / (Ns * R));
 #pragma unroll
@@ -210,39 +214,43 @@ __device__ __forceinline__ void load_twiddles(TwiddleCache &c, const float2 *__r
       }
     }
   }
-  if constexpr (Ns * R < N) load_twiddles<N, V, Ns * R, S + 1, INV>(c, tw);
+  if constexpr (Ns * R < N) load_twiddles<N, V, Ns * R, S + 1, INV, T>(c, tw);
 }
 
-// Stage S (sub-transform length Ns) of an N-point transform of V rows.
-template <int N, int V, int Ns, int S, bool INV>
+// Stage S (sub-transform length Ns) of an N-point transform of V rows.  With
+// SMIO the first stage reads and the last stage writes shared memory (the
+// column pass moves the data in and out itself); otherwise they read and
+// write global memory through load_in / store_out.
+template <int N, int V, int Ns, int S, bool INV, bool SMIO = false, int PAD = 0,
+          int T = kFftThreads>
 __device__ __forceinline__ void run_stages(const FftArgs &a, const float2 *__restrict__ in,
                                            float2 *__restrict__ out, float2 *sm,
                                            const TwiddleCache &tc, int row0) {
   constexpr int R = StageRadix<N, Ns>::value;
   constexpr bool FIRST = Ns == 1, LAST = Ns * R == N;
   constexpr int NB = V * (N / R);  // butterflies of the stage
-  constexpr int Q = (NB + kFftThreads - 1) / kFftThreads;
+  constexpr int Q = (NB + T - 1) / T;
   const int tid = threadIdx.x;
   float2 v[Q][R];
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
-    const int flat = tid + q * kFftThreads;
+    const int flat = tid + q * T;
     if (flat < NB) {
       const int rr = flat / (N / R), j = flat % (N / R);
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const int n = j + r * (N / R);
-        if constexpr (FIRST)
+        if constexpr (FIRST && !SMIO)
           v[q][r] = load_in<INV>(a, in, row0 + rr, n);
         else
-          v[q][r] = sm[sidx<N>(rr, n)];
+          v[q][r] = sm[sidx<N, PAD>(rr, n)];
       }
     }
   }
-  if constexpr (!FIRST) __syncthreads();  // every read of this stage is done
+  if constexpr (!FIRST || SMIO) __syncthreads();  // every read of this stage is done
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
-    const int flat = tid + q * kFftThreads;
+    const int flat = tid + q * T;
     if (flat < NB) {
       const int rr = flat / (N / R), j = flat % (N / R);
       const int k = j % Ns;
@@ -252,16 +260,16 @@ __device__ __forceinline__ void run_stages(const FftArgs &a, const float2 *__res
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const int n = d + r * Ns;
-        if constexpr (LAST)
+        if constexpr (LAST && !SMIO)
           store_out<INV>(a, out, row0 + rr, n, v[q][r]);
         else
-          sm[sidx<N>(rr, n)] = v[q][r];
+          sm[sidx<N, PAD>(rr, n)] = v[q][r];
       }
     }
   }
   if constexpr (!LAST) {
     __syncthreads();
-    run_stages<N, V, Ns * R, S + 1, INV>(a, in, out, sm, tc, row0);
+    run_stages<N, V, Ns * R, S + 1, INV, SMIO, PAD, T>(a, in, out, sm, tc, row0);
   }
 }
 
@@ -273,6 +281,124 @@ __global__ void __launch_bounds__(kFftThreads, 4) fft_row_kernel(const FftArgs a
   TwiddleCache tc;
   load_twiddles<N, V, 1, 0, INV>(tc, static_cast<const float2 *>(a.tw_u));
   run_stages<N, V, 1, 0, INV>(a, in, out, fft_sm, tc, int(blockIdx.x) * V);
+}
+
+// One size group of a batch: member blockIdx.y's arguments from the channel
+// table; the CTAs past that member's last row return at once.
+template <int N, int V, bool INV>
+__global__ void __launch_bounds__(kFftThreads, 4) fft_row_group_kernel(
+    const ChannelIO<float> *__restrict__ chans, const int *__restrict__ members, int ld,
+    const float2 *__restrict__ tw) {
+  extern __shared__ float2 fft_sm[];
+  const ChannelIO<float> &c = chans[members[blockIdx.y]];
+  if (int(blockIdx.x) * V >= c.Ny) return;
+  FftArgs a;
+  a.Nx = c.Nx;
+  a.Ny = c.Ny;
+  a.Nu = c.Nu;
+  a.Nv = c.Nv;
+  a.x0 = c.x0;
+  a.y0 = c.y0;
+  a.ld = ld;
+  a.su = c.su;
+  a.sv = c.sv;
+  const float2 *in = static_cast<const float2 *>(INV ? c.work : c.x_in);
+  float2 *out = static_cast<float2 *>(INV ? c.x_out : c.pad);
+  TwiddleCache tc;
+  load_twiddles<N, V, 1, 0, INV>(tc, tw);
+  run_stages<N, V, 1, 0, INV>(a, in, out, fft_sm, tc, int(blockIdx.x) * V);
+}
+
+// Column pass: V adjacent columns per CTA, so that every row of the block is
+// one contiguous V x 8-byte segment (a full 32-byte sector at V = 4).  The
+// block is copied in with the column index fastest across threads, the
+// Stockham stages run on the V columns as V rows of shared memory, and the
+// result is copied out the same way.  Forward: only rows y0 ... y0+Ny-1 of
+// the input are read (the others are zero), all Nv rows are written.
+// Inverse: all rows are read, only rows y0 ... y0+Ny-1 are written.  With a
+// member table, the CTA's channel (column / Nu) gives y0 and Ny.
+// V = 8 columns (64-byte row segments) from 256 rows up, 16 below; 512
+// threads once the block holds 16K points, so that each thread keeps two
+// radix-16 butterflies in registers.  Measured on 2048 x 2048: 8 columns
+// and 512 threads 25 us per pass, 4 columns and 256 threads 29 us, 2
+// columns 33 us.
+constexpr int col_block(int N) { return N >= 256 ? 8 : 16; }
+constexpr int col_threads(int N) { return col_block(N) * N >= 16384 ? 512 : 256; }
+template <int N, int V>
+struct ColPad {
+  // rows of the block sit 16 / V banks (8-byte units) apart
+  static constexpr int value = ((16 / V) - (N + N / 32) % 16 + 16) % 16;
+};
+constexpr int kColUnroll = 8;
+
+template <int N, int V, bool INV, int T = kFftThreads, int UNROLL = kColUnroll, int MINB = 2>
+__global__ void __launch_bounds__(T, MINB) fft_col_kernel(const FftColArgs c) {
+  extern __shared__ float2 fft_sm[];
+  constexpr int PAD = ColPad<N, V>::value;
+  const int col0 = int(blockIdx.x) * V;
+  int y0 = c.y0, ny = c.Ny;
+  if (c.members) {
+    const ChannelIO<float> &io =
+        static_cast<const ChannelIO<float> *>(c.chans)[c.members[col0 / c.Nu]];
+    y0 = io.y0;
+    ny = io.Ny;
+  }
+  const float2 *in = static_cast<const float2 *>(c.in);
+  float2 *out = static_cast<float2 *>(c.out);
+  const size_t ld = size_t(c.ld);
+  TwiddleCache tc;
+  load_twiddles<N, V, 1, 0, INV, T>(tc, static_cast<const float2 *>(c.tw_v));
+  // UNROLL loads in flight per thread
+  for (int base = 0; base < N * V; base += T * UNROLL) {
+    float2 v[UNROLL];
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) {
+      const int e = base + u * T + int(threadIdx.x);
+      const int rr = e % V, n = e / V;
+      v[u] = (e < N * V && (INV || (n >= y0 && n < y0 + ny))) ? in[size_t(n) * ld + col0 + rr]
+                                                              : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) {
+      const int e = base + u * T + int(threadIdx.x);
+      if (e < N * V) fft_sm[sidx<N, PAD>(e % V, e / V)] = v[u];
+    }
+  }
+  __syncthreads();
+  run_stages<N, V, 1, 0, INV, true, PAD, T>(FftArgs{}, nullptr, nullptr, fft_sm, tc, 0);
+  __syncthreads();
+  for (int e = int(threadIdx.x); e < N * V; e += T) {
+    const int rr = e % V, n = e / V;
+    if (!INV || (n >= y0 && n < y0 + ny)) out[size_t(n) * ld + col0 + rr] = fft_sm[sidx<N, PAD>(rr, n)];
+  }
+}
+
+template <int N, bool INV>
+cudaError_t launch_cols(const FftColArgs &c, cudaStream_t s) {
+  constexpr int V = col_block(N), T = col_threads(N);
+  constexpr int PAD = ColPad<N, V>::value;
+  const size_t smem = sizeof(float2) * size_t(V) * (N + N / 32 + PAD);
+  auto fn = fft_col_kernel<N, V, INV, T, kColUnroll, T == 512 ? 1 : 2>;
+  if (smem > 48 * 1024) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+  }
+  fn<<<c.W / V, T, smem, s>>>(c);
+  return cudaGetLastError();
+}
+
+template <bool INV>
+cudaError_t launch_cols_n(const FftColArgs &c, cudaStream_t s) {
+  switch (c.Nv) {
+    case 64: return launch_cols<64, INV>(c, s);
+    case 128: return launch_cols<128, INV>(c, s);
+    case 256: return launch_cols<256, INV>(c, s);
+    case 512: return launch_cols<512, INV>(c, s);
+    case 1024: return launch_cols<1024, INV>(c, s);
+    case 2048: return launch_cols<2048, INV>(c, s);
+  }
+  return cudaErrorInvalidValue;
 }
 
 // Rows per CTA: enough to give every thread a butterfly in the first
@@ -295,8 +421,10 @@ cudaError_t launch_rows(const FftArgs &a, const void *in, void *out, cudaStream_
 }
 
 template <bool INV>
-cudaError_t launch_n(const FftArgs &a, const void *in, void *out, cudaStream_t s) {
-  if (a.Ny == 0) return cudaSuccess;
+cudaError_t launch_n(const FftArgs &a0, const void *in, void *out, cudaStream_t s) {
+  if (a0.Ny == 0) return cudaSuccess;
+  FftArgs a = a0;
+  if (a.ld == 0) a.ld = a.Nu;
   switch (a.Nu) {
     case 64: return launch_rows<64, INV>(a, in, out, s);
     case 128: return launch_rows<128, INV>(a, in, out, s);
@@ -305,6 +433,37 @@ cudaError_t launch_n(const FftArgs &a, const void *in, void *out, cudaStream_t s
     case 1024: return launch_rows<1024, INV>(a, in, out, s);
     case 2048: return launch_rows<2048, INV>(a, in, out, s);
     case 4096: return launch_rows<4096, INV>(a, in, out, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <int N, bool INV>
+cudaError_t launch_group(const ChannelIO<float> *chans, const int *members, int nmembers,
+                         int max_ny, int ld, const void *tw, cudaStream_t s) {
+  constexpr int V = rows_per_cta(N);
+  const size_t smem = sizeof(float2) * size_t(V) * (N + N / 32);
+  auto fn = fft_row_group_kernel<N, V, INV>;
+  if (smem > 48 * 1024) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+  }
+  const dim3 grid((max_ny + V - 1) / V, nmembers);
+  fn<<<grid, kFftThreads, smem, s>>>(chans, members, ld, static_cast<const float2 *>(tw));
+  return cudaGetLastError();
+}
+
+template <bool INV>
+cudaError_t launch_group_n(const ChannelIO<float> *chans, const int *members, int nmembers,
+                           int Nu, int max_ny, int ld, const void *tw, cudaStream_t s) {
+  switch (Nu) {
+    case 64: return launch_group<64, INV>(chans, members, nmembers, max_ny, ld, tw, s);
+    case 128: return launch_group<128, INV>(chans, members, nmembers, max_ny, ld, tw, s);
+    case 256: return launch_group<256, INV>(chans, members, nmembers, max_ny, ld, tw, s);
+    case 512: return launch_group<512, INV>(chans, members, nmembers, max_ny, ld, tw, s);
+    case 1024: return launch_group<1024, INV>(chans, members, nmembers, max_ny, ld, tw, s);
+    case 2048: return launch_group<2048, INV>(chans, members, nmembers, max_ny, ld, tw, s);
+    case 4096: return launch_group<4096, INV>(chans, members, nmembers, max_ny, ld, tw, s);
   }
   return cudaErrorInvalidValue;
 }
@@ -332,6 +491,29 @@ cudaError_t launch_fft_rows_forward(const FftArgs &a, const void *x, void *grid,
 cudaError_t launch_fft_rows_inverse(const FftArgs &a, const void *grid, void *x, cudaStream_t s) {
   if (!fft_rows_supported(a.Nu)) return cudaErrorInvalidValue;
   return launch_n<true>(a, grid, x, s);
+}
+
+bool fft_cols_supported(int Nv, int W) {
+  // at 4096 rows the block's registers would spill
+  if (!fft_rows_supported(Nv) || Nv > 2048 || W <= 0) return false;
+  return W % (Nv >= 256 ? 8 : 16) == 0;
+}
+
+cudaError_t launch_fft_cols(bool inverse, const FftColArgs &c, cudaStream_t s) {
+  if (!fft_cols_supported(c.Nv, c.W) || c.ld < c.W || (c.members && c.Nu <= 0) ||
+      (!c.members && (c.y0 < 0 || c.Ny < 0 || c.y0 + c.Ny > c.Nv)))
+    return cudaErrorInvalidValue;
+  return inverse ? launch_cols_n<true>(c, s) : launch_cols_n<false>(c, s);
+}
+
+cudaError_t launch_fft_rows_group(bool inverse, const void *chans, const int *members, int nmembers,
+                                  int Nu, int max_ny, int ld, const void *tw_u, cudaStream_t s) {
+  if (!fft_rows_supported(Nu) || ld < Nu || nmembers < 0 || nmembers > 65535)
+    return cudaErrorInvalidValue;
+  if (nmembers == 0 || max_ny == 0) return cudaSuccess;
+  const auto *c = static_cast<const ChannelIO<float> *>(chans);
+  return inverse ? launch_group_n<true>(c, members, nmembers, Nu, max_ny, ld, tw_u, s)
+                 : launch_group_n<false>(c, members, nmembers, Nu, max_ny, ld, tw_u, s);
 }
 
 }  // namespace pg

@@ -260,6 +260,7 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
   C *win = reinterpret_cast<C *>(smem_raw);
   const TaskHeaders th = load_headers(a, tk, smem_raw + a0.win_bytes);
   const C *grid = static_cast<const C *>(a.grid);
+  const size_t ld = size_t(a.ld ? a.ld : a.Nu);
   // Stage the (wrapped) window of the grid this tile's footprints touch.
   for (int idx = threadIdx.x; idx < WW * WH; idx += blockDim.x) {
     const int lp = idx / WW, lq = idx - lp * WW;
@@ -267,7 +268,7 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
     if (p >= a.Nv) p -= a.Nv;
     int q = tk.Q + lq;
     if (q >= a.Nu) q -= a.Nu;
-    cp_async<sizeof(C)>(win + win_offset(lp, lq, WS, G), grid + size_t(p) * a.Nu + q);
+    cp_async<sizeof(C)>(win + win_offset(lp, lq, WS, G), grid + size_t(p) * ld + q);
   }
   cp_async_wait_all();
   __syncthreads();
@@ -570,10 +571,11 @@ __device__ __forceinline__ void fold_tile(const FoldArgs &f, int t) {
             }
         }
       if (col) {
-        C *g = grid + size_t(P) * f.Nu + Q + lq;
+        const size_t ld = size_t(f.ld ? f.ld : f.Nu);
+        C *g = grid + size_t(P) * ld + Q + lq;
 #pragma unroll
         for (int r = 0; r < R; ++r)
-          if (lp[r] < H) g[size_t(lp[r]) * f.Nu] = s[r];
+          if (lp[r] < H) g[size_t(lp[r]) * ld] = s[r];
       }
     }
   }

@@ -75,7 +75,9 @@ class OperatorT final : public Operator {
   WorkspaceSizes workspace_sizes() const override;
   void forward_ws(const void *x, void *y, const Workspace &ws) override;
   void adjoint_ws(const void *y, void *x, const Workspace &ws) override;
-  void power_ws(void *x, int iters, double *sq, double *partial, const Workspace &ws) override;
+  void power_ws(void *x, int first, int count, double *sq, double *partial,
+                const Workspace &ws) override;
+  bool needs_column_plan() const override { return fused_fft_ && !own_cols_; }
 
  private:
   enum Stage { kPad = 0, kFftF, kDegrid, kGrid, kFold, kFftI, kCrop, kCompact, kExpand };
@@ -165,7 +167,12 @@ class OperatorT final : public Operator {
   bool fused_fft_ = false;
   cufftHandle fft_cols_ = 0;
   DeviceBuffer tw_u_;
-  bool use_fused_fft() const { return fused_fft_ && ws_->fft_cols != 0; }
+  // own_cols_: the column transforms run as the library's column pass
+  // (launch_fft_cols); otherwise through the workspace's cuFFT column plan
+  bool own_cols_ = false;
+  DeviceBuffer tw_v_;
+  bool use_fused_fft() const { return fused_fft_ && (own_cols_ || ws_->fft_cols != 0); }
+  FftColArgs col_args(const void *in, void *out) const;
   std::mutex mu_;
 
   DeviceBuffer task_order_, frac_, weight_, slot_user_, user_slot_, batches_, lane_code_, tasks_, tile_tasks_,
@@ -311,8 +318,16 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
     const std::vector<float> twu = fft_twiddles(Nu_);
     tw_u_.alloc(sizeof(float) * twu.size(), &bytes);
     tw_u_.upload(twu.data(), sizeof(float) * twu.size(), stream_);
+    own_cols_ = cfg.fft_columns != 1 && fft_cols_supported(Nv_, Nu_);
+    std::vector<float> twv;
+    if (own_cols_) {
+      twv = fft_twiddles(Nv_);
+      tw_v_.alloc(sizeof(float) * twv.size(), &bytes);
+      tw_v_.upload(twv.data(), sizeof(float) * twv.size(), stream_);
+    } else {
+      fft_cols_ = make_column_plan<real>(Nu_, Nv_, stream_, &bytes);
+    }
     cuda_check(cudaStreamSynchronize(stream_), "twiddle upload");
-    fft_cols_ = make_column_plan<real>(Nu_, Nv_, stream_, &bytes);
     fused_fft_ = true;
   }
   cufft_check(cufftSetStream(fft_, stream_), "cufftSetStream");
@@ -763,13 +778,31 @@ FftArgs OperatorT<real>::fft_args() const {
 }
 
 template <typename real>
+FftColArgs OperatorT<real>::col_args(const void *in, void *out) const {
+  FftColArgs c;
+  c.in = in;
+  c.out = out;
+  c.Nv = Nv_;
+  c.W = Nu_;
+  c.ld = Nu_;
+  c.y0 = y0_;
+  c.Ny = Ny_;
+  c.tw_v = tw_v_.get();
+  return c;
+}
+
+template <typename real>
 void OperatorT<real>::forward_slots(const void *x, void *caller_vis) {
   if (use_fused_fft()) {
     // row transforms of the image rows into ws->pad (its other rows stay
     // zero), then the column transform into ws->work
     mark_begin(kFftF);
     cuda_check(launch_fft_rows_forward(fft_args(), x, ws_->pad, ws_->stream), "fft rows");
-    cufft_check(Traits<real>::exec(ws_->fft_cols, ws_->pad, ws_->work, CUFFT_FORWARD), "cufftExec");
+    if (own_cols_)
+      cuda_check(launch_fft_cols(false, col_args(ws_->pad, ws_->work), ws_->stream), "fft columns");
+    else
+      cufft_check(Traits<real>::exec(ws_->fft_cols, ws_->pad, ws_->work, CUFFT_FORWARD),
+                  "cufftExec");
     mark_end(kFftF);
     degrid_slots(ws_->work, caller_vis);
     return;
@@ -790,7 +823,11 @@ void OperatorT<real>::adjoint_slots(void *x, const void *caller_vis) {
   grid_slots(ws_->work, caller_vis);
   if (use_fused_fft()) {
     mark_begin(kFftI);
-    cufft_check(Traits<real>::exec(ws_->fft_cols, ws_->work, ws_->work, CUFFT_INVERSE), "cufftExec");
+    if (own_cols_)
+      cuda_check(launch_fft_cols(true, col_args(ws_->work, ws_->work), ws_->stream), "fft columns");
+    else
+      cufft_check(Traits<real>::exec(ws_->fft_cols, ws_->work, ws_->work, CUFFT_INVERSE),
+                  "cufftExec");
     cuda_check(launch_fft_rows_inverse(fft_args(), ws_->work, x, ws_->stream), "fft rows");
     mark_end(kFftI);
     return;
@@ -881,13 +918,14 @@ void OperatorT<real>::adjoint_ws(const void *y, void *x, const Workspace &ws) {
 // sqrt(sq[i]) are those of power_method() bit for bit.  The stopping rule is
 // applied by the caller to the recorded estimates.
 template <typename real>
-void OperatorT<real>::power_ws(void *x, int iters, double *sq, double *partial,
+void OperatorT<real>::power_ws(void *x, int first, int count, double *sq, double *partial,
                                const Workspace &ws) {
   Workspace w = ws;
   w.unit_norm = true;
   with_workspace(w, [&] {
-    cuda_check(launch_fill<real>(x, N_, 1.0 / std::sqrt(double(N_)), w.stream), "fill");
-    for (int i = 0; i < iters; ++i) {
+    if (first == 0)
+      cuda_check(launch_fill<real>(x, N_, 1.0 / std::sqrt(double(N_)), w.stream), "fill");
+    for (int i = first; i < first + count; ++i) {
       normal_slots(x, x);
       cuda_check(launch_sq_norm<real>(x, N_, partial, sq + i, w.stream), "norm");
       cuda_check(launch_scale_rsqrt<real>(x, N_, sq + i, w.stream), "scale");

@@ -52,6 +52,10 @@ struct OperatorConfig {
   int class_cap = 0;
   // 1: the forward's caller-ordered output is stored at L2 evict-last priority
   int keep_store = 0;
+  // column transform of the fused FFT path (FP32, power-of-two grid):
+  // 0: the library's column pass where it applies (grid height <= 2048),
+  // 1: cuFFT's strided column plan
+  int fft_columns = 0;
 };
 
 // A plan fraction t + d (see PlanRequest::group) in precision `real`, kept
@@ -129,11 +133,14 @@ class Operator {
   virtual WorkspaceSizes workspace_sizes() const = 0;
   virtual void forward_ws(const void *x, void *y, const Workspace &ws) = 0;
   virtual void adjoint_ws(const void *y, void *x, const Workspace &ws) = 0;
-  // `iters` power-method rounds of Phi'^H Phi' from the normalised all-ones
-  // image in x (N complex scratch), the normalisation on the device; sq[i]
-  // (device) receives ||x||^2 of round i, partial is kNormBlocks doubles.
-  virtual void power_ws(void *x, int iters, double *sq, double *partial,
+  // Power-method rounds first ... first+count-1 of Phi'^H Phi' on x (N
+  // complex scratch), the normalisation on the device; round 0 starts from
+  // the normalised all-ones image.  sq[i] (device) receives ||x||^2 of round
+  // i, partial is kNormBlocks doubles.  Rounds may be enqueued in pieces.
+  virtual void power_ws(void *x, int first, int count, double *sq, double *partial,
                         const Workspace &ws) = 0;
+  // True when the applies need Workspace::fft_cols (a cuFFT column plan).
+  virtual bool needs_column_plan() const = 0;
 };
 
 }  // namespace pg

@@ -25,6 +25,17 @@ size_t up256(size_t b) { return (b + 255) / 256 * 256; }
 // A non-head request may overtake a head that does not fit the budget at
 // most this many times before admission waits for the head.
 constexpr int kMaxOvertakes = 16;
+// Power-method rounds of a norm request enqueued at a time (see enqueue).
+constexpr int kNormChunk = 4;
+// Pinned staging buffers of each size class a coverage uses, allocated when
+// the coverage is added: pinning host memory takes milliseconds, too long for
+// the submit path of a request.
+constexpr int kPinnedWarm = 2;
+size_t pinned_class(size_t bytes) {
+  size_t cls = 4096;
+  while (cls < bytes) cls <<= 1;
+  return cls;
+}
 
 }  // namespace
 
@@ -42,6 +53,13 @@ struct Server::Slot {
   std::map<int64_t, cufftHandle> col_plans;  // FP32 column transforms, same key
   bool busy = false;
   bool long_slot = false;  // serves norm requests (lowest stream priority)
+  // The slot's enqueue thread: the scheduler hands it an admitted job, and
+  // it enqueues the job's copies and launches on the slot's stream, so a
+  // long request's launches do not hold up admission of the others.
+  Job *job = nullptr;
+  std::condition_variable cv;
+  std::thread worker;
+  cudaEvent_t chunk_ev[2] = {nullptr, nullptr};  // the last two norm pieces enqueued
 };
 
 struct Server::Job {
@@ -111,9 +129,15 @@ Server::Server(const ServerConfig &cfg) : cfg_(cfg) {
     cuda_check(cudaStreamCreateWithPriority(&s->stream, cudaStreamNonBlocking,
                                             s->long_slot ? lo : hi),
                "cudaStreamCreateWithPriority");
+    for (cudaEvent_t &e : s->chunk_ev)
+      cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
     slots_.push_back(std::move(s));
   }
   stats_.bytes_budget = cfg.hbm_budget;
+  for (auto &s : slots_) {
+    Slot *sp = s.get();
+    sp->worker = std::thread([this, sp] { work(*sp); });
+  }
   thread_ = std::thread([this] { loop(); });
 }
 
@@ -125,11 +149,21 @@ Server::~Server() {
   }
   cv_.notify_all();
   if (thread_.joinable()) thread_.join();
+  // every admitted job has been enqueued and retired by now
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    workers_stop_ = true;
+  }
+  for (auto &s : slots_) s->cv.notify_all();
+  for (auto &s : slots_)
+    if (s->worker.joinable()) s->worker.join();
   DeviceGuard guard(cfg_.device);
   for (auto &s : slots_) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     for (auto &kv : s->plans) cufftDestroy(kv.second);
     for (auto &kv : s->col_plans) cufftDestroy(kv.second);
+    for (cudaEvent_t e : s->chunk_ev)
+      if (e) cudaEventDestroy(e);
     if (s->stream) cudaStreamDestroy(s->stream);
   }
   if (pool_) cudaMemPoolDestroy(pool_);
@@ -157,21 +191,32 @@ int Server::add_coverage(const OperatorConfig &cfg_in) {
   const int64_t key = plan_key(c->fp64, int(c->info.ftsizeu), int(c->info.ftsizev));
   std::lock_guard<std::mutex> lk(mu_);
   for (auto &s : slots_) {
-    if (s->plans.count(key)) continue;
-    cufftHandle h = 0;
-    cufft_check(cufftPlan2d(&h, int(c->info.ftsizev), int(c->info.ftsizeu),
-                            c->fp64 ? CUFFT_Z2Z : CUFFT_C2C),
-                "cufftPlan2d");
-    const cufftResult r = cufftSetStream(h, s->stream);
-    if (r != CUFFT_SUCCESS) {
-      cufftDestroy(h);
-      cufft_check(r, "cufftSetStream");
+    if (!s->plans.count(key)) {
+      cufftHandle h = 0;
+      cufft_check(cufftPlan2d(&h, int(c->info.ftsizev), int(c->info.ftsizeu),
+                              c->fp64 ? CUFFT_Z2Z : CUFFT_C2C),
+                  "cufftPlan2d");
+      const cufftResult r = cufftSetStream(h, s->stream);
+      if (r != CUFFT_SUCCESS) {
+        cufftDestroy(h);
+        cufft_check(r, "cufftSetStream");
+      }
+      s->plans[key] = h;
     }
-    s->plans[key] = h;
-    // the column transform of the fused FFT path (fft_kernels.h)
-    if (!c->fp64 && fft_rows_supported(int(c->info.ftsizeu)))
+    // the cuFFT column transform of the fused FFT path, where the operator
+    // does not run its own column pass (fft_kernels.h)
+    if (c->op->needs_column_plan() && !s->col_plans.count(key))
       s->col_plans[key] =
           make_column_plan<float>(int(c->info.ftsizeu), int(c->info.ftsizev), s->stream, nullptr);
+  }
+  // staging of the request kinds' inputs and outputs: 16 N, 16 M, 16 (M + N)
+  for (int64_t n : {16 * c->N, 16 * c->M, 16 * (c->M + c->N)}) {
+    const size_t cls = pinned_class(size_t(std::max<int64_t>(n, 1)));
+    while (int(pinned_free_.count(cls)) < kPinnedWarm) {
+      void *p = nullptr;
+      cuda_check(cudaHostAlloc(&p, cls, cudaHostAllocPortable), "cudaHostAlloc");
+      pinned_free_.emplace(cls, p);
+    }
   }
   std::lock_guard<std::mutex> ck(cov_mu_);
   coverages_.push_back(std::move(c));
@@ -205,8 +250,7 @@ int64_t Server::request_bytes(const Request &rq) const {
 }
 
 void *Server::pinned(size_t bytes) {
-  size_t cls = 4096;
-  while (cls < bytes) cls <<= 1;
+  const size_t cls = pinned_class(bytes);
   {
     std::lock_guard<std::mutex> lk(mu_);
     auto it = pinned_free_.find(cls);
@@ -221,9 +265,7 @@ void *Server::pinned(size_t bytes) {
   return p;
 }
 void Server::unpin(void *p, size_t bytes) {
-  size_t cls = 4096;
-  while (cls < bytes) cls <<= 1;
-  pinned_free_.emplace(cls, p);  // caller holds mu_
+  pinned_free_.emplace(pinned_class(bytes), p);  // caller holds mu_
 }
 
 int64_t Server::submit(const Request &rq) {
@@ -343,15 +385,51 @@ void Server::loop() {
       if (pending_.front()->overtaken >= kMaxOvertakes) break;
       ++it;
     }
-    if (!admitted.empty()) {
-      lk.unlock();
-      std::vector<Job *> failed;
-      for (Job *j : admitted)
-        if (!enqueue(*j)) failed.push_back(j);
-      lk.lock();
-      for (Job *j : failed) finish(*j);
+    for (Job *j : admitted) {
+      j->slot->job = j;
+      j->slot->cv.notify_one();
     }
     if (stop_ && pending_.empty() && inflight_ == 0) break;
+  }
+}
+
+// A slot's enqueue thread.  The cuFFT handles are looked up under the lock
+// (add_coverage inserts into the same maps); the launches are enqueued
+// without it.  Requests of one coverage still enqueue one at a time (the
+// operator serialises its workspace switch), those of different coverages
+// in parallel.
+void Server::work(Slot &slot) {
+  cudaSetDevice(cfg_.device);
+  std::unique_lock<std::mutex> lk(mu_);
+  for (;;) {
+    slot.cv.wait(lk, [&] { return slot.job != nullptr || workers_stop_; });
+    if (!slot.job) break;
+    Job *j = slot.job;
+    slot.job = nullptr;
+    cufftHandle fft = 0, cols = 0;
+    try {
+      const Coverage &c = coverage(j->rq.coverage);
+      const int64_t key = plan_key(c.fp64, int(c.info.ftsizeu), int(c.info.ftsizev));
+      fft = slot.plans.at(key);
+      const auto cp = slot.col_plans.find(key);
+      cols = cp == slot.col_plans.end() ? 0 : cp->second;
+    } catch (...) {
+      j->status = kInternal;
+      j->t_done = Clock::now();
+      finish(*j);
+      dirty_ = true;
+      cv_.notify_one();
+      continue;
+    }
+    lk.unlock();
+    const bool ok = enqueue(*j, fft, cols);
+    lk.lock();
+    if (!ok) {
+      // nothing will call back: retire the job here and wake the scheduler
+      finish(*j);
+      dirty_ = true;
+      cv_.notify_one();
+    }
   }
 }
 
@@ -368,7 +446,7 @@ void Server::reserve(Job &j, Slot &slot) {
 // Enqueues the request's copies and kernels on its slot's stream (called
 // without the server lock).  Returns false if enqueueing failed; the caller
 // then retires the job.
-bool Server::enqueue(Job &j) {
+bool Server::enqueue(Job &j, cufftHandle fft, cufftHandle fft_cols) {
   const Coverage &c = coverage(j.rq.coverage);
   Slot &slot = *j.slot;
   cudaStream_t s = slot.stream;
@@ -385,10 +463,8 @@ bool Server::enqueue(Job &j) {
     ws.work = take(size_t(c.ws.work));
     ws.tilebuf = take(size_t(c.ws.tilebuf));
     ws.slots = take(size_t(c.ws.slots));
-    const int64_t key = plan_key(c.fp64, int(c.info.ftsizeu), int(c.info.ftsizev));
-    ws.fft = slot.plans.at(key);
-    const auto cp = slot.col_plans.find(key);
-    ws.fft_cols = cp == slot.col_plans.end() ? 0 : cp->second;
+    ws.fft = fft;
+    ws.fft_cols = fft_cols;
     ws.stream = s;
     // the padded grid must be zero outside the image region
     cuda_check(cudaMemsetAsync(ws.pad, 0, size_t(c.ws.pad), s), "cudaMemsetAsync");
@@ -397,7 +473,17 @@ bool Server::enqueue(Job &j) {
       void *x = take(cs * size_t(c.N));
       double *sq = static_cast<double *>(take(sizeof(double) * j.rq.iters));
       double *partial = static_cast<double *>(take(sizeof(double) * kNormBlocks));
-      c.op->power_ws(x, j.rq.iters, sq, partial, ws);
+      // The rounds go in kNormChunk at a time, at most two pieces in
+      // flight: before enqueueing a piece this thread waits for the one two
+      // pieces back.  A whole request at once (about 11 launches a round)
+      // could fill the device's launch queue, and then every other
+      // request's launches wait behind it; it would also hold the
+      // coverage's lock for the whole enqueue.
+      for (int i0 = 0, k = 0; i0 < j.rq.iters; i0 += kNormChunk, ++k) {
+        if (k >= 2) cuda_check(cudaEventSynchronize(slot.chunk_ev[k & 1]), "cudaEventSynchronize");
+        c.op->power_ws(x, i0, std::min(kNormChunk, j.rq.iters - i0), sq, partial, ws);
+        cuda_check(cudaEventRecord(slot.chunk_ev[k & 1], s), "cudaEventRecord");
+      }
       cuda_check(cudaMemcpyAsync(j.host_out, sq, sizeof(double) * j.rq.iters,
                                  cudaMemcpyDeviceToHost, s),
                  "D2H");

@@ -11,6 +11,7 @@
 // request, so its result does not depend on what else is in flight.
 #pragma once
 #include <cuda_runtime_api.h>
+#include <cufft.h>
 
 #include <condition_variable>
 #include <cstdint>
@@ -97,7 +98,8 @@ class Server {
   struct Coverage;
   void loop();
   void reserve(Job &job, Slot &slot);
-  bool enqueue(Job &job);
+  void work(Slot &slot);
+  bool enqueue(Job &job, cufftHandle fft, cufftHandle fft_cols);
   void finish(Job &job);
   static void CUDART_CB on_done(void *job);
   void *pinned(size_t bytes);
@@ -120,7 +122,7 @@ class Server {
   int norm_slots_ = 1;  // slots that take norm requests (the first ones)
   std::condition_variable cv_;       // scheduler wake-ups
   std::condition_variable done_cv_;  // request completions
-  bool stop_ = false, dirty_ = false;
+  bool stop_ = false, dirty_ = false, workers_stop_ = false;
   std::thread thread_;
 };
 

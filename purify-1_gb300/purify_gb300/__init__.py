@@ -55,7 +55,7 @@ class Tuning(ctypes.Structure):
     _fields_ = [("threads", ctypes.c_int32), ("max_per_item", ctypes.c_int32),
                 ("tile", ctypes.c_int32), ("fused_permute", ctypes.c_int32),
                 ("cell_group", ctypes.c_int32), ("class_cap", ctypes.c_int32),
-                ("keep_store", ctypes.c_int32)]
+                ("keep_store", ctypes.c_int32), ("fft_columns", ctypes.c_int32)]
 
 
 class Info(ctypes.Structure):
@@ -86,7 +86,7 @@ class FbParams(ctypes.Structure):
 class BatchTuning(ctypes.Structure):
     _fields_ = [("tile", ctypes.c_int32), ("max_per_item", ctypes.c_int32),
                 ("degrid_threads", ctypes.c_int32), ("grid_threads", ctypes.c_int32),
-                ("cell_group", ctypes.c_int32)]
+                ("cell_group", ctypes.c_int32), ("fft_columns", ctypes.c_int32)]
 
 
 class BatchInfo(ctypes.Structure):
@@ -443,7 +443,7 @@ class MeasurementOperator:
             t = Tuning(int(tuning.get("threads", 0)), int(tuning.get("max_per_item", 0)),
                        int(tuning.get("tile", 0)), int(tuning.get("fused_permute", -1)),
                        int(tuning.get("cell_group", 0)), int(tuning.get("class_cap", 0)),
-                       int(tuning.get("keep_store", 0)))
+                       int(tuning.get("keep_store", 0)), int(tuning.get("fft_columns", 0)))
             _check(L.purify_gb300_operator_create_tuned(ctypes.byref(a), ctypes.byref(t),
                                                         ctypes.byref(h)))
         else:
@@ -664,7 +664,8 @@ class Batch:
         if tuning:
             t = BatchTuning(int(tuning.get("tile", 0)), int(tuning.get("max_per_item", 0)),
                             int(tuning.get("degrid_threads", 0)),
-                            int(tuning.get("grid_threads", 0)), int(tuning.get("cell_group", 0)))
+                            int(tuning.get("grid_threads", 0)), int(tuning.get("cell_group", 0)),
+                            int(tuning.get("fft_columns", 0)))
         _check(L.purify_gb300_batch_create(arr, n, float(oversample_ratio),
                                            KERNELS[kernel] if isinstance(kernel, str) else int(kernel),
                                            int(J), PRECISIONS[precision], int(device),
@@ -700,7 +701,7 @@ class Batch:
         _check(load().purify_gb300_batch_get_tuning(self._h, ctypes.byref(t)))
         return {"tile": t.tile, "max_per_item": t.max_per_item,
                 "degrid_threads": t.degrid_threads, "grid_threads": t.grid_threads,
-                "cell_group": t.cell_group}
+                "cell_group": t.cell_group, "fft_columns": t.fft_columns}
 
     def info(self):
         i = BatchInfo()

@@ -246,3 +246,34 @@ def test_batch_weights_any_kernel_fit(pg, cuda, J):
         y = op.forward(xs[k])
         assert rel_l2(host(vis[k]), host(y)) < TOL["fp32"], k
         assert rel_l2(host(xo[k]), host(op.adjoint(vis[k]))) < TOL["fp32"], k
+
+
+def test_fused_and_unfused_size_groups(pg, cuda):
+    """FP32 size groups of a power-of-two grid width run as interleaved grids
+    (one row-pass launch and one column plan per group); the others (here a
+    192-wide grid) keep the padded 2-D transform.  A batch mixing both must
+    still match every channel's own operator."""
+    torch = cuda
+    chans = []
+    for k, ((ny, nx), M) in enumerate(zip([(64, 64), (64, 96), (64, 64), (32, 96), (64, 64)],
+                                          [4000, 5000, 3000, 2000, 0])):
+        u, v = synthetic.gaussian_core_uv(M, 2 * nx, 2 * ny, 0.25, seed=40 + k)
+        chans.append(dict(u=u, v=v, imsizey=ny, imsizex=nx))
+    b = pg.Batch(chans, J=4, precision="fp32", tuning=TUNING)
+    assert b.info()["size_groups"] == 3
+    ops = single_ops(pg, chans, "fp32")
+    xs, ys = inputs(torch, chans, "fp32", seed=5)
+    vis = [torch.empty(c["u"].size, dtype=b.complex_dtype, device="cuda") for c in chans]
+    xo = [torch.empty_like(x) for x in xs]
+    b.bind(xs, vis, xo)
+    for _ in range(2):  # the padded grids keep their zero rows between applies
+        b.apply(1)
+    b.bind(xs, ys, xo)
+    b.apply(2)
+    torch.cuda.synchronize()
+    for k, op in enumerate(ops):
+        if chans[k]["u"].size:
+            assert rel_l2(host(vis[k]), host(op.forward(xs[k]))) < TOL["fp32"], k
+            assert rel_l2(host(xo[k]), host(op.adjoint(ys[k]))) < TOL["fp32"], k
+        else:
+            assert np.all(host(xo[k]) == 0)

@@ -116,13 +116,15 @@ def test_kernels_and_supports(pg, oracle_mod, cuda, kernel, J, precision):
     (64, 128, 2.0),      # 128 x 256, non-square
     (80, 40, 1.6),       # 128 x 64 grid around a non-power-of-two image (x0 = 12, y0 = 24)
     (256, 256, 2.0),     # 512^2
-    (1024, 2048, 2.0),   # 2048 x 4096: the largest row and column lengths
+    (1024, 2048, 2.0),   # 2048 x 4096: the largest row length, the column pass's largest height
+    (2048, 1024, 2.0),   # 4096 x 2048: columns of 4096 through cuFFT's column plan
 ])
 def test_fused_fft_grids(pg, oracle_mod, cuda, ny, nx, os):
     """FP32 operators on grids of power-of-two width run the fused row passes
     (correction + padding + row FFT, row FFT + cropping + correction) with a
-    column FFT instead of pad + 2-D FFT + crop; both directions against the
-    oracle and the adjoint dot-product test."""
+    column transform (the column pass up to 2048 rows, cuFFT above) instead of
+    pad + 2-D FFT + crop; both directions against the oracle and the adjoint
+    dot-product test."""
     torch = cuda
     rng = np.random.default_rng(ny + nx)
     M = 5000
@@ -139,6 +141,27 @@ def test_fused_fft_grids(pg, oracle_mod, cuda, ny, nx, os):
     lhs = np.vdot(yy, y)
     rhs = np.vdot(xx, x)
     assert abs(lhs - rhs) <= DOT_TOL["fp32"] * np.linalg.norm(y) * np.linalg.norm(yy)
+
+
+@pytest.mark.parametrize("ny,nx", [(256, 256), (80, 40), (512, 1024)])
+def test_column_pass_matches_cufft_columns(pg, cuda, ny, nx):
+    """The column pass (only the image rows read in the forward, written in
+    the adjoint) against cuFFT's strided column plan on the same operator
+    (tuning fft_columns = 1): the same transform up to FP32 rounding."""
+    torch = cuda
+    rng = np.random.default_rng(ny * 7 + nx)
+    M = 6000
+    u = rng.normal(0, nx / 3, M)
+    v = rng.normal(0, ny / 3, M)
+    ops = [pg.MeasurementOperator(u, v, None, None, ny, nx, 2.0 if ny != 80 else 1.6,
+                                  power_iters=0, kernel="kb", Ju=6, Jv=6, precision="fp32",
+                                  tuning={"fft_columns": c}) for c in (0, 1)]
+    x = to_dev(torch, rng.standard_normal(ny * nx) + 1j * rng.standard_normal(ny * nx), "fp32")
+    y = to_dev(torch, rng.standard_normal(M) + 1j * rng.standard_normal(M), "fp32")
+    f = [to_np(op.forward(x)) for op in ops]
+    a = [to_np(op.adjoint(y)) for op in ops]
+    assert rel_l2(f[0], f[1]) < 1e-6
+    assert rel_l2(a[0], a[1]) < 1e-6
 
 
 @pytest.mark.parametrize("precision", ["fp32", "fp64"])
