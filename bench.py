@@ -70,6 +70,8 @@ def parse():
                    help="base cells per work item along each axis: 1, 2, or 0 for the default")
     p.add_argument("--class-cap", type=int, default=0,
                    help="most items of one bank class per batch (0: default; tuning)")
+    p.add_argument("--grid-walk", type=int, default=0,
+                   help="1: G^H of Phi^H by the column walk instead of work items (tuning)")
     p.add_argument("--fft-columns", type=int, default=0,
                    help="1: cuFFT's column plan instead of the column pass (tuning)")
     p.add_argument("--keep-store", type=int, default=0,
@@ -85,7 +87,8 @@ def tuning_of(args):
     t = {k: v for k, v in (("threads", args.threads), ("max_per_item", args.max_per_item),
                            ("tile", args.tile), ("cell_group", args.cell_group),
                            ("class_cap", args.class_cap), ("keep_store", args.keep_store),
-                           ("fft_columns", args.fft_columns)) if v}
+                           ("fft_columns", args.fft_columns), ("grid_walk", args.grid_walk))
+         if v}
     if args.fused_permute >= 0:
         t["fused_permute"] = args.fused_permute
     return t or None
@@ -303,12 +306,21 @@ def kernel_bytes(info, s, caller_order_out=True):
     items = info["work_items"]
     lanes = 4 * items + 8 * (items // 32)
     windows = s * info["tasks"] * info["window_cells"]
-    return {
+    out = {
         "degrid": s * NuNv + s * S + (4 * S if caller_order_out else 0) + lanes + s * M,
         "grid": 2 * s * S + lanes + windows,
         "expand": 4 * S + s * S + s * M,
         "fold": windows + s * NuNv,
     }
+    nw = info.get("walk_tasks", 0)
+    if nw:
+        # the column walk of Phi^H: per slot (S = M) t and the visibility,
+        # per task 32 x 32 counts and 33 column starts, and its window
+        wwin = s * nw * info["window_cells"]
+        out["grid"] = 2 * s * M + 4 * (32 * 32 + 33) * nw + wwin
+        out["expand"] = 4 * M + 2 * s * M
+        out["fold"] = wwin + s * NuNv
+    return out
 
 
 def roofline_entry(kern, alg, dur_s, peak, peak_kind, traffic, survey_bytes=None):

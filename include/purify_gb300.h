@@ -115,6 +115,8 @@ typedef struct {
   int32_t fft_columns;   /* column transforms of the FP32 power-of-two FFT path: 0 = the
                             library's column pass (grid height <= 2048), 1 = cuFFT's
                             strided column plan */
+  int32_t grid_walk;     /* G^H of Phi^H: 1 = the column walk where it applies (tiles <= 32,
+                            single-cell items, J <= 8, J <= 6 in FP64), 0 = work items */
 } purify_gb300_tuning;
 int purify_gb300_operator_create_tuned(const purify_gb300_create_args *args,
                                        const purify_gb300_tuning *tuning,
@@ -228,6 +230,8 @@ typedef struct {
   int64_t window_cells;    /* grid cells of one task's accumulation window */
   int64_t factor_values;   /* w_term: complex row-factor values stored (0 otherwise) */
   int64_t cell_group;      /* base cells per work item along each axis (1 or 2) */
+  int64_t walk_tasks;      /* tasks of the column-walk G^H of Phi^H (0: it uses work items) */
+  int64_t walk_steps;      /* column steps of the walk: sum over its columns of the fullest row */
 } purify_gb300_info;
 int purify_gb300_operator_info(const purify_gb300_operator *op, purify_gb300_info *info);
 
@@ -289,6 +293,26 @@ int purify_gb300_plan_export(const purify_gb300_plan *plan, double *frac, double
                              int32_t *lane_code, int32_t *tasks, int32_t *tile_tasks,
                              int32_t *tu_start, int32_t *tv_start);
 int purify_gb300_plan_destroy(purify_gb300_plan *plan);
+/* The column-walk plan of G^H that Phi^H uses (tiles of 32, J x J taps):
+ * one task per occupied tile; lanes are the tile's rows, and a warp walks its
+ * base-cell columns in order.  Slots (S = M, no null slots) follow the walk:
+ * per task, per column q, per k = 0, 1, ...: the k-th visibility of every row
+ * with more than k in that column, rows ascending.  sizes[0..7] = M, tasks,
+ * tiles along u, tiles along v, window rows, window columns, window row
+ * stride (odd), column steps (sum over columns of the fullest row). */
+typedef struct purify_gb300_walk_plan purify_gb300_walk_plan;
+int purify_gb300_walk_plan_create(const double *u, const double *v, int64_t M, uint32_t ftsizeu,
+                                  uint32_t ftsizev, uint32_t J, purify_gb300_walk_plan **out);
+int purify_gb300_walk_plan_sizes(const purify_gb300_walk_plan *plan, int64_t *sizes);
+/* Per slot: frac (2 doubles: t_u with the phase sign (-1)^(k_u + k_v), t_v)
+ * and slot_user (caller index).  Per task: counts (32 columns x 32 rows),
+ * colstart (33: first slot of each column, then the end), tasks (8 int32:
+ * P, Q, H, W, 0, 0, tile, 0); task_order (launch order); tile_tasks (tiles +
+ * 1).  Any pointer may be NULL. */
+int purify_gb300_walk_plan_export(const purify_gb300_walk_plan *plan, double *frac,
+                                  int32_t *slot_user, int32_t *counts, int32_t *colstart,
+                                  int32_t *tasks, int32_t *task_order, int32_t *tile_tasks);
+int purify_gb300_walk_plan_destroy(purify_gb300_walk_plan *plan);
 /* Tap weights as the device evaluates them: for each t in [0, 1) the J values
  * (-1)^j kernel(t + J/2 - 1 - j), j = 0..J-1, from the fitted polynomials
  * evaluated in the precision's arithmetic (out: n * J doubles).  Returns the

@@ -25,6 +25,10 @@ struct purify_gb300_operator {
 struct purify_gb300_plan {
   pg::Plan plan;
 };
+struct purify_gb300_walk_plan {
+  pg::WalkPlan plan;
+  int ntu = 0, ntv = 0;
+};
 struct purify_gb300_psf {
   std::unique_ptr<pg::PsfConvolve> impl;
 };
@@ -124,6 +128,7 @@ pg::OperatorConfig to_config(const purify_gb300_create_args *a, const purify_gb3
     c.class_cap = t->class_cap;
     c.keep_store = t->keep_store;
     c.fft_columns = t->fft_columns;
+    c.grid_walk = t->grid_walk;
   }
   if (a->precision != PURIFY_GB300_FP32 && a->precision != PURIFY_GB300_FP64)
     throw pg::Error(pg::kInvalidArgument, "unknown precision");
@@ -387,6 +392,8 @@ int purify_gb300_operator_info(const purify_gb300_operator *op, purify_gb300_inf
     info->window_cells = i.window_cells;
     info->factor_values = i.factor_values;
     info->cell_group = i.cell_group;
+    info->walk_tasks = i.walk_tasks;
+    info->walk_steps = i.walk_steps;
   });
 }
 
@@ -540,6 +547,68 @@ int purify_gb300_plan_export(const purify_gb300_plan *p, double *frac, double *w
 }
 
 int purify_gb300_plan_destroy(purify_gb300_plan *p) {
+  delete p;
+  return PURIFY_GB300_OK;
+}
+
+int purify_gb300_walk_plan_create(const double *u, const double *v, int64_t M, uint32_t ftsizeu,
+                                  uint32_t ftsizev, uint32_t J, purify_gb300_walk_plan **out) {
+  if (!out) return null_arg("out");
+  *out = nullptr;
+  if (M > 0 && (!u || !v)) return null_arg("u / v");
+  return guard([&] {
+    pg::PlanRequest rq;
+    rq.u = u;
+    rq.v = v;
+    rq.M = M;
+    rq.Nu = int(ftsizeu);
+    rq.Nv = int(ftsizev);
+    rq.Ju = rq.Jv = int(J);
+    std::unique_ptr<purify_gb300_walk_plan> p(new purify_gb300_walk_plan);
+    try {
+      p->plan = pg::build_walk_plan(rq);
+    } catch (const std::invalid_argument &e) {
+      throw pg::Error(pg::kInvalidArgument, e.what());
+    }
+    p->ntu = pg::make_tiling(rq.Nu, rq.tile).n;
+    p->ntv = pg::make_tiling(rq.Nv, rq.tile).n;
+    *out = p.release();
+  });
+}
+int purify_gb300_walk_plan_sizes(const purify_gb300_walk_plan *p, int64_t *sizes) {
+  if (!p) return null_arg("plan");
+  if (!sizes) return null_arg("sizes");
+  const pg::WalkPlan &W = p->plan;
+  const int64_t s[8] = {W.M, int64_t(W.tasks.size()), p->ntu, p->ntv, W.win_rows, W.win_cols,
+                        W.win_stride, W.steps};
+  std::copy(s, s + 8, sizes);
+  return PURIFY_GB300_OK;
+}
+int purify_gb300_walk_plan_export(const purify_gb300_walk_plan *p, double *frac,
+                                  int32_t *slot_user, int32_t *counts, int32_t *colstart,
+                                  int32_t *tasks, int32_t *task_order, int32_t *tile_tasks) {
+  if (!p) return null_arg("plan");
+  const pg::WalkPlan &W = p->plan;
+  for (int64_t s = 0; s < W.M; ++s) {
+    if (frac) {
+      frac[2 * s] = W.flip[s] ? -W.frac_u[s] : W.frac_u[s];
+      frac[2 * s + 1] = W.frac_v[s];
+    }
+    if (slot_user) slot_user[s] = W.slot_user[s];
+  }
+  if (counts) std::copy(W.counts.begin(), W.counts.end(), counts);
+  if (colstart) std::copy(W.colstart.begin(), W.colstart.end(), colstart);
+  if (tasks)
+    for (size_t k = 0; k < W.tasks.size(); ++k) {
+      const pg::Task &t = W.tasks[k];
+      const int32_t row[8] = {t.P, t.Q, t.H, t.W, 0, 0, t.tile, 0};
+      std::copy(row, row + 8, tasks + 8 * k);
+    }
+  if (task_order) std::copy(W.task_order.begin(), W.task_order.end(), task_order);
+  if (tile_tasks) std::copy(W.tile_tasks.begin(), W.tile_tasks.end(), tile_tasks);
+  return PURIFY_GB300_OK;
+}
+int purify_gb300_walk_plan_destroy(purify_gb300_walk_plan *p) {
   delete p;
   return PURIFY_GB300_OK;
 }

@@ -264,6 +264,42 @@ cudaError_t launch_grid(const ApplyArgs<real> &a, const PolyTable<real> &poly, i
   return launch_apply<real, false>(false, b, poly, J, ntasks, smem, shape.threads, s);
 }
 
+template <typename real, int J, bool SUB>
+cudaError_t launch_walk_one(const WalkArgs<real> &a, const PolyTable<real> &poly, int ntasks,
+                            int threads, cudaStream_t s) {
+  const size_t smem = walk_smem_bytes(sizeof(real), a.win_rows, a.win_stride, a.max_steps);
+  auto fn = walk_grid_kernel<real, J, SUB>;
+  if (smem > 48 * 1024) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+  }
+  fn<<<ntasks, threads, smem, s>>>(a, poly);
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_walk_grid(const WalkArgs<real> &a, const PolyTable<real> &poly, int J,
+                             int ntasks, int threads, cudaStream_t s) {
+  if (ntasks == 0) return cudaSuccess;
+  if (threads != 32 * kWalkWarps || a.win_stride % 2 == 0 || a.max_steps < 1)
+    return cudaErrorInvalidValue;
+  const bool sub = poly.nsub_u > 1 || poly.nsub_v > 1;
+  switch (J) {
+#define PG_WALK(JJ)                                                                        case JJ:                                                                                   return sub ? launch_walk_one<real, JJ, true>(a, poly, ntasks, threads, s)                          : launch_walk_one<real, JJ, false>(a, poly, ntasks, threads, s);
+    PG_WALK(1)
+    PG_WALK(2)
+    PG_WALK(3)
+    PG_WALK(4)
+    PG_WALK(5)
+    PG_WALK(6)
+    PG_WALK(7)
+    PG_WALK(8)
+#undef PG_WALK
+  }
+  return cudaErrorInvalidValue;
+}
+
 template <typename real>
 cudaError_t launch_fold(const FoldArgs &f, cudaStream_t s) {
   fold_kernel<real><<<f.ntu * f.ntv, dim3(32, 8), 0, s>>>(f);
@@ -384,6 +420,8 @@ cudaError_t launch_fill(void *x, int64_t n, double value, cudaStream_t s) {
   template cudaError_t launch_grid<real>(const ApplyArgs<real> &, const PolyTable<real> &, int,   \
                                          int, int, int, const LaunchShape &, cudaStream_t);     \
   template cudaError_t launch_fold<real>(const FoldArgs &, cudaStream_t);                       \
+  template cudaError_t launch_walk_grid<real>(const WalkArgs<real> &, const PolyTable<real> &,  \
+                                              int, int, int, cudaStream_t);                     \
   template cudaError_t launch_pad<real>(const void *, const real *, const real *, void *, int,  \
                                         int, int, int, int, cudaStream_t);                      \
   template cudaError_t launch_crop<real>(const void *, const real *, const real *, void *, int, \

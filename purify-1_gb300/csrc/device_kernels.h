@@ -74,6 +74,33 @@ cudaError_t launch_grid(const ApplyArgs<real> &a, const PolyTable<real> &poly, i
                         int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
                         cudaStream_t s);
 
+// The same half of G^H on the column-walk plan (plan.h WalkPlan): slot-ordered
+// visibilities in, one window per task out, in the layout the fold reads.
+template <typename real>
+struct WalkArgs {
+  const Task *tasks = nullptr;
+  const int32_t *order = nullptr;     // launch order of the tasks
+  const int32_t *counts = nullptr;    // tasks x 32 columns x 32 rows
+  const int32_t *colstart = nullptr;  // tasks x 33
+  const void *frac = nullptr;         // S x (t_u, t_v), the phase flip in the sign of t_u
+  const void *slot_in = nullptr;      // S complex, slot order
+  void *tilebuf = nullptr;            // one window per task, slot_stride cells apart
+  int64_t slot_stride = 0;
+  int win_stride = 0;                 // odd
+  int win_rows = 0;                   // rows of the largest window
+  int max_steps = 0;                  // capacity of a warp's step list (plan's max_warp_steps)
+};
+template <typename real>
+cudaError_t launch_walk_grid(const WalkArgs<real> &a, const PolyTable<real> &poly, int J,
+                             int ntasks, int threads, cudaStream_t s);
+// Shared memory of a column-walk CTA: kWalkWarps windows of win_rows x
+// win_stride cells, and per warp a list of max_steps steps and its column
+// offsets into it.
+inline size_t walk_smem_bytes(int precision_bytes, int win_rows, int win_stride, int max_steps) {
+  return size_t(kWalkWarps) * (size_t(win_rows) * win_stride * 2 * precision_bytes +
+                               size_t(max_steps) * 8 + 9 * 4);
+}
+
 // Grouped forms: `a.tasks` lists the tasks of several operators (Task::channel
 // names the operator), `a.group` points at a device array of their ApplyArgs
 // and `a.group_task_base` at the first grouped task of each; win_rows /

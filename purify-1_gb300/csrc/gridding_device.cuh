@@ -486,6 +486,166 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
   }
 }
 
+// G^H on the column-walk plan, one CTA per task (an occupied tile), kWalkWarps
+// warps with a shared-memory window each.  Warp w takes the tile's base-cell
+// columns [w W / nw, (w + 1) W / nw); its lane r is row r.  Each lane keeps a
+// J x J block of the window in registers that slides along its row: the
+// block's physical column p holds window column q with q mod J = p.  At
+// column q the lane adds the visibilities of base cell (r, q) (their taps
+// reach columns q ... q + J - 1), then window column q is complete for this
+// lane and is flushed: J read-modify-writes of cells (r + jv, q), one per
+// step, steps ordered by __syncwarp.  In one step the 32 lanes touch 32
+// distinct rows of one column, which an odd row stride spreads over every
+// bank pair; a cell that two lanes reach (r + jv = r' + jv') is reached in
+// different steps.  After its last column the warp flushes the J - 1
+// columns its blocks still hold.  So a lane flushes J cells per column
+// instead of J x J per work item.
+//
+// The warp first lists its steps in shared memory, one (first slot, active
+// lanes) pair per (column, k), from its columns' counts; the main loop then
+// keeps kWalkAhead steps of slot loads in flight across column boundaries.
+// The windows are summed in warp order into the task's window, as in
+// grid_kernel.
+constexpr int kWalkAhead = 3;
+constexpr int kWalkMaxCols = 8;  // columns of one warp: 32 / kWalkWarps
+template <typename real, int J, bool SUB>
+__global__ void __launch_bounds__(128, (sizeof(real) == 4 && J <= 6) ? 4 : 2) walk_grid_kernel(const WalkArgs<real> a,
+                                                        const __grid_constant__ PolyTable<real> poly) {
+  using C = cplx<real>;
+  static_assert(kWalkMaxCols * kWalkWarps >= 32, "a warp's columns");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int task_id = a.order ? a.order[blockIdx.x] : int(blockIdx.x);
+  const Task tk = a.tasks[task_id];
+  const int WW = tk.W + J - 1, WH = tk.H + J - 1, WS = a.win_stride, WN = a.win_rows * WS;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  C *wins = reinterpret_cast<C *>(smem_raw);
+  int2 *steps = reinterpret_cast<int2 *>(smem_raw + size_t(nw) * WN * sizeof(C)) +
+                size_t(warp) * a.max_steps;
+  int *colstep = reinterpret_cast<int *>(smem_raw + size_t(nw) * WN * sizeof(C) +
+                                         size_t(nw) * a.max_steps * sizeof(int2)) +
+                 warp * (kWalkMaxCols + 1);
+  for (int idx = threadIdx.x; idx < nw * WN; idx += blockDim.x) wins[idx] = C{0, 0};
+  C *mine = wins + warp * WN;
+  const int q0 = warp * tk.W / nw, q1 = (warp + 1) * tk.W / nw;
+  const unsigned lt = (1u << lane) - 1u;
+  {
+    // the warp's step list: the counts of its columns in flight together
+    const int32_t *cnt = a.counts + size_t(task_id) * 32 * 32;
+    int c[kWalkMaxCols];
+#pragma unroll
+    for (int i = 0; i < kWalkMaxCols; ++i) c[i] = q0 + i < q1 ? __ldg(cnt + (q0 + i) * 32 + lane) : 0;
+    int base = q0 < q1 ? __ldg(a.colstart + size_t(task_id) * 33 + q0) : 0;
+    int n = 0;
+#pragma unroll
+    for (int i = 0; i < kWalkMaxCols; ++i) {
+      if (lane == 0) colstep[i] = n;
+      const int kmax = __reduce_max_sync(0xffffffffu, c[i]);
+      for (int k = 0; k < kmax; ++k) {
+        const unsigned m = __ballot_sync(0xffffffffu, c[i] > k);
+        if (lane == 0) steps[n] = make_int2(base, int(m));
+        base += __popc(m);
+        ++n;
+      }
+    }
+    if (lane == 0) colstep[kWalkMaxCols] = n;
+  }
+  __syncthreads();
+  const C *frac = static_cast<const C *>(a.frac);
+  const C *vin = static_cast<const C *>(a.slot_in);
+  const bool row_live = lane < tk.H;
+  const int nsteps = colstep[kWalkMaxCols];
+  // ring of the next kWalkAhead steps' loads
+  C rt[kWalkAhead], ry[kWalkAhead];
+  unsigned rm[kWalkAhead];
+  auto fetch = [&](int j, C &t, C &y, unsigned &m) {
+    m = 0;
+    if (j < nsteps) {
+      const int2 st = steps[j];
+      m = unsigned(st.y);
+      if ((m >> lane) & 1u) {
+        const int slot = st.x + __popc(m & lt);
+        t = stream_load(frac + slot);
+        y = __ldcs(vin + slot);
+      }
+    }
+  };
+#pragma unroll
+  for (int d = 0; d < kWalkAhead; ++d) {
+    rt[d] = C{0, 0};
+    ry[d] = C{0, 0};
+    fetch(d, rt[d], ry[d], rm[d]);
+  }
+  int i = 0;
+  C acc[J][J];
+#pragma unroll
+  for (int jv = 0; jv < J; ++jv)
+#pragma unroll
+    for (int p = 0; p < J; ++p) acc[jv][p] = C{0, 0};
+  if (q0 < q1) {
+    // columns qb, qb + 1, ... in blocks of J, so that a column's physical
+    // block column (q mod J) is known at compile time in the unrolled body
+    const int qb = q0 - q0 % J;
+    for (int qq = qb; qq < q1 + J - 1; qq += J) {
+#pragma unroll
+      for (int p = 0; p < J; ++p) {
+        const int q = qq + p;
+        if (q >= q0 && q < q1) {
+          const int end = colstep[q - q0 + 1];
+          for (; i < end; ++i) {
+            const C t = rt[0], yv = ry[0];
+            const unsigned m = rm[0];
+#pragma unroll
+            for (int d = 0; d + 1 < kWalkAhead; ++d) {
+              rt[d] = rt[d + 1];
+              ry[d] = ry[d + 1];
+              rm[d] = rm[d + 1];
+            }
+            fetch(i + kWalkAhead, rt[kWalkAhead - 1], ry[kWalkAhead - 1], rm[kWalkAhead - 1]);
+            if ((m >> lane) & 1u) {
+              const real sg = copysign(real(1), t.x);
+              real ku[J], kv[J];
+              tap_weights<real, J, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
+              tap_weights<real, J, SUB>(poly.v, poly.nsub_v, t.y, kv);
+              const C z{sg * yv.x, sg * yv.y};
+#pragma unroll
+              for (int jv = 0; jv < J; ++jv) {
+                const C az = mul2(z, splat(kv[jv]));
+#pragma unroll
+                for (int ju = 0; ju < J; ++ju)
+                  acc[jv][(p + ju) % J] = fma2(az, splat(ku[ju]), acc[jv][(p + ju) % J]);
+              }
+            }
+          }
+        }
+        if (q >= q0 && q < q1 + J - 1) {
+          // window column q is complete: flush physical column p
+#pragma unroll
+          for (int jv = 0; jv < J; ++jv) {
+            if (row_live) {
+              C *cell = mine + (lane + jv) * WS + q;
+              *cell = add2(*cell, acc[jv][p]);
+            }
+            acc[jv][p] = C{0, 0};
+            __syncwarp();
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  C *out = static_cast<C *>(a.tilebuf) + size_t(task_id) * a.slot_stride;
+  for (int idx = threadIdx.x; idx < WW * WH; idx += blockDim.x) {
+    const int lp = idx / WW, e = lp * WS + (idx - lp * WW);
+    C s = wins[e];
+    for (int w = 1; w < nw; ++w) {
+      const C o = wins[w * WN + e];
+      s.x += o.x;
+      s.y += o.y;
+    }
+    out[idx] = s;
+  }
+}
+
 // One CTA per tile.  A cell sums, in this order, the windows of its own
 // tile's tasks, then those of the tile above, the tile to the left and the
 // tile above-left, where their J - 1 halo rows / columns reach into it.

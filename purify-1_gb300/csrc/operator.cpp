@@ -37,6 +37,15 @@ real fraction_in_cell(double x) {
 template float fraction_in_cell<float>(double);
 template double fraction_in_cell<double>(double);
 
+namespace {
+// The column walk of G^H: CTA size (4 warps, a quarter of the tile's columns
+// each), and the fullest base cell it takes (one lane walks a cell's
+// visibilities alone; a coverage with fuller cells keeps the work items,
+// which split a cell over several lanes).
+constexpr int kWalkThreads = 128;
+constexpr int kWalkMaxCellCount = 256;
+}  // namespace
+
 void cuda_check(cudaError_t e, const char *what) {
   if (e == cudaSuccess) return;
   if (e == cudaErrorMemoryAllocation)
@@ -108,7 +117,10 @@ class OperatorT final : public Operator {
   // Phi' / Phi'^H with visibilities kept in slot order (power method).
   FftArgs fft_args() const;
   void forward_slots(const void *x, void *caller_vis = nullptr);
-  void adjoint_slots(void *x, const void *caller_vis = nullptr);
+  void adjoint_slots(void *x, const void *caller_vis = nullptr, bool walk = false);
+  // G^H of the column-walk plan: ws->slots (walk order) -> task windows -> grid
+  void walk_grid(void *grid);
+  void fold_into(void *grid, const void *windows, const int32_t *tile_tasks);
   // Phi'^H Phi' x with the visibilities kept in slot order between G and G^H
   // (power method, normal operator); the weights' conjugates are applied there.
   void normal_slots(const void *x, void *out);
@@ -170,6 +182,12 @@ class OperatorT final : public Operator {
   // own_cols_: the column transforms run as the library's column pass
   // (launch_fft_cols); otherwise through the workspace's cuFFT column plan
   bool own_cols_ = false;
+  // Column-walk plan of G^H (used by Phi^H from caller order when walk_)
+  bool walk_ = false;
+  int walk_ntasks_ = 0, walk_win_rows_ = 0, walk_win_stride_ = 0, walk_max_steps_ = 0;
+  int64_t walk_steps_ = 0;
+  DeviceBuffer walk_frac_, walk_user_, walk_weight_, walk_counts_, walk_colstart_, walk_tasks_,
+      walk_order_, walk_tile_tasks_;
   DeviceBuffer tw_v_;
   bool use_fused_fft() const { return fused_fft_ && (own_cols_ || ws_->fft_cols != 0); }
   FftColArgs col_args(const void *in, void *out) const;
@@ -370,6 +388,8 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
   info_.window_cells = slot_stride_;
   info_.factor_values = factor_values_;
   info_.cell_group = group_;
+  info_.walk_tasks = walk_ ? walk_ntasks_ : 0;
+  info_.walk_steps = walk_ ? walk_steps_ : 0;
 
   set_norm(1.0);
   if (cfg.power_iters > 0) power_method(cfg.power_iters, cfg.power_tol);
@@ -462,6 +482,64 @@ void OperatorT<real>::init_plain(const OperatorConfig &cfg, int64_t &bytes, Axis
   tu = plan.tu;
   tv = plan.tv;
   tile_tasks = plan.tile_tasks;
+
+  // The column-walk plan of G^H: single-cell items, tiles of at most 32, a
+  // support whose J x J register block stays in registers, and no cell so
+  // full that one lane would walk it alone for long.
+  const int jmax = sizeof(real) == 8 ? 6 : 8;
+  WalkPlan wp;
+  if (cfg.grid_walk == 1 && group_ == 1 && rq.tile <= 32 && cfg.Ju == cfg.Jv && cfg.Ju <= jmax &&
+      M_ > 0 && plan.max_cell_count <= kWalkMaxCellCount) {
+    try {
+      wp = build_walk_plan(rq);
+    } catch (const std::invalid_argument &e) {
+      throw Error(kInvalidArgument, e.what());
+    }
+    int optin = 0;
+    cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_),
+               "cudaDeviceGetAttribute");
+    walk_ = walk_smem_bytes(sizeof(real), wp.win_rows, wp.win_stride,
+                            std::max(wp.max_warp_steps, 1)) <= size_t(optin);
+  }
+  if (walk_) {
+    walk_max_steps_ = std::max(wp.max_warp_steps, 1);
+    walk_ntasks_ = int(wp.tasks.size());
+    walk_win_rows_ = wp.win_rows;
+    walk_win_stride_ = wp.win_stride;
+    walk_steps_ = wp.steps;
+    std::vector<C> wf(M_);
+    for (int64_t i = 0; i < M_; ++i) {
+      const real tu = fraction_in_cell<real>(wp.frac_u[i]);
+      wf[i] = C(wp.flip[i] ? -tu : tu, fraction_in_cell<real>(wp.frac_v[i]));
+    }
+    walk_frac_.alloc(sizeof(C) * M_, &bytes);
+    walk_frac_.upload(wf.data(), sizeof(C) * M_, stream_);
+    walk_user_.alloc(sizeof(int32_t) * M_, &bytes);
+    walk_user_.upload(wp.slot_user.data(), sizeof(int32_t) * M_, stream_);
+    std::vector<C> ww;
+    if (split_weights_) {
+      // caller weights in walk order, for the gather before G^H
+      const auto *w = reinterpret_cast<const std::complex<double> *>(cfg.weights);
+      ww.resize(M_);
+      for (int64_t s = 0; s < M_; ++s) {
+        const std::complex<double> x = w[wp.slot_user[s]];
+        ww[s] = C(real(x.real()), real(x.imag()));
+      }
+      walk_weight_.alloc(sizeof(C) * M_, &bytes);
+      walk_weight_.upload(ww.data(), sizeof(C) * M_, stream_);
+    }
+    walk_counts_.alloc(sizeof(int32_t) * wp.counts.size(), &bytes);
+    walk_counts_.upload(wp.counts.data(), sizeof(int32_t) * wp.counts.size(), stream_);
+    walk_colstart_.alloc(sizeof(int32_t) * wp.colstart.size(), &bytes);
+    walk_colstart_.upload(wp.colstart.data(), sizeof(int32_t) * wp.colstart.size(), stream_);
+    walk_tasks_.alloc(sizeof(Task) * wp.tasks.size(), &bytes);
+    walk_tasks_.upload(wp.tasks.data(), sizeof(Task) * wp.tasks.size(), stream_);
+    walk_order_.alloc(sizeof(int32_t) * wp.task_order.size(), &bytes);
+    walk_order_.upload(wp.task_order.data(), sizeof(int32_t) * wp.task_order.size(), stream_);
+    walk_tile_tasks_.alloc(sizeof(int32_t) * wp.tile_tasks.size(), &bytes);
+    walk_tile_tasks_.upload(wp.tile_tasks.data(), sizeof(int32_t) * wp.tile_tasks.size(), stream_);
+    cuda_check(cudaStreamSynchronize(stream_), "upload");
+  }
 }
 
 template <typename real>
@@ -686,7 +764,7 @@ void OperatorT<real>::grid_core(void *grid, const void *vis, const int32_t *slot
     cuda_check(launch_wgrid<real>(w, ntasks_, win_rows_, win_cols_, ws_->stream),
                "w grid");
     mark_end(kGrid);
-    fold_into(grid, windows);
+    fold_into(grid, windows, tile_tasks_.as<int32_t>());
     return;
   }
   ApplyArgs<real> a;
@@ -710,15 +788,36 @@ void OperatorT<real>::grid_core(void *grid, const void *vis, const int32_t *slot
   cuda_check(launch_grid<real>(a, poly_, J_, ntasks_, win_rows_, win_cols_, shape_, ws_->stream),
              "grid");
   mark_end(kGrid);
-  fold_into(grid, windows);
+  fold_into(grid, windows, tile_tasks_.as<int32_t>());
 }
 
 template <typename real>
-void OperatorT<real>::fold_into(void *grid, const void *windows) {
+void OperatorT<real>::walk_grid(void *grid) {
+  WalkArgs<real> a;
+  a.tasks = walk_tasks_.as<Task>();
+  a.order = walk_order_.as<int32_t>();
+  a.counts = walk_counts_.as<int32_t>();
+  a.colstart = walk_colstart_.as<int32_t>();
+  a.frac = walk_frac_.get();
+  a.slot_in = ws_->slots;
+  a.tilebuf = ws_->tilebuf;
+  a.slot_stride = slot_stride_;
+  a.win_stride = walk_win_stride_;
+  a.win_rows = walk_win_rows_;
+  a.max_steps = walk_max_steps_;
+  mark_begin(kGrid);
+  cuda_check(launch_walk_grid<real>(a, poly_, J_, walk_ntasks_, kWalkThreads, ws_->stream),
+             "walk grid");
+  mark_end(kGrid);
+  fold_into(grid, ws_->tilebuf, walk_tile_tasks_.as<int32_t>());
+}
+
+template <typename real>
+void OperatorT<real>::fold_into(void *grid, const void *windows, const int32_t *tile_tasks) {
   FoldArgs f;
   f.tilebuf = windows;
   f.slot_stride = slot_stride_;
-  f.tile_tasks = tile_tasks_.as<int32_t>();
+  f.tile_tasks = tile_tasks;
   f.tu_start = tu_start_.as<int32_t>();
   f.tv_start = tv_start_.as<int32_t>();
   f.tu_of = tu_of_.as<int32_t>();
@@ -819,8 +918,11 @@ void OperatorT<real>::forward_slots(const void *x, void *caller_vis) {
 }
 
 template <typename real>
-void OperatorT<real>::adjoint_slots(void *x, const void *caller_vis) {
-  grid_slots(ws_->work, caller_vis);
+void OperatorT<real>::adjoint_slots(void *x, const void *caller_vis, bool walk) {
+  if (walk)
+    walk_grid(ws_->work);
+  else
+    grid_slots(ws_->work, caller_vis);
   if (use_fused_fft()) {
     mark_begin(kFftI);
     if (own_cols_)
@@ -870,11 +972,17 @@ void OperatorT<real>::adjoint_on_stream(const void *y, void *x) {
     return;
   }
   mark_begin(kExpand);
-  cuda_check(launch_expand<real>(y, slot_user_.as<int32_t>(), ws_->slots, S_, ws_->stream,
-                                 keep_vis_l2_ && ws_ == &own_, slot_weights()),
-             "expand");
+  if (walk_)
+    cuda_check(launch_expand<real>(y, walk_user_.as<int32_t>(), ws_->slots, M_, ws_->stream,
+                                   keep_vis_l2_ && ws_ == &own_,
+                                   split_weights_ ? walk_weight_.get() : nullptr),
+               "expand");
+  else
+    cuda_check(launch_expand<real>(y, slot_user_.as<int32_t>(), ws_->slots, S_, ws_->stream,
+                                   keep_vis_l2_ && ws_ == &own_, slot_weights()),
+               "expand");
   mark_end(kExpand);
-  adjoint_slots(x);
+  adjoint_slots(x, nullptr, walk_);
 }
 
 template <typename real>

@@ -56,6 +56,11 @@ struct OperatorConfig {
   // 0: the library's column pass where it applies (grid height <= 2048),
   // 1: cuFFT's strided column plan
   int fft_columns = 0;
+  // G^H of Phi^H: 1 = the column walk (plan.h WalkPlan) where it applies,
+  // 0 = the work-item kernel.  The walk flushes a third of the shared-memory
+  // traffic but runs 2.2x the visibility steps on the 10^7 workload (a
+  // column lasts as long as its fullest row), and measured slower there.
+  int grid_walk = 0;
 };
 
 // A plan fraction t + d (see PlanRequest::group) in precision `real`, kept
@@ -78,6 +83,7 @@ struct OperatorInfo {
   double kernel_fit_error = 0, norm = 1;
   int device = 0;
   int64_t slots = 0, window_cells = 0, factor_values = 0, cell_group = 1;
+  int64_t walk_tasks = 0, walk_steps = 0;
 };
 
 // Scratch of one apply held outside the operator, so that several applies of

@@ -48,6 +48,9 @@ constexpr int kCoefF32 = 9;
 constexpr int kCoefF64 = 17;
 // Tile edge (in grid cells) of the uv tiling.
 constexpr int kTile = 32;
+// Warps of a column-walk task of G^H; warp w takes base-cell columns
+// [w W / kWalkWarps, (w + 1) W / kWalkWarps) of a tile W <= 32 wide.
+constexpr int kWalkWarps = 4;
 // Lanes per batch: every batch holds 32 work items, one per lane.
 constexpr int kBatch = 32;
 // Most batches one CTA task may hold (its headers are staged in shared memory).

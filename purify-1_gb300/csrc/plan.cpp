@@ -330,4 +330,138 @@ Plan build_plan(const PlanRequest &rq) {
   return P;
 }
 
+WalkPlan build_walk_plan(const PlanRequest &rq) {
+  if (rq.M < 0 || (rq.M > 0 && (!rq.u || !rq.v)))
+    throw std::invalid_argument("bad visibility coordinates");
+  if (rq.group != 1) throw std::invalid_argument("the column walk takes single-cell items only");
+  if (rq.Ju < 1 || rq.Jv < 1 || rq.Nu < rq.Ju || rq.Nv < rq.Jv)
+    throw std::invalid_argument("kernel support and grid do not fit");
+  if (rq.M > int64_t(INT32_MAX) / 2)
+    throw std::invalid_argument("more visibilities than int32 slot indices can address");
+  WalkPlan W;
+  W.M = rq.M;
+  const AxisTiling tu = make_tiling(rq.Nu, rq.tile), tv = make_tiling(rq.Nv, rq.tile);
+  const int ntu = tu.n, ntv = tv.n, ntiles = ntu * ntv, T = W.T;
+  int wmax = 0, hmax = 0;
+  for (int b = 0; b < ntu; ++b) wmax = std::max(wmax, tu.start[b + 1] - tu.start[b]);
+  for (int a = 0; a < ntv; ++a) hmax = std::max(hmax, tv.start[a + 1] - tv.start[a]);
+  if (wmax > T || hmax > T) throw std::invalid_argument("the column walk needs tiles of at most 32");
+  for (int b = 0; b < ntu; ++b)
+    if (tu.start[b + 1] - tu.start[b] < rq.Ju - 1)
+      throw std::invalid_argument("grid width is too small for the kernel support");
+  for (int a = 0; a < ntv; ++a)
+    if (tv.start[a + 1] - tv.start[a] < rq.Jv - 1)
+      throw std::invalid_argument("grid height is too small for the kernel support");
+  W.win_rows = hmax + rq.Jv - 1;
+  W.win_cols = wmax + rq.Ju - 1;
+  W.win_stride = W.win_cols | 1;
+
+  // Per visibility, as build_plan with group 1: fractions, phase flip, tile
+  // and the base cell (row lp, column lq) inside it.
+  const int64_t M = rq.M;
+  std::vector<double> fu(M), fv(M);
+  std::vector<uint8_t> flip(M);
+  std::vector<int32_t> tile(M);
+  std::vector<int16_t> row(M), col(M);
+#pragma omp parallel for schedule(static)
+  for (int64_t m = 0; m < M; ++m) {
+    const double su = rq.u[m] - rq.Ju * 0.5, sv = rq.v[m] - rq.Jv * 0.5;
+    const double ku = std::floor(su), kv = std::floor(sv);
+    fu[m] = su - ku;
+    fv[m] = sv - kv;
+    const int q0 = int(wrap(ku + 1, rq.Nu));
+    const int p0 = int(wrap(kv + 1, rq.Nv));
+    flip[m] = uint8_t((int64_t(ku) + int64_t(kv)) & 1);
+    const int a = tv.of[p0], b = tu.of[q0];
+    tile[m] = a * ntu + b;
+    row[m] = int16_t(p0 - tv.start[a]);
+    col[m] = int16_t(q0 - tu.start[b]);
+  }
+  // Cells: tile-major, then column, then row; visibilities of a cell in
+  // caller order (stable counting sort).
+  const int64_t cells = int64_t(ntiles) * T * T;
+  std::vector<int64_t> cell_first(cells + 1, 0);
+  auto cell_of = [&](int64_t m) { return (int64_t(tile[m]) * T + col[m]) * T + row[m]; };
+  for (int64_t m = 0; m < M; ++m) cell_first[cell_of(m) + 1]++;
+  for (int64_t c = 0; c < cells; ++c) cell_first[c + 1] += cell_first[c];
+  std::vector<int32_t> sorted(M);
+  {
+    std::vector<int64_t> fill(cell_first.begin(), cell_first.end() - 1);
+    for (int64_t m = 0; m < M; ++m) sorted[fill[cell_of(m)]++] = int32_t(m);
+  }
+  // Tasks: occupied tiles in tile order.
+  W.tile_tasks.assign(ntiles + 1, 0);
+  std::vector<int32_t> task_tile;
+  for (int t = 0; t < ntiles; ++t) {
+    if (cell_first[int64_t(t + 1) * T * T] > cell_first[int64_t(t) * T * T]) {
+      const int a = t / ntu, b = t % ntu;
+      Task tk{};
+      tk.P = tv.start[a];
+      tk.Q = tu.start[b];
+      tk.H = tv.start[a + 1] - tv.start[a];
+      tk.W = tu.start[b + 1] - tu.start[b];
+      tk.tile = t;
+      W.tasks.push_back(tk);
+      task_tile.push_back(t);
+    }
+    W.tile_tasks[t + 1] = int32_t(W.tasks.size());
+  }
+  const int64_t ntasks = int64_t(W.tasks.size());
+  W.counts.assign(size_t(ntasks) * T * T, 0);
+  W.colstart.assign(size_t(ntasks) * (T + 1), 0);
+  std::vector<int64_t> cost(ntasks, 0);
+  // Slot positions: the walk order within each task; task k's slots start
+  // at the number of visibilities of the tasks before it.
+  std::vector<int32_t> slot_of_sorted(M);
+  int max_count = 0, max_warp_steps = 0;
+#pragma omp parallel for schedule(dynamic, 16) reduction(max : max_count, max_warp_steps)
+  for (int64_t k = 0; k < ntasks; ++k) {
+    const int64_t c0 = int64_t(task_tile[k]) * T * T;
+    const int wk = W.tasks[k].W;
+    int64_t s = cell_first[c0];  // visibilities before this tile, in tile order
+    int warp_steps[kWalkWarps] = {0};
+    for (int q = 0; q < T; ++q) {
+      W.colstart[size_t(k) * (T + 1) + q] = int32_t(s);
+      int kmax = 0;
+      for (int r = 0; r < T; ++r) {
+        const int n = int(cell_first[c0 + int64_t(q) * T + r + 1] - cell_first[c0 + int64_t(q) * T + r]);
+        W.counts[(size_t(k) * T + q) * T + r] = n;
+        kmax = std::max(kmax, n);
+      }
+      max_count = std::max(max_count, kmax);
+      cost[k] += kmax;
+      for (int w = 0; w < kWalkWarps; ++w)
+        if (q >= w * wk / kWalkWarps && q < (w + 1) * wk / kWalkWarps) warp_steps[w] += kmax;
+      for (int j = 0; j < kmax; ++j)
+        for (int r = 0; r < T; ++r) {
+          const int64_t c = c0 + int64_t(q) * T + r;
+          if (cell_first[c + 1] - cell_first[c] > j) slot_of_sorted[cell_first[c] + j] = int32_t(s++);
+        }
+    }
+    W.colstart[size_t(k) * (T + 1) + T] = int32_t(s);
+    for (int w = 0; w < kWalkWarps; ++w) max_warp_steps = std::max(max_warp_steps, warp_steps[w]);
+  }
+  W.max_count = max_count;
+  W.max_warp_steps = max_warp_steps;
+  for (int64_t k = 0; k < ntasks; ++k) W.steps += cost[k];
+  W.task_order.resize(ntasks);
+  std::iota(W.task_order.begin(), W.task_order.end(), 0);
+  std::stable_sort(W.task_order.begin(), W.task_order.end(),
+                   [&](int32_t x, int32_t y) { return cost[x] > cost[y]; });
+  W.frac_u.assign(M, 0.0);
+  W.frac_v.assign(M, 0.0);
+  W.flip.assign(M, 0);
+  W.slot_user.assign(M, -1);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < M; ++i) {
+    const int32_t m = sorted[i];
+    const int64_t s = slot_of_sorted[i];
+    W.frac_u[s] = fu[m];
+    W.frac_v[s] = fv[m];
+    W.flip[s] = flip[m];
+    W.slot_user[s] = m;
+  }
+  return W;
+}
+
 }  // namespace pg

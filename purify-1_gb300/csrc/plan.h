@@ -100,6 +100,38 @@ PG_HD inline int win_cells(int rows, int WS, int group) {
 // Builds the plan.  Throws std::invalid_argument on bad input.
 Plan build_plan(const PlanRequest &req);
 
+// The column-walk plan of G^H (see walk_grid_kernel).  Tiles are those of the
+// item plan (PlanRequest::tile <= 32), one task per occupied tile.  A warp's
+// 32 lanes are the tile's rows; it walks the tile's base-cell columns in
+// order, and at column q lane r takes the visibilities whose base cell is
+// (r, q).  Slots follow that walk: per task, per column, per k = 0, 1, ...,
+// the k-th visibility of every row that has more than k in that column, in
+// row order.  There are no null slots (S = M): lane r's slot at step k is the
+// column's running base plus the number of lower rows still active.
+struct WalkPlan {
+  int64_t M = 0;
+  int T = 32;  // lanes (rows) per task block, and the column stride of counts
+  std::vector<Task> tasks;          // one per occupied tile, in tile order
+  std::vector<int32_t> task_order;  // launch order: most column steps first
+  std::vector<int32_t> tile_tasks;  // ntiles + 1 offsets into tasks
+  std::vector<int32_t> counts;      // tasks x T columns x 32 rows
+  std::vector<int32_t> colstart;    // tasks x (T + 1): first slot of each column, then the end
+  std::vector<double> frac_u, frac_v;  // per slot, as in Plan (t in [0, 1))
+  std::vector<uint8_t> flip;
+  std::vector<int32_t> slot_user;   // caller index of each slot
+  int win_rows = 0, win_cols = 0;
+  int win_stride = 0;   // odd, so that a column of 32 rows covers 16 bank pairs per half-warp
+  int64_t steps = 0;    // sum over tasks and columns of the column's largest count
+  int max_count = 0;    // largest count of one cell
+  // Most steps of one warp: the sum of its columns' largest counts, with a
+  // task's columns split over kWalkWarps warps as the kernel splits them.
+  int max_warp_steps = 0;
+};
+
+// Builds the column-walk plan (group 1 only; every tile at most 32 x 32).
+// Throws std::invalid_argument on bad input.
+WalkPlan build_walk_plan(const PlanRequest &req);
+
 // Splits [0, n) into ceil(n / tile) nearly equal ranges (>= 1 range).
 AxisTiling make_tiling(int n, int tile);
 

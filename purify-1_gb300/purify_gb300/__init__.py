@@ -55,7 +55,8 @@ class Tuning(ctypes.Structure):
     _fields_ = [("threads", ctypes.c_int32), ("max_per_item", ctypes.c_int32),
                 ("tile", ctypes.c_int32), ("fused_permute", ctypes.c_int32),
                 ("cell_group", ctypes.c_int32), ("class_cap", ctypes.c_int32),
-                ("keep_store", ctypes.c_int32), ("fft_columns", ctypes.c_int32)]
+                ("keep_store", ctypes.c_int32), ("fft_columns", ctypes.c_int32),
+                ("grid_walk", ctypes.c_int32)]
 
 
 class Info(ctypes.Structure):
@@ -68,6 +69,7 @@ class Info(ctypes.Structure):
         ("device_bytes", ctypes.c_int64), ("kernel_fit_error", ctypes.c_double),
         ("norm", ctypes.c_double), ("slots", ctypes.c_int64), ("window_cells", ctypes.c_int64),
         ("factor_values", ctypes.c_int64), ("cell_group", ctypes.c_int64),
+        ("walk_tasks", ctypes.c_int64), ("walk_steps", ctypes.c_int64),
     ]
 
 
@@ -134,7 +136,9 @@ EXPORTS = [
     "purify_gb300_uv_to_pixels", "purify_gb300_fb_default_params", "purify_gb300_forward_backward",
     "purify_gb300_last_error", "purify_gb300_version", "purify_gb300_plan_create",
     "purify_gb300_plan_sizes", "purify_gb300_plan_export", "purify_gb300_plan_destroy",
-    "purify_gb300_plan_create_grouped",
+    "purify_gb300_plan_create_grouped", "purify_gb300_walk_plan_create",
+    "purify_gb300_walk_plan_sizes", "purify_gb300_walk_plan_export",
+    "purify_gb300_walk_plan_destroy",
     "purify_gb300_kernel_taps", "purify_gb300_degrid", "purify_gb300_grid",
     "purify_gb300_correction", "purify_gb300_stage_timing", "purify_gb300_stage_times",
     "purify_gb300_operator_create_tuned", "purify_gb300_grid_no_alloc",
@@ -198,6 +202,11 @@ def load(path=None):
     L.purify_gb300_plan_sizes.argtypes = [vp, vp]
     L.purify_gb300_plan_export.argtypes = [vp] + [vp] * 10
     L.purify_gb300_plan_destroy.argtypes = [vp]
+    L.purify_gb300_walk_plan_create.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_uint32,
+                                                ctypes.c_uint32, ctypes.c_uint32, P(vp)]
+    L.purify_gb300_walk_plan_sizes.argtypes = [vp, vp]
+    L.purify_gb300_walk_plan_export.argtypes = [vp] + [vp] * 7
+    L.purify_gb300_walk_plan_destroy.argtypes = [vp]
     L.purify_gb300_kernel_taps.argtypes = [ctypes.c_int32, ctypes.c_uint32, ctypes.c_double,
                                            ctypes.c_int32, vp, ctypes.c_int64, vp,
                                            P(ctypes.c_double)]
@@ -353,6 +362,38 @@ class CoveragePlan:
         self.Nu, self.Nv, self.J = int(ftsizeu), int(ftsizev), int(J)
 
 
+class WalkPlan:
+    """Host-side copy of the column-walk plan of G^H (purify_gb300_walk_plan_*)."""
+
+    def __init__(self, u, v, ftsizeu, ftsizev, J):
+        L = load()
+        u = np.ascontiguousarray(u, dtype=np.float64).ravel()
+        v = np.ascontiguousarray(v, dtype=np.float64).ravel()
+        h = ctypes.c_void_p()
+        _check(L.purify_gb300_walk_plan_create(_np_ptr(u), _np_ptr(v), u.size, int(ftsizeu),
+                                               int(ftsizev), int(J), ctypes.byref(h)))
+        try:
+            sz = np.zeros(8, dtype=np.int64)
+            _check(L.purify_gb300_walk_plan_sizes(h, _np_ptr(sz)))
+            M, nt, ntu, ntv, wr, wc, ws, steps = (int(s) for s in sz)
+            self.frac = np.empty((M, 2))
+            self.slot_user = np.empty(M, dtype=np.int32)
+            self.counts = np.empty((nt, 32, 32), dtype=np.int32)
+            self.colstart = np.empty((nt, 33), dtype=np.int32)
+            self.tasks = np.empty((nt, 8), dtype=np.int32)
+            self.task_order = np.empty(nt, dtype=np.int32)
+            self.tile_tasks = np.empty(ntu * ntv + 1, dtype=np.int32)
+            _check(L.purify_gb300_walk_plan_export(
+                h, _np_ptr(self.frac), _np_ptr(self.slot_user), _np_ptr(self.counts),
+                _np_ptr(self.colstart), _np_ptr(self.tasks), _np_ptr(self.task_order),
+                _np_ptr(self.tile_tasks)))
+        finally:
+            L.purify_gb300_walk_plan_destroy(h)
+        self.M, self.ntu, self.ntv = M, ntu, ntv
+        self.win_rows, self.win_cols, self.win_stride, self.steps = wr, wc, ws, steps
+        self.Nu, self.Nv, self.J = int(ftsizeu), int(ftsizev), int(J)
+
+
 def _create_args(u, v, w, weights, imsizey, imsizex, oversample_ratio, power_iters, power_tol,
                  kernel, Ju, Jv, w_term, Jw, cellx, celly, precision, device, jw_rows):
     """CreateArgs of the reference's factory arguments; returns the struct and
@@ -443,7 +484,8 @@ class MeasurementOperator:
             t = Tuning(int(tuning.get("threads", 0)), int(tuning.get("max_per_item", 0)),
                        int(tuning.get("tile", 0)), int(tuning.get("fused_permute", -1)),
                        int(tuning.get("cell_group", 0)), int(tuning.get("class_cap", 0)),
-                       int(tuning.get("keep_store", 0)), int(tuning.get("fft_columns", 0)))
+                       int(tuning.get("keep_store", 0)), int(tuning.get("fft_columns", 0)),
+                       int(tuning.get("grid_walk", 0)))
             _check(L.purify_gb300_operator_create_tuned(ctypes.byref(a), ctypes.byref(t),
                                                         ctypes.byref(h)))
         else:

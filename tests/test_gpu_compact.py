@@ -5,8 +5,10 @@ and the reference's power-method checks of both (tests/operators.cc:171-215:
 the normalised operators have norm 1 within power_tol).
 
 Tolerances (relative L2): FP64 1e-10, FP32 1e-5 (the parity bars of the
-measurement operator); normal vs adjoint(forward): exact (same kernels on the
-same values, only the visibility order between the halves differs)."""
+measurement operator); normal vs adjoint(forward): exact (same kernels on
+the same values, only the visibility order between the halves differs);
+against the column-walk G^H (tuning grid_walk = 1): 1e-6 (FP32), 1e-13
+(FP64), the summation order."""
 import numpy as np
 import pytest
 
@@ -42,6 +44,11 @@ def test_normal_equals_forward_then_adjoint(pg, cuda, precision):
     b = op.adjoint(op.forward(x))
     torch.cuda.synchronize()
     assert torch.equal(a, b)
+    walk = pg.MeasurementOperator(u, v, None, wt, n, n, 2.0, power_iters=0, precision=precision,
+                                  tuning={"grid_walk": 1})
+    walk.set_norm(op.norm)
+    c = walk.adjoint(walk.forward(x))
+    assert rel_l2(host(c), host(a)) < (1e-6 if precision == "fp32" else 1e-13)
     # in place
     y = x.clone()
     op.normal_into(y, y)

@@ -448,8 +448,8 @@ def test_weights_with_sub_segmented_taps(pg, oracle_mod, cuda, kernel, J, precis
 def test_caller_order_grid_is_bit_identical(pg, cuda, small_config, precision):
     """G^H reading the caller-ordered visibilities directly (the grid kernel
     gathers them, fused_permute = 1) sums the same values in the same order
-    as the gather into slot order followed by the slot-ordered grid kernel:
-    the two adjoints are bit-identical, as are the forwards."""
+    as the gather into slot order followed by the slot-ordered grid kernel
+    (work items): the two adjoints are bit-identical, as are the forwards."""
     torch = cuda
     c = small_config
     ops = [pg.MeasurementOperator(c["u"], c["v"], None, None, 256, 256, 2.0, power_iters=0,
@@ -493,3 +493,54 @@ def test_unequal_and_wide_supports(pg, oracle_mod, cuda, kernel, Ju, Jv, precisi
     assert rel_l2(xx, oop.adjoint(yy)) < TOL[precision]
     n_gpu, n_ref = gop.power_method(20, 0.0), oop.power_method(20, 0.0)
     assert abs(n_gpu - n_ref) / n_ref < TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("J,kernel,weighted", [(6, "kb", False), (4, "kb", True), (1, "kb", False),
+                                              (6, "pswf", False), (5, "kbmin", False),
+                                              (8, "gauss", True)])
+def test_column_walk_adjoint(pg, oracle_mod, cuda, precision, J, kernel, weighted):
+    """With tuning grid_walk = 1, Phi^H runs G^H as the column walk (tiles
+    of 32, lanes = rows, one column flushed per step): against the oracle,
+    against the work-item kernel on the same coverage (only the summation
+    order differs), and repeatable bit for bit."""
+    torch = cuda
+    if precision == "fp64" and J > 6:
+        pytest.skip("FP64 walks up to J = 6")
+    rng = np.random.default_rng(J + 10 * weighted)
+    M, n = 30000, 96
+    u = np.concatenate([rng.normal(0, 8, M // 2), rng.uniform(-n, n, M - M // 2)])
+    v = np.concatenate([rng.normal(0, 8, M // 2), rng.uniform(-n, n, M - M // 2)])
+    u[:300], v[:300] = u[300:600], v[300:600]  # cells with several visibilities
+    wt = (rng.uniform(0.5, 2, M) * np.exp(1j * rng.uniform(0, 2 * np.pi, M))) if weighted else None
+    ops = [pg.MeasurementOperator(u, v, None, wt, n, n, 2.0, power_iters=0, kernel=kernel, Ju=J,
+                                  Jv=J, precision=precision, tuning={"grid_walk": g})
+           for g in (1, 0)]
+    assert ops[0].info()["walk_tasks"] > 0 and ops[1].info()["walk_tasks"] == 0
+    oop = oracle_mod.Operator(u, v, None, wt, n, n, 2.0, kernel=kernel, Ju=J, Jv=J)
+    y = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    yd = to_dev(torch, y, precision)
+    a = to_np(ops[0].adjoint(yd))
+    b = to_np(ops[1].adjoint(yd))
+    assert rel_l2(a, oop.adjoint(y)) < TOL[precision]
+    assert rel_l2(a, b) < (1e-6 if precision == "fp32" else 1e-13)
+    assert np.array_equal(a, to_np(ops[0].adjoint(yd)))
+
+
+def test_column_walk_falls_back_on_full_cells(pg, oracle_mod, cuda):
+    """A coverage with more than 256 visibilities on one base cell keeps the
+    work items (which split a cell over lanes) even when the walk is asked
+    for."""
+    torch = cuda
+    rng = np.random.default_rng(4)
+    M = 5000
+    u = rng.normal(0, 10, M)
+    v = rng.normal(0, 10, M)
+    u[:400] = 0.25
+    v[:400] = -0.5
+    op = pg.MeasurementOperator(u, v, None, None, 64, 64, 2.0, power_iters=0, kernel="kb", Ju=4,
+                                Jv=4, precision="fp32", tuning={"grid_walk": 1})
+    assert op.info()["walk_tasks"] == 0
+    y = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    oop = oracle_mod.Operator(u, v, None, None, 64, 64, 2.0, kernel="kb", Ju=4, Jv=4)
+    assert rel_l2(to_np(op.adjoint(to_dev(torch, y, "fp32"))), oop.adjoint(y)) < TOL["fp32"]
