@@ -192,7 +192,7 @@ struct StageRadix {
   static constexpr int value = rem % 16 == 0 ? 16 : rem;
 };
 
-template <int N, int V, int Ns, int S, bool INV, int T = kFftThreads>
+template <int N, int V, int Ns, int S, bool INV, int T = kFftThreads, bool COLIO = false>
 __device__ __forceinline__ void load_twiddles(TwiddleCache &c, const float2 *__restrict__ tw) {
   constexpr int R = StageRadix<N, Ns>::value;
   constexpr int NB = V * (N / R);
@@ -202,7 +202,8 @@ __device__ __forceinline__ void load_twiddles(TwiddleCache &c, const float2 *__r
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
       const int flat = int(threadIdx.x) + q * T;
-      const int j = flat % (N / R);
+      // the last stage of a column pass takes its butterflies column-fastest
+      const int j = (COLIO && Ns * R == N) ? flat / V : flat % (N / R);
       const int step = (j % Ns) * (N / (Ns * R));
 #pragma unroll
       for (int e = 0; e < kMaxPow; ++e) {
@@ -214,15 +215,20 @@ __device__ __forceinline__ void load_twiddles(TwiddleCache &c, const float2 *__r
       }
     }
   }
-  if constexpr (Ns * R < N) load_twiddles<N, V, Ns * R, S + 1, INV, T>(c, tw);
+  if constexpr (Ns * R < N) load_twiddles<N, V, Ns * R, S + 1, INV, T, COLIO>(c, tw);
 }
 
 // Stage S (sub-transform length Ns) of an N-point transform of V rows.  With
-// SMIO the first stage reads and the last stage writes shared memory (the
-// column pass moves the data in and out itself); otherwise they read and
-// write global memory through load_in / store_out.
-template <int N, int V, int Ns, int S, bool INV, bool SMIO = false, int PAD = 0,
-          int T = kFftThreads>
+// COLIO the V "rows" are
+// V adjacent columns of a grid with row stride a.ld starting at column row0:
+// the first and last stages take their butterflies column-fastest (thread
+// flat -> column flat mod V, butterfly flat / V), so that the V threads of a
+// butterfly index read or write one contiguous V x 8-byte row segment; the
+// first stage reads only rows a.y0 ... a.y0+a.Ny-1 (forward), the last writes
+// only those rows (inverse).  Otherwise the first and last stages go through
+// load_in / store_out.
+template <int N, int V, int Ns, int S, bool INV, int PAD = 0, int T = kFftThreads,
+          bool COLIO = false>
 __device__ __forceinline__ void run_stages(const FftArgs &a, const float2 *__restrict__ in,
                                            float2 *__restrict__ out, float2 *sm,
                                            const TwiddleCache &tc, int row0) {
@@ -236,23 +242,30 @@ __device__ __forceinline__ void run_stages(const FftArgs &a, const float2 *__res
   for (int q = 0; q < Q; ++q) {
     const int flat = tid + q * T;
     if (flat < NB) {
-      const int rr = flat / (N / R), j = flat % (N / R);
+      // column-fastest butterflies in the first and last stages of a column pass
+      const bool cm = COLIO && (FIRST || LAST);
+      const int rr = cm ? flat % V : flat / (N / R), j = cm ? flat / V : flat % (N / R);
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const int n = j + r * (N / R);
-        if constexpr (FIRST && !SMIO)
+        if constexpr (FIRST && COLIO)
+          v[q][r] = (INV || (n >= a.y0 && n < a.y0 + a.Ny))
+                        ? in[size_t(n) * a.ld + row0 + rr]
+                        : make_float2(0.f, 0.f);
+        else if constexpr (FIRST)
           v[q][r] = load_in<INV>(a, in, row0 + rr, n);
         else
           v[q][r] = sm[sidx<N, PAD>(rr, n)];
       }
     }
   }
-  if constexpr (!FIRST || SMIO) __syncthreads();  // every read of this stage is done
+  if constexpr (!FIRST) __syncthreads();  // every read of this stage is done
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     const int flat = tid + q * T;
     if (flat < NB) {
-      const int rr = flat / (N / R), j = flat % (N / R);
+      const bool cm = COLIO && (FIRST || LAST);
+      const int rr = cm ? flat % V : flat / (N / R), j = cm ? flat / V : flat % (N / R);
       const int k = j % Ns;
       if constexpr (!FIRST) twiddle<R>(v[q], tc.w[S][q]);
       dft<R, INV>(v[q]);
@@ -260,16 +273,19 @@ __device__ __forceinline__ void run_stages(const FftArgs &a, const float2 *__res
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const int n = d + r * Ns;
-        if constexpr (LAST && !SMIO)
+        if constexpr (LAST && COLIO) {
+          if (!INV || (n >= a.y0 && n < a.y0 + a.Ny)) out[size_t(n) * a.ld + row0 + rr] = v[q][r];
+        } else if constexpr (LAST) {
           store_out<INV>(a, out, row0 + rr, n, v[q][r]);
-        else
+        } else {
           sm[sidx<N, PAD>(rr, n)] = v[q][r];
+        }
       }
     }
   }
   if constexpr (!LAST) {
     __syncthreads();
-    run_stages<N, V, Ns * R, S + 1, INV, SMIO, PAD, T>(a, in, out, sm, tc, row0);
+    run_stages<N, V, Ns * R, S + 1, INV, PAD, T, COLIO>(a, in, out, sm, tc, row0);
   }
 }
 
@@ -310,18 +326,20 @@ __global__ void __launch_bounds__(kFftThreads, 4) fft_row_group_kernel(
 }
 
 // Column pass: V adjacent columns per CTA, so that every row of the block is
-// one contiguous V x 8-byte segment (a full 32-byte sector at V = 4).  The
-// block is copied in with the column index fastest across threads, the
-// Stockham stages run on the V columns as V rows of shared memory, and the
-// result is copied out the same way.  Forward: only rows y0 ... y0+Ny-1 of
-// the input are read (the others are zero), all Nv rows are written.
-// Inverse: all rows are read, only rows y0 ... y0+Ny-1 are written.  With a
-// member table, the CTA's channel (column / Nu) gives y0 and Ny.
+// one contiguous V x 8-byte segment.  The first stage reads the block's rows
+// from global memory and the last stage writes them, both with the column
+// index fastest across threads (run_stages COLIO); the stages in between run
+// on the V columns as V rows of shared memory.  Forward: only rows y0 ...
+// y0+Ny-1 of the input are read (the others are zero), all Nv rows are
+// written.  Inverse: all rows are read, only rows y0 ... y0+Ny-1 are written.
+// With a member table, the CTA's channel (column / Nu) gives y0 and Ny.
 // V = 8 columns (64-byte row segments) from 256 rows up, 16 below; 512
 // threads once the block holds 16K points, so that each thread keeps two
-// radix-16 butterflies in registers.  Measured on 2048 x 2048: 8 columns
-// and 512 threads 25 us per pass, 4 columns and 256 threads 29 us, 2
-// columns 33 us.
+// radix-16 butterflies in registers.  Measured on 2048 x 2048 (forward /
+// inverse): 8 columns and 512 threads 22.6 / 21.5 us per pass, 4 columns and
+// 256 threads 24.6 / 24.2 us, 2 columns 30.9 / 28.4 us; cuFFT's strided
+// plan 25.2 / 25.2 us; the same shapes with copy-in and copy-out passes
+// through shared memory 25.5 / 24.3 us.
 constexpr int col_block(int N) { return N >= 256 ? 8 : 16; }
 constexpr int col_threads(int N) { return col_block(N) * N >= 16384 ? 512 : 256; }
 template <int N, int V>
@@ -329,48 +347,29 @@ struct ColPad {
   // rows of the block sit 16 / V banks (8-byte units) apart
   static constexpr int value = ((16 / V) - (N + N / 32) % 16 + 16) % 16;
 };
-constexpr int kColUnroll = 8;
 
-template <int N, int V, bool INV, int T = kFftThreads, int UNROLL = kColUnroll, int MINB = 2>
-__global__ void __launch_bounds__(T, MINB) fft_col_kernel(const FftColArgs c) {
+// The column pass with its first and last stages on global memory directly
+// (run_stages COLIO): no copy-in and copy-out passes through shared memory.
+template <int N, int V, bool INV, int T, int MINB>
+__global__ void __launch_bounds__(T, MINB) fft_col_direct_kernel(const FftColArgs c) {
   extern __shared__ float2 fft_sm[];
   constexpr int PAD = ColPad<N, V>::value;
   const int col0 = int(blockIdx.x) * V;
-  int y0 = c.y0, ny = c.Ny;
+  FftArgs a;
+  a.y0 = c.y0;
+  a.Ny = c.Ny;
+  a.ld = c.ld;
   if (c.members) {
     const ChannelIO<float> &io =
         static_cast<const ChannelIO<float> *>(c.chans)[c.members[col0 / c.Nu]];
-    y0 = io.y0;
-    ny = io.Ny;
+    a.y0 = io.y0;
+    a.Ny = io.Ny;
   }
-  const float2 *in = static_cast<const float2 *>(c.in);
-  float2 *out = static_cast<float2 *>(c.out);
-  const size_t ld = size_t(c.ld);
   TwiddleCache tc;
-  load_twiddles<N, V, 1, 0, INV, T>(tc, static_cast<const float2 *>(c.tw_v));
-  // UNROLL loads in flight per thread
-  for (int base = 0; base < N * V; base += T * UNROLL) {
-    float2 v[UNROLL];
-#pragma unroll
-    for (int u = 0; u < UNROLL; ++u) {
-      const int e = base + u * T + int(threadIdx.x);
-      const int rr = e % V, n = e / V;
-      v[u] = (e < N * V && (INV || (n >= y0 && n < y0 + ny))) ? in[size_t(n) * ld + col0 + rr]
-                                                              : make_float2(0.f, 0.f);
-    }
-#pragma unroll
-    for (int u = 0; u < UNROLL; ++u) {
-      const int e = base + u * T + int(threadIdx.x);
-      if (e < N * V) fft_sm[sidx<N, PAD>(e % V, e / V)] = v[u];
-    }
-  }
-  __syncthreads();
-  run_stages<N, V, 1, 0, INV, true, PAD, T>(FftArgs{}, nullptr, nullptr, fft_sm, tc, 0);
-  __syncthreads();
-  for (int e = int(threadIdx.x); e < N * V; e += T) {
-    const int rr = e % V, n = e / V;
-    if (!INV || (n >= y0 && n < y0 + ny)) out[size_t(n) * ld + col0 + rr] = fft_sm[sidx<N, PAD>(rr, n)];
-  }
+  load_twiddles<N, V, 1, 0, INV, T, true>(tc, static_cast<const float2 *>(c.tw_v));
+  run_stages<N, V, 1, 0, INV, PAD, T, true>(a, static_cast<const float2 *>(c.in),
+                                                   static_cast<float2 *>(c.out), fft_sm, tc,
+                                                   col0);
 }
 
 template <int N, bool INV>
@@ -378,7 +377,7 @@ cudaError_t launch_cols(const FftColArgs &c, cudaStream_t s) {
   constexpr int V = col_block(N), T = col_threads(N);
   constexpr int PAD = ColPad<N, V>::value;
   const size_t smem = sizeof(float2) * size_t(V) * (N + N / 32 + PAD);
-  auto fn = fft_col_kernel<N, V, INV, T, kColUnroll, T == 512 ? 1 : 2>;
+  auto fn = fft_col_direct_kernel<N, V, INV, T, T == 512 ? 1 : 2>;
   if (smem > 48 * 1024) {
     const cudaError_t e =
         cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
