@@ -673,6 +673,66 @@ __device__ __forceinline__ void fold_tile(const FoldArgs &f, int t) {
   const C *__restrict__ buf = static_cast<const C *>(f.tilebuf);
   C *__restrict__ grid = static_cast<C *>(f.grid);
   constexpr int R = 4;
+  if (H == 32 && W == 32 && f.Jv <= 9 && f.Ju <= 33) {
+    // Full tile, halos of at most 8 rows: thread (lq, ty) owns rows ty + 8 r
+    // of column lq; a halo row ty < Jv - 1 is in r = 0 only.  The same sums
+    // in the same order as below, with the per-row tests folded away and two
+    // task windows' loads in flight.
+    const int lq = int(threadIdx.x), ty = int(threadIdx.y);
+    const bool top = ty < f.Jv - 1, left = lq < f.Ju - 1;
+    C s[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) s[r] = C{0, 0};
+    const C *own = buf + lq + ty * WWo;
+#pragma unroll 2
+    for (int k = own0; k < own1; ++k) {
+      const C *w = own + k * ss;
+      C v[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[r] = w[8 * r * WWo];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        s[r].x += v[r].x;
+        s[r].y += v[r].y;
+      }
+    }
+    if (top) {
+      const C *up = buf + Hu * WWo + lq + ty * WWo;
+      for (int k = up0; k < up1; ++k) {
+        const C v = up[k * ss];
+        s[0].x += v.x;
+        s[0].y += v.y;
+      }
+    }
+    if (left) {
+      const C *lf = buf + lq + Wl + ty * WWl;
+#pragma unroll 2
+      for (int k = lf0; k < lf1; ++k) {
+        const C *w = lf + k * ss;
+        C v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = w[8 * r * WWl];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          s[r].x += v[r].x;
+          s[r].y += v[r].y;
+        }
+      }
+      if (top) {
+        const C *dg = buf + Hu * WWl + lq + Wl + ty * WWl;
+        for (int k = dg0; k < dg1; ++k) {
+          const C v = dg[k * ss];
+          s[0].x += v.x;
+          s[0].y += v.y;
+        }
+      }
+    }
+    const size_t ld = size_t(f.ld ? f.ld : f.Nu);
+    C *g = grid + (size_t(P) + ty) * ld + Q + lq;
+#pragma unroll
+    for (int r = 0; r < R; ++r) g[size_t(8 * r) * ld] = s[r];
+    return;
+  }
   for (int c0 = 0; c0 < W; c0 += 32) {
     const int lq = c0 + int(threadIdx.x);
     const bool col = lq < W, left = lq < f.Ju - 1;
