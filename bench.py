@@ -463,9 +463,10 @@ def run_gb300(args):
         "stages_ms_per_launch": {k: (ms / nl if nl else None) for k, (ms, nl) in stages.items()},
         "directions": directions,
         "adjoint_dot_test_fp32": adjoint_test,
-        # own kernels per step: the forward row pass (or pad), degrid, expand,
-        # grid, fold, the inverse row pass (or crop)
-        "gpu_launches": 6 * args.steps,
+        # own kernels per step: the forward row and column passes, degrid,
+        # expand, grid, fold, the inverse column and row passes (cuFFT's
+        # column plan instead of the column passes with --fft-columns 1)
+        "gpu_launches": (6 if args.fft_columns == 1 else 8) * args.steps,
         "clocks": clocks,
     }
 
@@ -687,9 +688,10 @@ def run_wproj(args):
         "device_bytes": info["device_bytes"], "factor_values": info["factor_values"],
         "clocks": clocks, "kernel_bytes": wbytes,
         "roofline": roofline_entry(kern, wbytes[kern], dur, peak, peak_kind, None, survey),
-        # own kernels per step: the forward row pass, w degrid, w grid, fold,
-        # the inverse row pass
-        "gpu_launches": 5 * args.steps,
+        # own kernels per step: the forward row pass, w degrid, the compaction
+        # into caller order, the gather into slot order, w grid, fold, the
+        # inverse row pass (the 4096-row columns go through cuFFT)
+        "gpu_launches": 7 * args.steps,
     }
     # FP32 rows against the FP64 oracle on a row sample (rows are independent)
     try:
@@ -821,7 +823,9 @@ def run_batch(args):
                      "grid_launch": t_grd},
         "create_s": t_create, "generate_s": t_gen, "power_method_s": t_power,
         "power_iters": args.power_iters, "device_bytes": info["device_bytes"],
-        "gpu_launches": 6 * args.steps, "clocks": clocks,
+        # own kernels per step: per grid size a row and a column pass each way
+        # (3 sizes), degrid, the gather, grid, fold
+        "gpu_launches": (4 * info["size_groups"] + 4) * args.steps, "clocks": clocks,
         "roofline": {"bound": "hbm", "kernel": kern, "algorithmic_bytes": alg_deg,
                      "achieved": alg_deg / (dur * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": alg_deg / (dur * 1e-3) / 1e9 / peak, "peak_source": peak_kind,
@@ -1052,11 +1056,12 @@ def run_serve(args):
         "latency_ms": f32["latency_ms"], "serving": {k: {kk: vv for kk, vv in v.items()
                                                           if kk != "_res"}
                                                       for k, v in per_prec.items()},
-        # own kernels per request (FP32): conversions, the forward row pass
-        # (or pad), degrid, expand, grid, fold, the inverse row pass (or crop);
-        # a norm round: both row passes, degrid, grid, fold, two reduction
-        # kernels and the scale
-        "gpu_launches": int(sum({"forward_adjoint": 9, "adjoint": 6}.get(str(k), 1 + 8 * 50)
+        # own kernels per request (FP32): the conversions from and to c128,
+        # the forward row and column passes and degrid, and expand, grid,
+        # fold and the inverse column and row passes; a norm request: the
+        # fill, then per round both FFT directions, degrid, grid, fold, two
+        # reduction kernels and the scale
+        "gpu_launches": int(sum({"forward_adjoint": 11, "adjoint": 7}.get(str(k), 1 + 10 * 50)
                                 for k in kinds)),
     }
     if "fp64" in per_prec:
