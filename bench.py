@@ -323,17 +323,19 @@ def kernel_bytes(info, s, caller_order_out=True):
     return out
 
 
-def roofline_entry(kern, alg, dur_s, peak, peak_kind, traffic, survey_bytes=None):
+def roofline_entry(kern, alg, dur_s, peak, peak_kind, traffic, formula_bytes=None):
     """achieved / frac on the kernel's own bytes, frac_dram on its profiled
-    DRAM traffic, and (when given) the survey formula's bytes beside them."""
+    DRAM traffic, and (when given) the per-visibility formula's bytes
+    M (16 + 2 s) + s NuNv (u, v, weight and visibility per visibility, the
+    grid once) beside them."""
     achieved = alg / dur_s / 1e9
     r = {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
          "frac": achieved / peak, "peak_source": peak_kind, "algorithmic_bytes": alg,
          "duration_ms": dur_s * 1e3, "traffic": traffic,
          "frac_dram": (traffic / dur_s / 1e9 / peak) if traffic else None}
-    if survey_bytes:
-        r["survey_bytes"] = survey_bytes
-        r["frac_survey_bytes"] = survey_bytes / dur_s / 1e9 / peak
+    if formula_bytes:
+        r["formula_bytes"] = formula_bytes
+        r["frac_formula_bytes"] = formula_bytes / dur_s / 1e9 / peak
     return r
 
 
@@ -471,8 +473,8 @@ def run_gb300(args):
     }
 
     # roofline of the dominant kernel (degrid or grid): the bytes its own
-    # arguments carry (kernel_bytes), the survey's per-visibility formula
-    # beside it, and the profiled DRAM traffic per launch
+    # arguments carry (kernel_bytes), the per-visibility formula beside it,
+    # and the profiled DRAM traffic per launch
     s = 8
     kb = kernel_bytes(info, s, caller_order_out=True)
     kern = max(("degrid", "grid"), key=lambda k: stages[k][0] / max(stages[k][1], 1))
@@ -484,7 +486,7 @@ def run_gb300(args):
     out["roofline"] = roofline_entry(kern, kb[kern], dur, peak, peak_kind, traffic,
                                      M * (16 + 2 * s) + s * info["ftsizeu"] * info["ftsizev"])
     out["kernel_bytes"] = kb
-    # whole-step HBM view: B_fwd + B_adj of the survey's formula (c64)
+    # whole-step HBM view: B_fwd + B_adj of the per-visibility formula (c64)
     NuNv = info["ftsizeu"] * info["ftsizev"]
     b_step = 2 * M * (16 + 2 * s) + s * (7 * NuNv + 3 * N)
     out["step_roofline"] = {"algorithmic_bytes": b_step,
@@ -667,12 +669,12 @@ def run_wproj(args):
     # stored factors (info factor_values complex values, 2 rank S per row,
     # not the S^2 taps of explicit rows), per row its code (4), factor offset
     # (8) and weight (s), the M slot-ordered visibilities, and the grid once
-    # (degrid) or the task windows (grid).  The survey's estimate with
+    # (degrid) or the task windows (grid).  The per-visibility formula with
     # explicit FP32 rows (taps * s) is kept beside it.
     rows = info["factor_values"] * s8 + M * (4 + 8 + s8) + M * s8
     wbytes = {"degrid": rows + s8 * NuNv,
               "grid": rows + s8 * info["tasks"] * info["window_cells"]}
-    survey = M * (16 + 2 * s8) + taps * s8 + s8 * NuNv
+    formula = M * (16 + 2 * s8) + taps * s8 + s8 * NuNv
     kern = max(("degrid", "grid"), key=lambda k: stages[k][0] / max(stages[k][1], 1))
     dur = stages[kern][0] / max(stages[kern][1], 1) * 1e-3
     peak, peak_kind = measured_peak()
@@ -687,7 +689,7 @@ def run_wproj(args):
         "create_s": t_create, "generate_s": t_gen, "norm": norm,
         "device_bytes": info["device_bytes"], "factor_values": info["factor_values"],
         "clocks": clocks, "kernel_bytes": wbytes,
-        "roofline": roofline_entry(kern, wbytes[kern], dur, peak, peak_kind, None, survey),
+        "roofline": roofline_entry(kern, wbytes[kern], dur, peak, peak_kind, None, formula),
         # own kernels per step: the forward row pass, w degrid, the compaction
         # into caller order, the gather into slot order, w grid, fold, the
         # inverse row pass (the 4096-row columns go through cuFFT)
