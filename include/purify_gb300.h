@@ -105,9 +105,10 @@ typedef struct {
   int32_t fused_permute; /* 1: degrid/grid touch caller-ordered visibilities directly,
                             0: via a slot-ordered buffer and gather kernels, -1: default
                             (direct for Phi, gather for Phi^H) */
-  int32_t cell_group;    /* base cells per work item along each axis: 1, 2 (complex<float>
-                            with J <= 6: 2 x 2 cells share a (J + 1)^2 register block),
-                            or 0: 2 where allowed, else 1 */
+  int32_t cell_group;    /* base cells of a work item: 0 or 1 = one cell (the default);
+                            2 = an aligned 2 x 2 cell group, a (J + 1)^2 register block;
+                            3 = an aligned pair of cells of a row, a J x (J + 1) block
+                            (2 and 3: complex<float>, J <= 6) */
   int32_t class_cap;     /* most items of one shared-memory bank class in a batch of 32
                             (1 .. 16), or 0 for the default */
   int32_t keep_store;    /* 1: Phi's caller-ordered output is stored at L2 evict-last
@@ -229,7 +230,7 @@ typedef struct {
   int64_t slots;           /* per-slot coverage entries (M plus null slots; M with w_term) */
   int64_t window_cells;    /* grid cells of one task's accumulation window */
   int64_t factor_values;   /* w_term: complex row-factor values stored (0 otherwise) */
-  int64_t cell_group;      /* base cells per work item along each axis (1 or 2) */
+  int64_t cell_group;      /* work-item shape: 1 one cell, 2 a 2 x 2 group, 3 a pair of a row */
   int64_t walk_tasks;      /* tasks of the column-walk G^H of Phi^H (0: it uses work items) */
   int64_t walk_steps;      /* column steps of the walk: sum over its columns of the fullest row */
 } purify_gb300_info;
@@ -271,10 +272,11 @@ typedef struct purify_gb300_plan purify_gb300_plan;
 int purify_gb300_plan_create(const double *u, const double *v, const double *weights, int64_t M,
                              uint32_t ftsizeu, uint32_t ftsizev, uint32_t J,
                              purify_gb300_plan **out);
-/* The same plan with work items of group x group base cells (group 1 or 2;
- * with 2 an item is an aligned 2 x 2 cell group of its tile, lp and lq are
- * its anchor and each fraction carries the visibility's cell in the group
- * as its integer part: frac = t + d, d in {0, 1}). */
+/* The same plan with work items of several base cells (group 1, 2 or 3;
+ * with 2 an item is an aligned 2 x 2 cell group of its tile, with 3 an
+ * aligned pair of cells of a row; lp and lq are its anchor and each fraction
+ * carries the visibility's cell in the group as its integer part: frac =
+ * t + d, d in {0, 1}). */
 int purify_gb300_plan_create_grouped(const double *u, const double *v, const double *weights,
                                      int64_t M, uint32_t ftsizeu, uint32_t ftsizev, uint32_t J,
                                      int32_t group, purify_gb300_plan **out);
@@ -353,7 +355,7 @@ typedef struct {
   int32_t max_per_item;    /* visibilities of one base cell given to one lane */
   int32_t degrid_threads;  /* CTA threads of the grouped degrid launch */
   int32_t grid_threads;    /* CTA threads of the grouped grid launch */
-  int32_t cell_group;      /* base cells per work item along each axis (1, or 2 for FP32, J <= 6) */
+  int32_t cell_group;      /* work-item shape: 1, or 2 (2 x 2) / 3 (row pairs) for FP32, J <= 6 */
   int32_t fft_columns;     /* column transforms of FP32 power-of-two grids: 0 = the library's
                               column pass (grid height <= 2048), 1 = cuFFT's strided plan */
 } purify_gb300_batch_tuning;

@@ -459,7 +459,9 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     f.tv_of = m.at<int32_t>(ch.o_tv_of);
     f.ntu = ch.ntu;
     f.ntv = ch.ntv;
-    f.Ju = f.Jv = J_ + cfg_group_ - 1;  // windows reach JB - 1 cells into the next tiles
+    // windows reach a block's extent - 1 cells into the next tiles
+    f.Ju = J_ + group_u(cfg_group_) - 1;
+    f.Jv = J_ + group_v(cfg_group_) - 1;
     f.Nu = ch.Nu;
     f.Nv = ch.Nv;
     f.ld = groups_[ch.group].ld;
@@ -923,9 +925,9 @@ std::unique_ptr<Batch> Batch::create(const BatchConfig &cfg) {
   if (cfg.tile < 8 || cfg.tile > 128) throw Error(kInvalidArgument, "tile must be in [8, 128]");
   if (cfg.max_per_item < 1 || cfg.max_per_item > 64)
     throw Error(kInvalidArgument, "max_per_item must be in [1, 64]");
-  if (cfg.cell_group != 1 && cfg.cell_group != 2)
-    throw Error(kInvalidArgument, "cell_group must be 1 or 2");
-  if (cfg.cell_group == 2 && (cfg.fp64 || cfg.J > kMaxGroupJ))
+  if (cfg.cell_group < 1 || cfg.cell_group > 3)
+    throw Error(kInvalidArgument, "cell_group must be 1, 2 or 3");
+  if (cfg.cell_group >= 2 && (cfg.fp64 || cfg.J > kMaxGroupJ))
     throw Error(kUnsupported, "2 x 2 work items need complex<float> and J <= 6");
   for (size_t c = 0; c < cfg.channels.size(); ++c) {
     const ChannelSpec &s = cfg.channels[c];

@@ -58,10 +58,11 @@ __device__ __forceinline__ void tap_weights(const PolyAxis<real, NC> &P, int nsu
   }
 }
 
-// Tap weights of one axis over the register block of an item of G x G base
-// cells (G = 1 or 2; block JB = J + G - 1 cells).  With G = 2 the stored
-// fraction x = t + d carries the visibility's cell d in {0, 1} inside the
-// group: its J taps start at block cell d and the other block cell is 0.
+// Tap weights of one axis over the register block of an item that spans G
+// base cells along that axis (G = 1 or 2; block J + G - 1 cells).  With
+// G = 2 the stored fraction x = t + d carries the visibility's cell d in
+// {0, 1} inside the group: its J taps start at block cell d and the other
+// block cell is 0.
 template <typename real, int J, int G, bool SUB, int NC>
 __device__ __forceinline__ void block_taps(const PolyAxis<real, NC> &P, int nsub, real x,
                                            real (&k)[J + G - 1]) {
@@ -249,14 +250,15 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
                                                      const __grid_constant__ PolyTable<real> poly) {
   using C = cplx<real>;
   constexpr int CH = StageDepth<real, J>::value;
-  constexpr int JB = J + G - 1;  // register block of an item (G x G base cells)
+  // register block of an item (group code G: group_u x group_v base cells)
+  constexpr int JBU = J + group_u(G) - 1, JBV = J + group_v(G) - 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int task_id = a0.order ? a0.order[blockIdx.x] : int(blockIdx.x);
   const Task tk = a0.tasks[task_id];
   const auto &a = ArgsOf<real, GROUP>::get(a0, tk.channel);
   // the window in shared memory: WH rows of WW cells at row stride WS,
   // cell (r, c) at win_offset(r, c, WS, G)
-  const int WW = tk.W + JB - 1, WH = tk.H + JB - 1, WS = a.win_stride;
+  const int WW = tk.W + JBU - 1, WH = tk.H + JBV - 1, WS = a.win_stride;
   C *win = reinterpret_cast<C *>(smem_raw);
   const TaskHeaders th = load_headers(a, tk, smem_raw + a0.win_bytes);
   const C *grid = static_cast<const C *>(a.grid);
@@ -300,7 +302,7 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
   issue(ilb, ik0, 0);
   next_chunk<CH>(ilb, ik0, th.hdr, nw);
   int lb = warp, k0 = 0, buf = 0, cnt = 0;
-  C F[JB][JB];
+  C F[JBV][JBU];
   while (lb < nbt) {
     if (ilb < nbt) {
       issue(ilb, ik0, buf ^ 1);
@@ -315,9 +317,9 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
       cnt = item_count(code);
       const C *blk = win + win_offset(item_lp(code), item_lq(code), WS, G);
 #pragma unroll
-      for (int jv = 0; jv < JB; ++jv)
+      for (int jv = 0; jv < JBV; ++jv)
 #pragma unroll
-        for (int ju = 0; ju < JB; ++ju) F[jv][ju] = blk[win_offset(jv, ju, WS, G)];
+        for (int ju = 0; ju < JBU; ++ju) F[jv][ju] = blk[win_offset(jv, ju, WS, G)];
     }
     cp_async_wait_group<1>();
     const int n = min(CH, bt.y - k0);
@@ -325,15 +327,15 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
       const int k = k0 + j;
       const int e = (buf * CH + j) * 32 + lane;
       const C t = st_t[e];
-      real ku[JB], kv[JB];
-      block_taps<real, J, G, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
-      block_taps<real, J, G, SUB>(poly.v, poly.nsub_v, t.y, kv);
+      real ku[JBU], kv[JBV];
+      block_taps<real, J, group_u(G), SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
+      block_taps<real, J, group_v(G), SUB>(poly.v, poly.nsub_v, t.y, kv);
       C sum{0, 0};
 #pragma unroll
-      for (int jv = 0; jv < JB; ++jv) {
+      for (int jv = 0; jv < JBV; ++jv) {
         C row{0, 0};
 #pragma unroll
-        for (int ju = 0; ju < JB; ++ju) row = fma2(splat(ku[ju]), F[jv][ju], row);
+        for (int ju = 0; ju < JBU; ++ju) row = fma2(splat(ku[ju]), F[jv][ju], row);
         sum = fma2(splat(kv[jv]), row, sum);
       }
       // the phase sign (-1)^(k_u + k_v) rides in the sign of t_u
@@ -363,7 +365,8 @@ template <typename real, int J, int G, bool SUB, bool GROUP>
 __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
                                                    const __grid_constant__ PolyTable<real> poly) {
   using C = cplx<real>;
-  constexpr int JB = J + G - 1;  // register block of an item (G x G base cells)
+  // register block of an item (group code G: group_u x group_v base cells)
+  constexpr int JBU = J + group_u(G) - 1, JBV = J + group_v(G) - 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int task_id = a0.order ? a0.order[blockIdx.x] : int(blockIdx.x);
   const Task tk = a0.tasks[task_id];
@@ -371,7 +374,7 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
   // warp windows in shared memory: WH rows at row stride WS (WN cells each,
   // cell (r, c) at win_offset(r, c, WS, G)); the task window written out is
   // WH x WW, packed
-  const int WW = tk.W + JB - 1, WH = tk.H + JB - 1, WS = a.win_stride,
+  const int WW = tk.W + JBU - 1, WH = tk.H + JBV - 1, WS = a.win_stride,
             WN = win_cells(WH, WS, G);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   C *wins = reinterpret_cast<C *>(smem_raw);
@@ -419,11 +422,11 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
       adv(plb, pk);
       if (user) mq = index_at(plb, pk);
     }
-    C acc[JB][JB];
+    C acc[JBV][JBU];
 #pragma unroll
-    for (int jv = 0; jv < JB; ++jv)
+    for (int jv = 0; jv < JBV; ++jv)
 #pragma unroll
-      for (int ju = 0; ju < JB; ++ju) acc[jv][ju] = C{0, 0};
+      for (int ju = 0; ju < JBU; ++ju) acc[jv][ju] = C{0, 0};
     while (clb < nbt) {
       const C t = t0, yv = y0;
       t0 = t1;
@@ -438,15 +441,15 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
       // sign (-1)^(k_u + k_v) rides in the sign of t_u.
       const real sg = copysign(real(1), t.x);
       const real zr = sg * yv.x, zi = sg * yv.y;
-      real ku[JB], kv[JB];
-      block_taps<real, J, G, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
-      block_taps<real, J, G, SUB>(poly.v, poly.nsub_v, t.y, kv);
+      real ku[JBU], kv[JBV];
+      block_taps<real, J, group_u(G), SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
+      block_taps<real, J, group_v(G), SUB>(poly.v, poly.nsub_v, t.y, kv);
       const C z{zr, zi};
 #pragma unroll
-      for (int jv = 0; jv < JB; ++jv) {
+      for (int jv = 0; jv < JBV; ++jv) {
         const C az = mul2(z, splat(kv[jv]));
 #pragma unroll
-        for (int ju = 0; ju < JB; ++ju) acc[jv][ju] = fma2(az, splat(ku[ju]), acc[jv][ju]);
+        for (int ju = 0; ju < JBU; ++ju) acc[jv][ju] = fma2(az, splat(ku[ju]), acc[jv][ju]);
       }
       if (ck + 1 >= th.hdr[clb].y) {
         // Flush at the end of the batch.  The items of one batch have
@@ -457,9 +460,9 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
         const int cnt = item_count(code);
         C *blk = mine + win_offset(item_lp(code), item_lq(code), WS, G);
 #pragma unroll
-        for (int jv = 0; jv < JB; ++jv)
+        for (int jv = 0; jv < JBV; ++jv)
 #pragma unroll
-          for (int ju = 0; ju < JB; ++ju) {
+          for (int ju = 0; ju < JBU; ++ju) {
             if (cnt > 0) {
               C *cell = blk + win_offset(jv, ju, WS, G);
               *cell = add2(*cell, acc[jv][ju]);
@@ -852,6 +855,21 @@ cudaError_t launch_apply(bool degrid, const ApplyArgs<real> &a, const PolyTable<
         PG_CASE(4, 2)
         PG_CASE(5, 2)
         PG_CASE(6, 2)
+      }
+    }
+    return cudaErrorInvalidValue;
+  }
+  if (a.group_cells == 3) {
+    // pairs of cells of a row: complex<float> with J <= kMaxGroupJ (a
+    // J x (J + 1) block)
+    if constexpr (sizeof(real) == 4) {
+      switch (J) {
+        PG_CASE(1, 3)
+        PG_CASE(2, 3)
+        PG_CASE(3, 3)
+        PG_CASE(4, 3)
+        PG_CASE(5, 3)
+        PG_CASE(6, 3)
       }
     }
     return cudaErrorInvalidValue;

@@ -137,7 +137,9 @@ class OperatorT final : public Operator {
   int64_t M_ = 0, N_ = 0, S_ = 0;
   bool wmode_ = false;  // row-factor kernels (w-projection rows, or plain rows)
   bool rows_mode_ = false;  // plain separable rows on the row-factor kernels
-  int fold_J_ = 0;      // halo of the task windows + 1 (J, or the largest w support)
+  // halo of the task windows + 1 along u and v (J plus the group's extra
+  // cell, or the largest w support)
+  int fold_J_ = 0, fold_Jv_ = 0;
   DeviceBuffer wcode_, wfactor_, wfactors_, wchunks_, wtask_chunk_;
   int wchunk_values_ = 0;
   int64_t nnz_ = 0, occupied_ = 0, work_items_ = 0, factor_values_ = 0;
@@ -427,7 +429,9 @@ void OperatorT<real>::init_plain(const OperatorConfig &cfg, int64_t &bytes, Axis
   win_rows_ = plan.win_rows;
   win_cols_ = plan.win_cols;
   win_stride_ = plan.win_stride;
-  fold_J_ = J_ + group_ - 1;  // task windows reach JB - 1 cells into the next tiles
+  // task windows reach a block's extent - 1 cells into the next tiles
+  fold_J_ = J_ + group_u(group_) - 1;
+  fold_Jv_ = J_ + group_v(group_) - 1;
   S_ = plan.S;
   unit_weights_ = plan.unit_weights;
   split_weights_ = !unit_weights_;
@@ -584,7 +588,7 @@ void OperatorT<real>::init_w(const OperatorConfig &cfg, int64_t &bytes, AxisTili
   ntasks_ = int(plan.tasks.size());
   win_rows_ = plan.win_rows;
   win_cols_ = plan.win_cols;
-  fold_J_ = plan.Smax;
+  fold_J_ = fold_Jv_ = plan.Smax;
   S_ = M_;
   unit_weights_ = false;
   // the reference's non-zeros (Ju Jv per plain row; the stored rows pad to S^2)
@@ -825,7 +829,7 @@ void OperatorT<real>::fold_into(void *grid, const void *windows, const int32_t *
   f.ntu = ntu_;
   f.ntv = ntv_;
   f.Ju = fold_J_;
-  f.Jv = fold_J_;
+  f.Jv = fold_Jv_;
   f.Nu = Nu_;
   f.Nv = Nv_;
   f.grid = grid;
@@ -1383,10 +1387,11 @@ std::unique_ptr<Operator> Operator::create(const OperatorConfig &cfg) {
     throw Error(kUnsupported, "kernel support must be between 1 and 32 taps");
   if (cfg.class_cap < 0 || cfg.class_cap > 16)
     throw Error(kInvalidArgument, "class_cap must be 0 (default) or in [1, 16]");
-  if (cfg.cell_group < 0 || cfg.cell_group > 2)
-    throw Error(kInvalidArgument, "cell_group must be 0 (automatic), 1 or 2");
-  if (cfg.cell_group == 2 && (cfg.fp64 || cfg.Ju > kMaxGroupJ || cfg.w_term || cfg.Ju != cfg.Jv))
-    throw Error(kUnsupported, "2 x 2 work items need complex<float>, J <= 6 and no w-projection");
+  if (cfg.cell_group < 0 || cfg.cell_group > 3)
+    throw Error(kInvalidArgument, "cell_group must be 0 (automatic), 1, 2 or 3");
+  if (cfg.cell_group >= 2 && (cfg.fp64 || cfg.Ju > kMaxGroupJ || cfg.w_term || cfg.Ju != cfg.Jv))
+    throw Error(kUnsupported,
+                "2 x 2 and row-pair work items need complex<float>, J <= 6 and no w-projection");
   if (cfg.w_term && (cfg.M > 0 && !cfg.w))
     throw Error(kInvalidArgument, "w-projection needs the w coordinates");
   if (cfg.w_term && (cfg.Jw < 1 || cfg.Jw + cfg.Ju - 1 > kMaxWSupport) && !cfg.jw_rows)

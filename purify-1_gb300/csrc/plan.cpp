@@ -54,7 +54,7 @@ Plan build_plan(const PlanRequest &rq) {
   if (rq.tile < 1 || rq.tile > 255) throw std::invalid_argument("tile edge out of range");
   if (rq.max_batches_per_task < 1 || rq.max_batches_per_task > kMaxTaskBatches)
     throw std::invalid_argument("max_batches_per_task out of range");
-  if (rq.group != 1 && rq.group != 2) throw std::invalid_argument("group must be 1 or 2");
+  if (rq.group < 1 || rq.group > 3) throw std::invalid_argument("group must be 1, 2 or 3");
   if (rq.class_cap < 0 || rq.class_cap > 16) throw std::invalid_argument("class_cap out of range");
   for (int64_t m = 0; m < rq.M; ++m)
     if (!std::isfinite(rq.u[m]) || !std::isfinite(rq.v[m]))
@@ -68,10 +68,10 @@ Plan build_plan(const PlanRequest &rq) {
   P.Ju = rq.Ju;
   P.Jv = rq.Jv;
   P.group = rq.group;
-  const int G = rq.group;
+  const int G = rq.group, GU = group_u(G), GV = group_v(G);
   const int class_cap = rq.class_cap > 0 ? rq.class_cap : kClassCap;
   // register block of an item: the support plus the extra cell of a group
-  const int JBu = rq.Ju + G - 1, JBv = rq.Jv + G - 1;
+  const int JBu = rq.Ju + GU - 1, JBv = rq.Jv + GV - 1;
   P.tu = make_tiling(rq.Nu, rq.tile);
   P.tv = make_tiling(rq.Nv, rq.tile);
   // A window reaches JB - 1 cells into the next tile; it must not reach two
@@ -90,6 +90,9 @@ Plan build_plan(const PlanRequest &rq) {
   // Row stride of the tasks' shared-memory windows: the widest window.
   int WS = 0;
   for (int b = 0; b < ntu; ++b) WS = std::max(WS, P.tu.start[b + 1] - P.tu.start[b] + JBu - 1);
+  // Row pairs anchor at even columns: an odd stride keeps their offsets on
+  // all 16 bank pairs.
+  if (G == 3) WS |= 1;
   P.win_stride = WS;
   // Cell rank: tiles in row-major order, cells row-major inside a tile.
   std::vector<int64_t> tile_cell0(ntiles + 1, 0);
@@ -111,7 +114,7 @@ Plan build_plan(const PlanRequest &rq) {
   std::vector<uint8_t> flip(M);
   // With groups, a visibility's base cell inside its group (dx, dy) is added
   // to its fractions and the item is keyed by the group's anchor cell.
-  const int gmask = ~(G - 1);
+  const int umask = ~(GU - 1), vmask = ~(GV - 1);
 #pragma omp parallel for schedule(static)
   for (int64_t m = 0; m < M; ++m) {
     const double su = rq.u[m] - rq.Ju * 0.5, sv = rq.v[m] - rq.Jv * 0.5;
@@ -127,7 +130,7 @@ Plan build_plan(const PlanRequest &rq) {
     const int t = a * ntu + b;
     const int w = P.tu.start[b + 1] - P.tu.start[b];
     const int lp = p0 - P.tv.start[a], lq = q0 - P.tu.start[b];
-    const int ap = lp & gmask, aq = lq & gmask;
+    const int ap = lp & vmask, aq = lq & umask;
     tu[m] += double(lq - aq);
     tv[m] += double(lp - ap);
     rank[m] = tile_cell0[t] + int64_t(ap) * w + aq;
@@ -290,6 +293,10 @@ Plan build_plan(const PlanRequest &rq) {
       P.win_rows = std::max(P.win_rows, h + JBv - 1);
       P.win_cols = std::max(P.win_cols, w + JBu - 1);
     }
+
+  // Windows are sized and strided by win_cols: with row pairs the stride is
+  // the odd WS, which may be one wider than the widest window.
+  P.win_cols = std::max(P.win_cols, WS);
 
   // Launch order.  Longest tasks first makes the last wave of CTAs short;
   // that pays while the grid stays in L2 (<= kLptGridBytes as complex<float>).

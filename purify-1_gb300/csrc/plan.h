@@ -28,11 +28,13 @@ struct PlanRequest {
   int Ju = 4, Jv = 4;  // taps per axis
   int tile = kTile;
   int max_per_item = 16;         // visibilities of one cell handled by one lane
-  // Cells per work item along each axis (1 or 2).  With 2, an item is an
-  // aligned 2 x 2 group of base cells of its tile (anchored at even local
-  // row and column); its visibilities share one (J + 1) x (J + 1) register
-  // block, and each carries its cell inside the group in the integer part of
-  // its fractions (t_u + dx, t_v + dy with dx, dy in {0, 1}).
+  // Cells of a work item (group code): 1 = one base cell; 2 = an aligned
+  // 2 x 2 group of base cells of its tile (anchored at even local row and
+  // column), whose visibilities share one (J + 1) x (J + 1) register block;
+  // 3 = an aligned pair of adjacent cells of a row (anchored at an even
+  // local column), a J x (J + 1) block.  A visibility carries its cell
+  // inside the group in the integer part of its fractions (t_u + dx,
+  // t_v + dy with dx, dy in {0, 1}).
   int group = 1;
   // Most items of one bank class per batch (0: the default, see plan.cpp).
   int class_cap = 0;
@@ -75,14 +77,18 @@ struct Plan {
   // lane l preferably holds an item whose window offset (win_offset) is l
   // mod 16.
   int win_stride = 0;
-  // Cells per item along each axis (PlanRequest::group); the register block
-  // of an item is JB = J + group - 1 cells wide.
+  // Group code of the items (PlanRequest::group); the register block of an
+  // item is J + group_u - 1 cells wide and J + group_v - 1 high.
   int group = 1;
   // statistics
   int64_t occupied_cells = 0;
   int64_t real_items = 0;
   int max_cell_count = 0;
 };
+
+// Cells of a group along u and v (group code of PlanRequest::group).
+PG_HD constexpr int group_u(int group) { return group == 1 ? 1 : 2; }
+PG_HD constexpr int group_v(int group) { return group == 2 ? 2 : 1; }
 
 // Offset of window cell (r, c) in a shared-memory window of row stride WS.
 // Items of 2 x 2 groups sit at even rows and columns, which would leave

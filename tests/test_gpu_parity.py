@@ -359,11 +359,12 @@ def test_recorded_applies(pg, cuda, precision):
 
 @pytest.mark.parametrize("kernel,J", [("kb", 1), ("kb", 2), ("kb", 4), ("kb", 6), ("pswf", 6),
                                       ("gauss", 3), ("box", 5)])
-@pytest.mark.parametrize("group", [1, 2])
+@pytest.mark.parametrize("group", [1, 2, 3])
 def test_work_item_shapes(pg, oracle_mod, cuda, kernel, J, group):
-    """FP32 work items of single base cells (group 1) and of aligned 2 x 2
-    cell groups sharing a (J + 1)^2 register block (group 2): both against
-    the oracle, with complex weights, a dense core and a sparse tail, wrap-
+    """FP32 work items of single base cells (group 1), of aligned 2 x 2 cell
+    groups sharing a (J + 1)^2 register block (group 2) and of aligned pairs
+    of cells of a row sharing a J x (J + 1) block (group 3): against the
+    oracle, with complex weights, a dense core and a sparse tail, wrap-
     around, and bit-identical repeats; the plan reports the shape it used."""
     torch = cuda
     rng = np.random.default_rng(10 * J + group)

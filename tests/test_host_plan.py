@@ -35,14 +35,20 @@ def _lanes(plan, b):
         yield lane, lp, lq, cnt, [base + 32 * k + lane for k in range(kmax)]
 
 
+def group_uv(group):
+    """Cells of a work item along u and v: 1 x 1, 2 x 2, or a pair of a row."""
+    return (1 if group == 1 else 2), (2 if group == 2 else 1)
+
+
 def block_taps(plan, kernel="kb"):
-    """Tap vectors of every slot over its item's register block (JB = J +
-    group - 1 cells): the J taps at the fraction's cell d inside the group
-    (frac = t + d), zeros elsewhere — what block_taps evaluates on the device."""
+    """Tap vectors of every slot over its item's register block (J + g - 1
+    cells along an axis where the item spans g cells): the J taps at the
+    fraction's cell d inside the group (frac = t + d), zeros elsewhere — what
+    block_taps evaluates on the device."""
     import purify_gb300 as pg
-    J, G = plan.J, plan.group
+    J = plan.J
     out = []
-    for axis in (0, 1):
+    for axis, G in zip((0, 1), group_uv(plan.group)):
         f = plan.frac[:, axis]
         d = np.floor(f).astype(int) if G == 2 else np.zeros(f.size, dtype=int)
         assert d.min() >= 0 and d.max() <= G - 1
@@ -57,16 +63,17 @@ def block_taps(plan, kernel="kb"):
 
 def replay_degrid(plan, taps_u, taps_v, grid):
     """Slot values as degrid_kernel writes them, then compact_kernel."""
-    JB, Nu, Nv = plan.J + plan.group - 1, plan.Nu, plan.Nv
+    gu, gv = group_uv(plan.group)
+    JBU, JBV, Nu, Nv = plan.J + gu - 1, plan.J + gv - 1, plan.Nu, plan.Nv
     slots = np.zeros(plan.S, dtype=np.complex128)
     g = grid.reshape(Nv, Nu)
     for (P, Q, H, W, b0, b1, tile, _) in plan.tasks:
         for b in range(b0, b1):
             for lane, lp, lq, cnt, sl in _lanes(plan, b):
                 assert lp < H and lq < W
-                assert lp % plan.group == 0 and lq % plan.group == 0
-                rows = (P + lp + np.arange(JB)) % Nv
-                cols = (Q + lq + np.arange(JB)) % Nu
+                assert lp % gv == 0 and lq % gu == 0
+                rows = (P + lp + np.arange(JBV)) % Nv
+                cols = (Q + lq + np.arange(JBU)) % Nu
                 F = g[np.ix_(rows, cols)]
                 for k, i in enumerate(sl):
                     assert (plan.slot_user[i] >= 0) == (k < cnt)
@@ -77,11 +84,12 @@ def replay_degrid(plan, taps_u, taps_v, grid):
 def replay_grid(plan, taps_u, taps_v, vis):
     """expand_kernel, task windows as grid_kernel writes them, then
     fold_kernel's fixed-order sum."""
-    J, Nu, Nv = plan.J + plan.group - 1, plan.Nu, plan.Nv  # J: the block width
+    gu, gv = group_uv(plan.group)
+    JU, JV, Nu, Nv = plan.J + gu - 1, plan.J + gv - 1, plan.Nu, plan.Nv  # the block's extent
     slots = np.where(plan.slot_user >= 0, vis[np.maximum(plan.slot_user, 0)], 0)
     windows = []
     for (P, Q, H, W, b0, b1, tile, _) in plan.tasks:
-        win = np.zeros((H + J - 1, W + J - 1), dtype=np.complex128)
+        win = np.zeros((H + JV - 1, W + JU - 1), dtype=np.complex128)
         for b in range(b0, b1):
             cells = set()
             for lane, lp, lq, cnt, sl in _lanes(plan, b):
@@ -91,7 +99,7 @@ def replay_grid(plan, taps_u, taps_v, vis):
                 cells.add((lp, lq))
                 for i in sl:
                     z = np.conj(plan.weight[i]) * slots[i]
-                    win[lp:lp + J, lq:lq + J] += z * np.outer(taps_v[i], taps_u[i])
+                    win[lp:lp + JV, lq:lq + JU] += z * np.outer(taps_v[i], taps_u[i])
         windows.append(win)
     ntu, ntv = plan.ntu, plan.ntv
     grid = np.zeros((Nv, Nu), dtype=np.complex128)
@@ -104,9 +112,9 @@ def replay_grid(plan, taps_u, taps_v, vis):
             a2, b2 = (a - 1) % ntv, (b - 1) % ntu
             hp, wp = tv[a2 + 1] - tv[a2], tu[b2 + 1] - tu[b2]
             s = 0j
-            for (ta, tb, r, c, on) in ((a, b, lp, lq, True), (a2, b, lp + hp, lq, lp < J - 1),
-                                       (a, b2, lp, lq + wp, lq < J - 1),
-                                       (a2, b2, lp + hp, lq + wp, lp < J - 1 and lq < J - 1)):
+            for (ta, tb, r, c, on) in ((a, b, lp, lq, True), (a2, b, lp + hp, lq, lp < JV - 1),
+                                       (a, b2, lp, lq + wp, lq < JU - 1),
+                                       (a2, b2, lp + hp, lq + wp, lp < JV - 1 and lq < JU - 1)):
                 if not on:
                     continue
                 t = ta * ntu + tb
@@ -128,6 +136,9 @@ def replay_grid(plan, taps_u, taps_v, vis):
     (20, 5, 200, 3.0, 3, 2),
     (18, 5, 64, 9.0, 4, 2),     # 36-cell grid: tiles of 18, odd halo
     (25, 2, 400, 8.0, 5, 2),    # odd grid width (50): tiles of 25, a last group of one cell
+    (16, 4, 10, 1.0, 0, 3),     # pairs of cells of a row
+    (25, 2, 400, 8.0, 5, 3),    # pairs, odd tile width: a last pair of one cell
+    (48, 6, 3000, 20.0, 2, 3),
 ])
 def test_plan_replay_matches_oracle_G(pg, oracle_mod, n, J, M, spread, seed, group):
     rng = np.random.default_rng(seed)
@@ -181,7 +192,7 @@ def test_plan_balances_dense_cells(pg):
     assert (p.slot_user >= 0).sum() == 5000
 
 
-@pytest.mark.parametrize("group", [1, 2])
+@pytest.mark.parametrize("group", [1, 2, 3])
 def test_batch_lanes_are_bank_classes(pg, group):
     """Items sit on the lane of their bank class (window offset lp * stride +
     lq = lane, mod 16) wherever that lane was free, so half-warps mostly touch
@@ -198,7 +209,7 @@ def test_batch_lanes_are_bank_classes(pg, group):
     lp, lq, cnt = lc & 0xFF, (lc >> 8) & 0xFF, lc >> 16
     # window offset of the item's anchor (one extra cell per two rows with
     # 2 x 2 groups, whose anchors sit on even rows and columns)
-    r = (lp * p.win_stride + lq + (lp >> 1) * (group - 1)) & 15
+    r = (lp * p.win_stride + lq + (lp >> 1) * (group == 2)) & 15
     lane = np.arange(32)[None, :] & 15
     valid = cnt > 0
     on_class = ((r == lane) & valid).sum() / valid.sum()
