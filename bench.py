@@ -287,7 +287,7 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------- GPU ----
-def kernel_bytes(info, s, caller_order_out=True):
+def kernel_bytes(info, s, caller_order_out=True, caller_order_in=True):
     """Bytes each gridding-chain kernel's own arguments carry per launch
     (complex values of s bytes): what the kernel must read or write at least
     once, independent of how it does it.  Weights are not among them: a
@@ -296,10 +296,12 @@ def kernel_bytes(info, s, caller_order_out=True):
     degrid: the grid once, per slot t (s) [+ caller index (4) when it writes
             caller order], lane codes and batch headers, and the M
             visibilities it writes;
-    grid:   per slot t and the slot-ordered visibility (2 s), lane codes and
-            headers, and the task windows it writes;
+    grid:   per slot t (s), lane codes and headers, the task windows it
+            writes, and either the slot-ordered visibility (s per slot) or,
+            when it gathers caller order itself, the caller index (4 per
+            slot) and the M caller-ordered visibilities;
     expand: per slot the caller index (4) and the slot written (s), and the M
-            caller-ordered visibilities read;
+            caller-ordered visibilities read (only when grid reads slots);
     fold:   the task windows read and the grid written."""
     S, M = info["slots"], info["M"]
     NuNv = info["ftsizeu"] * info["ftsizev"]
@@ -308,10 +310,11 @@ def kernel_bytes(info, s, caller_order_out=True):
     windows = s * info["tasks"] * info["window_cells"]
     out = {
         "degrid": s * NuNv + s * S + (4 * S if caller_order_out else 0) + lanes + s * M,
-        "grid": 2 * s * S + lanes + windows,
-        "expand": 4 * S + s * S + s * M,
+        "grid": (s * S + 4 * S + s * M if caller_order_in else 2 * s * S) + lanes + windows,
         "fold": windows + s * NuNv,
     }
+    if not caller_order_in:
+        out["expand"] = 4 * S + s * S + s * M
     nw = info.get("walk_tasks", 0)
     if nw:
         # the column walk of Phi^H: per slot (S = M) t and the visibility,
@@ -446,6 +449,9 @@ def run_gb300(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms_per_step = float(t.item())
     value = world * M / (ms_per_step * 1e-3) / 1e6
+    # Phi^H's grid kernel gathers the caller-ordered visibilities itself
+    # unless the tuning asks for the slot-ordered path or the column walk
+    gather_in_grid = args.fused_permute != 0 and not args.grid_walk
 
     out = {
         "metric": METRIC, "value": value, "unit": "Mvis/s", "n_gpus": world,
@@ -466,9 +472,11 @@ def run_gb300(args):
         "directions": directions,
         "adjoint_dot_test_fp32": adjoint_test,
         # own kernels per step: the forward row and column passes, degrid,
-        # expand, grid, fold, the inverse column and row passes (cuFFT's
-        # column plan instead of the column passes with --fft-columns 1)
-        "gpu_launches": (6 if args.fft_columns == 1 else 8) * args.steps,
+        # grid (gathering caller order itself; expand before it when it does
+        # not), fold, the inverse column and row passes (cuFFT's column plan
+        # instead of the column passes with --fft-columns 1)
+        "gpu_launches": ((5 if args.fft_columns == 1 else 7) + (0 if gather_in_grid else 1))
+                        * args.steps,
         "clocks": clocks,
     }
 
@@ -476,13 +484,14 @@ def run_gb300(args):
     # arguments carry (kernel_bytes), the per-visibility formula beside it,
     # and the profiled DRAM traffic per launch
     s = 8
-    kb = kernel_bytes(info, s, caller_order_out=True)
+    kb = kernel_bytes(info, s, caller_order_out=True, caller_order_in=gather_in_grid)
     kern = max(("degrid", "grid"), key=lambda k: stages[k][0] / max(stages[k][1], 1))
     dur = stages[kern][0] / max(stages[kern][1], 1) * 1e-3
     peak, peak_kind = measured_peak()
     # the profiled traffic belongs to the headline workload only
     headline = (M == 10_000_000 and n == 1024 and args.J == 6 and not tuning_of(args))
-    traffic = profiled_traffic().get(kern) if headline else None
+    traffic = profiled_traffic().get(
+        "grid_caller_order" if kern == "grid" and gather_in_grid else kern) if headline else None
     out["roofline"] = roofline_entry(kern, kb[kern], dur, peak, peak_kind, traffic,
                                      M * (16 + 2 * s) + s * info["ftsizeu"] * info["ftsizev"])
     out["kernel_bytes"] = kb
@@ -1059,11 +1068,11 @@ def run_serve(args):
                                                           if kk != "_res"}
                                                       for k, v in per_prec.items()},
         # own kernels per request (FP32): the conversions from and to c128,
-        # the forward row and column passes and degrid, and expand, grid,
-        # fold and the inverse column and row passes; a norm request: the
-        # fill, then per round both FFT directions, degrid, grid, fold, two
-        # reduction kernels and the scale
-        "gpu_launches": int(sum({"forward_adjoint": 11, "adjoint": 7}.get(str(k), 1 + 10 * 50)
+        # the forward row and column passes and degrid, and grid (gathering
+        # caller order), fold and the inverse column and row passes; a norm
+        # request: the fill, then per round both FFT directions, degrid,
+        # grid, fold, two reduction kernels and the scale
+        "gpu_launches": int(sum({"forward_adjoint": 10, "adjoint": 6}.get(str(k), 1 + 10 * 50)
                                 for k in kinds)),
     }
     if "fp64" in per_prec:

@@ -104,7 +104,8 @@ typedef struct {
   int32_t tile;          /* uv tile edge in grid cells (<= 255) */
   int32_t fused_permute; /* 1: degrid/grid touch caller-ordered visibilities directly,
                             0: via a slot-ordered buffer and gather kernels, -1: default
-                            (direct for Phi, gather for Phi^H) */
+                            (direct in both directions; Phi^H of an operator with
+                            weights or with the column walk gathers into slot order) */
   int32_t cell_group;    /* base cells of a work item: 0 or 1 = one cell (the default);
                             2 = an aligned 2 x 2 cell group, a (J + 1)^2 register block;
                             3 = an aligned pair of cells of a row, a J x (J + 1) block

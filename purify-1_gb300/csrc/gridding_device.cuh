@@ -123,29 +123,53 @@ __device__ __forceinline__ void cp_async_wait_all() {
 }
 
 // Shared-memory layout of a task: the grid window(s), then the batch
-// headers {first slot, kmax} and the 32 lane codes of each batch, then the
-// per-warp staging buffers.
-constexpr size_t kHeaderBytes = kMaxTaskBatches * (sizeof(int2) + kBatch * sizeof(int));
+// headers {first slot, kmax}, then the per-warp staging buffers.  The lane
+// codes stay in global memory (L2): a warp reads its next batch's 32 codes
+// (128 bytes, one load per lane) while it works on the current batch, so
+// they cost no shared memory, which bounds the resident CTAs of small CTA
+// shapes.
+constexpr size_t kHeaderBytes = kMaxTaskBatches * sizeof(int2);
 struct TaskHeaders {
   int2 *hdr;
-  int *code;
+  const int32_t *code;  // the task's lane codes, batch * 32 + lane (global)
 };
-// Issues the asynchronous copies of a task's batch headers and lane codes;
-// the caller waits with cp_async_wait_all() + __syncthreads().
+// Issues the asynchronous copies of a task's batch headers; the caller waits
+// with cp_async_wait_all() + __syncthreads().
 template <typename A>
 __device__ __forceinline__ TaskHeaders load_headers(const A &a, const Task &tk,
                                                     unsigned char *base) {
   TaskHeaders h;
   h.hdr = reinterpret_cast<int2 *>(base);
-  h.code = reinterpret_cast<int *>(base + sizeof(int2) * kMaxTaskBatches);
+  h.code = a.lane_code + size_t(tk.batch_begin) * kBatch;
   const int nbt = tk.batch_end - tk.batch_begin;
   for (int k = threadIdx.x; k < nbt; k += blockDim.x)
     cp_async<8>(h.hdr + k, a.batches + tk.batch_begin + k);
-  // lane codes: 32 ints (128 bytes) per batch, copied in 16-byte pieces
-  const int *src = a.lane_code + size_t(tk.batch_begin) * kBatch;
-  for (int k = threadIdx.x; k < nbt * (kBatch / 4); k += blockDim.x)
-    cp_async<16>(h.code + 4 * k, src + 4 * k);
   return h;
+}
+// Row and column of the packed index idx of a window WW cells wide, for a
+// loop that advances idx by `step`: one division at the start instead of one
+// per element.
+struct WinCursor {
+  int lp, lq, dp, dq;
+  __device__ __forceinline__ WinCursor(int idx, int WW, int step) {
+    lp = idx / WW;
+    lq = idx - lp * WW;
+    dp = step / WW;
+    dq = step - dp * WW;
+  }
+  __device__ __forceinline__ void next(int WW) {
+    lq += dq;
+    lp += dp;
+    if (lq >= WW) {
+      lq -= WW;
+      ++lp;
+    }
+  }
+};
+// Lane code of this lane in batch lb of a task (0, an empty item, past the
+// task's last batch).
+__device__ __forceinline__ int lane_code_at(const TaskHeaders &th, int lb, int nbt, int lane) {
+  return lb < nbt ? __ldg(th.code + size_t(lb) * kBatch + lane) : 0;
 }
 
 // Visibility reads of the grid kernel.  Slot order: a streaming load of
@@ -264,8 +288,9 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
   const C *grid = static_cast<const C *>(a.grid);
   const size_t ld = size_t(a.ld ? a.ld : a.Nu);
   // Stage the (wrapped) window of the grid this tile's footprints touch.
-  for (int idx = threadIdx.x; idx < WW * WH; idx += blockDim.x) {
-    const int lp = idx / WW, lq = idx - lp * WW;
+  WinCursor cur(threadIdx.x, WW, blockDim.x);
+  for (int idx = threadIdx.x; idx < WW * WH; idx += blockDim.x, cur.next(WW)) {
+    const int lp = cur.lp, lq = cur.lq;
     int p = tk.P + lp;
     if (p >= a.Nv) p -= a.Nv;
     int q = tk.Q + lq;
@@ -302,6 +327,7 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
   issue(ilb, ik0, 0);
   next_chunk<CH>(ilb, ik0, th.hdr, nw);
   int lb = warp, k0 = 0, buf = 0, cnt = 0;
+  int code_n = lane_code_at(th, lb, nbt, lane);  // lane code of batch lb
   C F[JBV][JBU];
   while (lb < nbt) {
     if (ilb < nbt) {
@@ -312,8 +338,10 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
     }
     const int2 bt = th.hdr[lb];
     if (k0 == 0) {
-      // new batch: this lane's item and its J x J grid block
-      const int code = th.code[lb * kBatch + lane];
+      // new batch: this lane's item and its J x J grid block; the code of
+      // the warp's next batch is loaded now, to be ready when it starts
+      const int code = code_n;
+      code_n = lane_code_at(th, lb + nw, nbt, lane);
       cnt = item_count(code);
       const C *blk = win + win_offset(item_lp(code), item_lq(code), WS, G);
 #pragma unroll
@@ -379,7 +407,15 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   C *wins = reinterpret_cast<C *>(smem_raw);
   const TaskHeaders th = load_headers(a, tk, smem_raw + a0.win_bytes);
-  for (int idx = threadIdx.x; idx < nw * WN; idx += blockDim.x) wins[idx] = C{0, 0};
+  {
+    // zero the warp windows, 16 bytes per store (the windows start 16-byte
+    // aligned; an odd FP32 cell count leaves one 8-byte cell at the end)
+    const size_t bytes = size_t(nw) * WN * sizeof(C);
+    uint4 *z = reinterpret_cast<uint4 *>(smem_raw);
+    for (int idx = threadIdx.x; idx < int(bytes / 16); idx += blockDim.x)
+      z[idx] = make_uint4(0u, 0u, 0u, 0u);
+    if (bytes % 16 != 0 && threadIdx.x == 0) wins[nw * WN - 1] = C{0, 0};
+  }
   cp_async_wait_all();
   __syncthreads();
   C *mine = wins + warp * WN;
@@ -395,6 +431,9 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
     // gather (mq), so a gather never waits on its index load.
     int clb = warp, ck = 0;
     int plb = warp, pk = 0;
+    // lane codes of the compute cursor's batch and of the warp's next batch
+    int code_c = lane_code_at(th, clb, nbt, lane);
+    int code_n = lane_code_at(th, clb + nw, nbt, lane);
     auto adv = [&](int &lb, int &k) {
       if (k + 1 < th.hdr[lb].y) {
         ++k;
@@ -456,7 +495,9 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
         // distinct base cells, so at each (jv, ju) step the 32 lanes update
         // 32 distinct cells; steps are ordered by __syncwarp, which makes the
         // summation order a function of the plan.
-        const int code = th.code[clb * kBatch + lane];
+        const int code = code_c;
+        code_c = code_n;
+        code_n = lane_code_at(th, clb + 2 * nw, nbt, lane);
         const int cnt = item_count(code);
         C *blk = mine + win_offset(item_lp(code), item_lq(code), WS, G);
 #pragma unroll
@@ -477,8 +518,9 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
   __syncthreads();
   const int local_task = GROUP ? task_id - a0.group_task_base[tk.channel] : task_id;
   C *out = static_cast<C *>(a.tilebuf) + size_t(local_task) * a.slot_stride;
-  for (int idx = threadIdx.x; idx < WW * WH; idx += blockDim.x) {
-    const int lp = idx / WW, e = win_offset(lp, idx - lp * WW, WS, G);
+  WinCursor cur(threadIdx.x, WW, blockDim.x);
+  for (int idx = threadIdx.x; idx < WW * WH; idx += blockDim.x, cur.next(WW)) {
+    const int e = win_offset(cur.lp, cur.lq, WS, G);
     C s = wins[e];
     for (int w = 1; w < nw; ++w) {
       const C o = wins[w * WN + e];
@@ -637,8 +679,9 @@ __global__ void __launch_bounds__(128, (sizeof(real) == 4 && J <= 6) ? 4 : 2) wa
   }
   __syncthreads();
   C *out = static_cast<C *>(a.tilebuf) + size_t(task_id) * a.slot_stride;
-  for (int idx = threadIdx.x; idx < WW * WH; idx += blockDim.x) {
-    const int lp = idx / WW, e = lp * WS + (idx - lp * WW);
+  WinCursor cur(threadIdx.x, WW, blockDim.x);
+  for (int idx = threadIdx.x; idx < WW * WH; idx += blockDim.x, cur.next(WW)) {
+    const int e = cur.lp * WS + cur.lq;
     C s = wins[e];
     for (int w = 1; w < nw; ++w) {
       const C o = wins[w * WN + e];

@@ -269,13 +269,14 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
 
   shape_.threads = cfg.threads > 0 ? cfg.threads : 128;
   // Measured on the 10^7-visibility benchmark: the forward is faster writing
-  // caller order directly (scattered stores), the adjoint faster with a
-  // separate gather into slot order.  The w-projection kernels always use
-  // the slot-ordered buffer.
+  // caller order directly (scattered stores), and the adjoint faster with the
+  // grid kernel gathering caller order itself (two steps of gathers in
+  // flight per warp) than with a separate gather into slot order.  The
+  // w-projection kernels always use the slot-ordered buffer.
   fused_forward_ = !wmode_ && cfg.fused_permute != 0;
   keep_vis_l2_ = int64_t(sizeof(C)) * M_ <= kKeepVisL2Bytes;
   keep_store_ = cfg.keep_store != 0;
-  fused_adjoint_ = !wmode_ && cfg.fused_permute == 1;
+  fused_adjoint_ = !wmode_ && cfg.fused_permute != 0;
 
   cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
   cuda_check(cudaEventCreateWithFlags(&ev_in_, cudaEventDisableTiming), "cudaEventCreate");
@@ -288,8 +289,9 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
     init_w(cfg, bytes, tu, tv, tile_tasks);
   else
     init_plain(cfg, bytes, tu, tv, tile_tasks);
-  // split weights are applied to the slot-ordered buffer before G^H
-  if (split_weights_) fused_adjoint_ = false;
+  // split weights are applied to the slot-ordered buffer before G^H, and the
+  // column walk reads its own slot order
+  if (split_weights_ || walk_) fused_adjoint_ = false;
   ntu_ = tu.n;
   ntv_ = tv.n;
   slot_stride_ = int64_t(win_rows_) * win_cols_;
@@ -1073,13 +1075,14 @@ void OperatorT<real>::grid(const void *vis, void *grid, cudaStream_t user) {
   release(user);
 }
 
-// Scratch layout in the fixed array: the task windows, then the slot buffer,
-// each starting on a 256-byte boundary.
+// Scratch layout in the fixed array: the task windows, then (when the grid
+// kernel does not gather caller order itself) the slot buffer, each starting
+// on a 256-byte boundary.
 template <typename real>
 int64_t OperatorT<real>::no_alloc_bytes() const {
   auto up = [](int64_t b) { return (b + 255) / 256 * 256; };
   return up(int64_t(sizeof(C)) * slot_stride_ * std::max(ntasks_, 1)) +
-         up(int64_t(sizeof(C)) * std::max<int64_t>(S_, 1));
+         (fused_adjoint_ ? 0 : up(int64_t(sizeof(C)) * std::max<int64_t>(S_, 1)));
 }
 
 template <typename real>
@@ -1101,10 +1104,14 @@ void OperatorT<real>::grid_no_alloc(const void *vis, void *grid, cudaStream_t us
   // expand writes every slot (0 for null slots) and the grid kernels write
   // every cell of every task window, so nothing left in the array from an
   // earlier call is read.
-  cuda_check(launch_expand<real>(vis, slot_user_.as<int32_t>(), slots, S_, stream_, false,
-                                 slot_weights()),
-             "expand");
-  grid_core(grid, slots, nullptr, windows);
+  if (fused_adjoint_) {
+    grid_core(grid, vis, slot_user_.as<int32_t>(), windows);
+  } else {
+    cuda_check(launch_expand<real>(vis, slot_user_.as<int32_t>(), slots, S_, stream_, false,
+                                   slot_weights()),
+               "expand");
+    grid_core(grid, slots, nullptr, windows);
+  }
   release(user);
 }
 
