@@ -60,7 +60,7 @@ def parse():
                    help="timed Phi / Phi^H pairs of the full-size CPU baseline")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
-    p.add_argument("--e2e-steps", type=int, default=5, help="0 skips the end-to-end leg")
+    p.add_argument("--e2e-steps", type=int, default=20, help="0 skips the end-to-end leg")
     p.add_argument("--power-iters", type=int, default=20,
                    help="power-method rounds for the norm before timing (0: norm 1)")
     p.add_argument("--threads", type=int, default=0, help="CTA threads (tuning)")
@@ -591,14 +591,19 @@ def run_gb300(args):
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
+    e2e_ms = []
     for _ in range(args.e2e_steps):
+        t1 = time.perf_counter()
         e2e_step()
+        e2e_ms.append((time.perf_counter() - t1) * 1e3)
     t_e2e = (time.perf_counter() - t0) / args.e2e_steps
     if dist:
         t = torch.tensor([t_e2e], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         t_e2e = float(t.item())
     out["e2e"] = {"value": world * M / t_e2e / 1e6, "unit": "Mvis/s", "ms_per_step": t_e2e * 1e3,
+                  "steps": args.e2e_steps, "p50_ms": float(np.percentile(e2e_ms, 50)),
+                  "max_ms": float(max(e2e_ms)),
                   "h2d_bytes_per_step": 16 * (N + M), "d2h_bytes_per_step": 16 * (M + N),
                   "api": "purify_gb300_forward_host + purify_gb300_adjoint_host "
                          "(complex<double> host vectors)"}
@@ -1068,11 +1073,11 @@ def run_serve(args):
                                                           if kk != "_res"}
                                                       for k, v in per_prec.items()},
         # own kernels per request (FP32): the conversions from and to c128,
-        # the forward row and column passes and degrid, and grid (gathering
-        # caller order), fold and the inverse column and row passes; a norm
-        # request: the fill, then per round both FFT directions, degrid,
-        # grid, fold, two reduction kernels and the scale
-        "gpu_launches": int(sum({"forward_adjoint": 10, "adjoint": 6}.get(str(k), 1 + 10 * 50)
+        # the forward row and column passes and degrid, and expand, grid,
+        # fold and the inverse column and row passes; a norm request: the
+        # fill, then per round both FFT directions, degrid, grid, fold, two
+        # reduction kernels and the scale
+        "gpu_launches": int(sum({"forward_adjoint": 11, "adjoint": 7}.get(str(k), 1 + 10 * 50)
                                 for k in kinds)),
     }
     if "fp64" in per_prec:
