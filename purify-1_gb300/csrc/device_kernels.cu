@@ -85,6 +85,8 @@ __global__ void expand_kernel(const cplx<real> *__restrict__ in,
 
 template <typename real>
 __global__ void fold_kernel(const FoldArgs f) {
+  dev::pdl_launch_next();
+  dev::pdl_wait();  // the task windows are the previous kernel's output
   fold_tile<real>(f, blockIdx.x);
 }
 
@@ -302,8 +304,7 @@ cudaError_t launch_walk_grid(const WalkArgs<real> &a, const PolyTable<real> &pol
 
 template <typename real>
 cudaError_t launch_fold(const FoldArgs &f, cudaStream_t s) {
-  fold_kernel<real><<<f.ntu * f.ntv, dim3(32, 8), 0, s>>>(f);
-  return cudaGetLastError();
+  return launch_chain(fold_kernel<real>, dim3(f.ntu * f.ntv), dim3(32, 8), 0, s, f);
 }
 
 template <typename real>

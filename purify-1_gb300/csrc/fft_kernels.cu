@@ -18,6 +18,7 @@
 
 #include "device_kernels.h"
 #include "fft_kernels.h"
+#include "pdl.cuh"
 
 namespace pg {
 namespace {
@@ -294,8 +295,10 @@ __global__ void __launch_bounds__(kFftThreads, 4) fft_row_kernel(const FftArgs a
                                                               const float2 *__restrict__ in,
                                                               float2 *__restrict__ out) {
   extern __shared__ float2 fft_sm[];
+  dev::pdl_launch_next();
   TwiddleCache tc;
   load_twiddles<N, V, 1, 0, INV>(tc, static_cast<const float2 *>(a.tw_u));
+  dev::pdl_wait();  // `in` is the previous kernel's output
   run_stages<N, V, 1, 0, INV>(a, in, out, fft_sm, tc, int(blockIdx.x) * V);
 }
 
@@ -353,6 +356,7 @@ struct ColPad {
 template <int N, int V, bool INV, int T, int MINB>
 __global__ void __launch_bounds__(T, MINB) fft_col_direct_kernel(const FftColArgs c) {
   extern __shared__ float2 fft_sm[];
+  dev::pdl_launch_next();
   constexpr int PAD = ColPad<N, V>::value;
   const int col0 = int(blockIdx.x) * V;
   FftArgs a;
@@ -367,6 +371,7 @@ __global__ void __launch_bounds__(T, MINB) fft_col_direct_kernel(const FftColArg
   }
   TwiddleCache tc;
   load_twiddles<N, V, 1, 0, INV, T, true>(tc, static_cast<const float2 *>(c.tw_v));
+  dev::pdl_wait();  // c.in is the previous kernel's output
   run_stages<N, V, 1, 0, INV, PAD, T, true>(a, static_cast<const float2 *>(c.in),
                                                    static_cast<float2 *>(c.out), fft_sm, tc,
                                                    col0);
@@ -383,8 +388,7 @@ cudaError_t launch_cols(const FftColArgs &c, cudaStream_t s) {
         cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
   }
-  fn<<<c.W / V, T, smem, s>>>(c);
-  return cudaGetLastError();
+  return launch_chain(fn, dim3(c.W / V), dim3(T), smem, s, c);
 }
 
 template <bool INV>
@@ -414,9 +418,8 @@ cudaError_t launch_rows(const FftArgs &a, const void *in, void *out, cudaStream_
         cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
   }
-  fn<<<(a.Ny + V - 1) / V, kFftThreads, smem, s>>>(a, static_cast<const float2 *>(in),
-                                                   static_cast<float2 *>(out));
-  return cudaGetLastError();
+  return launch_chain(fn, dim3((a.Ny + V - 1) / V), dim3(kFftThreads), smem, s, a,
+                      static_cast<const float2 *>(in), static_cast<float2 *>(out));
 }
 
 template <bool INV>

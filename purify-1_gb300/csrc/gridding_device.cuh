@@ -11,6 +11,7 @@
 #include <cstdint>
 
 #include "cplx_ops.cuh"
+#include "pdl.cuh"
 #include "device_kernels.h"
 #include "plan.h"
 
@@ -277,6 +278,7 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
   // register block of an item (group code G: group_u x group_v base cells)
   constexpr int JBU = J + group_u(G) - 1, JBV = J + group_v(G) - 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  pdl_launch_next();
   const int task_id = a0.order ? a0.order[blockIdx.x] : int(blockIdx.x);
   const Task tk = a0.tasks[task_id];
   const auto &a = ArgsOf<real, GROUP>::get(a0, tk.channel);
@@ -287,6 +289,8 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
   const TaskHeaders th = load_headers(a, tk, smem_raw + a0.win_bytes);
   const C *grid = static_cast<const C *>(a.grid);
   const size_t ld = size_t(a.ld ? a.ld : a.Nu);
+  // the grid is the previous kernel's output
+  pdl_wait();
   // Stage the (wrapped) window of the grid this tile's footprints touch.
   WinCursor cur(threadIdx.x, WW, blockDim.x);
   for (int idx = threadIdx.x; idx < WW * WH; idx += blockDim.x, cur.next(WW)) {
@@ -396,6 +400,7 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
   // register block of an item (group code G: group_u x group_v base cells)
   constexpr int JBU = J + group_u(G) - 1, JBV = J + group_v(G) - 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  pdl_launch_next();
   const int task_id = a0.order ? a0.order[blockIdx.x] : int(blockIdx.x);
   const Task tk = a0.tasks[task_id];
   const auto &a = ArgsOf<real, GROUP>::get(a0, tk.channel);
@@ -418,6 +423,8 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
   }
   cp_async_wait_all();
   __syncthreads();
+  // the visibilities are the previous kernel's output
+  pdl_wait();
   C *mine = wins + warp * WN;
   const int nbt = tk.batch_end - tk.batch_begin;
   const C *frac = static_cast<const C *>(a.frac);
@@ -874,8 +881,7 @@ cudaError_t launch_one(bool degrid, const ApplyArgs<real> &a, const PolyTable<re
         cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
   }
-  fn<<<ntasks, threads, smem, s>>>(a, poly);
-  return cudaGetLastError();
+  return launch_chain(fn, dim3(ntasks), dim3(threads), smem, s, a, poly);
 }
 
 template <typename real, bool GROUP>
