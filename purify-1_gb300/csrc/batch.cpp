@@ -213,6 +213,7 @@ BatchT<real>::BatchT(const BatchConfig &cfg) {
     rq.tile = cfg.tile;
     rq.max_per_item = cfg.max_per_item;
     rq.group = cfg.cell_group;
+    rq.warps = (cfg.grid_threads > 0 ? cfg.grid_threads : cfg.threads) / 32;
     Plan plan;
     try {
       plan = build_plan(rq);

@@ -40,6 +40,67 @@ struct Item {
   int32_t cell;   // cell index inside the tile
   int32_t lp, lq;
 };
+
+// Batch order inside each task for the kernels' round-robin dealing (batch
+// i of a task goes to warp i mod nw).  A batch costs about kStepCost per
+// k-step plus kFlushCost for its block flush (warp instructions of the grid
+// kernel at J = 6).  The batches are taken heaviest first in rounds of nw;
+// in each round the heaviest goes to the warp with the least work so far.
+// The last, partial round goes to the lightest warps, and the warps are then
+// numbered by load so that round-robin dealing gives every warp its list.
+// On the 10^7-visibility workload this takes the mean over tasks of (mean
+// warp load / largest warp load) from 0.86 (plain longest-first order) to
+// 0.96.  Only the order of the batch records changes; slots stay put.
+constexpr int64_t kStepCost = 220, kFlushCost = 180;
+
+void balance_task_batches(Plan &P, int nw) {
+  if (nw <= 1) return;
+  std::vector<int32_t> order, wl(nw), pos;
+  std::vector<int64_t> load(nw);
+  std::vector<std::vector<int32_t>> lists(nw);
+  std::vector<int32_t> base, kmax, code;
+  for (const Task &tk : P.tasks) {
+    const int b0 = tk.batch_begin, n = tk.batch_end - tk.batch_begin;
+    if (n <= 1) continue;
+    auto cost = [&](int i) { return kStepCost * P.batch_kmax[b0 + i] + kFlushCost; };
+    order.resize(n);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost(x) > cost(y); });
+    std::fill(load.begin(), load.end(), 0);
+    for (auto &l : lists) l.clear();
+    const int full = n / nw, rem = n - full * nw;
+    auto by_load = [&] {
+      std::iota(wl.begin(), wl.end(), 0);
+      std::stable_sort(wl.begin(), wl.end(), [&](int x, int y) { return load[x] < load[y]; });
+    };
+    for (int r = 0; r < full; ++r) {
+      by_load();
+      for (int j = 0; j < nw; ++j) {
+        const int b = order[size_t(r) * nw + j];
+        lists[wl[j]].push_back(b);
+        load[wl[j]] += cost(b);
+      }
+    }
+    by_load();
+    for (int j = 0; j < rem; ++j) lists[wl[j]].push_back(order[size_t(full) * nw + j]);
+    // warp label j runs lists[wl[j]]: its r-th batch goes to position r nw + j
+    pos.assign(n, -1);
+    for (int j = 0; j < nw; ++j)
+      for (size_t r = 0; r < lists[wl[j]].size(); ++r) pos[r * nw + j] = lists[wl[j]][r];
+    base.assign(P.batch_base.begin() + b0, P.batch_base.begin() + b0 + n);
+    kmax.assign(P.batch_kmax.begin() + b0, P.batch_kmax.begin() + b0 + n);
+    code.assign(P.lane_code.begin() + size_t(b0) * kBatch,
+                P.lane_code.begin() + size_t(b0 + n) * kBatch);
+    for (int i = 0; i < n; ++i) {
+      const int src = pos[i];
+      if (src < 0) throw std::logic_error("balance_task_batches: unfilled position");
+      P.batch_base[b0 + i] = base[src];
+      P.batch_kmax[b0 + i] = kmax[src];
+      std::copy(code.begin() + size_t(src) * kBatch, code.begin() + size_t(src + 1) * kBatch,
+                P.lane_code.begin() + size_t(b0 + i) * kBatch);
+    }
+  }
+}
 }  // namespace
 
 Plan build_plan(const PlanRequest &rq) {
@@ -297,6 +358,7 @@ Plan build_plan(const PlanRequest &rq) {
   // Windows are sized and strided by win_cols: with row pairs the stride is
   // the odd WS, which may be one wider than the widest window.
   P.win_cols = std::max(P.win_cols, WS);
+  balance_task_batches(P, rq.warps);
 
   // Launch order.  Longest tasks first makes the last wave of CTAs short;
   // that pays while the grid stays in L2 (<= kLptGridBytes as complex<float>).

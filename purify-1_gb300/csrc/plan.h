@@ -40,6 +40,10 @@ struct PlanRequest {
   int class_cap = 0;
   int max_batches_per_task = kMaxTaskBatches;
   int64_t max_slots_per_task = 16384;
+  // Warps of the CTAs that will run the plan: the kernels deal a task's
+  // batches round-robin (batch i to warp i mod warps), and the planner
+  // orders each task's batches so that this dealing balances the warps.
+  int warps = 4;
 };
 
 // Tiling of one grid axis: tile b covers [start[b], start[b + 1]).
