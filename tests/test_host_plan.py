@@ -239,3 +239,38 @@ def test_plan_rejects_non_finite_coordinates(pg, bad):
     assert e.value.status == 1
     with pytest.raises(pg.PurifyError):
         pg.CoveragePlan(v, u, 64, 64, 4)
+
+
+def _warp_efficiency(plan, nw, order=None):
+    """Mean over tasks of (mean warp load / largest warp load) when batch i of
+    a task goes to warp i mod nw; a batch costs 220 per k-step plus 180 (the
+    planner's model).  `order` re-sorts each task's batches first."""
+    kmax = plan.batches[:, 1].astype(np.int64)
+    eff = []
+    for t in plan.tasks:
+        cost = 220.0 * kmax[t[4]:t[5]] + 180.0
+        if order is not None:
+            cost = order(cost)
+        loads = np.zeros(nw)
+        for i, c in enumerate(cost):
+            loads[i % nw] += c
+        eff.append(cost.sum() / nw / loads.max())
+    return float(np.mean(eff))
+
+
+def test_task_batches_balanced_over_warps(pg):
+    """The planner orders each task's batches (default: 4 warps) so that
+    round-robin dealing balances the warps better than the heaviest-first
+    order, and the reordering keeps every batch and every slot."""
+    rng = np.random.default_rng(21)
+    M, N = 300_000, 512
+    u = np.concatenate([rng.normal(0, 0.08 * N, M // 2), rng.uniform(-N / 2, N / 2, M - M // 2)])
+    v = np.concatenate([rng.normal(0, 0.08 * N, M // 2), rng.uniform(-N / 2, N / 2, M - M // 2)])
+    plan = pg.CoveragePlan(u, v, N, N, 6)
+    balanced = _warp_efficiency(plan, 4)
+    heaviest_first = _warp_efficiency(plan, 4, order=lambda c: np.sort(c)[::-1])
+    assert balanced >= 0.9 and balanced > heaviest_first + 0.05, (balanced, heaviest_first)
+    # every slot of every batch is a distinct slot of the plan
+    slots = np.concatenate([b + 32 * np.arange(k)[:, None] + np.arange(32)[None, :]
+                            for b, k in plan.batches], axis=None)
+    assert slots.size == plan.S and np.unique(slots).size == plan.S
