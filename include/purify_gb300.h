@@ -99,7 +99,8 @@ int purify_gb300_operator_destroy(purify_gb300_operator *op);
  * default.  No counterpart in the reference (its operator has no launch
  * shapes); the autotuner searches these. */
 typedef struct {
-  int32_t threads;       /* CTA threads of the degrid/grid kernels, multiple of 32, <= 256 */
+  int32_t threads;       /* CTA threads of the degrid/grid kernels, multiple of 32, <= 256
+                            (0: 64) */
   int32_t max_per_item;  /* visibilities of one base cell given to one lane (<= 65535) */
   int32_t tile;          /* uv tile edge in grid cells (<= 255) */
   int32_t fused_permute; /* 1: degrid/grid touch caller-ordered visibilities directly,
