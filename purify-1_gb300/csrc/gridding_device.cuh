@@ -230,7 +230,8 @@ struct ArgsOf<real, true> {
 };
 
 // Per-warp staging of the degrid kernel's coverage stream.  A warp walks its
-// batches in chunks of up to CH k-steps; while it computes one chunk, the
+// (batch, k) steps in chunks of CH steps, across batch boundaries; while it
+// computes one chunk, the
 // next chunk's per-slot data (t, and the caller index when the launch
 // writes caller order) is on its way into shared memory by cp.async, so a
 // whole chunk of loads is in flight per warp instead of one step.  Each lane
@@ -259,15 +260,6 @@ __device__ __forceinline__ void cp_async_commit() {
 template <int N>
 __device__ __forceinline__ void cp_async_wait_group() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
-template <int CH>
-__device__ __forceinline__ void next_chunk(int &lb, int &k0, const int2 *hdr, int nw) {
-  k0 += CH;
-  if (k0 >= hdr[lb].y) {
-    k0 = 0;
-    lb += nw;
-  }
 }
 
 template <typename real, int J, int G, bool SUB, bool GROUP>
@@ -316,47 +308,49 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
   int *st_m = reinterpret_cast<int *>(stg + 2 * CH * 32 * sizeof(C));
   const unsigned long long pol = l2_stream_policy();
   const unsigned long long kpol = l2_keep_policy();
-  auto issue = [&](int lb, int k0, int buf) {
-    const int2 bt = th.hdr[lb];
-    const int n = min(CH, bt.y - k0);
-    for (int j = 0; j < n; ++j) {
-      const size_t i = size_t(bt.x) + size_t(k0 + j) * kBatch + lane;
+  // A chunk is the next CH (batch, k) steps of this warp, across batch
+  // boundaries, so that a warp whose batches are short (one or two steps)
+  // still has CH steps of coverage loads in flight.  The producer cursor
+  // (plb, pk) issues chunk c + 1 while the compute cursor works on chunk c;
+  // both take min(CH, steps left) steps per chunk, so they stay in step.
+  auto issue = [&](int &lb, int &k, int buf) {
+    for (int j = 0; j < CH && lb < nbt; ++j) {
+      const size_t i = size_t(th.hdr[lb].x) + size_t(k) * kBatch + lane;
       const int e = (buf * CH + j) * 32 + lane;
       cp_async_stream<sizeof(C)>(st_t + e, frac + i, pol);
       if (user) cp_async_stream<4>(st_m + e, user + i, pol);
+      if (++k >= th.hdr[lb].y) {
+        k = 0;
+        lb += nw;
+      }
     }
     cp_async_commit();
   };
-  int ilb = warp, ik0 = 0;  // next chunk to issue
-  issue(ilb, ik0, 0);
-  next_chunk<CH>(ilb, ik0, th.hdr, nw);
-  int lb = warp, k0 = 0, buf = 0, cnt = 0;
+  int plb = warp, pk = 0;  // producer cursor: the next step to issue
+  issue(plb, pk, 0);
+  int lb = warp, k = 0, buf = 0, cnt = 0;
   int code_n = lane_code_at(th, lb, nbt, lane);  // lane code of batch lb
   C F[JBV][JBU];
   while (lb < nbt) {
-    if (ilb < nbt) {
-      issue(ilb, ik0, buf ^ 1);
-      next_chunk<CH>(ilb, ik0, th.hdr, nw);
-    } else {
+    if (plb < nbt)
+      issue(plb, pk, buf ^ 1);
+    else
       cp_async_commit();  // empty group: keeps "all but the newest group" meaning this chunk
-    }
-    const int2 bt = th.hdr[lb];
-    if (k0 == 0) {
-      // new batch: this lane's item and its J x J grid block; the code of
-      // the warp's next batch is loaded now, to be ready when it starts
-      const int code = code_n;
-      code_n = lane_code_at(th, lb + nw, nbt, lane);
-      cnt = item_count(code);
-      const C *blk = win + win_offset(item_lp(code), item_lq(code), WS, G);
-#pragma unroll
-      for (int jv = 0; jv < JBV; ++jv)
-#pragma unroll
-        for (int ju = 0; ju < JBU; ++ju) F[jv][ju] = blk[win_offset(jv, ju, WS, G)];
-    }
     cp_async_wait_group<1>();
-    const int n = min(CH, bt.y - k0);
-    for (int j = 0; j < n; ++j) {
-      const int k = k0 + j;
+    for (int j = 0; j < CH && lb < nbt; ++j) {
+      const int2 bt = th.hdr[lb];
+      if (k == 0) {
+        // new batch: this lane's item and its J x J grid block; the code of
+        // the warp's next batch is loaded now, to be ready when it starts
+        const int code = code_n;
+        code_n = lane_code_at(th, lb + nw, nbt, lane);
+        cnt = item_count(code);
+        const C *blk = win + win_offset(item_lp(code), item_lq(code), WS, G);
+#pragma unroll
+        for (int jv = 0; jv < JBV; ++jv)
+#pragma unroll
+          for (int ju = 0; ju < JBU; ++ju) F[jv][ju] = blk[win_offset(jv, ju, WS, G)];
+      }
       const int e = (buf * CH + j) * 32 + lane;
       const C t = st_t[e];
       real ku[JBU], kv[JBV];
@@ -386,9 +380,12 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
             out[m] = y;
         }
       }
+      if (++k >= bt.y) {
+        k = 0;
+        lb += nw;
+      }
     }
     buf ^= 1;
-    next_chunk<CH>(lb, k0, th.hdr, nw);
   }
   cp_async_wait_all();
 }
