@@ -74,6 +74,8 @@ def parse():
                    help="1: G^H of Phi^H by the column walk instead of work items (tuning)")
     p.add_argument("--fft-columns", type=int, default=0,
                    help="1: cuFFT's column plan instead of the column pass (tuning)")
+    p.add_argument("--normal-pass", type=int, default=0,
+                   help="1: the normal operator's G^H G in one pass over each task (tuning)")
     p.add_argument("--keep-store", type=int, default=0,
                    help="1: Phi stores its caller-ordered output at L2 evict-last priority (tuning)")
     p.add_argument("--fused-permute", type=int, default=-1,
@@ -87,7 +89,8 @@ def tuning_of(args):
     t = {k: v for k, v in (("threads", args.threads), ("max_per_item", args.max_per_item),
                            ("tile", args.tile), ("cell_group", args.cell_group),
                            ("class_cap", args.class_cap), ("keep_store", args.keep_store),
-                           ("fft_columns", args.fft_columns), ("grid_walk", args.grid_walk))
+                           ("fft_columns", args.fft_columns), ("grid_walk", args.grid_walk),
+                           ("normal_pass", args.normal_pass))
          if v}
     if args.fused_permute >= 0:
         t["fused_permute"] = args.fused_permute
@@ -451,7 +454,8 @@ def run_gb300(args):
     value = world * M / (ms_per_step * 1e-3) / 1e6
     # Phi^H's grid kernel gathers the caller-ordered visibilities itself
     # unless the tuning asks for the slot-ordered path or the column walk
-    gather_in_grid = args.fused_permute != 0 and not args.grid_walk
+    gather_in_grid = (args.fused_permute == 1 or (args.fused_permute < 0 and args.J >= 6)) \
+        and not args.grid_walk
 
     out = {
         "metric": METRIC, "value": value, "unit": "Mvis/s", "n_gpus": world,
@@ -471,12 +475,13 @@ def run_gb300(args):
         "stages_ms_per_launch": {k: (ms / nl if nl else None) for k, (ms, nl) in stages.items()},
         "directions": directions,
         "adjoint_dot_test_fp32": adjoint_test,
-        # own kernels per step: the forward row and column passes, degrid,
+        # own kernels per step: the forward row and column passes, degrid
+        # (compact after it on the slot-ordered forward, --fused-permute 0),
         # grid (gathering caller order itself; expand before it when it does
         # not), fold, the inverse column and row passes (cuFFT's column plan
         # instead of the column passes with --fft-columns 1)
-        "gpu_launches": ((5 if args.fft_columns == 1 else 7) + (0 if gather_in_grid else 1))
-                        * args.steps,
+        "gpu_launches": ((5 if args.fft_columns == 1 else 7) + (0 if gather_in_grid else 1) +
+                         (1 if args.fused_permute == 0 else 0)) * args.steps,
         "clocks": clocks,
     }
 

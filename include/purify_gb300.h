@@ -100,13 +100,14 @@ int purify_gb300_operator_destroy(purify_gb300_operator *op);
  * shapes); the autotuner searches these. */
 typedef struct {
   int32_t threads;       /* CTA threads of the degrid/grid kernels, multiple of 32, <= 256
-                            (0: 64) */
+                            (0: 64 for supports J >= 6, else 128) */
   int32_t max_per_item;  /* visibilities of one base cell given to one lane (<= 65535) */
   int32_t tile;          /* uv tile edge in grid cells (<= 255) */
   int32_t fused_permute; /* 1: degrid/grid touch caller-ordered visibilities directly,
                             0: via a slot-ordered buffer and gather kernels, -1: default
-                            (direct in both directions; Phi^H of an operator with
-                            weights or with the column walk gathers into slot order) */
+                            (Phi direct; Phi^H direct for supports J >= 6, else through
+                            the slot-ordered buffer, and always so with weights or with
+                            the column walk) */
   int32_t cell_group;    /* base cells of a work item: 0 or 1 = one cell (the default);
                             2 = an aligned 2 x 2 cell group, a (J + 1)^2 register block;
                             3 = an aligned pair of cells of a row, a J x (J + 1) block
@@ -120,6 +121,10 @@ typedef struct {
                             strided column plan */
   int32_t grid_walk;     /* G^H of Phi^H: 1 = the column walk where it applies (tiles <= 32,
                             single-cell items, J <= 8, J <= 6 in FP64), 0 = work items */
+  int32_t normal_pass;   /* G^H G of purify_gb300_normal and the power method: 0 = degrid
+                            then grid through the slot-ordered buffer, 1 = one pass over
+                            each task where it applies (FP32, unit weights, single-cell
+                            items, J <= 6); the results are bit-identical */
 } purify_gb300_tuning;
 int purify_gb300_operator_create_tuned(const purify_gb300_create_args *args,
                                        const purify_gb300_tuning *tuning,

@@ -42,6 +42,9 @@ namespace {
 // each), and the fullest base cell it takes (one lane walks a cell's
 // visibilities alone; a coverage with fuller cells keeps the work items,
 // which split a cell over several lanes).
+// Supports from which the default launch shape and adjoint path change
+// (see the constructor).
+constexpr int kWideSupport = 6;
 constexpr int kWalkThreads = 128;
 constexpr int kWalkMaxCellCount = 256;
 }  // namespace
@@ -124,6 +127,9 @@ class OperatorT final : public Operator {
   // Phi'^H Phi' x with the visibilities kept in slot order between G and G^H
   // (power method, normal operator); the weights' conjugates are applied there.
   void normal_slots(const void *x, void *out);
+  // F Z S x into ws->work; S^H Z^H F^H of ws->work into x
+  void forward_grid(const void *x);
+  void inverse_grid(void *x);
   // Slot-ordered weights for the gather before G^H, or null for unit weights.
   const void *slot_weights() const { return split_weights_ ? weight_.get() : nullptr; }
   void join(cudaStream_t user);
@@ -184,6 +190,10 @@ class OperatorT final : public Operator {
   // own_cols_: the column transforms run as the library's column pass
   // (launch_fft_cols); otherwise through the workspace's cuFFT column plan
   bool own_cols_ = false;
+  // Phi^H Phi's G^H G by normal_kernel in one pass (tuning normal_pass = 1;
+  // unit weights, FP32, single-cell items, J <= 6) instead of degrid then
+  // grid through the slot buffer.
+  bool one_pass_normal_ = false;
   // Column-walk plan of G^H (used by Phi^H from caller order when walk_)
   bool walk_ = false;
   int walk_ntasks_ = 0, walk_win_rows_ = 0, walk_win_stride_ = 0, walk_max_steps_ = 0;
@@ -267,19 +277,22 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
   for (int j = 0; j < Ny_; ++j)
     sv_[j] = 1.0 / kern_y.correction((y0_ + j + 0.5) / Nv_ - 0.5);
 
-  // Two warps per CTA by default: with each task's batches balanced over
-  // the warps (balance_task_batches), 64-thread CTAs measured 2% faster on
-  // the 10^7-visibility step than 128 (0.415 against 0.423 ms).
-  shape_.threads = cfg.threads > 0 ? cfg.threads : 64;
-  // Measured on the 10^7-visibility benchmark: the forward is faster writing
-  // caller order directly (scattered stores), and the adjoint faster with the
-  // grid kernel gathering caller order itself (two steps of gathers in
-  // flight per warp) than with a separate gather into slot order.  The
-  // w-projection kernels always use the slot-ordered buffer.
+  // Defaults measured on the 10^7-visibility workload (1024^2 image, KB,
+  // FP32).  Wide supports (J >= 6): 64-thread CTAs, and the adjoint's grid
+  // kernel gathers caller order itself; its per-visibility work hides the
+  // gathers' latency (J = 6: step 0.414 ms; 128 threads 0.423; a separate
+  // gather 0.47).  Narrow supports: 128-thread CTAs, and the adjoint gathers
+  // into slot order first, because the shorter steps leave the gathers
+  // exposed (J = 4: adjoint 0.221 ms that way against 0.297 ms gathering in
+  // the grid kernel).  The forward always writes caller order directly
+  // (scattered stores) unless the tuning asks for the slot-ordered path.
+  // The w-projection kernels always use the slot-ordered buffer.
+  const bool wide = J_ >= kWideSupport;
+  shape_.threads = cfg.threads > 0 ? cfg.threads : (wide ? 64 : 128);
   fused_forward_ = !wmode_ && cfg.fused_permute != 0;
   keep_vis_l2_ = int64_t(sizeof(C)) * M_ <= kKeepVisL2Bytes;
   keep_store_ = cfg.keep_store != 0;
-  fused_adjoint_ = !wmode_ && cfg.fused_permute != 0;
+  fused_adjoint_ = !wmode_ && (cfg.fused_permute == 1 || (cfg.fused_permute < 0 && wide));
 
   cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
   cuda_check(cudaEventCreateWithFlags(&ev_in_, cudaEventDisableTiming), "cudaEventCreate");
@@ -311,6 +324,8 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
       throw Error(kUnsupported, "tile / threads / support need " + std::to_string(need) +
                                     " bytes of shared memory per CTA; the device allows " +
                                     std::to_string(optin));
+    const size_t nsm = normal_smem_bytes(sizeof(real), J_, win_rows_, win_cols_, shape_, group_);
+    one_pass_normal_ = cfg.normal_pass == 1 && !split_weights_ && nsm > 0 && nsm <= size_t(optin);
   }
   {
     tile_tasks_.alloc(sizeof(int32_t) * tile_tasks.size(), &bytes);
@@ -901,7 +916,7 @@ FftColArgs OperatorT<real>::col_args(const void *in, void *out) const {
 }
 
 template <typename real>
-void OperatorT<real>::forward_slots(const void *x, void *caller_vis) {
+void OperatorT<real>::forward_grid(const void *x) {
   if (use_fused_fft()) {
     // row transforms of the image rows into ws->pad (its other rows stay
     // zero), then the column transform into ws->work
@@ -913,7 +928,6 @@ void OperatorT<real>::forward_slots(const void *x, void *caller_vis) {
       cufft_check(Traits<real>::exec(ws_->fft_cols, ws_->pad, ws_->work, CUFFT_FORWARD),
                   "cufftExec");
     mark_end(kFftF);
-    degrid_slots(ws_->work, caller_vis);
     return;
   }
   mark_begin(kPad);
@@ -924,15 +938,10 @@ void OperatorT<real>::forward_slots(const void *x, void *caller_vis) {
   mark_begin(kFftF);
   cufft_check(Traits<real>::exec(ws_->fft, ws_->pad, ws_->work, CUFFT_FORWARD), "cufftExec");
   mark_end(kFftF);
-  degrid_slots(ws_->work, caller_vis);
 }
 
 template <typename real>
-void OperatorT<real>::adjoint_slots(void *x, const void *caller_vis, bool walk) {
-  if (walk)
-    walk_grid(ws_->work);
-  else
-    grid_slots(ws_->work, caller_vis);
+void OperatorT<real>::inverse_grid(void *x) {
   if (use_fused_fft()) {
     mark_begin(kFftI);
     if (own_cols_)
@@ -955,7 +964,48 @@ void OperatorT<real>::adjoint_slots(void *x, const void *caller_vis, bool walk) 
 }
 
 template <typename real>
+void OperatorT<real>::forward_slots(const void *x, void *caller_vis) {
+  forward_grid(x);
+  degrid_slots(ws_->work, caller_vis);
+}
+
+template <typename real>
+void OperatorT<real>::adjoint_slots(void *x, const void *caller_vis, bool walk) {
+  if (walk)
+    walk_grid(ws_->work);
+  else
+    grid_slots(ws_->work, caller_vis);
+  inverse_grid(x);
+}
+
+template <typename real>
 void OperatorT<real>::normal_slots(const void *x, void *out) {
+  if (one_pass_normal_) {
+    // F Z S, then G^H G in one pass over each task into the task windows,
+    // fold, and S^H Z^H F^H
+    forward_grid(x);
+    ApplyArgs<real> a;
+    a.grid = ws_->work;
+    a.tilebuf = ws_->tilebuf;
+    a.tasks = tasks_.as<Task>();
+    a.batches = batches_.as<int2>();
+    a.lane_code = lane_code_.as<int32_t>();
+    a.frac = frac_.get();
+    a.Nu = Nu_;
+    a.Nv = Nv_;
+    a.win_stride = win_stride_;
+    a.group_cells = group_;
+    a.order = task_order_.as<int32_t>();
+    a.slot_stride = slot_stride_;
+    mark_begin(kGrid);
+    cuda_check(launch_normal<real>(a, poly_, J_, ntasks_, win_rows_, win_cols_, shape_,
+                                   ws_->stream),
+               "normal");
+    mark_end(kGrid);
+    fold_into(ws_->work, ws_->tilebuf, tile_tasks_.as<int32_t>());
+    inverse_grid(out);
+    return;
+  }
   forward_slots(x);
   if (split_weights_)
     cuda_check(launch_cmul<real>(ws_->slots, weight_.get(), S_, true, ws_->stream), "weights");
