@@ -129,6 +129,7 @@ pg::OperatorConfig to_config(const purify_gb300_create_args *a, const purify_gb3
     c.keep_store = t->keep_store;
     c.fft_columns = t->fft_columns;
     c.grid_walk = t->grid_walk;
+    c.normal_pass = t->normal_pass;
   }
   if (a->precision != PURIFY_GB300_FP32 && a->precision != PURIFY_GB300_FP64)
     throw pg::Error(pg::kInvalidArgument, "unknown precision");

@@ -255,6 +255,57 @@ cudaError_t launch_degrid(const ApplyArgs<real> &a, const PolyTable<real> &poly,
   b.stage_bytes = int(stage_bytes(sizeof(real), J, user));
   return launch_apply<real, false>(true, b, poly, J, ntasks, smem, shape.threads, s);
 }
+size_t normal_smem_bytes(int precision_bytes, int J, int win_rows, int win_cols,
+                         const LaunchShape &shape, int group) {
+  if (precision_bytes != 4 || group != 1 || J < 1 || J > 6) return 0;
+  return window_bytes(precision_bytes, win_rows, win_cols, shape, false, group) +
+         window_bytes(precision_bytes, win_rows, win_cols, shape, true, group) + kHeaderBytes;
+}
+
+template <typename real, int J, bool SUB>
+cudaError_t launch_normal_one(const ApplyArgs<real> &a, const PolyTable<real> &poly, int ntasks,
+                              size_t smem, int threads, cudaStream_t s) {
+  auto fn = normal_kernel<real, J, SUB>;
+  if (smem > 48 * 1024) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+  }
+  return launch_chain(fn, dim3(ntasks), dim3(threads), smem, s, a, poly);
+}
+
+template <typename real>
+cudaError_t launch_normal(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
+                          int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
+                          cudaStream_t s) {
+  if constexpr (sizeof(real) != 4) {
+    return cudaErrorInvalidValue;
+  } else {
+    const size_t smem = normal_smem_bytes(sizeof(real), J, win_rows, win_cols, shape,
+                                          a.group_cells);
+    if (smem == 0 || a.slot_user || a.group) return cudaErrorInvalidValue;
+    if (ntasks == 0) return cudaSuccess;
+    ApplyArgs<real> b = a;
+    b.stage_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, false, 1));
+    b.win_bytes = b.stage_bytes + int(window_bytes(sizeof(real), win_rows, win_cols, shape, true, 1));
+    const bool sub = poly.nsub_u > 1 || poly.nsub_v > 1;
+    switch (J) {
+#define PG_NORMAL(JJ)                                                                        \
+  case JJ:                                                                                   \
+    return sub ? launch_normal_one<real, JJ, true>(b, poly, ntasks, smem, shape.threads, s)  \
+               : launch_normal_one<real, JJ, false>(b, poly, ntasks, smem, shape.threads, s);
+      PG_NORMAL(1)
+      PG_NORMAL(2)
+      PG_NORMAL(3)
+      PG_NORMAL(4)
+      PG_NORMAL(5)
+      PG_NORMAL(6)
+#undef PG_NORMAL
+    }
+    return cudaErrorInvalidValue;
+  }
+}
+
 template <typename real>
 cudaError_t launch_grid(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
                         int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
@@ -420,6 +471,8 @@ cudaError_t launch_fill(void *x, int64_t n, double value, cudaStream_t s) {
                                            int, int, int, const LaunchShape &, cudaStream_t);   \
   template cudaError_t launch_grid<real>(const ApplyArgs<real> &, const PolyTable<real> &, int,   \
                                          int, int, int, const LaunchShape &, cudaStream_t);     \
+  template cudaError_t launch_normal<real>(const ApplyArgs<real> &, const PolyTable<real> &, int, \
+                                           int, int, int, const LaunchShape &, cudaStream_t);   \
   template cudaError_t launch_fold<real>(const FoldArgs &, cudaStream_t);                       \
   template cudaError_t launch_walk_grid<real>(const WalkArgs<real> &, const PolyTable<real> &,  \
                                               int, int, int, cudaStream_t);                     \

@@ -37,7 +37,9 @@ struct ApplyArgs {
   int keep_in = 0;
   int64_t slot_stride = 0;          // complex elements per tilebuf slot
   int win_bytes = 0;    // set by the launchers: shared bytes before the batch headers
-  int stage_bytes = 0;  // set by the launchers: per-warp staging stride
+  // set by the launchers: degrid, the per-warp staging stride; normal, the
+  // shared bytes of the grid window before the warp windows
+  int stage_bytes = 0;
   // Grouped launch over several operators: a device array of per-operator
   // ApplyArgs (indexed by Task::channel) and the first task of each operator
   // in the grouped task list (its tilebuf holds windows from that index on).
@@ -68,6 +70,17 @@ template <typename real>
 cudaError_t launch_degrid(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
                           int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
                           cudaStream_t s);
+// G^H G of the normal operator in one pass (unit weights): the grid at a.grid
+// -> one accumulated window per task at a.tilebuf, as launch_grid leaves
+// them for the slot-ordered output of launch_degrid.
+template <typename real>
+cudaError_t launch_normal(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
+                          int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
+                          cudaStream_t s);
+// Shared memory of launch_normal, or 0 where it does not apply (FP32,
+// single-cell items, J <= 6).
+size_t normal_smem_bytes(int precision_bytes, int J, int win_rows, int win_cols,
+                         const LaunchShape &shape, int group);
 // G^H, first half: visibilities -> one accumulated window per task.
 template <typename real>
 cudaError_t launch_grid(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,

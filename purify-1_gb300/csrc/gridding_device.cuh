@@ -535,6 +535,163 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
   }
 }
 
+// G^H G of the normal operator Phi^H Phi in one pass over each task (unit
+// weights, single-cell items).  The task's grid window is staged in shared
+// memory as in degrid_kernel, and the warp windows are zeroed as in
+// grid_kernel.  Each lane keeps its item's J x J grid block F and its J x J
+// accumulator block in registers.  Per visibility it evaluates the taps once,
+// contracts them with F (the visibility degrid_kernel computes, in its order),
+// and adds that value times the taps into the accumulator (grid_kernel's
+// order; the two phase signs cancel).  Null slots add nothing.  Flushes,
+// window sums and the task window written out are grid_kernel's.  So the
+// task windows are those grid_kernel makes from degrid_kernel's slot-ordered
+// output, bit for bit, without the slot-ordered vector and with one tap
+// evaluation per visibility instead of two.  Shared memory: the grid window
+// (a.stage_bytes bytes), the warp windows, then the batch headers at
+// a.win_bytes.
+template <typename real, int J, bool SUB>
+__global__ void __launch_bounds__(256) normal_kernel(const ApplyArgs<real> a,
+                                                     const __grid_constant__ PolyTable<real> poly) {
+  using C = cplx<real>;
+  constexpr int G = 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  pdl_launch_next();
+  const int task_id = a.order ? a.order[blockIdx.x] : int(blockIdx.x);
+  const Task tk = a.tasks[task_id];
+  const int WW = tk.W + J - 1, WH = tk.H + J - 1, WS = a.win_stride, WN = win_cells(WH, WS, G);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  C *gwin = reinterpret_cast<C *>(smem_raw);
+  C *wins = reinterpret_cast<C *>(smem_raw + a.stage_bytes);
+  const TaskHeaders th = load_headers(a, tk, smem_raw + a.win_bytes);
+  {
+    // zero the warp windows, 16 bytes per store (stage_bytes is a multiple
+    // of 16; an odd FP32 cell count leaves one 8-byte cell at the end)
+    const size_t bytes = size_t(nw) * WN * sizeof(C);
+    uint4 *z = reinterpret_cast<uint4 *>(smem_raw + a.stage_bytes);
+    for (int idx = threadIdx.x; idx < int(bytes / 16); idx += blockDim.x)
+      z[idx] = make_uint4(0u, 0u, 0u, 0u);
+    if (bytes % 16 != 0 && threadIdx.x == 0) wins[nw * WN - 1] = C{0, 0};
+  }
+  const C *grid = static_cast<const C *>(a.grid);
+  const size_t ld = size_t(a.ld ? a.ld : a.Nu);
+  pdl_wait();  // the grid is the previous kernel's output
+  WinCursor cur(threadIdx.x, WW, blockDim.x);
+  for (int idx = threadIdx.x; idx < WW * WH; idx += blockDim.x, cur.next(WW)) {
+    int p = tk.P + cur.lp;
+    if (p >= a.Nv) p -= a.Nv;
+    int q = tk.Q + cur.lq;
+    if (q >= a.Nu) q -= a.Nu;
+    cp_async<sizeof(C)>(gwin + win_offset(cur.lp, cur.lq, WS, G), grid + size_t(p) * ld + q);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  C *mine = wins + warp * WN;
+  const int nbt = tk.batch_end - tk.batch_begin;
+  const C *frac = static_cast<const C *>(a.frac);
+  if (warp < nbt) {
+    // compute cursor (clb, ck) and, two steps ahead, the prefetch cursor of
+    // the fractions, as in grid_kernel
+    int clb = warp, ck = 0;
+    int plb = warp, pk = 0;
+    int code_c = lane_code_at(th, clb, nbt, lane);
+    int code_n = lane_code_at(th, clb + nw, nbt, lane);
+    auto adv = [&](int &lb, int &k) {
+      if (k + 1 < th.hdr[lb].y) {
+        ++k;
+      } else {
+        k = 0;
+        lb += nw;
+      }
+    };
+    auto slot = [&](int lb, int k) { return size_t(th.hdr[lb].x) + size_t(k) * kBatch + lane; };
+    C t0 = stream_load(frac + slot(plb, pk));
+    adv(plb, pk);
+    C t1{0, 0};
+    if (plb < nbt) {
+      t1 = stream_load(frac + slot(plb, pk));
+      adv(plb, pk);
+    }
+    C F[J][J], acc[J][J];
+    int cnt = 0;
+    auto load_block = [&](int code) {
+      cnt = item_count(code);
+      const C *blk = gwin + win_offset(item_lp(code), item_lq(code), WS, G);
+#pragma unroll
+      for (int jv = 0; jv < J; ++jv)
+#pragma unroll
+        for (int ju = 0; ju < J; ++ju) F[jv][ju] = blk[win_offset(jv, ju, WS, G)];
+    };
+    load_block(code_c);
+#pragma unroll
+    for (int jv = 0; jv < J; ++jv)
+#pragma unroll
+      for (int ju = 0; ju < J; ++ju) acc[jv][ju] = C{0, 0};
+    while (clb < nbt) {
+      const C t = t0;
+      t0 = t1;
+      if (plb < nbt) {
+        t1 = stream_load(frac + slot(plb, pk));
+        adv(plb, pk);
+      }
+      real ku[J], kv[J];
+      block_taps<real, J, 1, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
+      block_taps<real, J, 1, SUB>(poly.v, poly.nsub_v, t.y, kv);
+      C sum{0, 0};
+#pragma unroll
+      for (int jv = 0; jv < J; ++jv) {
+        C row{0, 0};
+#pragma unroll
+        for (int ju = 0; ju < J; ++ju) row = fma2(splat(ku[ju]), F[jv][ju], row);
+        sum = fma2(splat(kv[jv]), row, sum);
+      }
+      if (ck < cnt) {
+#pragma unroll
+        for (int jv = 0; jv < J; ++jv) {
+          const C az = mul2(sum, splat(kv[jv]));
+#pragma unroll
+          for (int ju = 0; ju < J; ++ju) acc[jv][ju] = fma2(az, splat(ku[ju]), acc[jv][ju]);
+        }
+      }
+      if (ck + 1 >= th.hdr[clb].y) {
+        // flush at the end of the batch, as grid_kernel does
+        const int code = code_c;
+        code_c = code_n;
+        code_n = lane_code_at(th, clb + 2 * nw, nbt, lane);
+        const int fcnt = item_count(code);
+        C *blk = mine + win_offset(item_lp(code), item_lq(code), WS, G);
+#pragma unroll
+        for (int jv = 0; jv < J; ++jv)
+#pragma unroll
+          for (int ju = 0; ju < J; ++ju) {
+            if (fcnt > 0) {
+              C *cell = blk + win_offset(jv, ju, WS, G);
+              *cell = add2(*cell, acc[jv][ju]);
+            }
+            acc[jv][ju] = C{0, 0};
+            __syncwarp();
+          }
+        adv(clb, ck);
+        if (clb < nbt) load_block(code_c);
+      } else {
+        adv(clb, ck);
+      }
+    }
+  }
+  __syncthreads();
+  C *out = static_cast<C *>(a.tilebuf) + size_t(task_id) * a.slot_stride;
+  WinCursor oc(threadIdx.x, WW, blockDim.x);
+  for (int idx = threadIdx.x; idx < WW * WH; idx += blockDim.x, oc.next(WW)) {
+    const int e = win_offset(oc.lp, oc.lq, WS, G);
+    C s = wins[e];
+    for (int w = 1; w < nw; ++w) {
+      const C o = wins[w * WN + e];
+      s.x += o.x;
+      s.y += o.y;
+    }
+    out[idx] = s;
+  }
+}
+
 // G^H on the column-walk plan, one CTA per task (an occupied tile), kWalkWarps
 // warps with a shared-memory window each.  Warp w takes the tile's base-cell
 // columns [w W / nw, (w + 1) W / nw); its lane r is row r.  Each lane keeps a

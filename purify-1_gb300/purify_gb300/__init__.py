@@ -56,7 +56,7 @@ class Tuning(ctypes.Structure):
                 ("tile", ctypes.c_int32), ("fused_permute", ctypes.c_int32),
                 ("cell_group", ctypes.c_int32), ("class_cap", ctypes.c_int32),
                 ("keep_store", ctypes.c_int32), ("fft_columns", ctypes.c_int32),
-                ("grid_walk", ctypes.c_int32)]
+                ("grid_walk", ctypes.c_int32), ("normal_pass", ctypes.c_int32)]
 
 
 class Info(ctypes.Structure):
@@ -485,7 +485,7 @@ class MeasurementOperator:
                        int(tuning.get("tile", 0)), int(tuning.get("fused_permute", -1)),
                        int(tuning.get("cell_group", 0)), int(tuning.get("class_cap", 0)),
                        int(tuning.get("keep_store", 0)), int(tuning.get("fft_columns", 0)),
-                       int(tuning.get("grid_walk", 0)))
+                       int(tuning.get("grid_walk", 0)), int(tuning.get("normal_pass", 0)))
             _check(L.purify_gb300_operator_create_tuned(ctypes.byref(a), ctypes.byref(t),
                                                         ctypes.byref(h)))
         else:

@@ -56,6 +56,36 @@ def test_normal_equals_forward_then_adjoint(pg, cuda, precision):
     assert torch.equal(y, a)
 
 
+@pytest.mark.parametrize("kernel,J", [("kb", 4), ("kb", 6), ("pswf", 6), ("gauss", 3),
+                                      ("box", 1)])
+def test_one_pass_normal_is_bit_identical(pg, oracle_mod, cuda, kernel, J):
+    """G^H G of the normal operator in one pass over each task (tuning
+    normal_pass = 1: FP32, unit weights, single-cell items) evaluates the
+    taps once and keeps no slot-ordered vector, yet sums the same values in
+    the same order as degrid then grid: normal, in place and out of place,
+    and the power method are bit-identical to the default path, and match
+    the oracle.  A dense cell puts several visibilities on one item."""
+    torch = cuda
+    u, v, n = case(n=96, M=9000, seed=J)
+    u[:300], v[:300] = 1.3, -2.6
+    ops = [pg.MeasurementOperator(u, v, None, None, n, n, 2.0, power_iters=0, precision="fp32",
+                                  kernel=kernel, Ju=J, Jv=J, tuning={"normal_pass": p})
+           for p in (0, 1)]
+    x = dev(torch, synthetic.sky_image(n, n, seed=J), "fp32")
+    a, b = ops[0].normal(x), ops[1].normal(x)
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)
+    y = x.clone()
+    ops[1].normal_into(y, y)
+    torch.cuda.synchronize()
+    assert torch.equal(y, b)
+    assert ops[0].power_method(8, 0.0) == ops[1].power_method(8, 0.0)
+    oop = oracle_mod.Operator(u, v, None, None, n, n, 2.0, kernel=kernel, Ju=J, Jv=J)
+    oop.set_norm(ops[1].norm)
+    c = host(ops[1].normal(x))
+    assert rel_l2(c, oop.adjoint(oop.forward(host(x)))) < TOL["fp32"]
+
+
 @pytest.mark.parametrize("precision", ["fp32", "fp64"])
 def test_normal_vs_oracle_and_norm(pg, oracle_mod, cuda, precision):
     torch = cuda
