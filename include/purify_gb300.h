@@ -121,10 +121,11 @@ typedef struct {
                             strided column plan */
   int32_t grid_walk;     /* G^H of Phi^H: 1 = the column walk where it applies (tiles <= 32,
                             single-cell items, J <= 8, J <= 6 in FP64), 0 = work items */
-  int32_t normal_pass;   /* G^H G of purify_gb300_normal and the power method: 0 = degrid
-                            then grid through the slot-ordered buffer, 1 = one pass over
-                            each task where it applies (FP32, unit weights, single-cell
-                            items, J <= 6); the results are bit-identical */
+  int32_t normal_pass;   /* G^H G of purify_gb300_normal and the power method: 1 = one
+                            pass over each task where it applies (FP32, unit weights,
+                            single-cell items, J <= 6), 2 = degrid then grid through the
+                            slot-ordered buffer, 0 = default (one pass for J < 6); the
+                            results are bit-identical */
 } purify_gb300_tuning;
 int purify_gb300_operator_create_tuned(const purify_gb300_create_args *args,
                                        const purify_gb300_tuning *tuning,

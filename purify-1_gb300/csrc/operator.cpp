@@ -45,6 +45,10 @@ namespace {
 // Supports from which the default launch shape and adjoint path change
 // (see the constructor).
 constexpr int kWideSupport = 6;
+// Launch shape of normal_kernel: two warps per CTA.  Its two register
+// blocks per lane leave room for few warps, and its shared memory holds the
+// grid window besides the warp windows.
+constexpr LaunchShape kNormalShape{64};
 constexpr int kWalkThreads = 128;
 constexpr int kWalkMaxCellCount = 256;
 }  // namespace
@@ -324,8 +328,10 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
       throw Error(kUnsupported, "tile / threads / support need " + std::to_string(need) +
                                     " bytes of shared memory per CTA; the device allows " +
                                     std::to_string(optin));
-    const size_t nsm = normal_smem_bytes(sizeof(real), J_, win_rows_, win_cols_, shape_, group_);
-    one_pass_normal_ = cfg.normal_pass == 1 && !split_weights_ && nsm > 0 && nsm <= size_t(optin);
+    const size_t nsm =
+        normal_smem_bytes(sizeof(real), J_, win_rows_, win_cols_, kNormalShape, group_);
+    const bool want = cfg.normal_pass == 1 || (cfg.normal_pass == 0 && J_ < kWideSupport);
+    one_pass_normal_ = want && !split_weights_ && nsm > 0 && nsm <= size_t(optin);
   }
   {
     tile_tasks_.alloc(sizeof(int32_t) * tile_tasks.size(), &bytes);
@@ -998,7 +1004,7 @@ void OperatorT<real>::normal_slots(const void *x, void *out) {
     a.order = task_order_.as<int32_t>();
     a.slot_stride = slot_stride_;
     mark_begin(kGrid);
-    cuda_check(launch_normal<real>(a, poly_, J_, ntasks_, win_rows_, win_cols_, shape_,
+    cuda_check(launch_normal<real>(a, poly_, J_, ntasks_, win_rows_, win_cols_, kNormalShape,
                                    ws_->stream),
                "normal");
     mark_end(kGrid);

@@ -61,10 +61,11 @@ struct OperatorConfig {
   // traffic but runs 2.2x the visibility steps on the 10^7 workload (a
   // column lasts as long as its fullest row), and measured slower there.
   int grid_walk = 0;
-  // G^H G of the normal operator: 0 = degrid then grid through the slot
-  // buffer, 1 = normal_kernel's one pass where it applies.  The one pass
-  // evaluates the taps once and keeps no slot vector, but holds two J x J
-  // register blocks (194 registers at J = 6) and measured slower.
+  // G^H G of the normal operator: 1 = normal_kernel's one pass where it
+  // applies, 2 = degrid then grid through the slot buffer, 0 = the default
+  // (one pass for J < 6).  The one pass evaluates the taps once and keeps
+  // no slot vector, but holds two J x J register blocks (194 registers at
+  // J = 6, where it measured slower).
   int normal_pass = 0;
 };
 

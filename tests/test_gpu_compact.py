@@ -60,17 +60,20 @@ def test_normal_equals_forward_then_adjoint(pg, cuda, precision):
                                       ("box", 1)])
 def test_one_pass_normal_is_bit_identical(pg, oracle_mod, cuda, kernel, J):
     """G^H G of the normal operator in one pass over each task (tuning
-    normal_pass = 1: FP32, unit weights, single-cell items) evaluates the
+    normal_pass = 1, the default below J = 6; FP32, unit weights,
+    single-cell items) evaluates the
     taps once and keeps no slot-ordered vector, yet sums the same values in
-    the same order as degrid then grid: normal, in place and out of place,
-    and the power method are bit-identical to the default path, and match
+    the same order as degrid then grid (normal_pass = 2) with the same
+    two-warp CTAs: normal, in place and out of place, and the power method
+    are bit-identical to that path, and match
     the oracle.  A dense cell puts several visibilities on one item."""
     torch = cuda
     u, v, n = case(n=96, M=9000, seed=J)
     u[:300], v[:300] = 1.3, -2.6
     ops = [pg.MeasurementOperator(u, v, None, None, n, n, 2.0, power_iters=0, precision="fp32",
-                                  kernel=kernel, Ju=J, Jv=J, tuning={"normal_pass": p})
-           for p in (0, 1)]
+                                  kernel=kernel, Ju=J, Jv=J,
+                                  tuning={"normal_pass": p, "threads": 64})
+           for p in (2, 1)]
     x = dev(torch, synthetic.sky_image(n, n, seed=J), "fp32")
     a, b = ops[0].normal(x), ops[1].normal(x)
     torch.cuda.synchronize()
