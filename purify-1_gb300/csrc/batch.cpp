@@ -978,6 +978,9 @@ BatchTuning autotune_batch(const BatchConfig &cfg) {
   cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, cfg.device),
              "cudaDeviceGetAttribute");
   const int prec = cfg.fp64 ? 8 : 4;
+  // sub-segments of the tap fit (their coefficients take shared memory)
+  const int nsub = fit_axis(GriddingKernel(cfg.kernel, cfg.J, cfg.oversample_ratio), cfg.J,
+                            cfg.fp64 ? kCoefF64 : kCoefF32).nsub;
   BatchTuning best;
   double best_ms = -1;
   const int max_group = (!cfg.fp64 && cfg.J <= kMaxGroupJ) ? 2 : 1;
@@ -995,10 +998,10 @@ BatchTuning autotune_batch(const BatchConfig &cfg) {
       LaunchShape shape;
       shape.threads = threads;
       const bool degrid_fits =
-          degrid_smem_bytes(prec, cfg.J, bi.win_rows, bi.win_cols, shape, true, group) <=
+          degrid_smem_bytes(prec, cfg.J, bi.win_rows, bi.win_cols, shape, true, group, nsub) <=
           size_t(optin);
       const bool grid_fits =
-          grid_smem_bytes(prec, cfg.J, bi.win_rows, bi.win_cols, shape, false, group) <=
+          grid_smem_bytes(prec, cfg.J, bi.win_rows, bi.win_cols, shape, false, group, nsub) <=
           size_t(optin);
       if (!degrid_fits || !grid_fits) continue;
       b->set_launch_shapes(threads, threads);

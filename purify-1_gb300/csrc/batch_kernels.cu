@@ -158,7 +158,8 @@ cudaError_t launch_degrid_group(const ApplyArgs<real> &a, const PolyTable<real> 
                                 int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
                                 bool user, cudaStream_t s) {
   const size_t smem =
-      degrid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, a.group_cells);
+      degrid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, a.group_cells,
+                        poly_nsub(poly));
   ApplyArgs<real> b = a;
   b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, false, a.group_cells));
   b.stage_bytes = int(stage_bytes(sizeof(real), J, user));
@@ -168,7 +169,8 @@ template <typename real>
 cudaError_t launch_grid_group(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
                               int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
                               bool user, cudaStream_t s) {
-  const size_t smem = grid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, a.group_cells);
+  const size_t smem = grid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user,
+                                      a.group_cells, poly_nsub(poly));
   ApplyArgs<real> b = a;
   b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, true, a.group_cells));
   return launch_apply<real, true>(false, b, poly, J, ntasks, smem, shape.threads, s);

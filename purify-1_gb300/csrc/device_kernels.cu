@@ -234,13 +234,15 @@ int stream_blocks(int64_t n, int threads) {
 }  // namespace
 
 size_t degrid_smem_bytes(int precision_bytes, int J, int win_rows, int win_cols,
-                         const LaunchShape &shape, bool user, int group) {
+                         const LaunchShape &shape, bool user, int group, int nsub) {
   return window_bytes(precision_bytes, win_rows, win_cols, shape, false, group) + kHeaderBytes +
-         size_t(shape.threads / 32) * stage_bytes(precision_bytes, J, user);
+         size_t(shape.threads / 32) * stage_bytes(precision_bytes, J, user) +
+         coefficient_bytes(precision_bytes, J, nsub);
 }
-size_t grid_smem_bytes(int precision_bytes, int, int win_rows, int win_cols,
-                       const LaunchShape &shape, bool, int group) {
-  return window_bytes(precision_bytes, win_rows, win_cols, shape, true, group) + kHeaderBytes;
+size_t grid_smem_bytes(int precision_bytes, int J, int win_rows, int win_cols,
+                       const LaunchShape &shape, bool, int group, int nsub) {
+  return window_bytes(precision_bytes, win_rows, win_cols, shape, true, group) + kHeaderBytes +
+         coefficient_bytes(precision_bytes, J, nsub);
 }
 
 template <typename real>
@@ -248,18 +250,19 @@ cudaError_t launch_degrid(const ApplyArgs<real> &a, const PolyTable<real> &poly,
                           int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
                           cudaStream_t s) {
   const bool user = a.slot_user != nullptr;
-  const size_t smem =
-      degrid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, a.group_cells);
+  const size_t smem = degrid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user,
+                                        a.group_cells, poly_nsub(poly));
   ApplyArgs<real> b = a;
   b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, false, a.group_cells));
   b.stage_bytes = int(stage_bytes(sizeof(real), J, user));
   return launch_apply<real, false>(true, b, poly, J, ntasks, smem, shape.threads, s);
 }
 size_t normal_smem_bytes(int precision_bytes, int J, int win_rows, int win_cols,
-                         const LaunchShape &shape, int group) {
+                         const LaunchShape &shape, int group, int nsub) {
   if (precision_bytes != 4 || group != 1 || J < 1 || J > 6) return 0;
   return window_bytes(precision_bytes, win_rows, win_cols, shape, false, group) +
-         window_bytes(precision_bytes, win_rows, win_cols, shape, true, group) + kHeaderBytes;
+         window_bytes(precision_bytes, win_rows, win_cols, shape, true, group) + kHeaderBytes +
+         coefficient_bytes(precision_bytes, J, nsub);
 }
 
 template <typename real, int J, bool SUB>
@@ -282,7 +285,7 @@ cudaError_t launch_normal(const ApplyArgs<real> &a, const PolyTable<real> &poly,
     return cudaErrorInvalidValue;
   } else {
     const size_t smem = normal_smem_bytes(sizeof(real), J, win_rows, win_cols, shape,
-                                          a.group_cells);
+                                          a.group_cells, poly_nsub(poly));
     if (smem == 0 || a.slot_user || a.group) return cudaErrorInvalidValue;
     if (ntasks == 0) return cudaSuccess;
     ApplyArgs<real> b = a;
@@ -311,7 +314,8 @@ cudaError_t launch_grid(const ApplyArgs<real> &a, const PolyTable<real> &poly, i
                         int ntasks, int win_rows, int win_cols, const LaunchShape &shape,
                         cudaStream_t s) {
   const bool user = a.slot_user != nullptr;
-  const size_t smem = grid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user, a.group_cells);
+  const size_t smem = grid_smem_bytes(sizeof(real), J, win_rows, win_cols, shape, user,
+                                      a.group_cells, poly_nsub(poly));
   ApplyArgs<real> b = a;
   b.win_bytes = int(window_bytes(sizeof(real), win_rows, win_cols, shape, true, a.group_cells));
   return launch_apply<real, false>(false, b, poly, J, ntasks, smem, shape.threads, s);
@@ -320,7 +324,8 @@ cudaError_t launch_grid(const ApplyArgs<real> &a, const PolyTable<real> &poly, i
 template <typename real, int J, bool SUB>
 cudaError_t launch_walk_one(const WalkArgs<real> &a, const PolyTable<real> &poly, int ntasks,
                             int threads, cudaStream_t s) {
-  const size_t smem = walk_smem_bytes(sizeof(real), a.win_rows, a.win_stride, a.max_steps);
+  const size_t smem = walk_smem_bytes(sizeof(real), a.win_rows, a.win_stride, a.max_steps, J,
+                                      poly_nsub(poly));
   auto fn = walk_grid_kernel<real, J, SUB>;
   if (smem > 48 * 1024) {
     const cudaError_t e =
@@ -339,7 +344,10 @@ cudaError_t launch_walk_grid(const WalkArgs<real> &a, const PolyTable<real> &pol
     return cudaErrorInvalidValue;
   const bool sub = poly.nsub_u > 1 || poly.nsub_v > 1;
   switch (J) {
-#define PG_WALK(JJ)                                                                        case JJ:                                                                                   return sub ? launch_walk_one<real, JJ, true>(a, poly, ntasks, threads, s)                          : launch_walk_one<real, JJ, false>(a, poly, ntasks, threads, s);
+#define PG_WALK(JJ)                                                        \
+  case JJ:                                                                 \
+    return sub ? launch_walk_one<real, JJ, true>(a, poly, ntasks, threads, s) \
+               : launch_walk_one<real, JJ, false>(a, poly, ntasks, threads, s);
     PG_WALK(1)
     PG_WALK(2)
     PG_WALK(3)

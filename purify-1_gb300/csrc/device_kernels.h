@@ -60,10 +60,13 @@ struct LaunchShape {
 // Largest dynamic shared memory a launch of the given shape needs, in bytes:
 // user = visibilities in caller order (it sizes the degrid kernel's staging
 // buffers; the grid kernel has none).
+// nsub > 1 adds the tap coefficients the kernels copy into shared memory.
 size_t degrid_smem_bytes(int precision_bytes, int J, int win_rows, int win_cols,
-                         const LaunchShape &shape, bool user = true, int group = 1);
+                         const LaunchShape &shape, bool user = true, int group = 1,
+                         int nsub = 1);
 size_t grid_smem_bytes(int precision_bytes, int J, int win_rows, int win_cols,
-                       const LaunchShape &shape, bool user = false, int group = 1);
+                       const LaunchShape &shape, bool user = false, int group = 1,
+                       int nsub = 1);
 
 // G: tiles of the grid -> visibilities.
 template <typename real>
@@ -80,7 +83,7 @@ cudaError_t launch_normal(const ApplyArgs<real> &a, const PolyTable<real> &poly,
 // Shared memory of launch_normal, or 0 where it does not apply (FP32,
 // single-cell items, J <= 6).
 size_t normal_smem_bytes(int precision_bytes, int J, int win_rows, int win_cols,
-                         const LaunchShape &shape, int group);
+                         const LaunchShape &shape, int group, int nsub = 1);
 // G^H, first half: visibilities -> one accumulated window per task.
 template <typename real>
 cudaError_t launch_grid(const ApplyArgs<real> &a, const PolyTable<real> &poly, int J,
@@ -109,9 +112,19 @@ cudaError_t launch_walk_grid(const WalkArgs<real> &a, const PolyTable<real> &pol
 // Shared memory of a column-walk CTA: kWalkWarps windows of win_rows x
 // win_stride cells, and per warp a list of max_steps steps and its column
 // offsets into it.
-inline size_t walk_smem_bytes(int precision_bytes, int win_rows, int win_stride, int max_steps) {
-  return size_t(kWalkWarps) * (size_t(win_rows) * win_stride * 2 * precision_bytes +
-                               size_t(max_steps) * 8 + 9 * 4);
+// With nsub > 1 the tap coefficients follow, from the next 16-byte boundary
+// (walk_coefficient_offset).
+PG_HD inline size_t walk_coefficient_offset(int precision_bytes, int win_rows, int win_stride,
+                                            int max_steps) {
+  const size_t b = size_t(kWalkWarps) * (size_t(win_rows) * win_stride * 2 * precision_bytes +
+                                         size_t(max_steps) * 8 + 9 * 4);
+  return (b + 15) / 16 * 16;
+}
+inline size_t walk_smem_bytes(int precision_bytes, int win_rows, int win_stride, int max_steps,
+                              int J = 1, int nsub = 1) {
+  const size_t nc = precision_bytes == 8 ? 17 : 9;  // PolyCount<double>, PolyCount<float>
+  return walk_coefficient_offset(precision_bytes, win_rows, win_stride, max_steps) +
+         (nsub > 1 ? size_t(J) * nsub * nc * precision_bytes : 0);
 }
 
 // Grouped forms: `a.tasks` lists the tasks of several operators (Task::channel

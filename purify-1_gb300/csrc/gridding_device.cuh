@@ -24,18 +24,26 @@ namespace dev {
 // the family is even, so tap J-1-j at x is (-1)^(J-1) times tap j at -x: the
 // pair shares one evaluation split into even and odd parts,
 // P_j(x) = E(x^2) + x O(x^2), P_{J-1-j}(x) = (-1)^(J-1) (E(x^2) - x O(x^2)).
+//
+// With SUB the lanes of a warp read the coefficients of different
+// sub-segments.  From the parameter space those reads are served one
+// address at a time, so the kernels first copy the coefficients into shared
+// memory (stage_coefficients) and pass them as csm, laid out
+// [j][s][c] -> csm[(j nsub + s) NC + c]: the lanes' sub-segments sit NC words
+// apart, on different banks.
 template <typename real, int J, bool SUB, int NC>
 __device__ __forceinline__ void tap_weights(const PolyAxis<real, NC> &P, int nsub, real t,
-                                            real (&k)[J]) {
+                                            real (&k)[J], const real *csm = nullptr) {
   if (SUB) {
     const real ts = t * real(nsub);
     const int s = min(int(ts), nsub - 1);
     const real x = real(2) * (ts - real(s)) - real(1);
 #pragma unroll
     for (int j = 0; j < J; ++j) {
-      real acc = P.c[j][s][NC - 1];
+      const real *c = csm + (j * nsub + s) * NC;
+      real acc = c[NC - 1];
 #pragma unroll
-      for (int c = NC - 2; c >= 0; --c) acc = fma(acc, x, P.c[j][s][c]);
+      for (int i = NC - 2; i >= 0; --i) acc = fma(acc, x, c[i]);
       k[j] = acc;
     }
     return;
@@ -66,17 +74,31 @@ __device__ __forceinline__ void tap_weights(const PolyAxis<real, NC> &P, int nsu
 // block cell is 0.
 template <typename real, int J, int G, bool SUB, int NC>
 __device__ __forceinline__ void block_taps(const PolyAxis<real, NC> &P, int nsub, real x,
-                                           real (&k)[J + G - 1]) {
+                                           real (&k)[J + G - 1], const real *csm = nullptr) {
   if constexpr (G == 1) {
-    tap_weights<real, J, SUB>(P, nsub, x, k);
+    tap_weights<real, J, SUB>(P, nsub, x, k, csm);
   } else {
     const bool d = x >= real(1);
     real kk[J];
-    tap_weights<real, J, SUB>(P, nsub, d ? x - real(1) : x, kk);
+    tap_weights<real, J, SUB>(P, nsub, d ? x - real(1) : x, kk, csm);
     k[0] = d ? real(0) : kk[0];
 #pragma unroll
     for (int j = 1; j < J; ++j) k[j] = d ? kk[j - 1] : kk[j];
     k[J] = d ? kk[J - 1] : real(0);
+  }
+}
+
+// Copies the tap coefficients of the J taps and nsub sub-segments of P into
+// csm (layout of tap_weights); the caller's next __syncthreads publishes
+// them.  The register-block operators use one polynomial for both axes (one
+// kernel, Ju == Jv), so one copy serves u and v.
+template <typename real, int J, int NC>
+__device__ __forceinline__ void stage_coefficients(const PolyAxis<real, NC> &P, int nsub,
+                                                   real *csm) {
+  const int n = J * nsub * NC;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int c = i % NC, js = i / NC;
+    csm[i] = P.c[js / nsub][js % nsub][c];
   }
 }
 
@@ -281,6 +303,10 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
   const TaskHeaders th = load_headers(a, tk, smem_raw + a0.win_bytes);
   const C *grid = static_cast<const C *>(a.grid);
   const size_t ld = size_t(a.ld ? a.ld : a.Nu);
+  // tap coefficients of sub-segmented kernels, after the staging buffers
+  real *csm = reinterpret_cast<real *>(smem_raw + a0.win_bytes + kHeaderBytes +
+                                       size_t(blockDim.x >> 5) * a0.stage_bytes);
+  if (SUB) stage_coefficients<real, J>(poly.u, poly.nsub_u, csm);
   // the grid is the previous kernel's output
   pdl_wait();
   // Stage the (wrapped) window of the grid this tile's footprints touch.
@@ -354,8 +380,8 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
       const int e = (buf * CH + j) * 32 + lane;
       const C t = st_t[e];
       real ku[JBU], kv[JBV];
-      block_taps<real, J, group_u(G), SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
-      block_taps<real, J, group_v(G), SUB>(poly.v, poly.nsub_v, t.y, kv);
+      block_taps<real, J, group_u(G), SUB>(poly.u, poly.nsub_u, fabs(t.x), ku, csm);
+      block_taps<real, J, group_v(G), SUB>(poly.v, poly.nsub_v, t.y, kv, csm);
       C sum{0, 0};
 #pragma unroll
       for (int jv = 0; jv < JBV; ++jv) {
@@ -418,6 +444,9 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
       z[idx] = make_uint4(0u, 0u, 0u, 0u);
     if (bytes % 16 != 0 && threadIdx.x == 0) wins[nw * WN - 1] = C{0, 0};
   }
+  // tap coefficients of sub-segmented kernels, after the batch headers
+  real *csm = reinterpret_cast<real *>(smem_raw + a0.win_bytes + kHeaderBytes);
+  if (SUB) stage_coefficients<real, J>(poly.u, poly.nsub_u, csm);
   cp_async_wait_all();
   __syncthreads();
   // the visibilities are the previous kernel's output
@@ -485,8 +514,8 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
       const real sg = copysign(real(1), t.x);
       const real zr = sg * yv.x, zi = sg * yv.y;
       real ku[JBU], kv[JBV];
-      block_taps<real, J, group_u(G), SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
-      block_taps<real, J, group_v(G), SUB>(poly.v, poly.nsub_v, t.y, kv);
+      block_taps<real, J, group_u(G), SUB>(poly.u, poly.nsub_u, fabs(t.x), ku, csm);
+      block_taps<real, J, group_v(G), SUB>(poly.v, poly.nsub_v, t.y, kv, csm);
       const C z{zr, zi};
 #pragma unroll
       for (int jv = 0; jv < JBV; ++jv) {
@@ -572,6 +601,9 @@ __global__ void __launch_bounds__(256) normal_kernel(const ApplyArgs<real> a,
       z[idx] = make_uint4(0u, 0u, 0u, 0u);
     if (bytes % 16 != 0 && threadIdx.x == 0) wins[nw * WN - 1] = C{0, 0};
   }
+  // tap coefficients of sub-segmented kernels, after the batch headers
+  real *csm = reinterpret_cast<real *>(smem_raw + a.win_bytes + kHeaderBytes);
+  if (SUB) stage_coefficients<real, J>(poly.u, poly.nsub_u, csm);
   const C *grid = static_cast<const C *>(a.grid);
   const size_t ld = size_t(a.ld ? a.ld : a.Nu);
   pdl_wait();  // the grid is the previous kernel's output
@@ -634,8 +666,8 @@ __global__ void __launch_bounds__(256) normal_kernel(const ApplyArgs<real> a,
         adv(plb, pk);
       }
       real ku[J], kv[J];
-      block_taps<real, J, 1, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
-      block_taps<real, J, 1, SUB>(poly.v, poly.nsub_v, t.y, kv);
+      block_taps<real, J, 1, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku, csm);
+      block_taps<real, J, 1, SUB>(poly.v, poly.nsub_v, t.y, kv, csm);
       C sum{0, 0};
 #pragma unroll
       for (int jv = 0; jv < J; ++jv) {
@@ -731,6 +763,10 @@ __global__ void __launch_bounds__(128, (sizeof(real) == 4 && J <= 6) ? 4 : 2) wa
                                          size_t(nw) * a.max_steps * sizeof(int2)) +
                  warp * (kWalkMaxCols + 1);
   for (int idx = threadIdx.x; idx < nw * WN; idx += blockDim.x) wins[idx] = C{0, 0};
+  // tap coefficients of sub-segmented kernels, after the step lists
+  real *csm = reinterpret_cast<real *>(
+      smem_raw + walk_coefficient_offset(sizeof(real), a.win_rows, WS, a.max_steps));
+  if (SUB) stage_coefficients<real, J>(poly.u, poly.nsub_u, csm);
   C *mine = wins + warp * WN;
   const int q0 = warp * tk.W / nw, q1 = (warp + 1) * tk.W / nw;
   const unsigned lt = (1u << lane) - 1u;
@@ -810,8 +846,8 @@ __global__ void __launch_bounds__(128, (sizeof(real) == 4 && J <= 6) ? 4 : 2) wa
             if ((m >> lane) & 1u) {
               const real sg = copysign(real(1), t.x);
               real ku[J], kv[J];
-              tap_weights<real, J, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku);
-              tap_weights<real, J, SUB>(poly.v, poly.nsub_v, t.y, kv);
+              tap_weights<real, J, SUB>(poly.u, poly.nsub_u, fabs(t.x), ku, csm);
+              tap_weights<real, J, SUB>(poly.v, poly.nsub_v, t.y, kv, csm);
               const C z{sg * yv.x, sg * yv.y};
 #pragma unroll
               for (int jv = 0; jv < J; ++jv) {
@@ -1014,6 +1050,19 @@ inline size_t stage_bytes(int precision_bytes, int J, bool user) {
   const size_t CH = size_t(stage_depth(precision_bytes, J));
   const size_t c = 2 * size_t(precision_bytes);
   return 2 * CH * 32 * (c + (user ? 4 : 0));
+}
+
+// Shared bytes of the tap coefficients a kernel with sub-segmented taps
+// copies (stage_coefficients): J taps x nsub sub-segments x the precision's
+// coefficient count; none without sub-segments.
+inline size_t coefficient_bytes(int precision_bytes, int J, int nsub) {
+  if (nsub <= 1) return 0;
+  const size_t nc = precision_bytes == 8 ? PolyCount<double>::value : PolyCount<float>::value;
+  return (size_t(J) * nsub * nc * precision_bytes + 15) / 16 * 16;
+}
+template <typename real>
+inline int poly_nsub(const PolyTable<real> &poly) {
+  return poly.nsub_u > poly.nsub_v ? poly.nsub_u : poly.nsub_v;
 }
 
 inline size_t window_bytes(int precision_bytes, int win_rows, int win_cols, const LaunchShape &shape,

@@ -321,15 +321,16 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
     int optin = 0;
     cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_),
                "cudaDeviceGetAttribute");
+    const int nsub = std::max(poly_.nsub_u, poly_.nsub_v);
     const size_t need = std::max(
-        degrid_smem_bytes(sizeof(real), J_, win_rows_, win_cols_, shape_, true, group_),
-        grid_smem_bytes(sizeof(real), J_, win_rows_, win_cols_, shape_, true, group_));
+        degrid_smem_bytes(sizeof(real), J_, win_rows_, win_cols_, shape_, true, group_, nsub),
+        grid_smem_bytes(sizeof(real), J_, win_rows_, win_cols_, shape_, true, group_, nsub));
     if (need > size_t(optin))
       throw Error(kUnsupported, "tile / threads / support need " + std::to_string(need) +
                                     " bytes of shared memory per CTA; the device allows " +
                                     std::to_string(optin));
     const size_t nsm =
-        normal_smem_bytes(sizeof(real), J_, win_rows_, win_cols_, kNormalShape, group_);
+        normal_smem_bytes(sizeof(real), J_, win_rows_, win_cols_, kNormalShape, group_, nsub);
     const bool want = cfg.normal_pass == 1 || (cfg.normal_pass == 0 && J_ < kWideSupport);
     one_pass_normal_ = want && !split_weights_ && nsm > 0 && nsm <= size_t(optin);
   }
@@ -530,7 +531,8 @@ void OperatorT<real>::init_plain(const OperatorConfig &cfg, int64_t &bytes, Axis
     cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_),
                "cudaDeviceGetAttribute");
     walk_ = walk_smem_bytes(sizeof(real), wp.win_rows, wp.win_stride,
-                            std::max(wp.max_warp_steps, 1)) <= size_t(optin);
+                            std::max(wp.max_warp_steps, 1), J_,
+                            std::max(poly_.nsub_u, poly_.nsub_v)) <= size_t(optin);
   }
   if (walk_) {
     walk_max_steps_ = std::max(wp.max_warp_steps, 1);
