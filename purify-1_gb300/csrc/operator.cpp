@@ -49,6 +49,11 @@ constexpr int kWideSupport = 6;
 // blocks per lane leave room for few warps, and its shared memory holds the
 // grid window besides the warp windows.
 constexpr LaunchShape kNormalShape{64};
+// Host entry points of FP32 operators: the c128 <-> c64 conversion and the
+// host copies run in up to kCopyChunks chunks of at least kCopyChunkMin
+// values, overlapped (upload_c128, download_c128).
+constexpr int kCopyChunks = 8;
+constexpr int64_t kCopyChunkMin = int64_t(1) << 18;
 constexpr int kWalkThreads = 128;
 constexpr int kWalkMaxCellCount = 256;
 }  // namespace
@@ -140,6 +145,14 @@ class OperatorT final : public Operator {
   void release(cudaStream_t user);
   void upload_correction();
   void ensure_host_staging();
+  // Host complex<double> vector <-> device vector of the operator's type
+  // through the c128 staging buffer `stage`, in chunks: the conversion
+  // kernels run on stream_ and the copies on copy_stream_, so that each
+  // chunk's conversion overlaps the copies of the others.
+  void upload_c128(const double *host, void *stage, void *dev, int64_t n);
+  void download_c128(const void *dev, void *stage, double *host, int64_t n);
+  cudaStream_t copy_stream_ = nullptr;
+  std::vector<cudaEvent_t> copy_ev_;
 
   OperatorInfo info_;
   int device_ = 0;
@@ -678,6 +691,9 @@ OperatorT<real>::~OperatorT() {
   if (fft_cols_) cufftDestroy(fft_cols_);
   if (ev_in_) cudaEventDestroy(ev_in_);
   if (ev_out_) cudaEventDestroy(ev_out_);
+  if (copy_stream_) cudaStreamSynchronize(copy_stream_);
+  for (cudaEvent_t e : copy_ev_) cudaEventDestroy(e);
+  if (copy_stream_) cudaStreamDestroy(copy_stream_);
   if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -1256,8 +1272,49 @@ void OperatorT<real>::ensure_host_staging() {
   if (sizeof(real) != sizeof(double)) {
     xc_.alloc(sizeof(C) * size_t(N_), cnt);
     yc_.alloc(sizeof(C) * size_t(M_), cnt);
+    cuda_check(cudaStreamCreateWithFlags(&copy_stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    copy_ev_.resize(kCopyChunks + 1);
+    for (cudaEvent_t &e : copy_ev_)
+      cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
   }
   staging_ = true;
+}
+
+template <typename real>
+void OperatorT<real>::upload_c128(const double *host, void *stage, void *dev, int64_t n) {
+  const int64_t chunk = std::max<int64_t>(kCopyChunkMin, (n + kCopyChunks - 1) / kCopyChunks);
+  // the staging buffer is free once the work before this call on stream_ is
+  cuda_check(cudaEventRecord(copy_ev_[kCopyChunks], stream_), "cudaEventRecord");
+  cuda_check(cudaStreamWaitEvent(copy_stream_, copy_ev_[kCopyChunks], 0), "cudaStreamWaitEvent");
+  for (int64_t off = 0, k = 0; off < n; off += chunk, ++k) {
+    const int64_t len = std::min(chunk, n - off);
+    char *st = static_cast<char *>(stage) + 16 * off;
+    cuda_check(cudaMemcpyAsync(st, host + 2 * off, 16 * size_t(len), cudaMemcpyHostToDevice,
+                               copy_stream_),
+               "H2D");
+    cuda_check(cudaEventRecord(copy_ev_[k], copy_stream_), "cudaEventRecord");
+    cuda_check(cudaStreamWaitEvent(stream_, copy_ev_[k], 0), "cudaStreamWaitEvent");
+    cuda_check(launch_from_c128<real>(st, static_cast<C *>(dev) + off, len, stream_), "convert");
+  }
+}
+
+template <typename real>
+void OperatorT<real>::download_c128(const void *dev, void *stage, double *host, int64_t n) {
+  const int64_t chunk = std::max<int64_t>(kCopyChunkMin, (n + kCopyChunks - 1) / kCopyChunks);
+  for (int64_t off = 0, k = 0; off < n; off += chunk, ++k) {
+    const int64_t len = std::min(chunk, n - off);
+    char *st = static_cast<char *>(stage) + 16 * off;
+    cuda_check(launch_to_c128<real>(static_cast<const C *>(dev) + off, st, len, stream_),
+               "convert");
+    cuda_check(cudaEventRecord(copy_ev_[k], stream_), "cudaEventRecord");
+    cuda_check(cudaStreamWaitEvent(copy_stream_, copy_ev_[k], 0), "cudaStreamWaitEvent");
+    cuda_check(cudaMemcpyAsync(host + 2 * off, st, 16 * size_t(len), cudaMemcpyDeviceToHost,
+                               copy_stream_),
+               "D2H");
+  }
+  // later work on stream_ (which may rewrite the staging buffer) follows the copies
+  cuda_check(cudaEventRecord(copy_ev_[kCopyChunks], copy_stream_), "cudaEventRecord");
+  cuda_check(cudaStreamWaitEvent(stream_, copy_ev_[kCopyChunks], 0), "cudaStreamWaitEvent");
 }
 
 template <typename real>
@@ -1265,18 +1322,16 @@ void OperatorT<real>::forward_host(const double *x, double *y) {
   DeviceGuard guard(device_);
   std::lock_guard<std::mutex> lock(mu_);
   ensure_host_staging();
-  const bool f64 = sizeof(real) == sizeof(double);
+  if (sizeof(real) != sizeof(double)) {
+    upload_c128(x, x128_.get(), xc_.get(), N_);
+    forward_on_stream(xc_.get(), yc_.get());
+    download_c128(yc_.get(), y128_.get(), y, M_);
+    cuda_check(cudaStreamSynchronize(stream_), "forward_host");
+    return;
+  }
   cuda_check(cudaMemcpyAsync(x128_.get(), x, 16 * size_t(N_), cudaMemcpyHostToDevice, stream_),
              "H2D");
-  void *xin = x128_.get();
-  void *yout = y128_.get();
-  if (!f64) {
-    cuda_check(launch_from_c128<real>(x128_.get(), xc_.get(), N_, stream_), "convert");
-    xin = xc_.get();
-    yout = yc_.get();
-  }
-  forward_on_stream(xin, yout);
-  if (!f64) cuda_check(launch_to_c128<real>(yc_.get(), y128_.get(), M_, stream_), "convert");
+  forward_on_stream(x128_.get(), y128_.get());
   cuda_check(cudaMemcpyAsync(y, y128_.get(), 16 * size_t(M_), cudaMemcpyDeviceToHost, stream_),
              "D2H");
   cuda_check(cudaStreamSynchronize(stream_), "forward_host");
@@ -1287,18 +1342,16 @@ void OperatorT<real>::adjoint_host(const double *y, double *x) {
   DeviceGuard guard(device_);
   std::lock_guard<std::mutex> lock(mu_);
   ensure_host_staging();
-  const bool f64 = sizeof(real) == sizeof(double);
+  if (sizeof(real) != sizeof(double)) {
+    upload_c128(y, y128_.get(), yc_.get(), M_);
+    adjoint_on_stream(yc_.get(), xc_.get());
+    download_c128(xc_.get(), x128_.get(), x, N_);
+    cuda_check(cudaStreamSynchronize(stream_), "adjoint_host");
+    return;
+  }
   cuda_check(cudaMemcpyAsync(y128_.get(), y, 16 * size_t(M_), cudaMemcpyHostToDevice, stream_),
              "H2D");
-  void *yin = y128_.get();
-  void *xout = x128_.get();
-  if (!f64) {
-    cuda_check(launch_from_c128<real>(y128_.get(), yc_.get(), M_, stream_), "convert");
-    yin = yc_.get();
-    xout = xc_.get();
-  }
-  adjoint_on_stream(yin, xout);
-  if (!f64) cuda_check(launch_to_c128<real>(xc_.get(), x128_.get(), N_, stream_), "convert");
+  adjoint_on_stream(y128_.get(), x128_.get());
   cuda_check(cudaMemcpyAsync(x, x128_.get(), 16 * size_t(N_), cudaMemcpyDeviceToHost, stream_),
              "D2H");
   cuda_check(cudaStreamSynchronize(stream_), "adjoint_host");
