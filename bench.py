@@ -454,7 +454,7 @@ def run_gb300(args):
     value = world * M / (ms_per_step * 1e-3) / 1e6
     # Phi^H's grid kernel gathers the caller-ordered visibilities itself
     # unless the tuning asks for the slot-ordered path or the column walk
-    gather_in_grid = (args.fused_permute == 1 or (args.fused_permute < 0 and args.J >= 6)) \
+    gather_in_grid = (args.fused_permute == 1 or (args.fused_permute < 0 and args.J >= 4)) \
         and not args.grid_walk
 
     out = {

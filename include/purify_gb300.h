@@ -105,7 +105,7 @@ typedef struct {
   int32_t tile;          /* uv tile edge in grid cells (<= 255) */
   int32_t fused_permute; /* 1: degrid/grid touch caller-ordered visibilities directly,
                             0: via a slot-ordered buffer and gather kernels, -1: default
-                            (Phi direct; Phi^H direct for supports J >= 6, else through
+                            (Phi direct; Phi^H direct for supports J >= 4, else through
                             the slot-ordered buffer, and always so with weights or with
                             the column walk) */
   int32_t cell_group;    /* base cells of a work item: 0 or 1 = one cell (the default);

@@ -416,7 +416,21 @@ __global__ void __launch_bounds__(256) degrid_kernel(const ApplyArgs<real> a0,
   cp_async_wait_all();
 }
 
-template <typename real, int J, int G, bool SUB, bool GROUP>
+// Coverage loads the grid kernel keeps in flight per warp (depth, in steps)
+// and how many steps before its gather a caller index is loaded
+// (index_lead).  Wide supports: 2 and 1; a step's arithmetic covers the
+// latencies and registers are short (deeper measured slower at J = 6).
+// Below J = 6 the steps are short and registers to spare: 4 and 3.
+// CALLER: the instantiation launched to gather caller order (FP32, J < 6);
+// the slot-ordered launches keep 2 and 1, which measured faster there.
+template <typename real, int J, bool CALLER>
+struct GridAhead {
+  static constexpr bool narrow = sizeof(real) == 4 && J < 6 && CALLER;
+  static constexpr int depth = narrow ? 4 : 2;
+  static constexpr int index_lead = narrow ? 3 : 1;
+};
+
+template <typename real, int J, int G, bool SUB, bool GROUP, bool CALLER = false>
 __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
                                                    const __grid_constant__ PolyTable<real> poly) {
   using C = cplx<real>;
@@ -483,16 +497,51 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
     auto value_at = [&](int lb, int k, int m) {
       return user ? gather_vis<real>(vin, m, keep, kpol) : __ldcs(vin + slot(lb, k));
     };
-    int mq = user ? index_at(plb, pk) : -1;
-    C t0 = stream_load(frac + slot(plb, pk)), y0 = value_at(plb, pk, mq);
-    adv(plb, pk);
-    if (user) mq = index_at(plb, pk);
-    C t1{0, 0}, y1{0, 0};
-    if (plb < nbt) {
-      t1 = stream_load(frac + slot(plb, pk));
-      y1 = value_at(plb, pk, mq);
-      adv(plb, pk);
-      if (user) mq = index_at(plb, pk);
+    // D steps of loads in flight (tq[0], yq[0]: the compute cursor's).  In
+    // caller order a gather's index was loaded IL steps before it: IL = 1
+    // keeps one index (mq) beside the prefetch cursor; IL > 1 runs an index
+    // cursor (qlb, qk) IL - 1 steps past it, with the indices between in mr.
+    constexpr int D = GridAhead<real, J, CALLER>::depth;
+    constexpr int IL = GridAhead<real, J, CALLER>::index_lead;
+    int mq = -1;
+    int qlb = plb, qk = pk;
+    int mr[IL];
+    auto next_index = [&]() {
+      int m = -1;
+      if (qlb < nbt) {
+        m = index_at(qlb, qk);
+        adv(qlb, qk);
+      }
+      return m;
+    };
+    if constexpr (IL == 1) {
+      mq = user ? index_at(plb, pk) : -1;
+    } else {
+#pragma unroll
+      for (int i = 0; i < IL; ++i) mr[i] = user ? next_index() : -1;
+    }
+    auto prefetch = [&](C &t, C &y) {
+      t = stream_load(frac + slot(plb, pk));
+      if constexpr (IL == 1) {
+        y = value_at(plb, pk, mq);
+        adv(plb, pk);
+        if (user) mq = index_at(plb, pk);
+      } else {
+        y = value_at(plb, pk, mr[0]);
+        adv(plb, pk);
+        if (user) {
+#pragma unroll
+          for (int i = 0; i + 1 < IL; ++i) mr[i] = mr[i + 1];
+          mr[IL - 1] = next_index();
+        }
+      }
+    };
+    C tq[D], yq[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      tq[d] = C{0, 0};
+      yq[d] = C{0, 0};
+      if (d == 0 || plb < nbt) prefetch(tq[d], yq[d]);
     }
     C acc[JBV][JBU];
 #pragma unroll
@@ -500,15 +549,13 @@ __global__ void __launch_bounds__(256) grid_kernel(const ApplyArgs<real> a0,
 #pragma unroll
       for (int ju = 0; ju < JBU; ++ju) acc[jv][ju] = C{0, 0};
     while (clb < nbt) {
-      const C t = t0, yv = y0;
-      t0 = t1;
-      y0 = y1;
-      if (plb < nbt) {
-        t1 = stream_load(frac + slot(plb, pk));
-        y1 = value_at(plb, pk, mq);
-        adv(plb, pk);
-        if (user) mq = index_at(plb, pk);
+      const C t = tq[0], yv = yq[0];
+#pragma unroll
+      for (int d = 0; d + 1 < D; ++d) {
+        tq[d] = tq[d + 1];
+        yq[d] = yq[d + 1];
       }
+      if (plb < nbt) prefetch(tq[D - 1], yq[D - 1]);
       // Null slots hold a zero visibility, so they add nothing.  The phase
       // sign (-1)^(k_u + k_v) rides in the sign of t_u.
       const real sg = copysign(real(1), t.x);
@@ -1079,6 +1126,10 @@ template <typename real, int J, int G, bool SUB, bool GROUP>
 cudaError_t launch_one(bool degrid, const ApplyArgs<real> &a, const PolyTable<real> &poly,
                        int ntasks, size_t smem, int threads, cudaStream_t s) {
   auto fn = degrid ? degrid_kernel<real, J, G, SUB, GROUP> : grid_kernel<real, J, G, SUB, GROUP>;
+  if constexpr (sizeof(real) == 4 && J < 6 && G == 1 && !GROUP) {
+    // G^H gathering caller order at narrow supports: deeper prefetch
+    if (!degrid && a.slot_user) fn = grid_kernel<real, J, G, SUB, GROUP, true>;
+  }
   if (smem > 48 * 1024) {
     const cudaError_t e =
         cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));

@@ -45,6 +45,9 @@ namespace {
 // Supports from which the default launch shape and adjoint path change
 // (see the constructor).
 constexpr int kWideSupport = 6;
+// Supports from which the adjoint's grid kernel gathers caller order itself
+// by default.
+constexpr int kGatherInGridSupport = 4;
 // Launch shape of normal_kernel: two warps per CTA.  Its two register
 // blocks per lane leave room for few warps, and its shared memory holds the
 // grid window besides the warp windows.
@@ -298,18 +301,22 @@ OperatorT<real>::OperatorT(const OperatorConfig &cfg) {
   // FP32).  Wide supports (J >= 6): 64-thread CTAs, and the adjoint's grid
   // kernel gathers caller order itself; its per-visibility work hides the
   // gathers' latency (J = 6: step 0.414 ms; 128 threads 0.423; a separate
-  // gather 0.47).  Narrow supports: 128-thread CTAs, and the adjoint gathers
-  // into slot order first, because the shorter steps leave the gathers
-  // exposed (J = 4: adjoint 0.221 ms that way against 0.297 ms gathering in
-  // the grid kernel).  The forward always writes caller order directly
-  // (scattered stores) unless the tuning asks for the slot-ordered path.
-  // The w-projection kernels always use the slot-ordered buffer.
+  // gather 0.47).  Narrower supports: 128-thread CTAs.  From J = 4 the grid
+  // kernel gathers caller order with four steps of loads in flight and the
+  // indices three steps ahead (GridAhead; J = 4: adjoint 0.213 ms against
+  // 0.221 with the separate gather, J = 5: 0.233 against 0.241).  Below
+  // J = 4 the steps are too short and the adjoint gathers into slot order
+  // first (J = 2: adjoint 0.209 ms against 0.294).  The forward always
+  // writes caller order directly (scattered stores) unless the tuning asks
+  // for the slot-ordered path.  The w-projection kernels always use the
+  // slot-ordered buffer.
   const bool wide = J_ >= kWideSupport;
   shape_.threads = cfg.threads > 0 ? cfg.threads : (wide ? 64 : 128);
   fused_forward_ = !wmode_ && cfg.fused_permute != 0;
   keep_vis_l2_ = int64_t(sizeof(C)) * M_ <= kKeepVisL2Bytes;
   keep_store_ = cfg.keep_store != 0;
-  fused_adjoint_ = !wmode_ && (cfg.fused_permute == 1 || (cfg.fused_permute < 0 && wide));
+  fused_adjoint_ = !wmode_ && (cfg.fused_permute == 1 ||
+                               (cfg.fused_permute < 0 && J_ >= kGatherInGridSupport));
 
   cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
   cuda_check(cudaEventCreateWithFlags(&ev_in_, cudaEventDisableTiming), "cudaEventCreate");
