@@ -1077,12 +1077,13 @@ def run_serve(args):
         "latency_ms": f32["latency_ms"], "serving": {k: {kk: vv for kk, vv in v.items()
                                                           if kk != "_res"}
                                                       for k, v in per_prec.items()},
-        # own kernels per request (FP32): the conversions from and to c128,
-        # the forward row and column passes and degrid, and expand, grid,
-        # fold and the inverse column and row passes; a norm request: the
-        # fill, then per round both FFT directions, degrid, grid, fold, two
-        # reduction kernels and the scale
-        "gpu_launches": int(sum({"forward_adjoint": 11, "adjoint": 7}.get(str(k), 1 + 10 * 50)
+        # own kernels per request (FP32, KB J = 4): the conversions from and
+        # to c128, the forward row and column passes and degrid, and grid
+        # (gathering caller order), fold and the inverse column and row
+        # passes; a norm request: the fill, then per round both FFT
+        # directions, the one-pass normal kernel, fold, two reduction kernels
+        # and the scale
+        "gpu_launches": int(sum({"forward_adjoint": 10, "adjoint": 6}.get(str(k), 1 + 9 * 50)
                                 for k in kinds)),
     }
     if "fp64" in per_prec:

@@ -1058,11 +1058,9 @@ void OperatorT<real>::forward_on_stream(const void *x, void *y) {
 
 template <typename real>
 void OperatorT<real>::adjoint_on_stream(const void *y, void *x) {
-  // The grid kernel gathers caller order itself on the operator's own
-  // scratch.  The request server's concurrent workspaces keep the separate
-  // gather: on its Poisson stream the short requests' p99 latency was lower
-  // that way (equal throughput).
-  if (fused_adjoint_ && ws_ == &own_) {
+  // The grid kernel gathers caller order itself (fused_adjoint_), on the
+  // operator's own scratch and on the request server's workspaces alike.
+  if (fused_adjoint_) {
     adjoint_slots(x, y);
     return;
   }
